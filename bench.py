@@ -1,0 +1,322 @@
+"""Benchmark: MITC4 residual + Jacobian assembly (elements/s) on a GB300.
+
+Workload (the configuration the headline metric is quoted on): a 2.0 m
+square flat plate of 512 x 512 MITC4 shell elements (262,144 elements,
+263,169 nodes, 1,579,014 dof, 2,362,369 6x6 blocks), per-element thickness
+seeded uniform in [0.005, 0.02] (numpy default_rng(2)), E = 70e9, nu = 0.3,
+nodal pressure p(x, y) = 1e3 (1 + 0.5 sin(pi x) sin(pi y)) (x, y in metres),
+simply-supported edges (u, v, w fixed).  Synthetic data; the BCSR matrix
+(680 MB) and the state exceed the 129 MB L2, so no flush is needed between
+steps.
+
+One step = TACSAssembler::assembleJacobian(1, 0, 0, res, mat) semantics:
+zero, element residual + Jacobian for every element, scatter into BCSR,
+row-zero Dirichlet conditions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  --impl reference times the CPU restatement
+of the reference path (oracle/, all host threads) on a bounded sample of the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elements/s res+Jacobian assembly; adjoint grad s/solve, FP32-precond vs FP64"
+UNIT = "elements/s"
+
+
+def c2_problem(n=512, L=2.0, seed=2):
+    from tacs_gb300 import meshes
+    rng = np.random.default_rng(seed)
+    p = meshes.plate(n, n, L, L, t=0.01, E=70e9, nu=0.3, rho=2700.0,
+                     ys=2.7e8, thick=rng.uniform(0.005, 0.02, n * n))
+    e = meshes.plate_edges(n, n).astype(np.int32)
+    p["bc_nodes"], p["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
+    xyz = p["xpts"].reshape(-1, 3)
+    pn = 1e3 * (1.0 + 0.5 * np.sin(np.pi * xyz[:, 0]) * np.sin(np.pi * xyz[:, 1]))
+    conn = p["conn"].reshape(-1, 4)
+    p["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    p["pres_vals"] = pn[conn].ravel()
+    return p
+
+
+def algorithmic_bytes(p):
+    """Assembly traffic a perfect implementation moves once: node coords and
+    state read, connectivity + thickness read, residual write, BCSR write."""
+    nn, ne = p["nnodes"], p["nelem"]
+    n = int(np.sqrt(ne))
+    nnzb = (3 * (n + 1) - 2) ** 2
+    return nn * (3 + 6) * 8 + ne * (4 * 4 + 8) + nn * 6 * 8 + nnzb * 36 * 8
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fp:
+            d = json.load(fp)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(p_full, seconds=12.0):
+    """The oracle's threaded CPU assembly on a bounded sample (a 128 x 128
+    sub-plate of the same workload), elements/s."""
+    import oracle
+    n = 128
+    sub = c2_problem(n=n, L=2.0 * n / 512, seed=2)
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(sub, nthreads=threads)
+    u = np.zeros(o.ndof)
+    A = o.new_bcsr()
+    o.assemble_jac(u, A)  # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        o.assemble_jac(u, A)
+        reps += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    o.free(A)
+    return {"value": reps * sub["nelem"] / dt, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{reps} x assembleJacobian of a {n}x{n} sub-plate "
+                      f"({sub['nelem']} elements), {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p = c2_problem()
+    steps, warm = args.steps, args.warmup
+    import oracle
+    n = 128
+    sub = c2_problem(n=n, L=2.0 * n / 512, seed=2)
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(sub, nthreads=threads)
+    u = np.zeros(o.ndof)
+    A = o.new_bcsr()
+    for _ in range(warm):
+        o.assemble_jac(u, A)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.assemble_jac(u, A)
+    dt = time.perf_counter() - t0
+    value = steps * sub["nelem"] / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "MITC4 plate 512x512 (sampled 128x128)",
+                       "elements": int(p["nelem"]), "sample_elements": n * n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                             "kind": "port",
+                             "sample": f"{steps} x assembleJacobian of a "
+                                       f"{n}x{n} sub-plate"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", type=int, default=512)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from tacs_gb300 import problem
+    p = c2_problem(n=args.size)
+    M = problem.GpuModel(p)
+    u = M.vec()
+    res = M.vec()
+    mat = M.new_mat()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        M.assemble_jacobian(u, mat, res)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # zero-fill share of the step (the two memsets inside assembleJacobian)
+    z0 = torch.cuda.Event(enable_timing=True)
+    z1 = torch.cuda.Event(enable_timing=True)
+    z0.record(stream)
+    for _ in range(args.steps):
+        res.zero_()
+        mat.vals.zero_()
+    z1.record(stream)
+    torch.cuda.synchronize()
+    ms_zero = z0.elapsed_time(z1) / args.steps
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the public API with host buffers: design variables
+    # and state in (pinned), residual out.
+    thick_h = torch.as_tensor(np.asarray(p["thick"]), dtype=torch.float64).pin_memory()
+    u_h = torch.zeros(M.ndof, dtype=torch.float64).pin_memory()
+    res_h = torch.empty(M.ndof, dtype=torch.float64).pin_memory()
+    dv_d = M.dv_vec()
+    for _ in range(2):
+        dv_d.copy_(thick_h, non_blocking=True)
+        u.copy_(u_h, non_blocking=True)
+        M.set_design_vars(dv_d)
+        step()
+        res_h.copy_(res, non_blocking=True)
+    torch.cuda.synchronize()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(args.steps):
+        dv_d.copy_(thick_h, non_blocking=True)
+        u.copy_(u_h, non_blocking=True)
+        M.set_design_vars(dv_d)
+        step()
+        res_h.copy_(res, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3) / args.steps
+
+    nelem = p["nelem"]
+    value = world * nelem / (ms / 1e3)
+    peak, peak_src = measured_peaks()
+    algo = algorithmic_bytes(p)
+    kern_ms = max(ms - ms_zero, 1e-6)
+    achieved = algo / (kern_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"MITC4 plate {args.size}x{args.size}, "
+                               "assembleRes+assembleJacobian",
+                   "elements": int(nelem), "nodes": int(p["nnodes"]),
+                   "dof": int(M.ndof), "bcsr_blocks": int(mat.nnz),
+                   "l2": "inputs larger than L2 (680 MB BCSR), no flush",
+                   "colors": M.ncolors},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src,
+                     "kernel": "shell_assembly_kernel",
+                     "kernel_ms": kern_ms, "algorithmic_bytes": algo},
+        "e2e": {"value": world * nelem / (ms_e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(8 * (M.ndv + M.ndof)),
+                "d2h_bytes_per_step": int(8 * M.ndof)},
+        "gpu_launches": M.ncolors * args.steps + 2 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+/*
+  tacs_gb300 -- C ABI of the GB300 (sm_103a) implementation of the TACS
+  finite-element hot path: MITC4-shell and hex8 residual / Jacobian assembly
+  into 6x6 / 3x3 block-CSR, the BCSR mat-vec, ILU(0) / block-Jacobi
+  preconditioning inside GMRES, and the adjoint products.
+
+  Conventions
+  - Every call returns 0 on success or a negative TG_ERR_* code; the message
+    of the last failure on the calling thread is available from
+    tg_last_error().  No call aborts the process.
+  - Vectors are raw DEVICE pointers (double, node-major, vars_per_node per
+    node -- the layout of TACSBVec::getArray, src/bpmat/TACSBVec.cpp:983).
+    Design vectors hold one value per design variable.  Host-pointer
+    arguments are named *_host.
+  - `stream` is a cudaStream_t passed as void*; NULL means the legacy
+    default stream.  Calls only enqueue work (except where noted) and never
+    allocate device memory after the object's creation/initialisation.
+  - The library owns the device memory of the objects it creates; objects
+    are reference counted like TACSObject (src/TACSObject.h:112-146):
+    tg_*_create returns a reference, tg_*_decref releases one.
+  - Not re-entrant on one object: calls on the same object must be ordered
+    on one stream (the reference's objects are not re-entrant either).
+
+  Each entry point names the reference interface it replaces.
+*/
+#ifndef TACS_GB300_H
+#define TACS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_OK 0
+#define TG_ERR_ARG -1      /* invalid argument / size */
+#define TG_ERR_CUDA -2     /* a CUDA runtime call failed */
+#define TG_ERR_STATE -3    /* call out of order (e.g. not initialised) */
+#define TG_ERR_PIVOT -4    /* zero pivot in a diagonal block inverse */
+#define TG_ERR_NOCONV -5   /* iterative solve hit its iteration limit */
+#define TG_ERR_NONFINITE -6 /* NaN/Inf detected in a result */
+
+#define TG_ELEM_MITC4 0 /* TACSQuad4Shell, 6 dof/node */
+#define TG_ELEM_HEX8 1  /* TACSElement3D(LinearElasticity3D, LinearHexaBasis) */
+
+#define TG_MAT_NORMAL 0    /* MatrixOrientation TACS_MAT_NORMAL */
+#define TG_MAT_TRANSPOSE 1 /* TACS_MAT_TRANSPOSE */
+
+#define TG_PC_ILU0 0        /* TACSAdditiveSchwarz(mat, 0, fill): ILU(0) */
+#define TG_PC_BLOCK_JACOBI 1 /* inverted diagonal blocks only */
+#define TG_PC_ILU0_COLORED 2 /* ILU(0) of a multicolour node reordering */
+
+#define TG_PREC_FP64 0 /* preconditioner and inner mat-vec in FP64 */
+#define TG_PREC_FP32 1 /* FP32 factor / apply and inner mat-vec */
+
+#define TG_FUNC_COMPLIANCE 0 /* TACSCompliance */
+#define TG_FUNC_KS_FAILURE 1 /* TACSKSFailure, KS_CONTINUOUS */
+
+typedef struct tg_assembler tg_assembler;
+typedef struct tg_mat tg_mat;
+typedef struct tg_pc tg_pc;
+typedef struct tg_ksm tg_ksm;
+
+/* ---------------------------------------------------------------- errors */
+const char *tg_last_error(void);
+int tg_version(void);
+
+/* ------------------------------------------------------------- assembler */
+/* TACSAssembler::TACSAssembler + setElementConnectivity + setElements
+   (src/TACSAssembler.h:83-91).  conn holds npe node ids per element
+   (4 for MITC4 in TACSShellQuadBasis<2> order, 8 for hex8 in
+   TACSLinearHexaBasis order).  Material: TACSMaterialProperties(rho, ., E,
+   nu, ys) (src/constitutive/TACSMaterialProperties.h:44).  For shells the
+   transform is TACSShellNaturalTransform (transform = 0) or
+   TACSShellRefAxisTransform(ref_axis) (transform = 1)
+   (src/elements/shell/TACSShellElementTransform.h:21,95). */
+int tg_assembler_create(int elem_type, int num_nodes, int num_elements,
+                        const int *conn_host, double rho, double E, double nu,
+                        double ys, int transform, const double *ref_axis_host,
+                        tg_assembler **out);
+int tg_assembler_incref(tg_assembler *a);
+int tg_assembler_decref(tg_assembler *a);
+int tg_assembler_get_sizes(tg_assembler *a, int *vars_per_node, int *nnodes,
+                           int *nelems, int *ndvs, int *ncolors);
+
+/* TACSAssembler::addBCs(nnodes, nodes, nbcs, vars) with zero values
+   (src/TACSAssembler.h:109): dof k of node nodes[i] is constrained when
+   bit k of masks[i] is set. */
+int tg_assembler_add_bcs(tg_assembler *a, int n, const int *nodes_host,
+                         const int *masks_host);
+
+/* Per-element design variables: the thickness t of TACSIsoShellConstitutive
+   (src/constitutive/TACSIsoShellConstitutive.h:33) or t of
+   TACSSolidConstitutive (TACSSolidConstitutive.h:34) and its design
+   variable number tNum (-1: not a design variable). */
+int tg_assembler_set_element_dvs(tg_assembler *a, const double *t_host,
+                                 const int *dvnum_host);
+
+/* TACSAssembler::initialize (src/TACSAssembler.cpp:2519): builds the BCSR
+   non-zero pattern, the element colouring and the device-side maps.
+   Synchronous. */
+int tg_assembler_initialize(tg_assembler *a);
+
+/* TACSAssembler::setNodes (node vector, 3 doubles per node, device). */
+int tg_assembler_set_nodes(tg_assembler *a, const double *xpts,
+                           void *stream);
+/* TACSAssembler::setDesignVars: values indexed by design-variable number
+   (device); every element copies t = dvs[tNum]. */
+int tg_assembler_set_design_vars(tg_assembler *a, const double *dvs,
+                                 void *stream);
+
+/* Auxiliary loads (TACSAuxElements, src/TACSAuxElements.cpp:78):
+   TACSShellPressure with four nodal pressures per element
+   (src/elements/shell/TACSShellPressure.h:11-22), and TACSTraction3D face
+   tractions in global components (src/elements/TACSTraction3D.cpp:19). */
+int tg_assembler_set_pressure(tg_assembler *a, int n, const int *elems_host,
+                              const double *vals_host);
+int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems_host,
+                              const int *faces_host, const double *vals_host);
+
+/* TACSAssembler::assembleRes(res, lambda, applyBCs)
+   (src/TACSAssembler.cpp:4133).  vars: state (device). */
+int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,
+                    int apply_bcs, double *res, void *stream);
+
+/* TACSAssembler::assembleJacobian(alpha, beta, gamma, res, A, matOr,
+   lambda, applyBCs) (src/TACSAssembler.cpp:4291).  Static elements only:
+   beta and gamma must be 0.  res may be NULL. */
+int tg_assemble_jacobian(tg_assembler *a, double alpha, double beta,
+                         double gamma, const double *vars, double *res,
+                         tg_mat *A, int mat_orient, double lambda,
+                         int apply_bcs, void *stream);
+
+/* TACSAssembler::applyBCs(vec) (zero the constrained entries) */
+int tg_apply_bcs(tg_assembler *a, double *vec, void *stream);
+
+/* TACSAssembler::evalFunctions (src/TACSAssembler.cpp:4617) for
+   funcs[i] in {TG_FUNC_COMPLIANCE, TG_FUNC_KS_FAILURE}; ks_weight as in
+   TACSKSFailure(assembler, ksWeight).  Writes values to vals_host;
+   synchronises the stream. */
+int tg_eval_functions(tg_assembler *a, const double *vars, int nfuncs,
+                      const int *funcs_host, double ks_weight,
+                      double *vals_host, void *stream);
+
+/* TACSAssembler::addSVSens(alpha, beta, gamma, funcs, dfdu)
+   (src/TACSAssembler.cpp:4941): dfdu[i] += alpha * df_i/du.  Uses the KS
+   statistics of the last tg_eval_functions call on this assembler. */
+int tg_add_sv_sens(tg_assembler *a, const double *vars, int nfuncs,
+                   const int *funcs_host, double alpha, double **dfdu,
+                   void *stream);
+
+/* TACSAssembler::addDVSens(coef, funcs, dfdx) (src/TACSAssembler.cpp:4767)
+   dfdx[i] += coef * (partial) df_i/dx. */
+int tg_add_dv_sens(tg_assembler *a, const double *vars, int nfuncs,
+                   const int *funcs_host, double coef, double **dfdx,
+                   void *stream);
+
+/* TACSAssembler::addAdjointResProducts(scale, adjoints, dfdx, lambda)
+   (src/TACSAssembler.cpp:5033): dfdx[k] += scale * psi_k^T dR/dx. */
+int tg_add_adjoint_res_products(tg_assembler *a, const double *vars,
+                                double scale, int nadj, const double **psi,
+                                double **dfdx, void *stream);
+
+/* Fused total derivative for one function: dfdx = coef * df/dx
+   + scale * psi^T dR/dx in one pass (addDVSens followed by
+   addAdjointResProducts with the same element strains). */
+int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
+                            double coef, const double *psi, double scale,
+                            double *dfdx, void *stream);
+
+/* ------------------------------------------------------------------ BCSR */
+/* TACSAssembler::createMat (src/TACSAssembler.cpp:3384): a BCSR matrix with
+   the assembler's non-zero pattern (node graph plus diagonal, sorted
+   columns; BCSRMatData, src/bpmat/BCSRMatImpl.h:27-46). */
+int tg_mat_create(tg_assembler *a, tg_mat **out);
+int tg_mat_decref(tg_mat *A);
+/* BCSRMat::getArrays (src/bpmat/BCSRMat.h:82): device pointers */
+int tg_mat_get_arrays(tg_mat *A, int *bsize, int *nrows, const int **rowp,
+                      const int **cols, double **vals);
+/* BCSRMat::mult / TACSParallelMat::mult (src/bpmat/TACSParallelMat.cpp:248)
+   y = A x (device vectors). */
+int tg_mat_mult(tg_mat *A, const double *x, double *y, void *stream);
+/* FP32 copy of the matrix values and y = A x in FP32 (mixed precision) */
+int tg_mat_mult_f32(tg_mat *A, const float *x, float *y, void *stream);
+
+/* ------------------------------------------------------- preconditioners */
+/* TACSAdditiveSchwarz(mat, levFill = 0, fill)
+   (src/bpmat/TACSParallelMat.cpp:1190) with type TG_PC_ILU0, plus the
+   block-Jacobi and colour-reordered ILU(0) variants; precision
+   TG_PREC_FP32 keeps the factor in FP32. */
+int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out);
+int tg_pc_decref(tg_pc *pc);
+/* TACSAdditiveSchwarz::factor -> BCSRMat::factor (BCSRMatFact6.cpp:946).
+   Synchronises; returns TG_ERR_PIVOT (with the row in tg_last_error) on a
+   singular diagonal block. */
+int tg_pc_factor(tg_pc *pc, void *stream);
+/* TACSAdditiveSchwarz::applyFactor -> BCSRMat::applyFactor
+   (src/bpmat/BCSRMat.cpp:1326): y = (LU)^{-1} x. */
+int tg_pc_apply(tg_pc *pc, const double *x, double *y, void *stream);
+
+/* ------------------------------------------------------------------- KSM */
+/* GMRES(mat, pc, m, nrestart, isFlexible) (src/bpmat/KSM.h) with
+   setTolerances(rtol, atol).  mixed != 0 runs the preconditioner and the
+   inner mat-vec in FP32 (pc must be TG_PREC_FP32) inside FP64 GMRES with
+   FP64 Arnoldi and a true-residual iterative-refinement loop. */
+int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
+                  tg_ksm **out);
+int tg_ksm_decref(tg_ksm *k);
+int tg_ksm_set_tolerances(tg_ksm *k, double rtol, double atol);
+/* GMRES::solve(b, x, zero_guess) (src/bpmat/KSM.cpp:785).  Synchronous.
+   Returns 1 when converged, 0 when not (like the reference), or a negative
+   error code.  iters / resnorm (host) receive the iteration count and the
+   final (estimated, or true for mixed) residual norm. */
+int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
+                 int *iters, double *resnorm, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TACS_GB300_H */

@@ -1,0 +1,664 @@
+// Block-CSR linear algebra for sm_103a: the BCSR mat-vec (FP64 / FP32,
+// BCSRMatVecMult6/3, src/bpmat/BCSRMatMult6.cpp:82, BCSRMatMult3.cpp:28),
+// Dirichlet row zeroing (BCSRMat::zeroRow, src/bpmat/BCSRMat.cpp:2027),
+// level-scheduled block ILU(0) factor and triangular solves
+// (BCSRMatFactor6/3, BCSRMatApplyLower/Upper, BCSRMatFact6.cpp:946,
+// BCSRMatMult6.cpp:319-415), block Jacobi, deterministic reductions and the
+// GMRES vector kernels.
+#include <cmath>
+
+#include "tg_internal.h"
+
+namespace tg {
+namespace {
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+int blocks_for(size_t n, int threads, int per_sm = 8) {
+  size_t b = (n + threads - 1) / threads;
+  size_t cap = (size_t)num_sms() * per_sm;
+  if (b < 1) b = 1;
+  return (int)(b < cap ? b : cap);
+}
+
+// ------------------------------------------------------------ mat-vec
+// One thread per (block row, row within block): BS threads read the BS
+// rows of each BSxBS block, i.e. the whole contiguous block.
+template <int BS, typename T>
+__global__ void __launch_bounds__(256)
+    bcsr_mult_kernel(int nrows, const int *__restrict__ rowp,
+                     const int *__restrict__ cols, const T *__restrict__ A,
+                     const T *__restrict__ x, T *__restrict__ y) {
+  const int per_warp = 32 / BS;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / BS, ii = lane - BS * sub;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  if (sub >= per_warp) return;
+  for (int row = gw * per_warp + sub; row < nrows; row += nw * per_warp) {
+    T acc = 0;
+    const int end = rowp[row + 1];
+    for (int j = rowp[row]; j < end; j++) {
+      const T *a = &A[(size_t)BS * BS * j + BS * ii];
+      const T *xx = &x[(size_t)BS * cols[j]];
+      T s = 0;
+#pragma unroll
+      for (int jj = 0; jj < BS; jj++) s += a[jj] * xx[jj];
+      acc += s;
+    }
+    y[(size_t)BS * row + ii] = acc;
+  }
+}
+
+template <int BS, typename T>
+void mult_dispatch(int nrows, const int *rowp, const int *cols, const T *A,
+                   const T *x, T *y, cudaStream_t s) {
+  const int per_warp = 32 / BS;
+  size_t warps = (nrows + per_warp - 1) / per_warp;
+  int blocks = blocks_for(warps * 32, 256, 16);
+  bcsr_mult_kernel<BS, T><<<blocks, 256, 0, s>>>(nrows, rowp, cols, A, x, y);
+}
+
+// ---------------------------------------------------------------- BCs
+__global__ void apply_bcs_mat_kernel(int bs, int nbcs, const int *bc_nodes,
+                                     const int *bc_masks, const int *rowp,
+                                     const int *cols, double *A) {
+  for (int i = blockIdx.x * blockDim.y + threadIdx.y; i < nbcs;
+       i += gridDim.x * blockDim.y) {
+    const int row = bc_nodes[i], mask = bc_masks[i];
+    for (int j = rowp[row]; j < rowp[row + 1]; j++) {
+      double *a = &A[(size_t)bs * bs * j];
+      for (int k = threadIdx.x; k < bs * bs; k += blockDim.x) {
+        const int ii = k / bs, jj = k - bs * ii;
+        if (mask & (1 << ii)) {
+          a[k] = (cols[j] == row && ii == jj) ? 1.0 : 0.0;
+        }
+      }
+    }
+  }
+}
+
+__global__ void apply_bcs_res_kernel(int bs, int nbcs, const int *bc_nodes,
+                                     const int *bc_masks, const double *vars,
+                                     double *res) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbcs;
+       i += gridDim.x * blockDim.x) {
+    const int node = bc_nodes[i], mask = bc_masks[i];
+    for (int k = 0; k < bs; k++)
+      if (mask & (1 << k)) {
+        size_t d = (size_t)bs * node + k;
+        res[d] = vars ? vars[d] : 0.0;
+      }
+  }
+}
+
+__global__ void fill_kernel(double *x, double v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+__global__ void d2f_kernel(const double *x, float *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+__global__ void f2d_kernel(const float *x, double *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+__global__ void gather_dv_kernel(int nelem, const int *dvnum, const double *dvs,
+                                 double *thick) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem;
+       e += gridDim.x * blockDim.x)
+    if (dvnum[e] >= 0) thick[e] = dvs[dvnum[e]];
+}
+// dfdx[d] += sum over the elements of design variable d (element order)
+__global__ void scatter_dv_kernel(int ndv, const int *dv_ptr,
+                                  const int *dv_elems, const double *vals,
+                                  double *dfdx) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < ndv;
+       d += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int k = dv_ptr[d]; k < dv_ptr[d + 1]; k++) acc += vals[dv_elems[k]];
+    dfdx[d] += acc;
+  }
+}
+
+// ---------------------------------------------------------- reductions
+// Deterministic: fixed partition into npart partial results, then one
+// block combines them in a fixed tree order.
+template <int OP>  // 0 sum, 1 max, 2 ks-sum
+__global__ void reduce_partial_kernel(const double *x, const double *w,
+                                      size_t n, const double *dmax, double ksw,
+                                      double *partials) {
+  __shared__ double sh[256];
+  size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  size_t b = chunk * blockIdx.x, e = b + chunk < n ? b + chunk : n;
+  double acc = OP == 1 ? -1e300 : 0.0;
+  const double mx = (OP == 2) ? *dmax : 0.0;
+  for (size_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    if (OP == 0) acc += x[i];
+    else if (OP == 1) acc = x[i] > acc ? x[i] : acc;
+    else acc += w[i] * exp(ksw * (x[i] - mx));
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      if (OP == 1) sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
+                                         ? sh[threadIdx.x + s]
+                                         : sh[threadIdx.x];
+      else sh[threadIdx.x] += sh[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+template <int OP>
+__global__ void reduce_final_kernel(const double *partials, int npart,
+                                    double *out) {
+  __shared__ double sh[256];
+  double acc = OP == 1 ? -1e300 : 0.0;
+  for (int i = threadIdx.x; i < npart; i += blockDim.x) {
+    if (OP == 1) acc = partials[i] > acc ? partials[i] : acc;
+    else acc += partials[i];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      if (OP == 1) sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
+                                         ? sh[threadIdx.x + s]
+                                         : sh[threadIdx.x];
+      else sh[threadIdx.x] += sh[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// --------------------------------------------------------------- ILU(0)
+// Block inverse with partial pivoting then the explicit inverse, column by
+// column: BMatComputeInverse (src/bpmat/BCSRMatMult.cpp:308-386).
+// Lane 0 factors; lanes 0..n-1 form one column of the inverse each.
+template <int BS, typename T>
+__device__ void warp_block_inverse(T *a, T *lu, int *piv, int lane,
+                                   int *fail_flag, int row) {
+  if (lane == 0) {
+    for (int k = 0; k < BS * BS; k++) lu[k] = a[k];
+    int fail = 0;
+    for (int k = 0; k < BS - 1 && !fail; k++) {
+      int nk = BS * k, r = k;
+      double maxv = fabs((double)lu[nk + k]);
+      for (int j = k + 1; j < BS; j++) {
+        double t = fabs((double)lu[BS * j + k]);
+        if (t > maxv) {
+          maxv = t;
+          r = j;
+        }
+      }
+      piv[k] = r;
+      if (r != k)
+        for (int j = 0; j < BS; j++) {
+          T t = lu[nk + j];
+          lu[nk + j] = lu[BS * r + j];
+          lu[BS * r + j] = t;
+        }
+      if (lu[nk + k] == (T)0) {
+        fail = k + 1;
+        break;
+      }
+      for (int i = k + 1; i < BS; i++) lu[BS * i + k] = lu[BS * i + k] / lu[nk + k];
+      for (int i = k + 1; i < BS; i++)
+        for (int j = k + 1; j < BS; j++) lu[BS * i + j] -= lu[BS * i + k] * lu[nk + j];
+    }
+    if (!fail && lu[BS * BS - 1] == (T)0) fail = BS;
+    piv[BS] = fail;
+    if (fail) atomicCAS(fail_flag, 0, row + 1);
+  }
+  __syncwarp();
+  if (piv[BS]) return;
+  if (lane < BS) {
+    const int k = lane;
+    int ip = k;
+    for (int i = 0; i < BS - 1; i++) {
+      if (ip == piv[i]) ip = i;
+      else if (ip == i) ip = piv[i];
+    }
+    T col[BS];
+    for (int i = 0; i < ip; i++) col[i] = 0;
+    col[ip] = 1;
+    for (int i = ip + 1; i < BS; i++) {
+      T v = 0;
+      for (int j = ip; j < i; j++) v -= lu[BS * i + j] * col[j];
+      col[i] = v;
+    }
+    for (int i = BS - 1; i >= 0; i--) {
+      T v = col[i];
+      for (int j = i + 1; j < BS; j++) v -= lu[BS * i + j] * col[j];
+      col[i] = v / lu[BS * i + i];
+    }
+    for (int i = 0; i < BS; i++) a[BS * i + k] = col[i];
+  }
+  __syncwarp();
+}
+
+// One warp per row of one level (IKJ variant of BCSRMatFactor6/3):
+// for every lower block j in order: d = A_j D_{cj}^{-1};
+// A_k -= d A_p for the matching upper blocks of row cj; A_j = d.
+// Then the diagonal block is replaced by its inverse.
+template <int BS, typename T>
+__global__ void __launch_bounds__(128)
+    ilu0_factor_level_kernel(const int *__restrict__ rows, int nrows_lvl,
+                             const int *__restrict__ rowp,
+                             const int *__restrict__ cols,
+                             const int *__restrict__ diag,
+                             const int *__restrict__ upd_ptr,
+                             const int *__restrict__ upd_tgt,
+                             const int *__restrict__ upd_src, T *F,
+                             int *fail_flag) {
+  __shared__ T sd[4][BS * BS];
+  __shared__ T slu[4][BS * BS];
+  __shared__ int spiv[4][BS + 1];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * 4 + wid;
+  const int nw = gridDim.x * 4;
+  const int B2 = BS * BS;
+  for (int r = gw; r < nrows_lvl; r += nw) {
+    const int i = rows[r];
+    for (int j = rowp[i]; cols[j] < i; j++) {
+      const T *a = &F[(size_t)B2 * j];
+      const T *b = &F[(size_t)B2 * diag[cols[j]]];
+      for (int k = lane; k < B2; k += 32) {
+        const int rr = k / BS, cc = k - BS * rr;
+        T s = 0;
+#pragma unroll
+        for (int q = 0; q < BS; q++) s += a[BS * rr + q] * b[BS * q + cc];
+        sd[wid][k] = s;
+      }
+      __syncwarp();
+      for (int u = upd_ptr[j]; u < upd_ptr[j + 1]; u++) {
+        T *ak = &F[(size_t)B2 * upd_tgt[u]];
+        const T *bp = &F[(size_t)B2 * upd_src[u]];
+        for (int k = lane; k < B2; k += 32) {
+          const int rr = k / BS, cc = k - BS * rr;
+          T s = 0;
+#pragma unroll
+          for (int q = 0; q < BS; q++) s += sd[wid][BS * rr + q] * bp[BS * q + cc];
+          ak[k] -= s;
+        }
+      }
+      __syncwarp();
+      for (int k = lane; k < B2; k += 32) F[(size_t)B2 * j + k] = sd[wid][k];
+      __syncwarp();
+    }
+    warp_block_inverse<BS, T>(&F[(size_t)B2 * diag[i]], slu[wid], spiv[wid],
+                              lane, fail_flag, i);
+  }
+}
+
+// Diagonal-block inverses only (block Jacobi)
+template <int BS, typename T>
+__global__ void __launch_bounds__(128)
+    diag_inverse_kernel(int nrows, const int *__restrict__ diag, T *F,
+                        int *fail_flag) {
+  __shared__ T slu[4][BS * BS];
+  __shared__ int spiv[4][BS + 1];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * 4 + wid; i < nrows; i += gridDim.x * 4)
+    warp_block_inverse<BS, T>(&F[(size_t)BS * BS * diag[i]], slu[wid],
+                              spiv[wid], lane, fail_flag, i);
+}
+
+// Lower solve of one level: y_i = x_i - sum_{j<i} L_ij y_cj
+// (BCSRMatApplyLower6, unit lower)
+template <int BS, typename T>
+__global__ void __launch_bounds__(256)
+    ilu_lower_level_kernel(const int *__restrict__ rows, int nrows_lvl,
+                           const int *__restrict__ rowp,
+                           const int *__restrict__ cols,
+                           const T *__restrict__ F, const T *__restrict__ x,
+                           T *__restrict__ y) {
+  const int per_warp = 32 / BS;
+  const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
+  if (sub >= per_warp) return;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int r = gw * per_warp + sub; r < nrows_lvl; r += nw * per_warp) {
+    const int i = rows[r];
+    T z = x[(size_t)BS * i + ii];
+    for (int j = rowp[i]; cols[j] < i; j++) {
+      const T *a = &F[(size_t)BS * BS * j + BS * ii];
+      const T *yy = &y[(size_t)BS * cols[j]];
+      T s = 0;
+#pragma unroll
+      for (int c = 0; c < BS; c++) s += a[c] * yy[c];
+      z -= s;
+    }
+    y[(size_t)BS * i + ii] = z;
+  }
+}
+
+// Upper solve of one level: z_i = y_i - sum_{j>i} U_ij x_cj ; x_i = D_i^-1 z
+template <int BS, typename T>
+__global__ void __launch_bounds__(256)
+    ilu_upper_level_kernel(const int *__restrict__ rows, int nrows_lvl,
+                           const int *__restrict__ rowp,
+                           const int *__restrict__ cols,
+                           const int *__restrict__ diag,
+                           const T *__restrict__ F, const T *__restrict__ yin,
+                           T *__restrict__ xout) {
+  const int per_warp = 32 / BS;
+  const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nrounds = (nrows_lvl + nw * per_warp - 1) / (nw * per_warp);
+  for (int rd = 0; rd < nrounds; rd++) {
+    const int r = (rd * nw + gw) * per_warp + sub;
+    const bool active = sub < per_warp && r < nrows_lvl;
+    T z = 0;
+    int i = 0;
+    if (active) {
+      i = rows[r];
+      z = yin[(size_t)BS * i + ii];
+      for (int j = diag[i] + 1; j < rowp[i + 1]; j++) {
+        const T *a = &F[(size_t)BS * BS * j + BS * ii];
+        const T *xx = &xout[(size_t)BS * cols[j]];
+        T s = 0;
+#pragma unroll
+        for (int c = 0; c < BS; c++) s += a[c] * xx[c];
+        z -= s;
+      }
+    }
+    const int base = lane - ii;
+    T out = 0;
+    const T *dinv = active ? &F[(size_t)BS * BS * diag[i] + BS * ii] : nullptr;
+#pragma unroll
+    for (int c = 0; c < BS; c++) {
+      T zc = __shfl_sync(0xffffffffu, z, base + c);
+      if (active) out += dinv[c] * zc;
+    }
+    if (active) xout[(size_t)BS * i + ii] = out;
+  }
+}
+
+template <int BS, typename T>
+__global__ void __launch_bounds__(256)
+    block_jacobi_kernel(int nrows, const int *__restrict__ diag,
+                        const T *__restrict__ F, const T *__restrict__ x,
+                        T *__restrict__ y) {
+  const int per_warp = 32 / BS;
+  const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
+  if (sub >= per_warp) return;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw * per_warp + sub; i < nrows; i += nw * per_warp) {
+    const T *a = &F[(size_t)BS * BS * diag[i] + BS * ii];
+    const T *xx = &x[(size_t)BS * i];
+    T s = 0;
+#pragma unroll
+    for (int c = 0; c < BS; c++) s += a[c] * xx[c];
+    y[(size_t)BS * i + ii] = s;
+  }
+}
+
+// --------------------------------------------------------------- GMRES
+// partial dot products of w with the k basis vectors W_j (column j at
+// W + j*ld): partials[blk * k + j]
+__global__ void dots_partial_kernel(const double *__restrict__ W, size_t ld,
+                                    int k, const double *__restrict__ w,
+                                    double *__restrict__ partials) {
+  extern __shared__ double sh[];  // blockDim.x
+  size_t chunk = (ld + gridDim.x - 1) / gridDim.x;
+  size_t b = chunk * blockIdx.x, e = b + chunk < ld ? b + chunk : ld;
+  for (int j = 0; j < k; j++) {
+    const double *Wj = W + (size_t)j * ld;
+    double acc = 0.0;
+    for (size_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += Wj[i] * w[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * k + j] = sh[0];
+    __syncthreads();
+  }
+}
+__global__ void dots_final_kernel(const double *partials, int npart, int k,
+                                  double *h) {
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    double acc = 0.0;
+    for (int p = 0; p < npart; p++) acc += partials[(size_t)p * k + j];
+    h[j] = acc;
+  }
+}
+__global__ void gemv_sub_kernel(const double *__restrict__ W, size_t ld, int k,
+                                const double *__restrict__ h,
+                                double *__restrict__ w) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ld;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double acc = w[i];
+    for (int j = 0; j < k; j++) acc -= h[j] * W[(size_t)j * ld + i];
+    w[i] = acc;
+  }
+}
+__global__ void axpy_kernel(double a, const double *x, double *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void scale_kernel(double a, double *x, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    x[i] *= a;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- launchers
+void launch_bcsr_mult(int bsize, int nrows, const int *rowp, const int *cols,
+                      const double *A, const double *x, double *y,
+                      cudaStream_t s) {
+  if (bsize == 6) mult_dispatch<6, double>(nrows, rowp, cols, A, x, y, s);
+  else mult_dispatch<3, double>(nrows, rowp, cols, A, x, y, s);
+}
+void launch_bcsr_mult_f32(int bsize, int nrows, const int *rowp,
+                          const int *cols, const float *A, const float *x,
+                          float *y, cudaStream_t s) {
+  if (bsize == 6) mult_dispatch<6, float>(nrows, rowp, cols, A, x, y, s);
+  else mult_dispatch<3, float>(nrows, rowp, cols, A, x, y, s);
+}
+void launch_apply_bcs_mat(int bsize, int nbcs, const int *bc_nodes,
+                          const int *bc_masks, const int *rowp,
+                          const int *cols, double *A, cudaStream_t s) {
+  if (nbcs <= 0) return;
+  dim3 th(32, 4);
+  int blocks = (nbcs + 3) / 4;
+  if (blocks > 4096) blocks = 4096;
+  apply_bcs_mat_kernel<<<blocks, th, 0, s>>>(bsize, nbcs, bc_nodes, bc_masks,
+                                             rowp, cols, A);
+}
+void launch_apply_bcs_res(int bsize, int nbcs, const int *bc_nodes,
+                          const int *bc_masks, const double *vars,
+                          double *res, cudaStream_t s) {
+  if (nbcs <= 0) return;
+  apply_bcs_res_kernel<<<blocks_for(nbcs, 256), 256, 0, s>>>(
+      bsize, nbcs, bc_nodes, bc_masks, vars, res);
+}
+void launch_fill(double *x, double v, size_t n, cudaStream_t s) {
+  if (!n) return;
+  fill_kernel<<<blocks_for(n, 256), 256, 0, s>>>(x, v, n);
+}
+void launch_d2f(const double *x, float *y, size_t n, cudaStream_t s) {
+  if (!n) return;
+  d2f_kernel<<<blocks_for(n, 256), 256, 0, s>>>(x, y, n);
+}
+void launch_f2d(const float *x, double *y, size_t n, cudaStream_t s) {
+  if (!n) return;
+  f2d_kernel<<<blocks_for(n, 256), 256, 0, s>>>(x, y, n);
+}
+void launch_gather_dv(int nelem, const int *dvnum, const double *dvs,
+                      double *thick, cudaStream_t s) {
+  if (nelem <= 0) return;
+  gather_dv_kernel<<<blocks_for(nelem, 256), 256, 0, s>>>(nelem, dvnum, dvs,
+                                                          thick);
+}
+void launch_scatter_dv(int ndv, const int *dv_ptr, const int *dv_elems,
+                       const double *vals, double *dfdx, cudaStream_t s) {
+  if (ndv <= 0) return;
+  scatter_dv_kernel<<<blocks_for(ndv, 256), 256, 0, s>>>(ndv, dv_ptr,
+                                                         dv_elems, vals, dfdx);
+}
+void launch_reduce_max(const double *x, size_t n, double *partials, int npart,
+                       double *out, cudaStream_t s) {
+  reduce_partial_kernel<1><<<npart, 256, 0, s>>>(x, nullptr, n, nullptr, 0.0,
+                                                 partials);
+  reduce_final_kernel<1><<<1, 256, 0, s>>>(partials, npart, out);
+}
+void launch_reduce_sum(const double *x, size_t n, double *partials, int npart,
+                       double *out, cudaStream_t s) {
+  reduce_partial_kernel<0><<<npart, 256, 0, s>>>(x, nullptr, n, nullptr, 0.0,
+                                                 partials);
+  reduce_final_kernel<0><<<1, 256, 0, s>>>(partials, npart, out);
+}
+void launch_ks_sum(const double *fail, const double *wdet, size_t n,
+                   const double *dmax, double ksw, double *partials, int npart,
+                   double *out, cudaStream_t s) {
+  reduce_partial_kernel<2><<<npart, 256, 0, s>>>(fail, wdet, n, dmax, ksw,
+                                                 partials);
+  reduce_final_kernel<0><<<1, 256, 0, s>>>(partials, npart, out);
+}
+
+template <typename T>
+static void factor_level(const IluPlan &p, int level, T *F, cudaStream_t s) {
+  const int b = p.lvl_ptr_h[level], n = p.lvl_ptr_h[level + 1] - b;
+  if (n <= 0) return;
+  int blocks = (n + 3) / 4;
+  if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+  if (p.bsize == 6)
+    ilu0_factor_level_kernel<6, T><<<blocks, 128, 0, s>>>(
+        p.lvl_rows + b, n, p.rowp, p.cols, p.diag, p.upd_ptr, p.upd_tgt,
+        p.upd_src, F, p.d_fail);
+  else
+    ilu0_factor_level_kernel<3, T><<<blocks, 128, 0, s>>>(
+        p.lvl_rows + b, n, p.rowp, p.cols, p.diag, p.upd_ptr, p.upd_tgt,
+        p.upd_src, F, p.d_fail);
+}
+void launch_ilu0_factor_level(const IluPlan &p, int level, double *F,
+                              cudaStream_t s) {
+  factor_level<double>(p, level, F, s);
+}
+void launch_ilu0_factor_level_f32(const IluPlan &p, int level, float *F,
+                                  cudaStream_t s) {
+  factor_level<float>(p, level, F, s);
+}
+void launch_block_inverse_diag(const IluPlan &p, double *F, cudaStream_t s) {
+  int blocks = (p.nrows + 3) / 4;
+  if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+  if (p.bsize == 6)
+    diag_inverse_kernel<6, double><<<blocks, 128, 0, s>>>(p.nrows, p.diag, F,
+                                                          p.d_fail);
+  else
+    diag_inverse_kernel<3, double><<<blocks, 128, 0, s>>>(p.nrows, p.diag, F,
+                                                          p.d_fail);
+}
+
+template <typename T>
+static void apply_levels(const IluPlan &p, const T *F, const T *x, T *y,
+                         T *tmp, cudaStream_t s) {
+  const int per_warp = 32 / p.bsize;
+  const int nl = (int)p.lvl_ptr_h.size() - 1;
+  for (int L = 0; L < nl; L++) {
+    const int b = p.lvl_ptr_h[L], n = p.lvl_ptr_h[L + 1] - b;
+    int blocks = blocks_for((size_t)((n + per_warp - 1) / per_warp) * 32, 256, 16);
+    if (p.bsize == 6)
+      ilu_lower_level_kernel<6, T><<<blocks, 256, 0, s>>>(p.lvl_rows + b, n,
+                                                          p.rowp, p.cols, F, x,
+                                                          tmp);
+    else
+      ilu_lower_level_kernel<3, T><<<blocks, 256, 0, s>>>(p.lvl_rows + b, n,
+                                                          p.rowp, p.cols, F, x,
+                                                          tmp);
+  }
+  const int nu = (int)p.ulvl_ptr_h.size() - 1;
+  for (int L = 0; L < nu; L++) {
+    const int b = p.ulvl_ptr_h[L], n = p.ulvl_ptr_h[L + 1] - b;
+    int blocks = blocks_for((size_t)((n + per_warp - 1) / per_warp) * 32, 256, 16);
+    if (p.bsize == 6)
+      ilu_upper_level_kernel<6, T><<<blocks, 256, 0, s>>>(
+          p.ulvl_rows + b, n, p.rowp, p.cols, p.diag, F, tmp, y);
+    else
+      ilu_upper_level_kernel<3, T><<<blocks, 256, 0, s>>>(
+          p.ulvl_rows + b, n, p.rowp, p.cols, p.diag, F, tmp, y);
+  }
+}
+void launch_ilu0_apply(const IluPlan &p, const double *F, const double *x,
+                       double *y, double *tmp, cudaStream_t s) {
+  apply_levels<double>(p, F, x, y, tmp, s);
+}
+void launch_ilu0_apply_f32(const IluPlan &p, const float *F, const float *x,
+                           float *y, float *tmp, cudaStream_t s) {
+  apply_levels<float>(p, F, x, y, tmp, s);
+}
+void launch_block_jacobi_apply(const IluPlan &p, const double *F,
+                               const double *x, double *y, cudaStream_t s) {
+  const int per_warp = 32 / p.bsize;
+  int blocks = blocks_for((size_t)((p.nrows + per_warp - 1) / per_warp) * 32,
+                          256, 16);
+  if (p.bsize == 6)
+    block_jacobi_kernel<6, double><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F,
+                                                          x, y);
+  else
+    block_jacobi_kernel<3, double><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F,
+                                                          x, y);
+}
+void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,
+                                   const float *x, float *y, cudaStream_t s) {
+  const int per_warp = 32 / p.bsize;
+  int blocks = blocks_for((size_t)((p.nrows + per_warp - 1) / per_warp) * 32,
+                          256, 16);
+  if (p.bsize == 6)
+    block_jacobi_kernel<6, float><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F, x,
+                                                         y);
+  else
+    block_jacobi_kernel<3, float><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F, x,
+                                                         y);
+}
+
+void launch_dots(const double *W, size_t ld, int k, const double *w,
+                 double *partials, int npart, double *h, cudaStream_t s) {
+  dots_partial_kernel<<<npart, 256, 256 * sizeof(double), s>>>(W, ld, k, w,
+                                                               partials);
+  dots_final_kernel<<<1, 128, 0, s>>>(partials, npart, k, h);
+}
+void launch_gemv_sub(const double *W, size_t ld, int k, const double *h,
+                     double *w, size_t n, cudaStream_t s) {
+  (void)n;
+  gemv_sub_kernel<<<blocks_for(ld, 256), 256, 0, s>>>(W, ld, k, h, w);
+}
+void launch_axpy(double a, const double *x, double *y, size_t n,
+                 cudaStream_t s) {
+  if (!n) return;
+  axpy_kernel<<<blocks_for(n, 256), 256, 0, s>>>(a, x, y, n);
+}
+void launch_scale(double a, double *x, size_t n, cudaStream_t s) {
+  if (!n) return;
+  scale_kernel<<<blocks_for(n, 256), 256, 0, s>>>(a, x, n);
+}
+void launch_copy(const double *x, double *y, size_t n, cudaStream_t s) {
+  if (!n) return;
+  cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace tg

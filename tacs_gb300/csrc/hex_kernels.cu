@@ -1,0 +1,506 @@
+// Trilinear hex8 elasticity kernels (TACSElement3D with
+// TACSLinearElasticity3D(TACS_LINEAR_STRAIN) and TACSLinearHexaBasis) for
+// sm_103a.  One warp per element: 8 lanes build the Gauss-point Jacobians,
+// all lanes form the physical shape gradients, then the 36 upper 3x3 node
+// blocks of K = sum_q detXd_q B^T (t C) B are formed in the closed
+// isotropic form
+//   K_ab[i][i] = c0 Na_i Nb_i + G sum_{k!=i} Na_k Nb_k
+//   K_ab[i][j] = c1 Na_i Nb_j + G Na_j Nb_i           (i != j)
+// (the same product B^T C B as TACSElementBasis::addWeakMatrix with the
+// isotropic TACSMaterialProperties::evalTangentStiffness3D,
+// src/constitutive/TACSMaterialProperties.cpp:270-293) and added into the
+// 3x3 BCSR blocks; colouring makes the scatter atomic-free.
+#include <cmath>
+
+#include "tg_internal.h"
+
+namespace tg {
+namespace {
+
+#define TG_GPT 0.577350269189626
+
+struct HexSmem {
+  double X[24];
+  double u[24];
+  double w[24];
+  double det[8];
+  double J[8][9];
+  double Nx[8][24];
+  double e[8][6];
+  double g[8][6];
+  double coef[8];
+  double t;
+  int nodes[8];
+  int slot[64];
+};
+
+__device__ __forceinline__ double gauss2(int i) {
+  return i ? TG_GPT : -TG_GPT;
+}
+
+__device__ double inv3(const double *A, double *Ai) {
+  double det = (A[8] * (A[0] * A[4] - A[3] * A[1]) -
+                A[7] * (A[0] * A[5] - A[3] * A[2]) +
+                A[6] * (A[1] * A[5] - A[2] * A[4]));
+  double di = 1.0 / det;
+  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * di;
+  Ai[1] = -(A[1] * A[8] - A[2] * A[7]) * di;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * di;
+  Ai[3] = -(A[3] * A[8] - A[5] * A[6]) * di;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * di;
+  Ai[5] = -(A[0] * A[5] - A[2] * A[3]) * di;
+  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * di;
+  Ai[7] = -(A[0] * A[7] - A[1] * A[6]) * di;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * di;
+  return det;
+}
+
+// TACSLinearHexaBasis::computeBasis / computeBasisGradient
+// (src/elements/basis/TACSHexaBasis.cpp:137-170), node m = i + 2j + 4k
+__device__ __forceinline__ void hex_shape(const double *pt, double *N,
+                                          double *Nxi) {
+  double x[2] = {1.0 - pt[0], 1.0 + pt[0]};
+  double y[2] = {1.0 - pt[1], 1.0 + pt[1]};
+  double z[2] = {1.0 - pt[2], 1.0 + pt[2]};
+#pragma unroll
+  for (int m = 0; m < 8; m++) {
+    const int i = m & 1, j = (m >> 1) & 1, k = m >> 2;
+    const double si = i ? 1.0 : -1.0, sj = j ? 1.0 : -1.0, sk = k ? 1.0 : -1.0;
+    if (N) N[m] = 0.125 * x[i] * y[j] * z[k];
+    Nxi[3 * m] = 0.125 * si * y[j] * z[k];
+    Nxi[3 * m + 1] = 0.125 * x[i] * sj * z[k];
+    Nxi[3 * m + 2] = 0.125 * x[i] * y[j] * sk;
+  }
+}
+
+__device__ __constant__ unsigned char c_pair[36][2] = {
+    {0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {0, 6}, {0, 7}, {1, 1},
+    {1, 2}, {1, 3}, {1, 4}, {1, 5}, {1, 6}, {1, 7}, {2, 2}, {2, 3}, {2, 4},
+    {2, 5}, {2, 6}, {2, 7}, {3, 3}, {3, 4}, {3, 5}, {3, 6}, {3, 7}, {4, 4},
+    {4, 5}, {4, 6}, {4, 7}, {5, 5}, {5, 6}, {5, 7}, {6, 6}, {6, 7}, {7, 7}};
+
+struct HexC {
+  double c0, c1, G;
+};
+// TACSMaterialProperties::evalTangentStiffness3D, isotropic branch
+__device__ __forceinline__ HexC hex_c(const ElemParams &ep) {
+  HexC c;
+  double D = ep.E / ((1.0 + ep.nu) * (1.0 - 2.0 * ep.nu));
+  c.c0 = (1.0 - ep.nu) * D;
+  c.c1 = ep.nu * D;
+  c.G = 0.5 * ep.E / (1.0 + ep.nu);
+  return c;
+}
+__device__ __forceinline__ void hex_Ce(const HexC &c, const double *e,
+                                       double *s) {
+  s[0] = c.c0 * e[0] + c.c1 * e[1] + c.c1 * e[2];
+  s[1] = c.c1 * e[0] + c.c0 * e[1] + c.c1 * e[2];
+  s[2] = c.c1 * e[0] + c.c1 * e[1] + c.c0 * e[2];
+  s[3] = c.G * e[3];
+  s[4] = c.G * e[4];
+  s[5] = c.G * e[5];
+}
+
+__device__ __forceinline__ int find_slot(const int *rowp, const int *cols,
+                                         int row, int col) {
+  int lo = rowp[row], hi = rowp[row + 1] - 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    int c = cols[mid];
+    if (c == col) return mid;
+    if (c < col) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+__device__ void hex_load(HexSmem &S, const MeshView &m, int e,
+                         const double *vars, const double *vars2, int lane) {
+  if (lane < 8) S.nodes[lane] = m.conn[8 * e + lane];
+  if (lane == 0) S.t = m.thick[e];
+  __syncwarp();
+  if (lane < 24) {
+    const int nd = S.nodes[lane / 3], k = lane % 3;
+    S.X[lane] = m.xpts[3 * nd + k];
+    S.u[lane] = vars ? vars[3 * nd + k] : 0.0;
+    if (vars2) S.w[lane] = vars2[3 * nd + k];
+  }
+  __syncwarp();
+}
+
+// Gauss-point Jacobians and physical shape gradients
+// (TACSElementBasis::getFieldGradient, TACSElementBasis.cpp:266-330)
+__device__ void hex_geometry(HexSmem &S, int lane) {
+  if (lane < 8) {
+    const int q = lane;
+    double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1), gauss2(q >> 2)};
+    double Nxi[24], Xd[9];
+    hex_shape(pt, nullptr, Nxi);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        double v = 0.0;
+#pragma unroll
+        for (int mm = 0; mm < 8; mm++) v += Nxi[3 * mm + j] * S.X[3 * mm + i];
+        Xd[3 * i + j] = v;
+      }
+    S.det[q] = inv3(Xd, S.J[q]);
+  }
+  __syncwarp();
+  for (int idx = lane; idx < 64; idx += 32) {
+    const int q = idx >> 3, mm = idx & 7;
+    double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1), gauss2(q >> 2)};
+    // gradient of node mm only
+    double x[2] = {1.0 - pt[0], 1.0 + pt[0]};
+    double y[2] = {1.0 - pt[1], 1.0 + pt[1]};
+    double z[2] = {1.0 - pt[2], 1.0 + pt[2]};
+    const int i = mm & 1, j = (mm >> 1) & 1, k = mm >> 2;
+    const double n0 = 0.125 * (i ? 1.0 : -1.0) * y[j] * z[k];
+    const double n1 = 0.125 * x[i] * (j ? 1.0 : -1.0) * z[k];
+    const double n2 = 0.125 * x[i] * y[j] * (k ? 1.0 : -1.0);
+    const double *J = S.J[q];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      S.Nx[q][3 * mm + c] = n0 * J[c] + n1 * J[3 + c] + n2 * J[6 + c];
+  }
+  __syncwarp();
+}
+
+// strains at the 8 points (TACSLinearElasticity3D, linear branch,
+// TACSLinearElasticity.cpp:890-900): lanes 0..7
+__device__ __forceinline__ void hex_strain(const HexSmem &S, int q,
+                                           const double *v, double *e) {
+  double Ux[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int mm = 0; mm < 8; mm++)
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) Ux[3 * i + j] += v[3 * mm + i] * S.Nx[q][3 * mm + j];
+  e[0] = Ux[0];
+  e[1] = Ux[4];
+  e[2] = Ux[8];
+  e[3] = Ux[5] + Ux[7];
+  e[4] = Ux[2] + Ux[6];
+  e[5] = Ux[1] + Ux[3];
+}
+// (B^T s) component for dof (mm, i) at point q
+__device__ __forceinline__ double hex_bts(const HexSmem &S, int q, int mm,
+                                          int i, const double *s) {
+  const double *g = &S.Nx[q][3 * mm];
+  if (i == 0) return g[0] * s[0] + g[1] * s[5] + g[2] * s[4];
+  if (i == 1) return g[1] * s[1] + g[0] * s[5] + g[2] * s[3];
+  return g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    hex_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                        const double *__restrict__ vars, double lambda,
+                        double *__restrict__ res, double *__restrict__ mat,
+                        int transpose) {
+  __shared__ HexSmem smem[WARPS];
+  HexSmem &S = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const HexC c = hex_c(ep);
+  (void)transpose;  // K is symmetric by construction (mirrored blocks)
+
+  for (int idx = gw; idx < cr.count; idx += nw) {
+    const int e = cr.elem_list[idx];
+    hex_load(S, m, e, vars, nullptr, lane);
+    if (mat)
+      for (int k = lane; k < 64; k += 32)
+        S.slot[k] = find_slot(m.rowp, m.cols, S.nodes[k >> 3], S.nodes[k & 7]);
+    hex_geometry(S, lane);
+
+    if (res) {
+      if (lane < 8) {
+        double ev[6], s[6];
+        hex_strain(S, lane, S.u, ev);
+        hex_Ce(c, ev, s);
+        for (int k = 0; k < 6; k++) S.g[lane][k] = s[k] * S.t;
+      }
+      __syncwarp();
+      if (lane < 24) {
+        const int mm = lane / 3, i = lane % 3;
+        double rk = 0.0;
+        for (int q = 0; q < 8; q++) rk += S.det[q] * hex_bts(S, q, mm, i, S.g[q]);
+        // TACSTraction3D::addResidual (TACSTraction3D.cpp:87-125) with
+        // TACSElementBasis::getFaceNormal (TACSElementBasis.cpp:37-63)
+        if (m.trac_ptr) {
+          double aux = 0.0;
+          for (int tk = m.trac_ptr[e]; tk < m.trac_ptr[e + 1]; tk++) {
+            const int face = m.trac_face[tk];
+            const double tr = m.trac_val[3 * tk + i];
+            double t1d[3], t2d[3];
+            // face tangents (TACSHexaBasis.cpp:21-70)
+            const int f2 = face >> 1;
+            for (int n = 0; n < 4; n++) {
+              double a = gauss2(n & 1), b = gauss2(n >> 1);
+              double cc = -1.0 + 2.0 * (face & 1);
+              double pt[3];
+              if (f2 == 0) { pt[0] = cc; pt[1] = a; pt[2] = b; }
+              else if (f2 == 1) { pt[0] = a; pt[1] = cc; pt[2] = b; }
+              else { pt[0] = a; pt[1] = b; pt[2] = cc; }
+              double N[8], Nxi[24], Xd[9];
+              hex_shape(pt, N, Nxi);
+              for (int ii = 0; ii < 3; ii++)
+                for (int jj = 0; jj < 3; jj++) {
+                  double v = 0.0;
+                  for (int q = 0; q < 8; q++) v += Nxi[3 * q + jj] * S.X[3 * q + ii];
+                  Xd[3 * ii + jj] = v;
+                }
+              int ta, tb;  // parametric directions spanning the face
+              if (f2 == 0) { ta = 2; tb = 1; }
+              else if (f2 == 1) { ta = 0; tb = 2; }
+              else { ta = 1; tb = 0; }
+              if (face == 1) { ta = 1; tb = 2; }
+              if (face == 3) { ta = 2; tb = 0; }
+              if (face == 5) { ta = 0; tb = 1; }
+              for (int ii = 0; ii < 3; ii++) {
+                t1d[ii] = Xd[3 * ii + ta];
+                t2d[ii] = Xd[3 * ii + tb];
+              }
+              double nr[3] = {t1d[1] * t2d[2] - t1d[2] * t2d[1],
+                              t1d[2] * t2d[0] - t1d[0] * t2d[2],
+                              t1d[0] * t2d[1] - t1d[1] * t2d[0]};
+              double area = sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+              aux += area * N[mm] * -tr;
+            }
+          }
+          rk += lambda * aux;
+        }
+        res[3 * S.nodes[mm] + i] += rk;
+      }
+    }
+
+    if (mat) {
+      const double t = S.t;
+      for (int idx2 = lane; idx2 < 324; idx2 += 32) {
+        const int p = idx2 / 9, w = idx2 - 9 * p;
+        const int a = c_pair[p][0], b = c_pair[p][1];
+        const int i = w / 3, j = w - 3 * i;
+        double kij = 0.0;
+        for (int q = 0; q < 8; q++) {
+          const double *Na = &S.Nx[q][3 * a], *Nb = &S.Nx[q][3 * b];
+          double v;
+          if (i == j) {
+            double sh = 0.0;
+            for (int k = 0; k < 3; k++)
+              if (k != i) sh += Na[k] * Nb[k];
+            v = c.c0 * Na[i] * Nb[i] + c.G * sh;
+          } else {
+            v = c.c1 * Na[i] * Nb[j] + c.G * Na[j] * Nb[i];
+          }
+          kij += S.det[q] * (t * v);
+        }
+        const int s_ab = S.slot[8 * a + b], s_ba = S.slot[8 * b + a];
+        if (s_ab >= 0) mat[9 * (size_t)s_ab + w] += kij;
+        if (a != b && s_ba >= 0) mat[9 * (size_t)s_ba + 3 * j + i] += kij;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+struct HexFail {
+  double f, dfde[6];
+};
+// TACSSolidConstitutive::evalFailure / evalFailureStrainSens
+// (TACSSolidConstitutive.cpp:274-330) with vonMisesFailure3D(StressSens)
+__device__ HexFail hex_failure(const ElemParams &ep, const HexC &c,
+                               const double *e) {
+  HexFail o;
+  double s[6];
+  hex_Ce(c, e, s);
+  double f = sqrt(0.5 * ((s[0] - s[1]) * (s[0] - s[1]) +
+                         (s[0] - s[2]) * (s[0] - s[2]) +
+                         (s[1] - s[2]) * (s[1] - s[2]) +
+                         6.0 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5])));
+  double sens[6] = {0, 0, 0, 0, 0, 0};
+  if (f != 0.0) {
+    double fact = 0.5 / (ep.ys * f);
+    sens[0] = fact * (2.0 * s[0] - s[1] - s[2]);
+    sens[1] = fact * (2.0 * s[1] - s[0] - s[2]);
+    sens[2] = fact * (2.0 * s[2] - s[0] - s[1]);
+    sens[3] = 6.0 * fact * s[3];
+    sens[4] = 6.0 * fact * s[4];
+    sens[5] = 6.0 * fact * s[5];
+  }
+  o.f = f / ep.ys;
+  hex_Ce(c, sens, o.dfde);
+  return o;
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    hex_points_kernel(ElemParams ep, MeshView m, const double *__restrict__ vars,
+                      double *__restrict__ elem_fail,
+                      double *__restrict__ elem_wdet,
+                      double *__restrict__ elem_sed) {
+  __shared__ HexSmem smem[WARPS];
+  HexSmem &S = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const HexC c = hex_c(ep);
+  for (int e = gw; e < m.nelem; e += nw) {
+    hex_load(S, m, e, vars, nullptr, lane);
+    hex_geometry(S, lane);
+    if (lane < 8) {
+      double ev[6], s[6];
+      hex_strain(S, lane, S.u, ev);
+      hex_Ce(c, ev, s);
+      double sed = 0.0;
+      for (int k = 0; k < 6; k++) sed += ev[k] * (s[k] * S.t);
+      HexFail fo = hex_failure(ep, c, ev);
+      elem_fail[8 * (size_t)e + lane] = fo.f;
+      elem_wdet[8 * (size_t)e + lane] = S.det[lane];
+      S.coef[lane] = S.det[lane] * sed;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double acc = 0.0;
+      for (int q = 0; q < 8; q++) acc += S.coef[q];
+      elem_sed[e] = acc;
+    }
+    __syncwarp();
+  }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    hex_sv_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                  const double *__restrict__ vars, int func, KsStats ks,
+                  double alpha, double *__restrict__ dfdu) {
+  __shared__ HexSmem smem[WARPS];
+  HexSmem &S = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const HexC c = hex_c(ep);
+  for (int idx = gw; idx < cr.count; idx += nw) {
+    const int e = cr.elem_list[idx];
+    hex_load(S, m, e, vars, nullptr, lane);
+    hex_geometry(S, lane);
+    if (lane < 8) {
+      double ev[6], s[6];
+      hex_strain(S, lane, S.u, ev);
+      if (func == TG_FUNC_COMPLIANCE) {
+        hex_Ce(c, ev, s);
+        for (int k = 0; k < 6; k++) S.g[lane][k] = 2.0 * (s[k] * S.t);
+        S.coef[lane] = S.det[lane];
+      } else {
+        HexFail fo = hex_failure(ep, c, ev);
+        for (int k = 0; k < 6; k++) S.g[lane][k] = fo.dfde[k];
+        S.coef[lane] =
+            exp(ks.weight * (fo.f - ks.max)) / ks.sum * S.det[lane];
+      }
+    }
+    __syncwarp();
+    if (lane < 24) {
+      const int mm = lane / 3, i = lane % 3;
+      double acc = 0.0;
+      for (int q = 0; q < 8; q++) acc += S.coef[q] * hex_bts(S, q, mm, i, S.g[q]);
+      dfdu[3 * S.nodes[mm] + i] += alpha * acc;
+    }
+    __syncwarp();
+  }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    hex_dv_kernel(ElemParams ep, MeshView m, const double *__restrict__ vars,
+                  int func, KsStats ks, double coef,
+                  const double *__restrict__ psi, double scale,
+                  double *__restrict__ out) {
+  __shared__ HexSmem smem[WARPS];
+  HexSmem &S = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const HexC c = hex_c(ep);
+  for (int e = gw; e < m.nelem; e += nw) {
+    hex_load(S, m, e, vars, psi, lane);
+    hex_geometry(S, lane);
+    if (lane < 8) {
+      double ev[6], s[6], acc = 0.0;
+      hex_strain(S, lane, S.u, ev);
+      hex_Ce(c, ev, s);
+      if (func == TG_FUNC_COMPLIANCE) {
+        // TACSSolidConstitutive::addStressDVSens(e, e) (.cpp:181-209)
+        double v = 0.0;
+        for (int k = 0; k < 6; k++) v += s[k] * ev[k];
+        acc += coef * S.det[lane] * v;
+      }
+      // the solid failure index does not depend on t (no addFailureDVSens)
+      if (psi) {
+        double ep2[6];
+        hex_strain(S, lane, S.w, ep2);
+        double v = 0.0;
+        for (int k = 0; k < 6; k++) v += s[k] * ep2[k];
+        acc += scale * S.det[lane] * v;
+      }
+      S.coef[lane] = acc;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double acc = 0.0;
+      for (int q = 0; q < 8; q++) acc += S.coef[q];
+      out[e] = acc;
+    }
+    __syncwarp();
+  }
+  (void)ks;
+}
+
+constexpr int kWarps = 8;
+
+int grid_for(int count) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int need = (count + kWarps - 1) / kWarps;
+  int cap = sms * 4;
+  if (need < 1) need = 1;
+  return need < cap ? need : cap;
+}
+
+}  // namespace
+
+void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
+                         ColorRange cr, const double *vars, double lambda,
+                         double *res, double *mat, int transpose,
+                         cudaStream_t s) {
+  if (cr.count <= 0) return;
+  hex_assembly_kernel<kWarps><<<grid_for(cr.count), kWarps * 32, 0, s>>>(
+      ep, m, cr, vars, lambda, res, mat, transpose);
+}
+void launch_hex_points(const ElemParams &ep, const MeshView &m,
+                       const double *vars, double *elem_fail,
+                       double *elem_wdet, double *elem_sed, cudaStream_t s) {
+  if (m.nelem <= 0) return;
+  hex_points_kernel<kWarps><<<grid_for(m.nelem), kWarps * 32, 0, s>>>(
+      ep, m, vars, elem_fail, elem_wdet, elem_sed);
+}
+void launch_hex_sv_sens(const ElemParams &ep, const MeshView &m,
+                        ColorRange cr, const double *vars, int func,
+                        KsStats ks, double alpha, double *dfdu,
+                        cudaStream_t s) {
+  if (cr.count <= 0) return;
+  hex_sv_kernel<kWarps><<<grid_for(cr.count), kWarps * 32, 0, s>>>(
+      ep, m, cr, vars, func, ks, alpha, dfdu);
+}
+void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
+                   int func, KsStats ks, double coef, const double *psi,
+                   double scale, double *out, cudaStream_t s) {
+  if (m.nelem <= 0) return;
+  hex_dv_kernel<kWarps><<<grid_for(m.nelem), kWarps * 32, 0, s>>>(
+      ep, m, vars, func, ks, coef, psi, scale, out);
+}
+
+}  // namespace tg

@@ -1,0 +1,172 @@
+// Internal declarations shared by the sm_103a kernels and the C++ host
+// runtime of libtacs_gb300.  Not part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tacs_gb300.h"
+
+namespace tg {
+
+// Material and element constants shared by every element of one assembler.
+struct ElemParams {
+  int elem_type;  // TG_ELEM_MITC4 / TG_ELEM_HEX8
+  double rho, E, nu, ys;
+  int transform;       // shells: 0 natural, 1 reference axis
+  double ref_axis[3];  // normalised reference axis
+};
+
+// Device-side view of an assembler used by the element kernels.
+struct MeshView {
+  int nnodes, nelem, vpn, npe;
+  const int *conn;        // npe * nelem
+  const double *xpts;     // 3 * nnodes
+  const double *thick;    // nelem
+  const double *pres;     // 4 * nelem nodal pressures or nullptr
+  const int *trac_ptr;    // nelem + 1 (hex tractions) or nullptr
+  const int *trac_face;   // per traction entry
+  const double *trac_val; // 3 per traction entry
+  const int *rowp, *cols; // BCSR pattern
+};
+
+// One launch of an element kernel covers the elements of one colour:
+// elem_list[0..count) (no two share a node, so the scatter needs no atomics).
+struct ColorRange {
+  const int *elem_list;
+  int count;
+};
+
+// ---------------------------------------------------------------- kernels
+// (defined in shell_kernels.cu / hex_kernels.cu / bcsr_kernels.cu)
+
+// Residual (and optionally Jacobian) assembly of one colour.
+// mat may be nullptr (residual only); res may be nullptr (matrix only).
+void launch_shell_assembly(const ElemParams &ep, const MeshView &m,
+                           ColorRange cr, const double *vars, double lambda,
+                           double *res, double *mat, int transpose,
+                           cudaStream_t s);
+void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
+                         ColorRange cr, const double *vars, double lambda,
+                         double *res, double *mat, int transpose,
+                         cudaStream_t s);
+
+// Point quantities.  Pass 1 writes per-element, per-point failure values
+// and detXd-weighted strain energies; the KS reduction and the sensitivity
+// passes read them back.
+// elem_fail: nq per element; elem_wdet: nq per element; elem_sed: 1 per elem
+void launch_shell_points(const ElemParams &ep, const MeshView &m,
+                         const double *vars, double *elem_fail,
+                         double *elem_wdet, double *elem_sed,
+                         cudaStream_t s);
+void launch_hex_points(const ElemParams &ep, const MeshView &m,
+                       const double *vars, double *elem_fail,
+                       double *elem_wdet, double *elem_sed, cudaStream_t s);
+
+// dfdu += alpha * df/du for one colour.  func: TG_FUNC_*; for KS the
+// statistics ks_max / ks_sum / ks_weight are used.
+struct KsStats {
+  double max, sum, weight;
+};
+void launch_shell_sv_sens(const ElemParams &ep, const MeshView &m,
+                          ColorRange cr, const double *vars, int func,
+                          KsStats ks, double alpha, double *dfdu,
+                          cudaStream_t s);
+void launch_hex_sv_sens(const ElemParams &ep, const MeshView &m,
+                        ColorRange cr, const double *vars, int func,
+                        KsStats ks, double alpha, double *dfdu,
+                        cudaStream_t s);
+
+// Per-element design derivative: out[e] = coef * df/dt_e (func >= 0, or 0
+// when func < 0) + scale * psi_e^T dR_e/dt_e (psi may be nullptr).
+void launch_shell_dv(const ElemParams &ep, const MeshView &m,
+                     const double *vars, int func, KsStats ks, double coef,
+                     const double *psi, double scale, double *out,
+                     cudaStream_t s);
+void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
+                   int func, KsStats ks, double coef, const double *psi,
+                   double scale, double *out, cudaStream_t s);
+
+// ------------------------------------------------------- BCSR / vectors
+void launch_bcsr_mult(int bsize, int nrows, const int *rowp, const int *cols,
+                      const double *A, const double *x, double *y,
+                      cudaStream_t s);
+void launch_bcsr_mult_f32(int bsize, int nrows, const int *rowp,
+                          const int *cols, const float *A, const float *x,
+                          float *y, cudaStream_t s);
+void launch_apply_bcs_mat(int bsize, int nbcs, const int *bc_nodes,
+                          const int *bc_masks, const int *rowp,
+                          const int *cols, double *A, cudaStream_t s);
+void launch_apply_bcs_res(int bsize, int nbcs, const int *bc_nodes,
+                          const int *bc_masks, const double *vars,
+                          double *res, cudaStream_t s);
+void launch_fill(double *x, double v, size_t n, cudaStream_t s);
+void launch_d2f(const double *x, float *y, size_t n, cudaStream_t s);
+void launch_f2d(const float *x, double *y, size_t n, cudaStream_t s);
+void launch_gather_dv(int nelem, const int *dvnum, const double *dvs,
+                      double *thick, cudaStream_t s);
+void launch_scatter_dv(int ndv, const int *dv_ptr, const int *dv_elems,
+                       const double *elem_vals, double *dfdx, cudaStream_t s);
+
+// Deterministic reductions: partial sums per block then one final block.
+// Writes result to out (device scalar).
+void launch_reduce_max(const double *x, size_t n, double *partials,
+                       int npart, double *out, cudaStream_t s);
+void launch_reduce_sum(const double *x, size_t n, double *partials,
+                       int npart, double *out, cudaStream_t s);
+void launch_ks_sum(const double *fail, const double *wdet, size_t n,
+                   const double *dmax, double ksw, double *partials,
+                   int npart, double *out, cudaStream_t s);
+
+// Level-scheduled block ILU(0) (natural order) and block Jacobi.
+struct IluPlan {
+  int bsize, nrows;
+  const int *rowp, *cols, *diag;
+  // level sets of the lower solve / factor (rows in increasing order
+  // inside a level), and of the upper solve
+  std::vector<int> lvl_ptr_h, ulvl_ptr_h;
+  const int *lvl_rows, *ulvl_rows;
+  // factor update list: for each row, the (target, lower, upper) block
+  // triples of the IKJ update, grouped by lower block
+  const int *upd_ptr;  // per lower entry j: range into upd_tgt/upd_src
+  const int *upd_tgt, *upd_src;
+  int *d_fail;  // device int: first failing row + 1
+};
+void launch_ilu0_factor_level(const IluPlan &p, int level, double *F,
+                              cudaStream_t s);
+void launch_ilu0_factor_level_f32(const IluPlan &p, int level, float *F,
+                                  cudaStream_t s);
+void launch_block_inverse_diag(const IluPlan &p, double *F, cudaStream_t s);
+void launch_ilu0_apply(const IluPlan &p, const double *F, const double *x,
+                       double *y, double *tmp, cudaStream_t s);
+void launch_ilu0_apply_f32(const IluPlan &p, const float *F, const float *x,
+                           float *y, float *tmp, cudaStream_t s);
+void launch_block_jacobi_apply(const IluPlan &p, const double *F,
+                               const double *x, double *y, cudaStream_t s);
+void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,
+                                   const float *x, float *y, cudaStream_t s);
+
+// GMRES helpers (FP64 Arnoldi)
+void launch_dots(const double *W, size_t ld, int k, const double *w,
+                 double *partials, int npart, double *h, cudaStream_t s);
+void launch_gemv_sub(const double *W, size_t ld, int k, const double *h,
+                     double *w, size_t n, cudaStream_t s);
+void launch_axpy(double a, const double *x, double *y, size_t n,
+                 cudaStream_t s);
+void launch_scale(double a, double *x, size_t n, cudaStream_t s);
+void launch_copy(const double *x, double *y, size_t n, cudaStream_t s);
+
+// error reporting
+void set_error(const std::string &msg);
+int cuda_check(cudaError_t e, const char *what);
+
+}  // namespace tg
+
+#define TG_CUDA(call)                                 \
+  do {                                                \
+    cudaError_t _e = (call);                          \
+    if (_e != cudaSuccess) return tg::cuda_check(_e, #call); \
+  } while (0)

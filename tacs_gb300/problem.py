@@ -1,0 +1,298 @@
+"""Device-resident model built from a problem record (tacs_gb300.meshes).
+
+:class:`GpuModel` drives the C ABI of libtacs_gb300 with torch CUDA tensors
+as device storage.  It is the plumbing under the reference-style API in
+:mod:`tacs_gb300.TACS` and the object the tests and the benchmark use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class _DevArray:
+    """Exposes a raw device allocation to torch via __cuda_array_interface__."""
+
+    def __init__(self, ptr, n, typestr="<f8"):
+        self.__cuda_array_interface__ = {
+            "shape": (int(n),), "typestr": typestr, "data": (int(ptr), False),
+            "version": 3, "strides": None}
+
+
+def device_view(ptr, n, dtype=torch.float64):
+    typestr = {torch.float64: "<f8", torch.float32: "<f4",
+               torch.int32: "<i4"}[dtype]
+    return torch.as_tensor(_DevArray(ptr, n, typestr), device="cuda")
+
+
+class Mat:
+    """tg_mat: BCSR matrix with the assembler's pattern (device)."""
+
+    def __init__(self, model):
+        L = _lib.lib()
+        h = C.c_void_p()
+        check(L.tg_mat_create(model.handle, C.byref(h)), "tg_mat_create")
+        self.handle, self.model = h, model
+        bs, nr = C.c_int(), C.c_int()
+        rowp, cols, vals = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(L.tg_mat_get_arrays(h, C.byref(bs), C.byref(nr), C.byref(rowp),
+                                  C.byref(cols), C.byref(vals)))
+        self.bsize, self.nrows = bs.value, nr.value
+        self.rowp = device_view(rowp.value, self.nrows + 1, torch.int32)
+        nnz = int(self.rowp[-1].item())
+        self.nnz = nnz
+        self.cols = device_view(cols.value, nnz, torch.int32)
+        self.vals = device_view(vals.value, nnz * self.bsize ** 2)
+
+    def mult(self, x, y=None):
+        y = torch.empty_like(x) if y is None else y
+        check(_lib.lib().tg_mat_mult(self.handle, _p(x), _p(y), _stream()),
+              "tg_mat_mult")
+        return y
+
+    def __del__(self):
+        try:
+            _lib.lib().tg_mat_decref(self.handle)
+        except Exception:
+            pass
+
+
+class Pc:
+    """tg_pc: ILU(0) / block-Jacobi preconditioner, FP64 or FP32."""
+
+    def __init__(self, mat, kind=_lib.PC_ILU0, precision=_lib.PREC_FP64):
+        h = C.c_void_p()
+        check(_lib.lib().tg_pc_create(mat.handle, kind, precision,
+                                      C.byref(h)), "tg_pc_create")
+        self.handle, self.mat = h, mat
+
+    def factor(self):
+        check(_lib.lib().tg_pc_factor(self.handle, _stream()), "tg_pc_factor")
+
+    def apply(self, x, y=None):
+        y = torch.empty_like(x) if y is None else y
+        check(_lib.lib().tg_pc_apply(self.handle, _p(x), _p(y), _stream()),
+              "tg_pc_apply")
+        return y
+
+    def __del__(self):
+        try:
+            _lib.lib().tg_pc_decref(self.handle)
+        except Exception:
+            pass
+
+
+class Ksm:
+    """tg_ksm: restarted GMRES (optionally mixed precision)."""
+
+    def __init__(self, mat, pc, m=100, nrestart=2, mixed=False):
+        h = C.c_void_p()
+        check(_lib.lib().tg_ksm_create(mat.handle, pc.handle if pc else None,
+                                       m, nrestart, int(mixed), C.byref(h)),
+              "tg_ksm_create")
+        self.handle, self.mat, self.pc = h, mat, pc
+        self.iters, self.resnorm = 0, 0.0
+
+    def set_tolerances(self, rtol, atol=1e-30):
+        check(_lib.lib().tg_ksm_set_tolerances(self.handle, rtol, atol))
+
+    def solve(self, b, x=None, zero_guess=True):
+        x = torch.zeros_like(b) if x is None else x
+        it, rn = C.c_int(0), C.c_double(0.0)
+        flag = check(_lib.lib().tg_ksm_solve(self.handle, _p(b), _p(x),
+                                             int(zero_guess), C.byref(it),
+                                             C.byref(rn), _stream()),
+                     "tg_ksm_solve")
+        self.iters, self.resnorm = it.value, rn.value
+        return x, flag
+
+    def __del__(self):
+        try:
+            _lib.lib().tg_ksm_decref(self.handle)
+        except Exception:
+            pass
+
+
+class GpuModel:
+    """An initialised tg_assembler holding one mesh, its loads and DVs."""
+
+    def __init__(self, prob):
+        if not torch.cuda.is_available():
+            raise _lib.TacsGpuError("a CUDA device is required")
+        L = _lib.lib()
+        self.prob = prob
+        et = int(prob["elem_type"])
+        self.vpn = 6 if et == 0 else 3
+        self.nnodes, self.nelem = int(prob["nnodes"]), int(prob["nelem"])
+        self.ndof = self.vpn * self.nnodes
+        conn = np.ascontiguousarray(prob["conn"], np.int32)
+        rho, E, nu, ys = [float(v) for v in prob["mat"]]
+        axis = np.ascontiguousarray(prob.get("ref_axis", [1.0, 0, 0]),
+                                    np.float64)
+        h = C.c_void_p()
+        check(L.tg_assembler_create(et, self.nnodes, self.nelem,
+                                    conn.ctypes.data, rho, E, nu, ys,
+                                    int(prob.get("transform", 0)),
+                                    axis.ctypes.data, C.byref(h)),
+              "tg_assembler_create")
+        self.handle = h
+        bcn = np.ascontiguousarray(prob.get("bc_nodes", []), np.int32)
+        bcm = np.ascontiguousarray(prob.get("bc_masks", []), np.int32)
+        check(L.tg_assembler_add_bcs(h, len(bcn), bcn.ctypes.data,
+                                     bcm.ctypes.data), "add_bcs")
+        thick = np.ascontiguousarray(prob["thick"], np.float64)
+        dvnum = np.ascontiguousarray(prob["dvnum"], np.int32)
+        check(L.tg_assembler_set_element_dvs(h, thick.ctypes.data,
+                                             dvnum.ctypes.data), "dvs")
+        pe = np.ascontiguousarray(prob.get("pres_elems", []), np.int32)
+        if len(pe):
+            pv = np.ascontiguousarray(prob["pres_vals"], np.float64)
+            check(L.tg_assembler_set_pressure(h, len(pe), pe.ctypes.data,
+                                              pv.ctypes.data), "pressure")
+        te = np.ascontiguousarray(prob.get("trac_elems", []), np.int32)
+        if len(te):
+            tf = np.ascontiguousarray(prob["trac_faces"], np.int32)
+            tv = np.ascontiguousarray(prob["trac_vals"], np.float64)
+            check(L.tg_assembler_set_traction(h, len(te), te.ctypes.data,
+                                              tf.ctypes.data, tv.ctypes.data),
+                  "traction")
+        check(L.tg_assembler_initialize(h), "tg_assembler_initialize")
+        vpn, nn, ne, ndv, nc = (C.c_int() for _ in range(5))
+        check(L.tg_assembler_get_sizes(h, C.byref(vpn), C.byref(nn),
+                                       C.byref(ne), C.byref(ndv),
+                                       C.byref(nc)))
+        self.ndv, self.ncolors = ndv.value, nc.value
+        self.xpts = torch.as_tensor(np.asarray(prob["xpts"], np.float64),
+                                    device="cuda")
+        check(L.tg_assembler_set_nodes(h, _p(self.xpts), _stream()),
+              "set_nodes")
+        self.ks_weight = float(prob.get("ks_weight", 100.0))
+
+    def __del__(self):
+        try:
+            _lib.lib().tg_assembler_decref(self.handle)
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- api
+    def vec(self, values=None):
+        if values is None:
+            return torch.zeros(self.ndof, dtype=torch.float64, device="cuda")
+        return torch.as_tensor(np.asarray(values, np.float64),
+                               device="cuda").clone()
+
+    def set_design_vars(self, dvs):
+        check(_lib.lib().tg_assembler_set_design_vars(self.handle, _p(dvs),
+                                                      _stream()), "set_dvs")
+
+    def assemble_res(self, u, lam=1.0, apply_bcs=True, res=None):
+        res = torch.empty(self.ndof, dtype=torch.float64,
+                          device="cuda") if res is None else res
+        check(_lib.lib().tg_assemble_res(self.handle, _p(u), lam,
+                                         int(apply_bcs), _p(res), _stream()),
+              "tg_assemble_res")
+        return res
+
+    def new_mat(self):
+        return Mat(self)
+
+    def assemble_jacobian(self, u, mat, res=None, transpose=False,
+                          apply_bcs=True, lam=1.0):
+        check(_lib.lib().tg_assemble_jacobian(
+            self.handle, 1.0, 0.0, 0.0, _p(u), _p(res), mat.handle,
+            int(transpose), lam, int(apply_bcs), _stream()),
+            "tg_assemble_jacobian")
+        return res
+
+    def apply_bcs(self, x):
+        check(_lib.lib().tg_apply_bcs(self.handle, _p(x), _stream()))
+        return x
+
+    def eval_functions(self, u, funcs=(0, 1), ks_weight=None):
+        f = np.ascontiguousarray(funcs, np.int32)
+        out = np.zeros(len(f))
+        ksw = self.ks_weight if ks_weight is None else ks_weight
+        check(_lib.lib().tg_eval_functions(self.handle, _p(u), len(f),
+                                           f.ctypes.data, ksw,
+                                           out.ctypes.data, _stream()),
+              "tg_eval_functions")
+        return out
+
+    def add_sv_sens(self, u, funcs, dfdu, alpha=1.0):
+        f = np.ascontiguousarray(funcs, np.int32)
+        ptrs = (C.c_void_p * len(f))(*[t.data_ptr() for t in dfdu])
+        check(_lib.lib().tg_add_sv_sens(self.handle, _p(u), len(f),
+                                        f.ctypes.data, alpha, ptrs,
+                                        _stream()), "tg_add_sv_sens")
+
+    def add_dv_sens(self, u, funcs, dfdx, coef=1.0):
+        f = np.ascontiguousarray(funcs, np.int32)
+        ptrs = (C.c_void_p * len(f))(*[t.data_ptr() for t in dfdx])
+        check(_lib.lib().tg_add_dv_sens(self.handle, _p(u), len(f),
+                                        f.ctypes.data, coef, ptrs,
+                                        _stream()), "tg_add_dv_sens")
+
+    def add_adjoint_res_products(self, u, psis, dfdx, scale=1.0):
+        pp = (C.c_void_p * len(psis))(*[t.data_ptr() for t in psis])
+        dp = (C.c_void_p * len(dfdx))(*[t.data_ptr() for t in dfdx])
+        check(_lib.lib().tg_add_adjoint_res_products(
+            self.handle, _p(u), scale, len(psis), pp, dp, _stream()),
+            "tg_add_adjoint_res_products")
+
+    def add_total_derivative(self, u, func, psi, dfdx, coef=1.0, scale=-1.0):
+        check(_lib.lib().tg_add_total_derivative(
+            self.handle, _p(u), int(func), coef, _p(psi), scale, _p(dfdx),
+            _stream()), "tg_add_total_derivative")
+
+    def dv_vec(self):
+        return torch.zeros(self.ndv, dtype=torch.float64, device="cuda")
+
+
+def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
+                   pc_kind=_lib.PC_ILU0, mixed=False, funcs=(0, 1)):
+    """Linear static solve + adjoint gradients on the GPU, following the
+    reference harness (tests/integration_tests/static_analysis_base_test.py:
+    359-427): K(u=0) and R(0), ILU(0), GMRES for R - f, functions, dfdu,
+    adjoint solve with the same row-BC matrix, dfdx - psi^T dR/dx."""
+    dev = torch.device("cuda")
+    u0 = model.vec()
+    res = model.vec()
+    mat = model.new_mat()
+    model.assemble_jacobian(u0, mat, res)
+    prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
+    pc = Pc(mat, pc_kind, prec)
+    pc.factor()
+    ksm = Ksm(mat, pc, m, nrestart, mixed)
+    ksm.set_tolerances(rtol, atol)
+    f = torch.as_tensor(np.asarray(force, np.float64), device=dev).clone()
+    model.apply_bcs(f)
+    res -= f
+    ans, flag = ksm.solve(res)
+    u = -ans
+    iters = [ksm.iters]
+    fvals = model.eval_functions(u, funcs)
+    grads = []
+    for k, fn in enumerate(funcs):
+        dfdu = model.vec()
+        model.add_sv_sens(u, [fn], [dfdu])
+        model.apply_bcs(dfdu)
+        psi, _ = ksm.solve(dfdu)
+        iters.append(ksm.iters)
+        g = model.dv_vec()
+        model.add_total_derivative(u, fn, psi, g, 1.0, -1.0)
+        grads.append(g)
+    return dict(u=u, funcs=fvals, grads=grads, flag=flag, iters=iters,
+                mat=mat, pc=pc, ksm=ksm)

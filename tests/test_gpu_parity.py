@@ -1,0 +1,109 @@
+"""GPU parity: libtacs_gb300 (through its C ABI) against the reference's own
+outputs (tests/golden) and against the CPU oracle on seeded meshes.
+
+Tolerances (norm-wise max|a-b|/max|b|):
+  element-level results (residual, Jacobian blocks, mat-vec, function values,
+  state/design sensitivities, adjoint products): 1e-12;
+  ILU(0) apply on a shared matrix: 1e-9 (the block-ILU factors of thin shells
+  amplify last-bit differences of the FMA-contracted GPU arithmetic);
+  GMRES solutions, functions at the solution and total derivatives: 1e-7
+  (bounded by cond(K) x the 1e-12 solver tolerance).
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, load_case, rel
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+ELEM_TOL = 1e-12
+ILU_TOL = 1e-9
+SOLVE_TOL = 1e-7
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import problem
+    return problem
+
+
+def _h(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_residual_jacobian_matvec(gpu, name):
+    prob, ref = load_case(name)
+    if "u_test" not in prob:
+        pytest.skip("no unit state in this case")
+    M = gpu.GpuModel(prob)
+    u = M.vec(prob["u_test"])
+    assert rel(_h(M.assemble_res(u)), ref["res"]) < ELEM_TOL
+    assert rel(_h(M.assemble_res(u, apply_bcs=False)), ref["res_nobc"]) < ELEM_TOL
+    mat = M.new_mat()
+    res = M.vec()
+    M.assemble_jacobian(u, mat, res, apply_bcs=False)
+    assert np.array_equal(_h(mat.rowp), ref["jac_nobc_rowp"])
+    assert np.array_equal(_h(mat.cols), ref["jac_nobc_cols"])
+    if "jac_nobc_vals" in ref:
+        assert rel(_h(mat.vals), ref["jac_nobc_vals"]) < ELEM_TOL
+    M.assemble_jacobian(u, mat, res)
+    assert rel(_h(res), ref["jac_res"]) < ELEM_TOL
+    if "jac_vals" in ref:
+        assert rel(_h(mat.vals), ref["jac_vals"]) < ELEM_TOL
+    x = M.vec(prob["x_test"])
+    assert rel(_h(mat.mult(x)), ref["kx"]) < ELEM_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ilu0_apply_on_reference_matrix(gpu, name):
+    prob, ref = load_case(name)
+    if "jac_vals" not in ref:
+        pytest.skip("matrix not stored")
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    mat.vals.copy_(torch.as_tensor(ref["jac_vals"], device="cuda"))
+    pc = gpu.Pc(mat)
+    pc.factor()
+    y = pc.apply(M.vec(prob["x_test"]))
+    assert rel(_h(y), ref["ilu_apply"]) < ILU_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_functions_and_sensitivities(gpu, name):
+    prob, ref = load_case(name)
+    if "u_test" not in prob:
+        pytest.skip("no unit state in this case")
+    M = gpu.GpuModel(prob)
+    u = M.vec(prob["u_test"])
+    assert rel(M.eval_functions(u), ref["funcs_test"]) < ELEM_TOL
+    dc, dk = M.vec(), M.vec()
+    M.add_sv_sens(u, [0, 1], [dc, dk])
+    assert rel(_h(dc), ref["dfdu_test_comp"]) < ELEM_TOL
+    assert rel(_h(dk), ref["dfdu_test_ks"]) < ELEM_TOL
+    xc, xk = M.dv_vec(), M.dv_vec()
+    M.add_dv_sens(u, [0, 1], [xc, xk])
+    assert rel(_h(xc), ref["dfdx_test_comp"]) < ELEM_TOL
+    assert rel(_h(xk), ref["dfdx_test_ks"]) < 1e-11
+    xa = M.dv_vec()
+    M.add_adjoint_res_products(u, [M.vec(prob["psi_test"])], [xa])
+    assert rel(_h(xa), ref["adjres_test"]) < ELEM_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_static_solve_and_adjoint_gradient(gpu, name):
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    r = gpu.static_adjoint(M, prob["force"], prob.get("gmres_m", 100),
+                           prob.get("gmres_restart", 2),
+                           prob.get("rtol", 1e-12))
+    assert r["flag"] == 1
+    assert rel(_h(r["u"]), ref["u"]) < SOLVE_TOL
+    assert rel(r["funcs"], ref["funcs"]) < SOLVE_TOL
+    assert rel(_h(r["grads"][0]), ref["grad_comp"]) < SOLVE_TOL
+    assert rel(_h(r["grads"][1]), ref["grad_ks"]) < SOLVE_TOL
+    if "func_refs" in prob:  # the reference tests' own known answers
+        assert rel(r["funcs"], prob["func_refs"]) < 1e-8
