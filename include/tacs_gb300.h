@@ -214,6 +214,32 @@ int tg_ksm_set_tolerances(tg_ksm *k, double rtol, double atol);
 int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
                  int *iters, double *resnorm, void *stream);
 
+/* ------------------------------------------------- allocation-free entry */
+/* No counterpart in the reference.  Compliance and KS failure (the values of
+   TG_FUNC_COMPLIANCE and TG_FUNC_KS_FAILURE, in that order) of a mesh whose
+   arrays the caller owns, computed without allocating any device memory:
+   for callers that may not call cudaMalloc (a host framework that hands
+   out views of its own pre-allocated device arena, or a loop that has
+   frozen its memory footprint and must not allocate, since an allocation
+   can implicitly synchronise the device).
+   All pointers except ref_axis_host are device pointers: conn (npe per
+   element), xpts (3 per node), thick (one t per element), vars (state),
+   vals (2 doubles, written).  Working memory is one file-scope device
+   array sized for at most TG_NOALLOC_MAX_ELEMENTS elements; every GPU that
+   loads the library keeps it (about 4.5 MB) until the process exits.
+   Larger meshes are rejected with TG_ERR_ARG.  The first call on each
+   device looks up that array's device address (cudaGetSymbolAddress) with
+   the device current, so make the first call on a device before any stream
+   capture.  All calls share the array: calls that overlap on the GPU (for
+   example on two streams) race and must be serialised by the caller. */
+#define TG_NOALLOC_MAX_ELEMENTS 32768
+int tg_eval_functions_noalloc(int elem_type, int num_elements,
+                              const int *conn, const double *xpts,
+                              const double *thick, double E, double nu,
+                              double ys, int transform,
+                              const double *ref_axis_host, const double *vars,
+                              double ks_weight, double *vals, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
