@@ -302,7 +302,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,
-                     "kernel": "shell_assembly_kernel",
+                     "kernel": "shell_team_assembly_kernel",
                      "kernel_ms": kern_ms, "algorithmic_bytes": algo},
         "e2e": {"value": world * nelem / (ms_e2e / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": int(8 * (M.ndv + M.ndof)),

@@ -1,0 +1,482 @@
+// MITC4 residual + Jacobian assembly with 8-lane teams (4 elements per warp).
+//
+// GB300 executes FP64 at 1/64 of the FP32 rate: every warp-wide FP64
+// instruction holds the SM's FP64 pipe for 16 cycles whatever its active
+// lane count.  So each warp works on four elements at once (one per 8-lane
+// team), all four running the same instruction stream, and the element
+// matrix is formed with as few FP64 operations as the kinematics allow:
+//
+//   K = sum_q detXd_q B_q^T C B_q
+//     = Bty^T G Bty                         (membrane + transverse shear)
+//     + sum_q detXd_q Bb_q^T D Bb_q         (bending)
+//     + sum_q detXd_q drill (N_q Bd)^T (N_q Bd)   (drilling)
+//
+// with Bty the 9 x 24 MITC tying-strain rows, G = sum_q detXd_q M_q^T C_ms
+// M_q the 9 x 9 membrane/shear stiffness in tying-strain space (M_q maps the
+// tying strains to e0,e1,e2,e6,e7 at Gauss point q), Bb_q the bending rows
+// and Bd the 4 nodal drilling rows.  Factoring G = L diag(d) L^T and
+// D = L_D L_D^T turns K into a sum of 25 rank-one channels
+// K = sum_c z_c z_c^T, so each of the 300 upper-triangle entries costs 25
+// FMAs.  The kinematics (normals, transforms, tying strains, drilling
+// rows) are those of TACSShellElement::addJacobian
+// (src/elements/shell/TACSShellElement.h:436-641) as in shell_kernels.cu.
+// Elements of one launch share no node (colouring): the BCSR
+// read-modify-write and the residual scatter need no atomics.
+#include <cmath>
+
+#include "tg_internal.h"
+
+namespace tg {
+namespace {
+
+#include "shell_common.cuh"
+
+constexpr int kTeam = 8;
+constexpr int kTeamsPerWarp = 32 / kTeam;
+constexpr int kWarpsPerCta = 2;
+constexpr int kTeamsPerCta = kTeamsPerWarp * kWarpsPerCta;
+constexpr int kNchan = 25;
+
+struct TeamGeo {
+  double Bd[4][24];
+  double T[4][9], P[4][9], Q[4][9];
+  double G[9][9];
+};
+
+struct __align__(16) TeamSmem {
+  double X[12];
+  double u[24];
+  double fn[12];
+  double n0[4][3];
+  double det[4];
+  double sdet[4];
+  double pres[4];
+  double sd[9];   // sqrt of the LDL^T pivots of G
+  double y[kNchan];
+  double res[24];
+  double t;
+  double Z[kNchan][24];  // rows 0..8 start as Bty; 9..24 hold M/CM first
+  TeamGeo g;
+  int nodes[4];
+  int slot[16];
+  int pad[2];
+};
+
+// Shape functions of node k or Gauss point q (index < 4: node, else point)
+__device__ __forceinline__ void shape_at(int which, double *N, double *Na,
+                                         double *Nb) {
+  if (which < 4)
+    shape2(-1.0 + 2.0 * (which & 1), -1.0 + 2.0 * (which >> 1), N, Na, Nb);
+  else
+    shape2(gauss2((which - 4) & 1), gauss2((which - 4) >> 1), N, Na, Nb);
+}
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+    shell_team_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                               const double *__restrict__ vars, double lambda,
+                               double *__restrict__ res,
+                               double *__restrict__ mat, int *err_flag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned char s_ij[300][2];
+  TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
+  const int lane = threadIdx.x & 31;
+  const int tl = lane & (kTeam - 1);
+  const int team_in_cta = threadIdx.x / kTeam;
+  TeamSmem &S = teams[team_in_cta];
+
+  // upper-triangle (i <= j) enumeration of the 24 x 24 element matrix
+  for (int k = threadIdx.x; k < 300; k += blockDim.x) {
+    int j = 0, base = 0;
+    while (base + j + 1 <= k) {
+      base += j + 1;
+      j++;
+    }
+    s_ij[k][0] = (unsigned char)(k - base);
+    s_ij[k][1] = (unsigned char)j;
+  }
+  __syncthreads();
+
+  const int gteam = blockIdx.x * kTeamsPerCta + team_in_cta;
+  const int nteams = gridDim.x * kTeamsPerCta;
+  // uniform trip count across the warp (teams without an element idle)
+  const int warp_base = (blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5)) *
+                        kTeamsPerWarp;
+  const int rounds =
+      cr.count > warp_base ? (cr.count - warp_base + nteams - 1) / nteams : 0;
+
+  // per-element constitutive constants (TACSIsoShellConstitutive, tOffset 0)
+  const double Dm = ep.E / (1.0 - ep.nu * ep.nu);
+  const double A0[6] = {Dm, ep.nu * Dm, 0.0, Dm, 0.0, 0.5 * ep.E / (1.0 + ep.nu)};
+
+  for (int rd = 0; rd < rounds; rd++) {
+    const int idx = gteam + rd * nteams;
+    const bool active = idx < cr.count;
+    const int e = active ? cr.elem_list[idx] : 0;
+
+    // ---------------------------------------------------------- load
+    if (active) {
+      if (tl < 4) {
+        S.nodes[tl] = m.conn[4 * e + tl];
+        S.pres[tl] = m.pres ? m.pres[4 * e + tl] : 0.0;
+      }
+      if (tl == 0) S.t = m.thick[e];
+    }
+    __syncwarp();
+    if (active) {
+      for (int i = tl; i < 12; i += kTeam)
+        S.X[i] = m.xpts[3 * S.nodes[i / 3] + i % 3];
+      for (int i = tl; i < 24; i += kTeam)
+        S.u[i] = vars ? vars[6 * S.nodes[i / 6] + i % 6] : 0.0;
+      if (mat)
+        for (int i = tl; i < 16; i += kTeam)
+          S.slot[i] = find_slot(m.rowp, m.cols, S.nodes[i >> 2], S.nodes[i & 3]);
+    }
+    __syncwarp();
+
+    // --------------------------------------------------- node normals
+    double N[4], Na[4], Nb[4], Xxi[6];
+    if (tl < 4) {
+      shape_at(tl, N, Na, Nb);
+      grad3(Na, Nb, S.X, Xxi);
+      double a[3] = {Xxi[0], Xxi[2], Xxi[4]}, b[3] = {Xxi[1], Xxi[3], Xxi[5]};
+      double f[3];
+      cross3(a, b, f);
+      double nrm = sqrt(dot3(f, f));
+      if (nrm != 0.0) {
+        double s = 1.0 / nrm;
+        f[0] *= s; f[1] *= s; f[2] *= s;
+      }
+      S.fn[3 * tl] = f[0]; S.fn[3 * tl + 1] = f[1]; S.fn[3 * tl + 2] = f[2];
+    }
+    __syncwarp();
+
+    // ------------- frames at the 4 nodes (lanes 0-3) and 4 points (4-7)
+    {
+      shape_at(tl, N, Na, Nb);
+      grad3(Na, Nb, S.X, Xxi);
+      double nv[3];
+      if (tl < 4) {
+        nv[0] = S.fn[3 * tl]; nv[1] = S.fn[3 * tl + 1]; nv[2] = S.fn[3 * tl + 2];
+      } else {
+        interp3(N, S.fn, nv);
+      }
+      double T[9], Xd[9], Xdinv[9], XdinvT[9];
+      shell_transform(ep, Xxi, nv, T);
+      frame(Xxi, nv, Xd);
+      const double det = inv3(Xd, Xdinv);
+      mm3(Xdinv, T, XdinvT);
+      if (tl < 4) {
+        // nodal drilling row (TacsShellComputeDrillStrain +
+        // TacsShellAddDrillStrainSens, TACSShellUtilities.h:651-790)
+        const int k = tl;
+        double tmp[9], du0d[9], dCpt[9];
+        const double du0x[9] = {0.0, -0.5, 0.0, 0.5, 0.0, 0.0, 0.0, 0.0, 0.0};
+        mmT3(du0x, XdinvT, tmp);
+        mm3(T, tmp, du0d);
+        mm3(T, du0x, tmp);
+        mmT3(tmp, T, dCpt);
+        for (int mm = 0; mm < 4; mm++) {
+          for (int a = 0; a < 3; a++)
+            S.g.Bd[k][6 * mm + a] = Na[mm] * du0d[3 * a] + Nb[mm] * du0d[3 * a + 1];
+          S.g.Bd[k][6 * mm + 3] = 0.0;
+          S.g.Bd[k][6 * mm + 4] = 0.0;
+          S.g.Bd[k][6 * mm + 5] = 0.0;
+        }
+        S.g.Bd[k][6 * k + 3] = 0.0 + -(dCpt[7] - dCpt[5]);
+        S.g.Bd[k][6 * k + 4] = 0.0 + -(dCpt[2] - dCpt[6]);
+        S.g.Bd[k][6 * k + 5] = 0.0 + -(dCpt[3] - dCpt[1]);
+      } else {
+        // Gauss-point displacement-gradient terms (TacsShellComputeDispGrad,
+        // TACSShellUtilities.h:361-420)
+        const int q = tl - 4;
+        double nxi[6], Xdz[9], nXX[9], Qm[9];
+        grad3(Na, Nb, S.fn, nxi);
+        Xdz[0] = nxi[0]; Xdz[1] = nxi[1]; Xdz[2] = 0.0;
+        Xdz[3] = nxi[2]; Xdz[4] = nxi[3]; Xdz[5] = 0.0;
+        Xdz[6] = nxi[4]; Xdz[7] = nxi[5]; Xdz[8] = 0.0;
+        mm3(Xdinv, Xdz, nXX);
+        for (int i = 0; i < 9; i++) nXX[i] = -nXX[i];
+        mm3(nXX, XdinvT, Qm);
+        for (int i = 0; i < 9; i++) {
+          S.g.T[q][i] = T[i];
+          S.g.P[q][i] = XdinvT[i];
+          S.g.Q[q][i] = Qm[i];
+        }
+        S.det[q] = det;
+        S.n0[q][0] = nv[0]; S.n0[q][1] = nv[1]; S.n0[q][2] = nv[2];
+        S.sdet[q] = sqrt(fabs(det));
+        if (!(det > 0.0) && active && err_flag) atomicCAS(err_flag, 0, 1);
+      }
+    }
+    __syncwarp();
+
+    // ---------------------------------------- tying-strain rows (Bty)
+    // (TACSShellLinearModel::computeTyingStrain, TACSShellElementModel.h:28)
+    for (int t = tl; t < 9; t += kTeam) {
+      double n0[3];
+      shape2(c_ty_pt[t][0], c_ty_pt[t][1], N, Na, Nb);
+      grad3(Na, Nb, S.X, Xxi);
+      interp3(N, S.fn, n0);
+      const int f = c_ty_field[t];
+      // row = al*X,xi + be*X,eta + ga*n0 coefficients per node
+      for (int mm = 0; mm < 4; mm++) {
+        double al, be, ga;
+        if (f == 0) { al = Na[mm]; be = 0.0; ga = 0.0; }
+        else if (f == 1) { al = 0.0; be = Nb[mm]; ga = 0.0; }
+        else if (f == 2) { al = 0.5 * Nb[mm]; be = 0.5 * Na[mm]; ga = 0.0; }
+        else if (f == 3) { al = 0.0; be = 0.0; ga = 0.5 * Nb[mm]; }
+        else { al = 0.0; be = 0.0; ga = 0.5 * Na[mm]; }
+        for (int a = 0; a < 3; a++) {
+          double v;
+          if (f == 0) v = al * Xxi[2 * a];
+          else if (f == 1) v = be * Xxi[2 * a + 1];
+          else if (f == 2) v = 0.5 * (Na[mm] * Xxi[2 * a + 1] + Nb[mm] * Xxi[2 * a]);
+          else v = n0[a] * ga;
+          S.Z[t][6 * mm + a] = v;
+        }
+        for (int b = 0; b < 3; b++) {
+          double v = 0.0;
+          if (f >= 3) {
+            const int c = (f == 3) ? 1 : 0;
+            double acc = 0.0;
+            for (int i = 0; i < 3; i++)
+              acc += Xxi[2 * i + c] * dmap(&S.fn[3 * mm], i, b);
+            v = 0.5 * N[mm] * acc;
+          }
+          S.Z[t][6 * mm + 3 + b] = v;
+        }
+      }
+    }
+    __syncwarp();
+
+    // ------------------------------- M_q and C M_q (tying -> e0,e1,e2,e6,e7)
+    const double t_el = S.t;
+    double Ael[6], Del[6], As0, As2, drill;
+    {
+      const double I = t_el * t_el * t_el / 12.0;
+      for (int i = 0; i < 6; i++) {
+        Del[i] = I * A0[i];
+        Ael[i] = A0[i] * t_el;
+      }
+      As0 = As2 = (5.0 / 6.0) * Ael[5];
+      drill = 0.5 * 0.1 * (As0 + As2);
+    }
+    double *Mq = &S.Z[9][0];        // [4][5][9]
+    double *CMq = &S.Z[9][0] + 180; // [4][5][9]
+    for (int k = tl; k < 180; k += kTeam) {
+      const int q = k / 45, r = (k % 45) / 9, t = k % 9;
+      const double xi = gauss2(q & 1), eta = gauss2(q >> 1);
+      const double la0 = (xi - 1.0) * -0.5, la1 = (xi + 1.0) * 0.5;
+      const double lb0 = (eta - 1.0) * -0.5, lb1 = (eta + 1.0) * 0.5;
+      double nty;
+      switch (t) {
+        case 0: case 7: nty = lb0; break;
+        case 1: case 8: nty = lb1; break;
+        case 2: case 5: nty = la0; break;
+        case 3: case 6: nty = la1; break;
+        default: nty = 1.0;
+      }
+      const double *P = S.g.P[q];
+      const int i = c_ty_ij[c_ty_field[t]][0], j = c_ty_ij[c_ty_field[t]][1];
+      const int a = c_erc[r][0], c = c_erc[r][1];
+      double s = P[3 * i + a] * P[3 * j + c];
+      if (i != j) s += P[3 * j + a] * P[3 * i + c];
+      Mq[k] = c_efac[r] * nty * s;
+    }
+    __syncwarp();
+    for (int k = tl; k < 180; k += kTeam) {
+      const int q = k / 45, r = (k % 45) / 9, t = k % 9;
+      const double *M = &Mq[45 * q];
+      double v;
+      // C_ms = [A 0; 0 As] acting on (e0, e1, e2, e6, e7)
+      if (r == 0) v = Ael[0] * M[t] + Ael[1] * M[9 + t] + Ael[2] * M[18 + t];
+      else if (r == 1) v = Ael[1] * M[t] + Ael[3] * M[9 + t] + Ael[4] * M[18 + t];
+      else if (r == 2) v = Ael[2] * M[t] + Ael[4] * M[9 + t] + Ael[5] * M[18 + t];
+      else if (r == 3) v = As0 * M[27 + t];
+      else v = As2 * M[36 + t];
+      CMq[k] = v * S.det[q];
+    }
+    __syncwarp();
+    // G = sum_q detXd_q M_q^T C M_q (lower triangle, 45 entries)
+    for (int k = tl; k < 45; k += kTeam) {
+      int a = 0, base = 0;
+      while (base + a + 1 <= k) {
+        base += a + 1;
+        a++;
+      }
+      const int b = k - base;  // b <= a
+      double v = 0.0;
+      for (int q = 0; q < 4; q++)
+        for (int r = 0; r < 5; r++)
+          v += Mq[45 * q + 9 * r + a] * CMq[45 * q + 9 * r + b];
+      S.g.G[a][b] = v;
+    }
+    __syncwarp();
+    // LDL^T of G (right-looking); L stored below the diagonal
+    for (int k = 0; k < 9; k++) {
+      const double dk = S.g.G[k][k];
+      const double inv = dk > 0.0 ? 1.0 / dk : 0.0;
+      __syncwarp();
+      for (int i = k + 1 + tl; i < 9; i += kTeam) S.g.G[i][k] *= inv;
+      __syncwarp();
+      const int nr = 8 - k;
+      for (int p = tl; p < nr * (nr + 1) / 2; p += kTeam) {
+        int ii = 0, base = 0;
+        while (base + ii + 1 <= p) {
+          base += ii + 1;
+          ii++;
+        }
+        const int i = k + 1 + ii, j = k + 1 + (p - base);
+        S.g.G[i][j] -= S.g.G[i][k] * S.g.G[j][k] * dk;
+      }
+      if (tl == 0) S.sd[k] = dk > 0.0 ? sqrt(dk) : 0.0;
+      __syncwarp();
+    }
+    // membrane/shear channels: z_t = sd_t (L^T Bty)_t, column by column
+    for (int c = tl; c < 24; c += kTeam) {
+      double b[9];
+      for (int t = 0; t < 9; t++) b[t] = S.Z[t][c];
+      for (int t = 0; t < 9; t++) {
+        double v = b[t];
+        for (int t2 = t + 1; t2 < 9; t2++) v += S.g.G[t2][t] * b[t2];
+        S.Z[t][c] = S.sd[t] * v;
+      }
+    }
+    __syncwarp();
+
+    // bending channels: sqrt(detXd_q) L_D^T Bb_q with D = L_D L_D^T
+    double L00, L10, L20, L11, L21, L22;
+    {
+      // guarded: a zero thickness gives zero bending channels, not NaN
+      L00 = Del[0] > 0.0 ? sqrt(Del[0]) : 0.0;
+      L10 = L00 > 0.0 ? Del[1] / L00 : 0.0;
+      L20 = L00 > 0.0 ? Del[2] / L00 : 0.0;
+      const double d11 = Del[3] - L10 * L10;
+      L11 = d11 > 0.0 ? sqrt(d11) : 0.0;
+      L21 = L11 > 0.0 ? (Del[4] - L20 * L10) / L11 : 0.0;
+      const double d22 = Del[5] - L20 * L20 - L21 * L21;
+      L22 = d22 > 0.0 ? sqrt(d22) : 0.0;
+    }
+    for (int k = tl; k < 96; k += kTeam) {
+      const int q = k / 24, c = k % 24;
+      shape_at(4 + q, N, Na, Nb);
+      const int mm = c / 6, a = c - 6 * mm;
+      const double *T = S.g.T[q], *P = S.g.P[q], *Qm = S.g.Q[q];
+      double bb[3];
+      if (a < 3) {
+        const double cu0 = Na[mm] * Qm[0] + Nb[mm] * Qm[3];
+        const double cu1 = Na[mm] * Qm[1] + Nb[mm] * Qm[4];
+        bb[0] = T[3 * a] * cu0;
+        bb[1] = T[3 * a + 1] * cu1;
+        bb[2] = T[3 * a] * cu1 + T[3 * a + 1] * cu0;
+      } else {
+        const int b = a - 3;
+        const double cd0 = Na[mm] * P[0] + Nb[mm] * P[3] + N[mm] * Qm[6];
+        const double cd1 = Na[mm] * P[1] + Nb[mm] * P[4] + N[mm] * Qm[7];
+        const double *f = &S.fn[3 * mm];
+        bb[0] = bb[1] = bb[2] = 0.0;
+        for (int aa = 0; aa < 3; aa++) {
+          const double dm = dmap(f, aa, b);
+          bb[0] += (T[3 * aa] * cd0) * dm;
+          bb[1] += (T[3 * aa + 1] * cd1) * dm;
+          bb[2] += (T[3 * aa] * cd1 + T[3 * aa + 1] * cd0) * dm;
+        }
+      }
+      const double s = S.sdet[q];
+      S.Z[9 + 3 * q][c] = s * (L00 * bb[0] + L10 * bb[1] + L20 * bb[2]);
+      S.Z[10 + 3 * q][c] = s * (L11 * bb[1] + L21 * bb[2]);
+      S.Z[11 + 3 * q][c] = s * (L22 * bb[2]);
+    }
+    // drilling channels: sqrt(detXd_q drill) sum_k N_q[k] Bd_k
+    const double sdrill = drill > 0.0 ? sqrt(drill) : 0.0;
+    for (int k = tl; k < 96; k += kTeam) {
+      const int q = k / 24, c = k % 24;
+      shape_at(4 + q, N, Na, Nb);
+      double v = 0.0;
+      for (int kk = 0; kk < 4; kk++) v += N[kk] * S.g.Bd[kk][c];
+      S.Z[21 + q][c] = (S.sdet[q] * sdrill) * v;
+    }
+    __syncwarp();
+
+    // ------------------------------------------------------- residual
+    if (res) {
+      for (int c = tl; c < kNchan; c += kTeam) {
+        double v = 0.0;
+        for (int i = 0; i < 24; i++) v += S.Z[c][i] * S.u[i];
+        S.y[c] = v;
+      }
+      __syncwarp();
+      for (int i = tl; i < 24; i += kTeam) {
+        double r = 0.0;
+        for (int c = 0; c < kNchan; c++) r += S.Z[c][i] * S.y[c];
+        // TACSShellPressure::addResidual (TACSShellPressure.h:56-90)
+        const int mm = i / 6, a = i - 6 * mm;
+        if (m.pres && a < 3) {
+          double aux = 0.0;
+          for (int q = 0; q < 4; q++) {
+            shape_at(4 + q, N, Na, Nb);
+            const double pr = N[0] * S.pres[0] + N[1] * S.pres[1] +
+                              N[2] * S.pres[2] + N[3] * S.pres[3];
+            aux += N[mm] * (pr * -S.det[q] * S.n0[q][a]);
+          }
+          r += lambda * aux;
+        }
+        if (active) res[6 * S.nodes[mm] + a] += r;
+      }
+    }
+
+    // ------------------------------- K: 300 upper entries, mirrored
+    if (mat && active) {
+      for (int k = tl; k < 300; k += kTeam) {
+        const int i = s_ij[k][0], j = s_ij[k][1];
+        double v = 0.0;
+#pragma unroll 5
+        for (int c = 0; c < kNchan; c++) v += S.Z[c][i] * S.Z[c][j];
+        const int a = i / 6, ii = i - 6 * a, b = j / 6, jj = j - 6 * b;
+        const int s_ab = S.slot[4 * a + b];
+        if (s_ab >= 0) mat[36 * (size_t)s_ab + 6 * ii + jj] += v;
+        if (i != j) {
+          const int s_ba = S.slot[4 * b + a];
+          if (s_ba >= 0) mat[36 * (size_t)s_ba + 6 * jj + ii] += v;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+}  // namespace
+
+void launch_shell_team_assembly(const ElemParams &ep, const MeshView &m,
+                                ColorRange cr, const double *vars,
+                                double lambda, double *res, double *mat,
+                                int *err_flag, cudaStream_t s) {
+  if (cr.count <= 0) return;
+  static bool init = false;
+  const size_t smem = sizeof(TeamSmem) * kTeamsPerCta;
+  if (!init) {
+    cudaFuncSetAttribute(shell_team_assembly_kernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    init = true;
+  }
+  int need = (cr.count + kTeamsPerCta - 1) / kTeamsPerCta;
+  int cap = sm_count() * 3;
+  int grid = need < cap ? need : cap;
+  if (grid < 1) grid = 1;
+  shell_team_assembly_kernel<<<grid, kWarpsPerCta * 32, smem, s>>>(
+      ep, m, cr, vars, lambda, res, mat, err_flag);
+}
+
+}  // namespace tg

@@ -49,6 +49,12 @@ void launch_shell_assembly(const ElemParams &ep, const MeshView &m,
                            ColorRange cr, const double *vars, double lambda,
                            double *res, double *mat, int transpose,
                            cudaStream_t s);
+// 8-lane-team MITC4 assembly (shell_team.cu); err_flag (device int, may be
+// nullptr) is set when an element has a non-positive Jacobian determinant.
+void launch_shell_team_assembly(const ElemParams &ep, const MeshView &m,
+                                ColorRange cr, const double *vars,
+                                double lambda, double *res, double *mat,
+                                int *err_flag, cudaStream_t s);
 void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
                          ColorRange cr, const double *vars, double lambda,
                          double *res, double *mat, int transpose,

@@ -481,8 +481,8 @@ int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,
   MeshView m = a->view();
   for (int c = 0; c < a->ncolors(); c++) {
     if (a->ep.elem_type == TG_ELEM_MITC4)
-      launch_shell_assembly(a->ep, m, a->color(c), vars, lambda, res, nullptr,
-                            0, S(s));
+      launch_shell_team_assembly(a->ep, m, a->color(c), vars, lambda, res,
+                                 nullptr, nullptr, S(s));
     else
       launch_hex_assembly(a->ep, m, a->color(c), vars, lambda, res, nullptr, 0,
                           S(s));
@@ -522,8 +522,8 @@ int tg_assemble_jacobian(tg_assembler *a, double alpha, double beta,
   MeshView m = a->view();
   for (int c = 0; c < a->ncolors(); c++) {
     if (a->ep.elem_type == TG_ELEM_MITC4)
-      launch_shell_assembly(a->ep, m, a->color(c), vars, lambda, res,
-                            A->d_vals, orient, S(s));
+      launch_shell_team_assembly(a->ep, m, a->color(c), vars, lambda, res,
+                                 A->d_vals, nullptr, S(s));
     else
       launch_hex_assembly(a->ep, m, a->color(c), vars, lambda, res, A->d_vals,
                           orient, S(s));
