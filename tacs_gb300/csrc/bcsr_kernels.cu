@@ -414,33 +414,44 @@ __global__ void __launch_bounds__(256)
 
 // --------------------------------------------------------------- GMRES
 // partial dot products of w with the k basis vectors W_j (column j at
-// W + j*ld): partials[blk * k + j]
-__global__ void dots_partial_kernel(const double *__restrict__ W, size_t ld,
-                                    int k, const double *__restrict__ w,
-                                    double *__restrict__ partials) {
-  extern __shared__ double sh[];  // blockDim.x
-  size_t chunk = (ld + gridDim.x - 1) / gridDim.x;
+// W + j*ld): block (x, j) reduces chunk x of W_j . w into partials[j*nbx+x]
+__global__ void __launch_bounds__(256)
+    dots_partial_kernel(const double *__restrict__ W, size_t ld, int k,
+                        const double *__restrict__ w,
+                        double *__restrict__ partials) {
+  __shared__ double sh[8];
+  const int j = blockIdx.y, nbx = gridDim.x;
+  const double *Wj = W + (size_t)j * ld;
+  size_t chunk = (ld + nbx - 1) / nbx;
   size_t b = chunk * blockIdx.x, e = b + chunk < ld ? b + chunk : ld;
-  for (int j = 0; j < k; j++) {
-    const double *Wj = W + (size_t)j * ld;
-    double acc = 0.0;
-    for (size_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += Wj[i] * w[i];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * k + j] = sh[0];
-    __syncthreads();
+  double acc = 0.0;
+  for (size_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += Wj[i] * w[i];
+  for (int off = 16; off > 0; off >>= 1)
+    acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+    partials[(size_t)j * nbx + blockIdx.x] = t;
   }
 }
-__global__ void dots_final_kernel(const double *partials, int npart, int k,
+__global__ void dots_final_kernel(const double *partials, int nbx, int k,
                                   double *h) {
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
-    double acc = 0.0;
-    for (int p = 0; p < npart; p++) acc += partials[(size_t)p * k + j];
-    h[j] = acc;
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  __shared__ double sh[8];
+  double acc = 0.0;
+  for (int p = threadIdx.x; p < nbx; p += blockDim.x)
+    acc += partials[(size_t)j * nbx + p];
+  for (int off = 16; off > 0; off >>= 1)
+    acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+    h[j] = t;
   }
 }
 __global__ void gemv_sub_kernel(const double *__restrict__ W, size_t ld, int k,
@@ -462,6 +473,29 @@ __global__ void scale_kernel(double a, double *x, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
     x[i] *= a;
+}
+
+template <typename T>
+__global__ void gather_blocks_kernel(int nnz, int b2, const int *valmap,
+                                     const double *src, T *dst) {
+  const size_t n = (size_t)nnz * b2;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = i / b2, e = i - k * b2;
+    dst[i] = (T)src[(size_t)valmap[k] * b2 + e];
+  }
+}
+template <typename T>
+__global__ void permute_kernel(int nrows, int bs, const int *perm,
+                               const T *src, T *dst, int scatter) {
+  const size_t n = (size_t)nrows * bs;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i / bs, c = i - r * bs;
+    const size_t o = (size_t)perm[r] * bs + c;
+    if (scatter) dst[o] = src[i];
+    else dst[i] = src[o];
+  }
 }
 
 }  // namespace
@@ -638,9 +672,14 @@ void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,
 
 void launch_dots(const double *W, size_t ld, int k, const double *w,
                  double *partials, int npart, double *h, cudaStream_t s) {
-  dots_partial_kernel<<<npart, 256, 256 * sizeof(double), s>>>(W, ld, k, w,
-                                                               partials);
-  dots_final_kernel<<<1, 128, 0, s>>>(partials, npart, k, h);
+  if (k <= 0) return;
+  // npart partials in total: nbx chunks for each of the k vectors
+  int nbx = npart / k;
+  size_t need = (ld + 2047) / 2048;
+  if ((size_t)nbx > need) nbx = (int)need;
+  if (nbx < 1) nbx = 1;
+  dots_partial_kernel<<<dim3(nbx, k), 256, 0, s>>>(W, ld, k, w, partials);
+  dots_final_kernel<<<k, 128, 0, s>>>(partials, nbx, k, h);
 }
 void launch_gemv_sub(const double *W, size_t ld, int k, const double *h,
                      double *w, size_t n, cudaStream_t s) {
@@ -659,6 +698,37 @@ void launch_scale(double a, double *x, size_t n, cudaStream_t s) {
 void launch_copy(const double *x, double *y, size_t n, cudaStream_t s) {
   if (!n) return;
   cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+}
+
+void launch_gather_blocks(int nnz, int b2, const int *valmap,
+                          const double *src, double *dst, cudaStream_t s) {
+  gather_blocks_kernel<double><<<blocks_for((size_t)nnz * b2, 256), 256, 0, s>>>(
+      nnz, b2, valmap, src, dst);
+}
+void launch_gather_blocks_f32(int nnz, int b2, const int *valmap,
+                              const double *src, float *dst, cudaStream_t s) {
+  gather_blocks_kernel<float><<<blocks_for((size_t)nnz * b2, 256), 256, 0, s>>>(
+      nnz, b2, valmap, src, dst);
+}
+void launch_permute_gather(int nrows, int bs, const int *perm,
+                           const double *src, double *dst, cudaStream_t s) {
+  permute_kernel<double><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
+      nrows, bs, perm, src, dst, 0);
+}
+void launch_permute_scatter(int nrows, int bs, const int *perm,
+                            const double *src, double *dst, cudaStream_t s) {
+  permute_kernel<double><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
+      nrows, bs, perm, src, dst, 1);
+}
+void launch_permute_gather_f32(int nrows, int bs, const int *perm,
+                               const float *src, float *dst, cudaStream_t s) {
+  permute_kernel<float><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
+      nrows, bs, perm, src, dst, 0);
+}
+void launch_permute_scatter_f32(int nrows, int bs, const int *perm,
+                                const float *src, float *dst, cudaStream_t s) {
+  permute_kernel<float><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
+      nrows, bs, perm, src, dst, 1);
 }
 
 }  // namespace tg

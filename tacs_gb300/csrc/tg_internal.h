@@ -150,6 +150,20 @@ void launch_ilu0_apply(const IluPlan &p, const double *F, const double *x,
                        double *y, double *tmp, cudaStream_t s);
 void launch_ilu0_apply_f32(const IluPlan &p, const float *F, const float *x,
                            float *y, float *tmp, cudaStream_t s);
+// colour-reordered ILU(0): value gather through a block map and vector
+// permutation (dst[r] = src[perm[r]] / dst[perm[r]] = src[r], bs per node)
+void launch_gather_blocks(int nnz, int b2, const int *valmap,
+                          const double *src, double *dst, cudaStream_t s);
+void launch_gather_blocks_f32(int nnz, int b2, const int *valmap,
+                              const double *src, float *dst, cudaStream_t s);
+void launch_permute_gather(int nrows, int bs, const int *perm,
+                           const double *src, double *dst, cudaStream_t s);
+void launch_permute_scatter(int nrows, int bs, const int *perm,
+                            const double *src, double *dst, cudaStream_t s);
+void launch_permute_gather_f32(int nrows, int bs, const int *perm,
+                               const float *src, float *dst, cudaStream_t s);
+void launch_permute_scatter_f32(int nrows, int bs, const int *perm,
+                                const float *src, float *dst, cudaStream_t s);
 void launch_block_jacobi_apply(const IluPlan &p, const double *F,
                                const double *x, double *y, cudaStream_t s);
 void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,

@@ -153,11 +153,25 @@ struct tg_pc {
   double *d_F = nullptr, *d_tmp = nullptr;
   float *d_F32 = nullptr, *d_x32 = nullptr, *d_y32 = nullptr,
         *d_tmp32 = nullptr;
+  double *d_gx = nullptr, *d_gy = nullptr;  // FP64 apply in/out buffers
+  // colour-reordered variant: permuted pattern, value map, permutation and
+  // permuted work vectors
+  int *d_prowp = nullptr, *d_pcols = nullptr, *d_pdiag = nullptr;
+  int *d_valmap = nullptr, *d_perm = nullptr;
+  double *d_px = nullptr, *d_py = nullptr;
+  float *d_px32 = nullptr, *d_py32 = nullptr;
+  int ncolors = 0;
+  // the level-by-level triangular solves replayed as one CUDA graph
+  cudaGraphExec_t apply_exec = nullptr;
   bool factored = false;
   ~tg_pc() {
+    if (apply_exec) cudaGraphExecDestroy(apply_exec);
     dfree(d_lvl_rows); dfree(d_ulvl_rows); dfree(d_upd_ptr);
     dfree(d_upd_tgt); dfree(d_upd_src); dfree(d_fail); dfree(d_F);
     dfree(d_tmp); dfree(d_F32); dfree(d_x32); dfree(d_y32); dfree(d_tmp32);
+    dfree(d_gx); dfree(d_gy); dfree(d_prowp); dfree(d_pcols); dfree(d_pdiag);
+    dfree(d_valmap); dfree(d_perm); dfree(d_px); dfree(d_py);
+    dfree(d_px32); dfree(d_py32);
   }
 };
 
@@ -172,7 +186,7 @@ struct tg_ksm {
   double *d_h = nullptr, *d_h2 = nullptr, *d_partials = nullptr;
   double *d_r = nullptr, *d_d = nullptr;
   float *d_v32 = nullptr, *d_z32 = nullptr, *d_w32 = nullptr;
-  int npart = 256;
+  int npart = 4096;
   ~tg_ksm() {
     dfree(d_W); dfree(d_work); dfree(d_work2); dfree(d_h); dfree(d_h2);
     dfree(d_partials); dfree(d_r); dfree(d_d); dfree(d_v32); dfree(d_z32);
@@ -731,10 +745,10 @@ int tg_mat_mult_f32(tg_mat *A, const float *x, float *y, void *s) {
 // Level sets of the block lower / upper triangles and the IKJ update list
 // of ILU(0) with the pattern of A (BCSRMat(comm, A, levFill = 0, fill),
 // src/bpmat/BCSRMat.cpp:138).
-static int build_ilu_plan(tg_pc *pc) {
-  tg_assembler *a = pc->A->a;
-  const int n = a->nnodes;
-  const auto &rowp = a->rowp_h, &cols = a->cols_h, &diag = a->diag_h;
+static int build_ilu_plan(tg_pc *pc, const std::vector<int> &rowp,
+                          const std::vector<int> &cols,
+                          const std::vector<int> &diag) {
+  const int n = (int)rowp.size() - 1;
   std::vector<int> lvl(n, 0), ulvl(n, 0);
   int nl = 0, nu = 0;
   for (int i = 0; i < n; i++) {
@@ -795,8 +809,9 @@ static int build_ilu_plan(tg_pc *pc) {
 int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
   if (!A || !out) return fail(TG_ERR_ARG, "tg_pc_create: NULL argument");
   *out = nullptr;
-  if (type != TG_PC_ILU0 && type != TG_PC_BLOCK_JACOBI)
-    return fail(TG_ERR_ARG, "tg_pc_create: preconditioner type not available");
+  if (type != TG_PC_ILU0 && type != TG_PC_BLOCK_JACOBI &&
+      type != TG_PC_ILU0_COLORED)
+    return fail(TG_ERR_ARG, "tg_pc_create: unknown preconditioner type");
   if (precision != TG_PREC_FP64 && precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_pc_create: bad precision");
   tg_pc *pc = new tg_pc();
@@ -806,12 +821,73 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
   pc->precision = precision;
   tg_assembler *a = A->a;
   int rc = 0;
-  if (type == TG_PC_ILU0) rc = build_ilu_plan(pc);
+  const int *rowp_d = a->d_rowp, *cols_d = a->d_cols, *diag_d = a->d_diag;
+  if (type == TG_PC_ILU0) {
+    rc = build_ilu_plan(pc, a->rowp_h, a->cols_h, a->diag_h);
+  } else if (type == TG_PC_ILU0_COLORED) {
+    // greedy colouring of the node graph: nodes of one colour are never
+    // neighbours, so with the nodes ordered by colour the ILU(0) factor and
+    // both triangular solves proceed one colour at a time
+    const int nn = a->nnodes;
+    std::vector<int> color(nn, -1);
+    int ncol = 0;
+    for (int i = 0; i < nn; i++) {
+      uint64_t used = 0;
+      for (int j = a->rowp_h[i]; j < a->rowp_h[i + 1]; j++) {
+        int c = color[a->cols_h[j]];
+        if (c >= 0 && c < 64) used |= (1ull << c);
+      }
+      int c = 0;
+      while (c < 64 && ((used >> c) & 1ull)) c++;
+      color[i] = c;
+      ncol = std::max(ncol, c + 1);
+    }
+    pc->ncolors = ncol;
+    std::vector<int> perm(nn), iperm(nn);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(),
+                     [&](int x, int y) { return color[x] < color[y]; });
+    for (int r = 0; r < nn; r++) iperm[perm[r]] = r;
+    std::vector<int> prowp(nn + 1, 0), pcols, pdiag(nn), valmap;
+    pcols.reserve(a->cols_h.size());
+    valmap.reserve(a->cols_h.size());
+    std::vector<std::pair<int, int>> row;
+    for (int r = 0; r < nn; r++) {
+      const int o = perm[r];
+      row.clear();
+      for (int j = a->rowp_h[o]; j < a->rowp_h[o + 1]; j++)
+        row.push_back({iperm[a->cols_h[j]], j});
+      std::sort(row.begin(), row.end());
+      for (auto &e : row) {
+        if (e.first == r) pdiag[r] = (int)pcols.size();
+        pcols.push_back(e.first);
+        valmap.push_back(e.second);
+      }
+      prowp[r + 1] = (int)pcols.size();
+    }
+    rc = build_ilu_plan(pc, prowp, pcols, pdiag);
+    if (!rc) rc = upload(&pc->d_prowp, prowp);
+    if (!rc) rc = upload(&pc->d_pcols, pcols);
+    if (!rc) rc = upload(&pc->d_pdiag, pdiag);
+    if (!rc) rc = upload(&pc->d_valmap, valmap);
+    if (!rc) rc = upload(&pc->d_perm, perm);
+    rowp_d = pc->d_prowp;
+    cols_d = pc->d_pcols;
+    diag_d = pc->d_pdiag;
+  }
   const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
   const size_t n = (size_t)A->nrows * A->bsize;
   if (!rc) rc = dalloc(&pc->d_fail, 1);
   if (!rc) rc = dalloc(&pc->d_F, nv);
   if (!rc) rc = dalloc(&pc->d_tmp, n);
+  if (!rc && type == TG_PC_ILU0_COLORED) {
+    rc = dalloc(&pc->d_px, n);
+    if (!rc) rc = dalloc(&pc->d_py, n);
+    if (!rc && precision == TG_PREC_FP32) rc = dalloc(&pc->d_px32, n);
+    if (!rc && precision == TG_PREC_FP32) rc = dalloc(&pc->d_py32, n);
+  }
+  if (!rc) rc = dalloc(&pc->d_gx, n);
+  if (!rc) rc = dalloc(&pc->d_gy, n);
   if (!rc && precision == TG_PREC_FP32) {
     rc = dalloc(&pc->d_F32, nv);
     if (!rc) rc = dalloc(&pc->d_x32, n);
@@ -825,9 +901,9 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
   IluPlan &p = pc->plan;
   p.bsize = A->bsize;
   p.nrows = A->nrows;
-  p.rowp = a->d_rowp;
-  p.cols = a->d_cols;
-  p.diag = a->d_diag;
+  p.rowp = rowp_d;
+  p.cols = cols_d;
+  p.diag = diag_d;
   p.lvl_rows = pc->d_lvl_rows;
   p.ulvl_rows = pc->d_ulvl_rows;
   p.upd_ptr = pc->d_upd_ptr;
@@ -851,7 +927,22 @@ int tg_pc_factor(tg_pc *pc, void *s) {
   tg_mat *A = pc->A;
   const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
   TG_CUDA(cudaMemsetAsync(pc->d_fail, 0, sizeof(int), S(s)));
-  if (pc->type == TG_PC_ILU0) {
+  if (pc->type == TG_PC_ILU0_COLORED) {
+    const int nl = (int)pc->plan.lvl_ptr_h.size() - 1;
+    const int b2 = A->bsize * A->bsize;
+    if (pc->precision == TG_PREC_FP64) {
+      launch_gather_blocks(A->nnz, b2, pc->d_valmap, A->d_vals, pc->d_F, S(s));
+      for (int L = 0; L < nl; L++)
+        launch_ilu0_factor_level(pc->plan, L, pc->d_F, S(s));
+    } else {
+      launch_gather_blocks_f32(A->nnz, b2, pc->d_valmap, A->d_vals, pc->d_F32,
+                               S(s));
+      for (int L = 0; L < nl; L++)
+        launch_ilu0_factor_level_f32(pc->plan, L, pc->d_F32, S(s));
+      int rc = ensure_f32(A, S(s));
+      if (rc) return rc;
+    }
+  } else if (pc->type == TG_PC_ILU0) {
     const int nl = (int)pc->plan.lvl_ptr_h.size() - 1;
     if (pc->precision == TG_PREC_FP64) {
       TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
@@ -890,23 +981,71 @@ int tg_pc_factor(tg_pc *pc, void *s) {
   return 0;
 }
 
+// Apply the factored preconditioner to the pc's internal input buffer
+// (d_gx, or d_x32 in FP32) into its output buffer (d_gy / d_y32).  The ILU(0)
+// level sequence (2 x number of levels launches) is captured once into a
+// CUDA graph and replayed.
+static int pc_apply_internal(tg_pc *pc, cudaStream_t s) {
+  if (pc->type == TG_PC_BLOCK_JACOBI) {
+    if (pc->precision == TG_PREC_FP64)
+      launch_block_jacobi_apply(pc->plan, pc->d_F, pc->d_gx, pc->d_gy, s);
+    else
+      launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
+                                    s);
+    return 0;
+  }
+  if (!pc->apply_exec) {
+    cudaStream_t cs;
+    TG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      const int bs = pc->A->bsize, nr = pc->A->nrows;
+      if (pc->type == TG_PC_ILU0_COLORED) {
+        if (pc->precision == TG_PREC_FP64) {
+          launch_permute_gather(nr, bs, pc->d_perm, pc->d_gx, pc->d_px, cs);
+          launch_ilu0_apply(pc->plan, pc->d_F, pc->d_px, pc->d_py, pc->d_tmp,
+                            cs);
+          launch_permute_scatter(nr, bs, pc->d_perm, pc->d_py, pc->d_gy, cs);
+        } else {
+          launch_permute_gather_f32(nr, bs, pc->d_perm, pc->d_x32, pc->d_px32,
+                                    cs);
+          launch_ilu0_apply_f32(pc->plan, pc->d_F32, pc->d_px32, pc->d_py32,
+                                pc->d_tmp32, cs);
+          launch_permute_scatter_f32(nr, bs, pc->d_perm, pc->d_py32,
+                                     pc->d_y32, cs);
+        }
+      } else if (pc->precision == TG_PREC_FP64) {
+        launch_ilu0_apply(pc->plan, pc->d_F, pc->d_gx, pc->d_gy, pc->d_tmp, cs);
+      } else {
+        launch_ilu0_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
+                              pc->d_tmp32, cs);
+      }
+      e = cudaStreamEndCapture(cs, &g);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&pc->apply_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return cuda_check(e, "ILU(0) apply graph capture");
+  }
+  TG_CUDA(cudaGraphLaunch(pc->apply_exec, s));
+  return 0;
+}
+
 int tg_pc_apply(tg_pc *pc, const double *x, double *y, void *s) {
   if (!pc || !x || !y) return fail(TG_ERR_ARG, "tg_pc_apply: NULL argument");
   if (!pc->factored) return fail(TG_ERR_STATE, "tg_pc_apply before factor");
   const size_t n = (size_t)pc->A->nrows * pc->A->bsize;
+  int rc;
   if (pc->precision == TG_PREC_FP64) {
-    if (pc->type == TG_PC_ILU0)
-      launch_ilu0_apply(pc->plan, pc->d_F, x, y, pc->d_tmp, S(s));
-    else
-      launch_block_jacobi_apply(pc->plan, pc->d_F, x, y, S(s));
+    TG_CUDA(cudaMemcpyAsync(pc->d_gx, x, n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, S(s)));
+    if ((rc = pc_apply_internal(pc, S(s)))) return rc;
+    TG_CUDA(cudaMemcpyAsync(y, pc->d_gy, n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, S(s)));
   } else {
     launch_d2f(x, pc->d_x32, n, S(s));
-    if (pc->type == TG_PC_ILU0)
-      launch_ilu0_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
-                            pc->d_tmp32, S(s));
-    else
-      launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
-                                    S(s));
+    if ((rc = pc_apply_internal(pc, S(s)))) return rc;
     launch_f2d(pc->d_y32, y, n, S(s));
   }
   TG_CUDA(cudaGetLastError());
@@ -981,17 +1120,14 @@ static int apply_op(tg_ksm *k, const double *v, double *z, double *w,
                     cudaStream_t s) {
   tg_mat *A = k->A;
   if (k->mixed) {
-    launch_d2f(v, k->d_v32, k->n, s);
     tg_pc *pc = k->pc;
-    if (pc->type == TG_PC_ILU0)
-      launch_ilu0_apply_f32(pc->plan, pc->d_F32, k->d_v32, k->d_z32,
-                            pc->d_tmp32, s);
-    else
-      launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, k->d_v32, k->d_z32, s);
+    launch_d2f(v, pc->d_x32, k->n, s);
+    int rc = pc_apply_internal(pc, s);
+    if (rc) return rc;
     launch_bcsr_mult_f32(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
-                         A->d_vals32, k->d_z32, k->d_w32, s);
+                         A->d_vals32, pc->d_y32, k->d_w32, s);
     launch_f2d(k->d_w32, w, k->n, s);
-    if (z) launch_f2d(k->d_z32, z, k->n, s);
+    if (z) launch_f2d(pc->d_y32, z, k->n, s);
     return 0;
   }
   const double *src = v;
@@ -1100,14 +1236,10 @@ static int gmres_core(tg_ksm *k, const double *b, double *x, int zero_guess,
     launch_gemv_sub(W, n, niters, k->d_h, k->d_work, n, s);
     if (k->mixed) {
       tg_pc *pc = k->pc;
-      launch_d2f(k->d_work, k->d_v32, n, s);
-      if (pc->type == TG_PC_ILU0)
-        launch_ilu0_apply_f32(pc->plan, pc->d_F32, k->d_v32, k->d_z32,
-                              pc->d_tmp32, s);
-      else
-        launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, k->d_v32, k->d_z32,
-                                      s);
-      launch_f2d(k->d_z32, k->d_work2, n, s);
+      launch_d2f(k->d_work, pc->d_x32, n, s);
+      int rc = pc_apply_internal(pc, s);
+      if (rc) return rc;
+      launch_f2d(pc->d_y32, k->d_work2, n, s);
       launch_axpy(1.0, k->d_work2, x, n, s);
     } else if (k->pc) {
       int rc = tg_pc_apply(k->pc, k->d_work, k->d_work2, s);
@@ -1124,10 +1256,19 @@ static int gmres_core(tg_ksm *k, const double *b, double *x, int zero_guess,
   return flag;
 }
 
+static int ksm_solve_impl(tg_ksm *k, const double *b, double *x,
+                          int zero_guess, int *iters, double *resnorm,
+                          cudaStream_t s);
+
 int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
                  int *iters, double *resnorm, void *sv) {
   if (!k || !b || !x) return fail(TG_ERR_ARG, "tg_ksm_solve: NULL argument");
-  cudaStream_t s = S(sv);
+  return ksm_solve_impl(k, b, x, zero_guess, iters, resnorm, S(sv));
+}
+
+static int ksm_solve_impl(tg_ksm *k, const double *b, double *x,
+                          int zero_guess, int *iters, double *resnorm,
+                          cudaStream_t s) {
   if (iters) *iters = 0;
   if (!k->mixed)
     return gmres_core(k, b, x, zero_guess, k->rtol, k->atol, k->nrestart + 1,
@@ -1139,9 +1280,13 @@ int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
   int rc = dnorm(k, b, &bnorm, s);
   if (rc) return rc;
   if (zero_guess) TG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
-  const int max_outer = 50 * (k->nrestart + 1);
-  double rn = bnorm;
-  for (int outer = 0; outer < max_outer; outer++) {
+  // Each inner solve runs restarted GMRES with the FP32 operator to a
+  // relative 1e-6 (or its restart limit); the FP64 true residual then
+  // drives the next correction.  Stops when the true residual meets rtol,
+  // or when a correction no longer reduces it (stagnation).
+  const int max_outer = 20;
+  double rn = bnorm, prev = 0.0;
+  for (int outer = 0; outer <= max_outer; outer++) {
     // r = b - A x in FP64
     launch_bcsr_mult(k->A->bsize, k->A->nrows, k->A->a->d_rowp,
                      k->A->a->d_cols, k->A->d_vals, x, k->d_r, s);
@@ -1153,9 +1298,13 @@ int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
     if (!std::isfinite(rn))
       return fail(TG_ERR_NONFINITE, "mixed GMRES: non-finite true residual");
     if (rn <= k->rtol * bnorm || rn < k->atol) return 1;
-    // inner correction: A d = r to a relative 1e-6 in one restart cycle
+    if (outer > 0 && rn > 0.5 * prev) return 0;  // stagnated
+    if (outer == max_outer) break;
+    prev = rn;
     int it = 0;
-    rc = gmres_core(k, k->d_r, k->d_d, 1, 1e-6, 0.0, 1, &it, nullptr, s);
+    const double inner = std::max(1e-6, 0.1 * k->rtol * bnorm / rn);
+    rc = gmres_core(k, k->d_r, k->d_d, 1, inner, 0.0, k->nrestart + 1, &it,
+                    nullptr, s);
     if (rc < 0) return rc;
     if (iters) *iters += it;
     launch_axpy(1.0, k->d_d, x, n, s);
