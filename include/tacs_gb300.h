@@ -168,6 +168,28 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
                             double coef, const double *psi, double scale,
                             double *dfdx, void *stream);
 
+/* ------------------------------------------------------ element segments */
+/* No reference counterpart (the reference holds one model per assembler).
+   elem_ptr (host, nseg+1, elem_ptr[0] = 0 < ... < elem_ptr[nseg] =
+   elements) splits the elements into contiguous ranges, e.g. independent
+   meshes batched into one assembler; every range then has its own
+   compliance and KS aggregate (TACSCompliance / TACSKSFailure evaluated
+   over that range's elements only). */
+int tg_assembler_set_segments(tg_assembler *a, int nseg, const int *elem_ptr);
+/* Per-range function values vals[nseg] (host) of TG_FUNC_COMPLIANCE or
+   TG_FUNC_KS_FAILURE; keeps the per-range KS statistics for the calls
+   below (evaluate again whenever vars changes).  Synchronises. */
+int tg_eval_functions_segments(tg_assembler *a, const double *vars, int func,
+                               double ks_weight, double *vals, void *stream);
+/* dfdu += alpha * d f_g / du where each element contributes to the function
+   of its own range (addSVSens per range, summed into one vector). */
+int tg_add_sv_sens_segments(tg_assembler *a, const double *vars, int func,
+                            double alpha, double *dfdu, void *stream);
+/* tg_add_total_derivative with each element's own range function. */
+int tg_add_total_derivative_segments(tg_assembler *a, const double *vars,
+                                     int func, double coef, const double *psi,
+                                     double scale, double *dfdx, void *stream);
+
 /* ------------------------------------------------------------------ BCSR */
 /* TACSAssembler::createMat (src/TACSAssembler.cpp:3384): a BCSR matrix with
    the assembler's non-zero pattern (node graph plus diagonal, sorted
@@ -213,6 +235,26 @@ int tg_ksm_set_tolerances(tg_ksm *k, double rtol, double atol);
    final (estimated, or true for mixed) residual norm. */
 int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
                  int *iters, double *resnorm, void *stream);
+/* No reference counterpart (the reference runs one GMRES per system).
+   Splits the block rows into nseg ranges, row_ptr[0] = 0 <
+   row_ptr[1] < ... < row_ptr[nseg] = rows (host array), that the matrix
+   does not couple (a block-diagonal matrix, e.g. several meshes in one
+   assembler; TG_ERR_ARG otherwise).  Every range is then solved as its own
+   system with its own Krylov basis, residual and convergence test.  With
+   segments set, tg_ksm_solve returns 1 only when every range converged
+   and reports the largest iteration count and residual. */
+int tg_ksm_set_segments(tg_ksm *k, int nseg, const int *row_ptr);
+/* nrhs right-hand sides in one solve: B and X hold nrhs vectors of
+   rows x bsize entries one after another (device).  The nseg x nrhs
+   systems (index rhs * nseg + range) run as one batched restarted GMRES:
+   one mat-vec and one preconditioner application per step cover all of
+   them.  iters, flags (1 converged, 0 not) and resnorms receive one entry
+   per system (host arrays, may be NULL).  Returns 1 when every system
+   converged, 0 when not, or a negative error code.  Synchronous.  At most
+   1024 systems per solve. */
+int tg_ksm_solve_multi(tg_ksm *k, int nrhs, const double *B, double *X,
+                       int zero_guess, int *iters, int *flags,
+                       double *resnorms, void *stream);
 
 /* ------------------------------------------------- allocation-free entry */
 /* No counterpart in the reference.  Compliance and KS failure (the values of

@@ -64,6 +64,13 @@ SIGNATURES = [
     ("tg_ksm_decref", _I, [_P]),
     ("tg_ksm_set_tolerances", _I, [_P, _D, _D]),
     ("tg_ksm_solve", _I, [_P, _P, _P, _I, _IP, _DP, _P]),
+    ("tg_ksm_set_segments", _I, [_P, _I, _P]),
+    ("tg_assembler_set_segments", _I, [_P, _I, _P]),
+    ("tg_eval_functions_segments", _I, [_P, _P, _I, _D, _P, _P]),
+    ("tg_add_sv_sens_segments", _I, [_P, _P, _I, _D, _P, _P]),
+    ("tg_add_total_derivative_segments", _I, [_P, _P, _I, _D, _P, _D, _P,
+                                              _P]),
+    ("tg_ksm_solve_multi", _I, [_P, _I, _P, _P, _I, _P, _P, _P, _P]),
     ("tg_eval_functions_noalloc", _I, [_I, _I, _P, _P, _P, _D, _D, _D, _I,
                                        _P, _P, _D, _P, _P]),
 ]

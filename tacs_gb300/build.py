@@ -15,8 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libtacs_gb300.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["tg_runtime.cu", "shell_kernels.cu", "hex_kernels.cu",
-           "bcsr_kernels.cu", "noalloc.cu", "shell_team.cu"]
+SOURCES = ["tg_runtime.cu", "tg_krylov.cu", "shell_kernels.cu",
+           "hex_kernels.cu", "bcsr_kernels.cu", "krylov_kernels.cu",
+           "noalloc.cu", "shell_team.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr"]

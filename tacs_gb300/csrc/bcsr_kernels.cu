@@ -7,6 +7,8 @@
 // GMRES vector kernels.
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "tg_internal.h"
 
 namespace tg {
@@ -32,12 +34,13 @@ int blocks_for(size_t n, int threads, int per_sm = 8) {
 
 // ------------------------------------------------------------ mat-vec
 // One thread per (block row, row within block): BS threads read the BS
-// rows of each BSxBS block, i.e. the whole contiguous block.
-template <int BS, typename T>
+// rows of each BSxBS block, i.e. the whole contiguous block.  NR right-hand
+// sides (vectors ld apart) share each block read from memory.
+template <int BS, int NR, typename T>
 __global__ void __launch_bounds__(256)
     bcsr_mult_kernel(int nrows, const int *__restrict__ rowp,
                      const int *__restrict__ cols, const T *__restrict__ A,
-                     const T *__restrict__ x, T *__restrict__ y) {
+                     const T *__restrict__ x, T *__restrict__ y, size_t ld) {
   const int per_warp = 32 / BS;
   const int lane = threadIdx.x & 31;
   const int sub = lane / BS, ii = lane - BS * sub;
@@ -45,27 +48,56 @@ __global__ void __launch_bounds__(256)
   const int nw = (gridDim.x * blockDim.x) >> 5;
   if (sub >= per_warp) return;
   for (int row = gw * per_warp + sub; row < nrows; row += nw * per_warp) {
-    T acc = 0;
+    T acc[NR];
+#pragma unroll
+    for (int l = 0; l < NR; l++) acc[l] = 0;
     const int end = rowp[row + 1];
+#pragma unroll 3
     for (int j = rowp[row]; j < end; j++) {
       const T *a = &A[(size_t)BS * BS * j + BS * ii];
-      const T *xx = &x[(size_t)BS * cols[j]];
-      T s = 0;
+      T av[BS];
 #pragma unroll
-      for (int jj = 0; jj < BS; jj++) s += a[jj] * xx[jj];
-      acc += s;
+      for (int jj = 0; jj < BS; jj++) av[jj] = a[jj];
+      const size_t xo = (size_t)BS * cols[j];
+#pragma unroll
+      for (int l = 0; l < NR; l++) {
+        const T *xx = &x[l * ld + xo];
+        T s = 0;
+#pragma unroll
+        for (int jj = 0; jj < BS; jj++) s += av[jj] * xx[jj];
+        acc[l] += s;
+      }
     }
-    y[(size_t)BS * row + ii] = acc;
+#pragma unroll
+    for (int l = 0; l < NR; l++) y[l * ld + (size_t)BS * row + ii] = acc[l];
   }
 }
 
 template <int BS, typename T>
 void mult_dispatch(int nrows, const int *rowp, const int *cols, const T *A,
-                   const T *x, T *y, cudaStream_t s) {
+                   const T *x, T *y, int nrhs, size_t ld, cudaStream_t s) {
   const int per_warp = 32 / BS;
   size_t warps = (nrows + per_warp - 1) / per_warp;
   int blocks = blocks_for(warps * 32, 256, 16);
-  bcsr_mult_kernel<BS, T><<<blocks, 256, 0, s>>>(nrows, rowp, cols, A, x, y);
+  for (int l = 0; l < nrhs;) {
+    const int left = nrhs - l;
+    if (left >= 4) {
+      bcsr_mult_kernel<BS, 4, T><<<blocks, 256, 0, s>>>(nrows, rowp, cols, A,
+                                                        x + l * ld, y + l * ld,
+                                                        ld);
+      l += 4;
+    } else if (left >= 2) {
+      bcsr_mult_kernel<BS, 2, T><<<blocks, 256, 0, s>>>(nrows, rowp, cols, A,
+                                                        x + l * ld, y + l * ld,
+                                                        ld);
+      l += 2;
+    } else {
+      bcsr_mult_kernel<BS, 1, T><<<blocks, 256, 0, s>>>(nrows, rowp, cols, A,
+                                                        x + l * ld, y + l * ld,
+                                                        ld);
+      l += 1;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- BCs
@@ -321,14 +353,14 @@ __global__ void __launch_bounds__(128)
 }
 
 // Lower solve of one level: y_i = x_i - sum_{j<i} L_ij y_cj
-// (BCSRMatApplyLower6, unit lower)
-template <int BS, typename T>
+// (BCSRMatApplyLower6, unit lower); NR vectors ld apart per block read.
+template <int BS, int NR, typename T>
 __global__ void __launch_bounds__(256)
     ilu_lower_level_kernel(const int *__restrict__ rows, int nrows_lvl,
                            const int *__restrict__ rowp,
                            const int *__restrict__ cols,
                            const T *__restrict__ F, const T *__restrict__ x,
-                           T *__restrict__ y) {
+                           T *__restrict__ y, size_t ld) {
   const int per_warp = 32 / BS;
   const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
   if (sub >= per_warp) return;
@@ -336,28 +368,38 @@ __global__ void __launch_bounds__(256)
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int r = gw * per_warp + sub; r < nrows_lvl; r += nw * per_warp) {
     const int i = rows[r];
-    T z = x[(size_t)BS * i + ii];
+    T z[NR];
+#pragma unroll
+    for (int l = 0; l < NR; l++) z[l] = x[l * ld + (size_t)BS * i + ii];
     for (int j = rowp[i]; cols[j] < i; j++) {
       const T *a = &F[(size_t)BS * BS * j + BS * ii];
-      const T *yy = &y[(size_t)BS * cols[j]];
-      T s = 0;
+      T av[BS];
 #pragma unroll
-      for (int c = 0; c < BS; c++) s += a[c] * yy[c];
-      z -= s;
+      for (int c = 0; c < BS; c++) av[c] = a[c];
+      const size_t yo = (size_t)BS * cols[j];
+#pragma unroll
+      for (int l = 0; l < NR; l++) {
+        const T *yy = &y[l * ld + yo];
+        T s = 0;
+#pragma unroll
+        for (int c = 0; c < BS; c++) s += av[c] * yy[c];
+        z[l] -= s;
+      }
     }
-    y[(size_t)BS * i + ii] = z;
+#pragma unroll
+    for (int l = 0; l < NR; l++) y[l * ld + (size_t)BS * i + ii] = z[l];
   }
 }
 
 // Upper solve of one level: z_i = y_i - sum_{j>i} U_ij x_cj ; x_i = D_i^-1 z
-template <int BS, typename T>
+template <int BS, int NR, typename T>
 __global__ void __launch_bounds__(256)
     ilu_upper_level_kernel(const int *__restrict__ rows, int nrows_lvl,
                            const int *__restrict__ rowp,
                            const int *__restrict__ cols,
                            const int *__restrict__ diag,
                            const T *__restrict__ F, const T *__restrict__ yin,
-                           T *__restrict__ xout) {
+                           T *__restrict__ xout, size_t ld) {
   const int per_warp = 32 / BS;
   const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -366,29 +408,50 @@ __global__ void __launch_bounds__(256)
   for (int rd = 0; rd < nrounds; rd++) {
     const int r = (rd * nw + gw) * per_warp + sub;
     const bool active = sub < per_warp && r < nrows_lvl;
-    T z = 0;
+    T z[NR];
+#pragma unroll
+    for (int l = 0; l < NR; l++) z[l] = 0;
     int i = 0;
     if (active) {
       i = rows[r];
-      z = yin[(size_t)BS * i + ii];
+#pragma unroll
+      for (int l = 0; l < NR; l++) z[l] = yin[l * ld + (size_t)BS * i + ii];
       for (int j = diag[i] + 1; j < rowp[i + 1]; j++) {
         const T *a = &F[(size_t)BS * BS * j + BS * ii];
-        const T *xx = &xout[(size_t)BS * cols[j]];
-        T s = 0;
+        T av[BS];
 #pragma unroll
-        for (int c = 0; c < BS; c++) s += a[c] * xx[c];
-        z -= s;
+        for (int c = 0; c < BS; c++) av[c] = a[c];
+        const size_t xo = (size_t)BS * cols[j];
+#pragma unroll
+        for (int l = 0; l < NR; l++) {
+          const T *xx = &xout[l * ld + xo];
+          T s = 0;
+#pragma unroll
+          for (int c = 0; c < BS; c++) s += av[c] * xx[c];
+          z[l] -= s;
+        }
       }
     }
     const int base = lane - ii;
-    T out = 0;
-    const T *dinv = active ? &F[(size_t)BS * BS * diag[i] + BS * ii] : nullptr;
+    T dv[BS];
+    if (active) {
+      const T *dinv = &F[(size_t)BS * BS * diag[i] + BS * ii];
 #pragma unroll
-    for (int c = 0; c < BS; c++) {
-      T zc = __shfl_sync(0xffffffffu, z, base + c);
-      if (active) out += dinv[c] * zc;
+      for (int c = 0; c < BS; c++) dv[c] = dinv[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < BS; c++) dv[c] = 0;
     }
-    if (active) xout[(size_t)BS * i + ii] = out;
+#pragma unroll
+    for (int l = 0; l < NR; l++) {
+      T out = 0;
+#pragma unroll
+      for (int c = 0; c < BS; c++) {
+        T zc = __shfl_sync(0xffffffffu, z[l], base + c);
+        out += dv[c] * zc;
+      }
+      if (active) xout[l * ld + (size_t)BS * i + ii] = out;
+    }
   }
 }
 
@@ -396,7 +459,7 @@ template <int BS, typename T>
 __global__ void __launch_bounds__(256)
     block_jacobi_kernel(int nrows, const int *__restrict__ diag,
                         const T *__restrict__ F, const T *__restrict__ x,
-                        T *__restrict__ y) {
+                        T *__restrict__ y, int nrhs, size_t ld) {
   const int per_warp = 32 / BS;
   const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
   if (sub >= per_warp) return;
@@ -404,11 +467,13 @@ __global__ void __launch_bounds__(256)
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int i = gw * per_warp + sub; i < nrows; i += nw * per_warp) {
     const T *a = &F[(size_t)BS * BS * diag[i] + BS * ii];
-    const T *xx = &x[(size_t)BS * i];
-    T s = 0;
+    for (int l = 0; l < nrhs; l++) {
+      const T *xx = &x[l * ld + (size_t)BS * i];
+      T s = 0;
 #pragma unroll
-    for (int c = 0; c < BS; c++) s += a[c] * xx[c];
-    y[(size_t)BS * i + ii] = s;
+      for (int c = 0; c < BS; c++) s += a[c] * xx[c];
+      y[l * ld + (size_t)BS * i + ii] = s;
+    }
   }
 }
 
@@ -487,14 +552,289 @@ __global__ void gather_blocks_kernel(int nnz, int b2, const int *valmap,
 }
 template <typename T>
 __global__ void permute_kernel(int nrows, int bs, const int *perm,
-                               const T *src, T *dst, int scatter) {
+                               const T *src, T *dst, int scatter, int nrhs) {
   const size_t n = (size_t)nrows * bs;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const size_t r = i / bs, c = i - r * bs;
-    const size_t o = (size_t)perm[r] * bs + c;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+       i < n * nrhs; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = i / n, k = i - l * n;
+    const size_t r = k / bs, c = k - r * bs;
+    const size_t o = l * n + (size_t)perm[r] * bs + c;
     if (scatter) dst[o] = src[i];
     else dst[i] = src[o];
+  }
+}
+// Both ILU(0) triangular solves in one launch.  Each thread-block cluster
+// owns a group of independent matrix components and walks their merged
+// level schedule (lower levels, then upper levels); the rows of a level are
+// striped over the cluster's CTAs, 6 (or 3) lanes per block row as in the
+// level kernels above, and a hardware cluster barrier separates the levels.
+//
+// Latency, not bandwidth, bounds this walk, so only the neighbour values
+// produced by earlier levels are loaded after a barrier.  The level
+// pointers sit in shared memory; a row's descriptor (row, first block,
+// block count, diagonal block and the first MAXB block columns) is loaded
+// two levels ahead and its factor entries, right-hand side and, for the
+// upper solve, D^-1 row and lower-solve value one level ahead; those loads
+// are issued between the barrier's arrive (which releases the level's
+// stores) and its wait, so they overlap the barrier instead of delaying the
+// release.  Values produced
+// inside the launch (tmp, y) are read with ld.global.cg so they come from
+// L2, where the barrier's release/acquire ordering makes the other CTAs'
+// stores visible.  Same arithmetic per row as the level kernels.
+template <int MAXB>
+struct RowDesc {
+  int i, jbeg, nb, dpos;
+  int col[MAXB];
+};
+
+template <int MAXB>
+__device__ __forceinline__ void load_desc(RowDesc<MAXB> &d,
+                                          const int4 *__restrict__ desc,
+                                          int pos) {
+  constexpr int DW = 1 + MAXB / 4;
+  const int4 h = desc[(size_t)DW * pos];
+  d.i = h.x;
+  d.jbeg = h.y;
+  d.nb = h.z;
+  d.dpos = h.w;
+#pragma unroll
+  for (int q = 0; q < MAXB / 4; q++) {
+    const int4 c = desc[(size_t)DW * pos + 1 + q];
+    d.col[4 * q] = c.x;
+    d.col[4 * q + 1] = c.y;
+    d.col[4 * q + 2] = c.z;
+    d.col[4 * q + 3] = c.w;
+  }
+}
+
+template <int BS, int NR, int MAXB, typename T>
+struct RowData {
+  T a[MAXB][BS];
+  T base[NR];  // x_i (lower) or tmp_i (upper)
+  T dinv[BS];  // upper only
+};
+
+template <int BS, int NR, int MAXB, bool UPPER, typename T>
+__device__ __forceinline__ void load_data(RowData<BS, NR, MAXB, T> &p,
+                                          const RowDesc<MAXB> &d,
+                                          const T *__restrict__ F,
+                                          const T *__restrict__ basev,
+                                          size_t ld, int ii) {
+#pragma unroll
+  for (int q = 0; q < MAXB; q++) {
+    if (q < d.nb) {
+      const T *a = &F[(size_t)BS * BS * (d.jbeg + q) + BS * ii];
+#pragma unroll
+      for (int c = 0; c < BS; c++) p.a[q][c] = a[c];
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NR; l++)
+    p.base[l] = UPPER ? __ldcg(&basev[l * ld + (size_t)BS * d.i + ii])
+                      : basev[l * ld + (size_t)BS * d.i + ii];
+  if (UPPER) {
+    const T *dv = &F[(size_t)BS * BS * d.dpos + BS * ii];
+#pragma unroll
+    for (int c = 0; c < BS; c++) p.dinv[c] = dv[c];
+  }
+}
+
+// z = base - sum over the row's blocks of A_q v_cq (v read from L2)
+template <int BS, int NR, int MAXB, typename T>
+__device__ __forceinline__ void row_product(const RowDesc<MAXB> &d,
+                                            const RowData<BS, NR, MAXB, T> &p,
+                                            const int *__restrict__ cols,
+                                            const T *__restrict__ F,
+                                            const T *v, size_t ld, int ii,
+                                            T *z) {
+#pragma unroll
+  for (int l = 0; l < NR; l++) {
+    z[l] = p.base[l];
+    // all neighbour values of this right-hand side load together
+    T vv[MAXB][BS];
+#pragma unroll
+    for (int q = 0; q < MAXB; q++) {
+      if (q < d.nb) {
+        const size_t vo = (size_t)BS * d.col[q];
+#pragma unroll
+        for (int c = 0; c < BS; c++) vv[q][c] = __ldcg(&v[l * ld + vo + c]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < MAXB; q++) {
+      if (q < d.nb) {
+        T s = 0;
+#pragma unroll
+        for (int c = 0; c < BS; c++) s += p.a[q][c] * vv[q][c];
+        z[l] -= s;
+      }
+    }
+  }
+  for (int q = MAXB; q < d.nb; q++) {  // rows with more blocks than MAXB
+    const int j = d.jbeg + q;
+    const T *a = &F[(size_t)BS * BS * j + BS * ii];
+    const size_t vo = (size_t)BS * cols[j];
+#pragma unroll
+    for (int l = 0; l < NR; l++) {
+      const T *w = &v[l * ld + vo];
+      T s = 0;
+#pragma unroll
+      for (int c = 0; c < BS; c++) s += a[c] * __ldcg(w + c);
+      z[l] -= s;
+    }
+  }
+}
+
+template <int BS, int NR, int MAXB, typename T>
+__global__ void __launch_bounds__(256)
+    ilu_cluster_kernel(IluClusterView cv, const int *__restrict__ cols,
+                       const T *__restrict__ F, const T *__restrict__ x,
+                       T *__restrict__ tmp, T *__restrict__ y, size_t ld) {
+  namespace cg = cooperative_groups;
+  extern __shared__ int s_lp[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int cs = (int)cl.num_blocks();
+  const int g = blockIdx.x / cs;
+  const int rank = (int)cl.block_rank();
+  const int per_warp = 32 / BS;
+  const int lane = threadIdx.x & 31, sub = lane / BS, ii = lane - BS * sub;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int slots = nwarps * per_warp;  // rows per CTA per pass
+  const bool has_slot = sub < per_warp;
+  const int k0 = (warp * per_warp + (has_slot ? sub : 0)) * cs + rank;
+  const int stride = slots * cs;
+  // level pointers of this group: lower (nl + 1) then upper (nu + 1)
+  const int l0 = cv.grp_lvl[g], nl = cv.grp_lvl[g + 1] - l0 - 1;
+  const int u0 = cv.grp_ulvl[g], nu = cv.grp_ulvl[g + 1] - u0 - 1;
+  int *s_up = s_lp + nl + 1;
+  for (int t = threadIdx.x; t <= nl; t += blockDim.x) s_lp[t] = cv.lvl_ptr[l0 + t];
+  for (int t = threadIdx.x; t <= nu; t += blockDim.x) s_up[t] = cv.ulvl_ptr[u0 + t];
+  __syncthreads();
+  RowDesc<MAXB> D, Dn;
+  RowData<BS, NR, MAXB, T> P;
+  // ------------------------------------------------------------ lower
+  {
+    bool have = nl > 0 && has_slot && s_lp[0] + k0 < s_lp[1];
+    bool have_n = nl > 1 && has_slot && s_lp[1] + k0 < s_lp[2];
+    if (have) load_desc<MAXB>(D, cv.ldesc, s_lp[0] + k0);
+    if (have_n) load_desc<MAXB>(Dn, cv.ldesc, s_lp[1] + k0);
+    if (have) load_data<BS, NR, MAXB, false, T>(P, D, F, x, ld, ii);
+    for (int L = 0; L < nl; L++) {
+      const int b = s_lp[L], e = s_lp[L + 1];
+      if (have) {
+        T z[NR];
+        row_product<BS, NR, MAXB, T>(D, P, cols, F, tmp, ld, ii, z);
+#pragma unroll
+        for (int l = 0; l < NR; l++)
+          tmp[l * ld + (size_t)BS * D.i + ii] = z[l];
+        for (int k = k0 + stride; b + k < e; k += stride) {
+          RowDesc<MAXB> D2;
+          load_desc<MAXB>(D2, cv.ldesc, b + k);
+          load_data<BS, NR, MAXB, false, T>(P, D2, F, x, ld, ii);
+          row_product<BS, NR, MAXB, T>(D2, P, cols, F, tmp, ld, ii, z);
+#pragma unroll
+          for (int l = 0; l < NR; l++)
+            tmp[l * ld + (size_t)BS * D2.i + ii] = z[l];
+        }
+      }
+      // arrive (releasing this level's stores), then load level L+1's data
+      // and level L+2's descriptor while the barrier completes
+      auto tok = cl.barrier_arrive();
+      have = have_n;
+      D = Dn;
+      if (have) load_data<BS, NR, MAXB, false, T>(P, D, F, x, ld, ii);
+      have_n = L + 2 < nl && has_slot && s_lp[L + 2] + k0 < s_lp[L + 3];
+      if (have_n) load_desc<MAXB>(Dn, cv.ldesc, s_lp[L + 2] + k0);
+      cl.barrier_wait(std::move(tok));
+    }
+  }
+  // ------------------------------------------------------------ upper
+  {
+    bool have = nu > 0 && has_slot && s_up[0] + k0 < s_up[1];
+    bool have_n = nu > 1 && has_slot && s_up[1] + k0 < s_up[2];
+    if (have) load_desc<MAXB>(D, cv.udesc, s_up[0] + k0);
+    if (have_n) load_desc<MAXB>(Dn, cv.udesc, s_up[1] + k0);
+    if (have) load_data<BS, NR, MAXB, true, T>(P, D, F, tmp, ld, ii);
+    const int base_lane = lane - ii;
+    for (int L = 0; L < nu; L++) {
+      const int b = s_up[L], e = s_up[L + 1];
+      // every lane of a warp runs the same rounds: the D^-1 product
+      // exchanges z through shuffles
+      const int nrounds = (e - b + stride - 1) / stride;
+      for (int rd = 0; rd < nrounds; rd++) {
+        const int k = k0 + rd * stride;
+        const bool active = has_slot && b + k < e;
+        if (rd > 0 && active) {
+          load_desc<MAXB>(D, cv.udesc, b + k);
+          load_data<BS, NR, MAXB, true, T>(P, D, F, tmp, ld, ii);
+        }
+        T z[NR];
+#pragma unroll
+        for (int l = 0; l < NR; l++) z[l] = 0;
+        if (active) row_product<BS, NR, MAXB, T>(D, P, cols, F, y, ld, ii, z);
+#pragma unroll
+        for (int l = 0; l < NR; l++) {
+          T out = 0;
+#pragma unroll
+          for (int c = 0; c < BS; c++) {
+            const T zc = __shfl_sync(0xffffffffu, z[l], base_lane + c);
+            out += (active ? P.dinv[c] : T(0)) * zc;
+          }
+          if (active) y[l * ld + (size_t)BS * D.i + ii] = out;
+        }
+      }
+      auto tok = cl.barrier_arrive();
+      have = have_n;
+      D = Dn;
+      if (have) load_data<BS, NR, MAXB, true, T>(P, D, F, tmp, ld, ii);
+      have_n = L + 2 < nu && has_slot && s_up[L + 2] + k0 < s_up[L + 3];
+      if (have_n) load_desc<MAXB>(Dn, cv.udesc, s_up[L + 2] + k0);
+      cl.barrier_wait(std::move(tok));
+    }
+  }
+}
+
+// One block per element segment: KS max, KS sum and compliance over the
+// segment's points, each a fixed-order block reduction.
+__device__ double block_reduce(double v, bool is_max, double *sh) {
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = is_max ? fmax(v, o) : v + o;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = sh[0];
+  for (int q = 1; q < (int)(blockDim.x >> 5); q++)
+    t = is_max ? fmax(t, sh[q]) : t + sh[q];
+  __syncthreads();
+  return t;
+}
+__global__ void __launch_bounds__(256)
+    segment_functions_kernel(const double *__restrict__ fail,
+                             const double *__restrict__ wdet,
+                             const double *__restrict__ sed, int nq,
+                             const int *__restrict__ seg_ptr, double ksw,
+                             KsStats *__restrict__ out_ks,
+                             double *__restrict__ out_comp) {
+  __shared__ double sh[8];
+  const int g = blockIdx.x;
+  const size_t e0 = seg_ptr[g], e1 = seg_ptr[g + 1];
+  double mx = -INFINITY;
+  for (size_t i = e0 * nq + threadIdx.x; i < e1 * nq; i += blockDim.x)
+    mx = fmax(mx, fail[i]);
+  mx = block_reduce(mx, true, sh);
+  double sm = 0.0;
+  for (size_t i = e0 * nq + threadIdx.x; i < e1 * nq; i += blockDim.x)
+    sm += wdet[i] * exp(ksw * (fail[i] - mx));
+  sm = block_reduce(sm, false, sh);
+  double c = 0.0;
+  for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) c += sed[e];
+  c = block_reduce(c, false, sh);
+  if (threadIdx.x == 0) {
+    out_ks[g].max = mx;
+    out_ks[g].sum = sm;
+    out_ks[g].weight = ksw;
+    out_comp[g] = c;
   }
 }
 
@@ -503,15 +843,17 @@ __global__ void permute_kernel(int nrows, int bs, const int *perm,
 // ------------------------------------------------------------- launchers
 void launch_bcsr_mult(int bsize, int nrows, const int *rowp, const int *cols,
                       const double *A, const double *x, double *y,
-                      cudaStream_t s) {
-  if (bsize == 6) mult_dispatch<6, double>(nrows, rowp, cols, A, x, y, s);
-  else mult_dispatch<3, double>(nrows, rowp, cols, A, x, y, s);
+                      cudaStream_t s, int nrhs, size_t ld) {
+  if (bsize == 6)
+    mult_dispatch<6, double>(nrows, rowp, cols, A, x, y, nrhs, ld, s);
+  else mult_dispatch<3, double>(nrows, rowp, cols, A, x, y, nrhs, ld, s);
 }
 void launch_bcsr_mult_f32(int bsize, int nrows, const int *rowp,
                           const int *cols, const float *A, const float *x,
-                          float *y, cudaStream_t s) {
-  if (bsize == 6) mult_dispatch<6, float>(nrows, rowp, cols, A, x, y, s);
-  else mult_dispatch<3, float>(nrows, rowp, cols, A, x, y, s);
+                          float *y, cudaStream_t s, int nrhs, size_t ld) {
+  if (bsize == 6)
+    mult_dispatch<6, float>(nrows, rowp, cols, A, x, y, nrhs, ld, s);
+  else mult_dispatch<3, float>(nrows, rowp, cols, A, x, y, nrhs, ld, s);
 }
 void launch_apply_bcs_mat(int bsize, int nbcs, const int *bc_nodes,
                           const int *bc_masks, const int *rowp,
@@ -574,6 +916,16 @@ void launch_ks_sum(const double *fail, const double *wdet, size_t n,
   reduce_final_kernel<0><<<1, 256, 0, s>>>(partials, npart, out);
 }
 
+void launch_segment_functions(const double *elem_fail, const double *elem_wdet,
+                              const double *elem_sed, int nq,
+                              const int *seg_elem_ptr, int nseg, double ksw,
+                              KsStats *seg_ks, double *seg_comp,
+                              cudaStream_t s) {
+  if (nseg <= 0) return;
+  segment_functions_kernel<<<nseg, 256, 0, s>>>(
+      elem_fail, elem_wdet, elem_sed, nq, seg_elem_ptr, ksw, seg_ks, seg_comp);
+}
+
 template <typename T>
 static void factor_level(const IluPlan &p, int level, T *F, cudaStream_t s) {
   const int b = p.lvl_ptr_h[level], n = p.lvl_ptr_h[level + 1] - b;
@@ -608,66 +960,172 @@ void launch_block_inverse_diag(const IluPlan &p, double *F, cudaStream_t s) {
                                                           p.d_fail);
 }
 
+template <int BS, int NR, typename T>
+static void level_pair(const IluPlan &p, bool upper, int L, const T *F,
+                       const T *in, T *out, size_t ld, cudaStream_t s) {
+  const int per_warp = 32 / BS;
+  const std::vector<int> &ptr = upper ? p.ulvl_ptr_h : p.lvl_ptr_h;
+  const int b = ptr[L], n = ptr[L + 1] - b;
+  int blocks = blocks_for((size_t)((n + per_warp - 1) / per_warp) * 32, 256, 16);
+  if (upper)
+    ilu_upper_level_kernel<BS, NR, T><<<blocks, 256, 0, s>>>(
+        p.ulvl_rows + b, n, p.rowp, p.cols, p.diag, F, in, out, ld);
+  else
+    ilu_lower_level_kernel<BS, NR, T><<<blocks, 256, 0, s>>>(
+        p.lvl_rows + b, n, p.rowp, p.cols, F, in, out, ld);
+}
+
+template <int BS, typename T>
+static void level_multi(const IluPlan &p, bool upper, int L, const T *F,
+                        const T *in, T *out, int nrhs, size_t ld,
+                        cudaStream_t s) {
+  for (int l = 0; l < nrhs;) {
+    const int left = nrhs - l;
+    const size_t o = l * ld;
+    if (left >= 4) {
+      level_pair<BS, 4, T>(p, upper, L, F, in + o, out + o, ld, s);
+      l += 4;
+    } else if (left >= 2) {
+      level_pair<BS, 2, T>(p, upper, L, F, in + o, out + o, ld, s);
+      l += 2;
+    } else {
+      level_pair<BS, 1, T>(p, upper, L, F, in + o, out + o, ld, s);
+      l += 1;
+    }
+  }
+}
+
+
+template <int BS, int NR, typename T>
+static void cluster_launch(const IluPlan &p, const T *F, const T *x, T *y,
+                           T *tmp, size_t ld, cudaStream_t s) {
+  auto kern = ilu_cluster_kernel<BS, NR, (BS == 6 ? 4 : 8), T>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                         1);
+    attr = true;
+  }
+  const size_t smem = sizeof(int) * (size_t)p.cluster.max_lp;
+  static size_t smem_set = 0;
+  if (smem > smem_set && smem > 48 * 1024) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    smem_set = smem;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.cluster.ngroups * p.cluster.cs);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = p.cluster.cs;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, p.cluster, p.cols, F, x, tmp, y, ld);
+}
+
+// Largest cluster size (of 16, 8, 4, 2, 1) the device can schedule for the
+// cluster triangular-solve kernel.
+int ilu_cluster_max_size() {
+  auto kern = ilu_cluster_kernel<6, 4, 4, double>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                       1);
+  for (int cs = 16; cs > 1; cs >>= 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(256);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n > 0)
+      return cs;
+    cudaGetLastError();
+  }
+  return 1;
+}
+
+template <typename T>
+static void apply_cluster(const IluPlan &p, const T *F, const T *x, T *y,
+                          T *tmp, int nrhs, size_t ld, cudaStream_t s) {
+  for (int l = 0; l < nrhs;) {
+    const int left = nrhs - l;
+    const size_t o = l * ld;
+    const int nr = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
+    if (p.bsize == 6) {
+      if (nr == 4) cluster_launch<6, 4, T>(p, F, x + o, y + o, tmp + o, ld, s);
+      else if (nr == 2) cluster_launch<6, 2, T>(p, F, x + o, y + o, tmp + o, ld, s);
+      else cluster_launch<6, 1, T>(p, F, x + o, y + o, tmp + o, ld, s);
+    } else {
+      if (nr == 4) cluster_launch<3, 4, T>(p, F, x + o, y + o, tmp + o, ld, s);
+      else if (nr == 2) cluster_launch<3, 2, T>(p, F, x + o, y + o, tmp + o, ld, s);
+      else cluster_launch<3, 1, T>(p, F, x + o, y + o, tmp + o, ld, s);
+    }
+    l += nr;
+  }
+}
+
 template <typename T>
 static void apply_levels(const IluPlan &p, const T *F, const T *x, T *y,
-                         T *tmp, cudaStream_t s) {
-  const int per_warp = 32 / p.bsize;
+                         T *tmp, int nrhs, size_t ld, cudaStream_t s) {
+  if (p.cluster.ngroups > 0) {
+    apply_cluster<T>(p, F, x, y, tmp, nrhs, ld, s);
+    return;
+  }
   const int nl = (int)p.lvl_ptr_h.size() - 1;
   for (int L = 0; L < nl; L++) {
-    const int b = p.lvl_ptr_h[L], n = p.lvl_ptr_h[L + 1] - b;
-    int blocks = blocks_for((size_t)((n + per_warp - 1) / per_warp) * 32, 256, 16);
-    if (p.bsize == 6)
-      ilu_lower_level_kernel<6, T><<<blocks, 256, 0, s>>>(p.lvl_rows + b, n,
-                                                          p.rowp, p.cols, F, x,
-                                                          tmp);
-    else
-      ilu_lower_level_kernel<3, T><<<blocks, 256, 0, s>>>(p.lvl_rows + b, n,
-                                                          p.rowp, p.cols, F, x,
-                                                          tmp);
+    if (p.bsize == 6) level_multi<6, T>(p, false, L, F, x, tmp, nrhs, ld, s);
+    else level_multi<3, T>(p, false, L, F, x, tmp, nrhs, ld, s);
   }
   const int nu = (int)p.ulvl_ptr_h.size() - 1;
   for (int L = 0; L < nu; L++) {
-    const int b = p.ulvl_ptr_h[L], n = p.ulvl_ptr_h[L + 1] - b;
-    int blocks = blocks_for((size_t)((n + per_warp - 1) / per_warp) * 32, 256, 16);
-    if (p.bsize == 6)
-      ilu_upper_level_kernel<6, T><<<blocks, 256, 0, s>>>(
-          p.ulvl_rows + b, n, p.rowp, p.cols, p.diag, F, tmp, y);
-    else
-      ilu_upper_level_kernel<3, T><<<blocks, 256, 0, s>>>(
-          p.ulvl_rows + b, n, p.rowp, p.cols, p.diag, F, tmp, y);
+    if (p.bsize == 6) level_multi<6, T>(p, true, L, F, tmp, y, nrhs, ld, s);
+    else level_multi<3, T>(p, true, L, F, tmp, y, nrhs, ld, s);
   }
 }
 void launch_ilu0_apply(const IluPlan &p, const double *F, const double *x,
-                       double *y, double *tmp, cudaStream_t s) {
-  apply_levels<double>(p, F, x, y, tmp, s);
+                       double *y, double *tmp, cudaStream_t s, int nrhs,
+                       size_t ld) {
+  apply_levels<double>(p, F, x, y, tmp, nrhs, ld, s);
 }
 void launch_ilu0_apply_f32(const IluPlan &p, const float *F, const float *x,
-                           float *y, float *tmp, cudaStream_t s) {
-  apply_levels<float>(p, F, x, y, tmp, s);
+                           float *y, float *tmp, cudaStream_t s, int nrhs,
+                           size_t ld) {
+  apply_levels<float>(p, F, x, y, tmp, nrhs, ld, s);
 }
 void launch_block_jacobi_apply(const IluPlan &p, const double *F,
-                               const double *x, double *y, cudaStream_t s) {
+                               const double *x, double *y, cudaStream_t s,
+                               int nrhs, size_t ld) {
   const int per_warp = 32 / p.bsize;
   int blocks = blocks_for((size_t)((p.nrows + per_warp - 1) / per_warp) * 32,
                           256, 16);
   if (p.bsize == 6)
     block_jacobi_kernel<6, double><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F,
-                                                          x, y);
+                                                          x, y, nrhs, ld);
   else
     block_jacobi_kernel<3, double><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F,
-                                                          x, y);
+                                                          x, y, nrhs, ld);
 }
 void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,
-                                   const float *x, float *y, cudaStream_t s) {
+                                   const float *x, float *y, cudaStream_t s,
+                                   int nrhs, size_t ld) {
   const int per_warp = 32 / p.bsize;
   int blocks = blocks_for((size_t)((p.nrows + per_warp - 1) / per_warp) * 32,
                           256, 16);
   if (p.bsize == 6)
     block_jacobi_kernel<6, float><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F, x,
-                                                         y);
+                                                         y, nrhs, ld);
   else
     block_jacobi_kernel<3, float><<<blocks, 256, 0, s>>>(p.nrows, p.diag, F, x,
-                                                         y);
+                                                         y, nrhs, ld);
 }
 
 void launch_dots(const double *W, size_t ld, int k, const double *w,
@@ -711,24 +1169,32 @@ void launch_gather_blocks_f32(int nnz, int b2, const int *valmap,
       nnz, b2, valmap, src, dst);
 }
 void launch_permute_gather(int nrows, int bs, const int *perm,
-                           const double *src, double *dst, cudaStream_t s) {
-  permute_kernel<double><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
-      nrows, bs, perm, src, dst, 0);
+                           const double *src, double *dst, cudaStream_t s,
+                           int nrhs) {
+  permute_kernel<double>
+      <<<blocks_for((size_t)nrows * bs * nrhs, 256), 256, 0, s>>>(
+          nrows, bs, perm, src, dst, 0, nrhs);
 }
 void launch_permute_scatter(int nrows, int bs, const int *perm,
-                            const double *src, double *dst, cudaStream_t s) {
-  permute_kernel<double><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
-      nrows, bs, perm, src, dst, 1);
+                            const double *src, double *dst, cudaStream_t s,
+                            int nrhs) {
+  permute_kernel<double>
+      <<<blocks_for((size_t)nrows * bs * nrhs, 256), 256, 0, s>>>(
+          nrows, bs, perm, src, dst, 1, nrhs);
 }
 void launch_permute_gather_f32(int nrows, int bs, const int *perm,
-                               const float *src, float *dst, cudaStream_t s) {
-  permute_kernel<float><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
-      nrows, bs, perm, src, dst, 0);
+                               const float *src, float *dst, cudaStream_t s,
+                               int nrhs) {
+  permute_kernel<float>
+      <<<blocks_for((size_t)nrows * bs * nrhs, 256), 256, 0, s>>>(
+          nrows, bs, perm, src, dst, 0, nrhs);
 }
 void launch_permute_scatter_f32(int nrows, int bs, const int *perm,
-                                const float *src, float *dst, cudaStream_t s) {
-  permute_kernel<float><<<blocks_for((size_t)nrows * bs, 256), 256, 0, s>>>(
-      nrows, bs, perm, src, dst, 1);
+                                const float *src, float *dst, cudaStream_t s,
+                                int nrhs) {
+  permute_kernel<float>
+      <<<blocks_for((size_t)nrows * bs * nrhs, 256), 256, 0, s>>>(
+          nrows, bs, perm, src, dst, 1, nrhs);
 }
 
 }  // namespace tg

@@ -381,6 +381,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   const HexC c = hex_c(ep);
   for (int idx = gw; idx < cr.count; idx += nw) {
     const int e = cr.elem_list[idx];
+    const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
     hex_load(S, m, e, vars, nullptr, lane);
     hex_geometry(S, lane);
     if (lane < 8) {
@@ -394,7 +395,7 @@ __global__ void __launch_bounds__(WARPS * 32)
         HexFail fo = hex_failure(ep, c, ev);
         for (int k = 0; k < 6; k++) S.g[lane][k] = fo.dfde[k];
         S.coef[lane] =
-            exp(ks.weight * (fo.f - ks.max)) / ks.sum * S.det[lane];
+            exp(kk.weight * (fo.f - kk.max)) / kk.sum * S.det[lane];
       }
     }
     __syncwarp();

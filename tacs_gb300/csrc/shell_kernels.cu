@@ -375,6 +375,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   const int nw = gridDim.x * WARPS;
   for (int idx = gw; idx < cr.count; idx += nw) {
     const int e = cr.elem_list[idx];
+    const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
     load_element(S, m, e, vars, nullptr, lane);
     shell_build_B(S, ep, lane);
     shell_strains(S, S.u, S.e, lane);
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(WARPS * 32)
         FailOut fo = shell_failure(ep, S.t, ev);
         for (int r = 0; r < 6; r++) S.g[q][r] = fo.dfde[r];
         S.g[q][6] = S.g[q][7] = S.g[q][8] = 0.0;
-        S.coef[q] = exp(ks.weight * (fo.f - ks.max)) / ks.sum * S.det[q];
+        S.coef[q] = exp(kk.weight * (fo.f - kk.max)) / kk.sum * S.det[q];
       }
     }
     __syncwarp();
@@ -422,6 +423,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
   const int nw = gridDim.x * WARPS;
   for (int e = gw; e < m.nelem; e += nw) {
+    const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
     load_element(S, m, e, vars, psi, lane);
     shell_build_B(S, ep, lane);
     shell_strains(S, S.u, S.e, lane);
@@ -438,7 +440,7 @@ __global__ void __launch_bounds__(WARPS * 32)
           acc += coef * S.det[q] * shell_stress_dv(ep, S.t, ev, ev);
         } else {
           FailOut fo = shell_failure(ep, S.t, ev);
-          double dfdq = S.det[q] * exp(ks.weight * (fo.f - ks.max)) / ks.sum;
+          double dfdq = S.det[q] * exp(kk.weight * (fo.f - kk.max)) / kk.sum;
           acc += coef * dfdq * fo.dfdt;
         }
       }

@@ -20,6 +20,12 @@ struct ElemParams {
   double ref_axis[3];  // normalised reference axis
 };
 
+// KS aggregate statistics: max over the points and sum of w detXd
+// exp(weight (f - max)) (TACSKSFailure, src/functions/TACSKSFailure.cpp).
+struct KsStats {
+  double max, sum, weight;
+};
+
 // Device-side view of an assembler used by the element kernels.
 struct MeshView {
   int nnodes, nelem, vpn, npe;
@@ -31,6 +37,10 @@ struct MeshView {
   const int *trac_face;   // per traction entry
   const double *trac_val; // 3 per traction entry
   const int *rowp, *cols; // BCSR pattern
+  // element segments (independent meshes in one assembler): when elem_seg
+  // is set, the KS sensitivities of element e use seg_ks[elem_seg[e]]
+  const int *elem_seg;
+  const struct KsStats *seg_ks;
 };
 
 // One launch of an element kernel covers the elements of one colour:
@@ -73,10 +83,7 @@ void launch_hex_points(const ElemParams &ep, const MeshView &m,
                        double *elem_wdet, double *elem_sed, cudaStream_t s);
 
 // dfdu += alpha * df/du for one colour.  func: TG_FUNC_*; for KS the
-// statistics ks_max / ks_sum / ks_weight are used.
-struct KsStats {
-  double max, sum, weight;
-};
+// statistics ks (or the element's segment statistics) are used.
 void launch_shell_sv_sens(const ElemParams &ep, const MeshView &m,
                           ColorRange cr, const double *vars, int func,
                           KsStats ks, double alpha, double *dfdu,
@@ -97,12 +104,14 @@ void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
                    double scale, double *out, cudaStream_t s);
 
 // ------------------------------------------------------- BCSR / vectors
+// nrhs vectors ld apart (ld may be 0 when nrhs == 1)
 void launch_bcsr_mult(int bsize, int nrows, const int *rowp, const int *cols,
                       const double *A, const double *x, double *y,
-                      cudaStream_t s);
+                      cudaStream_t s, int nrhs = 1, size_t ld = 0);
 void launch_bcsr_mult_f32(int bsize, int nrows, const int *rowp,
                           const int *cols, const float *A, const float *x,
-                          float *y, cudaStream_t s);
+                          float *y, cudaStream_t s, int nrhs = 1,
+                          size_t ld = 0);
 void launch_apply_bcs_mat(int bsize, int nbcs, const int *bc_nodes,
                           const int *bc_masks, const int *rowp,
                           const int *cols, double *A, cudaStream_t s);
@@ -126,6 +135,31 @@ void launch_reduce_sum(const double *x, size_t n, double *partials,
 void launch_ks_sum(const double *fail, const double *wdet, size_t n,
                    const double *dmax, double ksw, double *partials,
                    int npart, double *out, cudaStream_t s);
+// Per-segment compliance and KS statistics over contiguous element ranges
+// seg_elem_ptr[g]..seg_elem_ptr[g+1] (nq points per element).
+void launch_segment_functions(const double *elem_fail, const double *elem_wdet,
+                              const double *elem_sed, int nq,
+                              const int *seg_elem_ptr, int nseg, double ksw,
+                              KsStats *seg_ks, double *seg_comp,
+                              cudaStream_t s);
+
+// Cluster schedule of the ILU(0) triangular solves: the matrix's
+// independent components are grouped, one thread-block cluster of cs CTAs
+// per group.  Group g's lower levels are lvl_ptr[grp_lvl[g] ..
+// grp_lvl[g+1]) (level pointers into ldesc), its upper levels likewise in
+// ulvl_ptr / udesc.  A row descriptor is 1 + MAXB/4 int4s (MAXB = 4 for
+// 6x6 blocks, 8 for 3x3): {row, first block, block count, diagonal block}
+// and the columns of the first MAXB blocks -- the strictly lower blocks
+// rowp[i]..diag[i] for the lower solve, diag[i]+1..rowp[i+1] for the upper
+// one.  max_lp: the most level pointers (lower + upper) of any group.
+// ngroups == 0: no cluster schedule.
+struct IluClusterView {
+  int ngroups, cs, max_lp;
+  const int *grp_lvl, *lvl_ptr;
+  const int4 *ldesc;
+  const int *grp_ulvl, *ulvl_ptr;
+  const int4 *udesc;
+};
 
 // Level-scheduled block ILU(0) (natural order) and block Jacobi.
 struct IluPlan {
@@ -140,16 +174,20 @@ struct IluPlan {
   const int *upd_ptr;  // per lower entry j: range into upd_tgt/upd_src
   const int *upd_tgt, *upd_src;
   int *d_fail;  // device int: first failing row + 1
+  IluClusterView cluster;  // triangular solves in one cluster launch
 };
 void launch_ilu0_factor_level(const IluPlan &p, int level, double *F,
                               cudaStream_t s);
 void launch_ilu0_factor_level_f32(const IluPlan &p, int level, float *F,
                                   cudaStream_t s);
 void launch_block_inverse_diag(const IluPlan &p, double *F, cudaStream_t s);
+int ilu_cluster_max_size();
 void launch_ilu0_apply(const IluPlan &p, const double *F, const double *x,
-                       double *y, double *tmp, cudaStream_t s);
+                       double *y, double *tmp, cudaStream_t s, int nrhs = 1,
+                       size_t ld = 0);
 void launch_ilu0_apply_f32(const IluPlan &p, const float *F, const float *x,
-                           float *y, float *tmp, cudaStream_t s);
+                           float *y, float *tmp, cudaStream_t s,
+                           int nrhs = 1, size_t ld = 0);
 // colour-reordered ILU(0): value gather through a block map and vector
 // permutation (dst[r] = src[perm[r]] / dst[perm[r]] = src[r], bs per node)
 void launch_gather_blocks(int nnz, int b2, const int *valmap,
@@ -157,17 +195,23 @@ void launch_gather_blocks(int nnz, int b2, const int *valmap,
 void launch_gather_blocks_f32(int nnz, int b2, const int *valmap,
                               const double *src, float *dst, cudaStream_t s);
 void launch_permute_gather(int nrows, int bs, const int *perm,
-                           const double *src, double *dst, cudaStream_t s);
+                           const double *src, double *dst, cudaStream_t s,
+                           int nrhs = 1);
 void launch_permute_scatter(int nrows, int bs, const int *perm,
-                            const double *src, double *dst, cudaStream_t s);
+                            const double *src, double *dst, cudaStream_t s,
+                            int nrhs = 1);
 void launch_permute_gather_f32(int nrows, int bs, const int *perm,
-                               const float *src, float *dst, cudaStream_t s);
+                               const float *src, float *dst, cudaStream_t s,
+                               int nrhs = 1);
 void launch_permute_scatter_f32(int nrows, int bs, const int *perm,
-                                const float *src, float *dst, cudaStream_t s);
+                                const float *src, float *dst, cudaStream_t s,
+                                int nrhs = 1);
 void launch_block_jacobi_apply(const IluPlan &p, const double *F,
-                               const double *x, double *y, cudaStream_t s);
+                               const double *x, double *y, cudaStream_t s,
+                               int nrhs = 1, size_t ld = 0);
 void launch_block_jacobi_apply_f32(const IluPlan &p, const float *F,
-                                   const float *x, float *y, cudaStream_t s);
+                                   const float *x, float *y, cudaStream_t s,
+                                   int nrhs = 1, size_t ld = 0);
 
 // GMRES helpers (FP64 Arnoldi)
 void launch_dots(const double *W, size_t ld, int k, const double *w,
@@ -178,6 +222,53 @@ void launch_axpy(double a, const double *x, double *y, size_t n,
                  cudaStream_t s);
 void launch_scale(double a, double *x, size_t n, cudaStream_t s);
 void launch_copy(const double *x, double *y, size_t n, cudaStream_t s);
+
+// Batched GMRES (krylov_kernels.cu).  A multivector of nrhs vectors (ld
+// apart) is split into systems; chunks of at most 256 * ept entries never
+// cross a system.  All arrays are device memory.
+struct KrylovChunks {
+  const int *start;    // offset of the chunk in the multivector
+  const int *len;      // entries in the chunk
+  const int *sys;      // system of the chunk
+  const int *sys_ptr;  // nsys + 1: chunk range of each system
+  int nchunks, nsys, ept;
+};
+struct KrylovState {
+  int m, nsys;
+  double atol;
+  double *H;         // nsys x (m+1) x m, column-major Hessenberg per system
+  double *Qc, *Qs;   // nsys x m Givens rotations
+  double *res;       // nsys x (m+1) rotated residual, then -y
+  double *h1, *h2;   // nsys x (m+1) the two Gram-Schmidt projections
+  double *nrm2;      // nsys squared norms
+  double *scale;     // nsys basis-vector scale (0 for inactive systems)
+  double *rhs_norm;  // nsys first-cycle residual norms
+  double *rn;        // nsys latest residual (estimate or true)
+  double *rtol;      // nsys relative tolerances
+  int *active, *converged, *done, *err, *niters, *iters;  // nsys each
+  int *first;        // 1 before the first cycle of a solve
+  int *it;           // current Arnoldi index
+  int *nactive;      // systems still iterating
+};
+void launch_kr_dots(const double *W, size_t ld, const int *kdev, int kofs,
+                    int kmax, const double *w, const KrylovChunks &ch,
+                    double *partials, double *out, int ldo, cudaStream_t s);
+void launch_kr_gemv_sub(const double *W, size_t ld, const int *kdev, int kofs,
+                        int kmax, const double *coef, int ldc,
+                        const KrylovChunks &ch, double *w, double *normparts,
+                        cudaStream_t s);
+void launch_kr_norm_final(const double *normparts, const KrylovChunks &ch,
+                          double *out, cudaStream_t s);
+void launch_kr_scale_store(const double *w, const KrylovChunks &ch,
+                           const double *scale, double *W, size_t ld,
+                           const int *it, double *v, cudaStream_t s);
+void launch_kr_residual(const double *b, double *r, size_t n, cudaStream_t s);
+void launch_kr_axpy(const double *x, double *y, size_t n, cudaStream_t s);
+void launch_kr_mask(double *x, const KrylovChunks &ch, const double *scale,
+                    cudaStream_t s);
+void launch_kr_cycle_init(const KrylovState &st, cudaStream_t s);
+void launch_kr_arnoldi(const KrylovState &st, cudaStream_t s);
+void launch_kr_solve_y(const KrylovState &st, cudaStream_t s);
 
 // error reporting
 void set_error(const std::string &msg);

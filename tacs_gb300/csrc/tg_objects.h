@@ -1,0 +1,252 @@
+// Host-side objects behind the opaque handles of the C ABI (assembler,
+// BCSR matrix, preconditioner, Krylov solver) and the small allocation
+// helpers shared by the runtime translation units.  Internal header.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "tg_internal.h"
+
+namespace tg {
+
+template <typename T>
+inline int dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) return cuda_check(e, "cudaMalloc");
+  return 0;
+}
+template <typename T>
+inline int upload(T **p, const std::vector<T> &h) {
+  int rc = dalloc(p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) {
+    cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_check(e, "cudaMemcpy H2D");
+  }
+  return 0;
+}
+template <typename T>
+inline void dfree(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+inline int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+struct tg_assembler {
+  int refcount = 1;
+  ElemParams ep{};
+  int nnodes = 0, nelem = 0, vpn = 0, npe = 0;
+  std::vector<int> conn_h;
+  std::vector<int> bc_nodes_h, bc_masks_h;
+  std::vector<double> thick_h;
+  std::vector<int> dvnum_h;
+  std::vector<double> pres_h;  // 4 per element (zeros where unloaded)
+  bool has_pres = false;
+  std::vector<int> trac_ptr_h, trac_face_h;
+  std::vector<double> trac_val_h;
+  bool initialized = false;
+  int ndv = 0;
+  // BCSR pattern
+  std::vector<int> rowp_h, cols_h, diag_h;
+  // colouring
+  std::vector<int> color_ptr_h, color_elems_h;
+  // device
+  int *d_conn = nullptr;
+  double *d_xpts = nullptr, *d_thick = nullptr, *d_pres = nullptr;
+  int *d_dvnum = nullptr, *d_trac_ptr = nullptr, *d_trac_face = nullptr;
+  double *d_trac_val = nullptr;
+  int *d_bc_nodes = nullptr, *d_bc_masks = nullptr;
+  int *d_rowp = nullptr, *d_cols = nullptr, *d_diag = nullptr;
+  int *d_color_elems = nullptr;
+  int *d_dv_ptr = nullptr, *d_dv_elems = nullptr;
+  double *d_elem_fail = nullptr, *d_elem_wdet = nullptr;
+  double *d_elem_sed = nullptr, *d_elem_val = nullptr;
+  double *d_partials = nullptr, *d_scalars = nullptr;
+  int npart = 512;
+  KsStats ks{0.0, 1.0, 100.0};
+  bool ks_valid = false;
+  // element segments (independent meshes): contiguous element ranges
+  int nseg = 0;
+  std::vector<int> seg_elem_ptr_h;
+  int *d_elem_seg = nullptr, *d_seg_elem_ptr = nullptr;
+  KsStats *d_seg_ks = nullptr;
+  double *d_seg_comp = nullptr;
+  bool seg_ks_valid = false;
+
+  int nq() const { return ep.elem_type == TG_ELEM_MITC4 ? 4 : 8; }
+
+  MeshView view() const {
+    MeshView m;
+    m.nnodes = nnodes;
+    m.nelem = nelem;
+    m.vpn = vpn;
+    m.npe = npe;
+    m.conn = d_conn;
+    m.xpts = d_xpts;
+    m.thick = d_thick;
+    m.pres = has_pres ? d_pres : nullptr;
+    m.trac_ptr = trac_val_h.empty() ? nullptr : d_trac_ptr;
+    m.trac_face = d_trac_face;
+    m.trac_val = d_trac_val;
+    m.rowp = d_rowp;
+    m.cols = d_cols;
+    m.elem_seg = nullptr;
+    m.seg_ks = nullptr;
+    return m;
+  }
+  // view whose KS sensitivities use the per-segment statistics
+  MeshView view_segments() const {
+    MeshView m = view();
+    m.elem_seg = d_elem_seg;
+    m.seg_ks = d_seg_ks;
+    return m;
+  }
+  ColorRange color(int c) const {
+    ColorRange r;
+    r.elem_list = d_color_elems + color_ptr_h[c];
+    r.count = color_ptr_h[c + 1] - color_ptr_h[c];
+    return r;
+  }
+  int ncolors() const { return (int)color_ptr_h.size() - 1; }
+
+  ~tg_assembler() {
+    dfree(d_conn); dfree(d_xpts); dfree(d_thick); dfree(d_pres);
+    dfree(d_dvnum); dfree(d_trac_ptr); dfree(d_trac_face); dfree(d_trac_val);
+    dfree(d_bc_nodes); dfree(d_bc_masks); dfree(d_rowp); dfree(d_cols);
+    dfree(d_diag); dfree(d_color_elems); dfree(d_dv_ptr); dfree(d_dv_elems);
+    dfree(d_elem_fail); dfree(d_elem_wdet); dfree(d_elem_sed);
+    dfree(d_elem_val); dfree(d_partials); dfree(d_scalars);
+    dfree(d_elem_seg); dfree(d_seg_elem_ptr); dfree(d_seg_ks);
+    dfree(d_seg_comp);
+  }
+};
+
+struct tg_mat {
+  int refcount = 1;
+  tg_assembler *a = nullptr;
+  int bsize = 0, nrows = 0, nnz = 0;
+  double *d_vals = nullptr;
+  float *d_vals32 = nullptr;
+  ~tg_mat() {
+    dfree(d_vals);
+    dfree(d_vals32);
+  }
+};
+
+struct tg_pc {
+  int refcount = 1;
+  tg_mat *A = nullptr;
+  int type = TG_PC_ILU0, precision = TG_PREC_FP64;
+  IluPlan plan{};
+  int *d_lvl_rows = nullptr, *d_ulvl_rows = nullptr;
+  int *d_upd_ptr = nullptr, *d_upd_tgt = nullptr, *d_upd_src = nullptr;
+  int *d_fail = nullptr;
+  double *d_F = nullptr, *d_tmp = nullptr;
+  float *d_F32 = nullptr, *d_x32 = nullptr, *d_y32 = nullptr,
+        *d_tmp32 = nullptr;
+  double *d_gx = nullptr, *d_gy = nullptr;  // FP64 apply in/out buffers
+  // colour-reordered variant: permuted pattern, value map, permutation and
+  // permuted work vectors
+  int *d_prowp = nullptr, *d_pcols = nullptr, *d_pdiag = nullptr;
+  int *d_valmap = nullptr, *d_perm = nullptr;
+  double *d_px = nullptr, *d_py = nullptr;
+  float *d_px32 = nullptr, *d_py32 = nullptr;
+  int ncolors = 0;
+  // cluster schedule of the triangular solves (natural-order ILU(0))
+  int *d_cl_grp_lvl = nullptr, *d_cl_lvl_ptr = nullptr, *d_cl_rows = nullptr;
+  int *d_cl_grp_ulvl = nullptr, *d_cl_ulvl_ptr = nullptr,
+      *d_cl_urows = nullptr;
+  // the level-by-level triangular solves replayed as one CUDA graph
+  cudaGraphExec_t apply_exec = nullptr;
+  bool factored = false;
+  ~tg_pc() {
+    if (apply_exec) cudaGraphExecDestroy(apply_exec);
+    dfree(d_lvl_rows); dfree(d_ulvl_rows); dfree(d_upd_ptr);
+    dfree(d_upd_tgt); dfree(d_upd_src); dfree(d_fail); dfree(d_F);
+    dfree(d_tmp); dfree(d_F32); dfree(d_x32); dfree(d_y32); dfree(d_tmp32);
+    dfree(d_gx); dfree(d_gy); dfree(d_prowp); dfree(d_pcols); dfree(d_pdiag);
+    dfree(d_valmap); dfree(d_perm); dfree(d_px); dfree(d_py);
+    dfree(d_px32); dfree(d_py32); dfree(d_cl_grp_lvl); dfree(d_cl_lvl_ptr);
+    dfree(d_cl_rows); dfree(d_cl_grp_ulvl); dfree(d_cl_ulvl_ptr);
+    dfree(d_cl_urows);
+  }
+};
+
+// Restarted GMRES over nsys = nseg x nrhs systems (tg_krylov.cu).  The
+// device buffers are sized for one multivector width (nrhs) at a time and
+// the CUDA graphs of a cycle are captured against them.
+struct tg_ksm {
+  int refcount = 1;
+  tg_mat *A = nullptr;
+  tg_pc *pc = nullptr;
+  int m = 0, nrestart = 0, mixed = 0;
+  double rtol = 1e-8, atol = 1e-30;
+  size_t n = 0;                 // rows x block size of A
+  std::vector<int> seg_rows;    // nseg + 1 block-row offsets of the systems
+  int nrhs = 0;                 // current multivector width (0: not laid out)
+  size_t N = 0;                 // nrhs * n
+  int nsys = 0;
+  // multivector buffers
+  double *d_W = nullptr, *d_v = nullptr, *d_w = nullptr, *d_z = nullptr;
+  double *d_z2 = nullptr, *d_B = nullptr, *d_X = nullptr;
+  double *d_Bo = nullptr, *d_Xo = nullptr;             // mixed outer loop
+  double *d_t64 = nullptr, *d_px = nullptr, *d_py = nullptr;  // FP64 pc
+  float *d_x32 = nullptr, *d_y32 = nullptr, *d_w32 = nullptr;
+  float *d_t32 = nullptr, *d_px32 = nullptr, *d_py32 = nullptr;
+  double *d_partials = nullptr, *d_normparts = nullptr;
+  // chunk list
+  int *d_cstart = nullptr, *d_clen = nullptr, *d_csys = nullptr;
+  int *d_sys_ptr = nullptr;
+  KrylovChunks ch{};
+  // per-system state (one allocation of doubles, one of ints)
+  double *d_sd = nullptr;
+  int *d_si = nullptr;
+  KrylovState st{};
+  int *h_pinned = nullptr;      // nactive read-back
+  // graphs: cycle start, one Arnoldi step ([0] FP64 operator, [1] FP32
+  // operator for mixed precision) and cycle end
+  cudaGraphExec_t g_start = nullptr, g_iter[2] = {nullptr, nullptr},
+                  g_end = nullptr;
+  void free_layout() {
+    if (g_start) cudaGraphExecDestroy(g_start);
+    if (g_end) cudaGraphExecDestroy(g_end);
+    for (int i = 0; i < 2; i++) {
+      if (g_iter[i]) cudaGraphExecDestroy(g_iter[i]);
+      g_iter[i] = nullptr;
+    }
+    g_start = g_end = nullptr;
+    dfree(d_W); dfree(d_v); dfree(d_w); dfree(d_z); dfree(d_z2); dfree(d_B);
+    dfree(d_X); dfree(d_Bo); dfree(d_Xo); dfree(d_t64); dfree(d_px);
+    dfree(d_py); dfree(d_x32); dfree(d_y32); dfree(d_w32); dfree(d_t32);
+    dfree(d_px32); dfree(d_py32); dfree(d_partials); dfree(d_normparts);
+    dfree(d_cstart); dfree(d_clen); dfree(d_csys); dfree(d_sys_ptr);
+    dfree(d_sd); dfree(d_si);
+    nrhs = 0;
+    N = 0;
+  }
+  ~tg_ksm() {
+    free_layout();
+    if (h_pinned) cudaFreeHost(h_pinned);
+  }
+};
+
+static inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+namespace tg {
+// M^{-1} on nrhs vectors ld apart (tg_runtime.cu); FP64 buffers for a FP64
+// pc, FP32 for a FP32 pc
+int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
+              void *tmp, void *px, void *py, cudaStream_t s);
+}  // namespace tg

@@ -7,11 +7,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <string>
 #include <vector>
 
-#include "tg_internal.h"
+#include "tg_objects.h"
 
 namespace tg {
 
@@ -25,176 +26,8 @@ int cuda_check(cudaError_t e, const char *what) {
   return TG_ERR_CUDA;
 }
 
-template <typename T>
-static int dalloc(T **p, size_t n) {
-  *p = nullptr;
-  if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-  if (e != cudaSuccess) return cuda_check(e, "cudaMalloc");
-  return 0;
-}
-template <typename T>
-static int upload(T **p, const std::vector<T> &h) {
-  int rc = dalloc(p, h.size());
-  if (rc) return rc;
-  if (!h.empty()) {
-    cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T),
-                               cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_check(e, "cudaMemcpy H2D");
-  }
-  return 0;
-}
-template <typename T>
-static void dfree(T *&p) {
-  if (p) cudaFree(p);
-  p = nullptr;
-}
-
-static int fail(int code, const std::string &msg) {
-  set_error(msg);
-  return code;
-}
-
 }  // namespace tg
 
-using namespace tg;
-
-struct tg_assembler {
-  int refcount = 1;
-  ElemParams ep{};
-  int nnodes = 0, nelem = 0, vpn = 0, npe = 0;
-  std::vector<int> conn_h;
-  std::vector<int> bc_nodes_h, bc_masks_h;
-  std::vector<double> thick_h;
-  std::vector<int> dvnum_h;
-  std::vector<double> pres_h;  // 4 per element (zeros where unloaded)
-  bool has_pres = false;
-  std::vector<int> trac_ptr_h, trac_face_h;
-  std::vector<double> trac_val_h;
-  bool initialized = false;
-  int ndv = 0;
-  // BCSR pattern
-  std::vector<int> rowp_h, cols_h, diag_h;
-  // colouring
-  std::vector<int> color_ptr_h, color_elems_h;
-  // device
-  int *d_conn = nullptr;
-  double *d_xpts = nullptr, *d_thick = nullptr, *d_pres = nullptr;
-  int *d_dvnum = nullptr, *d_trac_ptr = nullptr, *d_trac_face = nullptr;
-  double *d_trac_val = nullptr;
-  int *d_bc_nodes = nullptr, *d_bc_masks = nullptr;
-  int *d_rowp = nullptr, *d_cols = nullptr, *d_diag = nullptr;
-  int *d_color_elems = nullptr;
-  int *d_dv_ptr = nullptr, *d_dv_elems = nullptr;
-  double *d_elem_fail = nullptr, *d_elem_wdet = nullptr;
-  double *d_elem_sed = nullptr, *d_elem_val = nullptr;
-  double *d_partials = nullptr, *d_scalars = nullptr;
-  int npart = 512;
-  KsStats ks{0.0, 1.0, 100.0};
-  bool ks_valid = false;
-
-  int nq() const { return ep.elem_type == TG_ELEM_MITC4 ? 4 : 8; }
-
-  MeshView view() const {
-    MeshView m;
-    m.nnodes = nnodes;
-    m.nelem = nelem;
-    m.vpn = vpn;
-    m.npe = npe;
-    m.conn = d_conn;
-    m.xpts = d_xpts;
-    m.thick = d_thick;
-    m.pres = has_pres ? d_pres : nullptr;
-    m.trac_ptr = trac_val_h.empty() ? nullptr : d_trac_ptr;
-    m.trac_face = d_trac_face;
-    m.trac_val = d_trac_val;
-    m.rowp = d_rowp;
-    m.cols = d_cols;
-    return m;
-  }
-  ColorRange color(int c) const {
-    ColorRange r;
-    r.elem_list = d_color_elems + color_ptr_h[c];
-    r.count = color_ptr_h[c + 1] - color_ptr_h[c];
-    return r;
-  }
-  int ncolors() const { return (int)color_ptr_h.size() - 1; }
-
-  ~tg_assembler() {
-    dfree(d_conn); dfree(d_xpts); dfree(d_thick); dfree(d_pres);
-    dfree(d_dvnum); dfree(d_trac_ptr); dfree(d_trac_face); dfree(d_trac_val);
-    dfree(d_bc_nodes); dfree(d_bc_masks); dfree(d_rowp); dfree(d_cols);
-    dfree(d_diag); dfree(d_color_elems); dfree(d_dv_ptr); dfree(d_dv_elems);
-    dfree(d_elem_fail); dfree(d_elem_wdet); dfree(d_elem_sed);
-    dfree(d_elem_val); dfree(d_partials); dfree(d_scalars);
-  }
-};
-
-struct tg_mat {
-  int refcount = 1;
-  tg_assembler *a = nullptr;
-  int bsize = 0, nrows = 0, nnz = 0;
-  double *d_vals = nullptr;
-  float *d_vals32 = nullptr;
-  ~tg_mat() {
-    dfree(d_vals);
-    dfree(d_vals32);
-  }
-};
-
-struct tg_pc {
-  int refcount = 1;
-  tg_mat *A = nullptr;
-  int type = TG_PC_ILU0, precision = TG_PREC_FP64;
-  IluPlan plan{};
-  int *d_lvl_rows = nullptr, *d_ulvl_rows = nullptr;
-  int *d_upd_ptr = nullptr, *d_upd_tgt = nullptr, *d_upd_src = nullptr;
-  int *d_fail = nullptr;
-  double *d_F = nullptr, *d_tmp = nullptr;
-  float *d_F32 = nullptr, *d_x32 = nullptr, *d_y32 = nullptr,
-        *d_tmp32 = nullptr;
-  double *d_gx = nullptr, *d_gy = nullptr;  // FP64 apply in/out buffers
-  // colour-reordered variant: permuted pattern, value map, permutation and
-  // permuted work vectors
-  int *d_prowp = nullptr, *d_pcols = nullptr, *d_pdiag = nullptr;
-  int *d_valmap = nullptr, *d_perm = nullptr;
-  double *d_px = nullptr, *d_py = nullptr;
-  float *d_px32 = nullptr, *d_py32 = nullptr;
-  int ncolors = 0;
-  // the level-by-level triangular solves replayed as one CUDA graph
-  cudaGraphExec_t apply_exec = nullptr;
-  bool factored = false;
-  ~tg_pc() {
-    if (apply_exec) cudaGraphExecDestroy(apply_exec);
-    dfree(d_lvl_rows); dfree(d_ulvl_rows); dfree(d_upd_ptr);
-    dfree(d_upd_tgt); dfree(d_upd_src); dfree(d_fail); dfree(d_F);
-    dfree(d_tmp); dfree(d_F32); dfree(d_x32); dfree(d_y32); dfree(d_tmp32);
-    dfree(d_gx); dfree(d_gy); dfree(d_prowp); dfree(d_pcols); dfree(d_pdiag);
-    dfree(d_valmap); dfree(d_perm); dfree(d_px); dfree(d_py);
-    dfree(d_px32); dfree(d_py32);
-  }
-};
-
-struct tg_ksm {
-  int refcount = 1;
-  tg_mat *A = nullptr;
-  tg_pc *pc = nullptr;
-  int m = 0, nrestart = 0, mixed = 0;
-  double rtol = 1e-8, atol = 1e-30;
-  size_t n = 0;
-  double *d_W = nullptr, *d_work = nullptr, *d_work2 = nullptr;
-  double *d_h = nullptr, *d_h2 = nullptr, *d_partials = nullptr;
-  double *d_r = nullptr, *d_d = nullptr;
-  float *d_v32 = nullptr, *d_z32 = nullptr, *d_w32 = nullptr;
-  int npart = 4096;
-  ~tg_ksm() {
-    dfree(d_W); dfree(d_work); dfree(d_work2); dfree(d_h); dfree(d_h2);
-    dfree(d_partials); dfree(d_r); dfree(d_d); dfree(d_v32); dfree(d_z32);
-    dfree(d_w32);
-  }
-};
-
-static inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
 extern "C" {
 
@@ -622,10 +455,10 @@ int tg_add_sv_sens(tg_assembler *a, const double *vars, int nfuncs,
   return 0;
 }
 
-static int elem_dv_pass(tg_assembler *a, const double *vars, int func,
-                        double coef, const double *psi, double scale,
-                        double *dfdx, cudaStream_t s) {
-  MeshView m = a->view();
+static int elem_dv_pass_view(tg_assembler *a, const MeshView &m,
+                             const double *vars, int func, double coef,
+                             const double *psi, double scale, double *dfdx,
+                             cudaStream_t s) {
   if (a->ep.elem_type == TG_ELEM_MITC4)
     launch_shell_dv(a->ep, m, vars, func, a->ks, coef, psi, scale,
                     a->d_elem_val, s);
@@ -636,6 +469,12 @@ static int elem_dv_pass(tg_assembler *a, const double *vars, int func,
                     s);
   TG_CUDA(cudaGetLastError());
   return 0;
+}
+static int elem_dv_pass(tg_assembler *a, const double *vars, int func,
+                        double coef, const double *psi, double scale,
+                        double *dfdx, cudaStream_t s) {
+  return elem_dv_pass_view(a, a->view(), vars, func, coef, psi, scale, dfdx,
+                           s);
 }
 
 int tg_add_dv_sens(tg_assembler *a, const double *vars, int nfuncs,
@@ -676,6 +515,100 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
   if (func == TG_FUNC_KS_FAILURE && !a->ks_valid)
     return fail(TG_ERR_STATE, "evaluate the KS function first");
   return elem_dv_pass(a, vars, func, coef, psi, scale, dfdx, S(s));
+}
+
+// ------------------------------------------------------ element segments
+int tg_assembler_set_segments(tg_assembler *a, int nseg,
+                              const int *elem_ptr) {
+  if (!a || nseg <= 0 || !elem_ptr)
+    return fail(TG_ERR_ARG, "tg_assembler_set_segments: bad arguments");
+  if (elem_ptr[0] != 0 || elem_ptr[nseg] != a->nelem)
+    return fail(TG_ERR_ARG,
+                "tg_assembler_set_segments: elem_ptr must span 0..elements");
+  std::vector<int> eseg(a->nelem);
+  for (int g = 0; g < nseg; g++) {
+    if (elem_ptr[g + 1] <= elem_ptr[g])
+      return fail(TG_ERR_ARG,
+                  "tg_assembler_set_segments: empty or unsorted range");
+    for (int e = elem_ptr[g]; e < elem_ptr[g + 1]; e++) eseg[e] = g;
+  }
+  dfree(a->d_elem_seg); dfree(a->d_seg_elem_ptr); dfree(a->d_seg_ks);
+  dfree(a->d_seg_comp);
+  a->seg_elem_ptr_h.assign(elem_ptr, elem_ptr + nseg + 1);
+  int rc = upload(&a->d_elem_seg, eseg);
+  if (!rc) rc = upload(&a->d_seg_elem_ptr, a->seg_elem_ptr_h);
+  if (!rc) rc = dalloc(&a->d_seg_ks, (size_t)nseg);
+  if (!rc) rc = dalloc(&a->d_seg_comp, (size_t)nseg);
+  if (rc) return rc;
+  a->nseg = nseg;
+  a->seg_ks_valid = false;
+  return 0;
+}
+
+int tg_eval_functions_segments(tg_assembler *a, const double *vars, int func,
+                               double ks_weight, double *vals, void *s) {
+  int rc = check_ready(a, "tg_eval_functions_segments");
+  if (rc) return rc;
+  if (!vars || !vals || a->nseg <= 0)
+    return fail(TG_ERR_ARG, "tg_eval_functions_segments: bad arguments");
+  if (func != TG_FUNC_COMPLIANCE && func != TG_FUNC_KS_FAILURE)
+    return fail(TG_ERR_ARG, "tg_eval_functions_segments: unknown function");
+  launch_points(a, vars, S(s));
+  launch_segment_functions(a->d_elem_fail, a->d_elem_wdet, a->d_elem_sed,
+                           a->nq(), a->d_seg_elem_ptr, a->nseg, ks_weight,
+                           a->d_seg_ks, a->d_seg_comp, S(s));
+  std::vector<KsStats> ks(a->nseg);
+  std::vector<double> comp(a->nseg);
+  TG_CUDA(cudaMemcpyAsync(ks.data(), a->d_seg_ks, a->nseg * sizeof(KsStats),
+                          cudaMemcpyDeviceToHost, S(s)));
+  TG_CUDA(cudaMemcpyAsync(comp.data(), a->d_seg_comp,
+                          a->nseg * sizeof(double), cudaMemcpyDeviceToHost,
+                          S(s)));
+  TG_CUDA(cudaStreamSynchronize(S(s)));
+  for (int g = 0; g < a->nseg; g++) {
+    vals[g] = func == TG_FUNC_COMPLIANCE
+                  ? comp[g]
+                  : ks[g].max + std::log(ks[g].sum) / ks_weight;
+    if (!std::isfinite(vals[g]))
+      return fail(TG_ERR_NONFINITE,
+                  "tg_eval_functions_segments: non-finite result");
+  }
+  a->seg_ks_valid = true;
+  return 0;
+}
+
+int tg_add_sv_sens_segments(tg_assembler *a, const double *vars, int func,
+                            double alpha, double *dfdu, void *s) {
+  int rc = check_ready(a, "tg_add_sv_sens_segments");
+  if (rc) return rc;
+  if (!vars || !dfdu || a->nseg <= 0)
+    return fail(TG_ERR_ARG, "tg_add_sv_sens_segments: bad arguments");
+  if (func == TG_FUNC_KS_FAILURE && !a->seg_ks_valid)
+    return fail(TG_ERR_STATE, "evaluate the segment KS functions first");
+  MeshView m = a->view_segments();
+  for (int c = 0; c < a->ncolors(); c++) {
+    if (a->ep.elem_type == TG_ELEM_MITC4)
+      launch_shell_sv_sens(a->ep, m, a->color(c), vars, func, a->ks, alpha,
+                           dfdu, S(s));
+    else
+      launch_hex_sv_sens(a->ep, m, a->color(c), vars, func, a->ks, alpha,
+                         dfdu, S(s));
+  }
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_add_total_derivative_segments(tg_assembler *a, const double *vars,
+                                     int func, double coef, const double *psi,
+                                     double scale, double *dfdx, void *s) {
+  int rc = check_ready(a, "tg_add_total_derivative_segments");
+  if (rc) return rc;
+  if (!vars || !dfdx || a->nseg <= 0)
+    return fail(TG_ERR_ARG, "tg_add_total_derivative_segments: bad arguments");
+  if (func == TG_FUNC_KS_FAILURE && !a->seg_ks_valid)
+    return fail(TG_ERR_STATE, "evaluate the segment KS functions first");
+  return elem_dv_pass_view(a, a->view_segments(), vars, func, coef, psi,
+                           scale, dfdx, S(s));
 }
 
 // ------------------------------------------------------------------ BCSR
@@ -742,6 +675,150 @@ int tg_mat_mult_f32(tg_mat *A, const float *x, float *y, void *s) {
 }
 
 // ------------------------------------------------------- preconditioners
+// Cluster schedule of the two triangular solves (IluClusterView): the
+// connected components of the matrix graph are independent, so components
+// are packed into groups (longest-processing-time first on their level
+// counts) and each group's levels are merged level by level.  The cluster
+// size follows the widest level: about 8 block rows per CTA in FP64 (the
+// FP64 pipe binds), 32 in FP32.
+static int build_cluster_schedule(tg_pc *pc, const std::vector<int> &rowp,
+                                  const std::vector<int> &cols,
+                                  const std::vector<int> &lvl,
+                                  const std::vector<int> &ulvl, int nl,
+                                  int nu) {
+  const int n = (int)rowp.size() - 1;
+  std::vector<int> parent(n);
+  std::iota(parent.begin(), parent.end(), 0);
+  std::function<int(int)> find = [&](int a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  for (int i = 0; i < n; i++)
+    for (int j = rowp[i]; j < rowp[i + 1]; j++) {
+      int a = find(i), b = find(cols[j]);
+      if (a != b) parent[std::max(a, b)] = std::min(a, b);
+    }
+  std::vector<int> comp_of(n), comp_id(n, -1);
+  int ncomp = 0;
+  for (int i = 0; i < n; i++) {
+    int r = find(i);
+    if (comp_id[r] < 0) comp_id[r] = ncomp++;
+    comp_of[i] = comp_id[r];
+  }
+  std::vector<int> cnl(ncomp, 0), cnu(ncomp, 0), crows(ncomp, 0);
+  for (int i = 0; i < n; i++) {
+    const int c = comp_of[i];
+    cnl[c] = std::max(cnl[c], lvl[i] + 1);
+    cnu[c] = std::max(cnu[c], ulvl[i] + 1);
+    crows[c]++;
+  }
+  std::vector<int> wl(nl, 0), wu(nu, 0);
+  for (int i = 0; i < n; i++) {
+    wl[lvl[i]]++;
+    wu[ulvl[i]]++;
+  }
+  const int width = std::max(*std::max_element(wl.begin(), wl.end()),
+                             *std::max_element(wu.begin(), wu.end()));
+  const int per_cta = pc->precision == TG_PREC_FP64 ? 8 : 32;
+  const int max_cs = ilu_cluster_max_size();
+  int cs = 1;
+  // the widest level over all components bounds the per-group width
+  while (cs < max_cs && cs * per_cta < width) cs *= 2;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int ngroups = std::max(1, std::min(ncomp, std::max(1, 2 * sms / cs)));
+  std::vector<int> order(ncomp);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<double> cost(ncomp);
+  for (int c = 0; c < ncomp; c++)
+    cost[c] = cnl[c] + cnu[c] + (double)crows[c] / (cs * 40.0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<double> load(ngroups, 0.0);
+  std::vector<int> grp_of_comp(ncomp);
+  for (int c : order) {
+    int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    grp_of_comp[c] = g;
+    load[g] += cost[c];
+  }
+  std::vector<int> gnl(ngroups, 0), gnu(ngroups, 0);
+  for (int c = 0; c < ncomp; c++) {
+    gnl[grp_of_comp[c]] = std::max(gnl[grp_of_comp[c]], cnl[c]);
+    gnu[grp_of_comp[c]] = std::max(gnu[grp_of_comp[c]], cnu[c]);
+  }
+  // level pointers: group g, level L -> rows of its components at level L
+  auto schedule = [&](const std::vector<int> &lv, const std::vector<int> &gn,
+                      std::vector<int> &grp, std::vector<int> &ptr,
+                      std::vector<int> &rows) {
+    grp.assign(ngroups + 1, 0);
+    for (int g = 0; g < ngroups; g++) grp[g + 1] = grp[g] + gn[g] + 1;
+    std::vector<int> cnt(grp[ngroups], 0);
+    for (int i = 0; i < n; i++) cnt[grp[grp_of_comp[comp_of[i]]] + lv[i]]++;
+    ptr.assign(grp[ngroups], 0);
+    int acc = 0;
+    for (size_t k = 0; k < cnt.size(); k++) {
+      ptr[k] = acc;
+      acc += cnt[k];
+    }
+    rows.assign(n, 0);
+    std::vector<int> fill(ptr);
+    for (int i = 0; i < n; i++)
+      rows[fill[grp[grp_of_comp[comp_of[i]]] + lv[i]]++] = i;
+  };
+  std::vector<int> grp_l, lptr, lrows, grp_u, uptr, urows;
+  schedule(lvl, gnl, grp_l, lptr, lrows);
+  schedule(ulvl, gnu, grp_u, uptr, urows);
+  std::vector<int> diag(n);
+  for (int i = 0; i < n; i++) {
+    int j = rowp[i];
+    while (cols[j] < i) j++;
+    diag[i] = j;
+  }
+  const int maxb = pc->A->bsize == 6 ? 4 : 8;
+  const int dw = 4 * (1 + maxb / 4);  // ints per descriptor
+  std::vector<int> ldesc(dw * (size_t)n, 0), udesc(dw * (size_t)n, 0);
+  for (int k = 0; k < n; k++) {
+    const int i = lrows[k];
+    int *d = &ldesc[(size_t)dw * k];
+    d[0] = i;
+    d[1] = rowp[i];
+    d[2] = diag[i] - rowp[i];
+    d[3] = diag[i];
+    for (int q = 0; q < maxb && q < d[2]; q++) d[4 + q] = cols[rowp[i] + q];
+    const int u = urows[k];
+    int *e = &udesc[(size_t)dw * k];
+    e[0] = u;
+    e[1] = diag[u] + 1;
+    e[2] = rowp[u + 1] - diag[u] - 1;
+    e[3] = diag[u];
+    for (int q = 0; q < maxb && q < e[2]; q++) e[4 + q] = cols[diag[u] + 1 + q];
+  }
+  int max_lp = 0;
+  for (int g = 0; g < ngroups; g++)
+    max_lp = std::max(max_lp, (grp_l[g + 1] - grp_l[g]) +
+                                  (grp_u[g + 1] - grp_u[g]));
+  int rc = 0;
+  if (!rc) rc = upload(&pc->d_cl_grp_lvl, grp_l);
+  if (!rc) rc = upload(&pc->d_cl_lvl_ptr, lptr);
+  if (!rc) rc = upload(&pc->d_cl_rows, ldesc);
+  if (!rc) rc = upload(&pc->d_cl_grp_ulvl, grp_u);
+  if (!rc) rc = upload(&pc->d_cl_ulvl_ptr, uptr);
+  if (!rc) rc = upload(&pc->d_cl_urows, udesc);
+  if (rc) return rc;
+  IluClusterView &v = pc->plan.cluster;
+  v.ngroups = ngroups;
+  v.cs = cs;
+  v.max_lp = max_lp;
+  v.grp_lvl = pc->d_cl_grp_lvl;
+  v.lvl_ptr = pc->d_cl_lvl_ptr;
+  v.ldesc = reinterpret_cast<const int4 *>(pc->d_cl_rows);
+  v.grp_ulvl = pc->d_cl_grp_ulvl;
+  v.ulvl_ptr = pc->d_cl_ulvl_ptr;
+  v.udesc = reinterpret_cast<const int4 *>(pc->d_cl_urows);
+  return 0;
+}
+
 // Level sets of the block lower / upper triangles and the IKJ update list
 // of ILU(0) with the pattern of A (BCSRMat(comm, A, levFill = 0, fill),
 // src/bpmat/BCSRMat.cpp:138).
@@ -798,6 +875,10 @@ static int build_ilu_plan(tg_pc *pc, const std::vector<int> &rowp,
     }
   }
   int rc;
+  if (pc->type == TG_PC_ILU0 && (rc = build_cluster_schedule(pc, rowp, cols,
+                                                             lvl, ulvl, nl,
+                                                             nu)))
+    return rc;
   if ((rc = upload(&pc->d_lvl_rows, lrows))) return rc;
   if ((rc = upload(&pc->d_ulvl_rows, urows))) return rc;
   if ((rc = upload(&pc->d_upd_ptr, upd_ptr))) return rc;
@@ -981,46 +1062,75 @@ int tg_pc_factor(tg_pc *pc, void *s) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace tg {
+
+// Enqueue M^{-1} on nrhs vectors (ld apart): in -> out.  Buffers are FP64
+// for a FP64 pc and FP32 for a FP32 pc; tmp (and px, py for the colour-
+// reordered factor) hold nrhs * ld entries.
+int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
+              void *tmp, void *px, void *py, cudaStream_t s) {
+  const int bs = pc->A->bsize, nr = pc->A->nrows;
+  const bool f64 = pc->precision == TG_PREC_FP64;
+  if (pc->type == TG_PC_BLOCK_JACOBI) {
+    if (f64)
+      launch_block_jacobi_apply(pc->plan, pc->d_F, (const double *)in,
+                                (double *)out, s, nrhs, ld);
+    else
+      launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, (const float *)in,
+                                    (float *)out, s, nrhs, ld);
+  } else if (pc->type == TG_PC_ILU0_COLORED) {
+    if (f64) {
+      launch_permute_gather(nr, bs, pc->d_perm, (const double *)in,
+                            (double *)px, s, nrhs);
+      launch_ilu0_apply(pc->plan, pc->d_F, (const double *)px, (double *)py,
+                        (double *)tmp, s, nrhs, ld);
+      launch_permute_scatter(nr, bs, pc->d_perm, (const double *)py,
+                             (double *)out, s, nrhs);
+    } else {
+      launch_permute_gather_f32(nr, bs, pc->d_perm, (const float *)in,
+                                (float *)px, s, nrhs);
+      launch_ilu0_apply_f32(pc->plan, pc->d_F32, (const float *)px,
+                            (float *)py, (float *)tmp, s, nrhs, ld);
+      launch_permute_scatter_f32(nr, bs, pc->d_perm, (const float *)py,
+                                 (float *)out, s, nrhs);
+    }
+  } else if (f64) {
+    launch_ilu0_apply(pc->plan, pc->d_F, (const double *)in, (double *)out,
+                      (double *)tmp, s, nrhs, ld);
+  } else {
+    launch_ilu0_apply_f32(pc->plan, pc->d_F32, (const float *)in,
+                          (float *)out, (float *)tmp, s, nrhs, ld);
+  }
+  return 0;
+}
+
+}  // namespace tg
+
+extern "C" {
+
 // Apply the factored preconditioner to the pc's internal input buffer
 // (d_gx, or d_x32 in FP32) into its output buffer (d_gy / d_y32).  The ILU(0)
 // level sequence (2 x number of levels launches) is captured once into a
 // CUDA graph and replayed.
 static int pc_apply_internal(tg_pc *pc, cudaStream_t s) {
-  if (pc->type == TG_PC_BLOCK_JACOBI) {
-    if (pc->precision == TG_PREC_FP64)
-      launch_block_jacobi_apply(pc->plan, pc->d_F, pc->d_gx, pc->d_gy, s);
-    else
-      launch_block_jacobi_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
-                                    s);
-    return 0;
-  }
+  const size_t n = (size_t)pc->A->nrows * pc->A->bsize;
+  const bool f64 = pc->precision == TG_PREC_FP64;
+  void *in = f64 ? (void *)pc->d_gx : (void *)pc->d_x32;
+  void *out = f64 ? (void *)pc->d_gy : (void *)pc->d_y32;
+  void *tmp = f64 ? (void *)pc->d_tmp : (void *)pc->d_tmp32;
+  void *px = f64 ? (void *)pc->d_px : (void *)pc->d_px32;
+  void *py = f64 ? (void *)pc->d_py : (void *)pc->d_py32;
+  if (pc->type == TG_PC_BLOCK_JACOBI)
+    return pc_launch(pc, 1, n, in, out, tmp, px, py, s);
   if (!pc->apply_exec) {
     cudaStream_t cs;
     TG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
-      const int bs = pc->A->bsize, nr = pc->A->nrows;
-      if (pc->type == TG_PC_ILU0_COLORED) {
-        if (pc->precision == TG_PREC_FP64) {
-          launch_permute_gather(nr, bs, pc->d_perm, pc->d_gx, pc->d_px, cs);
-          launch_ilu0_apply(pc->plan, pc->d_F, pc->d_px, pc->d_py, pc->d_tmp,
-                            cs);
-          launch_permute_scatter(nr, bs, pc->d_perm, pc->d_py, pc->d_gy, cs);
-        } else {
-          launch_permute_gather_f32(nr, bs, pc->d_perm, pc->d_x32, pc->d_px32,
-                                    cs);
-          launch_ilu0_apply_f32(pc->plan, pc->d_F32, pc->d_px32, pc->d_py32,
-                                pc->d_tmp32, cs);
-          launch_permute_scatter_f32(nr, bs, pc->d_perm, pc->d_py32,
-                                     pc->d_y32, cs);
-        }
-      } else if (pc->precision == TG_PREC_FP64) {
-        launch_ilu0_apply(pc->plan, pc->d_F, pc->d_gx, pc->d_gy, pc->d_tmp, cs);
-      } else {
-        launch_ilu0_apply_f32(pc->plan, pc->d_F32, pc->d_x32, pc->d_y32,
-                              pc->d_tmp32, cs);
-      }
+      pc_launch(pc, 1, n, in, out, tmp, px, py, cs);
       e = cudaStreamEndCapture(cs, &g);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&pc->apply_exec, g, 0);
@@ -1049,266 +1159,6 @@ int tg_pc_apply(tg_pc *pc, const double *x, double *y, void *s) {
     launch_f2d(pc->d_y32, y, n, S(s));
   }
   TG_CUDA(cudaGetLastError());
-  return 0;
-}
-
-// ------------------------------------------------------------------- KSM
-int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
-                  tg_ksm **out) {
-  if (!A || !out || m <= 0 || nrestart < 0)
-    return fail(TG_ERR_ARG, "tg_ksm_create: bad arguments");
-  if (mixed && (!pc || pc->precision != TG_PREC_FP32))
-    return fail(TG_ERR_ARG, "tg_ksm_create: mixed precision needs a FP32 pc");
-  tg_ksm *k = new tg_ksm();
-  k->A = A;
-  A->refcount++;
-  k->pc = pc;
-  if (pc) pc->refcount++;
-  k->m = m;
-  k->nrestart = nrestart;
-  k->mixed = mixed;
-  k->n = (size_t)A->nrows * A->bsize;
-  int rc = dalloc(&k->d_W, k->n * (m + 1));
-  if (!rc) rc = dalloc(&k->d_work, k->n);
-  if (!rc) rc = dalloc(&k->d_work2, k->n);
-  if (!rc) rc = dalloc(&k->d_h, m + 2);
-  if (!rc) rc = dalloc(&k->d_h2, m + 2);
-  if (!rc) rc = dalloc(&k->d_partials, (size_t)k->npart * (m + 2));
-  if (!rc) rc = dalloc(&k->d_r, k->n);
-  if (!rc) rc = dalloc(&k->d_d, k->n);
-  if (!rc && mixed) {
-    rc = dalloc(&k->d_v32, k->n);
-    if (!rc) rc = dalloc(&k->d_z32, k->n);
-    if (!rc) rc = dalloc(&k->d_w32, k->n);
-  }
-  if (rc) {
-    tg_ksm_decref(k);
-    return rc;
-  }
-  *out = k;
-  return 0;
-}
-int tg_ksm_decref(tg_ksm *k) {
-  if (!k) return 0;
-  if (--k->refcount == 0) {
-    tg_pc_decref(k->pc);
-    tg_mat_decref(k->A);
-    delete k;
-  }
-  return 0;
-}
-int tg_ksm_set_tolerances(tg_ksm *k, double rtol, double atol) {
-  if (!k) return fail(TG_ERR_ARG, "NULL ksm");
-  k->rtol = rtol;
-  k->atol = atol;
-  return 0;
-}
-
-// || x ||_2 via the dots kernel (device), returned on the host
-static int dnorm(tg_ksm *k, const double *x, double *out, cudaStream_t s) {
-  launch_dots(x, k->n, 1, x, k->d_partials, k->npart, k->d_h2, s);
-  double v;
-  TG_CUDA(cudaMemcpyAsync(&v, k->d_h2, sizeof(double), cudaMemcpyDeviceToHost,
-                          s));
-  TG_CUDA(cudaStreamSynchronize(s));
-  *out = std::sqrt(v);
-  return 0;
-}
-
-// op(v) = A M^{-1} v, with M^{-1} v kept in z (FP64 or through FP32)
-static int apply_op(tg_ksm *k, const double *v, double *z, double *w,
-                    cudaStream_t s) {
-  tg_mat *A = k->A;
-  if (k->mixed) {
-    tg_pc *pc = k->pc;
-    launch_d2f(v, pc->d_x32, k->n, s);
-    int rc = pc_apply_internal(pc, s);
-    if (rc) return rc;
-    launch_bcsr_mult_f32(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
-                         A->d_vals32, pc->d_y32, k->d_w32, s);
-    launch_f2d(k->d_w32, w, k->n, s);
-    if (z) launch_f2d(pc->d_y32, z, k->n, s);
-    return 0;
-  }
-  const double *src = v;
-  if (k->pc) {
-    int rc = tg_pc_apply(k->pc, v, z, s);
-    if (rc) return rc;
-    src = z;
-  }
-  launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols, A->d_vals,
-                   src, w, s);
-  return 0;
-}
-
-// One restarted-GMRES solve of A x = b (GMRES::solve, src/bpmat/KSM.cpp:785-
-// 970): right preconditioning, Givens rotations, convergence on the
-// estimated residual relative to the first cycle's initial residual.  The
-// Arnoldi step orthogonalises with two classical Gram-Schmidt passes
-// (batched dot products and one update each), which agrees with the
-// reference's modified Gram-Schmidt to rounding.
-static int gmres_core(tg_ksm *k, const double *b, double *x, int zero_guess,
-                      double rtol, double atol, int max_cycles, int *iters,
-                      double *resnorm, cudaStream_t s) {
-  const int m = k->m;
-  const size_t n = k->n;
-  double *W = k->d_W;
-  std::vector<double> H((size_t)(m + 1) * m, 0.0), res(m + 1, 0.0),
-      Qc(m, 0.0), Qs(m, 0.0), h(m + 2), h2(m + 2);
-  double rhs_norm = 0.0, rn = 0.0;
-  int flag = 0, total = 0;
-  for (int count = 0; count < max_cycles; count++) {
-    if (zero_guess && count == 0) {
-      TG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
-      launch_copy(b, W, n, s);
-      int rc = dnorm(k, W, &res[0], s);
-      if (rc) return rc;
-      if (res[0] > 0) launch_scale(1.0 / res[0], W, n, s);
-    } else {
-      launch_bcsr_mult(k->A->bsize, k->A->nrows, k->A->a->d_rowp,
-                       k->A->a->d_cols, k->A->d_vals, x, W, s);
-      launch_axpy(-1.0, b, W, n, s);
-      int rc = dnorm(k, W, &res[0], s);
-      if (rc) return rc;
-      if (res[0] > 0) launch_scale(-1.0 / res[0], W, n, s);
-    }
-    if (count == 0) rhs_norm = res[0];
-    rn = res[0];
-    int niters = 0;
-    if (res[0] < atol || res[0] == 0.0) {
-      flag = 1;
-      break;
-    }
-    for (int i = 0; i < m; i++) {
-      double *Wi = W + n * i, *Wn = W + n * (i + 1);
-      int rc = apply_op(k, Wi, k->d_work, Wn, s);
-      if (rc) return rc;
-      // CGS2: h = W^T w; w -= W h; twice
-      launch_dots(W, n, i + 1, Wn, k->d_partials, k->npart, k->d_h, s);
-      launch_gemv_sub(W, n, i + 1, k->d_h, Wn, n, s);
-      launch_dots(W, n, i + 1, Wn, k->d_partials, k->npart, k->d_h2, s);
-      launch_gemv_sub(W, n, i + 1, k->d_h2, Wn, n, s);
-      TG_CUDA(cudaMemcpyAsync(h.data(), k->d_h, sizeof(double) * (i + 1),
-                              cudaMemcpyDeviceToHost, s));
-      TG_CUDA(cudaMemcpyAsync(h2.data(), k->d_h2, sizeof(double) * (i + 1),
-                              cudaMemcpyDeviceToHost, s));
-      double nrm;
-      rc = dnorm(k, Wn, &nrm, s);  // synchronises
-      if (rc) return rc;
-      double *Hc = &H[(size_t)(m + 1) * i];
-      for (int j = 0; j <= i; j++) Hc[j] = h[j] + h2[j];
-      Hc[i + 1] = nrm;
-      if (nrm > 0) launch_scale(1.0 / nrm, Wn, n, s);
-      for (int j = 0; j < i; j++) {
-        double h1 = Hc[j], hh = Hc[j + 1];
-        Hc[j] = h1 * Qc[j] + hh * Qs[j];
-        Hc[j + 1] = -h1 * Qs[j] + hh * Qc[j];
-      }
-      double h1 = Hc[i], hh = Hc[i + 1];
-      double sq = std::sqrt(h1 * h1 + hh * hh);
-      Qc[i] = h1 / sq;
-      Qs[i] = hh / sq;
-      Hc[i] = h1 * Qc[i] + hh * Qs[i];
-      Hc[i + 1] = -h1 * Qs[i] + hh * Qc[i];
-      h1 = res[i];
-      res[i] = h1 * Qc[i];
-      res[i + 1] = -h1 * Qs[i];
-      niters++;
-      rn = std::fabs(res[i + 1]);
-      if (!std::isfinite(rn))
-        return fail(TG_ERR_NONFINITE, "GMRES: non-finite residual estimate");
-      if (rn < atol || rn < rtol * rhs_norm) {
-        flag = 1;
-        break;
-      }
-    }
-    total += niters;
-    for (int i = niters - 1; i >= 0; i--) {
-      for (int j = i + 1; j < niters; j++)
-        res[i] = res[i] - H[(size_t)(m + 1) * j + i] * res[j];
-      res[i] = res[i] / H[(size_t)(m + 1) * i + i];
-    }
-    // x += M^{-1} (sum_i res_i W_i)
-    TG_CUDA(cudaMemcpyAsync(k->d_h, res.data(), sizeof(double) * niters,
-                            cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemsetAsync(k->d_work, 0, n * sizeof(double), s));
-    launch_scale(-1.0, k->d_h, niters, s);
-    launch_gemv_sub(W, n, niters, k->d_h, k->d_work, n, s);
-    if (k->mixed) {
-      tg_pc *pc = k->pc;
-      launch_d2f(k->d_work, pc->d_x32, n, s);
-      int rc = pc_apply_internal(pc, s);
-      if (rc) return rc;
-      launch_f2d(pc->d_y32, k->d_work2, n, s);
-      launch_axpy(1.0, k->d_work2, x, n, s);
-    } else if (k->pc) {
-      int rc = tg_pc_apply(k->pc, k->d_work, k->d_work2, s);
-      if (rc) return rc;
-      launch_axpy(1.0, k->d_work2, x, n, s);
-    } else {
-      launch_axpy(1.0, k->d_work, x, n, s);
-    }
-    if (flag) break;
-  }
-  if (iters) *iters += total;
-  if (resnorm) *resnorm = rn;
-  TG_CUDA(cudaGetLastError());
-  return flag;
-}
-
-static int ksm_solve_impl(tg_ksm *k, const double *b, double *x,
-                          int zero_guess, int *iters, double *resnorm,
-                          cudaStream_t s);
-
-int tg_ksm_solve(tg_ksm *k, const double *b, double *x, int zero_guess,
-                 int *iters, double *resnorm, void *sv) {
-  if (!k || !b || !x) return fail(TG_ERR_ARG, "tg_ksm_solve: NULL argument");
-  return ksm_solve_impl(k, b, x, zero_guess, iters, resnorm, S(sv));
-}
-
-static int ksm_solve_impl(tg_ksm *k, const double *b, double *x,
-                          int zero_guess, int *iters, double *resnorm,
-                          cudaStream_t s) {
-  if (iters) *iters = 0;
-  if (!k->mixed)
-    return gmres_core(k, b, x, zero_guess, k->rtol, k->atol, k->nrestart + 1,
-                      iters, resnorm, s);
-  // Mixed precision: FP64 iterative refinement on the true residual around
-  // GMRES cycles whose preconditioner and mat-vec run in FP32.
-  const size_t n = k->n;
-  double bnorm;
-  int rc = dnorm(k, b, &bnorm, s);
-  if (rc) return rc;
-  if (zero_guess) TG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
-  // Each inner solve runs restarted GMRES with the FP32 operator to a
-  // relative 1e-6 (or its restart limit); the FP64 true residual then
-  // drives the next correction.  Stops when the true residual meets rtol,
-  // or when a correction no longer reduces it (stagnation).
-  const int max_outer = 20;
-  double rn = bnorm, prev = 0.0;
-  for (int outer = 0; outer <= max_outer; outer++) {
-    // r = b - A x in FP64
-    launch_bcsr_mult(k->A->bsize, k->A->nrows, k->A->a->d_rowp,
-                     k->A->a->d_cols, k->A->d_vals, x, k->d_r, s);
-    launch_scale(-1.0, k->d_r, n, s);
-    launch_axpy(1.0, b, k->d_r, n, s);
-    rc = dnorm(k, k->d_r, &rn, s);
-    if (rc) return rc;
-    if (resnorm) *resnorm = rn;
-    if (!std::isfinite(rn))
-      return fail(TG_ERR_NONFINITE, "mixed GMRES: non-finite true residual");
-    if (rn <= k->rtol * bnorm || rn < k->atol) return 1;
-    if (outer > 0 && rn > 0.5 * prev) return 0;  // stagnated
-    if (outer == max_outer) break;
-    prev = rn;
-    int it = 0;
-    const double inner = std::max(1e-6, 0.1 * k->rtol * bnorm / rn);
-    rc = gmres_core(k, k->d_r, k->d_d, 1, inner, 0.0, k->nrestart + 1, &it,
-                    nullptr, s);
-    if (rc < 0) return rc;
-    if (iters) *iters += it;
-    launch_axpy(1.0, k->d_d, x, n, s);
-  }
   return 0;
 }
 

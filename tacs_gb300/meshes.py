@@ -11,7 +11,7 @@ The node and element orderings follow the reference's own generated meshes:
   src/elements/basis/TACSHexaBasis.cpp:137-146).
 
 Every builder returns a plain dict of numpy arrays (the "problem" record
-understood by :mod:`tacs_gb300.assembler` and by the golden-vector tooling):
+understood by :mod:`tacs_gb300.problem` and by the golden-vector tooling):
 
 ``elem_type`` 0 = MITC4 shell (6 dof/node), 1 = hex8 (3 dof/node);
 ``xpts`` (nnodes*3 f64), ``conn`` (nelem*npe i32), ``thick`` (nelem f64),
@@ -179,3 +179,131 @@ def random_hex_elements(n, seed=0):
     conn = np.arange(8 * n).reshape(n, 8)
     th = 0.1 + 0.9 * rng.random(n)
     return _base(HEX, xpts, conn, th, np.arange(n), (2700.0, 70e9, 0.3, 2.7e8))
+
+
+def concat(probs):
+    """Independent meshes of one element type batched into one problem.
+
+    Nodes and elements are numbered mesh after mesh, so mesh g owns the
+    contiguous ranges ``seg_node_ptr[g]:seg_node_ptr[g+1]`` and
+    ``seg_elem_ptr[g]:seg_elem_ptr[g+1]`` and the Jacobian is block
+    diagonal.  Material constants are those of the first mesh.
+    """
+    et = probs[0]["elem_type"]
+    vpn = 6 if et == SHELL else 3
+    npe = 4 if et == SHELL else 8
+    node_ptr = np.cumsum([0] + [p["nnodes"] for p in probs])
+    elem_ptr = np.cumsum([0] + [p["nelem"] for p in probs])
+    cat = lambda k, dt: np.concatenate(  # noqa: E731
+        [np.asarray(p[k], dt).ravel() for p in probs])
+    conn = np.concatenate([np.asarray(p["conn"]).reshape(-1, npe) + node_ptr[g]
+                           for g, p in enumerate(probs)])
+    out = _base(et, cat("xpts", np.float64).reshape(-1, 3), conn,
+                cat("thick", np.float64),
+                np.concatenate([np.asarray(p["dvnum"]) + elem_ptr[g]
+                                for g, p in enumerate(probs)]),
+                probs[0]["mat"])
+    out["bc_nodes"] = np.concatenate(
+        [np.asarray(p["bc_nodes"], np.int64) + node_ptr[g]
+         for g, p in enumerate(probs)]).astype(np.int32)
+    out["bc_masks"] = cat("bc_masks", np.int32)
+    out["pres_elems"] = np.concatenate(
+        [np.asarray(p["pres_elems"], np.int64) + elem_ptr[g]
+         for g, p in enumerate(probs)]).astype(np.int32)
+    out["pres_vals"] = cat("pres_vals", np.float64)
+    out["force"] = cat("force", np.float64)
+    out["seg_node_ptr"] = node_ptr.astype(np.int32)
+    out["seg_elem_ptr"] = elem_ptr.astype(np.int32)
+    assert len(out["force"]) == vpn * out["nnodes"]
+    return out
+
+
+def clamped_plate(n, L=1.0, thick=None, pressure=1e3, t=0.01):
+    """n x n MITC4 plate on an L x L square, all edges clamped (mask 0x3F),
+    uniform pressure on every element."""
+    p = plate(n, n, Lx=L, Ly=L, t=t, thick=thick)
+    edges = plate_edges(n, n)
+    p["bc_nodes"] = edges.astype(np.int32)
+    p["bc_masks"] = np.full(len(edges), 0x3F, np.int32)
+    p["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    p["pres_vals"] = np.full(4 * n * n, float(pressure))
+    return p
+
+
+def batch_plates(count=48, seed=4, nmin=16, nmax=256, L=1.0, tmin=0.004,
+                 tmax=0.02, pressure=1e3, point_load=1e3):
+    """Independent clamped MITC4 plates of seeded uneven sizes in one problem.
+
+    Plate g is N_g x N_g elements on an L x L square with
+    N_g = round(nmin * (nmax / nmin)**u_g), u_g ~ U[0, 1]; per-element
+    thickness ~ U[tmin, tmax]; all edges clamped; uniform pressure on every
+    element.  Four load cases per plate: the pressure, and three point loads
+    of point_load in the w direction at seeded distinct interior nodes (one
+    per case).  Draws, in order, from numpy.random.default_rng(seed): the
+    count u's, then per plate its thicknesses and its three load nodes.
+    Returns the concatenated problem with ``plate_n`` and ``point_nodes``
+    (count x 3 global node ids) added.
+    """
+    rng = np.random.default_rng(seed)
+    u = rng.random(count)
+    sizes = np.rint(nmin * (nmax / nmin) ** u).astype(int)
+    probs, pts = [], []
+    for n in sizes:
+        th = rng.uniform(tmin, tmax, n * n)
+        p = clamped_plate(int(n), L=L, thick=th, pressure=pressure)
+        ids = np.arange((n + 1) ** 2).reshape(n + 1, n + 1)
+        interior = ids[1:-1, 1:-1].ravel()
+        pts.append(rng.choice(interior, 3, replace=False))
+        probs.append(p)
+    out = concat(probs)
+    out["plate_n"] = sizes
+    out["point_nodes"] = np.stack(
+        [pts[g] + out["seg_node_ptr"][g] for g in range(count)]).astype(
+            np.int64)
+    out["point_load"] = float(point_load)
+    return out
+
+
+def hex_c3(nx=128, ny=128, nz=64, seed=3, traction=-1e4, half=0.1):
+    """Topology-style solid block: nx x ny x nz hex8 on a 2 x 2 x 1 m block,
+    per-element density rho ~ U[0.1, 1] (numpy default_rng(seed)) with SIMP
+    stiffness E rho^3 carried as the element scale t = rho^3; the x = 0 face
+    clamped; a traction (0, 0, traction) Pa on the x = 2 face of the elements
+    whose face centroid lies within |y - 1| <= half, |z - 0.5| <= half.
+    ``rho`` holds the densities."""
+    rng = np.random.default_rng(seed)
+    rho = rng.uniform(0.1, 1.0, nx * ny * nz)
+    p = hex_block(nx, ny, nz, 2.0, 2.0, 1.0, thick=rho ** 3)
+    xyz = p["xpts"].reshape(-1, 3)
+    bcn = np.nonzero(xyz[:, 0] == 0.0)[0].astype(np.int32)
+    p["bc_nodes"], p["bc_masks"] = bcn, np.full(len(bcn), 0x7, np.int32)
+    ijk = p["elem_ijk"]
+    yc = (ijk[:, 1] + 0.5) * 2.0 / ny
+    zc = (ijk[:, 2] + 0.5) * 1.0 / nz
+    te = np.nonzero((ijk[:, 0] == nx - 1) & (np.abs(yc - 1.0) <= half)
+                    & (np.abs(zc - 0.5) <= half))[0]
+    p["trac_elems"] = te.astype(np.int32)
+    p["trac_faces"] = np.full(len(te), 1, np.int32)
+    p["trac_vals"] = np.tile([0.0, 0.0, float(traction)], len(te))
+    p["rho"] = rho
+    return p
+
+
+def cylinder_c5(nc=384, nz=256, R=1.0, L=3.0, t=0.005, axial=1e5,
+                pressure=5e3):
+    """Cylindrical shell, z = 0 ring clamped; at z = L an axial compressive
+    edge load of ``axial`` N/m as nodal forces -axial * 2 pi R / nc (z
+    direction) per ring node; internal pressure on every element (the
+    element normal of this connectivity points outward, +pressure pushes
+    outward).  One design variable (thickness) per element."""
+    p = cylinder(nc, nz, R=R, L=L, t=t)
+    ring0 = np.arange(nc)
+    p["bc_nodes"] = ring0.astype(np.int32)
+    p["bc_masks"] = np.full(nc, 0x3F, np.int32)
+    ne = nc * nz
+    p["pres_elems"] = np.arange(ne, dtype=np.int32)
+    p["pres_vals"] = np.full(4 * ne, float(pressure))
+    f = np.zeros((p["nnodes"], 6))
+    f[nc * nz + np.arange(nc), 2] = -axial * 2.0 * np.pi * R / nc
+    p["force"] = f.ravel()
+    return p

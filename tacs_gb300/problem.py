@@ -119,6 +119,30 @@ class Ksm:
         self.iters, self.resnorm = it.value, rn.value
         return x, flag
 
+    def set_segments(self, row_ptr):
+        """Independent row ranges (block-diagonal matrix): one system each."""
+        rp = np.ascontiguousarray(row_ptr, np.int32)
+        check(_lib.lib().tg_ksm_set_segments(self.handle, len(rp) - 1,
+                                             rp.ctypes.data),
+              "tg_ksm_set_segments")
+        self.nseg = len(rp) - 1
+
+    def solve_multi(self, B, X=None, zero_guess=True):
+        """B: (nrhs, n) device tensor.  Returns X, per-system iterations,
+        flags and residual norms (index rhs * nseg + range)."""
+        B = B.contiguous()
+        nrhs = B.shape[0]
+        X = torch.zeros_like(B) if X is None else X
+        ns = getattr(self, "nseg", 1) * nrhs
+        it = np.zeros(ns, np.int32)
+        fl = np.zeros(ns, np.int32)
+        rn = np.zeros(ns, np.float64)
+        rc = check(_lib.lib().tg_ksm_solve_multi(
+            self.handle, nrhs, _p(B), _p(X), int(zero_guess), it.ctypes.data,
+            fl.ctypes.data, rn.ctypes.data, _stream()), "tg_ksm_solve_multi")
+        self.iters = int(it.max()) if ns else 0
+        return X, it, fl, rn, rc
+
     def __del__(self):
         try:
             _lib.lib().tg_ksm_decref(self.handle)
@@ -260,6 +284,33 @@ class GpuModel:
     def dv_vec(self):
         return torch.zeros(self.ndv, dtype=torch.float64, device="cuda")
 
+    # ------------------------------------------------ element segments
+    def set_segments(self, elem_ptr):
+        ep = np.ascontiguousarray(elem_ptr, np.int32)
+        check(_lib.lib().tg_assembler_set_segments(self.handle, len(ep) - 1,
+                                                   ep.ctypes.data),
+              "tg_assembler_set_segments")
+        self.nseg = len(ep) - 1
+
+    def eval_functions_segments(self, u, func, ks_weight=None):
+        out = np.zeros(self.nseg)
+        ksw = self.ks_weight if ks_weight is None else ks_weight
+        check(_lib.lib().tg_eval_functions_segments(
+            self.handle, _p(u), int(func), ksw, out.ctypes.data, _stream()),
+            "tg_eval_functions_segments")
+        return out
+
+    def add_sv_sens_segments(self, u, func, dfdu, alpha=1.0):
+        check(_lib.lib().tg_add_sv_sens_segments(
+            self.handle, _p(u), int(func), alpha, _p(dfdu), _stream()),
+            "tg_add_sv_sens_segments")
+
+    def add_total_derivative_segments(self, u, func, psi, dfdx, coef=1.0,
+                                      scale=-1.0):
+        check(_lib.lib().tg_add_total_derivative_segments(
+            self.handle, _p(u), int(func), coef, _p(psi), scale, _p(dfdx),
+            _stream()), "tg_add_total_derivative_segments")
+
 
 def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
                    pc_kind=_lib.PC_ILU0, mixed=False, funcs=(0, 1)):
@@ -282,17 +333,77 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     res -= f
     ans, flag = ksm.solve(res)
     u = -ans
-    iters = [ksm.iters]
+    iters, flags = [ksm.iters], [flag]
     fvals = model.eval_functions(u, funcs)
     grads = []
     for k, fn in enumerate(funcs):
         dfdu = model.vec()
         model.add_sv_sens(u, [fn], [dfdu])
         model.apply_bcs(dfdu)
-        psi, _ = ksm.solve(dfdu)
+        psi, fl = ksm.solve(dfdu)
         iters.append(ksm.iters)
+        flags.append(fl)
         g = model.dv_vec()
         model.add_total_derivative(u, fn, psi, g, 1.0, -1.0)
         grads.append(g)
-    return dict(u=u, funcs=fvals, grads=grads, flag=flag, iters=iters,
-                mat=mat, pc=pc, ksm=ksm)
+    return dict(u=u, funcs=fvals, grads=grads, flag=flag, flags=flags,
+                iters=iters, mat=mat, pc=pc, ksm=ksm)
+
+
+def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
+                    pc_kind=_lib.PC_ILU0, mixed=False, func=1):
+    """Independent meshes (element / node segments set from the problem's
+    seg_elem_ptr / seg_node_ptr) under several load cases, solved and
+    differentiated together: one batched GMRES for all forward solves, the
+    per-mesh function of each load case, one batched GMRES for all adjoint
+    solves and the per-element total derivatives.
+
+    loads: (nlc, ndof) device tensor of nodal forces.  Returns the states
+    (nlc, ndof), per-mesh function values (nlc, nseg), per-element gradients
+    (nlc, ndv), per-system iteration counts and convergence flags of both
+    solves (index load_case * nseg + mesh).
+    """
+    prob = model.prob
+    model.set_segments(prob["seg_elem_ptr"])
+    nlc = loads.shape[0]
+    u0 = model.vec()
+    mat = model.new_mat()
+    model.assemble_jacobian(u0, mat, model.vec())
+    prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
+    pc = Pc(mat, pc_kind, prec)
+    pc.factor()
+    ksm = Ksm(mat, pc, m, nrestart, mixed)
+    ksm.set_tolerances(rtol, atol)
+    ksm.set_segments(prob["seg_node_ptr"])
+    F = loads.clone()
+    for lc in range(nlc):
+        model.apply_bcs(F[lc])
+    U, it_f, fl_f, _, _ = ksm.solve_multi(F)
+    fvals = np.zeros((nlc, model.nseg))
+    dfdu = torch.zeros_like(U)
+    for lc in range(nlc):
+        fvals[lc] = model.eval_functions_segments(U[lc], func)
+        model.add_sv_sens_segments(U[lc], func, dfdu[lc])
+        model.apply_bcs(dfdu[lc])
+    Psi, it_a, fl_a, _, _ = ksm.solve_multi(dfdu)
+    grads = torch.zeros(nlc, model.ndv, dtype=torch.float64, device="cuda")
+    for lc in range(nlc):
+        model.eval_functions_segments(U[lc], func)
+        model.add_total_derivative_segments(U[lc], func, Psi[lc], grads[lc],
+                                            1.0, -1.0)
+    return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,
+                iters_adj=it_a, flags_adj=fl_a, psi=Psi)
+
+
+def batch_loads(model):
+    """Load cases of a meshes.batch_plates problem: the consistent pressure
+    load (from the residual at u = 0) and one point load per seeded node."""
+    prob = model.prob
+    pn = np.asarray(prob["point_nodes"])
+    nlc = 1 + pn.shape[1]
+    F = torch.zeros(nlc, model.ndof, dtype=torch.float64, device="cuda")
+    F[0] = -model.assemble_res(model.vec(), apply_bcs=False)
+    idx = torch.as_tensor(model.vpn * pn + 2, device="cuda")
+    for c in range(pn.shape[1]):
+        F[1 + c, idx[:, c]] = float(prob["point_load"])
+    return F

@@ -1,0 +1,115 @@
+"""Batched solves on the GPU: several right-hand sides and several
+independent meshes (element / row segments) in one GMRES, checked against
+one-at-a-time GPU solves (themselves pinned to the reference through
+test_gpu_parity) and, for the multi-RHS case, a host direct solve.
+
+Tolerances: states, function values and gradients 1e-7 relative (the
+solver tolerance times the conditioning of the clamped plates)."""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-7
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import problem
+    return problem
+
+
+def _h(t):
+    return t.detach().cpu().numpy()
+
+
+def _dense(mat):
+    bs, nr = mat.bsize, mat.nrows
+    rowp, cols = _h(mat.rowp), _h(mat.cols)
+    vals = _h(mat.vals).reshape(-1, bs, bs)
+    A = np.zeros((nr * bs, nr * bs))
+    for i in range(nr):
+        for j in range(rowp[i], rowp[i + 1]):
+            c = cols[j]
+            A[i * bs:(i + 1) * bs, c * bs:(c + 1) * bs] = vals[j]
+    return A
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_multi_rhs_matches_direct_solve(gpu, mixed):
+    from tacs_gb300 import _lib, meshes
+    rng = np.random.default_rng(7)
+    p = meshes.clamped_plate(10, thick=rng.uniform(0.004, 0.02, 100))
+    M = gpu.GpuModel(p)
+    mat = M.new_mat()
+    M.assemble_jacobian(M.vec(), mat, M.vec())
+    pc = gpu.Pc(mat, _lib.PC_ILU0,
+                _lib.PREC_FP32 if mixed else _lib.PREC_FP64)
+    pc.factor()
+    ksm = gpu.Ksm(mat, pc, 60, 40, mixed)
+    ksm.set_tolerances(1e-10)
+    B = torch.zeros(3, M.ndof, dtype=torch.float64, device="cuda")
+    B[0] = -M.assemble_res(M.vec(), apply_bcs=False)
+    B[1, 6 * 60 + 2] = 1e3
+    B[2] = torch.as_tensor(rng.standard_normal(M.ndof), device="cuda")
+    for lc in range(3):
+        M.apply_bcs(B[lc])
+    X, it, fl, rn, rc = ksm.solve_multi(B)
+    assert rc == 1 and fl.all()
+    A = _dense(mat)
+    Xd = np.linalg.solve(A, _h(B).T).T
+    for lc in range(3):
+        assert rel(_h(X[lc]), Xd[lc]) < TOL
+    # the same systems one at a time give the same iterates' answer
+    for lc in range(3):
+        x1, f1 = ksm.solve(B[lc].clone())
+        assert f1 == 1
+        assert rel(_h(x1), Xd[lc]) < TOL
+
+
+@pytest.mark.parametrize("pc_kind,mixed", [(0, False), (0, True), (2, False)])
+def test_batched_meshes_match_independent_solves(gpu, pc_kind, mixed):
+    from tacs_gb300 import _lib, meshes
+    bp = meshes.batch_plates(count=3, seed=4, nmin=6, nmax=14)
+    M = gpu.GpuModel(bp)
+    F = gpu.batch_loads(M)
+    # m above the plates' free dof count: no restarted-GMRES stagnation
+    r = gpu.batched_adjoint(M, F, m=1300, nrestart=2, rtol=1e-10,
+                            pc_kind=pc_kind, mixed=mixed,
+                            func=_lib.FUNC_KS_FAILURE)
+    assert r["flags_fwd"].all() and r["flags_adj"].all()
+    nseg = len(bp["plate_n"])
+    nptr, eptr = bp["seg_node_ptr"], bp["seg_elem_ptr"]
+    for g in range(nseg):
+        n = int(bp["plate_n"][g])
+        pg = meshes.clamped_plate(n, thick=bp["thick"][eptr[g]:eptr[g + 1]])
+        Mg = gpu.GpuModel(pg)
+        mat = Mg.new_mat()
+        Mg.assemble_jacobian(Mg.vec(), mat, Mg.vec())
+        pc = gpu.Pc(mat, _lib.PC_ILU0)
+        pc.factor()
+        ksm = gpu.Ksm(mat, pc, 1300, 2)
+        ksm.set_tolerances(1e-12)
+        sl = slice(6 * nptr[g], 6 * nptr[g + 1])
+        for lc in range(F.shape[0]):
+            f = F[lc, sl].clone()
+            Mg.apply_bcs(f)
+            u, fl = ksm.solve(f)
+            assert fl == 1
+            assert rel(_h(r["u"][lc, sl]), _h(u)) < TOL
+            ks = Mg.eval_functions(u, [_lib.FUNC_KS_FAILURE])[0]
+            assert abs(r["funcs"][lc, g] - ks) < TOL * abs(ks)
+            dfdu = Mg.vec()
+            Mg.add_sv_sens(u, [_lib.FUNC_KS_FAILURE], [dfdu])
+            Mg.apply_bcs(dfdu)
+            psi, fl = ksm.solve(dfdu)
+            assert fl == 1
+            gr = Mg.dv_vec()
+            Mg.add_total_derivative(u, _lib.FUNC_KS_FAILURE, psi, gr, 1.0,
+                                    -1.0)
+            assert rel(_h(r["grads"][lc, eptr[g]:eptr[g + 1]]), _h(gr)) < TOL
