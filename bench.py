@@ -107,6 +107,118 @@ def adjoint_section(n, torch, colored=False):
     return out, p
 
 
+def hex_section(torch, steps=5):
+    """Hex8 SIMP block (128 x 128 x 64 elements, 3.24M dof, 28.6M 3x3
+    blocks): residual + Jacobian assembly throughput."""
+    from tacs_gb300 import meshes, problem
+    p = meshes.hex_c3()
+    M = problem.GpuModel(p)
+    u, res, mat = M.vec(), M.vec(), M.new_mat()
+    for _ in range(2):
+        M.assemble_jacobian(u, mat, res)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        M.assemble_jacobian(u, mat, res)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    nnzb = mat.nnz
+    algo = (p["nnodes"] * 6 * 8 + p["nelem"] * (8 * 4 + 8) + p["nnodes"] * 3 * 8
+            + nnzb * 9 * 8)
+    out = {"workload": "hex8 SIMP block 128x128x64 (2x2x1 m), clamped x=0, "
+                       "traction patch on x=2; assembleRes+assembleJacobian",
+           "elements": int(p["nelem"]), "dof": int(M.ndof),
+           "bcsr_blocks": int(nnzb), "ms_per_step": ms,
+           "elements_per_s": p["nelem"] / (ms / 1e3),
+           "hbm_gbs_algorithmic": algo / (ms / 1e3) / 1e9,
+           "algorithmic_bytes": int(algo)}
+    del M, mat, u, res
+    torch.cuda.empty_cache()
+    return out
+
+
+def cylinder_section(torch, nc=384, nz=256):
+    """Cylinder (384 x 256 MITC4, 592k dof): static solve and compliance
+    adjoint gradient, all-FP64 against mixed precision (FP32 factor and
+    mat-vec inside FP64 GMRES with true-residual refinement), both with the
+    colour-reordered ILU(0) (the natural order of a closed cylinder is one
+    sequential chain of 98,688 rows)."""
+    from tacs_gb300 import _lib, meshes, problem
+    c = meshes.cylinder_c5(nc, nz)
+    M = problem.GpuModel(c)
+    out = {"workload": f"cylinder R=1 L=3 t=0.005, {nc}x{nz} MITC4, clamped "
+                       "z=0, axial 1e5 N/m + 5e3 Pa; GMRES(200) to 1e-10, "
+                       "compliance adjoint gradient",
+           "elements": int(c["nelem"]), "dof": int(M.ndof)}
+    g = {}
+    for label, mixed in (("fp64_ilu0_colored", False),
+                         ("mixed_ilu0_colored", True)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = problem.static_adjoint(M, c["force"], 200, 30, 1e-10,
+                                   pc_kind=_lib.PC_ILU0_COLORED, mixed=mixed,
+                                   funcs=(0,))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        g[label] = (r["grads"][0].cpu().numpy(), r["funcs"][0])
+        out[label] = {"s_per_gradient": dt, "iters": r["iters"],
+                      "converged": [int(f) for f in r["flags"]],
+                      "compliance": float(r["funcs"][0])}
+    a, b = g["mixed_ilu0_colored"], g["fp64_ilu0_colored"]
+    out["mixed_ilu0_colored"]["grad_rel_err_vs_fp64"] = float(
+        np.abs(a[0] - b[0]).max() / np.abs(b[0]).max())
+    out["mixed_ilu0_colored"]["compliance_rel_err_vs_fp64"] = float(
+        abs(a[1] - b[1]) / abs(b[1]))
+    out["mixed_speedup_vs_fp64"] = (out["fp64_ilu0_colored"]["s_per_gradient"]
+                                    / out["mixed_ilu0_colored"]["s_per_gradient"])
+    del M
+    torch.cuda.empty_cache()
+    return out
+
+
+def batch_section(torch, count=48, nmax=256, m=100, nrestart=100):
+    """Independent clamped plates of seeded uneven sizes (N log-uniform in
+    [16, nmax]) in one assembler: 4 load cases per plate, one batched
+    GMRES for all forward solves and one for all adjoint solves, KS failure
+    (weight 100, yield 2.7e8) gradient per plate and load case; FP64 and
+    mixed precision."""
+    from tacs_gb300 import _lib, meshes, problem
+    bp = meshes.batch_plates(count=count, nmax=nmax)
+    M = problem.GpuModel(bp)
+    F = problem.batch_loads(M)
+    out = {"workload": f"{count} clamped MITC4 plates N~logU[16,{nmax}] "
+                       "(seed 4), 4 load cases each, KS(100) adjoint "
+                       f"gradients, GMRES({m}) to 1e-10, natural ILU(0)",
+           "plates": count, "elements": int(bp["nelem"]),
+           "dof": int(M.ndof), "systems": 4 * count}
+    g = {}
+    for label, mixed in (("fp64", False), ("mixed", True)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = problem.batched_adjoint(M, F, m=m, nrestart=nrestart, rtol=1e-10,
+                                    mixed=mixed, func=_lib.FUNC_KS_FAILURE)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        g[label] = r["grads"].cpu().numpy()
+        out[label] = {"s_per_batch": dt,
+                      "s_per_gradient": dt / (4 * count),
+                      "max_iters_fwd": int(r["iters_fwd"].max()),
+                      "max_iters_adj": int(r["iters_adj"].max()),
+                      "converged_fwd": int(r["flags_fwd"].sum()),
+                      "converged_adj": int(r["flags_adj"].sum())}
+    d = g["mixed"] - g["fp64"]
+    out["mixed"]["grad_rel_err_vs_fp64"] = float(
+        np.abs(d).max() / np.abs(g["fp64"]).max())
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["s_per_batch"] / \
+        out["mixed"]["s_per_batch"]
+    del M
+    torch.cuda.empty_cache()
+    return out
+
+
 def algorithmic_bytes(p):
     """Assembly traffic a perfect implementation moves once: node coords and
     state read, connectivity + thickness read, residual write, BCSR write."""
@@ -253,6 +365,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--adj-size", type=int, default=64)
+    ap.add_argument("--no-hex", action="store_true")
+    ap.add_argument("--cylinder", action="store_true")
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--batch-nmax", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -368,6 +484,13 @@ def main():
     if rank == 0 and args.adj_size > 0:
         adj, padj = adjoint_section(args.adj_size, torch)
         line["adjoint"] = adj
+    if rank == 0 and not args.no_hex:
+        line["hex_c3"] = hex_section(torch)
+    if rank == 0 and args.cylinder:
+        line["cylinder_c5"] = cylinder_section(torch)
+    if rank == 0 and args.batch > 0:
+        line["batch_c4"] = batch_section(torch, count=args.batch,
+                                         nmax=args.batch_nmax)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p)
         if args.adj_size > 0:

@@ -224,7 +224,10 @@ int tg_pc_apply(tg_pc *pc, const double *x, double *y, void *stream);
 /* GMRES(mat, pc, m, nrestart, isFlexible) (src/bpmat/KSM.h) with
    setTolerances(rtol, atol).  mixed != 0 runs the preconditioner and the
    inner mat-vec in FP32 (pc must be TG_PREC_FP32) inside FP64 GMRES with
-   FP64 Arnoldi and a true-residual iterative-refinement loop. */
+   FP64 Arnoldi and a true-residual iterative-refinement loop; a system
+   whose FP32 mat-vec passes stop paying switches to the FP64 mat-vec with
+   the FP32 preconditioner.  With a TG_PREC_FP32 pc the solver is flexible
+   GMRES (isFlexible = 1: it keeps M^{-1} v_j, m more vectors of memory). */
 int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
                   tg_ksm **out);
 int tg_ksm_decref(tg_ksm *k);

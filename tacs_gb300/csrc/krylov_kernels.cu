@@ -195,6 +195,15 @@ __global__ void kr_scale_store(const double *__restrict__ w, KrylovChunks ch,
   }
 }
 
+// Z_{*it} = z (flexible GMRES keeps every preconditioned basis vector)
+__global__ void kr_store_at(const double *__restrict__ z, double *__restrict__ Z,
+                            size_t ld, const int *__restrict__ it) {
+  const size_t base = (size_t)(*it) * ld;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ld;
+       i += (size_t)gridDim.x * blockDim.x)
+    Z[base + i] = z[i];
+}
+
 // r = b - r (r holds A x on entry)
 __global__ void kr_residual(const double *__restrict__ b, double *__restrict__ r,
                             size_t n) {
@@ -248,9 +257,13 @@ __global__ void kr_cycle_init(KrylovState st) {
                rn0 <= st.rtol[s] * st.rhs_norm[s]) {
       st.converged[s] = 1;
       act = 0;
+    } else if (!*st.first && *st.stall && rn0 > 0.9 * st.rn0prev[s]) {
+      st.done[s] = 1;  // stalled restart
+      act = 0;
     } else {
       act = 1;
     }
+    st.rn0prev[s] = rn0;
     st.active[s] = act;
     st.scale[s] = act ? 1.0 / rn0 : 0.0;
   }
@@ -395,6 +408,10 @@ void launch_kr_scale_store(const double *w, const KrylovChunks &ch,
                            const int *it, double *v, cudaStream_t s) {
   kr_scale_store<<<grid_chunks(ch.nchunks), 256, 0, s>>>(w, ch, scale, W, ld,
                                                           it, v);
+}
+void launch_kr_store_at(const double *z, double *Z, size_t ld, const int *it,
+                        cudaStream_t s) {
+  kr_store_at<<<grid_elems(ld), 256, 0, s>>>(z, Z, ld, it);
 }
 void launch_kr_residual(const double *b, double *r, size_t n, cudaStream_t s) {
   kr_residual<<<grid_elems(n), 256, 0, s>>>(b, r, n);

@@ -249,6 +249,9 @@ struct KrylovState {
   int *first;        // 1 before the first cycle of a solve
   int *it;           // current Arnoldi index
   int *nactive;      // systems still iterating
+  int *stall;        // 1: a restart that gains less than 10% on a
+                     // system's true residual ends that system's solve
+  double *rn0prev;   // nsys true residual at the previous cycle start
 };
 void launch_kr_dots(const double *W, size_t ld, const int *kdev, int kofs,
                     int kmax, const double *w, const KrylovChunks &ch,
@@ -262,6 +265,8 @@ void launch_kr_norm_final(const double *normparts, const KrylovChunks &ch,
 void launch_kr_scale_store(const double *w, const KrylovChunks &ch,
                            const double *scale, double *W, size_t ld,
                            const int *it, double *v, cudaStream_t s);
+void launch_kr_store_at(const double *z, double *Z, size_t ld, const int *it,
+                        cudaStream_t s);
 void launch_kr_residual(const double *b, double *r, size_t n, cudaStream_t s);
 void launch_kr_axpy(const double *x, double *y, size_t n, cudaStream_t s);
 void launch_kr_mask(double *x, const KrylovChunks &ch, const double *scale,

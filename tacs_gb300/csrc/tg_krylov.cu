@@ -9,6 +9,8 @@
 // (systems still iterating) every few steps to stop a cycle early.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -46,6 +48,7 @@ void enqueue_op(tg_ksm *k, int mode, cudaStream_t s) {
     if (k->pc) {
       enqueue_pc(k, k->d_v, k->d_z, s);
       src = k->d_z;
+      if (k->flexible) launch_kr_store_at(k->d_z, k->d_Z, k->N, k->st.it, s);
     }
     launch_bcsr_mult(A->bsize, A->nrows, rowp, cols, A->d_vals, src, k->d_w,
                      s, k->nrhs, k->n);
@@ -53,6 +56,10 @@ void enqueue_op(tg_ksm *k, int mode, cudaStream_t s) {
     launch_d2f(k->d_v, k->d_x32, k->N, s);
     pc_launch(k->pc, k->nrhs, k->n, k->d_x32, k->d_y32, k->d_t32, k->d_px32,
               k->d_py32, s);
+    if (k->flexible) {
+      launch_f2d(k->d_y32, k->d_z, k->N, s);
+      launch_kr_store_at(k->d_z, k->d_Z, k->N, k->st.it, s);
+    }
     launch_bcsr_mult_f32(A->bsize, A->nrows, rowp, cols, A->d_vals32,
                          k->d_y32, k->d_w32, s, k->nrhs, k->n);
     launch_f2d(k->d_w32, k->d_w, k->N, s);
@@ -93,6 +100,12 @@ void enqueue_iter(tg_ksm *k, int mode, cudaStream_t s) {
 void enqueue_end(tg_ksm *k, cudaStream_t s) {
   const size_t N = k->N;
   launch_kr_solve_y(k->st, s);
+  if (k->flexible) {
+    // x += Z y with the stored preconditioned vectors (flexible GMRES)
+    launch_kr_gemv_sub(k->d_Z, N, nullptr, k->m, k->m, k->st.res, k->m + 1,
+                       k->ch, k->d_X, nullptr, s);
+    return;
+  }
   cudaMemsetAsync(k->d_z, 0, N * sizeof(double), s);
   launch_kr_gemv_sub(k->d_W, N, nullptr, k->m, k->m, k->st.res, k->m + 1,
                      k->ch, k->d_z, nullptr, s);
@@ -154,6 +167,7 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   const int nchunks = (int)cstart.size();
   int rc = 0;
   if (!rc) rc = dalloc(&k->d_W, N * (m + 1));
+  if (!rc && k->flexible) rc = dalloc(&k->d_Z, N * m);
   if (!rc) rc = dalloc(&k->d_v, N);
   if (!rc) rc = dalloc(&k->d_w, N);
   if (!rc) rc = dalloc(&k->d_z, N);
@@ -184,8 +198,8 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   if (!rc) rc = upload(&k->d_sys_ptr, sys_ptr);
   // per-system state
   const size_t S1 = (size_t)nsys;
-  const size_t nd = S1 * ((size_t)(m + 1) * m + 2 * m + 3 * (m + 1) + 6);
-  const size_t ni = S1 * 6 + 3;
+  const size_t nd = S1 * ((size_t)(m + 1) * m + 2 * m + 3 * (m + 1) + 7);
+  const size_t ni = S1 * 6 + 4;
   if (!rc) rc = dalloc(&k->d_sd, nd);
   if (!rc) rc = dalloc(&k->d_si, ni);
   if (!rc && !k->h_pinned) {
@@ -196,6 +210,10 @@ int ensure_layout(tg_ksm *k, int nrhs) {
     k->free_layout();
     return rc;
   }
+  // every basis slot starts at zero: the end-of-cycle update multiplies
+  // slots past a system's step count by zero coefficients
+  cudaMemset(k->d_W, 0, N * (m + 1) * sizeof(double));
+  if (k->d_Z) cudaMemset(k->d_Z, 0, N * m * sizeof(double));
   cudaMemset(k->d_sd, 0, nd * sizeof(double));
   cudaMemset(k->d_si, 0, ni * sizeof(int));
   k->nrhs = nrhs;
@@ -219,6 +237,7 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   st.rhs_norm = p; p += S1;
   st.rn = p; p += S1;
   st.rtol = p; p += S1;
+  st.rn0prev = p; p += S1;
   p += S1;
   int *q = k->d_si;
   st.active = q; q += S1;
@@ -230,6 +249,7 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   st.first = q; q += 1;
   st.it = q; q += 1;
   st.nactive = q; q += 1;
+  st.stall = q; q += 1;
   // graphs
   rc = capture(&k->g_start, [&](cudaStream_t cs) { enqueue_start(k, cs); });
   if (!rc)
@@ -249,7 +269,7 @@ int set_rtols(tg_ksm *k, const std::vector<double> &v, cudaStream_t s) {
 }
 
 // Restarted GMRES on d_B -> d_X (state reset except done[]).
-int run_cycles(tg_ksm *k, int mode, cudaStream_t s) {
+int run_cycles(tg_ksm *k, int mode, int stall, cudaStream_t s) {
   const size_t S1 = (size_t)k->nsys;
   KrylovState &st = k->st;
   TG_CUDA(cudaMemsetAsync(st.converged, 0, S1 * sizeof(int), s));
@@ -258,6 +278,8 @@ int run_cycles(tg_ksm *k, int mode, cudaStream_t s) {
   const int one = 1;
   TG_CUDA(cudaMemcpyAsync(st.first, &one, sizeof(int), cudaMemcpyHostToDevice,
                           s));
+  TG_CUDA(cudaMemcpyAsync(st.stall, &stall, sizeof(int),
+                          cudaMemcpyHostToDevice, s));
   volatile int *hp = k->h_pinned;
   for (int cycle = 0; cycle <= k->nrestart; cycle++) {
     TG_CUDA(cudaGraphLaunch(k->g_start, s));
@@ -318,7 +340,7 @@ int fetch(std::vector<T> &h, const T *d, size_t n, cudaStream_t s) {
 // mat-vec with FP64 Arnoldi to a modest relative tolerance, and a system has
 // converged when its FP64 true residual meets rtol ||r0||.  Each pass
 // contracts the true residual by about cond(A) x the FP32 rounding of A;
-// when a pass gains less than 100x for some system, the remaining passes
+// when a pass gains less than 1e4x for some system, the remaining passes
 // apply A in FP64 (the preconditioner stays FP32) and solve to the full
 // tolerance, and a system stops when a pass no longer halves its residual.
 int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
@@ -338,6 +360,8 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
   int rc;
   const int max_outer = mode == 0 ? 2 : 30;
   const int mode_in = mode;
+  // TG_KSM_TRACE=1 prints each refinement pass's relative true residuals
+  const bool trace = std::getenv("TG_KSM_TRACE") != nullptr;
   for (int outer = 0; outer <= max_outer; outer++) {
     launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
                      A->d_vals, k->d_Xo, k->d_B, s, k->nrhs, k->n);
@@ -346,6 +370,27 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
     if (outer == 0) r0 = rn;
     int left = 0;
     bool to_fp64 = false;
+    // a correction that made a system's true residual larger is taken back
+    if (outer > 0) {
+      bool any = false;
+      for (int i = 0; i < ns; i++) {
+        mask[i] = (!done[i] && std::isfinite(rn[i]) && rn[i] > prev[i])
+                      ? 1.0 : 0.0;
+        any |= mask[i] != 0.0;
+      }
+      if (any) {
+        TG_CUDA(cudaMemcpyAsync(k->st.scale, mask.data(), ns * sizeof(double),
+                                cudaMemcpyHostToDevice, s));
+        launch_kr_mask(k->d_X, k->ch, k->st.scale, s);
+        launch_axpy(-1.0, k->d_X, k->d_Xo, N, s);
+        for (int i = 0; i < ns; i++)
+          if (mask[i] != 0.0) {
+            rn[i] = prev[i];
+            if (mode == 1) to_fp64 = true;
+            else done[i] = 1;
+          }
+      }
+    }
     for (int i = 0; i < ns; i++) {
       if (!std::isfinite(rn[i]))
         return fail(TG_ERR_NONFINITE, "GMRES: non-finite true residual");
@@ -354,9 +399,9 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
       if (met) {
         done[i] = 1;
         conv[i] = 1;
-      } else if (mode == 1 && outer > 0 && rn[i] > 1e-2 * prev[i]) {
+      } else if (mode == 1 && outer > 0 && rn[i] >= 1e-4 * prev[i]) {
         // a pass solved to 1e-6 with the FP32 mat-vec gained less than
-        // 100x: cond(A) x FP32 rounding is not small for this system, so
+        // 1e4x: cond(A) x FP32 rounding is not small for this system, so
         // the remaining passes keep the FP32 preconditioner but apply A in
         // FP64
         to_fp64 = true;
@@ -367,6 +412,13 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
       }
     }
     if (to_fp64) mode = 0;
+    if (trace) {
+      std::fprintf(stderr, "[tg_ksm] pass %d mode %d:", outer, mode);
+      for (int i = 0; i < ns; i++)
+        std::fprintf(stderr, " %d:%.3e%s", i, rn[i] / r0[i],
+                     done[i] ? (conv[i] ? "c" : "x") : "");
+      std::fprintf(stderr, "\n");
+    }
     for (int i = 0; i < ns; i++) {
       if (!done[i]) {
         left++;
@@ -393,7 +445,11 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                             cudaMemcpyHostToDevice, s));
     if ((rc = set_rtols(k, rt, s))) return rc;
     TG_CUDA(cudaMemsetAsync(k->d_X, 0, N * sizeof(double), s));
-    if ((rc = run_cycles(k, mode, s))) return rc;
+    // the first FP64 pass is the reference's GMRES (it restarts until its
+    // cycle limit); refinement passes and FP32 passes stop a system whose
+    // restarts stall
+    if ((rc = run_cycles(k, mode, !(mode_in == 0 && outer == 0), s)))
+      return rc;
     if ((rc = fetch(it, k->st.iters, ns, s))) return rc;
     std::vector<int> err;
     if ((rc = fetch(err, k->st.err, ns, s))) return rc;
@@ -440,6 +496,10 @@ int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
   k->mixed = mixed;
   k->n = (size_t)A->nrows * A->bsize;
   k->seg_rows = {0, A->nrows};
+  // an FP32 preconditioner is applied with FP32 rounding that differs
+  // between the Arnoldi vectors and their combination, so its solves keep
+  // every preconditioned vector (flexible GMRES) and update x from those
+  k->flexible = pc && pc->precision == TG_PREC_FP32;
   *out = k;
   return 0;
 }

@@ -199,7 +199,9 @@ struct tg_ksm {
   size_t N = 0;                 // nrhs * n
   int nsys = 0;
   // multivector buffers
+  int flexible = 0;             // keep Z_j = M^{-1} v_j (FP32 preconditioner)
   double *d_W = nullptr, *d_v = nullptr, *d_w = nullptr, *d_z = nullptr;
+  double *d_Z = nullptr;
   double *d_z2 = nullptr, *d_B = nullptr, *d_X = nullptr;
   double *d_Bo = nullptr, *d_Xo = nullptr;             // mixed outer loop
   double *d_t64 = nullptr, *d_px = nullptr, *d_py = nullptr;  // FP64 pc
@@ -228,6 +230,7 @@ struct tg_ksm {
     }
     g_start = g_end = nullptr;
     dfree(d_W); dfree(d_v); dfree(d_w); dfree(d_z); dfree(d_z2); dfree(d_B);
+    dfree(d_Z);
     dfree(d_X); dfree(d_Bo); dfree(d_Xo); dfree(d_t64); dfree(d_px);
     dfree(d_py); dfree(d_x32); dfree(d_y32); dfree(d_w32); dfree(d_t32);
     dfree(d_px32); dfree(d_py32); dfree(d_partials); dfree(d_normparts);

@@ -218,6 +218,12 @@ class GpuModel:
         return torch.as_tensor(np.asarray(values, np.float64),
                                device="cuda").clone()
 
+    def set_nodes(self, xpts):
+        """Node coordinates (3 per node, device tensor)."""
+        self.xpts = xpts
+        check(_lib.lib().tg_assembler_set_nodes(self.handle, _p(xpts),
+                                                _stream()), "set_nodes")
+
     def set_design_vars(self, dvs):
         check(_lib.lib().tg_assembler_set_design_vars(self.handle, _p(dvs),
                                                       _stream()), "set_dvs")
@@ -378,21 +384,22 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     F = loads.clone()
     for lc in range(nlc):
         model.apply_bcs(F[lc])
-    U, it_f, fl_f, _, _ = ksm.solve_multi(F)
+    U, it_f, fl_f, rn_f, _ = ksm.solve_multi(F)
     fvals = np.zeros((nlc, model.nseg))
     dfdu = torch.zeros_like(U)
     for lc in range(nlc):
         fvals[lc] = model.eval_functions_segments(U[lc], func)
         model.add_sv_sens_segments(U[lc], func, dfdu[lc])
         model.apply_bcs(dfdu[lc])
-    Psi, it_a, fl_a, _, _ = ksm.solve_multi(dfdu)
+    Psi, it_a, fl_a, rn_a, _ = ksm.solve_multi(dfdu)
     grads = torch.zeros(nlc, model.ndv, dtype=torch.float64, device="cuda")
     for lc in range(nlc):
         model.eval_functions_segments(U[lc], func)
         model.add_total_derivative_segments(U[lc], func, Psi[lc], grads[lc],
                                             1.0, -1.0)
     return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,
-                iters_adj=it_a, flags_adj=fl_a, psi=Psi)
+                iters_adj=it_a, flags_adj=fl_a, psi=Psi, resnorm_fwd=rn_f,
+                resnorm_adj=rn_a)
 
 
 def batch_loads(model):

@@ -40,11 +40,16 @@ def _dense(mat):
     return A
 
 
+# An FP32 ILU(0) factor is only a preconditioner where its rounding is not
+# amplified: the natural-order block factors of thin shells (thickness well
+# below the element size) amplify last-bit changes by up to ~1e9 (the
+# reference's own FP64 factors, see test_gpu_parity), so the FP32 cases
+# below use plates with thickness comparable to the element size.
 @pytest.mark.parametrize("mixed", [False, True])
 def test_multi_rhs_matches_direct_solve(gpu, mixed):
     from tacs_gb300 import _lib, meshes
     rng = np.random.default_rng(7)
-    p = meshes.clamped_plate(10, thick=rng.uniform(0.004, 0.02, 100))
+    p = meshes.clamped_plate(10, thick=rng.uniform(0.06, 0.12, 100))
     M = gpu.GpuModel(p)
     mat = M.new_mat()
     M.assemble_jacobian(M.vec(), mat, M.vec())
@@ -72,17 +77,24 @@ def test_multi_rhs_matches_direct_solve(gpu, mixed):
         assert rel(_h(x1), Xd[lc]) < TOL
 
 
-@pytest.mark.parametrize("pc_kind,mixed", [(0, False), (0, True), (2, False)])
-def test_batched_meshes_match_independent_solves(gpu, pc_kind, mixed):
+@pytest.mark.parametrize("pc_kind,mixed,tmin,tmax", [
+    (0, False, 0.004, 0.02), (2, False, 0.004, 0.02), (2, True, 0.004, 0.02),
+    (0, True, 0.05, 0.1)])
+def test_batched_meshes_match_independent_solves(gpu, pc_kind, mixed, tmin,
+                                                 tmax):
     from tacs_gb300 import _lib, meshes
-    bp = meshes.batch_plates(count=3, seed=4, nmin=6, nmax=14)
+    bp = meshes.batch_plates(count=3, seed=4, nmin=12, nmax=20, tmin=tmin,
+                             tmax=tmax)
     M = gpu.GpuModel(bp)
     F = gpu.batch_loads(M)
     # m above the plates' free dof count: no restarted-GMRES stagnation
-    r = gpu.batched_adjoint(M, F, m=1300, nrestart=2, rtol=1e-10,
+    r = gpu.batched_adjoint(M, F, m=1500, nrestart=2, rtol=1e-10,
                             pc_kind=pc_kind, mixed=mixed,
                             func=_lib.FUNC_KS_FAILURE)
-    assert r["flags_fwd"].all() and r["flags_adj"].all()
+    assert r["flags_fwd"].all(), (r["flags_fwd"], r["iters_fwd"],
+                                  r["resnorm_fwd"])
+    assert r["flags_adj"].all(), (r["flags_adj"], r["iters_adj"],
+                                  r["resnorm_adj"])
     nseg = len(bp["plate_n"])
     nptr, eptr = bp["seg_node_ptr"], bp["seg_elem_ptr"]
     for g in range(nseg):
@@ -93,7 +105,7 @@ def test_batched_meshes_match_independent_solves(gpu, pc_kind, mixed):
         Mg.assemble_jacobian(Mg.vec(), mat, Mg.vec())
         pc = gpu.Pc(mat, _lib.PC_ILU0)
         pc.factor()
-        ksm = gpu.Ksm(mat, pc, 1300, 2)
+        ksm = gpu.Ksm(mat, pc, 1500, 2)
         ksm.set_tolerances(1e-12)
         sl = slice(6 * nptr[g], 6 * nptr[g + 1])
         for lc in range(F.shape[0]):
