@@ -95,7 +95,8 @@ def adjoint_section(n, torch, colored=False):
             dt = time.perf_counter() - t0
         grads[label] = [g.cpu().numpy() for g in r["grads"]]
         out[label] = {"s_per_gradient": dt, "iters": r["iters"],
-                      "converged": [int(f) for f in r["flags"]]}
+                      "converged": [int(f) for f in r["flags"]],
+                      "ilu_schedule": r["pc"].schedule()}
     ref = grads["fp64_ilu0_natural"]
     for label in [r[0] for r in runs[1:]]:
         out[label]["grad_rel_err_vs_fp64_natural"] = [
@@ -179,7 +180,7 @@ def cylinder_section(torch, nc=384, nz=256):
     return out
 
 
-def batch_section(torch, count=48, nmax=256, m=100, nrestart=100):
+def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0):
     """Independent clamped plates of seeded uneven sizes (N log-uniform in
     [16, nmax]) in one assembler: 4 load cases per plate, one batched
     GMRES for all forward solves and one for all adjoint solves, KS failure
@@ -191,7 +192,9 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100):
     F = problem.batch_loads(M)
     out = {"workload": f"{count} clamped MITC4 plates N~logU[16,{nmax}] "
                        "(seed 4), 4 load cases each, KS(100) adjoint "
-                       f"gradients, GMRES({m}) to 1e-10, natural ILU(0)",
+                       f"gradients, GMRES({m}) to 1e-10, "
+                       + ("natural" if pc_kind == 0 else "colour-reordered")
+                       + " ILU(0)",
            "plates": count, "elements": int(bp["nelem"]),
            "dof": int(M.ndof), "systems": 4 * count}
     g = {}
@@ -199,7 +202,8 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r = problem.batched_adjoint(M, F, m=m, nrestart=nrestart, rtol=1e-10,
-                                    mixed=mixed, func=_lib.FUNC_KS_FAILURE)
+                                    pc_kind=pc_kind, mixed=mixed,
+                                    func=_lib.FUNC_KS_FAILURE)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         g[label] = r["grads"].cpu().numpy()
@@ -217,6 +221,17 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100):
     del M
     torch.cuda.empty_cache()
     return out
+
+
+def replica_time(ms, dist=None, device=None):
+    """Replicas only: every rank runs the whole workload on its own GPU;
+    the job's step time is the slowest rank's (max over ranks)."""
+    if dist is None or not dist.is_initialized():
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def algorithmic_bytes(p):
@@ -366,9 +381,10 @@ def main():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--adj-size", type=int, default=64)
     ap.add_argument("--no-hex", action="store_true")
-    ap.add_argument("--cylinder", action="store_true")
-    ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--batch-nmax", type=int, default=256)
+    ap.add_argument("--no-cylinder", action="store_true")
+    ap.add_argument("--batch", type=int, default=12)
+    ap.add_argument("--batch-nmax", type=int, default=96)
+    ap.add_argument("--batch-pc", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -422,10 +438,7 @@ def main():
     torch.cuda.synchronize()
     ms_zero = z0.elapsed_time(z1) / args.steps
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replica_time(ms, dist, "cuda")
 
     # end to end through the public API with host buffers: design variables
     # and state in (pinned), residual out.
@@ -486,11 +499,12 @@ def main():
         line["adjoint"] = adj
     if rank == 0 and not args.no_hex:
         line["hex_c3"] = hex_section(torch)
-    if rank == 0 and args.cylinder:
+    if rank == 0 and not args.no_cylinder:
         line["cylinder_c5"] = cylinder_section(torch)
     if rank == 0 and args.batch > 0:
         line["batch_c4"] = batch_section(torch, count=args.batch,
-                                         nmax=args.batch_nmax)
+                                         nmax=args.batch_nmax,
+                                         pc_kind=args.batch_pc)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p)
         if args.adj_size > 0:

@@ -219,6 +219,14 @@ int tg_pc_factor(tg_pc *pc, void *stream);
 /* TACSAdditiveSchwarz::applyFactor -> BCSRMat::applyFactor
    (src/bpmat/BCSRMat.cpp:1326): y = (LU)^{-1} x. */
 int tg_pc_apply(tg_pc *pc, const double *x, double *y, void *stream);
+/* No reference counterpart.  The schedule of the natural-order ILU(0)
+   triangular solves: thread-block cluster size and number of clusters (0
+   when the level kernels are used), lower + upper level count, and the
+   autotuner's measured time per solve pair in ms for cluster sizes
+   1, 2, 4, 8, 16 (tuned_ms, 5 entries, 0 where not measured; may be
+   NULL).  The autotuner runs once, at the first tg_pc_factor. */
+int tg_pc_get_schedule(tg_pc *pc, int *cluster_size, int *groups,
+                       int *levels, double *tuned_ms);
 
 /* ------------------------------------------------------------------- KSM */
 /* GMRES(mat, pc, m, nrestart, isFlexible) (src/bpmat/KSM.h) with

@@ -1,15 +1,13 @@
 // Trilinear hex8 elasticity kernels (TACSElement3D with
 // TACSLinearElasticity3D(TACS_LINEAR_STRAIN) and TACSLinearHexaBasis) for
-// sm_103a.  One warp per element: 8 lanes build the Gauss-point Jacobians,
-// all lanes form the physical shape gradients, then the 36 upper 3x3 node
-// blocks of K = sum_q detXd_q B^T (t C) B are formed in the closed
-// isotropic form
-//   K_ab[i][i] = c0 Na_i Nb_i + G sum_{k!=i} Na_k Nb_k
-//   K_ab[i][j] = c1 Na_i Nb_j + G Na_j Nb_i           (i != j)
-// (the same product B^T C B as TACSElementBasis::addWeakMatrix with the
-// isotropic TACSMaterialProperties::evalTangentStiffness3D,
+// sm_103a.  The 36 upper 3x3 node blocks of K = sum_q detXd_q B^T (t C) B
+// are formed in the closed isotropic form (the same product B^T C B as
+// TACSElementBasis::addWeakMatrix with the isotropic
+// TACSMaterialProperties::evalTangentStiffness3D,
 // src/constitutive/TACSMaterialProperties.cpp:270-293) and added into the
-// 3x3 BCSR blocks; colouring makes the scatter atomic-free.
+// 3x3 BCSR blocks; colouring makes the scatter atomic-free.  Assembly runs
+// in 8-lane teams; the point-quantity and sensitivity kernels use one warp
+// per element.
 #include <cmath>
 
 #include "tg_internal.h"
@@ -191,112 +189,222 @@ __device__ __forceinline__ double hex_bts(const HexSmem &S, int q, int mm,
   return g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
 }
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    hex_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
-                        const double *__restrict__ vars, double lambda,
-                        double *__restrict__ res, double *__restrict__ mat,
-                        int transpose) {
-  __shared__ HexSmem smem[WARPS];
-  HexSmem &S = smem[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
-  const int nw = gridDim.x * WARPS;
-  const HexC c = hex_c(ep);
-  (void)transpose;  // K is symmetric by construction (mirrored blocks)
-
-  for (int idx = gw; idx < cr.count; idx += nw) {
-    const int e = cr.elem_list[idx];
-    hex_load(S, m, e, vars, nullptr, lane);
-    if (mat)
-      for (int k = lane; k < 64; k += 32)
-        S.slot[k] = find_slot(m.rowp, m.cols, S.nodes[k >> 3], S.nodes[k & 7]);
-    hex_geometry(S, lane);
-
-    if (res) {
-      if (lane < 8) {
-        double ev[6], s[6];
-        hex_strain(S, lane, S.u, ev);
-        hex_Ce(c, ev, s);
-        for (int k = 0; k < 6; k++) S.g[lane][k] = s[k] * S.t;
-      }
-      __syncwarp();
-      if (lane < 24) {
-        const int mm = lane / 3, i = lane % 3;
-        double rk = 0.0;
-        for (int q = 0; q < 8; q++) rk += S.det[q] * hex_bts(S, q, mm, i, S.g[q]);
-        // TACSTraction3D::addResidual (TACSTraction3D.cpp:87-125) with
-        // TACSElementBasis::getFaceNormal (TACSElementBasis.cpp:37-63)
-        if (m.trac_ptr) {
-          double aux = 0.0;
-          for (int tk = m.trac_ptr[e]; tk < m.trac_ptr[e + 1]; tk++) {
-            const int face = m.trac_face[tk];
-            const double tr = m.trac_val[3 * tk + i];
-            double t1d[3], t2d[3];
-            // face tangents (TACSHexaBasis.cpp:21-70)
-            const int f2 = face >> 1;
-            for (int n = 0; n < 4; n++) {
-              double a = gauss2(n & 1), b = gauss2(n >> 1);
-              double cc = -1.0 + 2.0 * (face & 1);
-              double pt[3];
-              if (f2 == 0) { pt[0] = cc; pt[1] = a; pt[2] = b; }
-              else if (f2 == 1) { pt[0] = a; pt[1] = cc; pt[2] = b; }
-              else { pt[0] = a; pt[1] = b; pt[2] = cc; }
-              double N[8], Nxi[24], Xd[9];
-              hex_shape(pt, N, Nxi);
-              for (int ii = 0; ii < 3; ii++)
-                for (int jj = 0; jj < 3; jj++) {
-                  double v = 0.0;
-                  for (int q = 0; q < 8; q++) v += Nxi[3 * q + jj] * S.X[3 * q + ii];
-                  Xd[3 * ii + jj] = v;
-                }
-              int ta, tb;  // parametric directions spanning the face
-              if (f2 == 0) { ta = 2; tb = 1; }
-              else if (f2 == 1) { ta = 0; tb = 2; }
-              else { ta = 1; tb = 0; }
-              if (face == 1) { ta = 1; tb = 2; }
-              if (face == 3) { ta = 2; tb = 0; }
-              if (face == 5) { ta = 0; tb = 1; }
-              for (int ii = 0; ii < 3; ii++) {
-                t1d[ii] = Xd[3 * ii + ta];
-                t2d[ii] = Xd[3 * ii + tb];
-              }
-              double nr[3] = {t1d[1] * t2d[2] - t1d[2] * t2d[1],
-                              t1d[2] * t2d[0] - t1d[0] * t2d[2],
-                              t1d[0] * t2d[1] - t1d[1] * t2d[0]};
-              double area = sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
-              aux += area * N[mm] * -tr;
-            }
-          }
-          rk += lambda * aux;
+// Face-traction residual of one element for node a, direction i
+// (TACSTraction3D::addResidual, TACSTraction3D.cpp:87-125, with
+// TACSElementBasis::getFaceNormal, TACSElementBasis.cpp:37-63).
+__device__ double hex_traction(const MeshView &m, int e, const double *X,
+                               int a, int i) {
+  double aux = 0.0;
+  for (int tk = m.trac_ptr[e]; tk < m.trac_ptr[e + 1]; tk++) {
+    const int face = m.trac_face[tk];
+    const double tr = m.trac_val[3 * tk + i];
+    const int f2 = face >> 1;
+    for (int n = 0; n < 4; n++) {
+      const double u = gauss2(n & 1), v = gauss2(n >> 1);
+      const double cc = -1.0 + 2.0 * (face & 1);
+      double pt[3];
+      if (f2 == 0) { pt[0] = cc; pt[1] = u; pt[2] = v; }
+      else if (f2 == 1) { pt[0] = u; pt[1] = cc; pt[2] = v; }
+      else { pt[0] = u; pt[1] = v; pt[2] = cc; }
+      double N[8], Nxi[24], Xd[9];
+      hex_shape(pt, N, Nxi);
+      for (int ii = 0; ii < 3; ii++)
+        for (int jj = 0; jj < 3; jj++) {
+          double s = 0.0;
+          for (int q = 0; q < 8; q++) s += Nxi[3 * q + jj] * X[3 * q + ii];
+          Xd[3 * ii + jj] = s;
         }
-        res[3 * S.nodes[mm] + i] += rk;
+      // parametric directions spanning the face (TACSHexaBasis.cpp:21-70)
+      int ta, tb;
+      if (f2 == 0) { ta = 2; tb = 1; }
+      else if (f2 == 1) { ta = 0; tb = 2; }
+      else { ta = 1; tb = 0; }
+      if (face == 1) { ta = 1; tb = 2; }
+      if (face == 3) { ta = 2; tb = 0; }
+      if (face == 5) { ta = 0; tb = 1; }
+      double t1[3], t2[3];
+      for (int ii = 0; ii < 3; ii++) {
+        t1[ii] = Xd[3 * ii + ta];
+        t2[ii] = Xd[3 * ii + tb];
+      }
+      const double nr[3] = {t1[1] * t2[2] - t1[2] * t2[1],
+                            t1[2] * t2[0] - t1[0] * t2[2],
+                            t1[0] * t2[1] - t1[1] * t2[0]};
+      const double area = sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+      aux += area * N[a] * -tr;
+    }
+  }
+  return aux;
+}
+
+// Residual and Jacobian with 8-lane teams (4 elements per warp): lane q of
+// a team owns Gauss point q for the geometry and the residual and node q's
+// 8 block columns for the BCSR lookups; the 36 upper node pairs (a, b) are
+// spread over the team, each forming
+//   M_ab = sum_q w_q g_qa g_qb^T  (w_q = detXd_q t, g = physical gradient)
+//   K_ab = lambda M_ab + mu tr(M_ab) I + mu M_ab^T
+// which is B^T (t C) B for the isotropic tangent (lambda = c1, mu = G,
+// c0 = lambda + 2 mu).  Residual r = sum_q w_q B_q^T C e_q, summed over the
+// team's lanes by shuffles in a fixed order.
+struct HexTeam {
+  double X[24];
+  double u[24];
+  double w[8];
+  double G[8][8][3];  // [point][node][component]
+  double t;
+  int nodes[8];
+  int slot[64];
+};
+
+constexpr int kHexTeamsPerCta = 8;
+
+__global__ void __launch_bounds__(64)
+    hex_team_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                             const double *__restrict__ vars, double lambda,
+                             double *__restrict__ res,
+                             double *__restrict__ mat) {
+  __shared__ HexTeam teams[kHexTeamsPerCta];
+  const int tm = threadIdx.x >> 3, tl = threadIdx.x & 7;
+  HexTeam &S = teams[tm];
+  const HexC c = hex_c(ep);
+  const int nt = gridDim.x * kHexTeamsPerCta;
+  const int rounds = (cr.count + nt - 1) / nt;
+  for (int rd = 0; rd < rounds; rd++) {
+    const int idx = (rd * gridDim.x + blockIdx.x) * kHexTeamsPerCta + tm;
+    const bool active = idx < cr.count;
+    const int e = active ? cr.elem_list[idx] : 0;
+    if (active) {
+      const int nd = m.conn[8 * e + tl];
+      S.nodes[tl] = nd;
+      if (tl == 0) S.t = m.thick[e];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        S.X[3 * tl + k] = m.xpts[3 * nd + k];
+        S.u[3 * tl + k] = vars ? vars[3 * nd + k] : 0.0;
       }
     }
-
-    if (mat) {
-      const double t = S.t;
-      for (int idx2 = lane; idx2 < 324; idx2 += 32) {
-        const int p = idx2 / 9, w = idx2 - 9 * p;
-        const int a = c_pair[p][0], b = c_pair[p][1];
-        const int i = w / 3, j = w - 3 * i;
-        double kij = 0.0;
-        for (int q = 0; q < 8; q++) {
-          const double *Na = &S.Nx[q][3 * a], *Nb = &S.Nx[q][3 * b];
-          double v;
-          if (i == j) {
-            double sh = 0.0;
-            for (int k = 0; k < 3; k++)
-              if (k != i) sh += Na[k] * Nb[k];
-            v = c.c0 * Na[i] * Nb[i] + c.G * sh;
-          } else {
-            v = c.c1 * Na[i] * Nb[j] + c.G * Na[j] * Nb[i];
-          }
-          kij += S.det[q] * (t * v);
+    __syncwarp();
+    if (active && mat)
+      for (int b = 0; b < 8; b++)
+        S.slot[8 * tl + b] = find_slot(m.rowp, m.cols, S.nodes[tl],
+                                       S.nodes[b]);
+    // geometry at point q = tl (TACSElementBasis::getFieldGradient)
+    double Nxi[24], Jinv[9];
+    const int q = tl;
+    if (active) {
+      const double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1),
+                            gauss2(q >> 2)};
+      hex_shape(pt, nullptr, Nxi);
+      double Xd[9];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          double v = 0.0;
+#pragma unroll
+          for (int mm = 0; mm < 8; mm++) v += Nxi[3 * mm + j] * S.X[3 * mm + i];
+          Xd[3 * i + j] = v;
         }
+      const double det = inv3(Xd, Jinv);
+      S.w[q] = det * S.t;
+#pragma unroll
+      for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          S.G[q][a][k] = Nxi[3 * a] * Jinv[k] + Nxi[3 * a + 1] * Jinv[3 + k] +
+                         Nxi[3 * a + 2] * Jinv[6 + k];
+    }
+    __syncwarp();
+    if (res) {
+      // r_q = w_q B_q^T C e_q for the 24 dofs at point q = tl
+      double r[24];
+      {
+        double Ux[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (active)
+#pragma unroll
+          for (int a = 0; a < 8; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+              for (int j = 0; j < 3; j++)
+                Ux[3 * i + j] += S.u[3 * a + i] * S.G[q][a][j];
+        double ev[6] = {Ux[0], Ux[4], Ux[8], Ux[5] + Ux[7], Ux[2] + Ux[6],
+                        Ux[1] + Ux[3]};
+        double sv[6];
+        hex_Ce(c, ev, sv);
+        const double wq = active ? S.w[q] : 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; k++) sv[k] *= wq;
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+          const double g0 = active ? S.G[q][a][0] : 0.0;
+          const double g1 = active ? S.G[q][a][1] : 0.0;
+          const double g2 = active ? S.G[q][a][2] : 0.0;
+          r[3 * a] = g0 * sv[0] + g1 * sv[5] + g2 * sv[4];
+          r[3 * a + 1] = g1 * sv[1] + g0 * sv[5] + g2 * sv[3];
+          r[3 * a + 2] = g2 * sv[2] + g1 * sv[3] + g0 * sv[4];
+        }
+      }
+      // sum over the team's 8 points
+#pragma unroll
+      for (int off = 1; off < 8; off <<= 1)
+#pragma unroll
+        for (int k = 0; k < 24; k++)
+          r[k] += __shfl_xor_sync(0xffffffffu, r[k], off);
+      // lane tl keeps node tl's three entries (selected with constant
+      // indices so r stays in registers)
+      double ra[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+      for (int a = 0; a < 8; a++)
+        if (a == tl) {
+          ra[0] = r[3 * a];
+          ra[1] = r[3 * a + 1];
+          ra[2] = r[3 * a + 2];
+        }
+      if (active) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          double rk = ra[i];
+          if (m.trac_ptr) rk += lambda * hex_traction(m, e, S.X, tl, i);
+          res[3 * S.nodes[tl] + i] += rk;
+        }
+      }
+    }
+    if (mat && active) {
+      for (int p = tl; p < 36; p += 8) {
+        const int a = c_pair[p][0], b = c_pair[p][1];
+        double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int qq = 0; qq < 8; qq++) {
+          const double wq = S.w[qq];
+          const double ga[3] = {wq * S.G[qq][a][0], wq * S.G[qq][a][1],
+                                wq * S.G[qq][a][2]};
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) M[3 * i + j] += ga[i] * S.G[qq][b][j];
+        }
+        const double tr = M[0] + M[4] + M[8];
+        double K[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++)
+            K[3 * i + j] = c.c1 * M[3 * i + j] + c.G * M[3 * j + i] +
+                           (i == j ? c.G * tr : 0.0);
         const int s_ab = S.slot[8 * a + b], s_ba = S.slot[8 * b + a];
-        if (s_ab >= 0) mat[9 * (size_t)s_ab + w] += kij;
-        if (a != b && s_ba >= 0) mat[9 * (size_t)s_ba + 3 * j + i] += kij;
+        if (s_ab >= 0) {
+          double *blk = mat + 9 * (size_t)s_ab;
+#pragma unroll
+          for (int k = 0; k < 9; k++) blk[k] += K[k];
+        }
+        if (a != b && s_ba >= 0) {
+          double *blk = mat + 9 * (size_t)s_ba;
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) blk[3 * j + i] += K[3 * i + j];
+        }
       }
     }
     __syncwarp();
@@ -478,8 +586,18 @@ void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
                          double *res, double *mat, int transpose,
                          cudaStream_t s) {
   if (cr.count <= 0) return;
-  hex_assembly_kernel<kWarps><<<grid_for(cr.count), kWarps * 32, 0, s>>>(
-      ep, m, cr, vars, lambda, res, mat, transpose);
+  (void)transpose;  // K is symmetric by construction (mirrored blocks)
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int grid = (cr.count + kHexTeamsPerCta - 1) / kHexTeamsPerCta;
+  if (grid > sms * 16) grid = sms * 16;
+  hex_team_assembly_kernel<<<grid, 64, 0, s>>>(ep, m, cr, vars, lambda, res,
+                                               mat);
 }
 void launch_hex_points(const ElemParams &ep, const MeshView &m,
                        const double *vars, double *elem_fail,

@@ -1,18 +1,18 @@
-// MITC4 shell (TACSQuad4Shell) element kernels for sm_103a.
+// MITC4 shell (TACSQuad4Shell) point-quantity and sensitivity kernels for
+// sm_103a: function values (compliance, KS failure), addSVSens, and the
+// fused addDVSens + addAdjointResProducts pass.  Residual and Jacobian
+// assembly live in shell_team.cu.
 //
 // One warp owns one element at a time.  The element's strain-displacement
 // operators B_q (9 x 24 at each of the 4 Gauss points) are built
 // cooperatively in shared memory from exactly the reference kinematics
 // (node normals, nodal drilling strains, the 9 MITC tying strains, the
-// transform T, Xd^-1 T and the through-thickness term), then:
-//   residual  r = sum_q detXd_q B_q^T C e_q + loads   (TACSShellElement::
-//             addResidual, src/elements/shell/TACSShellElement.h:295-433)
-//   Jacobian  K = sum_q detXd_q B_q^T C B_q           (addJacobian,
-//             TACSShellElement.h:436-641, alpha = 1, beta = gamma = 0)
-// and K is added into the 6x6 BCSR blocks of the element's 16 node pairs.
-// Elements of one launch share no node (graph colouring), so the block
-// read-modify-writes and residual scatters need no atomics and the result
-// is bitwise deterministic.
+// transform T, Xd^-1 T and the through-thickness term); the strains
+// e_q = B_q u then feed the point quantities (TACSShellElement::
+// evalPointQuantity / addPointQuantitySVSens / addPointQuantityDVSens /
+// addAdjResProduct, src/elements/shell/TACSShellElement.h:918-1352).
+// The state-sensitivity pass runs colour by colour (elements of one launch
+// share no node), so its scatter needs no atomics and is deterministic.
 #include <cmath>
 
 #include "tg_internal.h"
@@ -34,13 +34,11 @@ struct ShellSmem {
   double n0[4][3];
   double M[4][5][9];
   double B[4][9][24];
-  double CB[4][9][24];
   double e[4][9];
   double g[4][9];
   double coef[4];
   double t;
   int nodes[4];
-  int slot[16];
 };
 
 // Build fn, Bd, Bty and the Gauss-point geometry, then B_q, for the element
@@ -236,99 +234,6 @@ __device__ __forceinline__ void load_element(ShellSmem &S, const MeshView &m,
 
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
-    shell_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
-                          const double *__restrict__ vars, double lambda,
-                          double *__restrict__ res, double *__restrict__ mat,
-                          int transpose) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  ShellSmem &S = reinterpret_cast<ShellSmem *>(smem_raw)[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
-  const int nw = gridDim.x * WARPS;
-
-  for (int idx = gw; idx < cr.count; idx += nw) {
-    const int e = cr.elem_list[idx];
-    load_element(S, m, e, vars, nullptr, lane);
-    if (mat && lane < 16)
-      S.slot[lane] = find_slot(m.rowp, m.cols, S.nodes[lane >> 2],
-                               S.nodes[lane & 3]);
-    shell_build_B(S, ep, lane);
-    const ShellStiff c = shell_stiff(ep, S.t);
-
-    if (res) {
-      shell_strains(S, S.u, S.e, lane);
-      for (int idx2 = lane; idx2 < 36; idx2 += 32) {
-        const int q = idx2 / 9, r = idx2 - 9 * q;
-        S.g[q][r] = shell_stress_row(c, S.e[q], r);
-      }
-      __syncwarp();
-      if (lane < 24) {
-        double rk = 0.0;
-        for (int q = 0; q < 4; q++) {
-          double v = 0.0;
-          for (int r = 0; r < 9; r++) v += S.B[q][r][lane] * S.g[q][r];
-          rk += S.det[q] * v;
-        }
-        // TACSShellPressure::addResidual (TACSShellPressure.h:56-90)
-        if (m.pres) {
-          const int mm = lane / 6, a = lane - 6 * mm;
-          double aux = 0.0;
-          if (a < 3) {
-            const double *pn = &m.pres[4 * e];
-            for (int q = 0; q < 4; q++) {
-              double N[4], Na[4], Nb[4];
-              shape2(gauss2(q % 2), gauss2(q / 2), N, Na, Nb);
-              double pr = N[0] * pn[0] + N[1] * pn[1] + N[2] * pn[2] +
-                          N[3] * pn[3];
-              aux += N[mm] * (pr * -S.det[q] * S.n0[q][a]);
-            }
-          }
-          rk += lambda * aux;
-        }
-        res[6 * S.nodes[lane / 6] + lane % 6] += rk;
-      }
-    }
-
-    if (mat) {
-      for (int idx2 = lane; idx2 < 864; idx2 += 32) {
-        const int q = idx2 / 216, rem = idx2 - 216 * q;
-        const int r = rem / 24, col = rem - 24 * r;
-        double ecol[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) ecol[k] = S.B[q][k][col];
-        S.CB[q][r][col] = shell_stress_row(c, ecol, r);
-      }
-      __syncwarp();
-      // upper blocks (a <= b): 10 blocks x 36 entries
-      for (int idx2 = lane; idx2 < 360; idx2 += 32) {
-        const int blk = idx2 / 36, w = idx2 - 36 * blk;
-        // blk -> (a, b) with a <= b
-        const int a = blk < 4 ? 0 : (blk < 7 ? 1 : (blk < 9 ? 2 : 3));
-        const int b = a + blk - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9)));
-        const int ii = w / 6, jj = w - 6 * ii;
-        const int i = 6 * a + ii, j = 6 * b + jj;
-        double kij = 0.0;
-        for (int q = 0; q < 4; q++) {
-          double v = 0.0;
-#pragma unroll
-          for (int r = 0; r < 9; r++) v += S.B[q][r][i] * S.CB[q][r][j];
-          kij += S.det[q] * v;
-        }
-        kij *= 1.0;
-        // TACS_MAT_TRANSPOSE writes K^T; K is symmetric by construction
-        // (upper blocks mirrored), so both orientations store the same.
-        (void)transpose;
-        const int s_ab = S.slot[4 * a + b], s_ba = S.slot[4 * b + a];
-        if (s_ab >= 0) mat[36 * (size_t)s_ab + w] += kij;
-        if (a != b && s_ba >= 0) mat[36 * (size_t)s_ba + 6 * jj + ii] += kij;
-      }
-    }
-    __syncwarp();
-  }
-}
-
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
     shell_points_kernel(ElemParams ep, MeshView m,
                         const double *__restrict__ vars,
                         double *__restrict__ elem_fail,
@@ -483,17 +388,6 @@ void prep(K kernel) {
 }
 
 }  // namespace
-
-void launch_shell_assembly(const ElemParams &ep, const MeshView &m,
-                           ColorRange cr, const double *vars, double lambda,
-                           double *res, double *mat, int transpose,
-                           cudaStream_t s) {
-  if (cr.count <= 0) return;
-  auto k = shell_assembly_kernel<kWarps>;
-  prep(k);
-  k<<<grid_for(cr.count, 2), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
-      ep, m, cr, vars, lambda, res, mat, transpose);
-}
 
 void launch_shell_points(const ElemParams &ep, const MeshView &m,
                          const double *vars, double *elem_fail,

@@ -55,10 +55,6 @@ struct ColorRange {
 
 // Residual (and optionally Jacobian) assembly of one colour.
 // mat may be nullptr (residual only); res may be nullptr (matrix only).
-void launch_shell_assembly(const ElemParams &ep, const MeshView &m,
-                           ColorRange cr, const double *vars, double lambda,
-                           double *res, double *mat, int transpose,
-                           cudaStream_t s);
 // 8-lane-team MITC4 assembly (shell_team.cu); err_flag (device int, may be
 // nullptr) is set when an element has a non-positive Jacobian determinant.
 void launch_shell_team_assembly(const ElemParams &ep, const MeshView &m,
@@ -251,6 +247,7 @@ struct KrylovState {
   int *nactive;      // systems still iterating
   int *stall;        // 1: a restart that gains less than 10% on a
                      // system's true residual ends that system's solve
+                     // (FP32 mat-vec passes)
   double *rn0prev;   // nsys true residual at the previous cycle start
 };
 void launch_kr_dots(const double *W, size_t ld, const int *kdev, int kofs,

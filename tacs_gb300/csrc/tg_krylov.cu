@@ -445,11 +445,10 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                             cudaMemcpyHostToDevice, s));
     if ((rc = set_rtols(k, rt, s))) return rc;
     TG_CUDA(cudaMemsetAsync(k->d_X, 0, N * sizeof(double), s));
-    // the first FP64 pass is the reference's GMRES (it restarts until its
-    // cycle limit); refinement passes and FP32 passes stop a system whose
-    // restarts stall
-    if ((rc = run_cycles(k, mode, !(mode_in == 0 && outer == 0), s)))
-      return rc;
+    // passes with the FP64 mat-vec restart until their cycle limit (the
+    // first one is the reference's GMRES); passes with the FP32 mat-vec stop
+    // a system whose restarts stall at the FP32 accuracy floor
+    if ((rc = run_cycles(k, mode, mode == 1, s))) return rc;
     if ((rc = fetch(it, k->st.iters, ns, s))) return rc;
     std::vector<int> err;
     if ((rc = fetch(err, k->st.err, ns, s))) return rc;

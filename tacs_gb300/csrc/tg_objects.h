@@ -168,6 +168,12 @@ struct tg_pc {
   int *d_cl_grp_lvl = nullptr, *d_cl_lvl_ptr = nullptr, *d_cl_rows = nullptr;
   int *d_cl_grp_ulvl = nullptr, *d_cl_ulvl_ptr = nullptr,
       *d_cl_urows = nullptr;
+  // schedule autotuner: the plan inputs and the measured time per cluster
+  // size (index = size; 0 = not measured)
+  bool tuned = false;
+  std::vector<int> tune_rowp, tune_cols, tune_lvl, tune_ulvl;
+  int tune_nl = 0, tune_nu = 0;
+  double tune_ms[17] = {0};
   // the level-by-level triangular solves replayed as one CUDA graph
   cudaGraphExec_t apply_exec = nullptr;
   bool factored = false;

@@ -685,7 +685,7 @@ static int build_cluster_schedule(tg_pc *pc, const std::vector<int> &rowp,
                                   const std::vector<int> &cols,
                                   const std::vector<int> &lvl,
                                   const std::vector<int> &ulvl, int nl,
-                                  int nu) {
+                                  int nu, int force_cs = 0) {
   const int n = (int)rowp.size() - 1;
   std::vector<int> parent(n);
   std::iota(parent.begin(), parent.end(), 0);
@@ -724,6 +724,7 @@ static int build_cluster_schedule(tg_pc *pc, const std::vector<int> &rowp,
   int cs = 1;
   // the widest level over all components bounds the per-group width
   while (cs < max_cs && cs * per_cta < width) cs *= 2;
+  if (force_cs > 0) cs = std::min(force_cs, max_cs);
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -798,6 +799,8 @@ static int build_cluster_schedule(tg_pc *pc, const std::vector<int> &rowp,
   for (int g = 0; g < ngroups; g++)
     max_lp = std::max(max_lp, (grp_l[g + 1] - grp_l[g]) +
                                   (grp_u[g + 1] - grp_u[g]));
+  dfree(pc->d_cl_grp_lvl); dfree(pc->d_cl_lvl_ptr); dfree(pc->d_cl_rows);
+  dfree(pc->d_cl_grp_ulvl); dfree(pc->d_cl_ulvl_ptr); dfree(pc->d_cl_urows);
   int rc = 0;
   if (!rc) rc = upload(&pc->d_cl_grp_lvl, grp_l);
   if (!rc) rc = upload(&pc->d_cl_lvl_ptr, lptr);
@@ -875,10 +878,17 @@ static int build_ilu_plan(tg_pc *pc, const std::vector<int> &rowp,
     }
   }
   int rc;
-  if (pc->type == TG_PC_ILU0 && (rc = build_cluster_schedule(pc, rowp, cols,
-                                                             lvl, ulvl, nl,
-                                                             nu)))
-    return rc;
+  if (pc->type == TG_PC_ILU0) {
+    if ((rc = build_cluster_schedule(pc, rowp, cols, lvl, ulvl, nl, nu)))
+      return rc;
+    // kept for the schedule autotuner
+    pc->tune_rowp = rowp;
+    pc->tune_cols = cols;
+    pc->tune_lvl = lvl;
+    pc->tune_ulvl = ulvl;
+    pc->tune_nl = nl;
+    pc->tune_nu = nu;
+  }
   if ((rc = upload(&pc->d_lvl_rows, lrows))) return rc;
   if ((rc = upload(&pc->d_ulvl_rows, urows))) return rc;
   if ((rc = upload(&pc->d_upd_ptr, upd_ptr))) return rc;
@@ -1003,6 +1013,63 @@ int tg_pc_decref(tg_pc *pc) {
   return 0;
 }
 
+}  // extern "C"
+
+// Schedule autotuner of the cluster triangular solves: after the first
+// factorisation, time both solves (CUDA events, 3 launches after one
+// warm-up) for every cluster size the device can schedule and keep the
+// fastest.  The width heuristic of build_cluster_schedule is only the
+// starting guess: the best size trades the FP64 work per CTA against the
+// cluster barrier's latency, which depends on the level widths.
+static int autotune_cluster(tg_pc *pc, cudaStream_t s) {
+  const size_t n = (size_t)pc->A->nrows * pc->A->bsize;
+  const bool f64 = pc->precision == TG_PREC_FP64;
+  void *in = f64 ? (void *)pc->d_gx : (void *)pc->d_x32;
+  void *out = f64 ? (void *)pc->d_gy : (void *)pc->d_y32;
+  void *tmp = f64 ? (void *)pc->d_tmp : (void *)pc->d_tmp32;
+  TG_CUDA(cudaMemsetAsync(in, 0, n * (f64 ? 8 : 4), s));
+  cudaEvent_t e0, e1;
+  TG_CUDA(cudaEventCreate(&e0));
+  TG_CUDA(cudaEventCreate(&e1));
+  const int max_cs = ilu_cluster_max_size();
+  int best_cs = pc->plan.cluster.cs;
+  float best = 1e30f;
+  for (int cs = 1; cs <= max_cs; cs *= 2) {
+    int rc = build_cluster_schedule(pc, pc->tune_rowp, pc->tune_cols,
+                                    pc->tune_lvl, pc->tune_ulvl, pc->tune_nl,
+                                    pc->tune_nu, cs);
+    if (rc) return rc;
+    pc_launch(pc, 1, n, in, out, tmp, nullptr, nullptr, s);
+    TG_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < 3; r++)
+      pc_launch(pc, 1, n, in, out, tmp, nullptr, nullptr, s);
+    TG_CUDA(cudaEventRecord(e1, s));
+    TG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    TG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    pc->tune_ms[cs] = ms / 3;
+    if (ms < best) {
+      best = ms;
+      best_cs = cs;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int rc = build_cluster_schedule(pc, pc->tune_rowp, pc->tune_cols,
+                                  pc->tune_lvl, pc->tune_ulvl, pc->tune_nl,
+                                  pc->tune_nu, best_cs);
+  if (rc) return rc;
+  if (pc->apply_exec) {  // captured against the previous schedule
+    cudaGraphExecDestroy(pc->apply_exec);
+    pc->apply_exec = nullptr;
+  }
+  pc->tuned = true;
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" {
+
 int tg_pc_factor(tg_pc *pc, void *s) {
   if (!pc) return fail(TG_ERR_ARG, "tg_pc_factor: NULL pc");
   tg_mat *A = pc->A;
@@ -1059,6 +1126,10 @@ int tg_pc_factor(tg_pc *pc, void *s) {
     return fail(TG_ERR_PIVOT, buf);
   }
   pc->factored = true;
+  if (pc->type == TG_PC_ILU0 && !pc->tuned && pc->plan.cluster.ngroups > 0) {
+    int rc = autotune_cluster(pc, S(s));
+    if (rc) return rc;
+  }
   return 0;
 }
 
@@ -1139,6 +1210,19 @@ static int pc_apply_internal(tg_pc *pc, cudaStream_t s) {
     if (e != cudaSuccess) return cuda_check(e, "ILU(0) apply graph capture");
   }
   TG_CUDA(cudaGraphLaunch(pc->apply_exec, s));
+  return 0;
+}
+
+int tg_pc_get_schedule(tg_pc *pc, int *cluster_size, int *groups,
+                       int *levels, double *tuned_ms) {
+  if (!pc) return fail(TG_ERR_ARG, "NULL pc");
+  const IluClusterView &v = pc->plan.cluster;
+  if (cluster_size) *cluster_size = v.ngroups ? v.cs : 0;
+  if (groups) *groups = v.ngroups;
+  if (levels)
+    *levels = (int)(pc->plan.lvl_ptr_h.size() + pc->plan.ulvl_ptr_h.size()) - 2;
+  if (tuned_ms)
+    for (int i = 0; i < 5; i++) tuned_ms[i] = pc->tune_ms[1 << i];
   return 0;
 }
 

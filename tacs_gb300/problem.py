@@ -88,6 +88,18 @@ class Pc:
               "tg_pc_apply")
         return y
 
+    def schedule(self):
+        """Cluster size, clusters, levels and the autotuner's timings."""
+        cs, ng, nl = C.c_int(), C.c_int(), C.c_int()
+        ms = np.zeros(5)
+        check(_lib.lib().tg_pc_get_schedule(self.handle, C.byref(cs),
+                                            C.byref(ng), C.byref(nl),
+                                            ms.ctypes.data))
+        return {"cluster_size": cs.value, "clusters": ng.value,
+                "levels": nl.value,
+                "tuned_ms": {1 << i: float(ms[i]) for i in range(5)
+                             if ms[i] > 0}}
+
     def __del__(self):
         try:
             _lib.lib().tg_pc_decref(self.handle)
