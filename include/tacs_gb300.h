@@ -232,10 +232,11 @@ int tg_pc_get_schedule(tg_pc *pc, int *cluster_size, int *groups,
 /* GMRES(mat, pc, m, nrestart, isFlexible) (src/bpmat/KSM.h) with
    setTolerances(rtol, atol).  mixed != 0 runs the preconditioner and the
    inner mat-vec in FP32 (pc must be TG_PREC_FP32) inside FP64 GMRES with
-   FP64 Arnoldi and a true-residual iterative-refinement loop; a system
-   whose FP32 mat-vec passes stop paying switches to the FP64 mat-vec with
-   the FP32 preconditioner.  With a TG_PREC_FP32 pc the solver is flexible
-   GMRES (isFlexible = 1: it keeps M^{-1} v_j, m more vectors of memory). */
+   FP64 Arnoldi and a true-residual iterative-refinement loop; when the
+   FP32 passes stop paying, the remaining passes run the all-FP64 solve
+   (an FP64 factor of the same matrix is made then).  With a TG_PREC_FP32
+   pc the solver is flexible GMRES (isFlexible = 1: it keeps M^{-1} v_j,
+   m more vectors of memory). */
 int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
                   tg_ksm **out);
 int tg_ksm_decref(tg_ksm *k);

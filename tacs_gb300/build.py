@@ -67,7 +67,8 @@ def build(force=False, verbose=False, extra=()):
         msg = "\n".join(f"--- {s}\n{o}" for s, o in failed)
         raise RuntimeError("nvcc failed:\n" + msg)
     if force or procs or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o",
+               LIB, *objs, "-lcudart"]
         subprocess.run(cmd, check=True)
     return LIB
 

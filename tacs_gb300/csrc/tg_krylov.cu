@@ -28,8 +28,9 @@ void enqueue_pc(tg_ksm *k, const double *in, double *out, cudaStream_t s) {
   if (!pc) {
     cudaMemcpyAsync(out, in, k->N * sizeof(double), cudaMemcpyDeviceToDevice,
                     s);
-  } else if (pc->precision == TG_PREC_FP64) {
-    pc_launch(pc, k->nrhs, k->n, in, out, k->d_t64, k->d_px, k->d_py, s);
+  } else if (pc->precision == TG_PREC_FP64 || k->mixed) {
+    // a mixed-precision solve's FP64 passes use the FP64 factor
+    pc_launch(pc, k->nrhs, k->n, in, out, k->d_t64, k->d_px, k->d_py, s, 1);
   } else {
     launch_d2f(in, k->d_x32, k->N, s);
     pc_launch(pc, k->nrhs, k->n, k->d_x32, k->d_y32, k->d_t32, k->d_px32,
@@ -177,7 +178,7 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   if (!rc) rc = dalloc(&k->d_Bo, N);
   if (!rc) rc = dalloc(&k->d_Xo, N);
   tg_pc *pc = k->pc;
-  if (!rc && pc && pc->precision == TG_PREC_FP64) {
+  if (!rc && pc && (pc->precision == TG_PREC_FP64 || k->mixed)) {
     rc = dalloc(&k->d_t64, N);
     if (!rc && pc->type == TG_PC_ILU0_COLORED) rc = dalloc(&k->d_px, N);
     if (!rc && pc->type == TG_PC_ILU0_COLORED) rc = dalloc(&k->d_py, N);
@@ -269,7 +270,8 @@ int set_rtols(tg_ksm *k, const std::vector<double> &v, cudaStream_t s) {
 }
 
 // Restarted GMRES on d_B -> d_X (state reset except done[]).
-int run_cycles(tg_ksm *k, int mode, int stall, cudaStream_t s) {
+int run_cycles(tg_ksm *k, int mode, int stall, cudaStream_t s,
+               int max_cycles = 0) {
   const size_t S1 = (size_t)k->nsys;
   KrylovState &st = k->st;
   TG_CUDA(cudaMemsetAsync(st.converged, 0, S1 * sizeof(int), s));
@@ -281,7 +283,9 @@ int run_cycles(tg_ksm *k, int mode, int stall, cudaStream_t s) {
   TG_CUDA(cudaMemcpyAsync(st.stall, &stall, sizeof(int),
                           cudaMemcpyHostToDevice, s));
   volatile int *hp = k->h_pinned;
-  for (int cycle = 0; cycle <= k->nrestart; cycle++) {
+  const int ncyc = max_cycles > 0 ? std::min(max_cycles, k->nrestart + 1)
+                                  : k->nrestart + 1;
+  for (int cycle = 0; cycle < ncyc; cycle++) {
     TG_CUDA(cudaGraphLaunch(k->g_start, s));
     TG_CUDA(cudaMemcpyAsync(k->h_pinned, st.nactive, sizeof(int),
                             cudaMemcpyDeviceToHost, s));
@@ -339,9 +343,10 @@ int fetch(std::vector<T> &h, const T *d, size_t n, cudaStream_t s) {
 // Mode 1 (mixed precision): every pass runs the FP32 preconditioner and
 // mat-vec with FP64 Arnoldi to a modest relative tolerance, and a system has
 // converged when its FP64 true residual meets rtol ||r0||.  Each pass
-// contracts the true residual by about cond(A) x the FP32 rounding of A;
-// when a pass gains less than 1e4x for some system, the remaining passes
-// apply A in FP64 (the preconditioner stays FP32) and solve to the full
+// contracts the true residual by about cond(A) x the FP32 rounding of A
+// (and by the FP32 factor's own accuracy); when a pass gains less than 1e4x
+// for some system, the remaining passes run the all-FP64 solve (an FP64
+// factor of the same matrix, made then, and the FP64 mat-vec) to the full
 // tolerance, and a system stops when a pass no longer halves its residual.
 int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                   int zero_guess, int *iters, int *flags, double *resn,
@@ -357,6 +362,8 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                             cudaMemcpyDeviceToDevice, s));
   std::vector<double> r0, rn, prev(ns, 0.0), rt(ns), mask(ns);
   std::vector<int> conv(ns, 0), done(ns, 0), it_total(ns, 0), it, pconv;
+  std::vector<int> fresh(ns, 0);  // mixed: system restarted from zero in FP64
+  std::vector<int> stuck(ns, 0);  // mixed: FP64 continuation did not converge
   int rc;
   const int max_outer = mode == 0 ? 2 : 30;
   const int mode_in = mode;
@@ -369,7 +376,7 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
     if ((rc = seg_norms(k, k->d_B, rn, s))) return rc;
     if (outer == 0) r0 = rn;
     int left = 0;
-    bool to_fp64 = false;
+    bool to_fp64 = false, restart_any = false;
     // a correction that made a system's true residual larger is taken back
     if (outer > 0) {
       bool any = false;
@@ -383,10 +390,15 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                                 cudaMemcpyHostToDevice, s));
         launch_kr_mask(k->d_X, k->ch, k->st.scale, s);
         launch_axpy(-1.0, k->d_X, k->d_Xo, N, s);
+        // the residual of the restored iterate drives the next pass
+        launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                         A->d_vals, k->d_Xo, k->d_B, s, k->nrhs, k->n);
+        launch_kr_residual(k->d_Bo, k->d_B, N, s);
         for (int i = 0; i < ns; i++)
           if (mask[i] != 0.0) {
             rn[i] = prev[i];
             if (mode == 1) to_fp64 = true;
+            else if (mode_in == 1 && !fresh[i]) stuck[i] = 1;
             else done[i] = 1;
           }
       }
@@ -405,13 +417,44 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
         // the remaining passes keep the FP32 preconditioner but apply A in
         // FP64
         to_fp64 = true;
-      } else if (outer > 0 && rn[i] > 0.5 * prev[i]) {
-        done[i] = 1;  // stagnated
+      } else if (stuck[i] || (outer > 0 && rn[i] > 0.5 * prev[i])) {
+        if (mode_in == 1 && mode == 0 && !fresh[i]) {
+          // the FP64 passes stalled from the mixed-precision iterate (its
+          // residual is left in the hardest modes, where restarted GMRES
+          // stagnates): solve this system again from zero, all in FP64
+          fresh[i] = 1;
+          restart_any = true;
+        } else {
+          done[i] = 1;  // stagnated
+        }
       } else if (outer == max_outer) {
         done[i] = 1;
       }
     }
-    if (to_fp64) mode = 0;
+    if (to_fp64) {
+      mode = 0;
+      if ((rc = pc_factor_fp64(k->pc, s))) return rc;
+    }
+    if (restart_any) {
+      std::vector<double> keep(ns);
+      for (int i = 0; i < ns; i++) {
+        const bool reset =
+            fresh[i] && (stuck[i] || rn[i] > 0.5 * prev[i]) && !done[i];
+        stuck[i] = 0;
+        keep[i] = reset ? 0.0 : 1.0;
+        if (reset) {
+          rn[i] = r0[i];
+          prev[i] = 2.0 * r0[i];  // the fresh solve's first pass always runs
+        }
+      }
+      TG_CUDA(cudaMemcpyAsync(k->st.scale, keep.data(), ns * sizeof(double),
+                              cudaMemcpyHostToDevice, s));
+      launch_kr_mask(k->d_Xo, k->ch, k->st.scale, s);
+      // the residual of a reset system is its right-hand side again
+      launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                       A->d_vals, k->d_Xo, k->d_B, s, k->nrhs, k->n);
+      launch_kr_residual(k->d_Bo, k->d_B, N, s);
+    }
     if (trace) {
       std::fprintf(stderr, "[tg_ksm] pass %d mode %d:", outer, mode);
       for (int i = 0; i < ns; i++)
@@ -448,7 +491,18 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
     // passes with the FP64 mat-vec restart until their cycle limit (the
     // first one is the reference's GMRES); passes with the FP32 mat-vec stop
     // a system whose restarts stall at the FP32 accuracy floor
+    // a mixed solve's FP64 pass that continues from the FP32 iterate and
+    // does not converge within its cycle limit (restarted GMRES can stall on
+    // the hard modes such a residual is left in) restarts that system from
+    // zero in FP64
+    const bool continuing = mode_in == 1 && mode == 0;
     if ((rc = run_cycles(k, mode, mode == 1, s))) return rc;
+    if (continuing) {
+      std::vector<int> ic;
+      if ((rc = fetch(ic, k->st.converged, ns, s))) return rc;
+      for (int i = 0; i < ns; i++)
+        if (!done[i] && !fresh[i] && !ic[i]) stuck[i] = 1;
+    }
     if ((rc = fetch(it, k->st.iters, ns, s))) return rc;
     std::vector<int> err;
     if ((rc = fetch(err, k->st.err, ns, s))) return rc;

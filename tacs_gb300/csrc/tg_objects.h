@@ -177,6 +177,7 @@ struct tg_pc {
   // the level-by-level triangular solves replayed as one CUDA graph
   cudaGraphExec_t apply_exec = nullptr;
   bool factored = false;
+  bool fp64_ready = false;  // FP32 pc: FP64 factor of the same matrix in d_F
   ~tg_pc() {
     if (apply_exec) cudaGraphExecDestroy(apply_exec);
     dfree(d_lvl_rows); dfree(d_ulvl_rows); dfree(d_upd_ptr);
@@ -257,5 +258,7 @@ namespace tg {
 // M^{-1} on nrhs vectors ld apart (tg_runtime.cu); FP64 buffers for a FP64
 // pc, FP32 for a FP32 pc
 int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
-              void *tmp, void *px, void *py, cudaStream_t s);
+              void *tmp, void *px, void *py, cudaStream_t s, int use_f64 = -1);
+// FP64 factor of an FP32 pc's matrix (for FP64 fallback passes)
+int pc_factor_fp64(tg_pc *pc, cudaStream_t s);
 }  // namespace tg

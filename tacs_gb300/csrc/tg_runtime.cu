@@ -1015,6 +1015,41 @@ int tg_pc_decref(tg_pc *pc) {
 
 }  // extern "C"
 
+namespace tg {
+
+// FP64 factor of an FP32 preconditioner's matrix, for the FP64 passes a
+// mixed-precision solve falls back to (kept in d_F beside the FP32 factor).
+int pc_factor_fp64(tg_pc *pc, cudaStream_t s) {
+  if (pc->precision == TG_PREC_FP64 || pc->fp64_ready) return 0;
+  tg_mat *A = pc->A;
+  const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
+  TG_CUDA(cudaMemsetAsync(pc->d_fail, 0, sizeof(int), s));
+  const int nl = (int)pc->plan.lvl_ptr_h.size() - 1;
+  if (pc->type == TG_PC_ILU0_COLORED) {
+    launch_gather_blocks(A->nnz, A->bsize * A->bsize, pc->d_valmap, A->d_vals,
+                         pc->d_F, s);
+    for (int L = 0; L < nl; L++) launch_ilu0_factor_level(pc->plan, L, pc->d_F, s);
+  } else if (pc->type == TG_PC_ILU0) {
+    TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
+                            cudaMemcpyDeviceToDevice, s));
+    for (int L = 0; L < nl; L++) launch_ilu0_factor_level(pc->plan, L, pc->d_F, s);
+  } else {
+    TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
+                            cudaMemcpyDeviceToDevice, s));
+    launch_block_inverse_diag(pc->plan, pc->d_F, s);
+  }
+  int hfail = 0;
+  TG_CUDA(cudaMemcpyAsync(&hfail, pc->d_fail, sizeof(int),
+                          cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  if (hfail)
+    return fail(TG_ERR_PIVOT, "FP64 factor: singular diagonal block");
+  pc->fp64_ready = true;
+  return 0;
+}
+
+}  // namespace tg
+
 // Schedule autotuner of the cluster triangular solves: after the first
 // factorisation, time both solves (CUDA events, 3 launches after one
 // warm-up) for every cluster size the device can schedule and keep the
@@ -1126,6 +1161,7 @@ int tg_pc_factor(tg_pc *pc, void *s) {
     return fail(TG_ERR_PIVOT, buf);
   }
   pc->factored = true;
+  pc->fp64_ready = false;
   if (pc->type == TG_PC_ILU0 && !pc->tuned && pc->plan.cluster.ngroups > 0) {
     int rc = autotune_cluster(pc, S(s));
     if (rc) return rc;
@@ -1141,9 +1177,9 @@ namespace tg {
 // for a FP64 pc and FP32 for a FP32 pc; tmp (and px, py for the colour-
 // reordered factor) hold nrhs * ld entries.
 int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
-              void *tmp, void *px, void *py, cudaStream_t s) {
+              void *tmp, void *px, void *py, cudaStream_t s, int use_f64) {
   const int bs = pc->A->bsize, nr = pc->A->nrows;
-  const bool f64 = pc->precision == TG_PREC_FP64;
+  const bool f64 = use_f64 < 0 ? pc->precision == TG_PREC_FP64 : use_f64 != 0;
   if (pc->type == TG_PC_BLOCK_JACOBI) {
     if (f64)
       launch_block_jacobi_apply(pc->plan, pc->d_F, (const double *)in,
