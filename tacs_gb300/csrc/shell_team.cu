@@ -77,22 +77,23 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
                                double *__restrict__ res,
                                double *__restrict__ mat, int *err_flag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned char s_ij[300][2];
+  __shared__ unsigned char s_tile[36][2];
   TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
   const int lane = threadIdx.x & 31;
   const int tl = lane & (kTeam - 1);
   const int team_in_cta = threadIdx.x / kTeam;
   TeamSmem &S = teams[team_in_cta];
 
-  // upper-triangle (i <= j) enumeration of the 24 x 24 element matrix
-  for (int k = threadIdx.x; k < 300; k += blockDim.x) {
-    int j = 0, base = 0;
-    while (base + j + 1 <= k) {
-      base += j + 1;
-      j++;
+  // the 24 x 24 element matrix as an 8 x 8 grid of 3 x 3 tiles (a tile
+  // never straddles two 6 x 6 node blocks); upper tiles (ti <= tj)
+  for (int k = threadIdx.x; k < 36; k += blockDim.x) {
+    int tj = 0, base = 0;
+    while (base + tj + 1 <= k) {
+      base += tj + 1;
+      tj++;
     }
-    s_ij[k][0] = (unsigned char)(k - base);
-    s_ij[k][1] = (unsigned char)j;
+    s_tile[k][0] = (unsigned char)(k - base);
+    s_tile[k][1] = (unsigned char)tj;
   }
   __syncthreads();
 
@@ -425,19 +426,44 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
       }
     }
 
-    // ------------------------------- K: 300 upper entries, mirrored
+    // ------------- K: 36 upper 3 x 3 tiles, each entry sum_c Z_ci Z_cj
+    // (register tiles: 6 shared loads per channel feed 9 products), the
+    // off-diagonal tiles mirrored into the transposed block
     if (mat && active) {
-      for (int k = tl; k < 300; k += kTeam) {
-        const int i = s_ij[k][0], j = s_ij[k][1];
-        double v = 0.0;
+      for (int k = tl; k < 36; k += kTeam) {
+        const int ti = s_tile[k][0], tj = s_tile[k][1];
+        const int i0 = 3 * ti, j0 = 3 * tj;
+        double v[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll 5
-        for (int c = 0; c < kNchan; c++) v += S.Z[c][i] * S.Z[c][j];
-        const int a = i / 6, ii = i - 6 * a, b = j / 6, jj = j - 6 * b;
+        for (int c = 0; c < kNchan; c++) {
+          const double zi[3] = {S.Z[c][i0], S.Z[c][i0 + 1], S.Z[c][i0 + 2]};
+          const double zj[3] = {S.Z[c][j0], S.Z[c][j0 + 1], S.Z[c][j0 + 2]};
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) v[3 * r + q] += zi[r] * zj[q];
+        }
+        const int a = ti >> 1, b = tj >> 1;
+        const int ii0 = 3 * (ti & 1), jj0 = 3 * (tj & 1);
         const int s_ab = S.slot[4 * a + b];
-        if (s_ab >= 0) mat[36 * (size_t)s_ab + 6 * ii + jj] += v;
-        if (i != j) {
+        if (s_ab >= 0) {
+          double *blk = mat + 36 * (size_t)s_ab;
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+              blk[6 * (ii0 + r) + jj0 + q] += v[3 * r + q];
+        }
+        if (ti != tj) {
           const int s_ba = S.slot[4 * b + a];
-          if (s_ba >= 0) mat[36 * (size_t)s_ba + 6 * jj + ii] += v;
+          if (s_ba >= 0) {
+            double *blk = mat + 36 * (size_t)s_ba;
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+              for (int q = 0; q < 3; q++)
+                blk[6 * (jj0 + q) + ii0 + r] += v[3 * r + q];
+          }
         }
       }
     }
