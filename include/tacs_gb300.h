@@ -190,6 +190,16 @@ int tg_add_total_derivative_segments(tg_assembler *a, const double *vars,
                                      int func, double coef, const double *psi,
                                      double scale, double *dfdx, void *stream);
 
+/* --------------------------------------------------------------- vectors */
+/* TACSBVec::axpy / scale / dot (src/bpmat/TACSBVec.cpp:215-408) on device
+   vectors of n doubles.  tg_vec_dot synchronises the stream and writes the
+   result to *out (host); it keeps a small reduction buffer per device. */
+int tg_vec_axpy(double alpha, const double *x, double *y, long n,
+                void *stream);
+int tg_vec_scale(double alpha, double *x, long n, void *stream);
+int tg_vec_dot(const double *x, const double *y, long n, double *out,
+               void *stream);
+
 /* ------------------------------------------------------------------ BCSR */
 /* TACSAssembler::createMat (src/TACSAssembler.cpp:3384): a BCSR matrix with
    the assembler's non-zero pattern (node graph plus diagonal, sorted

@@ -66,6 +66,9 @@ SIGNATURES = [
     ("tg_ksm_solve", _I, [_P, _P, _P, _I, _IP, _DP, _P]),
     ("tg_ksm_set_segments", _I, [_P, _I, _P]),
     ("tg_pc_get_schedule", _I, [_P, _IP, _IP, _IP, _P]),
+    ("tg_vec_axpy", _I, [_D, _P, _P, C.c_long, _P]),
+    ("tg_vec_scale", _I, [_D, _P, C.c_long, _P]),
+    ("tg_vec_dot", _I, [_P, _P, C.c_long, _DP, _P]),
     ("tg_assembler_set_segments", _I, [_P, _I, _P]),
     ("tg_eval_functions_segments", _I, [_P, _P, _I, _D, _P, _P]),
     ("tg_add_sv_sens_segments", _I, [_P, _P, _I, _D, _P, _P]),

@@ -341,6 +341,41 @@ int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,
   return 0;
 }
 
+// ---------------------------------------------------------------- vectors
+int tg_vec_axpy(double alpha, const double *x, double *y, long n, void *s) {
+  if ((!x || !y) && n > 0) return fail(TG_ERR_ARG, "tg_vec_axpy: NULL");
+  launch_axpy(alpha, x, y, (size_t)n, S(s));
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+int tg_vec_scale(double alpha, double *x, long n, void *s) {
+  if (!x && n > 0) return fail(TG_ERR_ARG, "tg_vec_scale: NULL");
+  launch_scale(alpha, x, (size_t)n, S(s));
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+int tg_vec_dot(const double *x, const double *y, long n, double *out,
+               void *s) {
+  if (!x || !y || !out) return fail(TG_ERR_ARG, "tg_vec_dot: NULL");
+  // reduction scratch, allocated once per device (calls on one device
+  // share it, so concurrent dot products on two streams must be ordered)
+  constexpr int kParts = 1024;
+  static double *scratch[64] = {nullptr};
+  int dev = 0;
+  TG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(TG_ERR_ARG, "tg_vec_dot: device id");
+  if (!scratch[dev]) {
+    int rc = dalloc(&scratch[dev], kParts + 1);
+    if (rc) return rc;
+  }
+  launch_dots(x, (size_t)n, 1, y, scratch[dev], kParts, scratch[dev] + kParts,
+              S(s));
+  TG_CUDA(cudaMemcpyAsync(out, scratch[dev] + kParts, sizeof(double),
+                          cudaMemcpyDeviceToHost, S(s)));
+  TG_CUDA(cudaStreamSynchronize(S(s)));
+  return 0;
+}
+
 int tg_apply_bcs(tg_assembler *a, double *vec, void *s) {
   int rc = check_ready(a, "tg_apply_bcs");
   if (rc) return rc;
