@@ -13,6 +13,8 @@ are given by the caller, as pyTACS element call-backs do.
 """
 from __future__ import annotations
 
+import re
+
 import numpy as np
 
 from . import meshes
@@ -97,8 +99,16 @@ def read_bdf(path, thickness=1.0, E=70e9, nu=0.3, rho=2700.0, ys=2.7e8):
     scale) ``thickness``.  Extra keys: ``grid_ids`` (GRID id of each node),
     ``elem_ids`` (element id of each element)."""
     with open(path) as fh:
-        cards = list(_cards(fh))
+        lines = fh.readlines()
+    cards = list(_cards(lines))
+    # component names from property comments ("$ ... Property 1 : PLATE")
+    names = {}
+    for line in lines:
+        m = re.match(r"\s*\$.*Property\s+(\d+)\s*:\s*(.*\S)", line)
+        if m:
+            names[int(m.group(1))] = m.group(2)
     cords, grids, quads, hexes, spcs, forces = {}, {}, [], [], [], []
+    pids = []
     for name, f in cards:
         if name == "CORD2R":
             cords[_int(f[0])] = _cord2r(f)
@@ -108,8 +118,10 @@ def read_bdf(path, thickness=1.0, E=70e9, nu=0.3, rho=2700.0, ys=2.7e8):
             grids[gid] = (cp, x)
         elif name == "CQUAD4":
             quads.append((_int(f[0]), [_int(v) for v in f[2:6]]))
+            pids.append(_int(f[1]))
         elif name == "CHEXA":
             hexes.append((_int(f[0]), [_int(v) for v in f[2:10]]))
+            pids.append(_int(f[1]))
         elif name == "SPC1":
             comps = f[1].strip()
             ids = [_int(v) for v in f[2:] if v.strip()]
@@ -162,4 +174,36 @@ def read_bdf(path, thickness=1.0, E=70e9, nu=0.3, rho=2700.0, ys=2.7e8):
     p["force"] = force.ravel()
     p["grid_ids"] = np.array(ids)
     p["elem_ids"] = np.array(eids)
+    p["elem_pids"] = np.array(pids, np.int32)
+    p["pid_names"] = {pid: names.get(pid, "") for pid in sorted(set(pids))}
     return p
+
+
+def write_bdf(path, p, pid_names=None):
+    """Free-field BDF of a problem record's GRIDs (basic frame, full
+    precision), CQUAD4 / CHEXA elements (property ids from ``elem_pids``,
+    default 1) and SPC1 cards, readable by read_bdf (ids: node index + 1,
+    element index + 1)."""
+    xyz = np.asarray(p["xpts"]).reshape(-1, 3)
+    shell = int(p["elem_type"]) == meshes.SHELL
+    npe = 4 if shell else 8
+    conn = np.asarray(p["conn"]).reshape(-1, npe)
+    pids = np.asarray(p.get("elem_pids", np.ones(len(conn), np.int32)))
+    order = (0, 1, 3, 2) if shell else (0, 1, 3, 2, 4, 5, 7, 6)
+    out = ["BEGIN BULK"]
+    for pid in sorted(set(int(x) for x in pids)):
+        nm = (pid_names or {}).get(pid, f"COMP{pid}")
+        out.append(f"$ Property {pid} : {nm}")
+        out.append(f"{'PSHELL' if shell else 'PSOLID'},{pid},1")
+    for k, x in enumerate(xyz):
+        out.append(f"GRID,{k + 1},0,{float(x[0])!r},{float(x[1])!r},{float(x[2])!r}")
+    name = "CQUAD4" if shell else "CHEXA"
+    for e, nodes in enumerate(conn):
+        ns = ",".join(str(int(nodes[q]) + 1) for q in order)
+        out.append(f"{name},{e + 1},{int(pids[e])},{ns}")
+    for node, mask in zip(p["bc_nodes"], p["bc_masks"]):
+        comps = "".join(str(k + 1) for k in range(6) if (int(mask) >> k) & 1)
+        out.append(f"SPC1,1,{comps},{int(node) + 1}")
+    out.append("ENDDATA")
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")
