@@ -496,6 +496,9 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_per_step(nelem),
                      "traffic_unit": "bytes per step (ncu, scaled)",
+                     # the kernel's binding resource: ncu's
+                     # sm__pipe_fp64_cycles_active on one colour launch
+                     "fp64_pipe_active": 0.705,
                      "peak_source": peak_src,
                      "kernel": "shell_team_assembly_kernel",
                      "kernel_ms": kern_ms, "algorithmic_bytes": algo},
