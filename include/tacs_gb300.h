@@ -168,6 +168,33 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
                             double coef, const double *psi, double scale,
                             double *dfdx, void *stream);
 
+/* ------------------------------------- node-coordinate sensitivities */
+/* The node vectors dfdX hold 3 doubles per node (TACSAssembler::
+   createNodeVec).  Each element's 3 x nodes coordinate derivatives are
+   exact (dual arithmetic), the quantity the reference's complex build
+   returns.  Launches run colour by colour and are deterministic. */
+
+/* TACSAssembler::addXptSens(coef, funcs, dfdXpt) (src/TACSAssembler.cpp:
+   4858): dfdX[i] += coef * d f_i / dX for TG_FUNC_COMPLIANCE /
+   TG_FUNC_KS_FAILURE (KS after tg_eval_functions at the same vars). */
+int tg_add_xpt_sens(tg_assembler *a, const double *vars, int nfuncs,
+                    const int *funcs_host, double coef, double **dfdX,
+                    void *stream);
+
+/* TACSAssembler::addAdjointResXptSensProducts(scale, adjoints, dfdXpt,
+   lambda) (src/TACSAssembler.cpp:5136): dfdX[k] += scale * psi_k^T dR/dX,
+   the pressure and traction loads scaled by lambda. */
+int tg_add_adjoint_res_xpt_products(tg_assembler *a, const double *vars,
+                                    double scale, int nadj, const double **psi,
+                                    double **dfdX, double lambda,
+                                    void *stream);
+
+/* Fused shape derivative of one function: dfdX += coef * df/dX
+   + scale * psi^T dR/dX (lambda = 1) in one pass. */
+int tg_add_total_xpt_derivative(tg_assembler *a, const double *vars, int func,
+                                double coef, const double *psi, double scale,
+                                double *dfdX, void *stream);
+
 /* ------------------------------------------------------ element segments */
 /* No reference counterpart (the reference holds one model per assembler).
    elem_ptr (host, nseg+1, elem_ptr[0] = 0 < ... < elem_ptr[nseg] =

@@ -193,6 +193,22 @@ class Oracle:
                                       C.c_double(scale), _ptr(d))
         return d
 
+    def xpt_sens(self, vars_, which, coef=1.0):
+        u = np.ascontiguousarray(vars_, np.float64)
+        d = np.zeros(3 * self.P.nnodes)
+        self.L.or_add_xpt_sens(C.byref(self.P), _ptr(u), int(which),
+                               C.c_double(coef), _ptr(d))
+        return d
+
+    def adj_res_xpt_product(self, vars_, psi, scale=1.0, lam=1.0):
+        u = np.ascontiguousarray(vars_, np.float64)
+        ps = np.ascontiguousarray(psi, np.float64)
+        d = np.zeros(3 * self.P.nnodes)
+        self.L.or_add_adj_res_xpt_product(C.byref(self.P), _ptr(u), _ptr(ps),
+                                          C.c_double(scale), C.c_double(lam),
+                                          _ptr(d))
+        return d
+
     def static_adjoint(self, force, m=100, nrestart=2, rtol=1e-12,
                        atol=1e-30, grads=True):
         f = np.ascontiguousarray(force, np.float64)

@@ -13,7 +13,8 @@
     2. the linear static solve R(u) = K u - f = 0 with GMRES + ILU(0);
     3. compliance and KS failure, their state sensitivities, the adjoint
        solve with the transposed assembly, and the total derivative
-       dfdx + (-1) * psi^T dR/dx.
+       dfdx + (-1) * psi^T dR/dx, and the same for the node coordinates
+       (addXptSens + addAdjointResXptSensProducts).
 */
 #include "ref_problem.h"
 
@@ -73,6 +74,11 @@ int main(int argc, char **argv) {
     dfdu[k]->incref();
     psi[k]->incref();
     dfdx[k]->incref();
+  }
+  TACSBVec *dfdX[2];
+  for (int k = 0; k < 2; k++) {
+    dfdX[k] = as->createNodeVec();
+    dfdX[k]->incref();
   }
   TacsScalar *arr;
 
@@ -138,6 +144,22 @@ int main(int argc, char **argv) {
       dfdx[0]->getArray(&arr);
       w.f64("adjres_test", arr, ndv);
     }
+
+    // Node-coordinate sensitivities at the prescribed state (exact in the
+    // complex build: the shell and load elements difference by complex
+    // step, the solid element is analytic)
+    for (int k = 0; k < 2; k++) dfdX[k]->zeroEntries();
+    as->addXptSens(1.0, 2, funcs, dfdX);
+    dfdX[0]->getArray(&arr);
+    w.f64("dfdX_test_comp", arr, 3 * m.nnodes);
+    dfdX[1]->getArray(&arr);
+    w.f64("dfdX_test_ks", arr, 3 * m.nnodes);
+    if (!psi_test.empty()) {
+      dfdX[0]->zeroEntries();
+      as->addAdjointResXptSensProducts(1.0, 1, psi, dfdX);
+      dfdX[0]->getArray(&arr);
+      w.f64("adjxpt_test", arr, 3 * m.nnodes);
+    }
   }
 
   // ---- 2. linear static solve -------------------------------------------
@@ -196,6 +218,15 @@ int main(int argc, char **argv) {
   w.f64("grad_comp", arr, ndv);
   dfdx[1]->getArray(&arr);
   w.f64("grad_ks", arr, ndv);
+
+  // total node-coordinate derivatives df/dX - psi^T dR/dX at the solution
+  for (int k = 0; k < 2; k++) dfdX[k]->zeroEntries();
+  as->addXptSens(1.0, 2, funcs, dfdX);
+  as->addAdjointResXptSensProducts(-1.0, 2, psi, dfdX);
+  dfdX[0]->getArray(&arr);
+  w.f64("grad_xpt_comp", arr, 3 * m.nnodes);
+  dfdX[1]->getArray(&arr);
+  w.f64("grad_xpt_ks", arr, 3 * m.nnodes);
 
   TacsFinalize();
   MPI_Finalize();

@@ -629,12 +629,11 @@ static void free_load_index(load_index *L) {
 }
 
 /* Element residual including its aux loads scaled by lambda
-   (TACSAssembler::assembleRes, TACSAssembler.cpp:4176-4225) */
-static void elem_residual(const or_problem *p, const load_index *L, int e,
-                          const double *vars, double lambda, double *res) {
-  double X[24], u[24];
-  gather(p, e, p->xpts, 3, X);
-  gather(p, e, vars, vpn_of(p), u);
+   (TACSAssembler::assembleRes, TACSAssembler.cpp:4176-4225), at element
+   coordinates X and element variables u. */
+static void elem_residual_at(const or_problem *p, const load_index *L, int e,
+                             const double *X, const double *u, double lambda,
+                             double *res) {
   memset(res, 0, 24 * sizeof(double));
   double t = p->thick[e];
   double aux[24];
@@ -654,6 +653,13 @@ static void elem_residual(const or_problem *p, const load_index *L, int e,
     }
   }
   for (int k = 0; k < 24; k++) res[k] += lambda * aux[k];
+}
+static void elem_residual(const or_problem *p, const load_index *L, int e,
+                          const double *vars, double lambda, double *res) {
+  double X[24], u[24];
+  gather(p, e, p->xpts, 3, X);
+  gather(p, e, vars, vpn_of(p), u);
+  elem_residual_at(p, L, e, X, u, lambda, res);
 }
 
 /* ------------------------------ threading ------------------------------ */
@@ -1506,6 +1512,118 @@ void or_add_adj_res_product(const or_problem *p, const double *vars,
     }
     dfdx[p->dvnum[el]] += acc;
   }
+}
+
+/* ------------------- node-coordinate sensitivities -------------------
+   Central differences of the element terms in each element coordinate,
+   step h = 1e-6 times the element's largest coordinate extent.  The
+   reference's own default for the shell and load elements is the same
+   difference taken forward (TACSElement::addAdjResXptProduct,
+   TACSElement.cpp:270; addPointQuantityXptSens, :746) or by complex step
+   in its complex build. */
+static double elem_extent(const double *X, int npe) {
+  double ext = 0.0;
+  for (int d = 0; d < 3; d++) {
+    double lo = X[d], hi = X[d];
+    for (int m = 1; m < npe; m++) {
+      if (X[3 * m + d] < lo) lo = X[3 * m + d];
+      if (X[3 * m + d] > hi) hi = X[3 * m + d];
+    }
+    if (hi - lo > ext) ext = hi - lo;
+  }
+  return ext;
+}
+
+/* Function terms of one element at coordinates X: which = 0 compliance
+   sum_q detXd e.s; which = 1 the KS sum sum_q detXd e^{rho (f - mx)} / (rho
+   ksum), whose derivative is TACSKSFailure::getElementXptSens
+   (TACSKSFailure.cpp:289-340) with dfdq, dfddetXd at their values. */
+static double elem_func_at(const or_problem *p, int el, const double *X,
+                           const double *u, int which, double mx,
+                           double ksum) {
+  double acc = 0.0;
+  double e[9];
+  if (p->elem_type == 0) {
+    shell_geo g;
+    shell_geometry(X, p, &g);
+    for (int q = 0; q < 4; q++) {
+      shell_strain(g.B[q], u, e);
+      e[8] = 0.0;
+      if (which == 0)
+        acc += g.detXd[q] * point_sed(p, p->thick[el], e, NULL);
+      else
+        acc += g.detXd[q] *
+               exp(p->ks_weight *
+                   (point_failure(p, p->thick[el], e, NULL, NULL) - mx));
+    }
+  } else {
+    hex_geo g;
+    hex_geometry(X, &g);
+    for (int q = 0; q < 8; q++) {
+      hex_strain(g.Nx[q], u, e);
+      if (which == 0)
+        acc += g.detXd[q] * point_sed(p, p->thick[el], e, NULL);
+      else
+        acc += g.detXd[q] *
+               exp(p->ks_weight *
+                   (point_failure(p, p->thick[el], e, NULL, NULL) - mx));
+    }
+  }
+  return which == 0 ? acc : acc / (p->ks_weight * ksum);
+}
+
+/* TACSAssembler::addXptSens (TACSAssembler.cpp:4858-4920) */
+void or_add_xpt_sens(const or_problem *p, const double *vars, int which,
+                     double coef, double *dfdX) {
+  double mx = 0.0, ksum = 1.0;
+  if (which == 1) ks_stats(p, vars, &mx, &ksum);
+  const int npe = npe_of(p);
+  for (int el = 0; el < p->nelem; el++) {
+    double X[24], u[24];
+    gather(p, el, p->xpts, 3, X);
+    gather(p, el, vars, vpn_of(p), u);
+    const double h = 1e-6 * elem_extent(X, npe);
+    for (int k = 0; k < 3 * npe; k++) {
+      const double x0 = X[k];
+      X[k] = x0 + h;
+      const double fp = elem_func_at(p, el, X, u, which, mx, ksum);
+      X[k] = x0 - h;
+      const double fm = elem_func_at(p, el, X, u, which, mx, ksum);
+      X[k] = x0;
+      dfdX[3 * (size_t)p->conn[npe * el + k / 3] + k % 3] +=
+          coef * (fp - fm) / (2.0 * h);
+    }
+  }
+}
+
+/* TACSAssembler::addAdjointResXptSensProducts (TACSAssembler.cpp:
+   5136-5205): element residual and its loads (scaled by lambda) */
+void or_add_adj_res_xpt_product(const or_problem *p, const double *vars,
+                                const double *psi, double scale,
+                                double lambda, double *dfdX) {
+  load_index L;
+  build_load_index(p, &L);
+  const int npe = npe_of(p), vpn = vpn_of(p), nv = npe * vpn;
+  for (int el = 0; el < p->nelem; el++) {
+    double X[24], u[24], ps[24], rp[24], rm[24];
+    gather(p, el, p->xpts, 3, X);
+    gather(p, el, vars, vpn, u);
+    gather(p, el, psi, vpn, ps);
+    const double h = 1e-6 * elem_extent(X, npe);
+    for (int k = 0; k < 3 * npe; k++) {
+      const double x0 = X[k];
+      X[k] = x0 + h;
+      elem_residual_at(p, &L, el, X, u, lambda, rp);
+      X[k] = x0 - h;
+      elem_residual_at(p, &L, el, X, u, lambda, rm);
+      X[k] = x0;
+      double d = 0.0;
+      for (int i = 0; i < nv; i++) d += ps[i] * (rp[i] - rm[i]);
+      dfdX[3 * (size_t)p->conn[npe * el + k / 3] + k % 3] +=
+          scale * d / (2.0 * h);
+    }
+  }
+  free_load_index(&L);
 }
 
 /* The full static-solve + adjoint-gradient step, following

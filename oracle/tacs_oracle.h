@@ -93,6 +93,12 @@ void or_add_dv_sens(const or_problem *p, const double *vars, int which,
                     double scale, double *dfdx);
 void or_add_adj_res_product(const or_problem *p, const double *vars,
                             const double *psi, double scale, double *dfdx);
+/* Node-coordinate sensitivities (3 per node), central differences */
+void or_add_xpt_sens(const or_problem *p, const double *vars, int which,
+                     double coef, double *dfdX);
+void or_add_adj_res_xpt_product(const or_problem *p, const double *vars,
+                                const double *psi, double scale,
+                                double lambda, double *dfdX);
 
 /* Convenience: full static solve + both gradients (the timed CPU step). */
 int or_static_adjoint(const or_problem *p, int m, int nrestart, double rtol,

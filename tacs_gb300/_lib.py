@@ -50,6 +50,9 @@ SIGNATURES = [
     ("tg_add_dv_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),
     ("tg_add_adjoint_res_products", _I, [_P, _P, _D, _I, _P, _P, _P]),
     ("tg_add_total_derivative", _I, [_P, _P, _I, _D, _P, _D, _P, _P]),
+    ("tg_add_xpt_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),
+    ("tg_add_adjoint_res_xpt_products", _I, [_P, _P, _D, _I, _P, _P, _D, _P]),
+    ("tg_add_total_xpt_derivative", _I, [_P, _P, _I, _D, _P, _D, _P, _P]),
     ("tg_mat_create", _I, [_P, C.POINTER(_P)]),
     ("tg_mat_decref", _I, [_P]),
     ("tg_mat_get_arrays", _I, [_P, _IP, _IP, C.POINTER(_P), C.POINTER(_P),

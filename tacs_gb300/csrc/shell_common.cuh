@@ -1,6 +1,9 @@
 // Device helpers of the MITC4 shell kernels (TACSQuad4Shell kinematics,
 // TACSIsoShellConstitutive, point quantities).  Included by the shell
-// kernel translation units inside namespace tg::<anonymous>.
+// kernel translation units inside namespace tg::<anonymous>.  The helpers
+// that depend on the node coordinates are templates over the scalar type:
+// double for assembly and the point quantities, ad::Dual for the
+// node-coordinate sensitivities.
 #pragma once
 
 // TacsGaussQuadPts2 (src/elements/basis/TACSGaussQuadrature.h:26)
@@ -10,21 +13,24 @@ __device__ __forceinline__ double gauss2(int i) {
   return i ? TG_GPT : -TG_GPT;
 }
 
-__device__ __forceinline__ double dot3(const double *a, const double *b) {
+template <class A, class B>
+__device__ __forceinline__ auto dot3(const A *a, const B *b)
+    -> decltype(a[0] * b[0]) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
-__device__ __forceinline__ void cross3(const double *x, const double *y,
-                                       double *o) {
+template <class R>
+__device__ __forceinline__ void cross3(const R *x, const R *y, R *o) {
   o[0] = x[1] * y[2] - x[2] * y[1];
   o[1] = x[2] * y[0] - x[0] * y[2];
   o[2] = x[0] * y[1] - x[1] * y[0];
 }
 // inv3x3 (src/elements/TACSElementAlgebra.h:1980)
-__device__ double inv3(const double *A, double *Ai) {
-  double det = (A[8] * (A[0] * A[4] - A[3] * A[1]) -
-                A[7] * (A[0] * A[5] - A[3] * A[2]) +
-                A[6] * (A[1] * A[5] - A[2] * A[4]));
-  double di = 1.0 / det;
+template <class R>
+__device__ R inv3(const R *A, R *Ai) {
+  R det = (A[8] * (A[0] * A[4] - A[3] * A[1]) -
+           A[7] * (A[0] * A[5] - A[3] * A[2]) +
+           A[6] * (A[1] * A[5] - A[2] * A[4]));
+  R di = 1.0 / det;
   Ai[0] = (A[4] * A[8] - A[5] * A[7]) * di;
   Ai[1] = -(A[1] * A[8] - A[2] * A[7]) * di;
   Ai[2] = (A[1] * A[5] - A[2] * A[4]) * di;
@@ -36,8 +42,8 @@ __device__ double inv3(const double *A, double *Ai) {
   Ai[8] = (A[0] * A[4] - A[1] * A[3]) * di;
   return det;
 }
-__device__ __forceinline__ void mm3(const double *A, const double *B,
-                                    double *C) {
+template <class RA, class RB, class RC>
+__device__ __forceinline__ void mm3(const RA *A, const RB *B, RC *C) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -45,8 +51,8 @@ __device__ __forceinline__ void mm3(const double *A, const double *B,
       C[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] +
                      A[3 * i + 2] * B[6 + j];
 }
-__device__ __forceinline__ void mmT3(const double *A, const double *B,
-                                     double *C) {
+template <class RA, class RB, class RC>
+__device__ __forceinline__ void mmT3(const RA *A, const RB *B, RC *C) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -63,11 +69,12 @@ __device__ __forceinline__ void shape2(double xi, double eta, double *N,
   Na[0] = -0.5 * nb0; Na[1] = 0.5 * nb0; Na[2] = -0.5 * nb1; Na[3] = 0.5 * nb1;
   Nb[0] = na0 * -0.5; Nb[1] = na1 * -0.5; Nb[2] = na0 * 0.5; Nb[3] = na1 * 0.5;
 }
+template <class R>
 __device__ __forceinline__ void grad3(const double *Na, const double *Nb,
-                                      const double *X, double *Xxi) {
+                                      const R *X, R *Xxi) {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    double a = 0.0, b = 0.0;
+    R a = 0.0, b = 0.0;
 #pragma unroll
     for (int m = 0; m < 4; m++) {
       a += Na[m] * X[3 * m + k];
@@ -77,18 +84,18 @@ __device__ __forceinline__ void grad3(const double *Na, const double *Nb,
     Xxi[2 * k + 1] = b;
   }
 }
-__device__ __forceinline__ void interp3(const double *N, const double *X,
-                                        double *o) {
+template <class R>
+__device__ __forceinline__ void interp3(const double *N, const R *X, R *o) {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    double a = 0.0;
+    R a = 0.0;
 #pragma unroll
     for (int m = 0; m < 4; m++) a += N[m] * X[3 * m + k];
     o[k] = a;
   }
 }
-__device__ __forceinline__ void frame(const double *Xxi, const double *n,
-                                      double *Xd) {
+template <class R>
+__device__ __forceinline__ void frame(const R *Xxi, const R *n, R *Xd) {
   Xd[0] = Xxi[0]; Xd[1] = Xxi[1]; Xd[2] = n[0];
   Xd[3] = Xxi[2]; Xd[4] = Xxi[3]; Xd[5] = n[1];
   Xd[6] = Xxi[4]; Xd[7] = Xxi[5]; Xd[8] = n[2];
@@ -96,34 +103,36 @@ __device__ __forceinline__ void frame(const double *Xxi, const double *n,
 // TACSShellNaturalTransform / TACSShellRefAxisTransform::computeTransform
 // (src/elements/shell/TACSShellElementTransform.h:24-93, 95-160), including
 // the natural transform's three-fold subtraction of d*n[0] from t1[0].
-__device__ void shell_transform(const ElemParams &ep, const double *Xxi,
-                                const double *n0, double *T) {
-  double n[3] = {n0[0], n0[1], n0[2]};
-  double inv = 1.0 / sqrt(dot3(n, n));
+template <class R>
+__device__ void shell_transform(const ElemParams &ep, const R *Xxi,
+                                const R *n0, R *T) {
+  R n[3] = {n0[0], n0[1], n0[2]};
+  R inv = 1.0 / sqrt(dot3(n, n));
   n[0] *= inv; n[1] *= inv; n[2] *= inv;
-  double t1[3];
+  R t1[3];
   if (ep.transform == 0) {
     t1[0] = Xxi[0]; t1[1] = Xxi[2]; t1[2] = Xxi[4];
-    double d = dot3(n, t1);
+    R d = dot3(n, t1);
     t1[0] = t1[0] - d * n[0];
     t1[0] = t1[0] - d * n[0];
     t1[0] = t1[0] - d * n[0];
   } else {
-    double an = dot3(ep.ref_axis, n);
+    R an = dot3(ep.ref_axis, n);
     t1[0] = ep.ref_axis[0] - an * n[0];
     t1[1] = ep.ref_axis[1] - an * n[1];
     t1[2] = ep.ref_axis[2] - an * n[2];
   }
   inv = 1.0 / sqrt(dot3(t1, t1));
   t1[0] *= inv; t1[1] *= inv; t1[2] *= inv;
-  double t2[3];
+  R t2[3];
   cross3(n, t1, t2);
   T[0] = t1[0]; T[3] = t1[1]; T[6] = t1[2];
   T[1] = t2[0]; T[4] = t2[1]; T[7] = t2[2];
   T[2] = n[0];  T[5] = n[1];  T[8] = n[2];
 }
 // director map d = q x fn: entry (i, b) of the 3x3 map for node m
-__device__ __forceinline__ double dmap(const double *f, int i, int b) {
+template <class R>
+__device__ __forceinline__ R dmap(const R *f, int i, int b) {
   // rows: [0, f2, -f1], [-f2, 0, f0], [f1, -f0, 0]
   if (i == b) return 0.0;
   if (i == 0) return b == 1 ? f[2] : -f[1];
@@ -167,8 +176,9 @@ __device__ __forceinline__ ShellStiff shell_stiff(const ElemParams &ep,
   return c;
 }
 // TACSShellConstitutive::computeStress (TACSShellConstitutive.h:133-155)
-__device__ __forceinline__ double shell_stress_row(const ShellStiff &c,
-                                                   const double *e, int r) {
+template <class R>
+__device__ __forceinline__ R shell_stress_row(const ShellStiff &c, const R *e,
+                                              int r) {
   switch (r) {
     case 0: return c.A[0] * e[0] + c.A[1] * e[1] + c.A[2] * e[2];
     case 1: return c.A[1] * e[0] + c.A[3] * e[1] + c.A[4] * e[2];
@@ -200,16 +210,19 @@ __device__ __forceinline__ int find_slot(const int *rowp, const int *cols,
 // (TACSShellElement::evalPointQuantity, TACSShellElement.h:1015-1072):
 // failure value (TACSIsoShellConstitutive::evalFailure, .cpp:254-300),
 // detXd, and sum_q detXd_q e.s (strain energy, TACSCompliance).
-struct FailOut {
-  double f, dfde[6], dfdt;
+template <class R>
+struct FailOutT {
+  R f, dfde[6], dfdt;
 };
-__device__ FailOut shell_failure(const ElemParams &ep, double t,
-                                 const double *e) {
-  FailOut o;
+using FailOut = FailOutT<double>;
+template <class R>
+__device__ FailOutT<R> shell_failure(const ElemParams &ep, double t,
+                                     const R *e) {
+  FailOutT<R> o;
   double Dm = ep.E / (1.0 - ep.nu * ep.nu);
   double A0[6] = {Dm, ep.nu * Dm, 0.0, Dm, 0.0, 0.5 * ep.E / (1.0 + ep.nu)};
   double ht = 0.5 * t, hb = -(0.5) * t;
-  double et[3], eb[3], st[3], sb[3];
+  R et[3], eb[3], st[3], sb[3];
   for (int i = 0; i < 3; i++) {
     et[i] = e[i] + ht * e[3 + i];
     eb[i] = e[i] + hb * e[3 + i];
@@ -221,11 +234,11 @@ __device__ FailOut shell_failure(const ElemParams &ep, double t,
   sb[1] = A0[1] * eb[0] + A0[3] * eb[1] + A0[4] * eb[2];
   sb[2] = A0[2] * eb[0] + A0[4] * eb[1] + A0[5] * eb[2];
   // vonMisesFailure2D / StressSens (TACSMaterialProperties.cpp:481-500)
-  double ftop = sqrt(st[0] * st[0] + st[1] * st[1] - st[0] * st[1] +
+  R ftop = sqrt(st[0] * st[0] + st[1] * st[1] - st[0] * st[1] +
                      3.0 * st[2] * st[2]);
-  double fbot = sqrt(sb[0] * sb[0] + sb[1] * sb[1] - sb[0] * sb[1] +
+  R fbot = sqrt(sb[0] * sb[0] + sb[1] * sb[1] - sb[0] * sb[1] +
                      3.0 * sb[2] * sb[2]);
-  double pt[3] = {0, 0, 0}, pb[3] = {0, 0, 0};
+  R pt[3] = {0.0, 0.0, 0.0}, pb[3] = {0.0, 0.0, 0.0};
   if (ftop != 0.0) {
     pt[0] = (st[0] - 0.5 * st[1]) / (ftop * ep.ys);
     pt[1] = (st[1] - 0.5 * st[0]) / (ftop * ep.ys);
@@ -236,13 +249,13 @@ __device__ FailOut shell_failure(const ElemParams &ep, double t,
     pb[1] = (sb[1] - 0.5 * sb[0]) / (fbot * ep.ys);
     pb[2] = (3.0 * sb[2]) / (fbot * ep.ys);
   }
-  double top = ftop / ep.ys, bot = fbot / ep.ys;
-  double mx = (top > bot) ? top : bot;
+  R top = ftop / ep.ys, bot = fbot / ep.ys;
+  R mx = (top > bot) ? top : bot;
   const double ksw = 100.0;  // TACSIsoShellConstitutive.cpp:42
-  double ksum = exp(ksw * (top - mx)) + exp(ksw * (bot - mx));
+  R ksum = exp(ksw * (top - mx)) + exp(ksw * (bot - mx));
   o.f = mx + log(ksum) / ksw;
-  double ft = exp(ksw * (top - mx)) / ksum, fb = exp(ksw * (bot - mx)) / ksum;
-  double phit[3], phib[3];
+  R ft = exp(ksw * (top - mx)) / ksum, fb = exp(ksw * (bot - mx)) / ksum;
+  R phit[3], phib[3];
   phit[0] = A0[0] * pt[0] + A0[1] * pt[1] + A0[2] * pt[2];
   phit[1] = A0[1] * pt[0] + A0[3] * pt[1] + A0[4] * pt[2];
   phit[2] = A0[2] * pt[0] + A0[4] * pt[1] + A0[5] * pt[2];

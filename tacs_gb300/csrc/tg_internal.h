@@ -99,6 +99,18 @@ void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
                    int func, KsStats ks, double coef, const double *psi,
                    double scale, double *out, cudaStream_t s);
 
+// Node-coordinate sensitivities of one colour, added into dfdX (3 per
+// node): coef d f/dX for func (TG_FUNC_*, or -1 for none) plus, when psi is
+// set, scale psi^T dR/dX with the loads scaled by lambda.
+void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
+                      const double *vars, int func, KsStats ks, double coef,
+                      const double *psi, double scale, double lambda,
+                      double *dfdX, cudaStream_t s);
+void launch_hex_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
+                    const double *vars, int func, KsStats ks, double coef,
+                    const double *psi, double scale, double lambda,
+                    double *dfdX, cudaStream_t s);
+
 // ------------------------------------------------------- BCSR / vectors
 // nrhs vectors ld apart (ld may be 0 when nrhs == 1)
 void launch_bcsr_mult(int bsize, int nrows, const int *rowp, const int *cols,

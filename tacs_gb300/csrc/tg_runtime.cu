@@ -552,6 +552,74 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
   return elem_dv_pass(a, vars, func, coef, psi, scale, dfdx, S(s));
 }
 
+// ------------------------------------------ node-coordinate sensitivities
+static int xpt_pass(tg_assembler *a, const double *vars, int func, double coef,
+                    const double *psi, double scale, double lambda,
+                    double *dfdX, cudaStream_t s) {
+  const MeshView m = a->view();
+  for (int c = 0; c < a->ncolors(); c++) {
+    if (a->ep.elem_type == TG_ELEM_MITC4)
+      launch_shell_xpt(a->ep, m, a->color(c), vars, func, a->ks, coef, psi,
+                       scale, lambda, dfdX, s);
+    else
+      launch_hex_xpt(a->ep, m, a->color(c), vars, func, a->ks, coef, psi,
+                     scale, lambda, dfdX, s);
+  }
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_add_xpt_sens(tg_assembler *a, const double *vars, int nfuncs,
+                    const int *funcs, double coef, double **dfdX, void *s) {
+  int rc = check_ready(a, "tg_add_xpt_sens");
+  if (rc) return rc;
+  if (!vars || nfuncs < 0 || (nfuncs > 0 && (!funcs || !dfdX)))
+    return fail(TG_ERR_ARG, "tg_add_xpt_sens: bad arguments");
+  for (int i = 0; i < nfuncs; i++) {
+    if (funcs[i] != TG_FUNC_COMPLIANCE && funcs[i] != TG_FUNC_KS_FAILURE)
+      return fail(TG_ERR_ARG, "tg_add_xpt_sens: unknown function");
+    if (funcs[i] == TG_FUNC_KS_FAILURE && !a->ks_valid)
+      return fail(TG_ERR_STATE,
+                  "tg_add_xpt_sens: evaluate the KS function first");
+    if (!dfdX[i]) return fail(TG_ERR_ARG, "tg_add_xpt_sens: NULL output");
+    if ((rc = xpt_pass(a, vars, funcs[i], coef, nullptr, 0.0, 0.0, dfdX[i],
+                       S(s))))
+      return rc;
+  }
+  return 0;
+}
+
+int tg_add_adjoint_res_xpt_products(tg_assembler *a, const double *vars,
+                                    double scale, int nadj, const double **psi,
+                                    double **dfdX, double lambda, void *s) {
+  int rc = check_ready(a, "tg_add_adjoint_res_xpt_products");
+  if (rc) return rc;
+  if (!vars || nadj < 0 || (nadj > 0 && (!psi || !dfdX)))
+    return fail(TG_ERR_ARG, "tg_add_adjoint_res_xpt_products: bad arguments");
+  for (int k = 0; k < nadj; k++) {
+    if (!psi[k] || !dfdX[k])
+      return fail(TG_ERR_ARG, "tg_add_adjoint_res_xpt_products: NULL vector");
+    if ((rc = xpt_pass(a, vars, -1, 0.0, psi[k], scale, lambda, dfdX[k],
+                       S(s))))
+      return rc;
+  }
+  return 0;
+}
+
+int tg_add_total_xpt_derivative(tg_assembler *a, const double *vars, int func,
+                                double coef, const double *psi, double scale,
+                                double *dfdX, void *s) {
+  int rc = check_ready(a, "tg_add_total_xpt_derivative");
+  if (rc) return rc;
+  if (!vars || !dfdX)
+    return fail(TG_ERR_ARG, "tg_add_total_xpt_derivative: NULL");
+  if (func != TG_FUNC_COMPLIANCE && func != TG_FUNC_KS_FAILURE)
+    return fail(TG_ERR_ARG, "tg_add_total_xpt_derivative: unknown function");
+  if (func == TG_FUNC_KS_FAILURE && !a->ks_valid)
+    return fail(TG_ERR_STATE, "evaluate the KS function first");
+  return xpt_pass(a, vars, func, coef, psi, scale, 1.0, dfdX, S(s));
+}
+
 // ------------------------------------------------------ element segments
 int tg_assembler_set_segments(tg_assembler *a, int nseg,
                               const int *elem_ptr) {

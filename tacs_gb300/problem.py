@@ -302,6 +302,35 @@ class GpuModel:
     def dv_vec(self):
         return torch.zeros(self.ndv, dtype=torch.float64, device="cuda")
 
+    # ------------------------------------- node-coordinate sensitivities
+    def node_vec(self):
+        """Zero node vector, 3 per node (TACSAssembler::createNodeVec)."""
+        return torch.zeros(3 * self.nnodes, dtype=torch.float64, device="cuda")
+
+    def add_xpt_sens(self, u, funcs, dfdX, coef=1.0):
+        """dfdX[i] += coef d f_i / dX (TACSAssembler::addXptSens)."""
+        f = np.ascontiguousarray(funcs, np.int32)
+        ptrs = (C.c_void_p * len(f))(*[t.data_ptr() for t in dfdX])
+        check(_lib.lib().tg_add_xpt_sens(self.handle, _p(u), len(f),
+                                         f.ctypes.data, coef, ptrs,
+                                         _stream()), "tg_add_xpt_sens")
+
+    def add_adjoint_res_xpt_products(self, u, psis, dfdX, scale=1.0,
+                                     lam=1.0):
+        """dfdX[k] += scale psi_k^T dR/dX
+        (TACSAssembler::addAdjointResXptSensProducts)."""
+        pp = (C.c_void_p * len(psis))(*[t.data_ptr() for t in psis])
+        dp = (C.c_void_p * len(dfdX))(*[t.data_ptr() for t in dfdX])
+        check(_lib.lib().tg_add_adjoint_res_xpt_products(
+            self.handle, _p(u), scale, len(psis), pp, dp, lam, _stream()),
+            "tg_add_adjoint_res_xpt_products")
+
+    def add_total_xpt_derivative(self, u, func, psi, dfdX, coef=1.0,
+                                 scale=-1.0):
+        check(_lib.lib().tg_add_total_xpt_derivative(
+            self.handle, _p(u), int(func), coef, _p(psi), scale, _p(dfdX),
+            _stream()), "tg_add_total_xpt_derivative")
+
     # ------------------------------------------------ element segments
     def set_segments(self, elem_ptr):
         ep = np.ascontiguousarray(elem_ptr, np.int32)
@@ -353,7 +382,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     u = -ans
     iters, flags = [ksm.iters], [flag]
     fvals = model.eval_functions(u, funcs)
-    grads = []
+    grads, psis = [], []
     for k, fn in enumerate(funcs):
         dfdu = model.vec()
         model.add_sv_sens(u, [fn], [dfdu])
@@ -364,8 +393,9 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
         g = model.dv_vec()
         model.add_total_derivative(u, fn, psi, g, 1.0, -1.0)
         grads.append(g)
-    return dict(u=u, funcs=fvals, grads=grads, flag=flag, flags=flags,
-                iters=iters, mat=mat, pc=pc, ksm=ksm)
+        psis.append(psi)
+    return dict(u=u, funcs=fvals, grads=grads, psis=psis, flag=flag,
+                flags=flags, iters=iters, mat=mat, pc=pc, ksm=ksm)
 
 
 def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,

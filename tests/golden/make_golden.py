@@ -11,6 +11,13 @@ Run here (where the reference sources are present):
     make -C oracle/ref REF=<path to tacs>
     python tests/golden/make_golden.py
 
+The node-coordinate sensitivities come from the reference's complex build
+(``make -C oracle/ref REF=<path to tacs> cplx``), whose shell and load
+elements form them by complex step and so exactly; they are added to the
+stored fixtures with
+
+    python tests/golden/make_golden.py --xpt [case ...]
+
 The fixtures are committed; the GPU machine never needs the reference.
 """
 from __future__ import annotations
@@ -29,6 +36,9 @@ sys.path.insert(0, ROOT)
 from tacs_gb300 import meshes  # noqa: E402
 
 GEN = os.path.join(ROOT, "oracle", "_ref", "gen_golden")
+GEN_CPLX = os.path.join(ROOT, "oracle", "_ref", "gen_golden_cplx")
+XPT_KEYS = ("dfdX_test_comp", "dfdX_test_ks", "adjxpt_test", "grad_xpt_comp",
+            "grad_xpt_ks")
 
 INT_KEYS = {"elem_type", "nnodes", "nelem", "conn", "dvnum", "transform",
             "bc_nodes", "bc_masks", "pres_elems", "trac_elems", "trac_faces",
@@ -71,11 +81,11 @@ def read_tgarr(path):
     return out
 
 
-def run_reference(prob):
+def run_reference(prob, gen=GEN):
     with tempfile.TemporaryDirectory() as td:
         pin, pout = os.path.join(td, "p.bin"), os.path.join(td, "o.bin")
         write_tgarr(pin, prob)
-        subprocess.run([GEN, pin, pout], check=True)
+        subprocess.run([gen, pin, pout], check=True)
         return read_tgarr(pout)
 
 
@@ -274,5 +284,24 @@ def main(names=None):
               f" size={os.path.getsize(path)}")
 
 
+def add_xpt(names=None):
+    """Run the complex build on each stored fixture's inputs and add its
+    node-coordinate sensitivities as ref_<key>."""
+    for name in (names or CASES):
+        path = os.path.join(HERE, name + ".npz")
+        rec = dict(np.load(path))
+        prob = {k[3:]: v for k, v in rec.items() if k.startswith("in_")}
+        ref = run_reference(prob, GEN_CPLX)
+        for k in XPT_KEYS:
+            if k in ref:
+                rec["ref_" + k] = ref[k]
+        np.savez_compressed(path, **rec)
+        print(name, {k: float(np.abs(ref[k]).max()) for k in XPT_KEYS
+                     if k in ref})
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or None)
+    if sys.argv[1:2] == ["--xpt"]:
+        add_xpt(sys.argv[2:] or None)
+    else:
+        main(sys.argv[1:] or None)

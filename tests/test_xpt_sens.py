@@ -1,0 +1,152 @@
+"""Node-coordinate (shape) sensitivities: TACSAssembler::addXptSens and
+addAdjointResXptSensProducts (src/TACSAssembler.cpp:4858,5136).
+
+The fixtures hold the reference's complex-step values (its complex build,
+dh = 1e-30, i.e. exact derivatives); the GPU kernels differentiate in dual
+arithmetic, so the bar is rounding level:
+  element-level dfdX and psi^T dR/dX: 1e-10 (norm-wise);
+  total derivatives df/dX - psi^T dR/dX at the reference solution and
+  adjoints: 1e-7 (the two terms cancel by up to 1e6);
+  GPU against the central-difference oracle: 1e-7, KS 5e-6 (difference
+  truncation and rounding of the oracle);
+  the oracle against the fixtures (CPU): 1e-8, KS 5e-6;
+  GPU total derivative against central differences of GPU static solves:
+  1e-5 of the largest gradient entry.
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, load_case, rel
+
+XPT_TOL = 1e-10
+TOTAL_TOL = 1e-7
+FD_TOL, FD_KS_TOL = 1e-7, 5e-6
+
+XPT_CASES = [c for c in CASES if "u_test" in load_case(c)[0]]
+
+
+# ------------------------------------------------------------ CPU: oracle
+@pytest.mark.parametrize("name", XPT_CASES)
+def test_oracle_xpt_against_reference(name):
+    import oracle
+    prob, ref = load_case(name)
+    o = oracle.Oracle(prob)
+    u = prob["u_test"]
+    assert rel(o.xpt_sens(u, 0), ref["dfdX_test_comp"]) < 1e-8
+    assert rel(o.xpt_sens(u, 1), ref["dfdX_test_ks"]) < FD_KS_TOL
+    assert rel(o.adj_res_xpt_product(u, prob["psi_test"]),
+               ref["adjxpt_test"]) < 1e-8
+
+
+# ------------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import problem
+    return problem
+
+
+def _h(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", XPT_CASES)
+def test_xpt_element_level(gpu, name):
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    u = M.vec(prob["u_test"])
+    M.eval_functions(u)
+    dc, dk = M.node_vec(), M.node_vec()
+    M.add_xpt_sens(u, [0, 1], [dc, dk])
+    assert rel(_h(dc), ref["dfdX_test_comp"]) < XPT_TOL
+    assert rel(_h(dk), ref["dfdX_test_ks"]) < XPT_TOL
+    xa = M.node_vec()
+    M.add_adjoint_res_xpt_products(u, [M.vec(prob["psi_test"])], [xa])
+    assert rel(_h(xa), ref["adjxpt_test"]) < XPT_TOL
+    # coefficients scale linearly, contributions add
+    xb = M.node_vec()
+    M.add_adjoint_res_xpt_products(u, [M.vec(prob["psi_test"])], [xb],
+                                   scale=-2.0)
+    M.add_xpt_sens(u, [0], [xb], coef=3.0)
+    expect = 3.0 * ref["dfdX_test_comp"] - 2.0 * ref["adjxpt_test"]
+    assert rel(_h(xb), expect) < XPT_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_xpt_total_at_reference_solution(gpu, name):
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    u = M.vec(ref["u"])
+    M.eval_functions(u)
+    for fn, key in ((0, "comp"), (1, "ks")):
+        g = M.node_vec()
+        M.add_total_xpt_derivative(u, fn, M.vec(ref["psi_" + key]), g,
+                                   1.0, -1.0)
+        assert rel(_h(g), ref["grad_xpt_" + key]) < TOTAL_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["shell", "hex"])
+def test_xpt_against_oracle(gpu, kind):
+    import oracle
+    from tacs_gb300 import meshes
+    if kind == "shell":
+        prob = meshes.clamped_plate(12)
+        prob["xpts"] = prob["xpts"].copy()
+        rng = np.random.default_rng(11)
+        prob["xpts"][2::3] += 0.01 * rng.standard_normal(prob["nnodes"])
+    else:
+        prob = meshes.hex_c3(8, 8, 4, traction=-1e6, half=0.3)
+    rng = np.random.default_rng(5)
+    vpn = 6 if prob["elem_type"] == meshes.SHELL else 3
+    n = vpn * prob["nnodes"]
+    u = 1e-3 * rng.standard_normal(n)
+    psi = rng.standard_normal(n)
+    o = oracle.Oracle(prob)
+    M = gpu.GpuModel(prob)
+    uu = M.vec(u)
+    M.eval_functions(uu)
+    dc, dk, xa = M.node_vec(), M.node_vec(), M.node_vec()
+    M.add_xpt_sens(uu, [0, 1], [dc, dk])
+    M.add_adjoint_res_xpt_products(uu, [M.vec(psi)], [xa], lam=0.5)
+    assert rel(_h(dc), o.xpt_sens(u, 0)) < FD_TOL
+    assert rel(_h(dk), o.xpt_sens(u, 1)) < FD_KS_TOL
+    assert rel(_h(xa), o.adj_res_xpt_product(u, psi, lam=0.5)) < FD_TOL
+
+
+@pytest.mark.gpu
+def test_shape_derivative_against_solves(gpu):
+    """d f/dX of a clamped plate under pressure, from one adjoint solve,
+    against central differences of two full GPU static solves per
+    coordinate."""
+    import torch
+    from tacs_gb300 import meshes
+    prob = meshes.clamped_plate(8)
+    M = gpu.GpuModel(prob)
+    r = gpu.static_adjoint(M, prob["force"], 100, 4, 1e-13)
+    assert r["flag"] == 1
+    grads = []
+    for k in range(2):
+        g = M.node_vec()
+        M.add_total_xpt_derivative(r["u"], k, r["psis"][k], g, 1.0, -1.0)
+        grads.append(_h(g))
+    x0 = torch.as_tensor(prob["xpts"], device="cuda").clone()
+    h = 1e-5
+    for node, d in ((30, 0), (40, 1), (22, 0)):
+        j = 3 * node + d
+        fvals = []
+        for sgn in (1.0, -1.0):
+            x = x0.clone()
+            x[j] += sgn * h
+            M.set_nodes(x)
+            rr = gpu.static_adjoint(M, prob["force"], 100, 4, 1e-13)
+            fvals.append(rr["funcs"])
+        M.set_nodes(x0)
+        fd = (fvals[0] - fvals[1]) / (2 * h)
+        for k in range(2):
+            err = abs(fd[k] - grads[k][j]) / np.abs(grads[k]).max()
+            assert err < 1e-5, (node, d, k, fd[k], grads[k][j])
