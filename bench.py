@@ -97,6 +97,8 @@ def adjoint_section(n, torch, colored=False):
         out[label] = {"s_per_gradient": dt, "iters": r["iters"],
                       "converged": [int(f) for f in r["flags"]],
                       "ilu_schedule": r["pc"].schedule()}
+        if label == "fp64_ilu0_natural":
+            out["shape_derivative"] = xpt_timing(M, r, torch)
     ref = grads["fp64_ilu0_natural"]
     for label in [r[0] for r in runs[1:]]:
         out[label]["grad_rel_err_vs_fp64_natural"] = [
@@ -106,6 +108,29 @@ def adjoint_section(n, torch, colored=False):
         out["fp64_ilu0_natural"]["s_per_gradient"]
         / out["mixed_ilu0_natural"]["s_per_gradient"])
     return out, p
+
+
+def xpt_timing(M, r, torch, reps=3):
+    """Node-coordinate total derivative df/dX - psi^T dR/dX of compliance
+    and KS from a solved state and its adjoints (the dual-number
+    addXptSens + addAdjointResXptSensProducts pass), CUDA-event time per
+    function."""
+    u, psis = r["u"], r["psis"]
+    gX = M.node_vec()
+    ms = []
+    for fn in (0, 1):
+        M.eval_functions(u, [fn])
+        M.add_total_xpt_derivative(u, fn, psis[fn], gX)  # warm-up
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            M.add_total_xpt_derivative(u, fn, psis[fn], gX)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1) / reps)
+    return {"ms_per_function": ms,
+            "elements_per_s": [M.nelem / (t / 1e3) for t in ms]}
 
 
 def hex_section(torch, steps=5):
@@ -508,6 +533,19 @@ def main():
         "gpu_launches": M.ncolors * args.steps + 2 * args.steps,
         "clocks": clk,
     }
+    if rank == 0:
+        # node-coordinate total derivatives on the same plate at a seeded
+        # state and adjoint (the kernel's cost does not depend on values)
+        g = torch.Generator(device="cuda").manual_seed(7)
+        us = 1e-4 * torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                                generator=g)
+        ps = torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                         generator=g)
+        line["shape_derivative"] = xpt_timing(M, {"u": us, "psis": [ps, ps]},
+                                              torch)
+        line["shape_derivative"]["workload"] = (
+            f"MITC4 plate {args.size}x{args.size}: df/dX - psi^T dR/dX of "
+            "compliance and KS")
     if rank == 0 and args.adj_size > 0:
         adj, padj = adjoint_section(args.adj_size, torch)
         line["adjoint"] = adj

@@ -364,6 +364,36 @@ class TACSAssembler {
                                       numAdjoints, ps.data(), ds.data(), 0),
           "addAdjointResProducts");
   }
+  // TACSAssembler::addXptSens (src/TACSAssembler.cpp:4858): node vectors
+  // from createNodeVec, 3 entries per node
+  void addXptSens(double coef, int numFuncs, TACSFunction **funcs,
+                  TACSBVec **dfdXpt) {
+    for (int i = 0; i < numFuncs; i++) {
+      double f;
+      const int kind = funcs[i]->kind();
+      check(tg_eval_functions(a_, vars_->getArray(), 1, &kind,
+                              funcs[i]->ksWeight(), &f, 0),
+            "addXptSens");
+      double *d = dfdXpt[i]->getArray();
+      check(tg_add_xpt_sens(a_, vars_->getArray(), 1, &kind, coef, &d, 0),
+            "addXptSens");
+    }
+  }
+  // TACSAssembler::addAdjointResXptSensProducts (src/TACSAssembler.cpp:5136)
+  void addAdjointResXptSensProducts(double scale, int numAdjoints,
+                                    TACSBVec **adjoint, TACSBVec **dfdXpt,
+                                    double lambda = 1.0) {
+    std::vector<const double *> ps(numAdjoints);
+    std::vector<double *> ds(numAdjoints);
+    for (int i = 0; i < numAdjoints; i++) {
+      ps[i] = adjoint[i]->getArray();
+      ds[i] = dfdXpt[i]->getArray();
+    }
+    check(tg_add_adjoint_res_xpt_products(a_, vars_->getArray(), scale,
+                                          numAdjoints, ps.data(), ds.data(),
+                                          lambda, 0),
+          "addAdjointResXptSensProducts");
+  }
 
  private:
   int vpn_, nnodes_, nelems_, ndv_ = 0;

@@ -6,7 +6,8 @@ Assembler (create, setElementConnectivity, setElements, addBCs,
 initialize, createVec / createNodeVec / createDesignVec / createMat,
 setNodes, setDesignVars, setVariables, setAuxElements, assembleRes,
 assembleJacobian, applyBCs, evalFunctions, addSVSens, addDVSens,
-addAdjointResProducts), Vec, Mat, Pc, KSM and AuxElements.  Vectors live on
+addAdjointResProducts, addXptSens, addAdjointResXptSensProducts), Vec, Mat,
+Pc, KSM and AuxElements.  Vectors live on
 the GPU; getArray() returns a host copy that is written back to the device
 before the vector is next used, so the reference's ``vec.getArray()[:] =``
 idiom works.  A single process owns the whole model (the comm argument is
@@ -365,3 +366,25 @@ class Assembler:
         self._model.add_adjoint_res_products(
             self._vars._sync(), [a._sync() for a in adjoints],
             [d.dev for d in dfdx], alpha)
+
+    def addXptSens(self, funcs, dfdXpts, alpha=1.0):
+        """Assembler.addXptSens (tacs/TACS.pyx): dfdX += alpha d f / dX."""
+        u = self._vars._sync()
+        self._model.eval_functions(u, [f.kind for f in funcs],
+                                   ks_weight=self._ksw(funcs))
+        for d in dfdXpts:
+            d._sync()
+            d._host = None
+        self._model.add_xpt_sens(u, [f.kind for f in funcs],
+                                 [d.dev for d in dfdXpts], alpha)
+
+    def addAdjointResXptSensProducts(self, adjoints, dfdXpts, alpha=1.0,
+                                     loadScale=1.0):
+        """Assembler.addAdjointResXptSensProducts (tacs/TACS.pyx):
+        dfdX += alpha psi^T dR/dX."""
+        for d in dfdXpts:
+            d._sync()
+            d._host = None
+        self._model.add_adjoint_res_xpt_products(
+            self._vars._sync(), [a._sync() for a in adjoints],
+            [d.dev for d in dfdXpts], alpha, loadScale)

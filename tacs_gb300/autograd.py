@@ -7,7 +7,9 @@ solve K^T psi = df/du with the same factorisation (K is symmetric with the
 reference's row-and-column boundary conditions, so the forward matrix is
 reused as TACSAssembler::assembleJacobian(..., TRANSPOSE) would produce it),
 then df/dx - psi^T dR/dx from the fused addDVSens + addAdjointResProducts
-kernel.  This is the reference's own adjoint recipe
+kernel (and, for node coordinates, df/dX - psi^T dR/dX from the dual-number
+addXptSens + addAdjointResXptSensProducts kernel).  This is the reference's
+own adjoint recipe
 (tests/integration_tests/static_analysis_base_test.py:359-427,
 tacs/problems/static.py:1140-1279) behind torch's autograd.
 
@@ -60,8 +62,10 @@ class StaticSolver:
         self.iters = []
         self.flags = []
 
-    def solve(self, x):
+    def solve(self, x, xpts=None):
         M = self.model
+        if xpts is not None:
+            M.set_nodes(xpts.detach().to(torch.float64).contiguous())
         M.set_design_vars(x.detach().to(torch.float64).contiguous())
         r0 = M.vec()
         M.assemble_jacobian(M.vec(), self.mat, r0)
@@ -88,9 +92,14 @@ class StaticSolver:
         return np.array([[M.eval_functions(self.u[lc], [func])[0]]
                          for lc in range(self.nlc)])
 
-    def gradients(self, func, weights):
-        """sum over (load case, mesh) of weights * d f / d x."""
+    def gradients(self, func, weights, xpts=False):
+        """sum over (load case, mesh) of weights * d f / d x; with xpts, also
+        the node-coordinate gradient (addXptSens +
+        addAdjointResXptSensProducts) and the pair (g, gX) is returned."""
         M = self.model
+        if xpts and self.segments:
+            raise NotImplementedError("node-coordinate gradients of "
+                                      "segmented models")
         W = np.asarray(weights, np.float64).reshape(self.nlc, -1)
         dfdu = torch.zeros_like(self.u)
         for lc in range(self.nlc):
@@ -117,6 +126,7 @@ class StaticSolver:
             raise _lib.TacsGpuError(
                 f"adjoint GMRES did not converge (flags {fl.tolist()})")
         g = M.dv_vec()
+        gX = M.node_vec() if xpts else None
         for lc in range(self.nlc):
             if self.segments:
                 # coefficient of df/dx per element = the mesh weight
@@ -132,26 +142,40 @@ class StaticSolver:
                 M.eval_functions(self.u[lc], [func])
                 M.add_total_derivative(self.u[lc], func, Psi[lc], g,
                                        float(W[lc, 0]), -1.0)
-        return g
+                if xpts:
+                    M.add_total_xpt_derivative(self.u[lc], func, Psi[lc], gX,
+                                               float(W[lc, 0]), -1.0)
+        return (g, gX) if xpts else g
 
 
 class StaticFunctional(torch.autograd.Function):
-    """f = StaticFunctional.apply(x, solver, func) -> (nlc, nmesh) tensor."""
+    """f = StaticFunctional.apply(x, solver, func, xpts) -> (nlc, nmesh)
+    tensor; xpts (node coordinates, 3 per node) may be None."""
 
     @staticmethod
-    def forward(ctx, x, solver, func):
-        solver.solve(x)
+    def forward(ctx, x, solver, func, xpts=None):
+        solver.solve(x, xpts)
         f = solver.functions(func)
         ctx.solver, ctx.func = solver, func
         ctx.x_shape, ctx.x_dtype = x.shape, x.dtype
+        ctx.has_xpts = xpts is not None
+        if ctx.has_xpts:
+            ctx.X_shape, ctx.X_dtype = xpts.shape, xpts.dtype
         return torch.as_tensor(f, dtype=torch.float64, device=x.device)
 
     @staticmethod
     def backward(ctx, gout):
         w = gout.detach().cpu().numpy()
-        g = ctx.solver.gradients(ctx.func, w)
-        return g.to(ctx.x_dtype).reshape(ctx.x_shape), None, None
+        want_X = ctx.has_xpts and ctx.needs_input_grad[3]
+        if want_X:
+            g, gX = ctx.solver.gradients(ctx.func, w, xpts=True)
+            gX = gX.to(ctx.X_dtype).reshape(ctx.X_shape)
+        else:
+            g, gX = ctx.solver.gradients(ctx.func, w), None
+        return g.to(ctx.x_dtype).reshape(ctx.x_shape), None, None, gX
 
 
-def static_functional(x, solver, func=_lib.FUNC_COMPLIANCE):
-    return StaticFunctional.apply(x, solver, func)
+def static_functional(x, solver, func=_lib.FUNC_COMPLIANCE, xpts=None):
+    """Structural functional of the design variables x (and, when given,
+    of the node coordinates xpts) through a linear static solve."""
+    return StaticFunctional.apply(x, solver, func, xpts)

@@ -12,11 +12,13 @@ pattern (tacs/pytacs.py, tacs/problems/static.py):
     funcs, sens = {}, {}
     sp.evalFunctions(funcs)               # funcs["pressure_compliance"]
     sp.evalFunctionsSens(sens)            # sens[...]["struct"]: d f / d x
+                                          # sens[...]["Xpts"]: d f / d X
 
 Models come from tacs_gb300.bdf (one element type per model); the element
 call-back returns tacs_gb300.elements objects over one material.  Functions
-are Compliance and KSFailure; node-coordinate sensitivities ("Xpts") are
-not computed.  Every solve, function and sensitivity runs on the GPU.
+are Compliance and KSFailure, with design-variable ("struct") and
+node-coordinate ("Xpts", 3 per node in the BDF's node order)
+sensitivities.  Every solve, function and sensitivity runs on the GPU.
 """
 from __future__ import annotations
 
@@ -127,6 +129,7 @@ class StaticProblem:
         self.functionList = {}
         self.x = fea.getOrigDesignVars()
         self._model = None
+        self._xpts = None
         self.u = None
 
     def setOption(self, name, value):
@@ -137,6 +140,17 @@ class StaticProblem:
 
     def setDesignVars(self, x):
         self.x = np.asarray(x, np.float64).copy()
+
+    def getNodes(self):
+        """Node coordinates, 3 per node (TACSProblem.getNodes)."""
+        return np.asarray(self.fea.record["xpts"], np.float64).copy() \
+            if self._xpts is None else self._xpts.copy()
+
+    def setNodes(self, Xpts):
+        """New node coordinates for this problem (TACSProblem.setNodes)."""
+        self._xpts = np.asarray(Xpts, np.float64).ravel().copy()
+        if self._model is not None:
+            self._model.set_nodes(torch.as_tensor(self._xpts, device="cuda"))
 
     # -------------------------------------------------------------- loads
     def _node_index(self, ids, nastranOrdering):
@@ -194,6 +208,8 @@ class StaticProblem:
                 pe = np.nonzero(self.pressure)[0]
                 rec["pres_elems"] = pe.astype(np.int32)
                 rec["pres_vals"] = np.repeat(self.pressure[pe], 4)
+            if self._xpts is not None:
+                rec["xpts"] = self._xpts
             self._model = GpuModel(rec)
             self._mat = self._model.new_mat()
             self._pc = Pc(self._mat)
@@ -246,6 +262,13 @@ class StaticProblem:
             if flag != 1:
                 raise _lib.TacsGpuError(f"{self.name}: adjoint GMRES did not "
                                         "converge")
-            g = M.dv_vec()
-            M.add_total_derivative(self.u, kind, psi, g, 1.0, -1.0)
-            funcsSens[f"{self.name}_{f}"] = {"struct": g.cpu().numpy()}
+            out = {}
+            if includeDVSens:
+                g = M.dv_vec()
+                M.add_total_derivative(self.u, kind, psi, g, 1.0, -1.0)
+                out["struct"] = g.cpu().numpy()
+            if includeXptSens:
+                gx = M.node_vec()
+                M.add_total_xpt_derivative(self.u, kind, psi, gx, 1.0, -1.0)
+                out["Xpts"] = gx.cpu().numpy()
+            funcsSens[f"{self.name}_{f}"] = out

@@ -76,20 +76,26 @@ int main() {
   double fvals[2];
   assembler.evalFunctions(2, funcs, fvals);
 
-  std::vector<double> grads[2];
+  std::vector<double> grads[2], gradX[2];
   for (int k = 0; k < 2; k++) {
     TACSBVec *dfdu = assembler.createVec(), *psi = assembler.createVec();
     TACSBVec *dfdx = assembler.createDesignVec();
+    TACSBVec *dfdX = assembler.createNodeVec();
     assembler.addSVSens(1.0, 0.0, 0.0, 1, &funcs[k], &dfdu);
     assembler.applyBCs(dfdu);
     gmres.solve(dfdu, psi);
     assembler.addDVSens(1.0, 1, &funcs[k], &dfdx);
     assembler.addAdjointResProducts(-1.0, 1, &psi, &dfdx);
+    assembler.addXptSens(1.0, 1, &funcs[k], &dfdX);
+    assembler.addAdjointResXptSensProducts(-1.0, 1, &psi, &dfdX);
     grads[k].resize(dfdx->getSize());
     dfdx->getValues(grads[k].data());
+    gradX[k].resize(dfdX->getSize());
+    dfdX->getValues(gradX[k].data());
     delete dfdu;
     delete psi;
     delete dfdx;
+    delete dfdX;
   }
   std::printf("{\"flag\": %d, \"funcs\": [%.17g, %.17g]", flag, fvals[0],
               fvals[1]);
@@ -97,6 +103,10 @@ int main() {
     std::printf(", \"grad%d\": [", k);
     for (size_t i = 0; i < grads[k].size(); i++)
       std::printf("%s%.17g", i ? ", " : "", grads[k][i]);
+    std::printf("]");
+    std::printf(", \"gradX%d\": [", k);
+    for (size_t i = 0; i < gradX[k].size(); i++)
+      std::printf("%s%.17g", i ? ", " : "", gradX[k][i]);
     std::printf("]");
   }
   std::printf("}\n");

@@ -8,6 +8,8 @@
   rounding through a 1e-12 GMRES solve, ~1e-10 relative, divided by h stays
   below 1e-5; with h = 1e-6 x that rounding term alone reaches ~1e-3);
 * SIMP-style chaining (x -> x^3 in torch) through autograd;
+* node-coordinate gradients against the reference's complex-step shape
+  derivative and against central differences along a shape mode;
 * several load cases and several meshes in one functional call against the
   batched adjoint gradients.
 """
@@ -77,6 +79,40 @@ def test_autograd_central_differences(gpu, func):
         fm = ag.static_functional(xm, solver, func).item()
         fd = (fp - fm) / (2 * h)
         assert abs(fd - g[d]) <= FD_TOL * np.abs(g).max(), (d, fd, g[d])
+
+
+@pytest.mark.parametrize("name", ["shell_plate8", "hex_block"])
+def test_autograd_node_coordinates(gpu, name):
+    """Gradient with respect to the node coordinates: against the
+    reference's complex-step total shape derivative (1e-7), and, for a
+    torch-side parametrisation X(s) = X0 + s V, against central differences
+    of the functional in s."""
+    problem, ag = gpu
+    prob, ref = load_case(name)
+    M = problem.GpuModel(prob)
+    solver = ag.StaticSolver(M, prob["force"], m=prob.get("gmres_m", 100),
+                             nrestart=50, rtol=prob.get("rtol", 1e-12))
+    x = _dv_vector(prob, M.ndv)
+    X0 = torch.as_tensor(prob["xpts"], device="cuda")
+    X = X0.clone().requires_grad_(True)
+    f = ag.static_functional(x, solver, 0, xpts=X)
+    f.sum().backward()
+    assert rel(X.grad.cpu().numpy(), ref["grad_xpt_comp"]) < TOL
+    # a smooth shape mode: in-plane (x) bulge of the interior
+    V = torch.zeros_like(X0).reshape(-1, 3)
+    P = X0.reshape(-1, 3)
+    V[:, 0] = torch.sin(np.pi * P[:, 0] / P[:, 0].max()) * \
+        torch.sin(np.pi * P[:, 1] / P[:, 1].max())
+    V = V.reshape(-1)
+    s = torch.zeros((), dtype=torch.float64, device="cuda",
+                    requires_grad=True)
+    f = ag.static_functional(x, solver, 0, xpts=X0 + s * V)
+    (dfds,) = torch.autograd.grad(f.sum(), s)
+    h = 1e-5
+    fp = ag.static_functional(x, solver, 0, xpts=X0 + h * V).item()
+    fm = ag.static_functional(x, solver, 0, xpts=X0 - h * V).item()
+    fd = (fp - fm) / (2 * h)
+    assert abs(fd - dfds.item()) < FD_TOL * abs(dfds.item()) + 1e-12
 
 
 def test_autograd_simp_chain_rule(gpu):

@@ -54,3 +54,5 @@ def test_cpp_driver_matches_reference(tmp_path):
     assert rel(d["funcs"], ref["funcs"]) < 1e-7
     assert rel(np.array(d["grad0"]), ref["grad_comp"]) < 1e-7
     assert rel(np.array(d["grad1"]), ref["grad_ks"]) < 1e-7
+    assert rel(np.array(d["gradX0"]), ref["grad_xpt_comp"]) < 1e-7
+    assert rel(np.array(d["gradX1"]), ref["grad_xpt_ks"]) < 1e-7

@@ -4,7 +4,8 @@ way the reference's test_shell_plate_quad.py drives pytacs: the reference's
 the element call-back with one thickness design variable for the PLATE
 component, a 100 kPa pressure case and a 10 kN point load at GRID 81,
 compliance and KS failure (weight 10) against the known answers of that
-test (1e-8), and the design sensitivity against central differences."""
+test (1e-8), and the design and node-coordinate sensitivities against
+central differences of the solves."""
 import numpy as np
 import pytest
 
@@ -89,3 +90,26 @@ def test_pytacs_static_problems_match_reference(tmp_path):
     sp.setDesignVars(t0)
     fd = (vals[0] - vals[1]) / (2 * h)
     assert abs(fd - g) < 1e-5 * abs(g)
+    # node-coordinate sensitivities ("Xpts") of both functions against
+    # central differences of the solves, in-plane coordinates of two nodes
+    sp.solve()
+    sens = {}
+    sp.evalFunctionsSens(sens)
+    X0 = sp.getNodes()
+    h = 1e-6
+    for key in ("compliance", "ks_vmfailure"):
+        gx = sens["pressure_" + key]["Xpts"]
+        assert gx.shape == X0.shape
+        for j in (3 * 38 + 0, 3 * 50 + 1):
+            vals = []
+            for s in (1.0, -1.0):
+                X = X0.copy()
+                X[j] += s * h
+                sp.setNodes(X)
+                sp.solve()
+                f = {}
+                sp.evalFunctions(f, [key])
+                vals.append(f["pressure_" + key])
+            sp.setNodes(X0)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - gx[j]) < 1e-5 * np.abs(gx).max(), (key, j)
