@@ -248,6 +248,13 @@ int tg_mat_mult_f32(tg_mat *A, const float *x, float *y, void *stream);
    block-Jacobi and colour-reordered ILU(0) variants; precision
    TG_PREC_FP32 keeps the factor in FP32. */
 int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out);
+/* TACSAdditiveSchwarz(mat, levFill, fill) with levFill > 0: block ILU(k)
+   on the level-of-fill pattern of BCSRMat::computeILUk
+   (src/bpmat/BCSRMat.cpp:625); levFill = 0 is tg_pc_create(TG_PC_ILU0).
+   The pattern is built here on the host, once. */
+int tg_pc_create_iluk(tg_mat *A, int lev_fill, int precision, tg_pc **out);
+/* Level of fill and the factor's block count (nnz(ILU)). */
+int tg_pc_get_fill(tg_pc *pc, int *lev_fill, int *nnz_factor);
 int tg_pc_decref(tg_pc *pc);
 /* TACSAdditiveSchwarz::factor -> BCSRMat::factor (BCSRMatFact6.cpp:946).
    Synchronises; returns TG_ERR_PIVOT (with the row in tg_last_error) on a

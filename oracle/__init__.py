@@ -147,6 +147,12 @@ class Oracle:
         fail = self.L.or_ilu0_factor(C.byref(A), C.byref(F))
         return F, fail
 
+    def iluk(self, A, lev_fill):
+        """ILU(lev_fill) factor (its own pattern) of A."""
+        F = _Bcsr()
+        fail = self.L.or_iluk_factor(C.byref(A), int(lev_fill), C.byref(F))
+        return F, fail
+
     def ilu0_apply(self, F, x):
         x = np.ascontiguousarray(x, np.float64)
         y = np.zeros_like(x)

@@ -8,7 +8,8 @@
   The call sequence mirrors the reference's own static test harness
   (tests/integration_tests/static_analysis_base_test.py:359-427):
     1. at a given state u_test: assembleRes, assembleJacobian (BCSR arrays),
-       K*x, ILU(0) apply (TACSAdditiveSchwarz(mat, 0, 10.0)), addSVSens,
+       K*x, ILU(0) apply (TACSAdditiveSchwarz(mat, 0, 10.0)) and ILU(1),
+       ILU(2) applies (levFill 1, 2), addSVSens,
        addDVSens and addAdjointResProducts with a given psi_test;
     2. the linear static solve R(u) = K u - f = 0 with GMRES + ILU(0);
     3. compliance and KS failure, their state sensitivities, the adjoint
@@ -112,6 +113,16 @@ int main(int argc, char **argv) {
       pc->applyFactor(vec, out);
       out->getArray(&arr);
       w.f64("ilu_apply", arr, ndof);
+      // ILU(k): TACSAdditiveSchwarz(mat, levFill, fill) with levFill 1, 2
+      for (int lev = 1; lev <= 2; lev++) {
+        TACSAdditiveSchwarz *pk = new TACSAdditiveSchwarz(mat, lev, 10.0);
+        pk->incref();
+        pk->factor();
+        pk->applyFactor(vec, out);
+        out->getArray(&arr);
+        w.f64(lev == 1 ? "ilu1_apply" : "ilu2_apply", arr, ndof);
+        pk->decref();
+      }
       TACSMat *pcmat;
       pc->getMat(&pcmat);
     }

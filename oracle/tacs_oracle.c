@@ -988,6 +988,8 @@ static int block_inverse(double *Ainv, double *A, int n) {
    (BCSRMatFact6.cpp:946-1330, BCSRMatFact3.cpp:30-146).  Off-diagonal
    lower blocks become L_ij = A_ij D_j^{-1}, the stored diagonal blocks are
    the inverses D_i^{-1}. */
+static int ilu_numeric(or_bcsr *F);
+
 int or_ilu0_factor(const or_bcsr *A, or_bcsr *F) {
   int bs = A->bsize, n = A->nrows;
   size_t b2 = (size_t)bs * bs, nnz = A->rowp[n];
@@ -1003,6 +1005,16 @@ int or_ilu0_factor(const or_bcsr *A, or_bcsr *F) {
     memcpy(F->diag, A->diag, sizeof(int) * n);
   }
   memcpy(F->vals, A->vals, sizeof(double) * nnz * b2);
+  return ilu_numeric(F);
+}
+
+/* Numeric block ILU in F's own pattern (IKJ: row i's lower blocks become
+   L_ij = A_ij D_j^{-1} and update the blocks of row i that row j's upper
+   part reaches; the diagonal blocks end as D_i^{-1}), BCSRMatFactor6 /
+   BCSRMatFactor3 (BCSRMatFact6.cpp:946-1330, BCSRMatFact3.cpp:30-146). */
+static int ilu_numeric(or_bcsr *F) {
+  const int bs = F->bsize, n = F->nrows;
+  const size_t b2 = (size_t)bs * bs;
   const int *rowp = F->rowp, *cols = F->cols, *diag = F->diag;
   double *V = F->vals;
   double d[64], D[64];
@@ -1041,6 +1053,102 @@ int or_ilu0_factor(const or_bcsr *A, or_bcsr *F) {
     if (info > 0 && !fail) fail = i + 1;
   }
   return fail;
+}
+
+/* ILU(k) pattern (BCSRMat::computeILUk, BCSRMat.cpp:625-730): within row
+   i, every entry (i, c) left of the diagonal, taken in increasing c, meets
+   the upper entries (c, j) of the finished row c; (i, j) gets level
+   lev(i, c) + lev(c, j) + 1 if smaller than its current level, or is
+   inserted (row kept sorted) if new and at most lev_fill.  A's entries
+   have level 0 and the diagonal is always present. */
+static void iluk_symbolic(const or_bcsr *A, int lev_fill, or_bcsr *F,
+                          int **levs_out) {
+  const int n = A->nrows;
+  size_t cap = (size_t)A->rowp[n] * 2 + n + 16, size = 0;
+  int *cols = (int *)malloc(sizeof(int) * cap);
+  int *levs = (int *)malloc(sizeof(int) * cap);
+  int *rowp = (int *)malloc(sizeof(int) * (n + 1));
+  int *diag = (int *)malloc(sizeof(int) * (n ? n : 1));
+  int *rc = (int *)malloc(sizeof(int) * (n + 1));
+  int *rl = (int *)malloc(sizeof(int) * (n + 1));
+  rowp[0] = 0;
+  for (int i = 0; i < n; i++) {
+    int nr = 0, has_diag = 0;
+    for (int j = A->rowp[i]; j < A->rowp[i + 1]; j++) {
+      if (A->cols[j] == i) has_diag = 1;
+      rc[nr] = A->cols[j];
+      rl[nr++] = 0;
+    }
+    if (!has_diag) {
+      int p = 0;
+      while (p < nr && rc[p] < i) p++;
+      for (int m = nr; m > p; m--) {
+        rc[m] = rc[m - 1];
+        rl[m] = rl[m - 1];
+      }
+      rc[p] = i;
+      rl[p] = 0;
+      nr++;
+    }
+    for (int j = 0; j < nr && rc[j] < i; j++) {
+      const int c = rc[j], lc = rl[j];
+      int p = j + 1;
+      for (int q = diag[c] + 1; q < rowp[c + 1]; q++) {
+        const int col = cols[q], lev = lc + levs[q] + 1;
+        while (p < nr && rc[p] < col) p++;
+        if (p < nr && rc[p] == col) {
+          if (lev < rl[p]) rl[p] = lev;
+        } else if (lev <= lev_fill) {
+          for (int m = nr; m > p; m--) {
+            rc[m] = rc[m - 1];
+            rl[m] = rl[m - 1];
+          }
+          rc[p] = col;
+          rl[p] = lev;
+          nr++;
+        }
+      }
+    }
+    if (size + nr > cap) {
+      cap = 2 * (size + nr);
+      cols = (int *)realloc(cols, sizeof(int) * cap);
+      levs = (int *)realloc(levs, sizeof(int) * cap);
+    }
+    for (int k = 0; k < nr; k++) {
+      if (rc[k] == i) diag[i] = (int)size;
+      cols[size] = rc[k];
+      levs[size++] = rl[k];
+    }
+    rowp[i + 1] = (int)size;
+  }
+  free(rc);
+  free(rl);
+  F->bsize = A->bsize;
+  F->nrows = n;
+  F->rowp = rowp;
+  F->cols = cols;
+  F->diag = diag;
+  F->vals = (double *)malloc(sizeof(double) *
+                             (size * (size_t)A->bsize * A->bsize + 1));
+  if (levs_out) *levs_out = levs;
+  else free(levs);
+}
+
+/* TACSAdditiveSchwarz(mat, levFill, fill) + factor: ILU(lev_fill) of A.
+   F is built on the first call (F->rowp == NULL) and refactored after. */
+int or_iluk_factor(const or_bcsr *A, int lev_fill, or_bcsr *F) {
+  if (!F->rowp) iluk_symbolic(A, lev_fill, F, NULL);
+  const int n = A->nrows;
+  const size_t b2 = (size_t)A->bsize * A->bsize;
+  memset(F->vals, 0, sizeof(double) * F->rowp[n] * b2);
+  for (int i = 0; i < n; i++) {
+    int f = F->rowp[i];
+    for (int j = A->rowp[i]; j < A->rowp[i + 1]; j++) {
+      while (F->cols[f] < A->cols[j]) f++;
+      memcpy(&F->vals[b2 * f], &A->vals[b2 * j], sizeof(double) * b2);
+    }
+  }
+  return ilu_numeric(F);
 }
 
 /* BCSRMatApplyLower / BCSRMatApplyUpper (BCSRMatMult6.cpp:319-415) */

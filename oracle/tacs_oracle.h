@@ -79,7 +79,10 @@ void or_apply_bcs_vec(const or_problem *p, double *x);
 
 /* Linear algebra */
 void or_bcsr_mult(const or_bcsr *A, const double *x, double *y, int nthreads);
-int or_ilu0_factor(const or_bcsr *A, or_bcsr *F); /* F gets a copy */
+int or_ilu0_factor(const or_bcsr *A, or_bcsr *F);
+/* ILU(lev_fill) on the BCSRMat::computeILUk pattern; F->rowp == NULL on
+   the first call builds the pattern (F owns it; free with or_bcsr_free). */
+int or_iluk_factor(const or_bcsr *A, int lev_fill, or_bcsr *F); /* F gets a copy */
 void or_ilu0_apply(const or_bcsr *F, const double *x, double *y);
 int or_gmres(const or_bcsr *A, const or_bcsr *F, const double *b, double *x,
              int m, int nrestart, double rtol, double atol, int *iters,

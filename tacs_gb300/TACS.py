@@ -105,18 +105,16 @@ class Mat:
 
 
 class Pc:
-    """TACS.Pc(mat, lev_fill=..., ratio_fill=..., reorder=...): block ILU(0)
-    (TACSAdditiveSchwarz with levFill = 0) on the GPU.  lev_fill must be 0;
-    precision='fp32' keeps the factor in FP32."""
+    """TACS.Pc(mat, lev_fill=..., ratio_fill=..., reorder=...): block ILU(k)
+    (TACSAdditiveSchwarz(mat, lev_fill, ratio_fill)) on the GPU, in the
+    natural order (reorder is not applied); precision='fp32' keeps the
+    factor in FP32."""
 
     def __init__(self, mat, lev_fill=0, ratio_fill=10.0, reorder=False,
                  precision="fp64"):
-        if lev_fill != 0:
-            raise NotImplementedError("ILU(k) with k > 0 is not on the GPU "
-                                      "path; use lev_fill=0")
         prec = _lib.PREC_FP32 if precision == "fp32" else _lib.PREC_FP64
         self.mat = mat
-        self.pc = _Pc(mat.gm, _lib.PC_ILU0, prec)
+        self.pc = _Pc(mat.gm, _lib.PC_ILU0, prec, lev_fill=int(lev_fill))
 
     def factor(self):
         self.pc.factor()

@@ -60,6 +60,8 @@ SIGNATURES = [
     ("tg_mat_mult", _I, [_P, _P, _P, _P]),
     ("tg_mat_mult_f32", _I, [_P, _P, _P, _P]),
     ("tg_pc_create", _I, [_P, _I, _I, C.POINTER(_P)]),
+    ("tg_pc_create_iluk", _I, [_P, _I, _I, _P]),
+    ("tg_pc_get_fill", _I, [_P, _P, _P]),
     ("tg_pc_decref", _I, [_P]),
     ("tg_pc_factor", _I, [_P, _P]),
     ("tg_pc_apply", _I, [_P, _P, _P, _P]),

@@ -547,7 +547,8 @@ __global__ void gather_blocks_kernel(int nnz, int b2, const int *valmap,
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const size_t k = i / b2, e = i - k * b2;
-    dst[i] = (T)src[(size_t)valmap[k] * b2 + e];
+    const int m = valmap[k];
+    dst[i] = m >= 0 ? (T)src[(size_t)m * b2 + e] : (T)0;
   }
 }
 template <typename T>

@@ -149,6 +149,9 @@ struct tg_pc {
   int refcount = 1;
   tg_mat *A = nullptr;
   int type = TG_PC_ILU0, precision = TG_PREC_FP64;
+  // ILU(k): level of fill and block count of the factor's pattern (fnnz =
+  // the matrix's block count for ILU(0) and block Jacobi)
+  int lev_fill = 0, fnnz = 0;
   IluPlan plan{};
   int *d_lvl_rows = nullptr, *d_ulvl_rows = nullptr;
   int *d_upd_ptr = nullptr, *d_upd_tgt = nullptr, *d_upd_src = nullptr;
@@ -157,8 +160,9 @@ struct tg_pc {
   float *d_F32 = nullptr, *d_x32 = nullptr, *d_y32 = nullptr,
         *d_tmp32 = nullptr;
   double *d_gx = nullptr, *d_gy = nullptr;  // FP64 apply in/out buffers
-  // colour-reordered variant: permuted pattern, value map, permutation and
-  // permuted work vectors
+  // colour-reordered variant and ILU(k): the factor's own pattern, the map
+  // from its blocks to the matrix's (-1: fill, starts at zero), and for the
+  // colour order the permutation and permuted work vectors
   int *d_prowp = nullptr, *d_pcols = nullptr, *d_pdiag = nullptr;
   int *d_valmap = nullptr, *d_perm = nullptr;
   double *d_px = nullptr, *d_py = nullptr;

@@ -925,6 +925,59 @@ static int build_cluster_schedule(tg_pc *pc, const std::vector<int> &rowp,
   return 0;
 }
 
+// Pattern of ILU(k) (BCSRMat::computeILUk, src/bpmat/BCSRMat.cpp:625-730):
+// row by row, each stored entry (i, c) of row i left of the diagonal
+// combines with the strictly upper entries (c, j) of the already finished
+// row c; the product would fill (i, j) at level lev(i, c) + lev(c, j) + 1.
+// An existing entry keeps the smaller level, a new one is inserted (rows
+// stay sorted) when its level is at most lev_fill.  The matrix's own blocks
+// have level 0.  valmap gives each factor block's block in the matrix, or
+// -1 for fill.
+static void iluk_pattern(const std::vector<int> &rowp,
+                         const std::vector<int> &cols, int lev_fill,
+                         std::vector<int> &frowp, std::vector<int> &fcols,
+                         std::vector<int> &fdiag, std::vector<int> &valmap) {
+  const int n = (int)rowp.size() - 1;
+  std::vector<int> flev;
+  frowp.assign(n + 1, 0);
+  fdiag.assign(n, 0);
+  fcols.clear();
+  valmap.clear();
+  std::vector<int> rc, rl;
+  for (int i = 0; i < n; i++) {
+    rc.assign(cols.begin() + rowp[i], cols.begin() + rowp[i + 1]);
+    rl.assign(rc.size(), 0);
+    auto at = std::lower_bound(rc.begin(), rc.end(), i);
+    if (at == rc.end() || *at != i) {
+      rl.insert(rl.begin() + (at - rc.begin()), 0);
+      rc.insert(at, i);
+    }
+    for (size_t j = 0; j < rc.size() && rc[j] < i; j++) {
+      const int c = rc[j], lc = rl[j];
+      size_t p = j + 1;
+      for (int q = fdiag[c] + 1; q < frowp[c + 1]; q++) {
+        const int col = fcols[q], lev = lc + flev[q] + 1;
+        while (p < rc.size() && rc[p] < col) p++;
+        if (p < rc.size() && rc[p] == col) {
+          if (lev < rl[p]) rl[p] = lev;
+        } else if (lev <= lev_fill) {
+          rc.insert(rc.begin() + p, col);
+          rl.insert(rl.begin() + p, lev);
+        }
+      }
+    }
+    int a = rowp[i];
+    for (size_t j = 0; j < rc.size(); j++) {
+      if (rc[j] == i) fdiag[i] = (int)fcols.size();
+      while (a < rowp[i + 1] && cols[a] < rc[j]) a++;
+      valmap.push_back(a < rowp[i + 1] && cols[a] == rc[j] ? a : -1);
+      fcols.push_back(rc[j]);
+      flev.push_back(rl[j]);
+    }
+    frowp[i + 1] = (int)fcols.size();
+  }
+}
+
 // Level sets of the block lower / upper triangles and the IKJ update list
 // of ILU(0) with the pattern of A (BCSRMat(comm, A, levFill = 0, fill),
 // src/bpmat/BCSRMat.cpp:138).
@@ -1000,7 +1053,8 @@ static int build_ilu_plan(tg_pc *pc, const std::vector<int> &rowp,
   return 0;
 }
 
-int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
+static int pc_create(tg_mat *A, int type, int lev_fill, int precision,
+                     tg_pc **out) {
   if (!A || !out) return fail(TG_ERR_ARG, "tg_pc_create: NULL argument");
   *out = nullptr;
   if (type != TG_PC_ILU0 && type != TG_PC_BLOCK_JACOBI &&
@@ -1008,15 +1062,32 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
     return fail(TG_ERR_ARG, "tg_pc_create: unknown preconditioner type");
   if (precision != TG_PREC_FP64 && precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_pc_create: bad precision");
+  if (lev_fill < 0 || (lev_fill > 0 && type != TG_PC_ILU0))
+    return fail(TG_ERR_ARG, "tg_pc_create: fill levels need TG_PC_ILU0");
   tg_pc *pc = new tg_pc();
   pc->A = A;
   A->refcount++;
   pc->type = type;
   pc->precision = precision;
+  pc->lev_fill = lev_fill;
+  pc->fnnz = A->nnz;
   tg_assembler *a = A->a;
   int rc = 0;
   const int *rowp_d = a->d_rowp, *cols_d = a->d_cols, *diag_d = a->d_diag;
-  if (type == TG_PC_ILU0) {
+  if (type == TG_PC_ILU0 && lev_fill > 0) {
+    std::vector<int> frowp, fcols, fdiag, valmap;
+    iluk_pattern(a->rowp_h, a->cols_h, lev_fill, frowp, fcols, fdiag,
+                 valmap);
+    pc->fnnz = (int)fcols.size();
+    rc = build_ilu_plan(pc, frowp, fcols, fdiag);
+    if (!rc) rc = upload(&pc->d_prowp, frowp);
+    if (!rc) rc = upload(&pc->d_pcols, fcols);
+    if (!rc) rc = upload(&pc->d_pdiag, fdiag);
+    if (!rc) rc = upload(&pc->d_valmap, valmap);
+    rowp_d = pc->d_prowp;
+    cols_d = pc->d_pcols;
+    diag_d = pc->d_pdiag;
+  } else if (type == TG_PC_ILU0) {
     rc = build_ilu_plan(pc, a->rowp_h, a->cols_h, a->diag_h);
   } else if (type == TG_PC_ILU0_COLORED) {
     // greedy colouring of the node graph: nodes of one colour are never
@@ -1069,7 +1140,7 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
     cols_d = pc->d_pcols;
     diag_d = pc->d_pdiag;
   }
-  const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
+  const size_t nv = (size_t)pc->fnnz * A->bsize * A->bsize;
   const size_t n = (size_t)A->nrows * A->bsize;
   if (!rc) rc = dalloc(&pc->d_fail, 1);
   if (!rc) rc = dalloc(&pc->d_F, nv);
@@ -1107,6 +1178,18 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
   *out = pc;
   return 0;
 }
+int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
+  return pc_create(A, type, 0, precision, out);
+}
+int tg_pc_create_iluk(tg_mat *A, int lev_fill, int precision, tg_pc **out) {
+  return pc_create(A, TG_PC_ILU0, lev_fill, precision, out);
+}
+int tg_pc_get_fill(tg_pc *pc, int *lev_fill, int *nnz_factor) {
+  if (!pc) return fail(TG_ERR_ARG, "tg_pc_get_fill: NULL pc");
+  if (lev_fill) *lev_fill = pc->lev_fill;
+  if (nnz_factor) *nnz_factor = pc->fnnz;
+  return 0;
+}
 int tg_pc_decref(tg_pc *pc) {
   if (!pc) return 0;
   if (--pc->refcount == 0) {
@@ -1133,8 +1216,12 @@ int pc_factor_fp64(tg_pc *pc, cudaStream_t s) {
                          pc->d_F, s);
     for (int L = 0; L < nl; L++) launch_ilu0_factor_level(pc->plan, L, pc->d_F, s);
   } else if (pc->type == TG_PC_ILU0) {
-    TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
-                            cudaMemcpyDeviceToDevice, s));
+    if (pc->lev_fill > 0)
+      launch_gather_blocks(pc->fnnz, A->bsize * A->bsize, pc->d_valmap,
+                           A->d_vals, pc->d_F, s);
+    else
+      TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
+                              cudaMemcpyDeviceToDevice, s));
     for (int L = 0; L < nl; L++) launch_ilu0_factor_level(pc->plan, L, pc->d_F, s);
   } else {
     TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
@@ -1230,13 +1317,22 @@ int tg_pc_factor(tg_pc *pc, void *s) {
     }
   } else if (pc->type == TG_PC_ILU0) {
     const int nl = (int)pc->plan.lvl_ptr_h.size() - 1;
+    const int b2 = A->bsize * A->bsize;
     if (pc->precision == TG_PREC_FP64) {
-      TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
-                              cudaMemcpyDeviceToDevice, S(s)));
+      if (pc->lev_fill > 0)
+        launch_gather_blocks(pc->fnnz, b2, pc->d_valmap, A->d_vals, pc->d_F,
+                             S(s));
+      else
+        TG_CUDA(cudaMemcpyAsync(pc->d_F, A->d_vals, nv * sizeof(double),
+                                cudaMemcpyDeviceToDevice, S(s)));
       for (int L = 0; L < nl; L++)
         launch_ilu0_factor_level(pc->plan, L, pc->d_F, S(s));
     } else {
-      launch_d2f(A->d_vals, pc->d_F32, nv, S(s));
+      if (pc->lev_fill > 0)
+        launch_gather_blocks_f32(pc->fnnz, b2, pc->d_valmap, A->d_vals,
+                                 pc->d_F32, S(s));
+      else
+        launch_d2f(A->d_vals, pc->d_F32, nv, S(s));
       for (int L = 0; L < nl; L++)
         launch_ilu0_factor_level_f32(pc->plan, L, pc->d_F32, S(s));
       int rc = ensure_f32(A, S(s));

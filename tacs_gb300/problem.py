@@ -71,13 +71,28 @@ class Mat:
 
 
 class Pc:
-    """tg_pc: ILU(0) / block-Jacobi preconditioner, FP64 or FP32."""
+    """tg_pc: ILU(k) / block-Jacobi preconditioner, FP64 or FP32."""
 
-    def __init__(self, mat, kind=_lib.PC_ILU0, precision=_lib.PREC_FP64):
+    def __init__(self, mat, kind=_lib.PC_ILU0, precision=_lib.PREC_FP64,
+                 lev_fill=0):
         h = C.c_void_p()
-        check(_lib.lib().tg_pc_create(mat.handle, kind, precision,
-                                      C.byref(h)), "tg_pc_create")
+        if lev_fill > 0:
+            if kind != _lib.PC_ILU0:
+                raise ValueError("fill levels need the natural-order ILU")
+            check(_lib.lib().tg_pc_create_iluk(mat.handle, int(lev_fill),
+                                               precision, C.byref(h)),
+                  "tg_pc_create_iluk")
+        else:
+            check(_lib.lib().tg_pc_create(mat.handle, kind, precision,
+                                          C.byref(h)), "tg_pc_create")
         self.handle, self.mat = h, mat
+
+    def fill(self):
+        """(level of fill, blocks in the factor)."""
+        lev, nnz = C.c_int(), C.c_int()
+        check(_lib.lib().tg_pc_get_fill(self.handle, C.byref(lev),
+                                        C.byref(nnz)))
+        return lev.value, nnz.value
 
     def factor(self):
         check(_lib.lib().tg_pc_factor(self.handle, _stream()), "tg_pc_factor")

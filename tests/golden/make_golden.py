@@ -18,6 +18,8 @@ stored fixtures with
 
     python tests/golden/make_golden.py --xpt [case ...]
 
+and the ILU(1) / ILU(2) applies of the real build with ``--iluk``.
+
 The fixtures are committed; the GPU machine never needs the reference.
 """
 from __future__ import annotations
@@ -284,24 +286,29 @@ def main(names=None):
               f" size={os.path.getsize(path)}")
 
 
-def add_xpt(names=None):
-    """Run the complex build on each stored fixture's inputs and add its
-    node-coordinate sensitivities as ref_<key>."""
+ILUK_KEYS = ("ilu1_apply", "ilu2_apply")
+
+
+def add_keys(names, gen, keys):
+    """Run a reference build on each stored fixture's inputs and add the
+    given outputs as ref_<key> (the stored inputs and outputs stay)."""
     for name in (names or CASES):
         path = os.path.join(HERE, name + ".npz")
         rec = dict(np.load(path))
         prob = {k[3:]: v for k, v in rec.items() if k.startswith("in_")}
-        ref = run_reference(prob, GEN_CPLX)
-        for k in XPT_KEYS:
+        ref = run_reference(prob, gen)
+        for k in keys:
             if k in ref:
                 rec["ref_" + k] = ref[k]
         np.savez_compressed(path, **rec)
-        print(name, {k: float(np.abs(ref[k]).max()) for k in XPT_KEYS
+        print(name, {k: float(np.abs(ref[k]).max()) for k in keys
                      if k in ref})
 
 
 if __name__ == "__main__":
     if sys.argv[1:2] == ["--xpt"]:
-        add_xpt(sys.argv[2:] or None)
+        add_keys(sys.argv[2:], GEN_CPLX, XPT_KEYS)
+    elif sys.argv[1:2] == ["--iluk"]:
+        add_keys(sys.argv[2:], GEN, ILUK_KEYS)
     else:
         main(sys.argv[1:] or None)
