@@ -105,16 +105,20 @@ class Mat:
 
 
 class Pc:
-    """TACS.Pc(mat, lev_fill=..., ratio_fill=..., reorder=...): block ILU(k)
-    (TACSAdditiveSchwarz(mat, lev_fill, ratio_fill)) on the GPU, in the
-    natural order (reorder is not applied); precision='fp32' keeps the
-    factor in FP32."""
+    """TACS.Pc(mat, lev_fill=..., ratio_fill=..., reorder=...).
 
-    def __init__(self, mat, lev_fill=0, ratio_fill=10.0, reorder=False,
-                 precision="fp64"):
+    For a matrix from createMat the reference builds
+    TACSAdditiveSchwarz(mat, 5, 10.0) whatever the keywords say (they
+    configure TACSSchurPc, tacs/TACS.pyx:1106-1139), so this is block
+    ILU(5) on the GPU in the natural order.  fill_level=k overrides the
+    level (an extension; 0 gives ILU(0)); precision='fp32' keeps the factor
+    in FP32."""
+
+    def __init__(self, mat, *args, precision="fp64", fill_level=5,
+                 **kwargs):
         prec = _lib.PREC_FP32 if precision == "fp32" else _lib.PREC_FP64
         self.mat = mat
-        self.pc = _Pc(mat.gm, _lib.PC_ILU0, prec, lev_fill=int(lev_fill))
+        self.pc = _Pc(mat.gm, _lib.PC_ILU0, prec, lev_fill=int(fill_level))
 
     def factor(self):
         self.pc.factor()

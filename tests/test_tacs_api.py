@@ -1,6 +1,7 @@
 """The reference-style Python interface (tacs_gb300.TACS / elements /
-constitutive / functions): a static analysis with adjoint gradients written
-the way the reference's integration tests drive tacs.TACS
+constitutive / functions): a static analysis with adjoint gradients (design
+variables and node coordinates) written the way the reference's
+integration tests drive tacs.TACS
 (tests/integration_tests/static_analysis_base_test.py:359-427), checked
 against the reference's own outputs (golden fixtures)."""
 import numpy as np
@@ -17,7 +18,8 @@ API = {
                   "setDesignVars", "setVariables", "getVariables",
                   "zeroVariables", "setAuxElements", "assembleRes",
                   "assembleJacobian", "applyBCs", "evalFunctions",
-                  "addSVSens", "addDVSens", "addAdjointResProducts"],
+                  "addSVSens", "addDVSens", "addAdjointResProducts",
+                  "addXptSens", "addAdjointResXptSensProducts"],
     "Vec": ["getArray", "zeroEntries", "copyValues", "scale", "axpy",
             "axpby", "norm", "dot", "setRand", "getVarsPerNode", "getSize"],
     "Mat": ["zeroEntries", "mult", "getMat"],
@@ -129,6 +131,11 @@ def test_static_adjoint_through_reference_api(name):
         dfdx = assembler.createDesignVec()
         assembler.addDVSens([fn], [dfdx])
         assembler.addAdjointResProducts([psi], [dfdx], -1.0)
-        grads.append(dfdx.getArray().copy())
-    assert rel(grads[0], ref["grad_comp"]) < TOL
-    assert rel(grads[1], ref["grad_ks"]) < TOL
+        dfdX = assembler.createNodeVec()
+        assembler.addXptSens([fn], [dfdX])
+        assembler.addAdjointResXptSensProducts([psi], [dfdX], -1.0)
+        grads.append((dfdx.getArray().copy(), dfdX.getArray().copy()))
+    assert rel(grads[0][0], ref["grad_comp"]) < TOL
+    assert rel(grads[1][0], ref["grad_ks"]) < TOL
+    assert rel(grads[0][1], ref["grad_xpt_comp"]) < TOL
+    assert rel(grads[1][1], ref["grad_xpt_ks"]) < TOL
