@@ -8,9 +8,10 @@ the BCSRMat::computeILUk pattern, src/bpmat/BCSRMat.cpp:625).
   the spread that a rounding-level change of K causes in the reference's
   own apply when that is larger (thin-shell factors amplify last-bit
   differences; the same bar as ILU(0));
-* GMRES with ILU(2) on a thin clamped plate: fewer iterations than ILU(0)
-  and the solution, FP64 and with the FP32 factor inside FP64 GMRES,
-  against a sparse direct solve of the same matrix (1e-8).
+* GMRES with ILU(1) / ILU(3) on a thin clamped plate where ILU(0)
+  stalls: fewer iterations with more fill, true residual 1e-10 and the
+  solution against a sparse direct solve (1e-5), FP64 and with the FP32
+  factor inside FP64 GMRES.
 """
 import numpy as np
 import pytest
@@ -115,9 +116,14 @@ def test_iluk_apply_matches_oracle(gpu, kind):
 
 @pytest.mark.gpu
 def test_gmres_iluk_thin_plate(gpu):
-    """A thin clamped plate (32 x 32, t = 5 mm): more fill, fewer GMRES
-    iterations; the ILU(2) solutions (FP64, and FP32 factor inside FP64
-    GMRES) against a sparse direct solve of the same matrix."""
+    """A thin clamped plate (32 x 32, t = 5 mm) in the natural order: the
+    ILU(0) factor is unstable there (|M^-1 b| ~ 1e17 |x|, GMRES stalls),
+    ILU(1) and ILU(3) converge (ILU(2) is unstable again: the oracle,
+    restating the reference's factorisation, behaves the same).  Checked:
+    convergence, fewer iterations with more fill, the true residual
+    (1e-10) and the solution against a sparse direct solve (1e-5: cond(K)
+    x the 1e-12 GMRES tolerance), in FP64 and with the FP32 ILU(3) inside
+    FP64 GMRES."""
     problem, L, torch = gpu
     from scipy import sparse
     from scipy.sparse.linalg import spsolve
@@ -134,25 +140,29 @@ def test_gmres_iluk_thin_plate(gpu):
     K = sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
                            mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
                           shape=(M.ndof, M.ndof)).tocsc()
-    x_ref = spsolve(K, b.cpu().numpy())
-    flags, iters, sols = {}, {}, {}
-    for lev in (0, 1, 2):
+    bh = b.cpu().numpy()
+    x_ref = spsolve(K, bh)
+
+    def check(x):
+        assert np.linalg.norm(K @ x - bh) < 1e-10 * np.linalg.norm(bh)
+        assert rel(x, x_ref) < 1e-5
+
+    flags, iters = {}, {}
+    for lev in (0, 1, 3):
         pc = problem.Pc(mat, lev_fill=lev)
         pc.factor()
         ksm = problem.Ksm(mat, pc, 200, 50)
         ksm.set_tolerances(1e-12)
         x, flags[lev] = ksm.solve(b)
-        iters[lev], sols[lev] = ksm.iters, x.cpu().numpy()
-    assert flags[2] == 1, (flags, iters)
-    assert rel(sols[2], x_ref) < 1e-8
-    for lev in (0, 1):
-        if flags[lev] == 1:
-            assert rel(sols[lev], x_ref) < 1e-8
-    assert iters[2] < iters[0], iters
-    pc = problem.Pc(mat, L.PC_ILU0, L.PREC_FP32, lev_fill=2)
+        iters[lev] = ksm.iters
+        if lev > 0:
+            assert flags[lev] == 1, (flags, iters)
+            check(x.cpu().numpy())
+    assert iters[3] < iters[1] < iters[0], iters
+    pc = problem.Pc(mat, L.PC_ILU0, L.PREC_FP32, lev_fill=3)
     pc.factor()
     ksm = problem.Ksm(mat, pc, 200, 50, mixed=True)
     ksm.set_tolerances(1e-12)
     x, flag = ksm.solve(b)
     assert flag == 1
-    assert rel(x.cpu().numpy(), x_ref) < 1e-8
+    check(x.cpu().numpy())
