@@ -77,22 +77,26 @@ def adjoint_section(n, torch, colored=False):
     p = clamped_plate(n)
     M = problem.GpuModel(p)
     f0 = np.zeros(M.ndof)
-    runs = [("fp64_ilu0_natural", _lib.PC_ILU0, False, 1),
-            ("mixed_ilu0_natural", _lib.PC_ILU0, True, 1)]
+    # (label, pc type, mixed, fill level); ILU(5) is what the reference's
+    # Python Pc builds for an assembler matrix (TACSAdditiveSchwarz(mat, 5))
+    runs = [("fp64_ilu0_natural", _lib.PC_ILU0, False, 0),
+            ("mixed_ilu0_natural", _lib.PC_ILU0, True, 0),
+            ("fp64_ilu3_natural", _lib.PC_ILU0, False, 3),
+            ("mixed_ilu3_natural", _lib.PC_ILU0, True, 3),
+            ("fp64_ilu5_natural", _lib.PC_ILU0, False, 5)]
     if colored:
-        runs += [("fp64_ilu0_colored", _lib.PC_ILU0_COLORED, False, 1),
-                 ("mixed_ilu0_colored", _lib.PC_ILU0_COLORED, True, 1)]
+        runs += [("fp64_ilu0_colored", _lib.PC_ILU0_COLORED, False, 0),
+                 ("mixed_ilu0_colored", _lib.PC_ILU0_COLORED, True, 0)]
     out, grads = {"workload": f"clamped MITC4 plate {n}x{n}, GMRES(100) "
                               "to 1e-10, compliance + KS(100) gradients",
                   "elements": n * n, "dof": int(M.ndof)}, {}
-    for label, kind, mixed, reps in runs:
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            r = problem.static_adjoint(M, f0, 100, 400, 1e-10, pc_kind=kind,
-                                       mixed=mixed)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
+    for label, kind, mixed, lev in runs:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = problem.static_adjoint(M, f0, 100, 400, 1e-10, pc_kind=kind,
+                                   mixed=mixed, lev_fill=lev)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
         grads[label] = [g.cpu().numpy() for g in r["grads"]]
         out[label] = {"s_per_gradient": dt, "iters": r["iters"],
                       "converged": [int(f) for f in r["flags"]],
@@ -107,6 +111,9 @@ def adjoint_section(n, torch, colored=False):
     out["mixed_speedup_vs_fp64_natural"] = (
         out["fp64_ilu0_natural"]["s_per_gradient"]
         / out["mixed_ilu0_natural"]["s_per_gradient"])
+    out["ilu3_speedup_vs_ilu0_fp64"] = (
+        out["fp64_ilu0_natural"]["s_per_gradient"]
+        / out["fp64_ilu3_natural"]["s_per_gradient"])
     return out, p
 
 
@@ -205,7 +212,8 @@ def cylinder_section(torch, nc=384, nz=256):
     return out
 
 
-def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0):
+def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0,
+                  lev_fill=0):
     """Independent clamped plates of seeded uneven sizes (N log-uniform in
     [16, nmax]) in one assembler: 4 load cases per plate, one batched
     GMRES for all forward solves and one for all adjoint solves, KS failure
@@ -219,7 +227,7 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0):
                        "(seed 4), 4 load cases each, KS(100) adjoint "
                        f"gradients, GMRES({m}) to 1e-10, "
                        + ("natural" if pc_kind == 0 else "colour-reordered")
-                       + " ILU(0)",
+                       + f" ILU({lev_fill})",
            "plates": count, "elements": int(bp["nelem"]),
            "dof": int(M.ndof), "systems": 4 * count}
     g = {}
@@ -228,7 +236,8 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0):
         t0 = time.perf_counter()
         r = problem.batched_adjoint(M, F, m=m, nrestart=nrestart, rtol=1e-10,
                                     pc_kind=pc_kind, mixed=mixed,
-                                    func=_lib.FUNC_KS_FAILURE)
+                                    func=_lib.FUNC_KS_FAILURE,
+                                    lev_fill=lev_fill)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         g[label] = r["grads"].cpu().numpy()
@@ -419,6 +428,8 @@ def main():
     ap.add_argument("--batch", type=int, default=12)
     ap.add_argument("--batch-nmax", type=int, default=96)
     ap.add_argument("--batch-pc", type=int, default=0)
+    ap.add_argument("--batch-fill", type=int, default=0,
+                    help="ILU fill level of the batched solves")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -556,7 +567,8 @@ def main():
     if rank == 0 and args.batch > 0:
         line["batch_c4"] = batch_section(torch, count=args.batch,
                                          nmax=args.batch_nmax,
-                                         pc_kind=args.batch_pc)
+                                         pc_kind=args.batch_pc,
+                                         lev_fill=args.batch_fill)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p)
         if args.adj_size > 0:

@@ -36,7 +36,7 @@ class StaticSolver:
 
     def __init__(self, model, loads, m=100, nrestart=50, rtol=1e-12,
                  atol=1e-30, pc_kind=_lib.PC_ILU0, mixed=False,
-                 include_element_loads=True, segments=False):
+                 include_element_loads=True, segments=False, lev_fill=0):
         self.model = model
         F = torch.as_tensor(np.asarray(loads, np.float64) if not
                             torch.is_tensor(loads) else loads,
@@ -53,7 +53,7 @@ class StaticSolver:
             model.set_segments(model.prob["seg_elem_ptr"])
         self.mat = model.new_mat()
         prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-        self.pc = Pc(self.mat, pc_kind, prec)
+        self.pc = Pc(self.mat, pc_kind, prec, lev_fill=lev_fill)
         self.ksm = Ksm(self.mat, self.pc, m, nrestart, mixed)
         self.ksm.set_tolerances(rtol, atol)
         if segments:

@@ -375,7 +375,8 @@ class GpuModel:
 
 
 def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
-                   pc_kind=_lib.PC_ILU0, mixed=False, funcs=(0, 1)):
+                   pc_kind=_lib.PC_ILU0, mixed=False, funcs=(0, 1),
+                   lev_fill=0):
     """Linear static solve + adjoint gradients on the GPU, following the
     reference harness (tests/integration_tests/static_analysis_base_test.py:
     359-427): K(u=0) and R(0), ILU(0), GMRES for R - f, functions, dfdu,
@@ -386,7 +387,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     mat = model.new_mat()
     model.assemble_jacobian(u0, mat, res)
     prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-    pc = Pc(mat, pc_kind, prec)
+    pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
     pc.factor()
     ksm = Ksm(mat, pc, m, nrestart, mixed)
     ksm.set_tolerances(rtol, atol)
@@ -414,7 +415,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
 
 
 def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
-                    pc_kind=_lib.PC_ILU0, mixed=False, func=1):
+                    pc_kind=_lib.PC_ILU0, mixed=False, func=1, lev_fill=0):
     """Independent meshes (element / node segments set from the problem's
     seg_elem_ptr / seg_node_ptr) under several load cases, solved and
     differentiated together: one batched GMRES for all forward solves, the
@@ -433,7 +434,7 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     mat = model.new_mat()
     model.assemble_jacobian(u0, mat, model.vec())
     prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-    pc = Pc(mat, pc_kind, prec)
+    pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
     pc.factor()
     ksm = Ksm(mat, pc, m, nrestart, mixed)
     ksm.set_tolerances(rtol, atol)
