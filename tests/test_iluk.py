@@ -151,14 +151,15 @@ def test_gmres_iluk_thin_plate(gpu):
     for lev in (0, 1, 3):
         pc = problem.Pc(mat, lev_fill=lev)
         pc.factor()
-        ksm = problem.Ksm(mat, pc, 200, 50)
+        # ILU(0) only has to show that it does not converge quickly
+        ksm = problem.Ksm(mat, pc, 200, 2 if lev == 0 else 50)
         ksm.set_tolerances(1e-12)
         x, flags[lev] = ksm.solve(b)
         iters[lev] = ksm.iters
         if lev > 0:
             assert flags[lev] == 1, (flags, iters)
             check(x.cpu().numpy())
-    assert iters[3] < iters[1] < iters[0], iters
+    assert iters[3] < iters[1] < 600 <= iters[0], iters
     pc = problem.Pc(mat, L.PC_ILU0, L.PREC_FP32, lev_fill=3)
     pc.factor()
     ksm = problem.Ksm(mat, pc, 200, 50, mixed=True)
