@@ -113,8 +113,14 @@ class pyTACS:
 class StaticProblem:
     """Linear static analysis (tacs/problems/static.py) on the GPU."""
 
+    # The reference factors the matrix completely (PCFillLevel 1000 on a
+    # Schur matrix, tacs/problems/static.py:59,329); the GPU path has no
+    # direct factorisation, so the fill level is capped at MAX_FILL (block
+    # ILU(5)) and the Krylov space is larger than the reference's 10.
+    MAX_FILL = 5
     defaults = {"subSpaceSize": 100, "nRestarts": 20,
-                "L2ConvergenceRel": 1e-12, "L2Convergence": 1e-30}
+                "L2ConvergenceRel": 1e-12, "L2Convergence": 1e-30,
+                "PCFillLevel": 1000}
 
     def __init__(self, name, fea, options=None):
         self.name, self.fea = name, fea
@@ -212,7 +218,9 @@ class StaticProblem:
                 rec["xpts"] = self._xpts
             self._model = GpuModel(rec)
             self._mat = self._model.new_mat()
-            self._pc = Pc(self._mat)
+            lev = max(0, min(int(self.options["PCFillLevel"]),
+                             self.MAX_FILL))
+            self._pc = Pc(self._mat, lev_fill=lev)
             self._ksm = Ksm(self._mat, self._pc, self.options["subSpaceSize"],
                             self.options["nRestarts"])
             self._ksm.set_tolerances(self.options["L2ConvergenceRel"],
