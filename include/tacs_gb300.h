@@ -1,7 +1,7 @@
 /*
   tacs_gb300 -- C ABI of the GB300 (sm_103a) implementation of the TACS
   finite-element hot path: MITC4-shell and hex8 residual / Jacobian assembly
-  into 6x6 / 3x3 block-CSR, the BCSR mat-vec, ILU(0) / block-Jacobi
+  into 6x6 / 3x3 block-CSR, the BCSR mat-vec, ILU(k) / block-Jacobi
   preconditioning inside GMRES, and the adjoint products.
 
   Conventions
@@ -46,7 +46,7 @@ extern "C" {
 #define TG_MAT_NORMAL 0    /* MatrixOrientation TACS_MAT_NORMAL */
 #define TG_MAT_TRANSPOSE 1 /* TACS_MAT_TRANSPOSE */
 
-#define TG_PC_ILU0 0        /* TACSAdditiveSchwarz(mat, 0, fill): ILU(0) */
+#define TG_PC_ILU0 0        /* TACSAdditiveSchwarz(mat, levFill, fill): ILU */
 #define TG_PC_BLOCK_JACOBI 1 /* inverted diagonal blocks only */
 #define TG_PC_ILU0_COLORED 2 /* ILU(0) of a multicolour node reordering */
 

@@ -162,7 +162,8 @@ class BCSRMat {
   tg_mat *m_ = nullptr;
 };
 
-/* TACSAdditiveSchwarz(mat, levFill = 0, fill): block ILU(0). */
+/* TACSAdditiveSchwarz(mat, levFill, fill): block ILU(levFill) on the
+   computeILUk pattern (levFill = 0: the matrix's own pattern). */
 class TACSAdditiveSchwarz {
  public:
   TACSAdditiveSchwarz(BCSRMat *mat, int levFill, double fill,
