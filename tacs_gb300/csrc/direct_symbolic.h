@@ -1,0 +1,445 @@
+// Host analysis of the direct (complete) block factorisation of a
+// symmetric block pattern: header-only C++ without CUDA, so the library and
+// the CPU tests compile the same code.
+//
+//   nested_dissection   fill-reducing node order (level-structure bisection)
+//   analyse             elimination tree, column structures, fundamental
+//                       supernodes, their fronts, the supernodal tree and
+//                       its levels, the extend-add maps and the map of the
+//                       matrix's lower blocks into the fronts
+//
+// The numeric phase is a multifrontal block Cholesky (the stiffness matrix
+// with row-and-column boundary conditions is symmetric positive definite):
+// for each supernode, children before parents, its front (the supernode's
+// rows x its columns, dense, bs x bs per block) gathers the matrix's lower
+// blocks and the children's update matrices, the leading diagonal block is
+// factored, the rows below are solved against it, and the Schur update of
+// the rows below goes to the parent.  This replaces the complete-fill
+// row-by-row factorisation of the reference's direct preconditioner
+// (TACSSchurPc with levFill 1000, src/bpmat/TACSSchurMat.cpp:1510-1600,
+// and BCSRMat::computeILUk, src/bpmat/BCSRMat.cpp:625) with the same
+// solution.
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace tg {
+namespace direct {
+
+// Nested dissection by level structures.  A connected part larger than
+// `leaf` vertices is split at a level set of a breadth-first search from a
+// pseudo-peripheral vertex (the level where the cumulative count passes
+// half the part): the levels before it and after it share no edge, so the
+// level set separates them.  Each part is ordered before its separator,
+// recursively, so the separator rows come last and the complete factor
+// fills only within the parts' own blocks and the separators.  Parts of at
+// most `leaf` vertices are ordered by reverse Cuthill-McKee (breadth-first
+// from a pseudo-peripheral vertex, reversed).  Disconnected parts are
+// ordered one after the other.  The pattern must be symmetric; perm[r] is
+// the original row placed at position r.
+class NestedDissection {
+ public:
+  NestedDissection(const std::vector<int> &rowp, const std::vector<int> &cols,
+                   int leaf)
+      : rowp_(rowp), cols_(cols), leaf_(leaf < 1 ? 1 : leaf) {}
+
+  std::vector<int> order() {
+    const int n = (int)rowp_.size() - 1;
+    part_.assign(n, 0);
+    dist_.assign(n, -1);
+    out_.clear();
+    out_.reserve(n);
+    std::vector<int> all(n);
+    for (int i = 0; i < n; i++) all[i] = i;
+    next_id_ = 1;
+    split(all, 0);
+    return out_;
+  }
+
+ private:
+  const std::vector<int> &rowp_, &cols_;
+  int leaf_;
+  int next_id_ = 1;
+  std::vector<int> part_;  // subgraph id of each unordered vertex, -1 once
+                           // ordered or held for a separator
+  std::vector<int> dist_;
+  std::vector<int> out_;
+
+  // breadth-first search inside subgraph `id` from src: visit order in
+  // `vis`, distances in dist_ (reset by the caller through `vis`)
+  void bfs(int id, int src, std::vector<int> &vis) {
+    vis.clear();
+    vis.push_back(src);
+    dist_[src] = 0;
+    for (size_t h = 0; h < vis.size(); h++) {
+      const int v = vis[h];
+      for (int j = rowp_[v]; j < rowp_[v + 1]; j++) {
+        const int w = cols_[j];
+        if (part_[w] == id && dist_[w] < 0) {
+          dist_[w] = dist_[v] + 1;
+          vis.push_back(w);
+        }
+      }
+    }
+  }
+  void clear_dist(const std::vector<int> &vis) {
+    for (int v : vis) dist_[v] = -1;
+  }
+  int degree(int v) const { return rowp_[v + 1] - rowp_[v]; }
+
+  // pseudo-peripheral vertex of the connected part containing start:
+  // repeated searches from the farthest, lowest-degree vertex while the
+  // eccentricity grows; vis / dist_ keep the search from the returned
+  // vertex
+  int peripheral(int id, int start, std::vector<int> &vis) {
+    int src = start, ecc = -1;
+    for (int it = 0; it < 8; it++) {
+      bfs(id, src, vis);
+      const int far = dist_[vis.back()];
+      if (far <= ecc) break;
+      ecc = far;
+      int best = vis.back();
+      for (size_t k = vis.size(); k-- > 0;) {
+        const int v = vis[k];
+        if (dist_[v] < far) break;
+        if (degree(v) < degree(best)) best = v;
+      }
+      if (best == src) break;
+      clear_dist(vis);
+      src = best;
+    }
+    return src;
+  }
+
+  void emit_rcm(const std::vector<int> &vis) {
+    for (size_t k = vis.size(); k-- > 0;) {
+      out_.push_back(vis[k]);
+      part_[vis[k]] = -1;
+    }
+  }
+
+  // order the vertices `verts` (all with part_ == id), one connected part
+  // after the other
+  void split(const std::vector<int> &verts, int id) {
+    if (verts.empty()) return;
+    std::vector<int> vis;
+    bfs(id, verts[0], vis);
+    clear_dist(vis);
+    if (vis.size() == verts.size()) {
+      split_connected(verts, id);
+      return;
+    }
+    std::vector<std::pair<std::vector<int>, int>> parts;
+    for (int v : verts) {
+      if (part_[v] != id) continue;
+      bfs(id, v, vis);
+      clear_dist(vis);
+      const int cid = next_id_++;
+      for (int w : vis) part_[w] = cid;
+      parts.push_back({vis, cid});
+    }
+    for (auto &pc : parts) split_connected(pc.first, pc.second);
+  }
+
+  void split_connected(const std::vector<int> &verts, int id) {
+    std::vector<int> vis;
+    peripheral(id, verts[0], vis);
+    const int nlev = dist_[vis.back()] + 1;
+    if ((int)verts.size() <= leaf_ || nlev < 3) {
+      clear_dist(vis);
+      emit_rcm(vis);
+      return;
+    }
+    // separator level: the smallest level set among those where the
+    // cumulative count lies between 35 % and 65 % of the part (the median
+    // level when none does), kept off the first and last level so that
+    // both sides are non-empty
+    std::vector<int> count(nlev, 0);
+    for (int v : vis) count[dist_[v]]++;
+    const double nv = (double)verts.size();
+    size_t acc = 0;
+    int sep = -1, median = 1;
+    for (int L = 1; L < nlev - 1; L++) {
+      const size_t before = acc + count[L - 1];
+      acc = before;
+      const double lo = before / nv, hi = (before + count[L]) / nv;
+      if (lo < 0.5) median = L;
+      if (hi >= 0.35 && lo <= 0.65 && (sep < 0 || count[L] < count[sep]))
+        sep = L;
+    }
+    if (sep < 0) sep = median;
+    const int ida = next_id_++, idb = next_id_++;
+    std::vector<int> a, b, sp;
+    for (int v : vis) {
+      const int d = dist_[v];
+      if (d < sep) {
+        part_[v] = ida;
+        a.push_back(v);
+      } else if (d > sep) {
+        part_[v] = idb;
+        b.push_back(v);
+      } else {
+        part_[v] = -1;
+        sp.push_back(v);
+      }
+    }
+    clear_dist(vis);
+    split(a, ida);
+    split(b, idb);
+    for (int v : sp) out_.push_back(v);
+  }
+};
+
+inline std::vector<int> nested_dissection(const std::vector<int> &rowp,
+                                          const std::vector<int> &cols,
+                                          int leaf = 64) {
+  NestedDissection nd(rowp, cols, leaf);
+  return nd.order();
+}
+
+
+
+// Result of the analysis.  Indices called "position" are in the permuted
+// order (position r holds original row perm[r]).
+struct Analysis {
+  int n = 0;                  // block rows
+  std::vector<int> perm, iperm;
+  std::vector<int> parent;    // elimination tree over positions, -1 = root
+  // supernode s owns the consecutive positions [sn_col[s], sn_col[s + 1])
+  std::vector<int> sn_col;
+  // front rows of s: its own positions, then the positions below them in
+  // increasing order; rows [sn_rowptr[s], sn_rowptr[s + 1]) of sn_rows
+  std::vector<int> sn_rowptr, sn_rows;
+  std::vector<int> sn_parent;  // supernodal tree, -1 = root
+  // levels of the supernodal tree (0 = leaves; a supernode's children are
+  // all on lower levels): supernodes of level L are
+  // level_sn[level_ptr[L] .. level_ptr[L + 1])
+  std::vector<int> level_ptr, level_sn;
+  // extend-add: the update rows of s (its front rows after its own
+  // columns) as row offsets inside the parent's front
+  std::vector<int> ea_ptr, ea_rel;  // ea_ptr per supernode
+  // the matrix's blocks in the lower triangle of the fronts: for block k
+  // of supernode s (asm_ptr[s] .. asm_ptr[s + 1]): the matrix block
+  // asm_blk[k] goes to front block row asm_row[k], column asm_colidx[k]
+  std::vector<int> asm_ptr, asm_blk, asm_row, asm_col;
+  // totals
+  int64_t factor_blocks = 0;   // blocks of L (lower triangle, diagonal incl.)
+  int64_t front_blocks = 0;    // sum over fronts of rows x rows
+  int64_t flops_scalar(int bs) const;
+};
+
+// Dense work of the numeric phase in scalar flops for block size bs:
+// per supernode with m front rows and c own columns (scalar sizes
+// M = m bs, C = c bs): Cholesky C^3 / 3, triangular solve (M - C) C^2,
+// update (M - C)^2 C.
+inline int64_t Analysis::flops_scalar(int bs) const {
+  int64_t f = 0;
+  for (size_t s = 0; s + 1 < sn_col.size(); s++) {
+    const int64_t c = (int64_t)(sn_col[s + 1] - sn_col[s]) * bs;
+    const int64_t m = (int64_t)(sn_rowptr[s + 1] - sn_rowptr[s]) * bs;
+    f += c * c * c / 3 + (m - c) * c * c + (m - c) * (m - c) * c;
+  }
+  return f;
+}
+
+// rowp / cols: symmetric block pattern with sorted columns and every
+// diagonal present (the assembler's); perm: the node order (new -> old).
+inline Analysis analyse(const std::vector<int> &rowp,
+                        const std::vector<int> &cols,
+                        const std::vector<int> &perm) {
+  Analysis a;
+  const int n = (int)rowp.size() - 1;
+  a.n = n;
+  a.perm = perm;
+  a.iperm.assign(n, 0);
+  for (int r = 0; r < n; r++) a.iperm[perm[r]] = r;
+
+  // lower neighbours of each position (positions < r), sorted
+  std::vector<int> lptr(n + 1, 0), ladj;
+  ladj.reserve(cols.size() / 2 + n);
+  for (int r = 0; r < n; r++) {
+    const int o = perm[r];
+    const size_t b = ladj.size();
+    for (int j = rowp[o]; j < rowp[o + 1]; j++) {
+      const int c = a.iperm[cols[j]];
+      if (c < r) ladj.push_back(c);
+    }
+    std::sort(ladj.begin() + b, ladj.end());
+    lptr[r + 1] = (int)ladj.size();
+  }
+
+  // elimination tree (Liu's algorithm with path compression)
+  a.parent.assign(n, -1);
+  std::vector<int> anc(n, -1);
+  for (int r = 0; r < n; r++) {
+    for (int k = lptr[r]; k < lptr[r + 1]; k++) {
+      int i = ladj[k];
+      while (anc[i] != -1 && anc[i] != r) {
+        const int t = anc[i];
+        anc[i] = r;
+        i = t;
+      }
+      if (anc[i] == -1) {
+        anc[i] = r;
+        a.parent[i] = r;
+      }
+    }
+  }
+
+  // column structures of L below the diagonal: the upper neighbours of
+  // column j in A, merged with the structures of j's children minus j
+  // (children come before parents, so one pass in increasing order)
+  std::vector<int> uptr(n + 1, 0), uadj;  // upper neighbours (> r)
+  {
+    std::vector<int> cnt(n, 0);
+    for (int r = 0; r < n; r++)
+      for (int k = lptr[r]; k < lptr[r + 1]; k++) cnt[ladj[k]]++;
+    for (int r = 0; r < n; r++) uptr[r + 1] = uptr[r] + cnt[r];
+    uadj.resize(uptr[n]);
+    std::vector<int> fill(uptr.begin(), uptr.end() - 1);
+    for (int r = 0; r < n; r++)  // increasing r: rows of each list sorted
+      for (int k = lptr[r]; k < lptr[r + 1]; k++)
+        uadj[fill[ladj[k]]++] = r;
+  }
+  std::vector<int> first_child(n, -1), next_sib(n, -1);
+  for (int j = n - 1; j >= 0; j--) {
+    const int p = a.parent[j];
+    if (p >= 0) {
+      next_sib[j] = first_child[p];
+      first_child[p] = j;
+    }
+  }
+  std::vector<std::vector<int>> colstruct(n);
+  std::vector<int> count(n, 0), nchild(n, 0);
+  std::vector<int> mark(n, -1);
+  for (int j = 0; j < n; j++) {
+    std::vector<int> &s = colstruct[j];
+    for (int k = uptr[j]; k < uptr[j + 1]; k++) {
+      s.push_back(uadj[k]);
+      mark[uadj[k]] = j;
+    }
+    for (int c = first_child[j]; c >= 0; c = next_sib[c]) {
+      nchild[j]++;
+      for (int i : colstruct[c])
+        if (i != j && mark[i] != j) {
+          mark[i] = j;
+          s.push_back(i);
+        }
+    }
+    std::sort(s.begin(), s.end());
+    count[j] = (int)s.size();
+  }
+
+  // fundamental supernodes: j + 1 joins j's supernode when it is j's
+  // parent, j is its only child and the structures nest (count drops by 1)
+  a.sn_col.clear();
+  a.sn_col.push_back(0);
+  for (int j = 1; j < n; j++) {
+    const bool join = a.parent[j - 1] == j && nchild[j] == 1 &&
+                      count[j - 1] == count[j] + 1;
+    if (!join) a.sn_col.push_back(j);
+  }
+  if (n > 0) a.sn_col.push_back(n);
+  const int ns = (int)a.sn_col.size() - 1;
+  std::vector<int> sn_of(n);
+  for (int s = 0; s < ns; s++)
+    for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++) sn_of[j] = s;
+
+  // fronts: own positions, then the structure of the supernode's first
+  // column below its last column
+  a.sn_rowptr.assign(ns + 1, 0);
+  a.sn_rows.clear();
+  for (int s = 0; s < ns; s++) {
+    const int c0 = a.sn_col[s], c1 = a.sn_col[s + 1];
+    for (int j = c0; j < c1; j++) a.sn_rows.push_back(j);
+    for (int i : colstruct[c0])
+      if (i >= c1) a.sn_rows.push_back(i);
+    a.sn_rowptr[s + 1] = (int)a.sn_rows.size();
+    const int64_t m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    const int64_t c = c1 - c0;
+    a.front_blocks += m * m;
+    a.factor_blocks += c * (c + 1) / 2 + (m - c) * c;
+  }
+  colstruct.clear();
+  colstruct.shrink_to_fit();
+
+  a.sn_parent.assign(ns, -1);
+  for (int s = 0; s < ns; s++) {
+    const int p = a.parent[a.sn_col[s + 1] - 1];
+    a.sn_parent[s] = p < 0 ? -1 : sn_of[p];
+  }
+
+  // levels: leaves 0, a parent one above its highest child
+  std::vector<int> lev(ns, 0);
+  int nlev = ns > 0 ? 1 : 0;
+  for (int s = 0; s < ns; s++) {  // children precede parents in positions
+    const int p = a.sn_parent[s];
+    if (p >= 0 && lev[p] < lev[s] + 1) lev[p] = lev[s] + 1;
+    nlev = std::max(nlev, lev[s] + 1);
+  }
+  a.level_ptr.assign(nlev + 1, 0);
+  for (int s = 0; s < ns; s++) a.level_ptr[lev[s] + 1]++;
+  for (int L = 0; L < nlev; L++) a.level_ptr[L + 1] += a.level_ptr[L];
+  a.level_sn.assign(ns, 0);
+  {
+    std::vector<int> fill(a.level_ptr.begin(), a.level_ptr.end() - 1);
+    for (int s = 0; s < ns; s++) a.level_sn[fill[lev[s]]++] = s;
+  }
+
+  // extend-add maps: each update row of s as a row of the parent's front
+  a.ea_ptr.assign(ns + 1, 0);
+  a.ea_rel.clear();
+  for (int s = 0; s < ns; s++) {
+    const int p = a.sn_parent[s];
+    const int own = a.sn_col[s + 1] - a.sn_col[s];
+    const int *rows = &a.sn_rows[a.sn_rowptr[s]];
+    const int m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    if (p >= 0) {
+      const int *prow = &a.sn_rows[a.sn_rowptr[p]];
+      const int pm = a.sn_rowptr[p + 1] - a.sn_rowptr[p];
+      int q = 0;
+      for (int k = own; k < m; k++) {  // both lists sorted
+        while (q < pm && prow[q] < rows[k]) q++;
+        a.ea_rel.push_back(q);  // q < pm: the parent's front holds it
+      }
+    }
+    a.ea_ptr[s + 1] = (int)a.ea_rel.size();
+  }
+
+  // the matrix's lower blocks (position i >= j) in the front of j's
+  // supernode: block row = index of i in the front rows, block column =
+  // j - first column
+  a.asm_ptr.assign(ns + 1, 0);
+  a.asm_blk.clear();
+  a.asm_row.clear();
+  a.asm_col.clear();
+  for (int s = 0; s < ns; s++) {
+    const int *rows = &a.sn_rows[a.sn_rowptr[s]];
+    const int m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++) {
+      const int oj = perm[j];
+      // column j of the permuted matrix = row oj of A (symmetric pattern);
+      // the block stored at (row perm[i], col oj) is A_(i, j)
+      for (int k = rowp[oj]; k < rowp[oj + 1]; k++) {
+        const int i = a.iperm[cols[k]];
+        if (i < j) continue;
+        const int pos = (int)(std::lower_bound(rows, rows + m, i) - rows);
+        // block (i, j) of A lives in row perm[i]: find column oj there
+        const int oi = cols[k];
+        const int *rb = &cols[rowp[oi]], *re = &cols[rowp[oi + 1]];
+        const int blk = rowp[oi] + (int)(std::lower_bound(rb, re, oj) - rb);
+        a.asm_blk.push_back(blk);
+        a.asm_row.push_back(pos);
+        a.asm_col.push_back(j - a.sn_col[s]);
+      }
+    }
+    a.asm_ptr[s + 1] = (int)a.asm_blk.size();
+  }
+  return a;
+}
+
+}  // namespace direct
+}  // namespace tg

@@ -1,0 +1,177 @@
+// CPU check of the direct factorisation's host analysis
+// (tacs_gb300/csrc/direct_symbolic.h): a plain dense multifrontal block
+// Cholesky driven by the analysis, and the triangular solves, on the host.
+// Built by tests/test_direct_symbolic.py with g++ and called through
+// ctypes; test infrastructure only.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "direct_symbolic.h"
+
+using tg::direct::Analysis;
+
+namespace {
+
+// Cholesky of the leading c x c block of the row-major m x m matrix F (lower
+// triangle), then L21 = F21 L11^-T and F22 -= L21 L21^T.  Returns 0 or the
+// 1-based failing pivot.
+int front_factor(double *F, int m, int c) {
+  for (int k = 0; k < c; k++) {
+    double d = F[(size_t)k * m + k];
+    for (int q = 0; q < k; q++) d -= F[(size_t)k * m + q] * F[(size_t)k * m + q];
+    if (!(d > 0.0)) return k + 1;
+    d = std::sqrt(d);
+    F[(size_t)k * m + k] = d;
+    for (int i = k + 1; i < m; i++) {
+      double s = F[(size_t)i * m + k];
+      for (int q = 0; q < k; q++) s -= F[(size_t)i * m + q] * F[(size_t)k * m + q];
+      F[(size_t)i * m + k] = s / d;
+    }
+  }
+  for (int i = c; i < m; i++)
+    for (int j = c; j <= i; j++) {
+      double s = 0.0;
+      for (int q = 0; q < c; q++) s += F[(size_t)i * m + q] * F[(size_t)j * m + q];
+      F[(size_t)i * m + j] -= s;
+    }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Analysis statistics for the node order `perm` (nullptr: nested
+// dissection with `leaf`): out = {supernodes, levels, factor blocks, front
+// blocks, scalar flops for bs}.
+int dc_analyse(int n, const int *rowp, const int *cols, const int *perm,
+               int leaf, int bs, double *out) {
+  std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
+  std::vector<int> p = perm ? std::vector<int>(perm, perm + n)
+                            : tg::direct::nested_dissection(rp, cs, leaf);
+  std::vector<int> seen(n, 0);
+  for (int v : p) {
+    if (v < 0 || v >= n || seen[v]) return -1;
+    seen[v] = 1;
+  }
+  Analysis a = tg::direct::analyse(rp, cs, p);
+  out[0] = (double)(a.sn_col.size() - 1);
+  out[1] = (double)(a.level_ptr.size() - 1);
+  out[2] = (double)a.factor_blocks;
+  out[3] = (double)a.front_blocks;
+  out[4] = (double)a.flops_scalar(bs);
+  return 0;
+}
+
+// x = A^-1 b for the symmetric positive definite BCSR matrix (rowp, cols,
+// vals; bs x bs row-major blocks), factored by the multifrontal scheme in
+// nested-dissection order.
+int dc_solve(int n, int bs, const int *rowp, const int *cols,
+             const double *vals, const double *b, double *x, int leaf) {
+  std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
+  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf);
+  Analysis a = tg::direct::analyse(rp, cs, perm);
+  const int ns = (int)a.sn_col.size() - 1;
+  const size_t b2 = (size_t)bs * bs;
+  std::vector<std::vector<double>> L(ns), U(ns);
+  for (int L0 = 0; L0 + 1 < (int)a.level_ptr.size(); L0++) {
+    for (int t = a.level_ptr[L0]; t < a.level_ptr[L0 + 1]; t++) {
+      const int s = a.level_sn[t];
+      const int mb = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+      const int cb = a.sn_col[s + 1] - a.sn_col[s];
+      const int m = mb * bs, c = cb * bs;
+      std::vector<double> F((size_t)m * m, 0.0);
+      for (int k = a.asm_ptr[s]; k < a.asm_ptr[s + 1]; k++) {
+        const double *blk = &vals[b2 * a.asm_blk[k]];
+        const int r0 = a.asm_row[k] * bs, c0 = a.asm_col[k] * bs;
+        for (int r = 0; r < bs; r++)
+          for (int q = 0; q < bs; q++)
+            F[(size_t)(r0 + r) * m + c0 + q] += blk[r * bs + q];
+      }
+      // children's update matrices (children sit on lower levels)
+      for (int ch = 0; ch < s; ch++) {
+        if (a.sn_parent[ch] != s) continue;
+        const int cm = (a.sn_rowptr[ch + 1] - a.sn_rowptr[ch]) -
+                       (a.sn_col[ch + 1] - a.sn_col[ch]);
+        const int *rel = &a.ea_rel[a.ea_ptr[ch]];
+        const std::vector<double> &Uc = U[ch];
+        const int um = cm * bs;
+        for (int k1 = 0; k1 < cm; k1++)
+          for (int k2 = 0; k2 <= k1; k2++)
+            for (int r = 0; r < bs; r++)
+              for (int q = 0; q < bs; q++) {
+                const int ur = k1 * bs + r, uc = k2 * bs + q;
+                if (uc > ur) continue;
+                F[(size_t)(rel[k1] * bs + r) * m + rel[k2] * bs + q] +=
+                    Uc[(size_t)ur * um + uc];
+              }
+        U[ch].clear();
+        U[ch].shrink_to_fit();
+      }
+      // mirror the diagonal blocks' upper halves are never read
+      const int rc = front_factor(F.data(), m, c);
+      if (rc) return rc;
+      L[s].assign((size_t)m * c, 0.0);
+      for (int i = 0; i < m; i++)
+        for (int j = 0; j < c && j <= i; j++)
+          L[s][(size_t)i * c + j] = F[(size_t)i * m + j];
+      const int um = m - c;
+      U[s].assign((size_t)um * um, 0.0);
+      for (int i = 0; i < um; i++)
+        for (int j = 0; j <= i; j++)
+          U[s][(size_t)i * um + j] = F[(size_t)(c + i) * m + c + j];
+    }
+  }
+  // solves in positions
+  std::vector<double> y((size_t)n * bs);
+  for (int r = 0; r < n; r++)
+    for (int q = 0; q < bs; q++) y[(size_t)r * bs + q] = b[(size_t)perm[r] * bs + q];
+  for (int s = 0; s < ns; s++) {
+    const int mb = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    const int cb = a.sn_col[s + 1] - a.sn_col[s];
+    const int m = mb * bs, c = cb * bs;
+    const int *rows = &a.sn_rows[a.sn_rowptr[s]];
+    std::vector<double> z(m);
+    for (int k = 0; k < mb; k++)
+      for (int q = 0; q < bs; q++) z[k * bs + q] = y[(size_t)rows[k] * bs + q];
+    for (int i = 0; i < c; i++) {
+      double v = z[i];
+      for (int j = 0; j < i; j++) v -= L[s][(size_t)i * c + j] * z[j];
+      z[i] = v / L[s][(size_t)i * c + i];
+    }
+    for (int i = c; i < m; i++) {
+      double v = 0.0;
+      for (int j = 0; j < c; j++) v += L[s][(size_t)i * c + j] * z[j];
+      z[i] -= v;
+    }
+    for (int k = 0; k < mb; k++)
+      for (int q = 0; q < bs; q++) y[(size_t)rows[k] * bs + q] = z[k * bs + q];
+  }
+  for (int s = ns - 1; s >= 0; s--) {
+    const int mb = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    const int cb = a.sn_col[s + 1] - a.sn_col[s];
+    const int m = mb * bs, c = cb * bs;
+    const int *rows = &a.sn_rows[a.sn_rowptr[s]];
+    std::vector<double> z(m);
+    for (int k = 0; k < mb; k++)
+      for (int q = 0; q < bs; q++) z[k * bs + q] = y[(size_t)rows[k] * bs + q];
+    for (int j = 0; j < c; j++) {
+      double v = 0.0;
+      for (int i = c; i < m; i++) v += L[s][(size_t)i * c + j] * z[i];
+      z[j] -= v;
+    }
+    for (int i = c - 1; i >= 0; i--) {
+      double v = z[i];
+      for (int j = i + 1; j < c; j++) v -= L[s][(size_t)j * c + i] * z[j];
+      z[i] = v / L[s][(size_t)i * c + i];
+    }
+    for (int k = 0; k < cb; k++)
+      for (int q = 0; q < bs; q++) y[(size_t)rows[k] * bs + q] = z[k * bs + q];
+  }
+  for (int r = 0; r < n; r++)
+    for (int q = 0; q < bs; q++) x[(size_t)perm[r] * bs + q] = y[(size_t)r * bs + q];
+  return 0;
+}
+
+}  // extern "C"
