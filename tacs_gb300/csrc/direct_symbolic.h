@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <iterator>
+#include <map>
 #include <vector>
 
 namespace tg {
@@ -225,9 +227,17 @@ struct Analysis {
   // of supernode s (asm_ptr[s] .. asm_ptr[s + 1]): the matrix block
   // asm_blk[k] goes to front block row asm_row[k], column asm_colidx[k]
   std::vector<int> asm_ptr, asm_blk, asm_row, asm_col;
+  // storage plan, in blocks of bs x bs: supernode s keeps its factor
+  // panel (front rows x own columns, dense) at l_off[s] of an array of
+  // l_total blocks, and its update matrix ((front rows - own columns)^2,
+  // dense) at u_off[s] of a pool of u_peak blocks; the pool is reused, an
+  // update living from its supernode's level to its parent's level
+  std::vector<int64_t> l_off, u_off;
+  int64_t l_total = 0, u_peak = 0;
   // totals
   int64_t factor_blocks = 0;   // blocks of L (lower triangle, diagonal incl.)
   int64_t front_blocks = 0;    // sum over fronts of rows x rows
+  int64_t zero_blocks = 0;     // explicit zeros added by amalgamation
   int64_t flops_scalar(int bs) const;
 };
 
@@ -245,11 +255,20 @@ inline int64_t Analysis::flops_scalar(int bs) const {
   return f;
 }
 
+struct Analysis;
+inline void plan_storage(Analysis &a);
+
+struct AnalysisOptions {
+  bool amalgamate = true;  // relaxed supernode amalgamation
+  int max_columns = 64;    // widest merged supernode (block columns)
+};
+
 // rowp / cols: symmetric block pattern with sorted columns and every
 // diagonal present (the assembler's); perm: the node order (new -> old).
 inline Analysis analyse(const std::vector<int> &rowp,
                         const std::vector<int> &cols,
-                        const std::vector<int> &perm) {
+                        const std::vector<int> &perm,
+                        const AnalysisOptions &opt = AnalysisOptions()) {
   Analysis a;
   const int n = (int)rowp.size() - 1;
   a.n = n;
@@ -335,42 +354,108 @@ inline Analysis analyse(const std::vector<int> &rowp,
 
   // fundamental supernodes: j + 1 joins j's supernode when it is j's
   // parent, j is its only child and the structures nest (count drops by 1)
-  a.sn_col.clear();
-  a.sn_col.push_back(0);
+  std::vector<int> first;
+  first.push_back(0);
   for (int j = 1; j < n; j++) {
     const bool join = a.parent[j - 1] == j && nchild[j] == 1 &&
                       count[j - 1] == count[j] + 1;
-    if (!join) a.sn_col.push_back(j);
+    if (!join) first.push_back(j);
   }
-  if (n > 0) a.sn_col.push_back(n);
-  const int ns = (int)a.sn_col.size() - 1;
+  int ns = (int)first.size();
+  if (n == 0) ns = 0;
+  std::vector<int> last(ns);  // one past the last column
+  for (int s = 0; s < ns; s++) last[s] = s + 1 < ns ? first[s + 1] : n;
   std::vector<int> sn_of(n);
   for (int s = 0; s < ns; s++)
-    for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++) sn_of[j] = s;
-
-  // fronts: own positions, then the structure of the supernode's first
-  // column below its last column
-  a.sn_rowptr.assign(ns + 1, 0);
-  a.sn_rows.clear();
+    for (int j = first[s]; j < last[s]; j++) sn_of[j] = s;
+  // fronts: own positions, then the structure of the first column below
+  // the last column
+  std::vector<std::vector<int>> rows(ns);
+  std::vector<int> spar(ns, -1);
   for (int s = 0; s < ns; s++) {
-    const int c0 = a.sn_col[s], c1 = a.sn_col[s + 1];
-    for (int j = c0; j < c1; j++) a.sn_rows.push_back(j);
-    for (int i : colstruct[c0])
-      if (i >= c1) a.sn_rows.push_back(i);
-    a.sn_rowptr[s + 1] = (int)a.sn_rows.size();
-    const int64_t m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
-    const int64_t c = c1 - c0;
-    a.front_blocks += m * m;
-    a.factor_blocks += c * (c + 1) / 2 + (m - c) * c;
+    for (int j = first[s]; j < last[s]; j++) rows[s].push_back(j);
+    for (int i : colstruct[first[s]])
+      if (i >= last[s]) rows[s].push_back(i);
+    const int p = a.parent[last[s] - 1];
+    spar[s] = p < 0 ? -1 : sn_of[p];
   }
   colstruct.clear();
   colstruct.shrink_to_fit();
 
-  a.sn_parent.assign(ns, -1);
-  for (int s = 0; s < ns; s++) {
-    const int p = a.parent[a.sn_col[s + 1] - 1];
-    a.sn_parent[s] = p < 0 ? -1 : sn_of[p];
+  // relaxed amalgamation: a child whose columns end where its parent's
+  // begin is merged into the parent when the explicit zeros this adds to
+  // the merged factor stay below a fraction that shrinks with its width
+  // (wide dense fronts suit the GPU, but not at the price of much extra
+  // work); merged rows = the child's columns + the parent's rows, which
+  // hold every row of the child
+  std::vector<int64_t> zeros(ns, 0);
+  std::vector<char> alive(ns, 1);
+  // a merged supernode's parent links resolve through rep (union-find)
+  std::vector<int> rep(ns);
+  for (int t = 0; t < ns; t++) rep[t] = t;
+  auto find = [&](int t) {
+    while (rep[t] != t) t = rep[t] = rep[rep[t]];
+    return t;
+  };
+  if (opt.amalgamate) {
+    auto entries = [](int64_t c, int64_t m) {
+      return c * (c + 1) / 2 + c * (m - c);
+    };
+    for (int p = ns - 1; p > 0; p--) {
+      if (!alive[p]) continue;
+      while (true) {
+        if (first[p] == 0) break;
+        const int c = sn_of[first[p] - 1];
+        if (!alive[c] || spar[c] < 0 || find(spar[c]) != p) break;
+        const int64_t nc = last[c] - first[c], np = last[p] - first[p];
+        const int64_t mc = (int64_t)rows[c].size(),
+                      mp = (int64_t)rows[p].size();
+        const int64_t add = nc * (mp - (mc - nc));
+        const int64_t z = zeros[c] + zeros[p] + add;
+        const int64_t tot = entries(nc + np, nc + mp);
+        const int64_t w = nc + np;
+        const double frac = w <= 4 ? 0.5 : w <= 16 ? 0.25 : w <= 48 ? 0.1
+                                                               : 0.05;
+        if (w > opt.max_columns || (double)z > frac * (double)tot) break;
+        // merge c into p
+        std::vector<int> merged;
+        merged.reserve(nc + mp);
+        for (int j = first[c]; j < last[c]; j++) merged.push_back(j);
+        merged.insert(merged.end(), rows[p].begin(), rows[p].end());
+        rows[p].swap(merged);
+        rows[c].clear();
+        rows[c].shrink_to_fit();
+        for (int j = first[c]; j < last[c]; j++) sn_of[j] = p;
+        first[p] = first[c];
+        zeros[p] = z;
+        alive[c] = 0;
+        rep[c] = p;  // c's children now hang on p
+      }
+    }
   }
+  // renumber the surviving supernodes in column order
+  std::vector<int> newid(ns, -1);
+  int nsurv = 0;
+  for (int s = 0; s < ns; s++)
+    if (alive[s]) newid[s] = nsurv++;
+  a.sn_col.assign(nsurv + 1, 0);
+  a.sn_rowptr.assign(nsurv + 1, 0);
+  a.sn_parent.assign(nsurv, -1);
+  a.sn_rows.clear();
+  for (int s = 0; s < ns; s++) {
+    if (!alive[s]) continue;
+    const int t = newid[s];
+    a.sn_col[t] = first[s];
+    a.sn_rows.insert(a.sn_rows.end(), rows[s].begin(), rows[s].end());
+    a.sn_rowptr[t + 1] = (int)a.sn_rows.size();
+    a.sn_parent[t] = spar[s] < 0 ? -1 : newid[find(spar[s])];
+    const int64_t m = (int64_t)rows[s].size(), c = last[s] - first[s];
+    a.front_blocks += m * m;
+    a.factor_blocks += c * (c + 1) / 2 + (m - c) * c;
+    a.zero_blocks += zeros[s];
+  }
+  if (nsurv > 0) a.sn_col[nsurv] = n;
+  ns = nsurv;
 
   // levels: leaves 0, a parent one above its highest child
   std::vector<int> lev(ns, 0);
@@ -438,7 +523,97 @@ inline Analysis analyse(const std::vector<int> &rowp,
     }
     a.asm_ptr[s + 1] = (int)a.asm_blk.size();
   }
+  plan_storage(a);
   return a;
+}
+
+// First-fit allocator over [0, top) with coalescing free intervals.
+class PoolPlan {
+ public:
+  int64_t alloc(int64_t size) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= size) {
+        const int64_t off = it->first, rest = it->second - size;
+        free_.erase(it);
+        if (rest > 0) free_[off + size] = rest;
+        return off;
+      }
+    }
+    const int64_t off = top_;
+    top_ += size;
+    peak_ = std::max(peak_, top_);
+    return off;
+  }
+  void release(int64_t off, int64_t size) {
+    if (size <= 0) return;
+    auto it = free_.emplace(off, size).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && off + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+        it = pv;
+      }
+    }
+    if (it->first + it->second == top_) {
+      top_ = it->first;
+      free_.erase(it);
+    }
+  }
+  int64_t peak() const { return peak_; }
+
+ private:
+  std::map<int64_t, int64_t> free_;
+  int64_t top_ = 0, peak_ = 0;
+};
+
+// Factor panels back to back; updates from a pool: the supernodes of a
+// level allocate theirs, and the updates their children handed up are
+// released once the level is done.
+inline void plan_storage(Analysis &a) {
+  const int ns = (int)a.sn_col.size() - 1;
+  a.l_off.assign(ns, 0);
+  a.u_off.assign(ns, -1);
+  int64_t acc = 0;
+  for (int s = 0; s < ns; s++) {
+    const int64_t m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    const int64_t c = a.sn_col[s + 1] - a.sn_col[s];
+    a.l_off[s] = acc;
+    acc += m * c;
+  }
+  a.l_total = acc;
+  std::vector<int> cptr(ns + 1, 0), cl(ns > 0 ? ns : 1);
+  for (int s = 0; s < ns; s++)
+    if (a.sn_parent[s] >= 0) cptr[a.sn_parent[s] + 1]++;
+  for (int s = 0; s < ns; s++) cptr[s + 1] += cptr[s];
+  {
+    std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+    for (int s = 0; s < ns; s++)
+      if (a.sn_parent[s] >= 0) cl[fill[a.sn_parent[s]]++] = s;
+  }
+  auto usize = [&](int s) {
+    const int64_t u = (a.sn_rowptr[s + 1] - a.sn_rowptr[s]) -
+                      (a.sn_col[s + 1] - a.sn_col[s]);
+    return u * u;
+  };
+  PoolPlan pool;
+  for (size_t L = 0; L + 1 < a.level_ptr.size(); L++) {
+    for (int t = a.level_ptr[L]; t < a.level_ptr[L + 1]; t++) {
+      const int s = a.level_sn[t];
+      if (usize(s) > 0 && a.sn_parent[s] >= 0) a.u_off[s] = pool.alloc(usize(s));
+    }
+    for (int t = a.level_ptr[L]; t < a.level_ptr[L + 1]; t++) {
+      const int s = a.level_sn[t];
+      for (int k = cptr[s]; k < cptr[s + 1]; k++)
+        if (a.u_off[cl[k]] >= 0) pool.release(a.u_off[cl[k]], usize(cl[k]));
+    }
+  }
+  a.u_peak = pool.peak();
 }
 
 }  // namespace direct

@@ -3,6 +3,7 @@
 // Cholesky driven by the analysis, and the triangular solves, on the host.
 // Built by tests/test_direct_symbolic.py with g++ and called through
 // ctypes; test infrastructure only.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -64,6 +65,44 @@ int dc_analyse(int n, const int *rowp, const int *cols, const int *perm,
   return 0;
 }
 
+// Storage plan check: out = {factor panel blocks, update pool peak blocks,
+// sum of live update blocks at the busiest level, overlapping live pairs}.
+int dc_plan(int n, const int *rowp, const int *cols, int leaf, double *out) {
+  std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
+  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf);
+  Analysis a = tg::direct::analyse(rp, cs, perm);
+  const int ns = (int)a.sn_col.size() - 1;
+  std::vector<int> lev(ns);
+  for (size_t L = 0; L + 1 < a.level_ptr.size(); L++)
+    for (int t = a.level_ptr[L]; t < a.level_ptr[L + 1]; t++)
+      lev[a.level_sn[t]] = (int)L;
+  int64_t worst = 0, bad = 0;
+  for (size_t L = 0; L + 1 < a.level_ptr.size(); L++) {
+    // live at level L: made at or below L, consumed at or above L
+    std::vector<std::pair<int64_t, int64_t>> iv;
+    int64_t sum = 0;
+    for (int s = 0; s < ns; s++) {
+      if (a.u_off[s] < 0) continue;
+      if (lev[s] > (int)L || lev[a.sn_parent[s]] < (int)L) continue;
+      const int64_t u = (a.sn_rowptr[s + 1] - a.sn_rowptr[s]) -
+                        (a.sn_col[s + 1] - a.sn_col[s]);
+      iv.push_back({a.u_off[s], a.u_off[s] + u * u});
+      sum += u * u;
+    }
+    std::sort(iv.begin(), iv.end());
+    for (size_t k = 1; k < iv.size(); k++)
+      if (iv[k].first < iv[k - 1].second) bad++;
+    for (auto &v : iv)
+      if (v.second > a.u_peak) bad++;
+    worst = std::max(worst, sum);
+  }
+  out[0] = (double)a.l_total;
+  out[1] = (double)a.u_peak;
+  out[2] = (double)worst;
+  out[3] = (double)bad;
+  return 0;
+}
+
 // x = A^-1 b for the symmetric positive definite BCSR matrix (rowp, cols,
 // vals; bs x bs row-major blocks), factored by the multifrontal scheme in
 // nested-dissection order.
@@ -74,7 +113,10 @@ int dc_solve(int n, int bs, const int *rowp, const int *cols,
   Analysis a = tg::direct::analyse(rp, cs, perm);
   const int ns = (int)a.sn_col.size() - 1;
   const size_t b2 = (size_t)bs * bs;
-  std::vector<std::vector<double>> L(ns), U(ns);
+  // factor panels and the update pool laid out by the analysis' plan
+  std::vector<double> Lall((size_t)a.l_total * b2), pool((size_t)a.u_peak * b2);
+  auto Lp = [&](int s) { return &Lall[(size_t)a.l_off[s] * b2]; };
+  auto Up = [&](int s) { return &pool[(size_t)a.u_off[s] * b2]; };
   for (int L0 = 0; L0 + 1 < (int)a.level_ptr.size(); L0++) {
     for (int t = a.level_ptr[L0]; t < a.level_ptr[L0 + 1]; t++) {
       const int s = a.level_sn[t];
@@ -95,7 +137,7 @@ int dc_solve(int n, int bs, const int *rowp, const int *cols,
         const int cm = (a.sn_rowptr[ch + 1] - a.sn_rowptr[ch]) -
                        (a.sn_col[ch + 1] - a.sn_col[ch]);
         const int *rel = &a.ea_rel[a.ea_ptr[ch]];
-        const std::vector<double> &Uc = U[ch];
+        const double *Uc = Up(ch);
         const int um = cm * bs;
         for (int k1 = 0; k1 < cm; k1++)
           for (int k2 = 0; k2 <= k1; k2++)
@@ -106,21 +148,22 @@ int dc_solve(int n, int bs, const int *rowp, const int *cols,
                 F[(size_t)(rel[k1] * bs + r) * m + rel[k2] * bs + q] +=
                     Uc[(size_t)ur * um + uc];
               }
-        U[ch].clear();
-        U[ch].shrink_to_fit();
       }
-      // mirror the diagonal blocks' upper halves are never read
+      // (the upper halves of the diagonal blocks are never read)
       const int rc = front_factor(F.data(), m, c);
       if (rc) return rc;
-      L[s].assign((size_t)m * c, 0.0);
+      double *Ls = Lp(s);
       for (int i = 0; i < m; i++)
-        for (int j = 0; j < c && j <= i; j++)
-          L[s][(size_t)i * c + j] = F[(size_t)i * m + j];
+        for (int j = 0; j < c; j++)
+          Ls[(size_t)i * c + j] = j <= i ? F[(size_t)i * m + j] : 0.0;
       const int um = m - c;
-      U[s].assign((size_t)um * um, 0.0);
-      for (int i = 0; i < um; i++)
-        for (int j = 0; j <= i; j++)
-          U[s][(size_t)i * um + j] = F[(size_t)(c + i) * m + c + j];
+      if (um > 0 && a.sn_parent[s] >= 0) {
+        double *Us = Up(s);
+        for (int i = 0; i < um; i++)
+          for (int j = 0; j < um; j++)
+            Us[(size_t)i * um + j] = j <= i ? F[(size_t)(c + i) * m + c + j]
+                                            : 0.0;
+      }
     }
   }
   // solves in positions
@@ -137,12 +180,12 @@ int dc_solve(int n, int bs, const int *rowp, const int *cols,
       for (int q = 0; q < bs; q++) z[k * bs + q] = y[(size_t)rows[k] * bs + q];
     for (int i = 0; i < c; i++) {
       double v = z[i];
-      for (int j = 0; j < i; j++) v -= L[s][(size_t)i * c + j] * z[j];
-      z[i] = v / L[s][(size_t)i * c + i];
+      for (int j = 0; j < i; j++) v -= Lp(s)[(size_t)i * c + j] * z[j];
+      z[i] = v / Lp(s)[(size_t)i * c + i];
     }
     for (int i = c; i < m; i++) {
       double v = 0.0;
-      for (int j = 0; j < c; j++) v += L[s][(size_t)i * c + j] * z[j];
+      for (int j = 0; j < c; j++) v += Lp(s)[(size_t)i * c + j] * z[j];
       z[i] -= v;
     }
     for (int k = 0; k < mb; k++)
@@ -158,13 +201,13 @@ int dc_solve(int n, int bs, const int *rowp, const int *cols,
       for (int q = 0; q < bs; q++) z[k * bs + q] = y[(size_t)rows[k] * bs + q];
     for (int j = 0; j < c; j++) {
       double v = 0.0;
-      for (int i = c; i < m; i++) v += L[s][(size_t)i * c + j] * z[i];
+      for (int i = c; i < m; i++) v += Lp(s)[(size_t)i * c + j] * z[i];
       z[j] -= v;
     }
     for (int i = c - 1; i >= 0; i--) {
       double v = z[i];
-      for (int j = i + 1; j < c; j++) v -= L[s][(size_t)j * c + i] * z[j];
-      z[i] = v / L[s][(size_t)i * c + i];
+      for (int j = i + 1; j < c; j++) v -= Lp(s)[(size_t)j * c + i] * z[j];
+      z[i] = v / Lp(s)[(size_t)i * c + i];
     }
     for (int k = 0; k < cb; k++)
       for (int q = 0; q < bs; q++) y[(size_t)rows[k] * bs + q] = z[k * bs + q];

@@ -34,6 +34,7 @@ def dc(tmp_path_factory):
     P = C.c_void_p
     lib.dc_analyse.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, P]
     lib.dc_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int]
+    lib.dc_plan.argtypes = [C.c_int, P, P, C.c_int, P]
     return lib
 
 
@@ -121,3 +122,18 @@ def test_nested_dissection_fills_less(dc):
     # the natural order of a plate is one chain: few, wide supernodes but
     # as many tree levels as supernodes; dissection gives a shallow tree
     assert nd[1] < nat[1]
+
+
+@pytest.mark.parametrize("name,prob", list(_problems()),
+                         ids=[p[0] for p in _problems()])
+def test_storage_plan_has_no_overlap(dc, name, prob):
+    """Update matrices live from their supernode's level to their parent's:
+    no two live at the same level may share pool blocks, and the pool is
+    no larger than needed by more than the first-fit slack (2x the busiest
+    level)."""
+    n, bs, rowp, cols, vals = _matrix(prob)
+    out = np.zeros(4)
+    assert dc.dc_plan(n, _ptr(rowp), _ptr(cols), 8, _ptr(out)) == 0
+    l_total, peak, busiest, bad = out
+    assert bad == 0
+    assert busiest <= peak <= 2 * busiest + 1
