@@ -44,9 +44,14 @@ namespace direct {
 // the original row placed at position r.
 class NestedDissection {
  public:
+  // xyz (3 per vertex, may be null): with coordinates a part is bisected
+  // at the median of its widest coordinate instead (recursive coordinate
+  // bisection), the separator being the smaller of the two sides' rows of
+  // vertices that touch the other side -- straight cuts on meshes, where
+  // level sets from a corner are bent
   NestedDissection(const std::vector<int> &rowp, const std::vector<int> &cols,
-                   int leaf)
-      : rowp_(rowp), cols_(cols), leaf_(leaf < 1 ? 1 : leaf) {}
+                   int leaf, const double *xyz = nullptr)
+      : rowp_(rowp), cols_(cols), leaf_(leaf < 1 ? 1 : leaf), xyz_(xyz) {}
 
   std::vector<int> order() {
     const int n = (int)rowp_.size() - 1;
@@ -64,6 +69,7 @@ class NestedDissection {
  private:
   const std::vector<int> &rowp_, &cols_;
   int leaf_;
+  const double *xyz_;
   int next_id_ = 1;
   std::vector<int> part_;  // subgraph id of each unordered vertex, -1 once
                            // ordered or held for a separator
@@ -146,7 +152,63 @@ class NestedDissection {
     for (auto &pc : parts) split_connected(pc.first, pc.second);
   }
 
+  // coordinate bisection of a connected part; false when it cannot cut
+  bool split_coords(const std::vector<int> &verts, int id) {
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) lo[d] = hi[d] = xyz_[3 * (size_t)verts[0] + d];
+    for (int v : verts)
+      for (int d = 0; d < 3; d++) {
+        lo[d] = std::min(lo[d], xyz_[3 * (size_t)v + d]);
+        hi[d] = std::max(hi[d], xyz_[3 * (size_t)v + d]);
+      }
+    int ax = 0;
+    for (int d = 1; d < 3; d++)
+      if (hi[d] - lo[d] > hi[ax] - lo[ax]) ax = d;
+    std::vector<std::pair<double, int>> key(verts.size());
+    for (size_t k = 0; k < verts.size(); k++)
+      key[k] = {xyz_[3 * (size_t)verts[k] + ax], verts[k]};
+    const size_t half = key.size() / 2;
+    std::nth_element(key.begin(), key.begin() + half, key.end());
+    const int ida = next_id_++, idb = next_id_++;
+    for (size_t k = 0; k < key.size(); k++)
+      part_[key[k].second] = k < half ? ida : idb;
+    // rows of each side that touch the other side
+    std::vector<int> sa, sb;
+    for (int v : verts) {
+      const int own = part_[v], other = own == ida ? idb : ida;
+      for (int j = rowp_[v]; j < rowp_[v + 1]; j++)
+        if (part_[cols_[j]] == other) {
+          (own == ida ? sa : sb).push_back(v);
+          break;
+        }
+    }
+    std::vector<int> &sep = sa.size() < sb.size() ? sa : sb;
+    const int sep_id = sa.size() < sb.size() ? ida : idb;
+    std::vector<int> a, b;
+    for (int v : verts) {
+      if (part_[v] == ida) a.push_back(v);
+      else b.push_back(v);
+    }
+    const size_t na = a.size() - (sep_id == ida ? sep.size() : 0);
+    const size_t nb = b.size() - (sep_id == idb ? sep.size() : 0);
+    if (na == 0 || nb == 0) {  // undo: the level-structure split decides
+      for (int v : verts) part_[v] = id;
+      return false;
+    }
+    for (int v : sep) part_[v] = -1;
+    std::vector<int> a2, b2;
+    for (int v : a)
+      if (part_[v] == ida) a2.push_back(v);
+    for (int v : b)
+      if (part_[v] == idb) b2.push_back(v);
+    split(a2, ida);
+    split(b2, idb);
+    for (int v : sep) out_.push_back(v);
+    return true;
+  }
+
   void split_connected(const std::vector<int> &verts, int id) {
+    if (xyz_ && (int)verts.size() > leaf_ && split_coords(verts, id)) return;
     std::vector<int> vis;
     peripheral(id, verts[0], vis);
     const int nlev = dist_[vis.back()] + 1;
@@ -197,8 +259,9 @@ class NestedDissection {
 
 inline std::vector<int> nested_dissection(const std::vector<int> &rowp,
                                           const std::vector<int> &cols,
-                                          int leaf = 64) {
-  NestedDissection nd(rowp, cols, leaf);
+                                          int leaf = 64,
+                                          const double *xyz = nullptr) {
+  NestedDissection nd(rowp, cols, leaf, xyz);
   return nd.order();
 }
 

@@ -44,13 +44,13 @@ int front_factor(double *F, int m, int c) {
 extern "C" {
 
 // Analysis statistics for the node order `perm` (nullptr: nested
-// dissection with `leaf`): out = {supernodes, levels, factor blocks, front
+// dissection with `leaf`, by coordinates when xyz is given): out = {supernodes, levels, factor blocks, front
 // blocks, scalar flops for bs}.
 int dc_analyse(int n, const int *rowp, const int *cols, const int *perm,
-               int leaf, int bs, double *out) {
+               int leaf, int bs, const double *xyz, double *out) {
   std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
   std::vector<int> p = perm ? std::vector<int>(perm, perm + n)
-                            : tg::direct::nested_dissection(rp, cs, leaf);
+                            : tg::direct::nested_dissection(rp, cs, leaf, xyz);
   std::vector<int> seen(n, 0);
   for (int v : p) {
     if (v < 0 || v >= n || seen[v]) return -1;
@@ -67,9 +67,10 @@ int dc_analyse(int n, const int *rowp, const int *cols, const int *perm,
 
 // Storage plan check: out = {factor panel blocks, update pool peak blocks,
 // sum of live update blocks at the busiest level, overlapping live pairs}.
-int dc_plan(int n, const int *rowp, const int *cols, int leaf, double *out) {
+int dc_plan(int n, const int *rowp, const int *cols, int leaf,
+            const double *xyz, double *out) {
   std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
-  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf);
+  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf, xyz);
   Analysis a = tg::direct::analyse(rp, cs, perm);
   const int ns = (int)a.sn_col.size() - 1;
   std::vector<int> lev(ns);
@@ -107,9 +108,10 @@ int dc_plan(int n, const int *rowp, const int *cols, int leaf, double *out) {
 // vals; bs x bs row-major blocks), factored by the multifrontal scheme in
 // nested-dissection order.
 int dc_solve(int n, int bs, const int *rowp, const int *cols,
-             const double *vals, const double *b, double *x, int leaf) {
+             const double *vals, const double *b, double *x, int leaf,
+             const double *xyz) {
   std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
-  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf);
+  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, leaf, xyz);
   Analysis a = tg::direct::analyse(rp, cs, perm);
   const int ns = (int)a.sn_col.size() - 1;
   const size_t b2 = (size_t)bs * bs;

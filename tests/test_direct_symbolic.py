@@ -32,9 +32,9 @@ def dc(tmp_path_factory):
                     SRC, "-o", out], check=True)
     lib = C.CDLL(out)
     P = C.c_void_p
-    lib.dc_analyse.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, P]
-    lib.dc_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int]
-    lib.dc_plan.argtypes = [C.c_int, P, P, C.c_int, P]
+    lib.dc_analyse.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, P, P]
+    lib.dc_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int, P]
+    lib.dc_plan.argtypes = [C.c_int, P, P, C.c_int, P, P]
     return lib
 
 
@@ -68,8 +68,9 @@ def _problems():
 
 @pytest.mark.parametrize("name,prob", list(_problems()),
                          ids=[p[0] for p in _problems()])
-@pytest.mark.parametrize("leaf", [1, 8, 64])
-def test_multifrontal_solve_is_exact(dc, name, prob, leaf):
+@pytest.mark.parametrize("leaf,coords", [(1, False), (8, False),
+                                         (64, False), (8, True)])
+def test_multifrontal_solve_is_exact(dc, name, prob, leaf, coords):
     """The assembled K carries the reference's row boundary conditions
     (identity rows, columns kept): K = [[K_ff, K_fb], [0, I]].  Its
     symmetric part Kt = K_ff + I (boundary columns zeroed too) is what the
@@ -97,8 +98,9 @@ def test_multifrontal_solve_is_exact(dc, name, prob, leaf):
     b = np.random.default_rng(1).standard_normal(n * bs)
     x = np.zeros_like(b)
     bb = b - E @ b
+    xyz = np.ascontiguousarray(prob["xpts"], np.float64) if coords else None
     rc = dc.dc_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals_t.ravel()),
-                     _ptr(bb), _ptr(x), leaf)
+                     _ptr(bb), _ptr(x), leaf, _ptr(xyz))
     assert rc == 0
     # backward error at rounding level; forward error within cond(K) x eps
     # of the sparse LU's
@@ -111,11 +113,11 @@ def test_nested_dissection_fills_less(dc):
     from tacs_gb300 import meshes
     n, bs, rowp, cols, vals = _matrix(meshes.clamped_plate(96))
     nd, nat = np.zeros(5), np.zeros(5)
-    assert dc.dc_analyse(n, _ptr(rowp), _ptr(cols), None, 64, bs,
+    assert dc.dc_analyse(n, _ptr(rowp), _ptr(cols), None, 64, bs, None,
                          _ptr(nd)) == 0
     ident = np.arange(n, dtype=np.int32)
     assert dc.dc_analyse(n, _ptr(rowp), _ptr(cols), _ptr(ident), 64, bs,
-                         _ptr(nat)) == 0
+                         None, _ptr(nat)) == 0
     # factor blocks and flops
     assert nd[2] < 0.5 * nat[2]
     assert nd[4] < 0.3 * nat[4]
@@ -133,7 +135,7 @@ def test_storage_plan_has_no_overlap(dc, name, prob):
     level)."""
     n, bs, rowp, cols, vals = _matrix(prob)
     out = np.zeros(4)
-    assert dc.dc_plan(n, _ptr(rowp), _ptr(cols), 8, _ptr(out)) == 0
+    assert dc.dc_plan(n, _ptr(rowp), _ptr(cols), 8, None, _ptr(out)) == 0
     l_total, peak, busiest, bad = out
     assert bad == 0
     assert busiest <= peak <= 2 * busiest + 1
