@@ -60,6 +60,7 @@ typedef struct tg_assembler tg_assembler;
 typedef struct tg_mat tg_mat;
 typedef struct tg_pc tg_pc;
 typedef struct tg_ksm tg_ksm;
+typedef struct tg_direct tg_direct;
 
 /* ---------------------------------------------------------------- errors */
 const char *tg_last_error(void);
@@ -167,6 +168,23 @@ int tg_add_adjoint_res_products(tg_assembler *a, const double *vars,
 int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
                             double coef, const double *psi, double scale,
                             double *dfdx, void *stream);
+
+/* ------------------------------------------- direct factorisation */
+/* Complete factorisation of an assembled matrix (the reference's direct
+   solve: TACSSchurPc with a large levFill, src/bpmat/TACSSchurMat.cpp:
+   1510-1600, same solution): nested dissection (by the node coordinates
+   when use_coords), supernodes and fronts analysed once on the host, then
+   a level-by-level multifrontal block Cholesky of K with its boundary
+   columns zeroed as well, so that x = A^-1 b for the assembled A with its
+   row boundary conditions.  FP64.  tg_direct_factor synchronises and
+   returns TG_ERR_PIVOT on a non-positive pivot.
+   stats: supernodes, tree levels, factor bytes, update-pool bytes, dense
+   flops, largest front (scalar rows). */
+int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out);
+int tg_direct_factor(tg_direct *d, void *stream);
+int tg_direct_solve(tg_direct *d, const double *b, double *x, void *stream);
+int tg_direct_get_stats(tg_direct *d, double *stats);
+int tg_direct_decref(tg_direct *d);
 
 /* ------------------------------------- node-coordinate sensitivities */
 /* The node vectors dfdX hold 3 doubles per node (TACSAssembler::

@@ -1,0 +1,343 @@
+// Kernels of the multifrontal block Cholesky (the numeric phase of the
+// direct factorisation; host analysis in direct_symbolic.h, launches in
+// direct_kernels.cu).  Included by direct_kernels.cu and, with
+// DK_EMULATE defined, by a CPU test harness that runs every CTA as one
+// thread in sequence: each kernel is written as phases separated by
+// __syncthreads() in which every thread strides over independent entries,
+// so one thread executing the phases in order computes the same result.
+//
+// Storage (one per factorisation): the front of supernode s (M x M
+// scalars, M = front rows x bs, lower triangle used) is split between its
+// factor panel -- the first C = own columns x bs columns of every front
+// row, row-major M x C at lstore + l_off[s] -- and its update matrix --
+// the trailing (M - C) x (M - C) part, row-major at pool + u_off[s], in a
+// pool shared across tree levels.  A level of the tree is processed as:
+// zero the fronts, scatter the matrix's lower blocks (boundary columns
+// zeroed so that the factored matrix is the symmetric Kt), add the
+// children's update matrices (one CTA per parent, children in a fixed
+// order: deterministic), then the partial Cholesky: small fronts one CTA
+// each, large fronts by 32-column panels (one CTA factors the panel, a
+// grid of 32 x 32 tiles updates the trailing front).  The solves pass
+// contribution vectors from children to parents the same way, so no two
+// CTAs write one entry.
+#pragma once
+
+#include "direct_view.h"
+
+#ifdef DK_EMULATE
+#define DK_DYN_SMEM(T, name) T *name = reinterpret_cast<T *>(dk_dyn_smem())
+#else
+#define DK_DYN_SMEM(T, name) extern __shared__ T name[]
+#endif
+
+namespace tg {
+namespace dk {
+namespace {
+
+#ifndef DK_EMULATE
+__device__ __forceinline__ bool dk_isfinite(double x) { return isfinite(x); }
+__device__ __forceinline__ double dk_sqrt(double x) { return sqrt(x); }
+#endif
+
+
+struct Front {
+  double *lp;  // M x C row-major panel
+  double *up;  // (M - C) x (M - C) row-major update, or nullptr
+  int M, C;
+  __device__ __forceinline__ double &at(int i, int j) const {  // i >= j
+    return j < C ? lp[(size_t)i * C + j]
+                 : up[(size_t)(i - C) * (M - C) + (j - C)];
+  }
+};
+
+__device__ __forceinline__ Front front_of(const DirectView &v, int s) {
+  Front f;
+  const int bs = v.bs;
+  f.M = (v.sn_rowptr[s + 1] - v.sn_rowptr[s]) * bs;
+  f.C = (v.sn_col[s + 1] - v.sn_col[s]) * bs;
+  f.lp = v.lstore + (size_t)v.l_off[s] * bs * bs;
+  f.up = v.u_off[s] >= 0 ? v.pool + (size_t)v.u_off[s] * bs * bs : nullptr;
+  return f;
+}
+
+// zero the fronts of the level's supernodes (one CTA each)
+__global__ void __launch_bounds__(256)
+    direct_zero_kernel(DirectView v, const int *__restrict__ sn, int count) {
+  if ((int)blockIdx.x >= count) return;
+  const Front f = front_of(v, sn[blockIdx.x]);
+  const size_t npan = (size_t)f.M * f.C;
+  for (size_t k = threadIdx.x; k < npan; k += blockDim.x) f.lp[k] = 0.0;
+  if (f.up) {
+    const size_t nu = (size_t)(f.M - f.C) * (f.M - f.C);
+    for (size_t k = threadIdx.x; k < nu; k += blockDim.x) f.up[k] = 0.0;
+  }
+}
+
+// the matrix's lower blocks into the fronts; entries in a boundary row or
+// column are 0 except the boundary dof's own diagonal (1)
+__global__ void __launch_bounds__(256)
+    direct_assemble_kernel(DirectView v, const int *__restrict__ sn,
+                           int count, const double *__restrict__ A) {
+  if ((int)blockIdx.x >= count) return;
+  const int s = sn[blockIdx.x];
+  const Front f = front_of(v, s);
+  const int bs = v.bs, b2 = bs * bs;
+  const int k0 = v.asm_ptr[s], k1 = v.asm_ptr[s + 1];
+  const size_t total = (size_t)(k1 - k0) * b2;
+  for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const int k = k0 + (int)(t / b2), e = (int)(t % b2);
+    const int r = e / bs, q = e - bs * (e / bs);
+    const int ir = v.asm_row[k] * bs + r, jc = v.asm_col[k] * bs + q;
+    if (jc > ir) continue;  // upper half of a diagonal block
+    const int rnode = v.perm[v.sn_rows[v.sn_rowptr[s] + v.asm_row[k]]];
+    const int cnode = v.perm[v.sn_col[s] + v.asm_col[k]];
+    const bool bc = ((v.bcmask[rnode] >> r) & 1) || ((v.bcmask[cnode] >> q) & 1);
+    double val = A[(size_t)v.asm_blk[k] * b2 + e];
+    if (bc) val = (rnode == cnode && r == q) ? 1.0 : 0.0;
+    f.at(ir, jc) = val;
+  }
+}
+
+// the children's update matrices into each parent front (one CTA per
+// parent, children one after another)
+__global__ void __launch_bounds__(256)
+    direct_extend_add_kernel(DirectView v, const int *__restrict__ sn,
+                             int count) {
+  if ((int)blockIdx.x >= count) return;
+  const int s = sn[blockIdx.x];
+  const Front f = front_of(v, s);
+  const int bs = v.bs;
+  for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
+    const int c = v.ch_list[k];
+    const Front fc = front_of(v, c);
+    const int um = fc.M - fc.C;
+    const int *rel = v.ea_rel + v.ea_ptr[c];
+    const size_t total = (size_t)um * um;
+    for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const int ur = (int)(t / um), uc = (int)(t % um);
+      if (uc > ur) continue;
+      const int i = rel[ur / bs] * bs + ur % bs;
+      const int j = rel[uc / bs] * bs + uc % bs;
+      f.at(i, j) += fc.up[t];
+    }
+    __syncthreads();
+  }
+}
+
+// partial Cholesky of whole small fronts, one CTA each (right-looking in
+// place); fail = first failing supernode + 1
+__global__ void __launch_bounds__(256)
+    direct_factor_small_kernel(DirectView v, const int *__restrict__ sn,
+                               int count, int *fail) {
+  if ((int)blockIdx.x >= count) return;
+  const int s = sn[blockIdx.x];
+  const Front f = front_of(v, s);
+  __shared__ double piv;
+  for (int k = 0; k < f.C; k++) {
+    if (threadIdx.x == 0) {
+      const double d = f.at(k, k);
+      if (!(d > 0.0) || !dk_isfinite(d)) {
+        atomicCAS(fail, 0, s + 1);
+        piv = 1.0;
+      } else {
+        piv = dk_sqrt(d);
+      }
+      f.at(k, k) = piv;
+    }
+    __syncthreads();
+    const double inv = 1.0 / piv;
+    for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
+      f.at(i, k) *= inv;
+    __syncthreads();
+    // trailing update of rows and columns > k
+    const int w = f.M - k - 1;
+    const size_t total = (size_t)w * w;
+    for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const int i = k + 1 + (int)(t / w), j = k + 1 + (int)(t % w);
+      if (j > i) continue;
+      f.at(i, j) -= f.at(i, k) * f.at(j, k);
+    }
+    __syncthreads();
+  }
+}
+
+// Large fronts.  Panel step: columns [k0, k0 + nb) of one front, all rows
+// from k0, factored by one CTA with the panel's own columns updated
+// left-looking inside the panel.
+__global__ void __launch_bounds__(256)
+    direct_panel_kernel(DirectView v, int s, int k0, int nb, int *fail) {
+  const Front f = front_of(v, s);
+  __shared__ double piv;
+  for (int k = k0; k < k0 + nb; k++) {
+    if (threadIdx.x == 0) {
+      const double d = f.at(k, k);
+      if (!(d > 0.0) || !dk_isfinite(d)) {
+        atomicCAS(fail, 0, s + 1);
+        piv = 1.0;
+      } else {
+        piv = dk_sqrt(d);
+      }
+      f.at(k, k) = piv;
+    }
+    __syncthreads();
+    const double inv = 1.0 / piv;
+    for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
+      f.at(i, k) *= inv;
+    __syncthreads();
+    // update the rest of the panel's columns (k, k0 + nb)
+    const int w = k0 + nb - k - 1;
+    if (w > 0) {
+      const int rows = f.M - k - 1;
+      const size_t total = (size_t)rows * w;
+      for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
+        const int i = k + 1 + (int)(t / w), j = k + 1 + (int)(t % w);
+        if (j > i) continue;
+        f.at(i, j) -= f.at(i, k) * f.at(j, k);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Trailing update after a panel: F(i, j) -= sum_q F(i, q) F(j, q) over the
+// panel's columns q, for k1 <= j <= i < M, in 32 x 32 tiles (blockIdx.x =
+// tile column, blockIdx.y = tile row; tiles above the diagonal exit).
+constexpr int kTile = 32, kPanel = 32;
+__global__ void __launch_bounds__(256)
+    direct_trailing_kernel(DirectView v, int s, int k0, int nb) {
+  const Front f = front_of(v, s);
+  const int k1 = k0 + nb;
+  const int tj = blockIdx.x, ti = blockIdx.y;
+  if (tj > ti) return;
+  const int i0 = k1 + ti * kTile, j0 = k1 + tj * kTile;
+  if (i0 >= f.M || j0 >= f.M) return;
+  __shared__ double Ai[kTile][kPanel + 1], Aj[kTile][kPanel + 1];
+  for (int t = threadIdx.x; t < kTile * nb; t += blockDim.x) {
+    const int r = t / nb, q = t % nb;
+    Ai[r][q] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : 0.0;
+    Aj[r][q] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kTile * kTile; t += blockDim.x) {
+    const int r = t / kTile, c = t % kTile;
+    const int i = i0 + r, j = j0 + c;
+    if (i >= f.M || j >= f.M || j > i) continue;
+    double acc = 0.0;
+    for (int q = 0; q < nb; q++) acc += Ai[r][q] * Aj[c][q];
+    f.at(i, j) -= acc;
+  }
+}
+
+// ----------------------------------------------------------------- solves
+// Forward: z = front rows of the supernode (own rows from y, the rows
+// below zero), plus the children's contribution vectors; L11 z1 = z1 and
+// z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
+__global__ void __launch_bounds__(256)
+    direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
+                          double *y, double *contrib) {
+  if ((int)blockIdx.x >= count) return;
+  DK_DYN_SMEM(double, z);
+  const int s = sn[blockIdx.x];
+  const Front f = front_of(v, s);
+  const int bs = v.bs;
+  const int *rows = v.sn_rows + v.sn_rowptr[s];
+  for (int t = threadIdx.x; t < f.M; t += blockDim.x)
+    z[t] = t < f.C ? y[(size_t)rows[t / bs] * bs + t % bs] : 0.0;
+  __syncthreads();
+  for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
+    const int c = v.ch_list[k];
+    const Front fc = front_of(v, c);
+    const int um = fc.M - fc.C;
+    const int *rel = v.ea_rel + v.ea_ptr[c];
+    const double *w = contrib + v.v_off[c];
+    for (int t = threadIdx.x; t < um; t += blockDim.x)
+      z[rel[t / bs] * bs + t % bs] += w[t];
+    __syncthreads();
+  }
+  for (int k = 0; k < f.C; k++) {
+    if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
+    __syncthreads();
+    const double zk = z[k];
+    for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
+      z[i] -= f.lp[(size_t)i * f.C + k] * zk;
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < f.C; t += blockDim.x)
+    y[(size_t)rows[t / bs] * bs + t % bs] = z[t];
+  if (v.sn_parent[s] >= 0) {
+    double *w = contrib + v.v_off[s];
+    for (int t = f.C + threadIdx.x; t < f.M; t += blockDim.x) w[t - f.C] = z[t];
+  }
+}
+
+// Backward: z1 = y1 - L21^T x2 (x2 from the ancestors, already final),
+// then L11^T z1 = z1; own rows to x.
+__global__ void __launch_bounds__(256)
+    direct_backward_kernel(DirectView v, const int *__restrict__ sn,
+                           int count, const double *y, double *x) {
+  if ((int)blockIdx.x >= count) return;
+  DK_DYN_SMEM(double, z);
+  const int s = sn[blockIdx.x];
+  const Front f = front_of(v, s);
+  const int bs = v.bs;
+  const int *rows = v.sn_rows + v.sn_rowptr[s];
+  for (int t = threadIdx.x; t < f.M; t += blockDim.x) {
+    const size_t g = (size_t)rows[t / bs] * bs + t % bs;
+    z[t] = t < f.C ? y[g] : x[g];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < f.C; j += blockDim.x) {
+    double acc = 0.0;
+    for (int i = f.C; i < f.M; i++) acc += f.lp[(size_t)i * f.C + j] * z[i];
+    z[j] -= acc;
+  }
+  __syncthreads();
+  for (int k = f.C - 1; k >= 0; k--) {
+    if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
+    __syncthreads();
+    const double zk = z[k];
+    for (int j = threadIdx.x; j < k; j += blockDim.x)
+      z[j] -= f.lp[(size_t)k * f.C + j] * zk;
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < f.C; t += blockDim.x)
+    x[(size_t)rows[t / bs] * bs + t % bs] = z[t];
+}
+
+// b' = b - K P b + P b (P keeps the boundary dofs) is formed as
+// tmp = P b, then K tmp by the mat-vec, then this kernel; and the
+// permutations into and out of the factor's order
+__global__ void direct_bc_mask_kernel(int n, int bs, const int *bcmask,
+                                      const double *b, double *out) {
+  const size_t N = (size_t)n * bs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int node = (int)(t / bs), r = (int)(t % bs);
+    out[t] = ((bcmask[node] >> r) & 1) ? b[t] : 0.0;
+  }
+}
+__global__ void direct_rhs_kernel(int n, int bs, const int *perm,
+                                  const double *b, const double *Kpb,
+                                  const double *pb, double *ypos) {
+  const size_t N = (size_t)n * bs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int pos = (int)(t / bs), r = (int)(t % bs);
+    const size_t g = (size_t)perm[pos] * bs + r;
+    ypos[t] = b[g] - Kpb[g] + pb[g];
+  }
+}
+__global__ void direct_unpermute_kernel(int n, int bs, const int *perm,
+                                        const double *xpos, double *x) {
+  const size_t N = (size_t)n * bs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int pos = (int)(t / bs), r = (int)(t % bs);
+    x[(size_t)perm[pos] * bs + r] = xpos[t];
+  }
+}
+
+
+}  // namespace
+}  // namespace dk
+}  // namespace tg

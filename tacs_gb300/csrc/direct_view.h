@@ -1,0 +1,20 @@
+// Device view of a multifrontal factorisation (direct_kernels.cuh): the
+// host analysis of direct_symbolic.h uploaded as it is, and the storage.
+// Plain C++ so that the kernels also compile for the CPU check.
+#pragma once
+
+#include <cstdint>
+
+namespace tg {
+
+struct DirectView {
+  int bs;
+  const int *perm, *bcmask;  // position -> node; boundary dof mask per node
+  const int *sn_col, *sn_rowptr, *sn_rows, *sn_parent;
+  const int *ea_ptr, *ea_rel, *asm_ptr, *asm_blk, *asm_row, *asm_col;
+  const int *ch_ptr, *ch_list;
+  const int64_t *l_off, *u_off, *v_off;
+  double *lstore, *pool;
+};
+
+}  // namespace tg

@@ -1,0 +1,264 @@
+// Direct (complete) factorisation of an assembled matrix: the host analysis
+// of direct_symbolic.h (nested dissection by the node coordinates,
+// supernodes, fronts, storage plan) and the level-by-level multifrontal
+// block Cholesky of direct_kernels.cu, behind the C ABI tg_direct_*.
+// Replaces the reference's complete factorisation (TACSSchurPc with a
+// large levFill, src/bpmat/TACSSchurMat.cpp:1510-1600) with the same
+// solution; the matrix's row boundary conditions are handled as
+// x = Kt^-1 (b - K P b + P b), Kt being K with the boundary columns zeroed
+// too (symmetric positive definite) and P keeping the boundary dofs.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "direct_symbolic.h"
+#include "tg_objects.h"
+
+// fronts of at most this many scalar rows are factored by one CTA each
+static constexpr int kSmallFront = 256;
+
+struct tg_direct {
+  int refcount = 1;
+  tg_mat *A = nullptr;
+  int n = 0, bs = 0, ns = 0, max_front = 0;
+  tg::direct::Analysis an;
+  std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
+  // per level: its small fronts (one launch, d_small) and its large ones
+  std::vector<int> small_ptr_h, large_ptr_h, large_h;
+  int *d_small = nullptr;
+  // device copies of the analysis
+  int *d_perm = nullptr, *d_bcmask = nullptr, *d_sn_col = nullptr,
+      *d_sn_rowptr = nullptr, *d_sn_rows = nullptr, *d_sn_parent = nullptr,
+      *d_ea_ptr = nullptr, *d_ea_rel = nullptr, *d_asm_ptr = nullptr,
+      *d_asm_blk = nullptr, *d_asm_row = nullptr, *d_asm_col = nullptr,
+      *d_ch_ptr = nullptr, *d_ch_list = nullptr, *d_level_sn = nullptr;
+  int64_t *d_l_off = nullptr, *d_u_off = nullptr, *d_v_off = nullptr;
+  double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
+  double *d_ypos = nullptr, *d_xpos = nullptr, *d_pb = nullptr,
+         *d_kpb = nullptr;
+  int *d_fail = nullptr;
+  bool factored = false;
+  tg::DirectView view() const {
+    tg::DirectView v;
+    v.bs = bs;
+    v.perm = d_perm;
+    v.bcmask = d_bcmask;
+    v.sn_col = d_sn_col;
+    v.sn_rowptr = d_sn_rowptr;
+    v.sn_rows = d_sn_rows;
+    v.sn_parent = d_sn_parent;
+    v.ea_ptr = d_ea_ptr;
+    v.ea_rel = d_ea_rel;
+    v.asm_ptr = d_asm_ptr;
+    v.asm_blk = d_asm_blk;
+    v.asm_row = d_asm_row;
+    v.asm_col = d_asm_col;
+    v.ch_ptr = d_ch_ptr;
+    v.ch_list = d_ch_list;
+    v.l_off = d_l_off;
+    v.u_off = d_u_off;
+    v.v_off = d_v_off;
+    v.lstore = d_lstore;
+    v.pool = d_pool;
+    return v;
+  }
+  ~tg_direct() {
+    using tg::dfree;
+    dfree(d_perm); dfree(d_bcmask); dfree(d_sn_col); dfree(d_sn_rowptr);
+    dfree(d_sn_rows); dfree(d_sn_parent); dfree(d_ea_ptr); dfree(d_ea_rel);
+    dfree(d_asm_ptr); dfree(d_asm_blk); dfree(d_asm_row); dfree(d_asm_col);
+    dfree(d_ch_ptr); dfree(d_ch_list); dfree(d_level_sn); dfree(d_l_off);
+    dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
+    dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
+    dfree(d_kpb); dfree(d_fail); dfree(d_small);
+  }
+};
+
+extern "C" {
+
+int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out) {
+  if (!A || !out) return fail(TG_ERR_ARG, "tg_direct_create: NULL argument");
+  *out = nullptr;
+  tg_assembler *a = A->a;
+  if (!a || !a->initialized)
+    return fail(TG_ERR_STATE, "tg_direct_create: assembler not initialised");
+  tg_direct *d = new tg_direct();
+  d->A = A;
+  A->refcount++;
+  d->n = A->nrows;
+  d->bs = A->bsize;
+  std::vector<double> xyz;
+  if (use_coords) {
+    xyz.resize((size_t)3 * a->nnodes);
+    cudaError_t e = cudaMemcpy(xyz.data(), a->d_xpts,
+                               xyz.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      tg_direct_decref(d);
+      return cuda_check(e, "tg_direct_create: node coordinates");
+    }
+  }
+  std::vector<int> perm = tg::direct::nested_dissection(
+      a->rowp_h, a->cols_h, 64, use_coords ? xyz.data() : nullptr);
+  d->an = tg::direct::analyse(a->rowp_h, a->cols_h, perm);
+  const tg::direct::Analysis &an = d->an;
+  d->ns = (int)an.sn_col.size() - 1;
+  d->level_ptr_h = an.level_ptr;
+  d->level_sn_h = an.level_sn;
+  d->front_m_h.resize(d->ns);
+  d->front_c_h.resize(d->ns);
+  std::vector<int> ch_ptr(d->ns + 1, 0), ch_list(d->ns > 0 ? d->ns : 1);
+  std::vector<int64_t> v_off(d->ns, 0);
+  int64_t vacc = 0;
+  for (int s = 0; s < d->ns; s++) {
+    d->front_m_h[s] = (an.sn_rowptr[s + 1] - an.sn_rowptr[s]) * d->bs;
+    d->front_c_h[s] = (an.sn_col[s + 1] - an.sn_col[s]) * d->bs;
+    d->max_front = std::max(d->max_front, d->front_m_h[s]);
+    v_off[s] = vacc;
+    vacc += d->front_m_h[s] - d->front_c_h[s];
+    if (an.sn_parent[s] >= 0) ch_ptr[an.sn_parent[s] + 1]++;
+  }
+  for (int s = 0; s < d->ns; s++) ch_ptr[s + 1] += ch_ptr[s];
+  {
+    std::vector<int> fill(ch_ptr.begin(), ch_ptr.end() - 1);
+    for (int s = 0; s < d->ns; s++)  // children in increasing order
+      if (an.sn_parent[s] >= 0) ch_list[fill[an.sn_parent[s]]++] = s;
+  }
+  std::vector<int> small_h;
+  d->small_ptr_h.assign(1, 0);
+  d->large_ptr_h.assign(1, 0);
+  for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+    for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+      const int sn = an.level_sn[t];
+      if (d->front_m_h[sn] > kSmallFront) d->large_h.push_back(sn);
+      else small_h.push_back(sn);
+    }
+    d->small_ptr_h.push_back((int)small_h.size());
+    d->large_ptr_h.push_back((int)d->large_h.size());
+  }
+  std::vector<int> bcmask(d->n, 0);
+  for (size_t k = 0; k < a->bc_nodes_h.size(); k++)
+    bcmask[a->bc_nodes_h[k]] |= a->bc_masks_h[k];
+  const size_t b2 = (size_t)d->bs * d->bs;
+  const size_t N = (size_t)d->n * d->bs;
+  int rc = 0;
+  if (!rc) rc = upload(&d->d_perm, an.perm);
+  if (!rc) rc = upload(&d->d_bcmask, bcmask);
+  if (!rc) rc = upload(&d->d_sn_col, an.sn_col);
+  if (!rc) rc = upload(&d->d_sn_rowptr, an.sn_rowptr);
+  if (!rc) rc = upload(&d->d_sn_rows, an.sn_rows);
+  if (!rc) rc = upload(&d->d_sn_parent, an.sn_parent);
+  if (!rc) rc = upload(&d->d_ea_ptr, an.ea_ptr);
+  if (!rc) rc = upload(&d->d_ea_rel, an.ea_rel);
+  if (!rc) rc = upload(&d->d_asm_ptr, an.asm_ptr);
+  if (!rc) rc = upload(&d->d_asm_blk, an.asm_blk);
+  if (!rc) rc = upload(&d->d_asm_row, an.asm_row);
+  if (!rc) rc = upload(&d->d_asm_col, an.asm_col);
+  if (!rc) rc = upload(&d->d_ch_ptr, ch_ptr);
+  if (!rc) rc = upload(&d->d_ch_list, ch_list);
+  if (!rc) rc = upload(&d->d_level_sn, an.level_sn);
+  if (!rc) rc = upload(&d->d_small, small_h);
+  if (!rc) rc = upload(&d->d_l_off, an.l_off);
+  if (!rc) rc = upload(&d->d_u_off, an.u_off);
+  if (!rc) rc = upload(&d->d_v_off, v_off);
+  if (!rc) rc = dalloc(&d->d_lstore, (size_t)an.l_total * b2);
+  if (!rc) rc = dalloc(&d->d_pool, (size_t)an.u_peak * b2);
+  if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc);
+  if (!rc) rc = dalloc(&d->d_ypos, N);
+  if (!rc) rc = dalloc(&d->d_xpos, N);
+  if (!rc) rc = dalloc(&d->d_pb, N);
+  if (!rc) rc = dalloc(&d->d_kpb, N);
+  if (!rc) rc = dalloc(&d->d_fail, 1);
+  if (!rc && (size_t)d->max_front * sizeof(double) > 227 * 1024)
+    rc = fail(TG_ERR_ARG, "tg_direct_create: front too large for a CTA's "
+                          "solve workspace");
+  if (rc) {
+    tg_direct_decref(d);
+    return rc;
+  }
+  tg::direct_set_smem(d->max_front);
+  *out = d;
+  return 0;
+}
+
+int tg_direct_decref(tg_direct *d) {
+  if (!d) return 0;
+  if (--d->refcount == 0) {
+    tg_mat_decref(d->A);
+    delete d;
+  }
+  return 0;
+}
+
+int tg_direct_factor(tg_direct *d, void *s) {
+  if (!d) return fail(TG_ERR_ARG, "tg_direct_factor: NULL");
+  const tg::DirectView v = d->view();
+  TG_CUDA(cudaMemsetAsync(d->d_fail, 0, sizeof(int), S(s)));
+  for (size_t L = 0; L + 1 < d->level_ptr_h.size(); L++) {
+    const int b = d->level_ptr_h[L], e = d->level_ptr_h[L + 1];
+    tg::launch_direct_level_assemble(v, d->d_level_sn + b, e - b,
+                                     d->A->d_vals, S(s));
+    // the level's small fronts in one launch, its large ones by panels
+    const int sb = d->small_ptr_h[L], se = d->small_ptr_h[L + 1];
+    tg::launch_direct_factor_small(v, d->d_small + sb, se - sb, d->d_fail,
+                                   S(s));
+    for (int t = d->large_ptr_h[L]; t < d->large_ptr_h[L + 1]; t++) {
+      const int sn = d->large_h[t];
+      tg::launch_direct_factor_large(v, sn, d->front_m_h[sn],
+                                     d->front_c_h[sn], d->d_fail, S(s));
+    }
+  }
+  int hfail = 0;
+  TG_CUDA(cudaMemcpyAsync(&hfail, d->d_fail, sizeof(int),
+                          cudaMemcpyDeviceToHost, S(s)));
+  TG_CUDA(cudaStreamSynchronize(S(s)));
+  TG_CUDA(cudaGetLastError());
+  if (hfail) {
+    char buf[128];
+    snprintf(buf, sizeof(buf),
+             "tg_direct_factor: non-positive pivot in supernode %d", hfail - 1);
+    return fail(TG_ERR_PIVOT, buf);
+  }
+  d->factored = true;
+  return 0;
+}
+
+int tg_direct_solve(tg_direct *d, const double *b, double *x, void *s) {
+  if (!d || !b || !x) return fail(TG_ERR_ARG, "tg_direct_solve: NULL");
+  if (!d->factored) return fail(TG_ERR_STATE, "tg_direct_solve: not factored");
+  const tg::DirectView v = d->view();
+  tg_mat *A = d->A;
+  tg::launch_direct_bc_mask(d->n, d->bs, d->d_bcmask, b, d->d_pb, S(s));
+  tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                       A->d_vals, d->d_pb, d->d_kpb, S(s));
+  tg::launch_direct_rhs(d->n, d->bs, d->d_perm, b, d->d_kpb, d->d_pb,
+                        d->d_ypos, S(s));
+  const int nl = (int)d->level_ptr_h.size() - 1;
+  for (int L = 0; L < nl; L++) {
+    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
+    tg::launch_direct_forward(v, d->d_level_sn + lb, le - lb, d->max_front,
+                              d->d_ypos, d->d_contrib, S(s));
+  }
+  for (int L = nl - 1; L >= 0; L--) {
+    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
+    tg::launch_direct_backward(v, d->d_level_sn + lb, le - lb, d->max_front,
+                               d->d_ypos, d->d_xpos, S(s));
+  }
+  tg::launch_direct_unpermute(d->n, d->bs, d->d_perm, d->d_xpos, x, S(s));
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_direct_get_stats(tg_direct *d, double *stats) {
+  if (!d || !stats) return fail(TG_ERR_ARG, "tg_direct_get_stats: NULL");
+  const size_t b2 = (size_t)d->bs * d->bs;
+  stats[0] = d->ns;
+  stats[1] = (double)d->level_ptr_h.size() - 1;
+  stats[2] = (double)d->an.l_total * b2 * sizeof(double);
+  stats[3] = (double)d->an.u_peak * b2 * sizeof(double);
+  stats[4] = (double)d->an.flops_scalar(d->bs);
+  stats[5] = d->max_front;
+  return 0;
+}
+
+}  // extern "C"

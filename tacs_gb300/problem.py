@@ -122,6 +122,42 @@ class Pc:
             pass
 
 
+class Direct:
+    """tg_direct: complete multifrontal factorisation of an assembled
+    matrix (the reference's direct solve), nested dissection by the node
+    coordinates; solve(b) returns A^-1 b for the assembled A with its row
+    boundary conditions."""
+
+    def __init__(self, mat, use_coords=True):
+        h = C.c_void_p()
+        check(_lib.lib().tg_direct_create(mat.handle, int(use_coords),
+                                          C.byref(h)), "tg_direct_create")
+        self.handle, self.mat = h, mat
+
+    def factor(self):
+        check(_lib.lib().tg_direct_factor(self.handle, _stream()),
+              "tg_direct_factor")
+
+    def solve(self, b, x=None):
+        x = torch.empty_like(b) if x is None else x
+        check(_lib.lib().tg_direct_solve(self.handle, _p(b), _p(x),
+                                         _stream()), "tg_direct_solve")
+        return x
+
+    def stats(self):
+        st = np.zeros(8)
+        check(_lib.lib().tg_direct_get_stats(self.handle, st.ctypes.data))
+        return {"supernodes": int(st[0]), "levels": int(st[1]),
+                "factor_bytes": st[2], "pool_bytes": st[3],
+                "flops": st[4], "max_front": int(st[5])}
+
+    def __del__(self):
+        try:
+            _lib.lib().tg_direct_decref(self.handle)
+        except Exception:
+            pass
+
+
 class Ksm:
     """tg_ksm: restarted GMRES (optionally mixed precision)."""
 

@@ -1,0 +1,187 @@
+// CPU run of the direct factorisation's GPU kernels
+// (tacs_gb300/csrc/direct_kernels.cuh): every CTA runs as one thread, in
+// sequence, which computes what the GPU does because each kernel is
+// written as phases of independent strided work separated by barriers.
+// The launch sequence mirrors tg_direct_factor / tg_direct_solve
+// (tacs_gb300/csrc/tg_direct.cu).  Built by tests/test_direct_symbolic.py
+// with g++ and called through ctypes; test infrastructure only.
+#define DK_EMULATE
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+struct EmuDim3 {
+  unsigned x, y, z;
+};
+static EmuDim3 threadIdx{0, 0, 0}, blockIdx{0, 0, 0}, blockDim{1, 1, 1},
+    gridDim{1, 1, 1};
+#define __global__
+#define __device__
+#define __forceinline__ inline
+#define __shared__ static
+#define __launch_bounds__(n)
+#define __syncthreads() ((void)0)
+static std::vector<double> g_dyn;
+static double *dk_dyn_smem() { return g_dyn.data(); }
+static inline int atomicCAS(int *a, int cmp, int val) {
+  const int old = *a;
+  if (old == cmp) *a = val;
+  return old;
+}
+namespace tg {
+namespace dk {
+namespace {
+inline bool dk_isfinite(double x) { return std::isfinite(x); }
+inline double dk_sqrt(double x) { return std::sqrt(x); }
+}  // namespace
+}  // namespace dk
+}  // namespace tg
+
+#include "direct_kernels.cuh"
+#include "direct_symbolic.h"
+
+using namespace tg::dk;
+
+template <class K, class... Args>
+static void launch(K kernel, unsigned gx, unsigned gy, size_t smem_doubles,
+                   Args... args) {
+  g_dyn.assign(smem_doubles + 1, 0.0);
+  gridDim = {gx, gy, 1};
+  for (unsigned y = 0; y < gy; y++)
+    for (unsigned x = 0; x < gx; x++) {
+      blockIdx = {x, y, 0};
+      kernel(args...);
+    }
+}
+
+extern "C" {
+
+// x = A^-1 b for the assembled BCSR matrix A with row boundary conditions
+// (bcmask per node), by the GPU kernels run on the CPU.  small_max: fronts
+// of at most this many scalar rows take the one-CTA kernel, larger ones the
+// panel path.  Returns 0, or the failing supernode + 1.
+int de_solve(int n, int bs, const int *rowp, const int *cols,
+             const double *vals, const int *bcmask_in, const double *xyz,
+             int small_max, const double *b, double *x) {
+  std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
+  std::vector<int> perm = tg::direct::nested_dissection(rp, cs, 64, xyz);
+  tg::direct::Analysis an = tg::direct::analyse(rp, cs, perm);
+  const int ns = (int)an.sn_col.size() - 1;
+  const size_t b2 = (size_t)bs * bs, N = (size_t)n * bs;
+  std::vector<int> fm(ns), fc(ns), ch_ptr(ns + 1, 0), ch_list(ns + 1);
+  std::vector<int64_t> v_off(ns, 0);
+  int64_t vacc = 0;
+  int max_front = 0;
+  for (int s = 0; s < ns; s++) {
+    fm[s] = (an.sn_rowptr[s + 1] - an.sn_rowptr[s]) * bs;
+    fc[s] = (an.sn_col[s + 1] - an.sn_col[s]) * bs;
+    max_front = std::max(max_front, fm[s]);
+    v_off[s] = vacc;
+    vacc += fm[s] - fc[s];
+    if (an.sn_parent[s] >= 0) ch_ptr[an.sn_parent[s] + 1]++;
+  }
+  for (int s = 0; s < ns; s++) ch_ptr[s + 1] += ch_ptr[s];
+  {
+    std::vector<int> fill(ch_ptr.begin(), ch_ptr.end() - 1);
+    for (int s = 0; s < ns; s++)
+      if (an.sn_parent[s] >= 0) ch_list[fill[an.sn_parent[s]]++] = s;
+  }
+  std::vector<int> bcmask(bcmask_in, bcmask_in + n);
+  std::vector<double> lstore((size_t)an.l_total * b2),
+      pool((size_t)an.u_peak * b2 + 1), contrib(vacc + 1), ypos(N), xpos(N),
+      pb(N), kpb(N);
+  int failflag = 0;
+  tg::DirectView v;
+  v.bs = bs;
+  v.perm = an.perm.data();
+  v.bcmask = bcmask.data();
+  v.sn_col = an.sn_col.data();
+  v.sn_rowptr = an.sn_rowptr.data();
+  v.sn_rows = an.sn_rows.data();
+  v.sn_parent = an.sn_parent.data();
+  v.ea_ptr = an.ea_ptr.data();
+  v.ea_rel = an.ea_rel.data();
+  v.asm_ptr = an.asm_ptr.data();
+  v.asm_blk = an.asm_blk.data();
+  v.asm_row = an.asm_row.data();
+  v.asm_col = an.asm_col.data();
+  v.ch_ptr = ch_ptr.data();
+  v.ch_list = ch_list.data();
+  v.l_off = an.l_off.data();
+  v.u_off = an.u_off.data();
+  v.v_off = v_off.data();
+  v.lstore = lstore.data();
+  v.pool = pool.data();
+
+  // factor: the sequence of tg_direct_factor (small fronts of a level in
+  // one launch, large ones panel by panel)
+  std::vector<int> small_h, small_ptr(1, 0), large_h, large_ptr(1, 0);
+  for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+    for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+      const int sn = an.level_sn[t];
+      if (fm[sn] > small_max) large_h.push_back(sn);
+      else small_h.push_back(sn);
+    }
+    small_ptr.push_back((int)small_h.size());
+    large_ptr.push_back((int)large_h.size());
+  }
+  for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
+    const int *lv = an.level_sn.data() + lb;
+    const int cnt = le - lb;
+    launch(direct_zero_kernel, cnt, 1, 0, v, lv, cnt);
+    launch(direct_assemble_kernel, cnt, 1, 0, v, lv, cnt, vals);
+    launch(direct_extend_add_kernel, cnt, 1, 0, v, lv, cnt);
+    const int sb = small_ptr[L], se = small_ptr[L + 1];
+    if (se > sb)
+      launch(direct_factor_small_kernel, se - sb, 1, 0, v,
+             (const int *)small_h.data() + sb, se - sb, &failflag);
+    for (int t = large_ptr[L]; t < large_ptr[L + 1]; t++) {
+      const int sn = large_h[t];
+      for (int k0 = 0; k0 < fc[sn]; k0 += kPanel) {
+        const int nb = std::min(kPanel, fc[sn] - k0);
+        launch(direct_panel_kernel, 1, 1, 0, v, sn, k0, nb, &failflag);
+        const int rest = fm[sn] - (k0 + nb);
+        if (rest > 0) {
+          const unsigned tiles = (rest + kTile - 1) / kTile;
+          launch(direct_trailing_kernel, tiles, tiles, 0, v, sn, k0, nb);
+        }
+      }
+    }
+  }
+  if (failflag) return failflag;
+
+  // solve: the sequence of tg_direct_solve
+  launch(direct_bc_mask_kernel, 1, 1, 0, n, bs, (const int *)bcmask.data(), b,
+         pb.data());
+  for (int i = 0; i < n; i++)  // the BCSR mat-vec
+    for (int r = 0; r < bs; r++) {
+      double acc = 0.0;
+      for (int j = rowp[i]; j < rowp[i + 1]; j++)
+        for (int q = 0; q < bs; q++)
+          acc += vals[b2 * j + r * bs + q] * pb[(size_t)cols[j] * bs + q];
+      kpb[(size_t)i * bs + r] = acc;
+    }
+  launch(direct_rhs_kernel, 1, 1, 0, n, bs, (const int *)an.perm.data(), b,
+         (const double *)kpb.data(), (const double *)pb.data(), ypos.data());
+  const int nl = (int)an.level_ptr.size() - 1;
+  for (int L = 0; L < nl; L++) {
+    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
+    launch(direct_forward_kernel, le - lb, 1, max_front, v,
+           (const int *)an.level_sn.data() + lb, le - lb, ypos.data(),
+           contrib.data());
+  }
+  for (int L = nl - 1; L >= 0; L--) {
+    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
+    launch(direct_backward_kernel, le - lb, 1, max_front, v,
+           (const int *)an.level_sn.data() + lb, le - lb,
+           (const double *)ypos.data(), xpos.data());
+  }
+  launch(direct_unpermute_kernel, 1, 1, 0, n, bs, (const int *)an.perm.data(),
+         (const double *)xpos.data(), x);
+  return 0;
+}
+
+}  // extern "C"

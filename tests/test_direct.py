@@ -1,0 +1,99 @@
+"""The direct factorisation on the GPU (tg_direct: nested dissection,
+supernodes, level-by-level multifrontal block Cholesky; the host analysis
+and the kernels are also checked on the CPU in test_direct_symbolic.py).
+
+* static solves K u = f - R(0) against the reference's own solutions
+  (golden fixtures): 1e-7, the GMRES tolerance of the reference's solve
+  times cond(K);
+* a thin simply supported plate, where ILU(0)-GMRES stalls: the true
+  residual at rounding level (1e-13 of |K| |u|) and agreement with a sparse
+  LU on the host (1e-6);
+* both orders (node coordinates and level structures) and refactoring
+  after new matrix values.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_case, rel
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import problem
+    return problem
+
+
+def _rhs(M, prob, mat):
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    f = M.vec(prob["force"])
+    M.apply_bcs(f)
+    return f - r0
+
+
+@pytest.mark.parametrize("name", ["shell_plate8", "shell_c1", "hex_block",
+                                  "shell_cyl"])
+@pytest.mark.parametrize("coords", [True, False])
+def test_direct_static_solve_matches_reference(gpu, name, coords):
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    b = _rhs(M, prob, mat)
+    d = gpu.Direct(mat, use_coords=coords)
+    d.factor()
+    u = d.solve(b)
+    assert rel(u.cpu().numpy(), ref["u"]) < 1e-7
+    st = d.stats()
+    assert st["supernodes"] > 0 and st["levels"] > 0
+
+
+def test_direct_thin_plate_where_ilu_stalls(gpu):
+    from scipy import sparse
+    from scipy.sparse.linalg import spsolve
+    from tacs_gb300 import meshes
+    n = 48
+    prob = meshes.plate(n, n, 2.0, 2.0, t=0.002)
+    e = meshes.plate_edges(n, n).astype(np.int32)
+    prob["bc_nodes"], prob["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
+    prob["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    prob["pres_vals"] = np.full(4 * n * n, 1e3)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    b = _rhs(M, prob, mat)
+    d = gpu.Direct(mat)
+    d.factor()
+    u = d.solve(b).cpu().numpy()
+    bs = mat.bsize
+    K = sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
+                           mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
+                          shape=(M.ndof, M.ndof)).tocsr()
+    bh = b.cpu().numpy()
+    Kinf = abs(K).sum(axis=1).max()
+    assert np.abs(K @ u - bh).max() < 1e-13 * Kinf * np.abs(u).max()
+    assert rel(u, spsolve(K.tocsc(), bh)) < 1e-6
+
+
+def test_direct_refactor_after_new_values(gpu):
+    from tacs_gb300 import meshes
+    rng = np.random.default_rng(3)
+    prob = meshes.clamped_plate(16, thick=rng.uniform(0.005, 0.02, 256))
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    b = _rhs(M, prob, mat)
+    d = gpu.Direct(mat)
+    d.factor()
+    u1 = d.solve(b)
+    # new thicknesses: same pattern, new values, same analysis
+    M.set_design_vars(torch.as_tensor(rng.uniform(0.005, 0.02, 256),
+                                      device="cuda"))
+    b2 = _rhs(M, prob, mat)
+    d.factor()
+    u2 = d.solve(b2)
+    r = mat.mult(u2) - b2
+    assert (r.abs().max() / b2.abs().max()).item() < 1e-9
+    assert not torch.equal(u1, u2)

@@ -139,3 +139,56 @@ def test_storage_plan_has_no_overlap(dc, name, prob):
     l_total, peak, busiest, bad = out
     assert bad == 0
     assert busiest <= peak <= 2 * busiest + 1
+
+
+# ------------------------------------------------------------------------
+# The GPU kernels of the numeric phase, run on the CPU (one thread per CTA,
+# tests/cpp/direct_emul.cpp) through the launch sequence of tg_direct.cu,
+# on the assembled matrices with their row boundary conditions.
+EMUL = os.path.join(ROOT, "tests", "cpp", "direct_emul.cpp")
+
+
+@pytest.fixture(scope="module")
+def de(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("de") / "libde.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", INC,
+                    EMUL, "-o", out], check=True)
+    lib = C.CDLL(out)
+    P = C.c_void_p
+    lib.de_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int, P, P]
+    return lib
+
+
+def _bcmask(prob):
+    m = np.zeros(int(prob["nnodes"]), np.int32)
+    for node, mask in zip(prob["bc_nodes"], prob["bc_masks"]):
+        m[int(node)] |= int(mask)
+    return m
+
+
+@pytest.mark.parametrize("name,prob", list(_problems()),
+                         ids=[p[0] for p in _problems()])
+@pytest.mark.parametrize("small_max,coords", [(256, True), (0, True),
+                                              (1 << 30, False)])
+def test_gpu_kernels_on_cpu_solve_assembled_system(de, name, prob, small_max,
+                                                   coords):
+    """small_max 0 sends every front through the panel + trailing-tile
+    path, 1 << 30 every front through the one-CTA kernel."""
+    from scipy import sparse
+    from scipy.sparse.linalg import spsolve
+    n, bs, rowp, cols, vals = _matrix(prob)
+    K = sparse.bsr_matrix((vals.reshape(-1, bs, bs), cols, rowp),
+                          shape=(n * bs, n * bs)).tocsr()
+    b = np.random.default_rng(2).standard_normal(n * bs)
+    x = np.zeros_like(b)
+    xyz = np.ascontiguousarray(prob["xpts"], np.float64) if coords else None
+    rc = de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
+                     _ptr(_bcmask(prob)), _ptr(xyz), small_max, _ptr(b),
+                     _ptr(x))
+    assert rc == 0
+    Kinf = abs(K).sum(axis=1).max()
+    assert np.abs(K @ x - b).max() < 1e-14 * Kinf * np.abs(x).max()
+    assert rel(x, spsolve(K.tocsc(), b)) < 1e-5
