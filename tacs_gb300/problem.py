@@ -412,21 +412,34 @@ class GpuModel:
 
 def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
                    pc_kind=_lib.PC_ILU0, mixed=False, funcs=(0, 1),
-                   lev_fill=0):
+                   lev_fill=0, direct=False):
     """Linear static solve + adjoint gradients on the GPU, following the
     reference harness (tests/integration_tests/static_analysis_base_test.py:
     359-427): K(u=0) and R(0), ILU(0), GMRES for R - f, functions, dfdu,
-    adjoint solve with the same row-BC matrix, dfdx - psi^T dR/dx."""
+    adjoint solve with the same row-BC matrix, dfdx - psi^T dR/dx.  With
+    direct, both solves use the complete factorisation (Direct) instead."""
     dev = torch.device("cuda")
     u0 = model.vec()
     res = model.vec()
     mat = model.new_mat()
     model.assemble_jacobian(u0, mat, res)
-    prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-    pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
-    pc.factor()
-    ksm = Ksm(mat, pc, m, nrestart, mixed)
-    ksm.set_tolerances(rtol, atol)
+    pc = ksm = dsol = None
+    if direct:
+        dsol = Direct(mat)
+        dsol.factor()
+
+        class _Exact:  # the solves' interface of Ksm
+            iters = 0
+
+            def solve(self, b):
+                return dsol.solve(b), 1
+        ksm = _Exact()
+    else:
+        prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
+        pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
+        pc.factor()
+        ksm = Ksm(mat, pc, m, nrestart, mixed)
+        ksm.set_tolerances(rtol, atol)
     f = torch.as_tensor(np.asarray(force, np.float64), device=dev).clone()
     model.apply_bcs(f)
     res -= f
@@ -447,7 +460,8 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
         grads.append(g)
         psis.append(psi)
     return dict(u=u, funcs=fvals, grads=grads, psis=psis, flag=flag,
-                flags=flags, iters=iters, mat=mat, pc=pc, ksm=ksm)
+                flags=flags, iters=iters, mat=mat, pc=pc, ksm=ksm,
+                direct=dsol)
 
 
 def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,

@@ -9,7 +9,8 @@ and the kernels are also checked on the CPU in test_direct_symbolic.py).
   residual at rounding level (1e-13 of |K| |u|) and agreement with a sparse
   LU on the host (1e-6);
 * both orders (node coordinates and level structures) and refactoring
-  after new matrix values.
+  after new matrix values;
+* the reference harness's adjoint gradients with both solves direct.
 """
 import numpy as np
 import pytest
@@ -97,3 +98,22 @@ def test_direct_refactor_after_new_values(gpu):
     r = mat.mult(u2) - b2
     assert (r.abs().max() / b2.abs().max()).item() < 1e-9
     assert not torch.equal(u1, u2)
+
+
+@pytest.mark.parametrize("name", ["shell_plate8", "hex_block", "shell_cyl"])
+def test_direct_adjoint_gradients_match_reference(gpu, name):
+    """The reference harness's static solve and adjoint with both solves
+    direct: functions, design and node-coordinate gradients against the
+    reference's (1e-7)."""
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    r = gpu.static_adjoint(M, prob["force"], direct=True)
+    assert rel(r["u"].cpu().numpy(), ref["u"]) < 1e-7
+    assert rel(r["funcs"], ref["funcs"]) < 1e-7
+    assert rel(r["grads"][0].cpu().numpy(), ref["grad_comp"]) < 1e-7
+    assert rel(r["grads"][1].cpu().numpy(), ref["grad_ks"]) < 1e-7
+    for k, key in ((0, "comp"), (1, "ks")):
+        M.eval_functions(r["u"], [k])
+        g = M.node_vec()
+        M.add_total_xpt_derivative(r["u"], k, r["psis"][k], g, 1.0, -1.0)
+        assert rel(g.cpu().numpy(), ref["grad_xpt_" + key]) < 1e-7
