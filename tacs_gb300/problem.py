@@ -465,7 +465,8 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
 
 
 def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
-                    pc_kind=_lib.PC_ILU0, mixed=False, func=1, lev_fill=0):
+                    pc_kind=_lib.PC_ILU0, mixed=False, func=1, lev_fill=0,
+                    direct=False):
     """Independent meshes (element / node segments set from the problem's
     seg_elem_ptr / seg_node_ptr) under several load cases, solved and
     differentiated together: one batched GMRES for all forward solves, the
@@ -483,23 +484,38 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     u0 = model.vec()
     mat = model.new_mat()
     model.assemble_jacobian(u0, mat, model.vec())
-    prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-    pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
-    pc.factor()
-    ksm = Ksm(mat, pc, m, nrestart, mixed)
-    ksm.set_tolerances(rtol, atol)
-    ksm.set_segments(prob["seg_node_ptr"])
+    if direct:
+        # one complete factorisation of the block-diagonal matrix; every
+        # load case and mesh is then exact (reported as converged in 0)
+        dsol = Direct(mat)
+        dsol.factor()
+        nsys = nlc * model.nseg
+
+        def solve_multi(B):
+            X = torch.empty_like(B)
+            for lc in range(B.shape[0]):
+                dsol.solve(B[lc], X[lc])
+            z = np.zeros(nsys, np.int32)
+            return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1
+    else:
+        prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
+        pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
+        pc.factor()
+        ksm = Ksm(mat, pc, m, nrestart, mixed)
+        ksm.set_tolerances(rtol, atol)
+        ksm.set_segments(prob["seg_node_ptr"])
+        solve_multi = ksm.solve_multi
     F = loads.clone()
     for lc in range(nlc):
         model.apply_bcs(F[lc])
-    U, it_f, fl_f, rn_f, _ = ksm.solve_multi(F)
+    U, it_f, fl_f, rn_f, _ = solve_multi(F)
     fvals = np.zeros((nlc, model.nseg))
     dfdu = torch.zeros_like(U)
     for lc in range(nlc):
         fvals[lc] = model.eval_functions_segments(U[lc], func)
         model.add_sv_sens_segments(U[lc], func, dfdu[lc])
         model.apply_bcs(dfdu[lc])
-    Psi, it_a, fl_a, rn_a, _ = ksm.solve_multi(dfdu)
+    Psi, it_a, fl_a, rn_a, _ = solve_multi(dfdu)
     grads = torch.zeros(nlc, model.ndv, dtype=torch.float64, device="cuda")
     for lc in range(nlc):
         model.eval_functions_segments(U[lc], func)
