@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .problem import Ksm, Pc
+from .problem import Direct, Ksm, Pc
 
 
 class StaticSolver:
@@ -36,7 +36,8 @@ class StaticSolver:
 
     def __init__(self, model, loads, m=100, nrestart=50, rtol=1e-12,
                  atol=1e-30, pc_kind=_lib.PC_ILU0, mixed=False,
-                 include_element_loads=True, segments=False, lev_fill=0):
+                 include_element_loads=True, segments=False, lev_fill=0,
+                 direct=False):
         self.model = model
         F = torch.as_tensor(np.asarray(loads, np.float64) if not
                             torch.is_tensor(loads) else loads,
@@ -52,12 +53,16 @@ class StaticSolver:
                                  "element, numbered like the elements")
             model.set_segments(model.prob["seg_elem_ptr"])
         self.mat = model.new_mat()
-        prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
-        self.pc = Pc(self.mat, pc_kind, prec, lev_fill=lev_fill)
-        self.ksm = Ksm(self.mat, self.pc, m, nrestart, mixed)
-        self.ksm.set_tolerances(rtol, atol)
-        if segments:
-            self.ksm.set_segments(model.prob["seg_node_ptr"])
+        self.direct = Direct(self.mat) if direct else None
+        if direct:
+            self.pc = self.ksm = None
+        else:
+            prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
+            self.pc = Pc(self.mat, pc_kind, prec, lev_fill=lev_fill)
+            self.ksm = Ksm(self.mat, self.pc, m, nrestart, mixed)
+            self.ksm.set_tolerances(rtol, atol)
+            if segments:
+                self.ksm.set_segments(model.prob["seg_node_ptr"])
         self.u = None
         self.iters = []
         self.flags = []
@@ -69,13 +74,16 @@ class StaticSolver:
         M.set_design_vars(x.detach().to(torch.float64).contiguous())
         r0 = M.vec()
         M.assemble_jacobian(M.vec(), self.mat, r0)
-        self.pc.factor()
+        if self.direct is not None:
+            self.direct.factor()
+        else:
+            self.pc.factor()
         B = self.F.clone()
         for lc in range(self.nlc):
             M.apply_bcs(B[lc])
             if self.include_element_loads:
                 B[lc] -= r0
-        U, it, fl, _, rc = self.ksm.solve_multi(B)
+        U, it, fl, _, rc = self._solve_multi(B)
         self.u = U
         self.iters.append(it)
         self.flags.append(fl)
@@ -83,6 +91,18 @@ class StaticSolver:
             raise _lib.TacsGpuError(
                 f"GMRES did not converge (flags {fl.tolist()})")
         return U
+
+    def _solve_multi(self, B):
+        """All load cases (and meshes): batched GMRES, or the complete
+        factorisation one load case at a time (exact, 0 iterations)."""
+        if self.direct is None:
+            return self.ksm.solve_multi(B)
+        X = torch.empty_like(B)
+        for lc in range(B.shape[0]):
+            self.direct.solve(B[lc], X[lc])
+        nsys = B.shape[0] * (self.model.nseg if self.segments else 1)
+        return (X, np.zeros(nsys, np.int32), np.ones(nsys, np.int32),
+                np.zeros(nsys), 1)
 
     def functions(self, func):
         M = self.model
@@ -119,7 +139,7 @@ class StaticSolver:
                     dfdu[lc, vpn * nptr[g]:vpn * nptr[g + 1]] *= W[lc, g]
         else:
             dfdu *= torch.as_tensor(W[:, 0], device="cuda")[:, None]
-        Psi, it, fl, _, rc = self.ksm.solve_multi(dfdu)
+        Psi, it, fl, _, rc = self._solve_multi(dfdu)
         self.iters.append(it)
         self.flags.append(fl)
         if rc != 1:

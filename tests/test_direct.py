@@ -132,3 +132,21 @@ def test_direct_batched_adjoint_matches_gmres(gpu):
     assert int(b["flags_fwd"].sum()) == b["flags_fwd"].size
     assert rel(a["funcs"], b["funcs"]) < 1e-8
     assert rel(a["grads"].cpu().numpy(), b["grads"].cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("func", [0, 1])
+def test_direct_autograd_matches_reference_adjoint(gpu, func):
+    """torch.autograd through the direct solves: the reference's adjoint
+    gradient (1e-7)."""
+    from tacs_gb300 import autograd as ag
+    prob, ref = load_case("shell_plate8")
+    M = gpu.GpuModel(prob)
+    solver = ag.StaticSolver(M, prob["force"], direct=True)
+    x = np.zeros(M.ndv)
+    x[np.asarray(prob["dvnum"])] = prob["thick"]
+    x = torch.as_tensor(x, device="cuda").requires_grad_(True)
+    f = ag.static_functional(x, solver, func)
+    assert abs(f.item() - ref["funcs"][func]) < 1e-7 * abs(ref["funcs"][func])
+    f.sum().backward()
+    g_ref = ref["grad_comp"] if func == 0 else ref["grad_ks"]
+    assert rel(x.grad.cpu().numpy(), g_ref) < 1e-7
