@@ -140,6 +140,56 @@ def xpt_timing(M, r, torch, reps=3):
             "elements_per_s": [M.nelem / (t / 1e3) for t in ms]}
 
 
+def c2_adjoint_section(torch, n=512):
+    """The 512 x 512 simply supported plate (per-element thickness, nodal
+    pressure field): compliance and its gradient with respect to the
+    262,144 thicknesses through torch.autograd, both solves by the complete
+    multifrontal factorisation (GMRES(80) + ILU(0) does not converge on
+    this plate).  Times the analysis, the factorisation, one solve and the
+    whole gradient."""
+    from tacs_gb300 import autograd as ag
+    from tacs_gb300 import problem
+    p = c2_problem(n=n)
+    M = problem.GpuModel(p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    solver = ag.StaticSolver(M, np.zeros(M.ndof), direct=True)
+    torch.cuda.synchronize()
+    t_analysis = time.perf_counter() - t0
+    x = torch.as_tensor(np.asarray(p["thick"]), device="cuda")
+    out = {"workload": f"simply supported MITC4 plate {n}x{n}, compliance "
+                       "gradient through torch.autograd, direct solves",
+           "elements": n * n, "dof": int(M.ndof),
+           "analysis_s": t_analysis, "factor": solver.direct.stats()}
+    for rep in range(2):  # the second pass is timed
+        xr = x.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f = ag.static_functional(xr, solver, 0)
+        f.sum().backward()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    out["s_per_gradient"] = dt
+    out["compliance"] = float(f.item())
+    b = M.vec()
+    M.assemble_res(M.vec(), res=b)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    solver.direct.factor()
+    e1.record()
+    torch.cuda.synchronize()
+    out["factor_ms"] = e0.elapsed_time(e1)
+    e0.record()
+    u = solver.direct.solve(b)
+    e1.record()
+    torch.cuda.synchronize()
+    out["solve_ms"] = e0.elapsed_time(e1)
+    r = solver.mat.mult(u) - b
+    out["true_residual_rel"] = float(r.abs().max() / b.abs().max())
+    return out
+
+
 def hex_section(torch, steps=5):
     """Hex8 SIMP block (128 x 128 x 64 elements, 3.24M dof, 28.6M 3x3
     blocks): residual + Jacobian assembly throughput."""
@@ -429,6 +479,9 @@ def main():
     ap.add_argument("--adj-size", type=int, default=64)
     ap.add_argument("--no-hex", action="store_true")
     ap.add_argument("--no-cylinder", action="store_true")
+    ap.add_argument("--c2-adjoint", action="store_true",
+                    help="the 512 x 512 plate's autograd gradient with "
+                         "direct solves")
     ap.add_argument("--batch", type=int, default=12)
     ap.add_argument("--batch-nmax", type=int, default=96)
     ap.add_argument("--batch-pc", type=int, default=0)
@@ -568,6 +621,8 @@ def main():
         line["adjoint"] = adj
     if rank == 0 and not args.no_hex:
         line["hex_c3"] = hex_section(torch)
+    if rank == 0 and args.c2_adjoint:
+        line["c2_adjoint"] = c2_adjoint_section(torch, args.size)
     if rank == 0 and not args.no_cylinder:
         line["cylinder_c5"] = cylinder_section(torch)
     if rank == 0 and args.batch > 0:
