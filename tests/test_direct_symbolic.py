@@ -64,6 +64,8 @@ def _problems():
     yield "hex 6x5x4", meshes.hex_c3(6, 5, 4)
     yield "cylinder", load_case("shell_cyl")[0]
     yield "4 plates", meshes.batch_plates(count=4, nmin=6, nmax=20)
+    yield "separate shells", load_case("shell_rand")[0]
+    yield "separate solids", load_case("hex_rand")[0]
 
 
 @pytest.mark.parametrize("name,prob", list(_problems()),
