@@ -28,7 +28,7 @@ import torch
 from . import _lib, bdf
 from . import elements as _el
 from . import functions as _fn
-from .problem import GpuModel, Ksm, Pc
+from .problem import Direct, GpuModel, Ksm, Pc
 
 
 class pyTACS:
@@ -110,6 +110,16 @@ class pyTACS:
         return StaticProblem(name, self, options)
 
 
+class _DirectSolves:
+    """The solve interface of Ksm over a Direct factorisation."""
+
+    def __init__(self, direct):
+        self.direct = direct
+
+    def solve(self, b):
+        return self.direct.solve(b), 1
+
+
 class StaticProblem:
     """Linear static analysis (tacs/problems/static.py) on the GPU."""
 
@@ -118,9 +128,11 @@ class StaticProblem:
     # direct factorisation, so the fill level is capped at MAX_FILL (block
     # ILU(5)) and the Krylov space is larger than the reference's 10.
     MAX_FILL = 5
+    # "directSolve" (an extension) solves both systems by the complete
+    # multifrontal factorisation instead, as the reference's default does
     defaults = {"subSpaceSize": 100, "nRestarts": 20,
                 "L2ConvergenceRel": 1e-12, "L2Convergence": 1e-30,
-                "PCFillLevel": 1000}
+                "PCFillLevel": 1000, "directSolve": False}
 
     def __init__(self, name, fea, options=None):
         self.name, self.fea = name, fea
@@ -218,13 +230,18 @@ class StaticProblem:
                 rec["xpts"] = self._xpts
             self._model = GpuModel(rec)
             self._mat = self._model.new_mat()
-            lev = max(0, min(int(self.options["PCFillLevel"]),
-                             self.MAX_FILL))
-            self._pc = Pc(self._mat, lev_fill=lev)
-            self._ksm = Ksm(self._mat, self._pc, self.options["subSpaceSize"],
-                            self.options["nRestarts"])
-            self._ksm.set_tolerances(self.options["L2ConvergenceRel"],
-                                     self.options["L2Convergence"])
+            if self.options["directSolve"]:
+                self._pc = Direct(self._mat)
+                self._ksm = _DirectSolves(self._pc)
+            else:
+                lev = max(0, min(int(self.options["PCFillLevel"]),
+                                 self.MAX_FILL))
+                self._pc = Pc(self._mat, lev_fill=lev)
+                self._ksm = Ksm(self._mat, self._pc,
+                                self.options["subSpaceSize"],
+                                self.options["nRestarts"])
+                self._ksm.set_tolerances(self.options["L2ConvergenceRel"],
+                                         self.options["L2Convergence"])
         return self._model
 
     def solve(self, Fext=None):

@@ -113,3 +113,35 @@ def test_pytacs_static_problems_match_reference(tmp_path):
             sp.setNodes(X0)
             fd = (vals[0] - vals[1]) / (2 * h)
             assert abs(fd - gx[j]) < 1e-5 * np.abs(gx).max(), (key, j)
+
+
+@pytest.mark.gpu
+def test_pytacs_direct_solve_matches_reference(tmp_path):
+    """The same problems solved by the complete factorisation (option
+    directSolve): the known answers (1e-8) and the same sensitivities as
+    the iterative solves (1e-7)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import functions, pytacs
+    path, ref = _bdf(tmp_path)
+    fea = pytacs.pyTACS(path)
+    fea.initialize(_callback)
+    out = {}
+    for direct in (False, True):
+        sp = fea.createStaticProblem("pressure",
+                                     options={"directSolve": direct})
+        sp.addPressureToComponents(fea.selectCompIDs(include="PLATE"), 100e3)
+        sp.addFunction("compliance", functions.Compliance)
+        sp.addFunction("ks_vmfailure", functions.KSFailure, ksWeight=10.0)
+        sp.solve()
+        funcs, sens = {}, {}
+        sp.evalFunctions(funcs)
+        sp.evalFunctionsSens(sens)
+        out[direct] = (funcs, sens)
+    funcs, sens = out[True]
+    for key in ("pressure_compliance", "pressure_ks_vmfailure"):
+        assert abs(funcs[key] / ref[key] - 1) < 1e-8, key
+        for part in ("struct", "Xpts"):
+            a, b = sens[key][part], out[False][1][key][part]
+            assert np.abs(a - b).max() < 1e-7 * np.abs(b).max(), (key, part)
