@@ -21,7 +21,7 @@ import torch
 
 from . import _lib
 from . import elements as _el
-from .problem import GpuModel, Ksm as _Ksm, Pc as _Pc
+from .problem import Direct as _Direct, GpuModel, Ksm as _Ksm, Pc as _Pc
 
 NORMAL, TRANSPOSE = _lib.MAT_NORMAL, _lib.MAT_TRANSPOSE
 
@@ -81,10 +81,13 @@ class Vec:
 
 
 class Mat:
-    """TACSParallelMat over a BCSRMat of the assembler's pattern."""
+    """TACSParallelMat over a BCSRMat of the assembler's pattern; with
+    schur=True the matrix of createSchurMat, whose Pc is the complete
+    factorisation."""
 
-    def __init__(self, assembler):
+    def __init__(self, assembler, schur=False):
         self.assembler = assembler
+        self.schur = schur
         self.gm = assembler._model.new_mat()
 
     def zeroEntries(self):
@@ -116,16 +119,30 @@ class Pc:
 
     def __init__(self, mat, *args, precision="fp64", fill_level=5,
                  **kwargs):
-        prec = _lib.PREC_FP32 if precision == "fp32" else _lib.PREC_FP64
         self.mat = mat
+        self.direct = None
+        if getattr(mat, "schur", False):
+            # TACSSchurPc(mat, lev_fill = 1000000 by default, ...): with one
+            # process a complete factorisation; lev_fill below that is not
+            # offered on this matrix
+            if int(kwargs.get("lev_fill", 1000000)) < 1000:
+                raise NotImplementedError("incomplete Schur factorisations "
+                                          "(lev_fill < 1000)")
+            self.direct = _Direct(mat.gm)
+            self.pc = None
+            return
+        prec = _lib.PREC_FP32 if precision == "fp32" else _lib.PREC_FP64
         self.pc = _Pc(mat.gm, _lib.PC_ILU0, prec, lev_fill=int(fill_level))
 
     def factor(self):
-        self.pc.factor()
+        (self.direct or self.pc).factor()
 
     def applyFactor(self, x, y):
         y._host = None
-        self.pc.apply(x._sync(), y.dev)
+        if self.direct is not None:
+            self.direct.solve(x._sync(), y.dev)
+        else:
+            self.pc.apply(x._sync(), y.dev)
 
 
 class KSM:
@@ -134,15 +151,23 @@ class KSM:
     with iterative refinement (needs Pc(..., precision='fp32'))."""
 
     def __init__(self, mat, pc, m, nrestart=1, isFlexible=0, mixed=False):
-        self.ksm = _Ksm(mat.gm, pc.pc if pc is not None else None, m,
-                        nrestart, mixed)
+        # with the complete factorisation as preconditioner GMRES converges
+        # in one step; the solve applies the factorisation directly
+        self.direct = pc.direct if pc is not None else None
+        self.ksm = None if self.direct is not None else _Ksm(
+            mat.gm, pc.pc if pc is not None else None, m, nrestart, mixed)
         self._iters, self._res = 0, 0.0
 
     def setTolerances(self, rtol, atol):
-        self.ksm.set_tolerances(rtol, atol)
+        if self.ksm is not None:
+            self.ksm.set_tolerances(rtol, atol)
 
     def solve(self, b, x, zero_guess=1):
         x._host = None
+        if self.direct is not None:
+            self.direct.solve(b._sync(), x.dev)
+            self._iters, self._res = 1, 0.0
+            return 1
         _, flag = self.ksm.solve(b._sync(), x.dev, bool(zero_guess))
         self._iters, self._res = self.ksm.iters, self.ksm.resnorm
         return flag
@@ -279,6 +304,11 @@ class Assembler:
 
     def createMat(self):
         return Mat(self)
+
+    def createSchurMat(self, order=None):
+        """The matrix pyTACS solves directly (createSchurMat); its Pc is the
+        complete factorisation."""
+        return Mat(self, schur=True)
 
     def getNumOwnedNodes(self):
         return self.nnodes

@@ -93,7 +93,10 @@ def _build(prob):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["shell_c1", "shell_plate8", "hex_block",
                                   "shell_cyl"])
-def test_static_adjoint_through_reference_api(name):
+@pytest.mark.parametrize("schur", [False, True])
+def test_static_adjoint_through_reference_api(name, schur):
+    """schur=True: createSchurMat with the default Pc, the reference's
+    direct solve (here the complete multifrontal factorisation)."""
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.fail("CUDA device required for -m gpu tests")
@@ -101,7 +104,7 @@ def test_static_adjoint_through_reference_api(name):
     prob, ref = load_case(name)
     assembler = _build(prob)
     res, ans = assembler.createVec(), assembler.createVec()
-    mat = assembler.createMat()
+    mat = assembler.createSchurMat() if schur else assembler.createMat()
     assembler.zeroVariables()
     assembler.assembleJacobian(1.0, 0.0, 0.0, res, mat)
     pc = TACS.Pc(mat)
