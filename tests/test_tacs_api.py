@@ -14,7 +14,7 @@ TOL = 1e-7
 API = {
     "Assembler": ["create", "setElementConnectivity", "setElements", "addBCs",
                   "initialize", "createVec", "createNodeVec",
-                  "createDesignVec", "createMat", "setNodes",
+                  "createDesignVec", "createMat", "createSchurMat", "setNodes",
                   "setDesignVars", "setVariables", "getVariables",
                   "zeroVariables", "setAuxElements", "assembleRes",
                   "assembleJacobian", "applyBCs", "evalFunctions",
