@@ -305,9 +305,10 @@ class Assembler:
     def createMat(self):
         return Mat(self)
 
-    def createSchurMat(self, order=None):
+    def createSchurMat(self, order_type=None):
         """The matrix pyTACS solves directly (createSchurMat); its Pc is the
-        complete factorisation."""
+        complete factorisation, ordered by nested dissection of the node
+        coordinates whatever order_type asks for."""
         return Mat(self, schur=True)
 
     def getNumOwnedNodes(self):
