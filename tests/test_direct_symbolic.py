@@ -194,3 +194,65 @@ def test_gpu_kernels_on_cpu_solve_assembled_system(de, name, prob, small_max,
     Kinf = abs(K).sum(axis=1).max()
     assert np.abs(K @ x - b).max() < 1e-14 * Kinf * np.abs(x).max()
     assert rel(x, spsolve(K.tocsc(), b)) < 1e-5
+
+
+def _random_spd(n, bs, deg, seed):
+    """A random symmetric block pattern (random geometric graph in 3D plus
+    a few long-range edges) with symmetric positive definite values."""
+    rng = np.random.default_rng(seed)
+    xyz = rng.random((n, 3))
+    rows = [set([i]) for i in range(n)]
+    order = np.argsort(xyz[:, 0])
+    for k, i in enumerate(order):
+        for j in order[k + 1:k + 1 + deg]:
+            if rng.random() < 0.6:
+                rows[i].add(int(j))
+                rows[int(j)].add(int(i))
+    for _ in range(n // 10):
+        i, j = rng.integers(0, n, 2)
+        rows[i].add(int(j))
+        rows[j].add(int(i))
+    rowp = np.zeros(n + 1, np.int32)
+    cols = []
+    for i in range(n):
+        c = sorted(rows[i])
+        cols += c
+        rowp[i + 1] = len(cols)
+    cols = np.array(cols, np.int32)
+    vals = np.zeros((len(cols), bs, bs))
+    for i in range(n):
+        for k in range(rowp[i], rowp[i + 1]):
+            j = cols[k]
+            if j > i:
+                blk = rng.standard_normal((bs, bs))
+                vals[k] = blk
+                kk = rowp[j] + np.searchsorted(cols[rowp[j]:rowp[j + 1]], i)
+                vals[kk] = blk.T
+    for i in range(n):  # diagonal dominance
+        k = rowp[i] + np.searchsorted(cols[rowp[i]:rowp[i + 1]], i)
+        s = np.abs(vals[rowp[i]:rowp[i + 1]]).sum() + 1.0
+        g = rng.standard_normal((bs, bs))
+        vals[k] = s * np.eye(bs) + 0.1 * (g + g.T)
+    return rowp, cols, vals.ravel(), xyz.ravel().copy()
+
+
+@pytest.mark.parametrize("n,bs,deg,seed", [(200, 3, 6, 1), (300, 6, 10, 2),
+                                           (500, 2, 20, 3), (64, 1, 40, 4)])
+@pytest.mark.parametrize("small_max,coords", [(256, True), (0, True),
+                                              (1 << 30, False)])
+def test_gpu_kernels_on_cpu_random_spd(de, n, bs, deg, seed, small_max,
+                                       coords):
+    """Random patterns (uneven degrees, long-range couplings, many
+    children per supernode) beyond the finite-element meshes."""
+    from scipy import sparse
+    rowp, cols, vals, xyz = _random_spd(n, bs, deg, seed)
+    K = sparse.bsr_matrix((vals.reshape(-1, bs, bs), cols, rowp),
+                          shape=(n * bs, n * bs)).tocsr()
+    b = np.random.default_rng(seed).standard_normal(n * bs)
+    x = np.zeros_like(b)
+    rc = de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
+                     _ptr(np.zeros(n, np.int32)),
+                     _ptr(xyz if coords else None), small_max, _ptr(b),
+                     _ptr(x))
+    assert rc == 0
+    assert rel(K @ x, b) < 1e-12
