@@ -185,6 +185,33 @@ class TACSAdditiveSchwarz {
   tg_pc *pc_ = nullptr;
 };
 
+/* TACSSchurPc(mat, levFill, fill, reorderSchur) with its default complete
+   fill: the reference's direct solve, here the complete multifrontal
+   factorisation (tg_direct); applyFactor(x, y) is y = A^-1 x. */
+class TACSSchurPc {
+ public:
+  explicit TACSSchurPc(BCSRMat *mat, int levFill = 1000000,
+                       double fill = 10.0, int reorderSchur = 1) {
+    (void)fill;
+    (void)reorderSchur;
+    if (levFill < 1000)
+      throw TACSError("TACSSchurPc: only the complete factorisation "
+                      "(levFill >= 1000) is on the GPU");
+    check(tg_direct_create(mat->handle(), 1, &d_), "TACSSchurPc");
+  }
+  ~TACSSchurPc() { tg_direct_decref(d_); }
+  TACSSchurPc(const TACSSchurPc &) = delete;
+  TACSSchurPc &operator=(const TACSSchurPc &) = delete;
+  void factor() { check(tg_direct_factor(d_, 0), "factor"); }
+  void applyFactor(const TACSBVec *x, TACSBVec *y) {
+    check(tg_direct_solve(d_, x->getArray(), y->getArray(), 0),
+          "applyFactor");
+  }
+
+ private:
+  tg_direct *d_ = nullptr;
+};
+
 /* GMRES(mat, pc, m, nrestart, isFlexible); mixed != 0 needs an FP32 pc. */
 class GMRES {
  public:

@@ -4,15 +4,19 @@
 // tests/integration_tests/static_analysis_base_test.py:359-427): the
 // 32 x 32 clamped MITC4 plate under 1e3 Pa, t = 0.01, one thickness design
 // variable per element.  Prints one JSON object: the compliance, the KS
-// failure value and both gradients.
+// failure value and both gradients.  With the argument "direct" both
+// solves use TACSSchurPc (the complete factorisation) instead of GMRES
+// with ILU(0).
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "tacs_gb300.hpp"
 
 using namespace tacs_gb300;
 
-int main() {
+int main(int argc, char **argv) {
+  const bool direct = argc > 1 && std::string(argv[1]) == "direct";
   const int n = 32, nx = n + 1, nnodes = nx * nx, nelems = n * n;
   std::vector<int> ptr(nelems + 1), conn(4 * nelems);
   for (int j = 0; j < n; j++)
@@ -66,7 +70,17 @@ int main() {
   pc.factor();
   GMRES gmres(mat, &pc, 300, 10, 0);
   gmres.setTolerances(1e-12, 1e-30);
-  const int flag = gmres.solve(res, ans);
+  TACSSchurPc *schur = nullptr;
+  if (direct) {
+    schur = new TACSSchurPc(mat);
+    schur->factor();
+  }
+  auto solve = [&](TACSBVec *b, TACSBVec *x) {
+    if (!direct) return gmres.solve(b, x);
+    schur->applyFactor(b, x);
+    return 1;
+  };
+  const int flag = solve(res, ans);
   ans->scale(-1.0);
   assembler.setVariables(ans);
 
@@ -83,7 +97,7 @@ int main() {
     TACSBVec *dfdX = assembler.createNodeVec();
     assembler.addSVSens(1.0, 0.0, 0.0, 1, &funcs[k], &dfdu);
     assembler.applyBCs(dfdu);
-    gmres.solve(dfdu, psi);
+    solve(dfdu, psi);
     assembler.addDVSens(1.0, 1, &funcs[k], &dfdx);
     assembler.addAdjointResProducts(-1.0, 1, &psi, &dfdx);
     assembler.addXptSens(1.0, 1, &funcs[k], &dfdX);
@@ -110,6 +124,7 @@ int main() {
     std::printf("]");
   }
   std::printf("}\n");
+  delete schur;
   delete X;
   delete res;
   delete ans;

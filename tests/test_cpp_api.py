@@ -32,7 +32,8 @@ def test_cpp_header_compiles():
 
 
 @pytest.mark.gpu
-def test_cpp_driver_matches_reference(tmp_path):
+@pytest.mark.parametrize("mode", ["gmres", "direct"])
+def test_cpp_driver_matches_reference(tmp_path, mode):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.fail("CUDA device required for -m gpu tests")
@@ -46,7 +47,8 @@ def test_cpp_driver_matches_reference(tmp_path):
                         f"-Wl,-rpath,{lib_dir}"],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    out = subprocess.run([exe] + (["direct"] if mode == "direct" else []),
+                         capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr
     d = json.loads(out.stdout)
     prob, ref = load_case("shell_c1")
