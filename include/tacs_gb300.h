@@ -176,13 +176,19 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
    when use_coords), supernodes and fronts analysed once on the host, then
    a level-by-level multifrontal block Cholesky of K with its boundary
    columns zeroed as well, so that x = A^-1 b for the assembled A with its
-   row boundary conditions.  FP64.  tg_direct_factor synchronises and
-   returns TG_ERR_PIVOT on a non-positive pivot.
-   stats: supernodes, tree levels, factor bytes, update-pool bytes, dense
-   flops, largest front (scalar rows). */
-int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out);
+   row boundary conditions.  precision TG_PREC_FP64, or TG_PREC_FP32 for a
+   factorisation in FP32 (from the FP64 matrix) applied by
+   tg_direct_solve_f32, e.g. as the preconditioner of an FP64 iteration.
+   tg_direct_factor synchronises and returns TG_ERR_PIVOT on a
+   non-positive pivot.
+   stats: supernodes, tree levels, factor bytes (FP64 storage), update-pool
+   bytes (FP64), dense flops, largest front (scalar rows), precision. */
+int tg_direct_create(tg_mat *A, int use_coords, int precision,
+                     tg_direct **out);
 int tg_direct_factor(tg_direct *d, void *stream);
 int tg_direct_solve(tg_direct *d, const double *b, double *x, void *stream);
+int tg_direct_solve_f32(tg_direct *d, const float *b, float *x,
+                        void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

@@ -197,7 +197,8 @@ class TACSSchurPc {
     if (levFill < 1000)
       throw TACSError("TACSSchurPc: only the complete factorisation "
                       "(levFill >= 1000) is on the GPU");
-    check(tg_direct_create(mat->handle(), 1, &d_), "TACSSchurPc");
+    check(tg_direct_create(mat->handle(), 1, TG_PREC_FP64, &d_),
+          "TACSSchurPc");
   }
   ~TACSSchurPc() { tg_direct_decref(d_); }
   TACSSchurPc(const TACSSchurPc &) = delete;

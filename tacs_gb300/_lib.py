@@ -50,9 +50,10 @@ SIGNATURES = [
     ("tg_add_dv_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),
     ("tg_add_adjoint_res_products", _I, [_P, _P, _D, _I, _P, _P, _P]),
     ("tg_add_total_derivative", _I, [_P, _P, _I, _D, _P, _D, _P, _P]),
-    ("tg_direct_create", _I, [_P, _I, _P]),
+    ("tg_direct_create", _I, [_P, _I, _I, _P]),
     ("tg_direct_factor", _I, [_P, _P]),
     ("tg_direct_solve", _I, [_P, _P, _P, _P]),
+    ("tg_direct_solve_f32", _I, [_P, _P, _P, _P]),
     ("tg_direct_get_stats", _I, [_P, _P]),
     ("tg_direct_decref", _I, [_P]),
     ("tg_add_xpt_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),

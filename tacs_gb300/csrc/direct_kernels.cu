@@ -19,68 +19,73 @@ int grid_1d(size_t n) {
 
 }  // namespace
 
+template <class T>
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
                                   int count, const double *A,
                                   cudaStream_t s) {
   if (count <= 0) return;
-  direct_zero_kernel<<<count, 256, 0, s>>>(v, sn, count);
-  direct_assemble_kernel<<<count, 256, 0, s>>>(v, sn, count, A);
-  direct_extend_add_kernel<<<count, 256, 0, s>>>(v, sn, count);
+  direct_zero_kernel<T><<<count, 256, 0, s>>>(v, sn, count);
+  direct_assemble_kernel<T><<<count, 256, 0, s>>>(v, sn, count, A);
+  direct_extend_add_kernel<T><<<count, 256, 0, s>>>(v, sn, count);
 }
 
+template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s) {
   if (count <= 0) return;
-  direct_factor_small_kernel<<<count, 256, 0, s>>>(v, sn, count, fail);
+  direct_factor_small_kernel<T><<<count, 256, 0, s>>>(v, sn, count, fail);
 }
 
+template <class T>
 void launch_direct_factor_large(const DirectView &v, int sn, int M, int C,
                                 int *fail, cudaStream_t s) {
   for (int k0 = 0; k0 < C; k0 += kPanel) {
     const int nb = C - k0 < kPanel ? C - k0 : kPanel;
-    direct_panel_kernel<<<1, 256, 0, s>>>(v, sn, k0, nb, fail);
+    direct_panel_kernel<T><<<1, 256, 0, s>>>(v, sn, k0, nb, fail);
     const int rest = M - (k0 + nb);
     if (rest > 0) {
       const int tiles = (rest + kTile - 1) / kTile;
-      direct_trailing_kernel<<<dim3(tiles, tiles), 256, 0, s>>>(v, sn, k0,
-                                                                 nb);
+      direct_trailing_kernel<T><<<dim3(tiles, tiles), 256, 0, s>>>(v, sn, k0,
+                                                                    nb);
     }
   }
 }
 
+template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
-                           int max_front, double *y, double *contrib,
-                           cudaStream_t s) {
+                           int max_front, T *y, T *contrib, cudaStream_t s) {
   if (count <= 0) return;
-  direct_forward_kernel<<<count, 256, sizeof(double) * max_front, s>>>(
+  direct_forward_kernel<T><<<count, 256, sizeof(T) * max_front, s>>>(
       v, sn, count, y, contrib);
 }
 
+template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
-                            int max_front, const double *y, double *x,
-                            cudaStream_t s) {
+                            int max_front, const T *y, T *x, cudaStream_t s) {
   if (count <= 0) return;
-  direct_backward_kernel<<<count, 256, sizeof(double) * max_front, s>>>(
+  direct_backward_kernel<T><<<count, 256, sizeof(T) * max_front, s>>>(
       v, sn, count, y, x);
 }
 
-void launch_direct_bc_mask(int n, int bs, const int *bcmask, const double *b,
-                           double *out, cudaStream_t s) {
-  direct_bc_mask_kernel<<<grid_1d((size_t)n * bs), 256, 0, s>>>(n, bs, bcmask,
-                                                                b, out);
+template <class T>
+void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
+                           T *out, cudaStream_t s) {
+  direct_bc_mask_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
+      n, bs, bcmask, b, out);
 }
 
-void launch_direct_rhs(int n, int bs, const int *perm, const double *b,
-                       const double *Kpb, const double *pb, double *ypos,
-                       cudaStream_t s) {
-  direct_rhs_kernel<<<grid_1d((size_t)n * bs), 256, 0, s>>>(n, bs, perm, b,
-                                                            Kpb, pb, ypos);
+template <class T>
+void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
+                       const T *Kpb, const T *pb, T *ypos, cudaStream_t s) {
+  direct_rhs_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
+      n, bs, perm, b, Kpb, pb, ypos);
 }
 
-void launch_direct_unpermute(int n, int bs, const int *perm,
-                             const double *xpos, double *x, cudaStream_t s) {
-  direct_unpermute_kernel<<<grid_1d((size_t)n * bs), 256, 0, s>>>(n, bs, perm,
-                                                                  xpos, x);
+template <class T>
+void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
+                             T *x, cudaStream_t s) {
+  direct_unpermute_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
+      n, bs, perm, xpos, x);
 }
 
 void direct_set_smem(int max_front) {
@@ -90,11 +95,39 @@ void direct_set_smem(int max_front) {
   const int bytes = (int)sizeof(double) * max_front;
   if (bytes > set) {
     set = bytes;
-    cudaFuncSetAttribute(direct_forward_kernel,
+    cudaFuncSetAttribute(direct_forward_kernel<double>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(direct_backward_kernel,
+    cudaFuncSetAttribute(direct_backward_kernel<double>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(direct_forward_kernel<float>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(direct_backward_kernel<float>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   }
 }
+
+#define TG_DIRECT_INSTANTIATE(T)                                            \
+  template void launch_direct_level_assemble<T>(const DirectView &,        \
+                                                const int *, int,          \
+                                                const double *, cudaStream_t); \
+  template void launch_direct_factor_small<T>(const DirectView &,          \
+                                              const int *, int, int *,     \
+                                              cudaStream_t);               \
+  template void launch_direct_factor_large<T>(const DirectView &, int, int,  \
+                                              int, int *, cudaStream_t);   \
+  template void launch_direct_forward<T>(const DirectView &, const int *,  \
+                                         int, int, T *, T *, cudaStream_t); \
+  template void launch_direct_backward<T>(const DirectView &, const int *, \
+                                          int, int, const T *, T *,        \
+                                          cudaStream_t);                   \
+  template void launch_direct_bc_mask<T>(int, int, const int *, const T *, \
+                                         T *, cudaStream_t);               \
+  template void launch_direct_rhs<T>(int, int, const int *, const T *,     \
+                                     const T *, const T *, T *,            \
+                                     cudaStream_t);                        \
+  template void launch_direct_unpermute<T>(int, int, const int *,          \
+                                           const T *, T *, cudaStream_t);
+TG_DIRECT_INSTANTIATE(double)
+TG_DIRECT_INSTANTIATE(float)
 
 }  // namespace tg

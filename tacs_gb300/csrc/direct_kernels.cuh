@@ -27,7 +27,9 @@
 #ifdef DK_EMULATE
 #define DK_DYN_SMEM(T, name) T *name = reinterpret_cast<T *>(dk_dyn_smem())
 #else
-#define DK_DYN_SMEM(T, name) extern __shared__ T name[]
+#define DK_DYN_SMEM(T, name)                                   \
+  extern __shared__ __align__(16) unsigned char dk_smem_raw[]; \
+  T *name = reinterpret_cast<T *>(dk_smem_raw)
 #endif
 
 namespace tg {
@@ -35,36 +37,54 @@ namespace dk {
 namespace {
 
 #ifndef DK_EMULATE
-__device__ __forceinline__ bool dk_isfinite(double x) { return isfinite(x); }
-__device__ __forceinline__ double dk_sqrt(double x) { return sqrt(x); }
+template <class T>
+__device__ __forceinline__ bool dk_isfinite(T x) { return isfinite(x); }
+template <class T>
+__device__ __forceinline__ T dk_sqrt(T x) { return sqrt(x); }
 #endif
 
 
+// T = double for the FP64 factorisation, float for the FP32 one (whose
+// storage is lstore32 / pool32)
+template <class T>
 struct Front {
-  double *lp;  // M x C row-major panel
-  double *up;  // (M - C) x (M - C) row-major update, or nullptr
+  T *lp;  // M x C row-major panel
+  T *up;  // (M - C) x (M - C) row-major update, or nullptr
   int M, C;
-  __device__ __forceinline__ double &at(int i, int j) const {  // i >= j
+  __device__ __forceinline__ T &at(int i, int j) const {  // i >= j
     return j < C ? lp[(size_t)i * C + j]
                  : up[(size_t)(i - C) * (M - C) + (j - C)];
   }
 };
 
-__device__ __forceinline__ Front front_of(const DirectView &v, int s) {
-  Front f;
+__device__ __forceinline__ double *dk_store(const DirectView &v, bool pool,
+                                            double *) {
+  return pool ? v.pool : v.lstore;
+}
+__device__ __forceinline__ float *dk_store(const DirectView &v, bool pool,
+                                           float *) {
+  return pool ? v.pool32 : v.lstore32;
+}
+
+template <class T>
+__device__ __forceinline__ Front<T> front_of(const DirectView &v, int s) {
+  Front<T> f;
   const int bs = v.bs;
   f.M = (v.sn_rowptr[s + 1] - v.sn_rowptr[s]) * bs;
   f.C = (v.sn_col[s + 1] - v.sn_col[s]) * bs;
-  f.lp = v.lstore + (size_t)v.l_off[s] * bs * bs;
-  f.up = v.u_off[s] >= 0 ? v.pool + (size_t)v.u_off[s] * bs * bs : nullptr;
+  f.lp = dk_store(v, false, (T *)nullptr) + (size_t)v.l_off[s] * bs * bs;
+  f.up = v.u_off[s] >= 0
+             ? dk_store(v, true, (T *)nullptr) + (size_t)v.u_off[s] * bs * bs
+             : nullptr;
   return f;
 }
 
 // zero the fronts of the level's supernodes (one CTA each)
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_zero_kernel(DirectView v, const int *__restrict__ sn, int count) {
   if ((int)blockIdx.x >= count) return;
-  const Front f = front_of(v, sn[blockIdx.x]);
+  const Front<T> f = front_of<T>(v, sn[blockIdx.x]);
   const size_t npan = (size_t)f.M * f.C;
   for (size_t k = threadIdx.x; k < npan; k += blockDim.x) f.lp[k] = 0.0;
   if (f.up) {
@@ -75,12 +95,13 @@ __global__ void __launch_bounds__(256)
 
 // the matrix's lower blocks into the fronts; entries in a boundary row or
 // column are 0 except the boundary dof's own diagonal (1)
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_assemble_kernel(DirectView v, const int *__restrict__ sn,
                            int count, const double *__restrict__ A) {
   if ((int)blockIdx.x >= count) return;
   const int s = sn[blockIdx.x];
-  const Front f = front_of(v, s);
+  const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs, b2 = bs * bs;
   const int k0 = v.asm_ptr[s], k1 = v.asm_ptr[s + 1];
   const size_t total = (size_t)(k1 - k0) * b2;
@@ -92,24 +113,25 @@ __global__ void __launch_bounds__(256)
     const int rnode = v.perm[v.sn_rows[v.sn_rowptr[s] + v.asm_row[k]]];
     const int cnode = v.perm[v.sn_col[s] + v.asm_col[k]];
     const bool bc = ((v.bcmask[rnode] >> r) & 1) || ((v.bcmask[cnode] >> q) & 1);
-    double val = A[(size_t)v.asm_blk[k] * b2 + e];
-    if (bc) val = (rnode == cnode && r == q) ? 1.0 : 0.0;
+    T val = (T)A[(size_t)v.asm_blk[k] * b2 + e];
+    if (bc) val = (rnode == cnode && r == q) ? T(1) : T(0);
     f.at(ir, jc) = val;
   }
 }
 
 // the children's update matrices into each parent front (one CTA per
 // parent, children one after another)
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_extend_add_kernel(DirectView v, const int *__restrict__ sn,
                              int count) {
   if ((int)blockIdx.x >= count) return;
   const int s = sn[blockIdx.x];
-  const Front f = front_of(v, s);
+  const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
     const int c = v.ch_list[k];
-    const Front fc = front_of(v, c);
+    const Front<T> fc = front_of<T>(v, c);
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
     const size_t total = (size_t)um * um;
@@ -126,16 +148,17 @@ __global__ void __launch_bounds__(256)
 
 // partial Cholesky of whole small fronts, one CTA each (right-looking in
 // place); fail = first failing supernode + 1
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_factor_small_kernel(DirectView v, const int *__restrict__ sn,
                                int count, int *fail) {
   if ((int)blockIdx.x >= count) return;
   const int s = sn[blockIdx.x];
-  const Front f = front_of(v, s);
-  __shared__ double piv;
+  const Front<T> f = front_of<T>(v, s);
+  __shared__ T piv;
   for (int k = 0; k < f.C; k++) {
     if (threadIdx.x == 0) {
-      const double d = f.at(k, k);
+      const T d = f.at(k, k);
       if (!(d > 0.0) || !dk_isfinite(d)) {
         atomicCAS(fail, 0, s + 1);
         piv = 1.0;
@@ -145,7 +168,7 @@ __global__ void __launch_bounds__(256)
       f.at(k, k) = piv;
     }
     __syncthreads();
-    const double inv = 1.0 / piv;
+    const T inv = T(1) / piv;
     for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
       f.at(i, k) *= inv;
     __syncthreads();
@@ -164,13 +187,14 @@ __global__ void __launch_bounds__(256)
 // Large fronts.  Panel step: columns [k0, k0 + nb) of one front, all rows
 // from k0, factored by one CTA with the panel's own columns updated
 // left-looking inside the panel.
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_panel_kernel(DirectView v, int s, int k0, int nb, int *fail) {
-  const Front f = front_of(v, s);
-  __shared__ double piv;
+  const Front<T> f = front_of<T>(v, s);
+  __shared__ T piv;
   for (int k = k0; k < k0 + nb; k++) {
     if (threadIdx.x == 0) {
-      const double d = f.at(k, k);
+      const T d = f.at(k, k);
       if (!(d > 0.0) || !dk_isfinite(d)) {
         atomicCAS(fail, 0, s + 1);
         piv = 1.0;
@@ -180,7 +204,7 @@ __global__ void __launch_bounds__(256)
       f.at(k, k) = piv;
     }
     __syncthreads();
-    const double inv = 1.0 / piv;
+    const T inv = T(1) / piv;
     for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
       f.at(i, k) *= inv;
     __syncthreads();
@@ -203,15 +227,16 @@ __global__ void __launch_bounds__(256)
 // panel's columns q, for k1 <= j <= i < M, in 32 x 32 tiles (blockIdx.x =
 // tile column, blockIdx.y = tile row; tiles above the diagonal exit).
 constexpr int kTile = 32, kPanel = 32;
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_trailing_kernel(DirectView v, int s, int k0, int nb) {
-  const Front f = front_of(v, s);
+  const Front<T> f = front_of<T>(v, s);
   const int k1 = k0 + nb;
   const int tj = blockIdx.x, ti = blockIdx.y;
   if (tj > ti) return;
   const int i0 = k1 + ti * kTile, j0 = k1 + tj * kTile;
   if (i0 >= f.M || j0 >= f.M) return;
-  __shared__ double Ai[kTile][kPanel + 1], Aj[kTile][kPanel + 1];
+  __shared__ T Ai[kTile][kPanel + 1], Aj[kTile][kPanel + 1];
   for (int t = threadIdx.x; t < kTile * nb; t += blockDim.x) {
     const int r = t / nb, q = t % nb;
     Ai[r][q] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : 0.0;
@@ -222,7 +247,7 @@ __global__ void __launch_bounds__(256)
     const int r = t / kTile, c = t % kTile;
     const int i = i0 + r, j = j0 + c;
     if (i >= f.M || j >= f.M || j > i) continue;
-    double acc = 0.0;
+    T acc = 0;
     for (int q = 0; q < nb; q++) acc += Ai[r][q] * Aj[c][q];
     f.at(i, j) -= acc;
   }
@@ -232,13 +257,14 @@ __global__ void __launch_bounds__(256)
 // Forward: z = front rows of the supernode (own rows from y, the rows
 // below zero), plus the children's contribution vectors; L11 z1 = z1 and
 // z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
-                          double *y, double *contrib) {
+                          T *y, T *contrib) {
   if ((int)blockIdx.x >= count) return;
-  DK_DYN_SMEM(double, z);
+  DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
-  const Front f = front_of(v, s);
+  const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   for (int t = threadIdx.x; t < f.M; t += blockDim.x)
@@ -246,10 +272,10 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
     const int c = v.ch_list[k];
-    const Front fc = front_of(v, c);
+    const Front<T> fc = front_of<T>(v, c);
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
-    const double *w = contrib + v.v_off[c];
+    const T *w = contrib + v.v_off[c];
     for (int t = threadIdx.x; t < um; t += blockDim.x)
       z[rel[t / bs] * bs + t % bs] += w[t];
     __syncthreads();
@@ -257,7 +283,7 @@ __global__ void __launch_bounds__(256)
   for (int k = 0; k < f.C; k++) {
     if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
     __syncthreads();
-    const double zk = z[k];
+    const T zk = z[k];
     for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
       z[i] -= f.lp[(size_t)i * f.C + k] * zk;
     __syncthreads();
@@ -265,20 +291,21 @@ __global__ void __launch_bounds__(256)
   for (int t = threadIdx.x; t < f.C; t += blockDim.x)
     y[(size_t)rows[t / bs] * bs + t % bs] = z[t];
   if (v.sn_parent[s] >= 0) {
-    double *w = contrib + v.v_off[s];
+    T *w = contrib + v.v_off[s];
     for (int t = f.C + threadIdx.x; t < f.M; t += blockDim.x) w[t - f.C] = z[t];
   }
 }
 
 // Backward: z1 = y1 - L21^T x2 (x2 from the ancestors, already final),
 // then L11^T z1 = z1; own rows to x.
+template <class T>
 __global__ void __launch_bounds__(256)
     direct_backward_kernel(DirectView v, const int *__restrict__ sn,
-                           int count, const double *y, double *x) {
+                           int count, const T *y, T *x) {
   if ((int)blockIdx.x >= count) return;
-  DK_DYN_SMEM(double, z);
+  DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
-  const Front f = front_of(v, s);
+  const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   for (int t = threadIdx.x; t < f.M; t += blockDim.x) {
@@ -287,7 +314,7 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   for (int j = threadIdx.x; j < f.C; j += blockDim.x) {
-    double acc = 0.0;
+    T acc = 0;
     for (int i = f.C; i < f.M; i++) acc += f.lp[(size_t)i * f.C + j] * z[i];
     z[j] -= acc;
   }
@@ -295,7 +322,7 @@ __global__ void __launch_bounds__(256)
   for (int k = f.C - 1; k >= 0; k--) {
     if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
     __syncthreads();
-    const double zk = z[k];
+    const T zk = z[k];
     for (int j = threadIdx.x; j < k; j += blockDim.x)
       z[j] -= f.lp[(size_t)k * f.C + j] * zk;
     __syncthreads();
@@ -307,18 +334,20 @@ __global__ void __launch_bounds__(256)
 // b' = b - K P b + P b (P keeps the boundary dofs) is formed as
 // tmp = P b, then K tmp by the mat-vec, then this kernel; and the
 // permutations into and out of the factor's order
+template <class T>
 __global__ void direct_bc_mask_kernel(int n, int bs, const int *bcmask,
-                                      const double *b, double *out) {
+                                      const T *b, T *out) {
   const size_t N = (size_t)n * bs;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
        t += (size_t)gridDim.x * blockDim.x) {
     const int node = (int)(t / bs), r = (int)(t % bs);
-    out[t] = ((bcmask[node] >> r) & 1) ? b[t] : 0.0;
+    out[t] = ((bcmask[node] >> r) & 1) ? b[t] : T(0);
   }
 }
+template <class T>
 __global__ void direct_rhs_kernel(int n, int bs, const int *perm,
-                                  const double *b, const double *Kpb,
-                                  const double *pb, double *ypos) {
+                                  const T *b, const T *Kpb, const T *pb,
+                                  T *ypos) {
   const size_t N = (size_t)n * bs;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
        t += (size_t)gridDim.x * blockDim.x) {
@@ -327,8 +356,9 @@ __global__ void direct_rhs_kernel(int n, int bs, const int *perm,
     ypos[t] = b[g] - Kpb[g] + pb[g];
   }
 }
+template <class T>
 __global__ void direct_unpermute_kernel(int n, int bs, const int *perm,
-                                        const double *xpos, double *x) {
+                                        const T *xpos, T *x) {
   const size_t N = (size_t)n * bs;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
        t += (size_t)gridDim.x * blockDim.x) {

@@ -14,7 +14,8 @@ struct DirectView {
   const int *ea_ptr, *ea_rel, *asm_ptr, *asm_blk, *asm_row, *asm_col;
   const int *ch_ptr, *ch_list;
   const int64_t *l_off, *u_off, *v_off;
-  double *lstore, *pool;
+  double *lstore, *pool;     // FP64 factor panels and update pool
+  float *lstore32, *pool32;  // the same storage for an FP32 factorisation
 };
 
 }  // namespace tg

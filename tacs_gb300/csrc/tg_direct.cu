@@ -17,10 +17,22 @@
 // fronts of at most this many scalar rows are factored by one CTA each
 static constexpr int kSmallFront = 256;
 
+static void bcsr_mult_t(const tg_mat *A, const double *a, const double *x,
+                        double *y, cudaStream_t s) {
+  tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols, a, x,
+                       y, s);
+}
+static void bcsr_mult_t(const tg_mat *A, const float *a, const float *x,
+                        float *y, cudaStream_t s) {
+  tg::launch_bcsr_mult_f32(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols, a,
+                           x, y, s);
+}
+
 struct tg_direct {
   int refcount = 1;
   tg_mat *A = nullptr;
   int n = 0, bs = 0, ns = 0, max_front = 0;
+  int precision = TG_PREC_FP64;
   tg::direct::Analysis an;
   std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
   // per level: its small fronts (one launch, d_small) and its large ones
@@ -36,6 +48,11 @@ struct tg_direct {
   double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
   double *d_ypos = nullptr, *d_xpos = nullptr, *d_pb = nullptr,
          *d_kpb = nullptr;
+  // FP32 factorisation: its storage, solve vectors and the matrix in FP32
+  float *d_lstore32 = nullptr, *d_pool32 = nullptr, *d_contrib32 = nullptr;
+  float *d_ypos32 = nullptr, *d_xpos32 = nullptr, *d_pb32 = nullptr,
+        *d_kpb32 = nullptr, *d_a32 = nullptr;
+  int64_t contrib_len = 0;
   int *d_fail = nullptr;
   bool factored = false;
   tg::DirectView view() const {
@@ -60,6 +77,8 @@ struct tg_direct {
     v.v_off = d_v_off;
     v.lstore = d_lstore;
     v.pool = d_pool;
+    v.lstore32 = d_lstore32;
+    v.pool32 = d_pool32;
     return v;
   }
   ~tg_direct() {
@@ -70,15 +89,20 @@ struct tg_direct {
     dfree(d_ch_ptr); dfree(d_ch_list); dfree(d_level_sn); dfree(d_l_off);
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
-    dfree(d_kpb); dfree(d_fail); dfree(d_small);
+    dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
+    dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
+    dfree(d_pb32); dfree(d_kpb32); dfree(d_a32);
   }
 };
 
 extern "C" {
 
-int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out) {
+int tg_direct_create(tg_mat *A, int use_coords, int precision,
+                     tg_direct **out) {
   if (!A || !out) return fail(TG_ERR_ARG, "tg_direct_create: NULL argument");
   *out = nullptr;
+  if (precision != TG_PREC_FP64 && precision != TG_PREC_FP32)
+    return fail(TG_ERR_ARG, "tg_direct_create: bad precision");
   tg_assembler *a = A->a;
   if (!a || !a->initialized)
     return fail(TG_ERR_STATE, "tg_direct_create: assembler not initialised");
@@ -87,6 +111,7 @@ int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out) {
   A->refcount++;
   d->n = A->nrows;
   d->bs = A->bsize;
+  d->precision = precision;
   std::vector<double> xyz;
   if (use_coords) {
     xyz.resize((size_t)3 * a->nnodes);
@@ -161,9 +186,21 @@ int tg_direct_create(tg_mat *A, int use_coords, tg_direct **out) {
   if (!rc) rc = upload(&d->d_l_off, an.l_off);
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
-  if (!rc) rc = dalloc(&d->d_lstore, (size_t)an.l_total * b2);
-  if (!rc) rc = dalloc(&d->d_pool, (size_t)an.u_peak * b2);
-  if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc);
+  d->contrib_len = vacc;
+  if (precision == TG_PREC_FP64) {
+    if (!rc) rc = dalloc(&d->d_lstore, (size_t)an.l_total * b2);
+    if (!rc) rc = dalloc(&d->d_pool, (size_t)an.u_peak * b2);
+    if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc);
+  } else {
+    if (!rc) rc = dalloc(&d->d_lstore32, (size_t)an.l_total * b2);
+    if (!rc) rc = dalloc(&d->d_pool32, (size_t)an.u_peak * b2);
+    if (!rc) rc = dalloc(&d->d_contrib32, (size_t)vacc);
+    if (!rc) rc = dalloc(&d->d_ypos32, N);
+    if (!rc) rc = dalloc(&d->d_xpos32, N);
+    if (!rc) rc = dalloc(&d->d_pb32, N);
+    if (!rc) rc = dalloc(&d->d_kpb32, N);
+    if (!rc) rc = dalloc(&d->d_a32, (size_t)A->nnz * b2);
+  }
   if (!rc) rc = dalloc(&d->d_ypos, N);
   if (!rc) rc = dalloc(&d->d_xpos, N);
   if (!rc) rc = dalloc(&d->d_pb, N);
@@ -190,23 +227,64 @@ int tg_direct_decref(tg_direct *d) {
   return 0;
 }
 
-int tg_direct_factor(tg_direct *d, void *s) {
-  if (!d) return fail(TG_ERR_ARG, "tg_direct_factor: NULL");
+}  // extern "C"
+
+template <class T>
+static void factor_levels(tg_direct *d, cudaStream_t s) {
   const tg::DirectView v = d->view();
-  TG_CUDA(cudaMemsetAsync(d->d_fail, 0, sizeof(int), S(s)));
   for (size_t L = 0; L + 1 < d->level_ptr_h.size(); L++) {
     const int b = d->level_ptr_h[L], e = d->level_ptr_h[L + 1];
-    tg::launch_direct_level_assemble(v, d->d_level_sn + b, e - b,
-                                     d->A->d_vals, S(s));
+    tg::launch_direct_level_assemble<T>(v, d->d_level_sn + b, e - b,
+                                        d->A->d_vals, s);
     // the level's small fronts in one launch, its large ones by panels
     const int sb = d->small_ptr_h[L], se = d->small_ptr_h[L + 1];
-    tg::launch_direct_factor_small(v, d->d_small + sb, se - sb, d->d_fail,
-                                   S(s));
+    tg::launch_direct_factor_small<T>(v, d->d_small + sb, se - sb, d->d_fail,
+                                      s);
     for (int t = d->large_ptr_h[L]; t < d->large_ptr_h[L + 1]; t++) {
       const int sn = d->large_h[t];
-      tg::launch_direct_factor_large(v, sn, d->front_m_h[sn],
-                                     d->front_c_h[sn], d->d_fail, S(s));
+      tg::launch_direct_factor_large<T>(v, sn, d->front_m_h[sn],
+                                        d->front_c_h[sn], d->d_fail, s);
     }
+  }
+}
+
+// x = A^-1 b in T: b' = b - K P b + P b, into the factor's order, the
+// level sweeps, back to the node order (K a: the matrix values in T)
+template <class T>
+static void solve_levels(tg_direct *d, const T *b, T *x, const T *a, T *pb,
+                         T *kpb, T *ypos, T *xpos, T *contrib,
+                         cudaStream_t s) {
+  const tg::DirectView v = d->view();
+  tg_mat *A = d->A;
+  tg::launch_direct_bc_mask<T>(d->n, d->bs, d->d_bcmask, b, pb, s);
+  bcsr_mult_t(A, a, pb, kpb, s);
+  tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, b, kpb, pb, ypos, s);
+  const int nl = (int)d->level_ptr_h.size() - 1;
+  for (int L = 0; L < nl; L++) {
+    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
+    tg::launch_direct_forward<T>(v, d->d_level_sn + lb, le - lb,
+                                 d->max_front, ypos, contrib, s);
+  }
+  for (int L = nl - 1; L >= 0; L--) {
+    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
+    tg::launch_direct_backward<T>(v, d->d_level_sn + lb, le - lb,
+                                  d->max_front, ypos, xpos, s);
+  }
+  tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, x, s);
+}
+
+extern "C" {
+
+int tg_direct_factor(tg_direct *d, void *s) {
+  if (!d) return fail(TG_ERR_ARG, "tg_direct_factor: NULL");
+  TG_CUDA(cudaMemsetAsync(d->d_fail, 0, sizeof(int), S(s)));
+  if (d->precision == TG_PREC_FP64) {
+    factor_levels<double>(d, S(s));
+  } else {
+    const tg_mat *A = d->A;
+    tg::launch_d2f(A->d_vals, d->d_a32,
+                   (size_t)A->nnz * A->bsize * A->bsize, S(s));
+    factor_levels<float>(d, S(s));
   }
   int hfail = 0;
   TG_CUDA(cudaMemcpyAsync(&hfail, d->d_fail, sizeof(int),
@@ -226,25 +304,23 @@ int tg_direct_factor(tg_direct *d, void *s) {
 int tg_direct_solve(tg_direct *d, const double *b, double *x, void *s) {
   if (!d || !b || !x) return fail(TG_ERR_ARG, "tg_direct_solve: NULL");
   if (!d->factored) return fail(TG_ERR_STATE, "tg_direct_solve: not factored");
-  const tg::DirectView v = d->view();
-  tg_mat *A = d->A;
-  tg::launch_direct_bc_mask(d->n, d->bs, d->d_bcmask, b, d->d_pb, S(s));
-  tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
-                       A->d_vals, d->d_pb, d->d_kpb, S(s));
-  tg::launch_direct_rhs(d->n, d->bs, d->d_perm, b, d->d_kpb, d->d_pb,
-                        d->d_ypos, S(s));
-  const int nl = (int)d->level_ptr_h.size() - 1;
-  for (int L = 0; L < nl; L++) {
-    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
-    tg::launch_direct_forward(v, d->d_level_sn + lb, le - lb, d->max_front,
-                              d->d_ypos, d->d_contrib, S(s));
-  }
-  for (int L = nl - 1; L >= 0; L--) {
-    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
-    tg::launch_direct_backward(v, d->d_level_sn + lb, le - lb, d->max_front,
-                               d->d_ypos, d->d_xpos, S(s));
-  }
-  tg::launch_direct_unpermute(d->n, d->bs, d->d_perm, d->d_xpos, x, S(s));
+  if (d->precision != TG_PREC_FP64)
+    return fail(TG_ERR_ARG, "tg_direct_solve: FP32 factorisation "
+                            "(use tg_direct_solve_f32)");
+  solve_levels<double>(d, b, x, d->A->d_vals, d->d_pb, d->d_kpb, d->d_ypos,
+                       d->d_xpos, d->d_contrib, S(s));
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_direct_solve_f32(tg_direct *d, const float *b, float *x, void *s) {
+  if (!d || !b || !x) return fail(TG_ERR_ARG, "tg_direct_solve_f32: NULL");
+  if (!d->factored)
+    return fail(TG_ERR_STATE, "tg_direct_solve_f32: not factored");
+  if (d->precision != TG_PREC_FP32)
+    return fail(TG_ERR_ARG, "tg_direct_solve_f32: FP64 factorisation");
+  solve_levels<float>(d, b, x, d->d_a32, d->d_pb32, d->d_kpb32,
+                      d->d_ypos32, d->d_xpos32, d->d_contrib32, S(s));
   TG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -258,6 +334,7 @@ int tg_direct_get_stats(tg_direct *d, double *stats) {
   stats[3] = (double)d->an.u_peak * b2 * sizeof(double);
   stats[4] = (double)d->an.flops_scalar(d->bs);
   stats[5] = d->max_front;
+  stats[6] = d->precision;
   return 0;
 }
 

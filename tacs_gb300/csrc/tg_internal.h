@@ -286,25 +286,31 @@ void launch_kr_arnoldi(const KrylovState &st, cudaStream_t s);
 void launch_kr_solve_y(const KrylovState &st, cudaStream_t s);
 
 // ------------------------------------------------ direct factorisation
+// multifrontal factorisation (direct_kernels.cu), T = double or float
+template <class T>
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
                                   int count, const double *A, cudaStream_t s);
+template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s);
+template <class T>
 void launch_direct_factor_large(const DirectView &v, int sn, int M, int C,
                                 int *fail, cudaStream_t s);
+template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
-                           int max_front, double *y, double *contrib,
-                           cudaStream_t s);
+                           int max_front, T *y, T *contrib, cudaStream_t s);
+template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
-                            int max_front, const double *y, double *x,
-                            cudaStream_t s);
-void launch_direct_bc_mask(int n, int bs, const int *bcmask, const double *b,
-                           double *out, cudaStream_t s);
-void launch_direct_rhs(int n, int bs, const int *perm, const double *b,
-                       const double *Kpb, const double *pb, double *ypos,
-                       cudaStream_t s);
-void launch_direct_unpermute(int n, int bs, const int *perm,
-                             const double *xpos, double *x, cudaStream_t s);
+                            int max_front, const T *y, T *x, cudaStream_t s);
+template <class T>
+void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
+                           T *out, cudaStream_t s);
+template <class T>
+void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
+                       const T *Kpb, const T *pb, T *ypos, cudaStream_t s);
+template <class T>
+void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
+                             T *x, cudaStream_t s);
 void direct_set_smem(int max_front);
 
 // error reporting

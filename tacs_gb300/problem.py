@@ -128,20 +128,25 @@ class Direct:
     coordinates; solve(b) returns A^-1 b for the assembled A with its row
     boundary conditions."""
 
-    def __init__(self, mat, use_coords=True):
+    def __init__(self, mat, use_coords=True, precision=_lib.PREC_FP64):
         h = C.c_void_p()
         check(_lib.lib().tg_direct_create(mat.handle, int(use_coords),
-                                          C.byref(h)), "tg_direct_create")
-        self.handle, self.mat = h, mat
+                                          int(precision), C.byref(h)),
+              "tg_direct_create")
+        self.handle, self.mat, self.precision = h, mat, precision
 
     def factor(self):
         check(_lib.lib().tg_direct_factor(self.handle, _stream()),
               "tg_direct_factor")
 
     def solve(self, b, x=None):
+        """x = A^-1 b; FP64 vectors for an FP64 factorisation, FP32 ones
+        for an FP32 factorisation."""
         x = torch.empty_like(b) if x is None else x
-        check(_lib.lib().tg_direct_solve(self.handle, _p(b), _p(x),
-                                         _stream()), "tg_direct_solve")
+        fn = (_lib.lib().tg_direct_solve_f32
+              if self.precision == _lib.PREC_FP32
+              else _lib.lib().tg_direct_solve)
+        check(fn(self.handle, _p(b), _p(x), _stream()), "tg_direct_solve")
         return x
 
     def stats(self):

@@ -33,8 +33,10 @@ static inline int atomicCAS(int *a, int cmp, int val) {
 namespace tg {
 namespace dk {
 namespace {
-inline bool dk_isfinite(double x) { return std::isfinite(x); }
-inline double dk_sqrt(double x) { return std::sqrt(x); }
+template <class T>
+inline bool dk_isfinite(T x) { return std::isfinite(x); }
+template <class T>
+inline T dk_sqrt(T x) { return std::sqrt(x); }
 }  // namespace
 }  // namespace dk
 }  // namespace tg
@@ -56,15 +58,25 @@ static void launch(K kernel, unsigned gx, unsigned gy, size_t smem_doubles,
     }
 }
 
-extern "C" {
+static void set_store(tg::DirectView &v, double *l, double *p) {
+  v.lstore = l;
+  v.pool = p;
+}
+static void set_store(tg::DirectView &v, float *l, float *p) {
+  v.lstore32 = l;
+  v.pool32 = p;
+}
 
 // x = A^-1 b for the assembled BCSR matrix A with row boundary conditions
-// (bcmask per node), by the GPU kernels run on the CPU.  small_max: fronts
-// of at most this many scalar rows take the one-CTA kernel, larger ones the
-// panel path.  Returns 0, or the failing supernode + 1.
-int de_solve(int n, int bs, const int *rowp, const int *cols,
-             const double *vals, const int *bcmask_in, const double *xyz,
-             int small_max, const double *b, double *x) {
+// (bcmask per node), by the GPU kernels run on the CPU in T (double: the
+// FP64 factorisation; float: the FP32 one, b and x converted).  small_max:
+// fronts of at most this many scalar rows take the one-CTA kernel, larger
+// ones the panel path.  Returns 0, or the failing supernode + 1.
+template <class T>
+static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
+                      const double *vals, const int *bcmask_in,
+                      const double *xyz, int small_max, const double *b_in,
+                      double *x_out) {
   std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
   std::vector<int> perm = tg::direct::nested_dissection(rp, cs, 64, xyz);
   tg::direct::Analysis an = tg::direct::analyse(rp, cs, perm);
@@ -89,9 +101,11 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
       if (an.sn_parent[s] >= 0) ch_list[fill[an.sn_parent[s]]++] = s;
   }
   std::vector<int> bcmask(bcmask_in, bcmask_in + n);
-  std::vector<double> lstore((size_t)an.l_total * b2),
+  std::vector<T> lstore((size_t)an.l_total * b2),
       pool((size_t)an.u_peak * b2 + 1), contrib(vacc + 1), ypos(N), xpos(N),
-      pb(N), kpb(N);
+      pb(N), kpb(N), bt(b_in, b_in + N), xt(N), vt(vals, vals + rowp[n] * b2);
+  const T *b = bt.data();
+  T *x = xt.data();
   int failflag = 0;
   tg::DirectView v;
   v.bs = bs;
@@ -112,8 +126,9 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
   v.l_off = an.l_off.data();
   v.u_off = an.u_off.data();
   v.v_off = v_off.data();
-  v.lstore = lstore.data();
-  v.pool = pool.data();
+  v.lstore = v.pool = nullptr;
+  v.lstore32 = v.pool32 = nullptr;
+  set_store(v, lstore.data(), pool.data());
 
   // factor: the sequence of tg_direct_factor (small fronts of a level in
   // one launch, large ones panel by panel)
@@ -131,22 +146,22 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
     const int *lv = an.level_sn.data() + lb;
     const int cnt = le - lb;
-    launch(direct_zero_kernel, cnt, 1, 0, v, lv, cnt);
-    launch(direct_assemble_kernel, cnt, 1, 0, v, lv, cnt, vals);
-    launch(direct_extend_add_kernel, cnt, 1, 0, v, lv, cnt);
+    launch(direct_zero_kernel<T>, cnt, 1, 0, v, lv, cnt);
+    launch(direct_assemble_kernel<T>, cnt, 1, 0, v, lv, cnt, vals);
+    launch(direct_extend_add_kernel<T>, cnt, 1, 0, v, lv, cnt);
     const int sb = small_ptr[L], se = small_ptr[L + 1];
     if (se > sb)
-      launch(direct_factor_small_kernel, se - sb, 1, 0, v,
+      launch(direct_factor_small_kernel<T>, se - sb, 1, 0, v,
              (const int *)small_h.data() + sb, se - sb, &failflag);
     for (int t = large_ptr[L]; t < large_ptr[L + 1]; t++) {
       const int sn = large_h[t];
       for (int k0 = 0; k0 < fc[sn]; k0 += kPanel) {
         const int nb = std::min(kPanel, fc[sn] - k0);
-        launch(direct_panel_kernel, 1, 1, 0, v, sn, k0, nb, &failflag);
+        launch(direct_panel_kernel<T>, 1, 1, 0, v, sn, k0, nb, &failflag);
         const int rest = fm[sn] - (k0 + nb);
         if (rest > 0) {
           const unsigned tiles = (rest + kTile - 1) / kTile;
-          launch(direct_trailing_kernel, tiles, tiles, 0, v, sn, k0, nb);
+          launch(direct_trailing_kernel<T>, tiles, tiles, 0, v, sn, k0, nb);
         }
       }
     }
@@ -154,34 +169,48 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
   if (failflag) return failflag;
 
   // solve: the sequence of tg_direct_solve
-  launch(direct_bc_mask_kernel, 1, 1, 0, n, bs, (const int *)bcmask.data(), b,
-         pb.data());
-  for (int i = 0; i < n; i++)  // the BCSR mat-vec
+  launch(direct_bc_mask_kernel<T>, 1, 1, 0, n, bs,
+         (const int *)bcmask.data(), b, pb.data());
+  for (int i = 0; i < n; i++)  // the BCSR mat-vec, in T
     for (int r = 0; r < bs; r++) {
-      double acc = 0.0;
+      T acc = 0;
       for (int j = rowp[i]; j < rowp[i + 1]; j++)
         for (int q = 0; q < bs; q++)
-          acc += vals[b2 * j + r * bs + q] * pb[(size_t)cols[j] * bs + q];
+          acc += vt[b2 * j + r * bs + q] * pb[(size_t)cols[j] * bs + q];
       kpb[(size_t)i * bs + r] = acc;
     }
-  launch(direct_rhs_kernel, 1, 1, 0, n, bs, (const int *)an.perm.data(), b,
-         (const double *)kpb.data(), (const double *)pb.data(), ypos.data());
+  launch(direct_rhs_kernel<T>, 1, 1, 0, n, bs, (const int *)an.perm.data(), b,
+         (const T *)kpb.data(), (const T *)pb.data(), ypos.data());
   const int nl = (int)an.level_ptr.size() - 1;
   for (int L = 0; L < nl; L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_forward_kernel, le - lb, 1, max_front, v,
+    launch(direct_forward_kernel<T>, le - lb, 1, max_front, v,
            (const int *)an.level_sn.data() + lb, le - lb, ypos.data(),
            contrib.data());
   }
   for (int L = nl - 1; L >= 0; L--) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_backward_kernel, le - lb, 1, max_front, v,
+    launch(direct_backward_kernel<T>, le - lb, 1, max_front, v,
            (const int *)an.level_sn.data() + lb, le - lb,
-           (const double *)ypos.data(), xpos.data());
+           (const T *)ypos.data(), xpos.data());
   }
-  launch(direct_unpermute_kernel, 1, 1, 0, n, bs, (const int *)an.perm.data(),
-         (const double *)xpos.data(), x);
+  launch(direct_unpermute_kernel<T>, 1, 1, 0, n, bs,
+         (const int *)an.perm.data(), (const T *)xpos.data(), x);
+  for (size_t k = 0; k < N; k++) x_out[k] = (double)x[k];
   return 0;
+}
+
+extern "C" {
+
+// precision: 0 FP64, 1 FP32
+int de_solve(int n, int bs, const int *rowp, const int *cols,
+             const double *vals, const int *bcmask, const double *xyz,
+             int small_max, int precision, const double *b, double *x) {
+  if (precision == 1)
+    return de_solve_t<float>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
+                             b, x);
+  return de_solve_t<double>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
+                            b, x);
 }
 
 }  // extern "C"

@@ -160,7 +160,8 @@ def de(tmp_path_factory):
                     EMUL, "-o", out], check=True)
     lib = C.CDLL(out)
     P = C.c_void_p
-    lib.de_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int, P, P]
+    lib.de_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int,
+                             C.c_int, P, P]
     return lib
 
 
@@ -188,7 +189,7 @@ def test_gpu_kernels_on_cpu_solve_assembled_system(de, name, prob, small_max,
     x = np.zeros_like(b)
     xyz = np.ascontiguousarray(prob["xpts"], np.float64) if coords else None
     rc = de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
-                     _ptr(_bcmask(prob)), _ptr(xyz), small_max, _ptr(b),
+                     _ptr(_bcmask(prob)), _ptr(xyz), small_max, 0, _ptr(b),
                      _ptr(x))
     assert rc == 0
     Kinf = abs(K).sum(axis=1).max()
@@ -252,7 +253,48 @@ def test_gpu_kernels_on_cpu_random_spd(de, n, bs, deg, seed, small_max,
     x = np.zeros_like(b)
     rc = de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
                      _ptr(np.zeros(n, np.int32)),
-                     _ptr(xyz if coords else None), small_max, _ptr(b),
+                     _ptr(xyz if coords else None), small_max, 0, _ptr(b),
                      _ptr(x))
     assert rc == 0
     assert rel(K @ x, b) < 1e-12
+
+
+
+@pytest.mark.parametrize("name,prob", list(_problems())[:4],
+                         ids=[p[0] for p in _problems()][:4])
+@pytest.mark.parametrize("small_max", [256, 0])
+def test_gpu_kernels_on_cpu_fp32_factor(de, name, prob, small_max):
+    """The FP32 factorisation: one FP32 solve is backward stable at FP32
+    level (|K x - b| <= 1e-5 |K| |x|), and iterative refinement with FP64
+    residuals and FP32 corrections reaches the FP64 solution (1e-10, and
+    the backward error of FP64, 1e-14 |K| |x|) within 6 steps.  The plain
+    relative residual cannot show this: these matrices have |K| |x| up to
+    1e9 |b|."""
+    from scipy import sparse
+    n, bs, rowp, cols, vals = _matrix(prob)
+    K = sparse.bsr_matrix((vals.reshape(-1, bs, bs), cols, rowp),
+                          shape=(n * bs, n * bs)).tocsr()
+    b = np.random.default_rng(5).standard_normal(n * bs)
+    xyz = np.ascontiguousarray(prob["xpts"], np.float64)
+    mask = _bcmask(prob)
+
+    def solve(r, prec):
+        r = np.ascontiguousarray(r, np.float64)
+        y = np.zeros_like(r)
+        assert de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
+                           _ptr(mask), _ptr(xyz), small_max, prec, _ptr(r),
+                           _ptr(y)) == 0
+        return y
+
+    Kinf = abs(K).sum(axis=1).max()
+
+    def eta(x):
+        return np.abs(K @ x - b).max() / (Kinf * np.abs(x).max())
+
+    x = solve(b, 1)
+    assert eta(x) < 1e-5
+    x64 = solve(b, 0)
+    for _ in range(6):
+        x = x + solve(b - K @ x, 1)
+    assert rel(x, x64) < 1e-10
+    assert eta(x) < 1e-14
