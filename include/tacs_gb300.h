@@ -189,6 +189,12 @@ int tg_direct_factor(tg_direct *d, void *stream);
 int tg_direct_solve(tg_direct *d, const double *b, double *x, void *stream);
 int tg_direct_solve_f32(tg_direct *d, const float *b, float *x,
                         void *stream);
+/* Mixed precision: x = A^-1 b in FP64 from an FP32 factorisation by
+   iterative refinement -- x = 0, then `steps` times x += FP32 solve of
+   the FP64 residual r = b - A x (each step gains the FP32 solve's
+   relative accuracy, about cond(A) 2^-24). */
+int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
+                            int steps, void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

@@ -53,7 +53,11 @@ class StaticSolver:
                                  "element, numbered like the elements")
             model.set_segments(model.prob["seg_elem_ptr"])
         self.mat = model.new_mat()
-        self.direct = Direct(self.mat) if direct else None
+        # direct: True / "fp64" complete factorisation, "mixed" in FP32
+        # with FP64 refinement of every solve
+        self.direct = Direct(self.mat, precision=_lib.PREC_FP32
+                             if direct == "mixed" else _lib.PREC_FP64) \
+            if direct else None
         if direct:
             self.pc = self.ksm = None
         else:

@@ -51,7 +51,9 @@ struct tg_direct {
   // FP32 factorisation: its storage, solve vectors and the matrix in FP32
   float *d_lstore32 = nullptr, *d_pool32 = nullptr, *d_contrib32 = nullptr;
   float *d_ypos32 = nullptr, *d_xpos32 = nullptr, *d_pb32 = nullptr,
-        *d_kpb32 = nullptr, *d_a32 = nullptr;
+        *d_kpb32 = nullptr, *d_a32 = nullptr, *d_r32 = nullptr,
+        *d_c32 = nullptr;
+  double *d_r = nullptr, *d_t = nullptr;  // refinement residual, scratch
   int64_t contrib_len = 0;
   int *d_fail = nullptr;
   bool factored = false;
@@ -91,7 +93,8 @@ struct tg_direct {
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
     dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
-    dfree(d_pb32); dfree(d_kpb32); dfree(d_a32);
+    dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
+    dfree(d_c32); dfree(d_r); dfree(d_t);
   }
 };
 
@@ -200,6 +203,10 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_pb32, N);
     if (!rc) rc = dalloc(&d->d_kpb32, N);
     if (!rc) rc = dalloc(&d->d_a32, (size_t)A->nnz * b2);
+    if (!rc) rc = dalloc(&d->d_r32, N);
+    if (!rc) rc = dalloc(&d->d_c32, N);
+    if (!rc) rc = dalloc(&d->d_r, N);
+    if (!rc) rc = dalloc(&d->d_t, N);
   }
   if (!rc) rc = dalloc(&d->d_ypos, N);
   if (!rc) rc = dalloc(&d->d_xpos, N);
@@ -321,6 +328,38 @@ int tg_direct_solve_f32(tg_direct *d, const float *b, float *x, void *s) {
     return fail(TG_ERR_ARG, "tg_direct_solve_f32: FP64 factorisation");
   solve_levels<float>(d, b, x, d->d_a32, d->d_pb32, d->d_kpb32,
                       d->d_ypos32, d->d_xpos32, d->d_contrib32, S(s));
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
+                            int steps, void *s) {
+  if (!d || !b || !x || steps < 1)
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined: bad arguments");
+  if (!d->factored)
+    return fail(TG_ERR_STATE, "tg_direct_solve_refined: not factored");
+  if (d->precision != TG_PREC_FP32)
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined: needs the FP32 "
+                            "factorisation");
+  tg_mat *A = d->A;
+  const size_t N = (size_t)d->n * d->bs;
+  // x = 0, r = b; then per step: x += FP32-solve(r), r = b - A x (FP64)
+  TG_CUDA(cudaMemsetAsync(x, 0, N * sizeof(double), S(s)));
+  tg::launch_copy(b, d->d_r, N, S(s));
+  for (int k = 0; k < steps; k++) {
+    tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
+    solve_levels<float>(d, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
+                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
+                        S(s));
+    tg::launch_f2d(d->d_c32, d->d_t, N, S(s));
+    tg::launch_axpy(1.0, d->d_t, x, N, S(s));
+    if (k + 1 < steps) {
+      tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                           A->d_vals, x, d->d_t, S(s));
+      tg::launch_copy(b, d->d_r, N, S(s));
+      tg::launch_axpy(-1.0, d->d_t, d->d_r, N, S(s));
+    }
+  }
   TG_CUDA(cudaGetLastError());
   return 0;
 }

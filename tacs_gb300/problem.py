@@ -139,13 +139,20 @@ class Direct:
         check(_lib.lib().tg_direct_factor(self.handle, _stream()),
               "tg_direct_factor")
 
-    def solve(self, b, x=None):
-        """x = A^-1 b; FP64 vectors for an FP64 factorisation, FP32 ones
-        for an FP32 factorisation."""
+    def solve(self, b, x=None, steps=6):
+        """x = A^-1 b.  FP64 factorisation: FP64 vectors.  FP32
+        factorisation: FP32 vectors are solved in FP32, FP64 ones by
+        `steps` steps of iterative refinement (FP64 residuals, FP32
+        corrections)."""
         x = torch.empty_like(b) if x is None else x
-        fn = (_lib.lib().tg_direct_solve_f32
-              if self.precision == _lib.PREC_FP32
-              else _lib.lib().tg_direct_solve)
+        L = _lib.lib()
+        if self.precision == _lib.PREC_FP32 and b.dtype == torch.float64:
+            check(L.tg_direct_solve_refined(self.handle, _p(b), _p(x),
+                                            int(steps), _stream()),
+                  "tg_direct_solve_refined")
+            return x
+        fn = (L.tg_direct_solve_f32 if self.precision == _lib.PREC_FP32
+              else L.tg_direct_solve)
         check(fn(self.handle, _p(b), _p(x), _stream()), "tg_direct_solve")
         return x
 
@@ -422,7 +429,8 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     reference harness (tests/integration_tests/static_analysis_base_test.py:
     359-427): K(u=0) and R(0), ILU(0), GMRES for R - f, functions, dfdu,
     adjoint solve with the same row-BC matrix, dfdx - psi^T dR/dx.  With
-    direct, both solves use the complete factorisation (Direct) instead."""
+    direct, both solves use the complete factorisation (Direct) instead;
+    direct="mixed" factors in FP32 and refines every solve in FP64."""
     dev = torch.device("cuda")
     u0 = model.vec()
     res = model.vec()
@@ -430,7 +438,8 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     model.assemble_jacobian(u0, mat, res)
     pc = ksm = dsol = None
     if direct:
-        dsol = Direct(mat)
+        dsol = Direct(mat, precision=_lib.PREC_FP32 if direct == "mixed"
+                      else _lib.PREC_FP64)
         dsol.factor()
 
         class _Exact:  # the solves' interface of Ksm
@@ -490,9 +499,11 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     mat = model.new_mat()
     model.assemble_jacobian(u0, mat, model.vec())
     if direct:
-        # one complete factorisation of the block-diagonal matrix; every
-        # load case and mesh is then exact (reported as converged in 0)
-        dsol = Direct(mat)
+        # one complete factorisation of the block-diagonal matrix (FP32 with
+        # FP64 refinement for direct="mixed"); every load case and mesh is
+        # then solved directly (reported as converged in 0 iterations)
+        dsol = Direct(mat, precision=_lib.PREC_FP32 if direct == "mixed"
+                      else _lib.PREC_FP64)
         dsol.factor()
         nsys = nlc * model.nseg
 

@@ -150,3 +150,20 @@ def test_direct_autograd_matches_reference_adjoint(gpu, func):
     f.sum().backward()
     g_ref = ref["grad_comp"] if func == 0 else ref["grad_ks"]
     assert rel(x.grad.cpu().numpy(), g_ref) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["shell_plate8", "hex_block"])
+def test_mixed_direct_adjoint_gradients(gpu, name):
+    """FP32 factorisation with FP64 refinement of every solve: the
+    reference's functions and gradients (1e-7) and the all-FP64 direct
+    gradients (1e-8)."""
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    r = gpu.static_adjoint(M, prob["force"], direct="mixed")
+    r64 = gpu.static_adjoint(M, prob["force"], direct=True)
+    assert rel(r["funcs"], ref["funcs"]) < 1e-7
+    assert rel(r["grads"][0].cpu().numpy(), ref["grad_comp"]) < 1e-7
+    assert rel(r["grads"][1].cpu().numpy(), ref["grad_ks"]) < 1e-7
+    for k in range(2):
+        assert rel(r["grads"][k].cpu().numpy(),
+                   r64["grads"][k].cpu().numpy()) < 1e-8
