@@ -49,6 +49,8 @@ extern "C" {
 #define TG_PC_ILU0 0        /* TACSAdditiveSchwarz(mat, levFill, fill): ILU */
 #define TG_PC_BLOCK_JACOBI 1 /* inverted diagonal blocks only */
 #define TG_PC_ILU0_COLORED 2 /* ILU(0) of a multicolour node reordering */
+#define TG_PC_DIRECT 3       /* complete factorisation (tg_direct); FP32:
+                                the factor of a mixed-precision solve */
 
 #define TG_PREC_FP64 0 /* preconditioner and inner mat-vec in FP64 */
 #define TG_PREC_FP32 1 /* FP32 factor / apply and inner mat-vec */
@@ -275,8 +277,9 @@ int tg_mat_mult_f32(tg_mat *A, const float *x, float *y, void *stream);
 /* ------------------------------------------------------- preconditioners */
 /* TACSAdditiveSchwarz(mat, levFill = 0, fill)
    (src/bpmat/TACSParallelMat.cpp:1190) with type TG_PC_ILU0, plus the
-   block-Jacobi and colour-reordered ILU(0) variants; precision
-   TG_PREC_FP32 keeps the factor in FP32. */
+   block-Jacobi and colour-reordered ILU(0) variants and TG_PC_DIRECT (the
+   complete factorisation of tg_direct_*, the reference's TACSSchurPc with
+   a large levFill); precision TG_PREC_FP32 keeps the factor in FP32. */
 int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out);
 /* TACSAdditiveSchwarz(mat, levFill, fill) with levFill > 0: block ILU(k)
    on the level-of-fill pattern of BCSRMat::computeILUk

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "libtacs_gb300.so")
 
 ELEM_MITC4, ELEM_HEX8 = 0, 1
 MAT_NORMAL, MAT_TRANSPOSE = 0, 1
-PC_ILU0, PC_BLOCK_JACOBI, PC_ILU0_COLORED = 0, 1, 2
+PC_ILU0, PC_BLOCK_JACOBI, PC_ILU0_COLORED, PC_DIRECT = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
 FUNC_COMPLIANCE, FUNC_KS_FAILURE = 0, 1
 

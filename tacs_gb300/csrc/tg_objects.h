@@ -182,7 +182,12 @@ struct tg_pc {
   cudaGraphExec_t apply_exec = nullptr;
   bool factored = false;
   bool fp64_ready = false;  // FP32 pc: FP64 factor of the same matrix in d_F
+  // TG_PC_DIRECT: the factorisation in the pc's precision, and for an FP32
+  // pc the FP64 one its FP64 fallback passes use
+  tg_direct *direct = nullptr, *direct64 = nullptr;
   ~tg_pc() {
+    if (direct) tg_direct_decref(direct);
+    if (direct64) tg_direct_decref(direct64);
     if (apply_exec) cudaGraphExecDestroy(apply_exec);
     dfree(d_lvl_rows); dfree(d_ulvl_rows); dfree(d_upd_ptr);
     dfree(d_upd_tgt); dfree(d_upd_src); dfree(d_fail); dfree(d_F);

@@ -1058,7 +1058,7 @@ static int pc_create(tg_mat *A, int type, int lev_fill, int precision,
   if (!A || !out) return fail(TG_ERR_ARG, "tg_pc_create: NULL argument");
   *out = nullptr;
   if (type != TG_PC_ILU0 && type != TG_PC_BLOCK_JACOBI &&
-      type != TG_PC_ILU0_COLORED)
+      type != TG_PC_ILU0_COLORED && type != TG_PC_DIRECT)
     return fail(TG_ERR_ARG, "tg_pc_create: unknown preconditioner type");
   if (precision != TG_PREC_FP64 && precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_pc_create: bad precision");
@@ -1074,6 +1074,24 @@ static int pc_create(tg_mat *A, int type, int lev_fill, int precision,
   tg_assembler *a = A->a;
   int rc = 0;
   const int *rowp_d = a->d_rowp, *cols_d = a->d_cols, *diag_d = a->d_diag;
+  if (type == TG_PC_DIRECT) {
+    // the complete factorisation: only the apply buffers of this object
+    const size_t n = (size_t)A->nrows * A->bsize;
+    rc = tg_direct_create(A, 1, precision, &pc->direct);
+    if (!rc) rc = dalloc(&pc->d_fail, 1);
+    if (!rc) rc = dalloc(&pc->d_gx, n);
+    if (!rc) rc = dalloc(&pc->d_gy, n);
+    if (!rc && precision == TG_PREC_FP32) rc = dalloc(&pc->d_x32, n);
+    if (!rc && precision == TG_PREC_FP32) rc = dalloc(&pc->d_y32, n);
+    if (rc) {
+      tg_pc_decref(pc);
+      return rc;
+    }
+    pc->plan.bsize = A->bsize;
+    pc->plan.nrows = A->nrows;
+    *out = pc;
+    return 0;
+  }
   if (type == TG_PC_ILU0 && lev_fill > 0) {
     std::vector<int> frowp, fcols, fdiag, valmap;
     iluk_pattern(a->rowp_h, a->cols_h, lev_fill, frowp, fcols, fdiag,
@@ -1207,6 +1225,16 @@ namespace tg {
 // mixed-precision solve falls back to (kept in d_F beside the FP32 factor).
 int pc_factor_fp64(tg_pc *pc, cudaStream_t s) {
   if (pc->precision == TG_PREC_FP64 || pc->fp64_ready) return 0;
+  if (pc->type == TG_PC_DIRECT) {
+    if (!pc->direct64) {
+      int rc = tg_direct_create(pc->A, 1, TG_PREC_FP64, &pc->direct64);
+      if (rc) return rc;
+    }
+    int rc = tg_direct_factor(pc->direct64, s);
+    if (rc) return rc;
+    pc->fp64_ready = true;
+    return 0;
+  }
   tg_mat *A = pc->A;
   const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
   TG_CUDA(cudaMemsetAsync(pc->d_fail, 0, sizeof(int), s));
@@ -1298,6 +1326,14 @@ extern "C" {
 int tg_pc_factor(tg_pc *pc, void *s) {
   if (!pc) return fail(TG_ERR_ARG, "tg_pc_factor: NULL pc");
   tg_mat *A = pc->A;
+  if (pc->type == TG_PC_DIRECT) {
+    int rc = tg_direct_factor(pc->direct, s);
+    if (!rc && pc->precision == TG_PREC_FP32) rc = ensure_f32(A, S(s));
+    if (rc) return rc;
+    pc->factored = true;
+    pc->fp64_ready = false;
+    return 0;
+  }
   const size_t nv = (size_t)A->nnz * A->bsize * A->bsize;
   TG_CUDA(cudaMemsetAsync(pc->d_fail, 0, sizeof(int), S(s)));
   if (pc->type == TG_PC_ILU0_COLORED) {
@@ -1379,6 +1415,22 @@ int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
               void *tmp, void *px, void *py, cudaStream_t s, int use_f64) {
   const int bs = pc->A->bsize, nr = pc->A->nrows;
   const bool f64 = use_f64 < 0 ? pc->precision == TG_PREC_FP64 : use_f64 != 0;
+  if (pc->type == TG_PC_DIRECT) {
+    // one direct solve per right-hand side (FP64 solves of an FP32 pc use
+    // its FP64 factorisation)
+    tg_direct *d = pc->precision == TG_PREC_FP64 ? pc->direct : pc->direct64;
+    for (int r = 0; r < nrhs; r++) {
+      int rc;
+      if (f64)
+        rc = tg_direct_solve(d, (const double *)in + r * ld,
+                             (double *)out + r * ld, s);
+      else
+        rc = tg_direct_solve_f32(pc->direct, (const float *)in + r * ld,
+                                 (float *)out + r * ld, s);
+      if (rc) return rc;
+    }
+    return 0;
+  }
   if (pc->type == TG_PC_BLOCK_JACOBI) {
     if (f64)
       launch_block_jacobi_apply(pc->plan, pc->d_F, (const double *)in,
@@ -1428,7 +1480,7 @@ static int pc_apply_internal(tg_pc *pc, cudaStream_t s) {
   void *tmp = f64 ? (void *)pc->d_tmp : (void *)pc->d_tmp32;
   void *px = f64 ? (void *)pc->d_px : (void *)pc->d_px32;
   void *py = f64 ? (void *)pc->d_py : (void *)pc->d_py32;
-  if (pc->type == TG_PC_BLOCK_JACOBI)
+  if (pc->type == TG_PC_BLOCK_JACOBI || pc->type == TG_PC_DIRECT)
     return pc_launch(pc, 1, n, in, out, tmp, px, py, s);
   if (!pc->apply_exec) {
     cudaStream_t cs;
@@ -1451,6 +1503,14 @@ static int pc_apply_internal(tg_pc *pc, cudaStream_t s) {
 int tg_pc_get_schedule(tg_pc *pc, int *cluster_size, int *groups,
                        int *levels, double *tuned_ms) {
   if (!pc) return fail(TG_ERR_ARG, "NULL pc");
+  if (pc->type == TG_PC_DIRECT) {  // no level schedule of its own
+    if (cluster_size) *cluster_size = 0;
+    if (groups) *groups = 0;
+    if (levels) *levels = 0;
+    if (tuned_ms)
+      for (int i = 0; i < 5; i++) tuned_ms[i] = 0.0;
+    return 0;
+  }
   const IluClusterView &v = pc->plan.cluster;
   if (cluster_size) *cluster_size = v.ngroups ? v.cs : 0;
   if (groups) *groups = v.ngroups;

@@ -167,3 +167,33 @@ def test_mixed_direct_adjoint_gradients(gpu, name):
     for k in range(2):
         assert rel(r["grads"][k].cpu().numpy(),
                    r64["grads"][k].cpu().numpy()) < 1e-8
+
+
+def test_direct_as_gmres_preconditioner(gpu):
+    """The complete factorisation as a GMRES preconditioner (TG_PC_DIRECT):
+    one or two iterations in FP64; in FP32 inside FP64 flexible GMRES with
+    refinement (GMRES-IR), the FP64 solution on a thin simply supported
+    plate to the true-residual tolerance."""
+    from tacs_gb300 import _lib, meshes
+    n = 32
+    prob = meshes.plate(n, n, 2.0, 2.0, t=0.002)
+    e = meshes.plate_edges(n, n).astype(np.int32)
+    prob["bc_nodes"], prob["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
+    prob["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    prob["pres_vals"] = np.full(4 * n * n, 1e3)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    b = _rhs(M, prob, mat)
+    pc = gpu.Pc(mat, _lib.PC_DIRECT)
+    pc.factor()
+    ksm = gpu.Ksm(mat, pc, 20, 2)
+    ksm.set_tolerances(1e-12)
+    x64, flag = ksm.solve(b)
+    assert flag == 1 and ksm.iters <= 3
+    pc32 = gpu.Pc(mat, _lib.PC_DIRECT, _lib.PREC_FP32)
+    pc32.factor()
+    ksm32 = gpu.Ksm(mat, pc32, 50, 10, mixed=True)
+    ksm32.set_tolerances(1e-12)
+    x32, flag = ksm32.solve(b)
+    assert flag == 1
+    assert rel(x32.cpu().numpy(), x64.cpu().numpy()) < 1e-8
