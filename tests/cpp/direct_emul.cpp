@@ -101,8 +101,10 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
       if (an.sn_parent[s] >= 0) ch_list[fill[an.sn_parent[s]]++] = s;
   }
   std::vector<int> bcmask(bcmask_in, bcmask_in + n);
+  // sized exactly as tg_direct.cu allocates them, so that a sanitizer
+  // build sees any access the GPU would make out of bounds
   std::vector<T> lstore((size_t)an.l_total * b2),
-      pool((size_t)an.u_peak * b2 + 1), contrib(vacc + 1), ypos(N), xpos(N),
+      pool((size_t)an.u_peak * b2), contrib(vacc), ypos(N), xpos(N),
       pb(N), kpb(N), bt(b_in, b_in + N), xt(N), vt(vals, vals + rowp[n] * b2);
   const T *b = bt.data();
   T *x = xt.data();
@@ -214,3 +216,56 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
 }
 
 }  // extern "C"
+
+#ifdef DE_MAIN
+// Stand-alone driver for a sanitizer build (-fsanitize=address,undefined):
+// reads one system written by tests/test_direct_symbolic.py, solves it in
+// FP64 and FP32, and prints the two solutions' max |K x - b|.
+#include <cstdio>
+#include <cstdlib>
+static bool read_all(FILE *f, void *p, size_t bytes) {
+  return bytes == 0 || fread(p, 1, bytes, f) == bytes;
+}
+int main(int argc, char **argv) {
+  if (argc < 3) return 2;
+  FILE *f = fopen(argv[1], "rb");
+  if (!f) return 2;
+  int hdr[4];  // n, bs, nnz, has_xyz
+  if (!read_all(f, hdr, sizeof hdr)) return 2;
+  const int n = hdr[0], bs = hdr[1], nnz = hdr[2];
+  const size_t N = (size_t)n * bs;
+  std::vector<int> rowp(n + 1), cols(nnz), mask(n);
+  std::vector<double> vals((size_t)nnz * bs * bs), xyz(3 * (size_t)n), b(N),
+      x(N);
+  bool ok = read_all(f, rowp.data(), sizeof(int) * rowp.size()) &&
+            read_all(f, cols.data(), sizeof(int) * cols.size()) &&
+            read_all(f, vals.data(), sizeof(double) * vals.size()) &&
+            read_all(f, mask.data(), sizeof(int) * mask.size()) &&
+            read_all(f, b.data(), sizeof(double) * N);
+  if (ok && hdr[3]) ok = read_all(f, xyz.data(), sizeof(double) * xyz.size());
+  fclose(f);
+  if (!ok) return 2;
+  const int small_max = atoi(argv[2]);
+  for (int prec = 0; prec < 2; prec++) {
+    const int rc = de_solve(n, bs, rowp.data(), cols.data(), vals.data(),
+                            mask.data(), hdr[3] ? xyz.data() : nullptr,
+                            small_max, prec, b.data(), x.data());
+    if (rc) {
+      printf("fail %d\n", rc);
+      return 1;
+    }
+    double res = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int r = 0; r < bs; r++) {
+        double acc = -b[(size_t)i * bs + r];
+        for (int j = rowp[i]; j < rowp[i + 1]; j++)
+          for (int q = 0; q < bs; q++)
+            acc += vals[(size_t)j * bs * bs + r * bs + q] *
+                   x[(size_t)cols[j] * bs + q];
+        res = std::max(res, std::fabs(acc));
+      }
+    printf("%d %.6e\n", prec, res);
+  }
+  return 0;
+}
+#endif

@@ -298,3 +298,54 @@ def test_gpu_kernels_on_cpu_fp32_factor(de, name, prob, small_max):
         x = x + solve(b - K @ x, 1)
     assert rel(x, x64) < 1e-10
     assert eta(x) < 1e-14
+
+
+def _write_system(path, n, bs, rowp, cols, vals, mask, b, xyz):
+    """The binary layout the sanitizer driver of direct_emul.cpp reads."""
+    with open(path, "wb") as f:
+        np.array([n, bs, len(cols), xyz is not None], np.int32).tofile(f)
+        rowp.astype(np.int32).tofile(f)
+        cols.astype(np.int32).tofile(f)
+        vals.astype(np.float64).tofile(f)
+        mask.astype(np.int32).tofile(f)
+        b.astype(np.float64).tofile(f)
+        if xyz is not None:
+            np.asarray(xyz, np.float64).ravel().tofile(f)
+
+
+def test_gpu_kernels_in_bounds_under_sanitizers(tmp_path):
+    """Every load and store the numeric kernels make stays inside the
+    buffers tg_direct.cu allocates: the emulation, with its buffers sized
+    exactly as on the device, built with AddressSanitizer and
+    UndefinedBehaviorSanitizer (any finding aborts), over meshes, a
+    disconnected set of solids and a random pattern, both front paths, FP64
+    and FP32.  The kernels' thread loops are all strided, so one thread per
+    CTA visits exactly the GPU's index set."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "de_san")
+    r = subprocess.run([cxx, "-O1", "-g", "-std=c++17",
+                        "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=all", "-DDE_MAIN", "-I", INC,
+                        EMUL, "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime unavailable: " + r.stderr[-200:])
+    from tacs_gb300 import meshes
+    cases = []
+    for prob in (meshes.clamped_plate(12), meshes.hex_c3(4, 3, 3),
+                 load_case("hex_rand")[0]):
+        n, bs, rowp, cols, vals = _matrix(prob)
+        cases.append((n, bs, rowp, cols, vals, _bcmask(prob),
+                      np.asarray(prob["xpts"], np.float64)))
+    rowp, cols, vals, xyz = _random_spd(120, 3, 12, 7)
+    cases.append((120, 3, rowp, cols, vals, np.zeros(120, np.int32), xyz))
+    sysf = str(tmp_path / "sys.bin")
+    for n, bs, rowp, cols, vals, mask, xyz in cases:
+        b = np.random.default_rng(n).standard_normal(n * bs)
+        _write_system(sysf, n, bs, rowp, cols, vals, mask, b, xyz)
+        for small_max in ("96", "0", str(1 << 30)):
+            r = subprocess.run([exe, sysf, small_max], capture_output=True,
+                               text=True, timeout=300)
+            assert r.returncode == 0, r.stdout + r.stderr[-3000:]
+            assert len(r.stdout.split()) == 4
