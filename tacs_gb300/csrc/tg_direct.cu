@@ -280,6 +280,27 @@ static void solve_levels(tg_direct *d, const T *b, T *x, const T *a, T *pb,
   tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, x, s);
 }
 
+namespace tg {
+
+int direct_enqueue_solve(tg_direct *d, const void *b, void *x, bool f32,
+                         cudaStream_t s) {
+  if (!d || !b || !x)
+    return fail(TG_ERR_ARG, "direct solve: NULL argument");
+  if (f32 != (d->precision == TG_PREC_FP32))
+    return fail(TG_ERR_ARG, "direct solve: precision of the factorisation");
+  if (f32)
+    solve_levels<float>(d, (const float *)b, (float *)x, d->d_a32, d->d_pb32,
+                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
+                        s);
+  else
+    solve_levels<double>(d, (const double *)b, (double *)x, d->A->d_vals,
+                         d->d_pb, d->d_kpb, d->d_ypos, d->d_xpos,
+                         d->d_contrib, s);
+  return 0;
+}
+
+}  // namespace tg
+
 extern "C" {
 
 int tg_direct_factor(tg_direct *d, void *s) {
@@ -314,8 +335,7 @@ int tg_direct_solve(tg_direct *d, const double *b, double *x, void *s) {
   if (d->precision != TG_PREC_FP64)
     return fail(TG_ERR_ARG, "tg_direct_solve: FP32 factorisation "
                             "(use tg_direct_solve_f32)");
-  solve_levels<double>(d, b, x, d->A->d_vals, d->d_pb, d->d_kpb, d->d_ypos,
-                       d->d_xpos, d->d_contrib, S(s));
+  tg::direct_enqueue_solve(d, b, x, false, S(s));
   TG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -326,8 +346,7 @@ int tg_direct_solve_f32(tg_direct *d, const float *b, float *x, void *s) {
     return fail(TG_ERR_STATE, "tg_direct_solve_f32: not factored");
   if (d->precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_direct_solve_f32: FP64 factorisation");
-  solve_levels<float>(d, b, x, d->d_a32, d->d_pb32, d->d_kpb32,
-                      d->d_ypos32, d->d_xpos32, d->d_contrib32, S(s));
+  tg::direct_enqueue_solve(d, b, x, true, S(s));
   TG_CUDA(cudaGetLastError());
   return 0;
 }

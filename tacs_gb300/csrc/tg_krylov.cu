@@ -251,8 +251,11 @@ int ensure_layout(tg_ksm *k, int nrhs) {
   st.it = q; q += 1;
   st.nactive = q; q += 1;
   st.stall = q; q += 1;
-  // graphs
-  rc = capture(&k->g_start, [&](cudaStream_t cs) { enqueue_start(k, cs); });
+  // graphs (a mixed solve's FP64 passes read the FP64 factor, which must
+  // have its buffers before they are captured)
+  if (!rc && k->mixed && k->pc) rc = pc_prepare_fp64(k->pc);
+  if (!rc)
+    rc = capture(&k->g_start, [&](cudaStream_t cs) { enqueue_start(k, cs); });
   if (!rc)
     rc = capture(&k->g_end, [&](cudaStream_t cs) { enqueue_end(k, cs); });
   for (int mode = 0; mode < (k->mixed ? 2 : 1) && !rc; mode++)

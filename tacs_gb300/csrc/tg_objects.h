@@ -270,4 +270,12 @@ int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
               void *tmp, void *px, void *py, cudaStream_t s, int use_f64 = -1);
 // FP64 factor of an FP32 pc's matrix (for FP64 fallback passes)
 int pc_factor_fp64(tg_pc *pc, cudaStream_t s);
+// Allocate (not factor) whatever pc_factor_fp64 will fill, so that graphs
+// captured before the fallback see its buffers
+int pc_prepare_fp64(tg_pc *pc);
+// Enqueue x = A^-1 b with a direct factorisation whether or not it is
+// factored yet (graph capture; tg_direct.cu): FP64 b, x for an FP64
+// factorisation, FP32 for an FP32 one
+int direct_enqueue_solve(tg_direct *d, const void *b, void *x, bool f32,
+                         cudaStream_t s);
 }  // namespace tg

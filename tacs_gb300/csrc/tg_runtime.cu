@@ -1223,14 +1223,19 @@ namespace tg {
 
 // FP64 factor of an FP32 preconditioner's matrix, for the FP64 passes a
 // mixed-precision solve falls back to (kept in d_F beside the FP32 factor).
+int pc_prepare_fp64(tg_pc *pc) {
+  if (pc->precision == TG_PREC_FP64 || pc->type != TG_PC_DIRECT ||
+      pc->direct64)
+    return 0;  // the ILU variants keep their FP64 factor from creation
+  return tg_direct_create(pc->A, 1, TG_PREC_FP64, &pc->direct64);
+}
+
 int pc_factor_fp64(tg_pc *pc, cudaStream_t s) {
   if (pc->precision == TG_PREC_FP64 || pc->fp64_ready) return 0;
   if (pc->type == TG_PC_DIRECT) {
-    if (!pc->direct64) {
-      int rc = tg_direct_create(pc->A, 1, TG_PREC_FP64, &pc->direct64);
-      if (rc) return rc;
-    }
-    int rc = tg_direct_factor(pc->direct64, s);
+    int rc = pc_prepare_fp64(pc);
+    if (rc) return rc;
+    rc = tg_direct_factor(pc->direct64, s);
     if (rc) return rc;
     pc->fp64_ready = true;
     return 0;
@@ -1417,16 +1422,17 @@ int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
   const bool f64 = use_f64 < 0 ? pc->precision == TG_PREC_FP64 : use_f64 != 0;
   if (pc->type == TG_PC_DIRECT) {
     // one direct solve per right-hand side (FP64 solves of an FP32 pc use
-    // its FP64 factorisation)
+    // its FP64 factorisation).  Enqueued without the factored check: a
+    // Krylov graph is captured before the FP64 fallback factors direct64.
     tg_direct *d = pc->precision == TG_PREC_FP64 ? pc->direct : pc->direct64;
     for (int r = 0; r < nrhs; r++) {
       int rc;
       if (f64)
-        rc = tg_direct_solve(d, (const double *)in + r * ld,
-                             (double *)out + r * ld, s);
+        rc = direct_enqueue_solve(d, (const double *)in + r * ld,
+                                  (double *)out + r * ld, false, s);
       else
-        rc = tg_direct_solve_f32(pc->direct, (const float *)in + r * ld,
-                                 (float *)out + r * ld, s);
+        rc = direct_enqueue_solve(pc->direct, (const float *)in + r * ld,
+                                  (float *)out + r * ld, true, s);
       if (rc) return rc;
     }
     return 0;
