@@ -17,6 +17,16 @@ CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+    config.addinivalue_line(
+        "markers", "direct: uses the direct (multifrontal) factorisation")
+
+
+def pytest_collection_modifyitems(session, config, items):
+    """Tests of the direct factorisation run after the others (stable
+    order otherwise): the iterative path's parity tests come first, so that
+    under -x a failure in the newer direct path cannot stop them."""
+    items[:] = ([i for i in items if i.get_closest_marker("direct") is None]
+                + [i for i in items if i.get_closest_marker("direct")])
 
 
 def load_case(name):

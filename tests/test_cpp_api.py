@@ -32,7 +32,8 @@ def test_cpp_header_compiles():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["gmres", "direct"])
+@pytest.mark.parametrize("mode", ["gmres", pytest.param(
+    "direct", marks=pytest.mark.direct)])
 def test_cpp_driver_matches_reference(tmp_path, mode):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():

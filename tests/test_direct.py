@@ -18,7 +18,7 @@ import pytest
 from conftest import load_case, rel
 
 torch = pytest.importorskip("torch")
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.direct]
 
 
 @pytest.fixture(scope="module")

@@ -116,6 +116,7 @@ def test_pytacs_static_problems_match_reference(tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.direct
 def test_pytacs_direct_solve_matches_reference(tmp_path):
     """The same problems solved by the complete factorisation (option
     directSolve): the known answers (1e-8) and the same sensitivities as

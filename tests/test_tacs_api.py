@@ -93,7 +93,8 @@ def _build(prob):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["shell_c1", "shell_plate8", "hex_block",
                                   "shell_cyl"])
-@pytest.mark.parametrize("schur", [False, True])
+@pytest.mark.parametrize("schur", [False, pytest.param(
+    True, marks=pytest.mark.direct)])
 def test_static_adjoint_through_reference_api(name, schur):
     """schur=True: createSchurMat with the default Pc, the reference's
     direct solve (here the complete multifrontal factorisation)."""

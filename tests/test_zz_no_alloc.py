@@ -1,8 +1,10 @@
 """The allocation-free entry point tg_eval_functions_noalloc, called
 through the C ABI, against the allocating path (tg_eval_functions).
 
-This file sorts last so that a run stopping at its first failure has
-already run every other test; it must also pass alone in a fresh process
+This file sorts after the other tests of the iterative path (only the
+direct factorisation's tests follow it) so that a run stopping at its
+first failure has already run those; it must also pass alone in a fresh
+process
 (the first call on the device performs the scratch-address set-up).
 """
 import ctypes as C
