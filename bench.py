@@ -217,7 +217,8 @@ def hex_section(torch, steps=5):
            "bcsr_blocks": int(nnzb), "ms_per_step": ms,
            "elements_per_s": p["nelem"] / (ms / 1e3),
            "hbm_gbs_algorithmic": algo / (ms / 1e3) / 1e9,
-           "algorithmic_bytes": int(algo)}
+           "algorithmic_bytes": int(algo),
+           "fp64": fp64_roofline("hex", p["nelem"] / (ms / 1e3))}
     del M, mat, u, res
     torch.cuda.empty_cache()
     return out
@@ -329,6 +330,39 @@ def traffic_per_step(nelem):
     per-element traffic is size independent (colour-by-colour block
     read-modify-write), so it scales with the elements of a step."""
     return int(135.4e6 / 16384 * nelem)
+
+
+# FP64 work per element of one residual + Jacobian assembly (flops: add,
+# sub, mul, div, sqrt; a fused multiply-add is two).
+#  - reference: the reference element's addJacobian(alpha=1, beta=gamma=0),
+#    counted by the operation-counting build of its sources
+#    (oracle/ref/opcount.h, `make -C oracle/ref opc && oracle/_ref/op_count`)
+#  - executed: this repository's kernels, from ncu's executed DFMA / DADD /
+#    DMUL thread instructions over one colour launch of 16,384 elements
+#    (shell: 256 x 256 plate; hex: 64 x 64 x 32 block)
+FP64_FLOPS_PER_ELEMENT = {
+    "shell": {"reference": 153602, "executed": 39574},
+    "hex": {"reference": 149808, "executed": 14204},
+}
+# nominal FP64 peak: 152 SMs x 2 FMA lanes per clock x 2 flops x 2.07 GHz
+FP64_PEAK_TFLOPS = 1.259
+
+
+def fp64_roofline(kind, elements_per_s):
+    """The kernel's FP64 throughput (executed flops) against the nominal
+    FP64 peak, and the reference-equivalent rate: the reference element's
+    flops for the same elements per second (above the peak when this
+    formulation needs fewer flops than the reference's)."""
+    f = FP64_FLOPS_PER_ELEMENT[kind]
+    ach = elements_per_s * f["executed"] / 1e12
+    ref = elements_per_s * f["reference"] / 1e12
+    return {"unit": "TFLOP/s", "peak": FP64_PEAK_TFLOPS,
+            "peak_source": "nominal (152 SMs x 2 FP64 FMA/clk x 2.07 GHz)",
+            "executed_flops_per_element": f["executed"],
+            "achieved": ach, "frac": ach / FP64_PEAK_TFLOPS,
+            "reference_flops_per_element": f["reference"],
+            "reference_equivalent": ref,
+            "reference_equivalent_frac": ref / FP64_PEAK_TFLOPS}
 
 
 def algorithmic_bytes(p):
@@ -596,7 +630,9 @@ def main():
                      "fp64_pipe_active": 0.705,
                      "peak_source": peak_src,
                      "kernel": "shell_team_assembly_kernel",
-                     "kernel_ms": kern_ms, "algorithmic_bytes": algo},
+                     "kernel_ms": kern_ms, "algorithmic_bytes": algo,
+                     "fp64": fp64_roofline("shell",
+                                           nelem / (kern_ms / 1e3))},
         "e2e": {"value": world * nelem / (ms_e2e / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": int(8 * (M.ndv + M.ndof)),
                 "d2h_bytes_per_step": int(8 * M.ndof)},

@@ -8,11 +8,12 @@ ill-conditioned shell systems, so they are compared at 1e-7 (bounded by
 cond(K) x the 1e-12 solver tolerance, not by the element arithmetic).
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
 
-from conftest import CASES, load_case, rel
+from conftest import CASES, ROOT, load_case, rel
 
 oracle = pytest.importorskip("oracle")
 
@@ -92,3 +93,22 @@ def test_static_solve_and_adjoint_gradient(case):
     assert rel(r["funcs"], ref["funcs"]) < SOLVE_TOL
     assert rel(r["grad_comp"], ref["grad_comp"]) < SOLVE_TOL
     assert rel(r["grad_ks"], ref["grad_ks"]) < SOLVE_TOL
+
+
+def test_fp64_work_constants_match_operation_counts():
+    """The per-element FP64 work bench.py quotes for the reference element
+    (its addJacobian) is what the operation-counting build of the
+    reference's sources prints (oracle/ref/opcount.h, op_count.cpp); runs
+    where that build exists (make -C oracle/ref opc)."""
+    import subprocess
+    exe = os.path.join(ROOT, "oracle", "_ref", "op_count")
+    if not os.path.exists(exe):
+        pytest.skip("operation-counting build not present")
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60,
+                         check=True).stdout
+    rows = {" ".join(line.split()[:-6]): int(line.split()[-1])
+            for line in out.splitlines()[1:] if line.strip()}
+    import bench
+    for kind in ("shell", "hex"):
+        assert rows[f"{kind} addJacobian"] == \
+            bench.FP64_FLOPS_PER_ELEMENT[kind]["reference"]
