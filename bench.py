@@ -119,25 +119,40 @@ def adjoint_section(n, torch, colored=False):
 
 def xpt_timing(M, r, torch, reps=3):
     """Node-coordinate total derivative df/dX - psi^T dR/dX of compliance
-    and KS from a solved state and its adjoints (the dual-number
-    addXptSens + addAdjointResXptSensProducts pass), CUDA-event time per
-    function."""
+    and KS from a solved state and its adjoints (the fused addXptSens +
+    addAdjointResXptSensProducts pass), CUDA-event time per function, for
+    both exact forms of the shell derivative: dual numbers per coordinate
+    (the default) and the reverse sweep per element; their largest
+    relative difference is reported beside the times."""
     u, psis = r["u"], r["psis"]
-    gX = M.node_vec()
-    ms = []
-    for fn in (0, 1):
-        M.eval_functions(u, [fn])
-        M.add_total_xpt_derivative(u, fn, psis[fn], gX)  # warm-up
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            M.add_total_xpt_derivative(u, fn, psis[fn], gX)
-        e1.record()
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1) / reps)
-    return {"ms_per_function": ms,
-            "elements_per_s": [M.nelem / (t / 1e3) for t in ms]}
+    out = {}
+    res = {}
+    for label, reverse in (("forward_dual", False), ("reverse_sweep", True)):
+        M.set_xpt_mode(reverse)
+        ms, grads = [], []
+        for fn in (0, 1):
+            M.eval_functions(u, [fn])
+            gX = M.node_vec()
+            M.add_total_xpt_derivative(u, fn, psis[fn], gX)  # warm-up
+            grads.append(gX.clone())
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                M.add_total_xpt_derivative(u, fn, psis[fn], gX)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1) / reps)
+        res[label] = grads
+        out[label] = {"ms_per_function": ms,
+                      "elements_per_s": [M.nelem / (t / 1e3) for t in ms]}
+    M.set_xpt_mode(False)
+    out["reverse_vs_forward_max_rel_diff"] = max(
+        float((a - b).abs().max() / b.abs().max())
+        for a, b in zip(res["reverse_sweep"], res["forward_dual"]))
+    out["reverse_speedup"] = (sum(out["forward_dual"]["ms_per_function"]) /
+                              sum(out["reverse_sweep"]["ms_per_function"]))
+    return out
 
 
 def c2_adjoint_section(torch, n=512):

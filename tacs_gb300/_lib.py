@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libtacs_gb300.so")
 ELEM_MITC4, ELEM_HEX8 = 0, 1
 MAT_NORMAL, MAT_TRANSPOSE = 0, 1
 PC_ILU0, PC_BLOCK_JACOBI, PC_ILU0_COLORED, PC_DIRECT = 0, 1, 2, 3
+XPT_FORWARD, XPT_REVERSE = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 FUNC_COMPLIANCE, FUNC_KS_FAILURE = 0, 1
 
@@ -58,6 +59,7 @@ SIGNATURES = [
     ("tg_direct_get_stats", _I, [_P, _P]),
     ("tg_direct_decref", _I, [_P]),
     ("tg_add_xpt_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),
+    ("tg_set_xpt_mode", _I, [_P, _I]),
     ("tg_add_adjoint_res_xpt_products", _I, [_P, _P, _D, _I, _P, _P, _D, _P]),
     ("tg_add_total_xpt_derivative", _I, [_P, _P, _I, _D, _P, _D, _P, _P]),
     ("tg_mat_create", _I, [_P, C.POINTER(_P)]),

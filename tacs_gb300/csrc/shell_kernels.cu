@@ -366,26 +366,30 @@ __global__ void __launch_bounds__(WARPS * 32)
 
 // ---------------------------------------------------------------------------
 // Node-coordinate sensitivities (TACSAssembler::addXptSens and
-// addAdjointResXptSensProducts, src/TACSAssembler.cpp:4858-4920,5136-5205).
-// One thread per (element, nodal coordinate k): the element's coordinates
-// are duals with dX_k = 1, and the thread differentiates exactly
-//   psi^T R_e(X): the shell residual sum_q detXd_q e_q(psi) . s(e_q(u))
-//     (TACSShellElement::addResidual, TACSShellElement.h:295-433) plus the
-//     pressure load scaled by lambda (TACSShellPressure::addResidual,
-//     TACSShellPressure.h:51-90);
-//   the element's function terms: compliance sum_q detXd_q e_q . s_q
-//     (TACSCompliance::getElementXptSens, TACSCompliance.cpp:129-156), or
-//     KS_CONTINUOUS with dfdq = detXd e^{rho (f - max)} / sum and
-//     dfddetXd = e^{rho (f - max)} / (rho sum) held at their values
-//     (TACSKSFailure::getElementXptSens, TACSKSFailure.cpp:289-340).
-// The strains come from the kinematics of shell_build_B applied to u and
-// psi directly: the nodal drilling strains, the 9 tying strains and, at
-// each Gauss point, the tying interpolation and the bending rows.
-using ad::Dual;
+// addAdjointResXptSensProducts, src/TACSAssembler.cpp:4858-4920,5136-5205):
+// per element, d/dX of scale psi^T R_e + coef f_e (shell residual and
+// pressure load; compliance or KS failure terms), defined and derived in
+// shell_xpt.cuh in two exact forms: forward (dual numbers,
+// shell_xpt_kernel, one thread per element coordinate) and reverse (a
+// hand-written adjoint sweep, shell_xpt_rev_kernel, one thread per
+// element).  Both scatter colour by colour without atomics.
+#include "shell_xpt.cuh"
 
-__device__ __forceinline__ void shell_corner(int k, double *N, double *Na,
-                                             double *Nb) {
-  shape2(-1.0 + 2.0 * (k % 2), -1.0 + 2.0 * (k / 2), N, Na, Nb);
+__device__ __forceinline__ void shell_xpt_load(const MeshView &m, int e,
+                                               const double *vars,
+                                               const double *psi,
+                                               ShellXptData &dt, int *nodes) {
+  for (int i = 0; i < 4; i++) nodes[i] = m.conn[4 * e + i];
+  for (int i = 0; i < 12; i++) dt.X[i] = m.xpts[3 * nodes[i / 3] + i % 3];
+  for (int i = 0; i < 24; i++) {
+    const int g = 6 * nodes[i / 6] + i % 6;
+    dt.u[i] = vars[g];
+    dt.w[i] = psi ? psi[g] : 0.0;
+  }
+  dt.t = m.thick[e];
+  dt.has_psi = psi != nullptr;
+  dt.has_pres = m.pres != nullptr;
+  for (int k = 0; k < 4; k++) dt.pres[k] = m.pres ? m.pres[4 * e + k] : 0.0;
 }
 
 __global__ void __launch_bounds__(128)
@@ -396,225 +400,32 @@ __global__ void __launch_bounds__(128)
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= 12LL * cr.count) return;
   const int e = cr.elem_list[idx / 12], kc = (int)(idx % 12);
+  ShellXptData dt;
   int nodes[4];
-  for (int i = 0; i < 4; i++) nodes[i] = m.conn[4 * e + i];
-  Dual X[12];
-  for (int i = 0; i < 12; i++)
-    X[i] = Dual(m.xpts[3 * nodes[i / 3] + i % 3], i == kc ? 1.0 : 0.0);
-  double u[24], w[24];
-  for (int i = 0; i < 24; i++) {
-    const int g = 6 * nodes[i / 6] + i % 6;
-    u[i] = vars[g];
-    w[i] = psi ? psi[g] : 0.0;
-  }
-  const double t = m.thick[e];
+  shell_xpt_load(m, e, vars, psi, dt, nodes);
   const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
-  double N[4], Na[4], Nb[4];
-  Dual Xxi[6];
-
-  // node normals (TacsShellComputeNodeNormals, TACSShellUtilities.h:301)
-  Dual fn[12];
-  for (int k = 0; k < 4; k++) {
-    shell_corner(k, N, Na, Nb);
-    grad3(Na, Nb, X, Xxi);
-    Dual a[3] = {Xxi[0], Xxi[2], Xxi[4]}, b[3] = {Xxi[1], Xxi[3], Xxi[5]};
-    Dual f[3];
-    cross3(a, b, f);
-    Dual nrm = sqrt(dot3(f, f));
-    if (nrm != 0.0) {
-      Dual sc = 1.0 / nrm;
-      f[0] *= sc; f[1] *= sc; f[2] *= sc;
-    }
-    fn[3 * k] = f[0]; fn[3 * k + 1] = f[1]; fn[3 * k + 2] = f[2];
-  }
-
-  // nodal drilling strains of u and psi (TacsShellComputeDrillStrain,
-  // TACSShellUtilities.h:651-790)
-  Dual ed_u[4], ed_w[4];
-  for (int k = 0; k < 4; k++) {
-    shell_corner(k, N, Na, Nb);
-    grad3(Na, Nb, X, Xxi);
-    const Dual *f = &fn[3 * k];
-    Dual Xdn[9], Tn[9], Xdinv[9], XdinvT[9], tmp[9], du0d[9], dCpt[9];
-    frame(Xxi, f, Xdn);
-    shell_transform(ep, Xxi, f, Tn);
-    inv3(Xdn, Xdinv);
-    mm3(Xdinv, Tn, XdinvT);
-    const double du0x[9] = {0.0, -0.5, 0.0, 0.5, 0.0, 0.0, 0.0, 0.0, 0.0};
-    mmT3(du0x, XdinvT, tmp);
-    mm3(Tn, tmp, du0d);
-    mm3(Tn, du0x, tmp);
-    mmT3(tmp, Tn, dCpt);
-    Dual su = 0.0, sw = 0.0;
-    for (int mm = 0; mm < 4; mm++)
-      for (int a = 0; a < 3; a++) {
-        const Dual v = Na[mm] * du0d[3 * a] + Nb[mm] * du0d[3 * a + 1];
-        su += v * u[6 * mm + a];
-        sw += v * w[6 * mm + a];
-      }
-    const Dual r3 = -(dCpt[7] - dCpt[5]), r4 = -(dCpt[2] - dCpt[6]),
-               r5 = -(dCpt[3] - dCpt[1]);
-    su += r3 * u[6 * k + 3] + r4 * u[6 * k + 4] + r5 * u[6 * k + 5];
-    sw += r3 * w[6 * k + 3] + r4 * w[6 * k + 4] + r5 * w[6 * k + 5];
-    ed_u[k] = su;
-    ed_w[k] = sw;
-  }
-
-  // tying strains of u and psi (TACSShellLinearModel::computeTyingStrain,
-  // TACSShellElementModel.h:28-73)
-  Dual ety_u[9], ety_w[9];
-  for (int ty = 0; ty < 9; ty++) {
-    Dual n0[3];
-    shape2(c_ty_pt[ty][0], c_ty_pt[ty][1], N, Na, Nb);
-    grad3(Na, Nb, X, Xxi);
-    interp3(N, fn, n0);
-    const int f = c_ty_field[ty];
-    Dual su = 0.0, sw = 0.0;
-    for (int mm = 0; mm < 4; mm++) {
-      for (int a = 0; a < 3; a++) {
-        Dual v;
-        if (f == 0) v = Na[mm] * Xxi[2 * a];
-        else if (f == 1) v = Nb[mm] * Xxi[2 * a + 1];
-        else if (f == 2)
-          v = 0.5 * (Na[mm] * Xxi[2 * a + 1] + Nb[mm] * Xxi[2 * a]);
-        else if (f == 3) v = 0.5 * n0[a] * Nb[mm];
-        else v = 0.5 * n0[a] * Na[mm];
-        su += v * u[6 * mm + a];
-        sw += v * w[6 * mm + a];
-      }
-      if (f >= 3) {
-        const int c = (f == 3) ? 1 : 0;
-        for (int b = 0; b < 3; b++) {
-          Dual acc = 0.0;
-          for (int i = 0; i < 3; i++)
-            acc += Xxi[2 * i + c] * dmap(&fn[3 * mm], i, b);
-          const Dual v = 0.5 * N[mm] * acc;
-          su += v * u[6 * mm + 3 + b];
-          sw += v * w[6 * mm + 3 + b];
-        }
-      }
-    }
-    ety_u[ty] = su;
-    ety_w[ty] = sw;
-  }
-
-  const ShellStiff cs = shell_stiff(ep, t);
-  Dual adj = 0.0, comp = 0.0;
-  double ks_d = 0.0;
-  for (int q = 0; q < 4; q++) {
-    const double xi = gauss2(q % 2), eta = gauss2(q / 2);
-    Dual n0[3], T[9], nxi[6], Xd[9], Xdz[9], Xdinv[9], nXX[9], P[9], Qm[9];
-    shape2(xi, eta, N, Na, Nb);
-    grad3(Na, Nb, X, Xxi);
-    interp3(N, fn, n0);
-    shell_transform(ep, Xxi, n0, T);
-    grad3(Na, Nb, fn, nxi);
-    frame(Xxi, n0, Xd);
-    Xdz[0] = nxi[0]; Xdz[1] = nxi[1]; Xdz[2] = 0.0;
-    Xdz[3] = nxi[2]; Xdz[4] = nxi[3]; Xdz[5] = 0.0;
-    Xdz[6] = nxi[4]; Xdz[7] = nxi[5]; Xdz[8] = 0.0;
-    const Dual det = inv3(Xd, Xdinv);
-    mm3(Xdinv, Xdz, nXX);
-    for (int i = 0; i < 9; i++) nXX[i] = -nXX[i];
-    mm3(Xdinv, T, P);
-    mm3(nXX, P, Qm);
-
-    Dual eu[9], ew[9];
-    // rows 0, 1, 2, 6, 7 from the tying strains (evalTyingInterp,
-    // TACSShellElementQuadBasis.h:552)
-    const double la0 = (xi - 1.0) * -0.5, la1 = (xi + 1.0) * 0.5;
-    const double lb0 = (eta - 1.0) * -0.5, lb1 = (eta + 1.0) * 0.5;
-    const double Nty[9] = {lb0, lb1, la0, la1, 1.0, la0, la1, lb0, lb1};
-    const int row_of[5] = {0, 1, 2, 6, 7};
-    for (int ri = 0; ri < 5; ri++) {
-      const int a = c_erc[ri][0], c = c_erc[ri][1];
-      Dual su = 0.0, sw = 0.0;
-      for (int ty = 0; ty < 9; ty++) {
-        const int i = c_ty_ij[c_ty_field[ty]][0], j = c_ty_ij[c_ty_field[ty]][1];
-        Dual pp = P[3 * i + a] * P[3 * j + c];
-        if (i != j) pp += P[3 * j + a] * P[3 * i + c];
-        const Dual mrt = c_efac[ri] * Nty[ty] * pp;
-        su += mrt * ety_u[ty];
-        sw += mrt * ety_w[ty];
-      }
-      eu[row_of[ri]] = su;
-      ew[row_of[ri]] = sw;
-    }
-    // row 8: drilling strain interpolated from the nodes
-    {
-      Dual su = 0.0, sw = 0.0;
-      for (int k = 0; k < 4; k++) {
-        su += N[k] * ed_u[k];
-        sw += N[k] * ed_w[k];
-      }
-      eu[8] = su;
-      ew[8] = sw;
-    }
-    // rows 3, 4, 5: bending (TACSShellLinearModel::evalStrain, .h:717-732)
-    {
-      Dual bu[3] = {0.0, 0.0, 0.0}, bw[3] = {0.0, 0.0, 0.0};
-      for (int mm = 0; mm < 4; mm++) {
-        const Dual cu0 = Na[mm] * Qm[0] + Nb[mm] * Qm[3];
-        const Dual cu1 = Na[mm] * Qm[1] + Nb[mm] * Qm[4];
-        const Dual cd0 = Na[mm] * P[0] + Nb[mm] * P[3] + N[mm] * Qm[6];
-        const Dual cd1 = Na[mm] * P[1] + Nb[mm] * P[4] + N[mm] * Qm[7];
-        for (int a = 0; a < 3; a++) {
-          const Dual v3 = T[3 * a] * cu0, v4 = T[3 * a + 1] * cu1;
-          const Dual v5 = T[3 * a] * cu1 + T[3 * a + 1] * cu0;
-          const double uu = u[6 * mm + a], ww = w[6 * mm + a];
-          bu[0] += v3 * uu; bu[1] += v4 * uu; bu[2] += v5 * uu;
-          bw[0] += v3 * ww; bw[1] += v4 * ww; bw[2] += v5 * ww;
-        }
-        for (int b = 0; b < 3; b++) {
-          Dual v3 = 0.0, v4 = 0.0, v5 = 0.0;
-          for (int aa = 0; aa < 3; aa++) {
-            const Dual dm = dmap(&fn[3 * mm], aa, b);
-            v3 += T[3 * aa] * cd0 * dm;
-            v4 += T[3 * aa + 1] * cd1 * dm;
-            v5 += (T[3 * aa] * cd1 + T[3 * aa + 1] * cd0) * dm;
-          }
-          const double uu = u[6 * mm + 3 + b], ww = w[6 * mm + 3 + b];
-          bu[0] += v3 * uu; bu[1] += v4 * uu; bu[2] += v5 * uu;
-          bw[0] += v3 * ww; bw[1] += v4 * ww; bw[2] += v5 * ww;
-        }
-      }
-      for (int r = 0; r < 3; r++) {
-        eu[3 + r] = bu[r];
-        ew[3 + r] = bw[r];
-      }
-    }
-
-    if (psi) {
-      Dual v = 0.0;
-      for (int r = 0; r < 9; r++) v += ew[r] * shell_stress_row(cs, eu, r);
-      adj += det * v;
-      if (m.pres) {
-        // TACSShellPressure: r_(mm,a) = -N_mm p detXd n0_a
-        double pr = 0.0;
-        for (int k = 0; k < 4; k++) pr += N[k] * m.pres[4 * e + k];
-        Dual wn = 0.0;
-        for (int mm = 0; mm < 4; mm++)
-          for (int a = 0; a < 3; a++) wn += (N[mm] * w[6 * mm + a]) * n0[a];
-        adj += lambda * (pr * -det * wn);
-      }
-    }
-    if (func >= 0) {
-      eu[8] = 0.0;  // point quantities exclude the drilling strain
-      if (func == TG_FUNC_COMPLIANCE) {
-        Dual sed = 0.0;
-        for (int r = 0; r < 9; r++) sed += eu[r] * shell_stress_row(cs, eu, r);
-        comp += det * sed;
-      } else {
-        const FailOutT<Dual> fo = shell_failure(ep, t, eu);
-        const double ex = ::exp(kk.weight * (fo.f.v - kk.max)) / kk.sum;
-        ks_d += ex / kk.weight * det.d + det.v * ex * fo.f.d;
-      }
-    }
-  }
-  double val = psi ? scale * adj.d : 0.0;
-  if (func == TG_FUNC_COMPLIANCE) val += coef * comp.d;
-  else if (func == TG_FUNC_KS_FAILURE) val += coef * ks_d;
+  const double val =
+      shell_xpt_forward(ep, dt, kc, func, kk, coef, scale, lambda);
   dfdX[3 * nodes[kc / 3] + kc % 3] += val;
+}
+
+__global__ void __launch_bounds__(128)
+    shell_xpt_rev_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                         const double *__restrict__ vars, int func,
+                         KsStats ks, double coef,
+                         const double *__restrict__ psi, double scale,
+                         double lambda, double *__restrict__ dfdX) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= cr.count) return;
+  const int e = cr.elem_list[idx];
+  ShellXptData dt;
+  int nodes[4];
+  shell_xpt_load(m, e, vars, psi, dt, nodes);
+  const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
+  double dX[12];
+  for (int i = 0; i < 12; i++) dX[i] = 0.0;
+  shell_xpt_reverse(ep, dt, func, kk, coef, scale, lambda, dX);
+  for (int i = 0; i < 12; i++) dfdX[3 * nodes[i / 3] + i % 3] += dX[i];
 }
 
 constexpr int kWarps = 4;
@@ -681,8 +492,13 @@ void launch_shell_dv(const ElemParams &ep, const MeshView &m,
 void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
                       const double *vars, int func, KsStats ks, double coef,
                       const double *psi, double scale, double lambda,
-                      double *dfdX, cudaStream_t s) {
+                      double *dfdX, int reverse, cudaStream_t s) {
   if (cr.count <= 0) return;
+  if (reverse) {
+    shell_xpt_rev_kernel<<<(unsigned)((cr.count + 127) / 128), 128, 0, s>>>(
+        ep, m, cr, vars, func, ks, coef, psi, scale, lambda, dfdX);
+    return;
+  }
   const long long n = 12LL * cr.count;
   shell_xpt_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
       ep, m, cr, vars, func, ks, coef, psi, scale, lambda, dfdX);

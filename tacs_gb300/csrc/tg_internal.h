@@ -10,22 +10,9 @@
 
 #include "../../include/tacs_gb300.h"
 #include "direct_view.h"
+#include "elem_params.h"
 
 namespace tg {
-
-// Material and element constants shared by every element of one assembler.
-struct ElemParams {
-  int elem_type;  // TG_ELEM_MITC4 / TG_ELEM_HEX8
-  double rho, E, nu, ys;
-  int transform;       // shells: 0 natural, 1 reference axis
-  double ref_axis[3];  // normalised reference axis
-};
-
-// KS aggregate statistics: max over the points and sum of w detXd
-// exp(weight (f - max)) (TACSKSFailure, src/functions/TACSKSFailure.cpp).
-struct KsStats {
-  double max, sum, weight;
-};
 
 // Device-side view of an assembler used by the element kernels.
 struct MeshView {
@@ -106,7 +93,7 @@ void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
 void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
                       const double *vars, int func, KsStats ks, double coef,
                       const double *psi, double scale, double lambda,
-                      double *dfdX, cudaStream_t s);
+                      double *dfdX, int reverse, cudaStream_t s);
 void launch_hex_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
                     const double *vars, int func, KsStats ks, double coef,
                     const double *psi, double scale, double lambda,

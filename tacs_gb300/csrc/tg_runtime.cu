@@ -560,12 +560,20 @@ static int xpt_pass(tg_assembler *a, const double *vars, int func, double coef,
   for (int c = 0; c < a->ncolors(); c++) {
     if (a->ep.elem_type == TG_ELEM_MITC4)
       launch_shell_xpt(a->ep, m, a->color(c), vars, func, a->ks, coef, psi,
-                       scale, lambda, dfdX, s);
+                       scale, lambda, dfdX, a->xpt_mode, s);
     else
       launch_hex_xpt(a->ep, m, a->color(c), vars, func, a->ks, coef, psi,
                      scale, lambda, dfdX, s);
   }
   TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_set_xpt_mode(tg_assembler *a, int mode) {
+  if (!a) return fail(TG_ERR_ARG, "tg_set_xpt_mode: NULL assembler");
+  if (mode != TG_XPT_FORWARD && mode != TG_XPT_REVERSE)
+    return fail(TG_ERR_ARG, "tg_set_xpt_mode: unknown mode");
+  a->xpt_mode = mode;
   return 0;
 }
 

@@ -370,6 +370,13 @@ class GpuModel:
         """Zero node vector, 3 per node (TACSAssembler::createNodeVec)."""
         return torch.zeros(3 * self.nnodes, dtype=torch.float64, device="cuda")
 
+    def set_xpt_mode(self, reverse):
+        """Shell coordinate derivatives by the reverse (adjoint) sweep, one
+        thread per element, instead of dual numbers per coordinate."""
+        check(_lib.lib().tg_set_xpt_mode(
+            self.handle, _lib.XPT_REVERSE if reverse else _lib.XPT_FORWARD),
+            "tg_set_xpt_mode")
+
     def add_xpt_sens(self, u, funcs, dfdX, coef=1.0):
         """dfdX[i] += coef d f_i / dX (TACSAssembler::addXptSens)."""
         f = np.ascontiguousarray(funcs, np.int32)

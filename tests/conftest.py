@@ -19,14 +19,22 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
     config.addinivalue_line(
         "markers", "direct: uses the direct (multifrontal) factorisation")
+    config.addinivalue_line(
+        "markers", "late: a newer kernel, run after the established tests")
+
+
+def _late(item):
+    return bool(item.get_closest_marker("direct")
+                or item.get_closest_marker("late"))
 
 
 def pytest_collection_modifyitems(session, config, items):
-    """Tests of the direct factorisation run after the others (stable
-    order otherwise): the iterative path's parity tests come first, so that
-    under -x a failure in the newer direct path cannot stop them."""
-    items[:] = ([i for i in items if i.get_closest_marker("direct") is None]
-                + [i for i in items if i.get_closest_marker("direct")])
+    """Tests of the direct factorisation and of other newer kernels run
+    after the others (stable order otherwise): the established parity tests
+    come first, so that under -x a failure in a newer path cannot stop
+    them."""
+    items[:] = ([i for i in items if not _late(i)]
+                + [i for i in items if _late(i)])
 
 
 def load_case(name):

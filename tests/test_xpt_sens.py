@@ -38,6 +38,82 @@ def test_oracle_xpt_against_reference(name):
                ref["adjxpt_test"]) < 1e-8
 
 
+# ------------------------------------ CPU: the two exact derivative forms
+@pytest.fixture(scope="module")
+def sx(tmp_path_factory):
+    """tacs_gb300/csrc/shell_xpt.cuh compiled for the host
+    (tests/cpp/shell_xpt_check.cpp)."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    from conftest import ROOT
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    out = str(tmp_path_factory.mktemp("sx") / "libsx.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I",
+                    os.path.join(ROOT, "tacs_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "cpp", "shell_xpt_check.cpp"),
+                    "-o", out], check=True)
+    lib = C.CDLL(out)
+    P = C.c_void_p
+    lib.sx_derivatives.argtypes = [P, P, P, P, C.c_double, P, C.c_int,
+                                   C.c_int, P, P, P, P]
+    return lib
+
+
+def _sx_elements(rng, n):
+    """Random shell elements: warped squares and patches of a cylinder."""
+    for k in range(n):
+        if k % 2:
+            X = (np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 1, 1, 0], float)
+                 * rng.uniform(0.3, 3.0) + rng.normal(0, 0.15, 12))
+        else:
+            R, th0, dth = rng.uniform(0.5, 3), rng.uniform(0, 6), 0.3
+            z0, dz = rng.uniform(-1, 1), rng.uniform(0.1, 0.5)
+            X = np.array([[R * np.cos(th0 + dth * i), R * np.sin(th0 + dth * i),
+                           z0 + dz * j] for j in (0, 1) for i in (0, 1)])
+            X = X.ravel() + rng.normal(0, 0.01, 12)
+        yield X
+
+
+@pytest.mark.parametrize("transform", [0, 1])
+@pytest.mark.parametrize("flags,func", [(1, -1), (3, -1), (0, 0), (0, 1),
+                                        (3, 0), (1, 1)])
+def test_shell_reverse_sweep_equals_dual_derivative(sx, transform, flags,
+                                                    func):
+    """The reverse (adjoint) sweep of shell_xpt.cuh gives the dual-number
+    derivative of every coordinate to rounding (1e-12 of the largest
+    entry): with and without the adjoint term (flags bit 0) and the
+    pressure load (bit 1), for no function, compliance and KS failure,
+    both transforms, on warped and curved elements."""
+    import ctypes as C
+    rng = np.random.default_rng(17 + 10 * transform + flags + 100 * (func + 1))
+    P = C.c_void_p
+
+    def ptr(a):
+        return a.ctypes.data_as(P)
+
+    for X in _sx_elements(rng, 12):
+        u = rng.normal(0, 2e-4, 24)
+        w = rng.normal(0, 1, 24)
+        pres = rng.uniform(5e2, 2e3, 4)
+        # reference axis near the element's first edge (never along its
+        # normal, where the transform is undefined)
+        axis = X[3:6] - X[0:3] + rng.normal(0, 0.1, 3)
+        axis /= np.linalg.norm(axis)
+        p = np.array([70e9, 0.3, 2.7e8, transform, *axis])
+        ks = np.array([0.05, 1.3, 100.0])
+        s = np.array([0.7, -1.3, 0.9])
+        f, r = np.zeros(12), np.zeros(12)
+        sx.sx_derivatives(ptr(p), ptr(np.ascontiguousarray(X)), ptr(u),
+                          ptr(w), rng.uniform(0.002, 0.02), ptr(pres), flags,
+                          func, ptr(ks), ptr(s), ptr(f), ptr(r))
+        assert np.abs(f).max() > 0
+        assert np.abs(f - r).max() < 1e-12 * np.abs(f).max()
+
+
 # ------------------------------------------------------------------- GPU
 @pytest.fixture(scope="module")
 def gpu():
@@ -73,6 +149,33 @@ def test_xpt_element_level(gpu, name):
     M.add_xpt_sens(u, [0], [xb], coef=3.0)
     expect = 3.0 * ref["dfdX_test_comp"] - 2.0 * ref["adjxpt_test"]
     assert rel(_h(xb), expect) < XPT_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.late
+@pytest.mark.parametrize("name", [c for c in XPT_CASES if "shell" in c])
+def test_shell_reverse_kernel_matches_reference(gpu, name):
+    """The reverse-sweep kernel (tg_set_xpt_mode TG_XPT_REVERSE): the
+    reference's complex-step values at element level (1e-10) and the
+    forward kernel's results (1e-12)."""
+    prob, ref = load_case(name)
+    M = gpu.GpuModel(prob)
+    u = M.vec(prob["u_test"])
+    M.eval_functions(u)
+    psi = M.vec(prob["psi_test"])
+    out = {}
+    for reverse in (False, True):
+        M.set_xpt_mode(reverse)
+        dc, dk, xa = M.node_vec(), M.node_vec(), M.node_vec()
+        M.add_xpt_sens(u, [0, 1], [dc, dk])
+        M.add_adjoint_res_xpt_products(u, [psi], [xa])
+        out[reverse] = [_h(dc), _h(dk), _h(xa)]
+    M.set_xpt_mode(False)
+    for got, key in zip(out[True], ("dfdX_test_comp", "dfdX_test_ks",
+                                    "adjxpt_test")):
+        assert rel(got, ref[key]) < XPT_TOL
+    for a, b in zip(out[True], out[False]):
+        assert rel(a, b) < 1e-12
 
 
 @pytest.mark.gpu
