@@ -234,6 +234,16 @@ def hex_section(torch, steps=5):
            "hbm_gbs_algorithmic": algo / (ms / 1e3) / 1e9,
            "algorithmic_bytes": int(algo),
            "fp64": fp64_roofline("hex", p["nelem"] / (ms / 1e3))}
+    # node-coordinate total derivatives at a seeded state and adjoint (the
+    # kernels' cost does not depend on the values)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    us = 1e-5 * torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                            generator=g)
+    ps = torch.randn(M.ndof, dtype=torch.float64, device="cuda", generator=g)
+    out["shape_derivative"] = xpt_timing(M, {"u": us, "psis": [ps, ps]},
+                                         torch, reps=2)
+    out["shape_derivative"]["workload"] = (
+        "hex8 block 128x128x64: df/dX - psi^T dR/dX of compliance and KS")
     del M, mat, u, res
     torch.cuda.empty_cache()
     return out

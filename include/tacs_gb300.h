@@ -227,11 +227,10 @@ int tg_add_total_xpt_derivative(tg_assembler *a, const double *vars, int func,
                                 double coef, const double *psi, double scale,
                                 double *dfdX, void *stream);
 
-/* How the shell element's coordinate derivatives above are formed (no
-   reference counterpart; both are exact): TG_XPT_FORWARD (default) dual
-   arithmetic, one thread per element coordinate; TG_XPT_REVERSE a
-   hand-written adjoint sweep, one thread per element.  Hex elements have
-   one form. */
+/* How the element coordinate derivatives above are formed (no reference
+   counterpart; both are exact): TG_XPT_FORWARD (default) dual arithmetic,
+   one thread per element coordinate; TG_XPT_REVERSE a hand-written
+   adjoint sweep, one thread per element. */
 #define TG_XPT_FORWARD 0
 #define TG_XPT_REVERSE 1
 int tg_set_xpt_mode(tg_assembler *a, int mode);

@@ -16,7 +16,7 @@
 namespace tg {
 namespace {
 
-#define TG_GPT 0.577350269189626
+#include "hex_common.cuh"
 
 struct HexSmem {
   double X[24];
@@ -33,73 +33,11 @@ struct HexSmem {
   int slot[64];
 };
 
-__device__ __forceinline__ double gauss2(int i) {
-  return i ? TG_GPT : -TG_GPT;
-}
-
-template <class R>
-__device__ R inv3(const R *A, R *Ai) {
-  R det = (A[8] * (A[0] * A[4] - A[3] * A[1]) -
-           A[7] * (A[0] * A[5] - A[3] * A[2]) +
-           A[6] * (A[1] * A[5] - A[2] * A[4]));
-  R di = 1.0 / det;
-  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * di;
-  Ai[1] = -(A[1] * A[8] - A[2] * A[7]) * di;
-  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * di;
-  Ai[3] = -(A[3] * A[8] - A[5] * A[6]) * di;
-  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * di;
-  Ai[5] = -(A[0] * A[5] - A[2] * A[3]) * di;
-  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * di;
-  Ai[7] = -(A[0] * A[7] - A[1] * A[6]) * di;
-  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * di;
-  return det;
-}
-
-// TACSLinearHexaBasis::computeBasis / computeBasisGradient
-// (src/elements/basis/TACSHexaBasis.cpp:137-170), node m = i + 2j + 4k
-__device__ __forceinline__ void hex_shape(const double *pt, double *N,
-                                          double *Nxi) {
-  double x[2] = {1.0 - pt[0], 1.0 + pt[0]};
-  double y[2] = {1.0 - pt[1], 1.0 + pt[1]};
-  double z[2] = {1.0 - pt[2], 1.0 + pt[2]};
-#pragma unroll
-  for (int m = 0; m < 8; m++) {
-    const int i = m & 1, j = (m >> 1) & 1, k = m >> 2;
-    const double si = i ? 1.0 : -1.0, sj = j ? 1.0 : -1.0, sk = k ? 1.0 : -1.0;
-    if (N) N[m] = 0.125 * x[i] * y[j] * z[k];
-    Nxi[3 * m] = 0.125 * si * y[j] * z[k];
-    Nxi[3 * m + 1] = 0.125 * x[i] * sj * z[k];
-    Nxi[3 * m + 2] = 0.125 * x[i] * y[j] * sk;
-  }
-}
-
 __device__ __constant__ unsigned char c_pair[36][2] = {
     {0, 0}, {0, 1}, {0, 2}, {0, 3}, {0, 4}, {0, 5}, {0, 6}, {0, 7}, {1, 1},
     {1, 2}, {1, 3}, {1, 4}, {1, 5}, {1, 6}, {1, 7}, {2, 2}, {2, 3}, {2, 4},
     {2, 5}, {2, 6}, {2, 7}, {3, 3}, {3, 4}, {3, 5}, {3, 6}, {3, 7}, {4, 4},
     {4, 5}, {4, 6}, {4, 7}, {5, 5}, {5, 6}, {5, 7}, {6, 6}, {6, 7}, {7, 7}};
-
-struct HexC {
-  double c0, c1, G;
-};
-// TACSMaterialProperties::evalTangentStiffness3D, isotropic branch
-__device__ __forceinline__ HexC hex_c(const ElemParams &ep) {
-  HexC c;
-  double D = ep.E / ((1.0 + ep.nu) * (1.0 - 2.0 * ep.nu));
-  c.c0 = (1.0 - ep.nu) * D;
-  c.c1 = ep.nu * D;
-  c.G = 0.5 * ep.E / (1.0 + ep.nu);
-  return c;
-}
-template <class R>
-__device__ __forceinline__ void hex_Ce(const HexC &c, const R *e, R *s) {
-  s[0] = c.c0 * e[0] + c.c1 * e[1] + c.c1 * e[2];
-  s[1] = c.c1 * e[0] + c.c0 * e[1] + c.c1 * e[2];
-  s[2] = c.c1 * e[0] + c.c1 * e[1] + c.c0 * e[2];
-  s[3] = c.G * e[3];
-  s[4] = c.G * e[4];
-  s[5] = c.G * e[5];
-}
 
 __device__ __forceinline__ int find_slot(const int *rowp, const int *cols,
                                          int row, int col) {
@@ -189,45 +127,6 @@ __device__ __forceinline__ double hex_bts(const HexSmem &S, int q, int mm,
   if (i == 0) return g[0] * s[0] + g[1] * s[5] + g[2] * s[4];
   if (i == 1) return g[1] * s[1] + g[0] * s[5] + g[2] * s[3];
   return g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
-}
-
-// Face quadrature point n of face `face`: shape functions N and the area
-// element |t1 x t2| (TACSElementBasis::getFaceNormal,
-// TACSElementBasis.cpp:37-63; face tangents TACSHexaBasis.cpp:21-70).
-template <class R>
-__device__ R hex_face_point(const R *X, int face, int n, double *N) {
-  const int f2 = face >> 1;
-  const double u = gauss2(n & 1), v = gauss2(n >> 1);
-  const double cc = -1.0 + 2.0 * (face & 1);
-  double pt[3];
-  if (f2 == 0) { pt[0] = cc; pt[1] = u; pt[2] = v; }
-  else if (f2 == 1) { pt[0] = u; pt[1] = cc; pt[2] = v; }
-  else { pt[0] = u; pt[1] = v; pt[2] = cc; }
-  double Nxi[24];
-  R Xd[9];
-  hex_shape(pt, N, Nxi);
-  for (int ii = 0; ii < 3; ii++)
-    for (int jj = 0; jj < 3; jj++) {
-      R s = 0.0;
-      for (int q = 0; q < 8; q++) s += Nxi[3 * q + jj] * X[3 * q + ii];
-      Xd[3 * ii + jj] = s;
-    }
-  int ta, tb;
-  if (f2 == 0) { ta = 2; tb = 1; }
-  else if (f2 == 1) { ta = 0; tb = 2; }
-  else { ta = 1; tb = 0; }
-  if (face == 1) { ta = 1; tb = 2; }
-  if (face == 3) { ta = 2; tb = 0; }
-  if (face == 5) { ta = 0; tb = 1; }
-  R t1[3], t2[3];
-  for (int ii = 0; ii < 3; ii++) {
-    t1[ii] = Xd[3 * ii + ta];
-    t2[ii] = Xd[3 * ii + tb];
-  }
-  const R nr[3] = {t1[1] * t2[2] - t1[2] * t2[1],
-                   t1[2] * t2[0] - t1[0] * t2[2],
-                   t1[0] * t2[1] - t1[1] * t2[0]};
-  return sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
 }
 
 // Face-traction residual of one element for node a, direction i
@@ -423,15 +322,6 @@ __global__ void __launch_bounds__(64)
 
 // TACSSolidConstitutive::evalFailure (TACSSolidConstitutive.cpp:274-300)
 // with vonMisesFailure3D: the von Mises stress of C e over ys
-template <class R>
-__device__ R hex_vm(const ElemParams &ep, const R *s) {
-  return sqrt(0.5 * ((s[0] - s[1]) * (s[0] - s[1]) +
-                     (s[0] - s[2]) * (s[0] - s[2]) +
-                     (s[1] - s[2]) * (s[1] - s[2]) +
-                     6.0 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]))) /
-         ep.ys;
-}
-
 struct HexFail {
   double f, dfde[6];
 };
@@ -586,15 +476,38 @@ __global__ void __launch_bounds__(WARPS * 32)
 
 // ---------------------------------------------------------------------------
 // Node-coordinate sensitivities (TACSElement3D::addAdjResXptProduct and
-// addPointQuantityXptSens, TACSElement3D.cpp:260-300,618-660; the traction
-// load through TACSElement::addAdjResXptProduct, TACSElement.cpp:270).
-// One thread per (element, nodal coordinate k) with dX_k = 1 in dual
-// arithmetic:
-//   psi^T R_e = sum_q detXd_q t e_q(psi) . C e_q(u)
-//               + lambda sum_faces sum_n area_n N_n . (-traction) . psi
-//   compliance = sum_q detXd_q e_q . t C e_q;  KS as for the shell, with the
-//   failure value vonMises(C e)/ys.
-using ad::Dual;
+// addPointQuantityXptSens): per element, d/dX of scale psi^T R_e + coef f_e
+// (elasticity residual and face tractions; compliance or KS failure
+// terms), defined in hex_xpt.cuh in two exact forms: forward (dual
+// numbers, hex_xpt_kernel, one thread per element coordinate) and reverse
+// (a hand-written adjoint sweep, hex_xpt_rev_kernel, one thread per
+// element).  Both scatter colour by colour without atomics.
+#include "hex_xpt.cuh"
+
+__device__ __forceinline__ void hex_xpt_load(const MeshView &m, int e,
+                                             const double *vars,
+                                             const double *psi,
+                                             HexXptData &dt, int *nodes) {
+  for (int i = 0; i < 8; i++) nodes[i] = m.conn[8 * e + i];
+  for (int i = 0; i < 24; i++) {
+    const int g = 3 * nodes[i / 3] + i % 3;
+    dt.X[i] = m.xpts[g];
+    dt.u[i] = vars[g];
+    dt.w[i] = psi ? psi[g] : 0.0;
+  }
+  dt.t = m.thick[e];
+  dt.has_psi = psi != nullptr;
+  if (m.trac_ptr) {
+    const int t0 = m.trac_ptr[e];
+    dt.ntrac = m.trac_ptr[e + 1] - t0;
+    dt.trac_face = m.trac_face + t0;
+    dt.trac_val = m.trac_val + 3 * t0;
+  } else {
+    dt.ntrac = 0;
+    dt.trac_face = nullptr;
+    dt.trac_val = nullptr;
+  }
+}
 
 __global__ void __launch_bounds__(128)
     hex_xpt_kernel(ElemParams ep, MeshView m, ColorRange cr,
@@ -604,86 +517,32 @@ __global__ void __launch_bounds__(128)
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= 24LL * cr.count) return;
   const int e = cr.elem_list[idx / 24], kc = (int)(idx % 24);
+  HexXptData dt;
   int nodes[8];
-  for (int i = 0; i < 8; i++) nodes[i] = m.conn[8 * e + i];
-  Dual X[24];
-  double u[24], w[24];
-  for (int i = 0; i < 24; i++) {
-    const int g = 3 * nodes[i / 3] + i % 3;
-    X[i] = Dual(m.xpts[g], i == kc ? 1.0 : 0.0);
-    u[i] = vars[g];
-    w[i] = psi ? psi[g] : 0.0;
-  }
-  const double t = m.thick[e];
+  hex_xpt_load(m, e, vars, psi, dt, nodes);
   const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
-  const HexC c = hex_c(ep);
-  Dual adj = 0.0, comp = 0.0;
-  double ks_d = 0.0;
-  for (int q = 0; q < 8; q++) {
-    const double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1), gauss2(q >> 2)};
-    double Nxi[24];
-    hex_shape(pt, nullptr, Nxi);
-    Dual Xd[9], J[9];
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) {
-        Dual v = 0.0;
-        for (int mm = 0; mm < 8; mm++) v += Nxi[3 * mm + j] * X[3 * mm + i];
-        Xd[3 * i + j] = v;
-      }
-    const Dual det = inv3(Xd, J);
-    Dual Uu[9], Uw[9];
-    for (int i = 0; i < 9; i++) Uu[i] = Uw[i] = 0.0;
-    for (int mm = 0; mm < 8; mm++) {
-      const double n0 = Nxi[3 * mm], n1 = Nxi[3 * mm + 1], n2 = Nxi[3 * mm + 2];
-      Dual g[3];
-      for (int cc = 0; cc < 3; cc++)
-        g[cc] = n0 * J[cc] + n1 * J[3 + cc] + n2 * J[6 + cc];
-      for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-          Uu[3 * i + j] += u[3 * mm + i] * g[j];
-          Uw[3 * i + j] += w[3 * mm + i] * g[j];
-        }
-    }
-    const Dual eu[6] = {Uu[0], Uu[4], Uu[8], Uu[5] + Uu[7], Uu[2] + Uu[6],
-                        Uu[1] + Uu[3]};
-    Dual s[6];
-    hex_Ce(c, eu, s);
-    if (psi) {
-      const Dual ew[6] = {Uw[0], Uw[4], Uw[8], Uw[5] + Uw[7], Uw[2] + Uw[6],
-                          Uw[1] + Uw[3]};
-      Dual v = 0.0;
-      for (int k = 0; k < 6; k++) v += ew[k] * s[k];
-      adj += det * t * v;
-    }
-    if (func == TG_FUNC_COMPLIANCE) {
-      Dual v = 0.0;
-      for (int k = 0; k < 6; k++) v += eu[k] * (s[k] * t);
-      comp += det * v;
-    } else if (func == TG_FUNC_KS_FAILURE) {
-      const Dual f = hex_vm(ep, s);
-      const double ex = ::exp(kk.weight * (f.v - kk.max)) / kk.sum;
-      ks_d += ex / kk.weight * det.d + det.v * ex * f.d;
-    }
-  }
-  if (psi && m.trac_ptr && lambda != 0.0) {
-    for (int tk = m.trac_ptr[e]; tk < m.trac_ptr[e + 1]; tk++) {
-      const int face = m.trac_face[tk];
-      const double *tr = &m.trac_val[3 * tk];
-      for (int n = 0; n < 4; n++) {
-        double N[8];
-        const Dual area = hex_face_point(X, face, n, N);
-        double pw = 0.0;
-        for (int a = 0; a < 8; a++)
-          pw += N[a] * (-tr[0] * w[3 * a] - tr[1] * w[3 * a + 1] -
-                        tr[2] * w[3 * a + 2]);
-        adj += lambda * (area * pw);
-      }
-    }
-  }
-  double val = psi ? scale * adj.d : 0.0;
-  if (func == TG_FUNC_COMPLIANCE) val += coef * comp.d;
-  else if (func == TG_FUNC_KS_FAILURE) val += coef * ks_d;
+  const double val =
+      hex_xpt_forward(ep, dt, kc, func, kk, coef, scale, lambda);
   dfdX[3 * nodes[kc / 3] + kc % 3] += val;
+}
+
+__global__ void __launch_bounds__(128)
+    hex_xpt_rev_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                       const double *__restrict__ vars, int func, KsStats ks,
+                       double coef, const double *__restrict__ psi,
+                       double scale, double lambda,
+                       double *__restrict__ dfdX) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= cr.count) return;
+  const int e = cr.elem_list[idx];
+  HexXptData dt;
+  int nodes[8];
+  hex_xpt_load(m, e, vars, psi, dt, nodes);
+  const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
+  double dX[24];
+  for (int i = 0; i < 24; i++) dX[i] = 0.0;
+  hex_xpt_reverse(ep, dt, func, kk, coef, scale, lambda, dX);
+  for (int i = 0; i < 24; i++) dfdX[3 * nodes[i / 3] + i % 3] += dX[i];
 }
 
 constexpr int kWarps = 8;
@@ -748,8 +607,13 @@ void launch_hex_dv(const ElemParams &ep, const MeshView &m, const double *vars,
 void launch_hex_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
                     const double *vars, int func, KsStats ks, double coef,
                     const double *psi, double scale, double lambda,
-                    double *dfdX, cudaStream_t s) {
+                    double *dfdX, int reverse, cudaStream_t s) {
   if (cr.count <= 0) return;
+  if (reverse) {
+    hex_xpt_rev_kernel<<<(unsigned)((cr.count + 127) / 128), 128, 0, s>>>(
+        ep, m, cr, vars, func, ks, coef, psi, scale, lambda, dfdX);
+    return;
+  }
   const long long n = 24LL * cr.count;
   hex_xpt_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
       ep, m, cr, vars, func, ks, coef, psi, scale, lambda, dfdX);

@@ -97,7 +97,7 @@ void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
 void launch_hex_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,
                     const double *vars, int func, KsStats ks, double coef,
                     const double *psi, double scale, double lambda,
-                    double *dfdX, cudaStream_t s);
+                    double *dfdX, int reverse, cudaStream_t s);
 
 // ------------------------------------------------------- BCSR / vectors
 // nrhs vectors ld apart (ld may be 0 when nrhs == 1)

@@ -77,7 +77,7 @@ struct tg_assembler {
   int npart = 512;
   KsStats ks{0.0, 1.0, 100.0};
   bool ks_valid = false;
-  // shell node-coordinate derivatives: 0 forward (dual), 1 reverse
+  // node-coordinate derivatives: 0 forward (dual), 1 reverse sweep
   int xpt_mode = 0;
   // element segments (independent meshes): contiguous element ranges
   int nseg = 0;

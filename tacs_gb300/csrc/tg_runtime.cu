@@ -563,7 +563,7 @@ static int xpt_pass(tg_assembler *a, const double *vars, int func, double coef,
                        scale, lambda, dfdX, a->xpt_mode, s);
     else
       launch_hex_xpt(a->ep, m, a->color(c), vars, func, a->ks, coef, psi,
-                     scale, lambda, dfdX, s);
+                     scale, lambda, dfdX, a->xpt_mode, s);
   }
   TG_CUDA(cudaGetLastError());
   return 0;

@@ -371,8 +371,8 @@ class GpuModel:
         return torch.zeros(3 * self.nnodes, dtype=torch.float64, device="cuda")
 
     def set_xpt_mode(self, reverse):
-        """Shell coordinate derivatives by the reverse (adjoint) sweep, one
-        thread per element, instead of dual numbers per coordinate."""
+        """Element coordinate derivatives by the reverse (adjoint) sweep,
+        one thread per element, instead of dual numbers per coordinate."""
         check(_lib.lib().tg_set_xpt_mode(
             self.handle, _lib.XPT_REVERSE if reverse else _lib.XPT_FORWARD),
             "tg_set_xpt_mode")

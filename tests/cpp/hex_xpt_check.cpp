@@ -1,0 +1,60 @@
+// CPU check of the hex8 node-coordinate derivative
+// (tacs_gb300/csrc/hex_xpt.cuh): the same device functions compiled for the
+// host, the reverse sweep against the dual-number forward derivative of
+// every coordinate.  Built by tests/test_xpt_sens.py with g++ and called
+// through ctypes; test infrastructure only.
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __constant__
+#include <cmath>
+
+#include "../../include/tacs_gb300.h"
+#include "dual.cuh"
+#include "elem_params.h"
+
+namespace tg {
+namespace {
+#include "hex_common.cuh"
+#include "hex_xpt.cuh"
+}  // namespace
+}  // namespace tg
+
+extern "C" {
+
+// p: E, nu, ys; ks: max, sum, weight; s: coef, scale, lambda; faces /
+// tvals: ntrac face tractions.  has_psi: the adjoint term is present.
+// fwd[24]: forward derivative per coordinate; rev[24]: the reverse sweep.
+void hx_derivatives(const double *p, const double *X, const double *u,
+                    const double *w, double t, int has_psi, int ntrac,
+                    const int *faces, const double *tvals, int func,
+                    const double *ks, const double *s, double *fwd,
+                    double *rev) {
+  tg::ElemParams ep;
+  ep.elem_type = TG_ELEM_HEX8;
+  ep.rho = 2700.0;
+  ep.E = p[0];
+  ep.nu = p[1];
+  ep.ys = p[2];
+  ep.transform = 0;
+  ep.ref_axis[0] = 1.0;
+  ep.ref_axis[1] = ep.ref_axis[2] = 0.0;
+  tg::HexXptData dt;
+  for (int i = 0; i < 24; i++) {
+    dt.X[i] = X[i];
+    dt.u[i] = u[i];
+    dt.w[i] = w[i];
+  }
+  dt.t = t;
+  dt.has_psi = has_psi != 0;
+  dt.ntrac = ntrac;
+  dt.trac_face = faces;
+  dt.trac_val = tvals;
+  const tg::KsStats kk{ks[0], ks[1], ks[2]};
+  for (int kc = 0; kc < 24; kc++)
+    fwd[kc] = tg::hex_xpt_forward(ep, dt, kc, func, kk, s[0], s[1], s[2]);
+  for (int i = 0; i < 24; i++) rev[i] = 0.0;
+  tg::hex_xpt_reverse(ep, dt, func, kk, s[0], s[1], s[2], rev);
+}
+
+}  // extern "C"
