@@ -18,6 +18,8 @@ XPT_FORWARD, XPT_REVERSE = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 FUNC_COMPLIANCE, FUNC_KS_FAILURE = 0, 1
 
+ERR_ARG, ERR_CUDA, ERR_STATE, ERR_PIVOT, ERR_NOCONV, ERR_NONFINITE = \
+    -1, -2, -3, -4, -5, -6
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "bad call order",
           -4: "zero pivot", -5: "no convergence", -6: "non-finite value"}
 

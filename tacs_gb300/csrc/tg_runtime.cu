@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "mesh_graph.h"
 #include "tg_objects.h"
 
 namespace tg {
@@ -109,9 +110,10 @@ int tg_assembler_add_bcs(tg_assembler *a, int n, const int *nodes,
     return fail(TG_ERR_ARG, "tg_assembler_add_bcs: bad arguments");
   if (a->initialized)
     return fail(TG_ERR_STATE, "tg_assembler_add_bcs after initialize");
-  for (int i = 0; i < n; i++) {
+  for (int i = 0; i < n; i++)  // validate before changing anything
     if (nodes[i] < 0 || nodes[i] >= a->nnodes)
       return fail(TG_ERR_ARG, "tg_assembler_add_bcs: node out of range");
+  for (int i = 0; i < n; i++) {
     // merge with an existing entry for the node (TACSBcMap::addBC)
     bool merged = false;
     for (size_t k = 0; k < a->bc_nodes_h.size(); k++)
@@ -131,12 +133,10 @@ int tg_assembler_add_bcs(tg_assembler *a, int n, const int *nodes,
 int tg_assembler_set_element_dvs(tg_assembler *a, const double *t,
                                  const int *dvnum) {
   if (!a) return fail(TG_ERR_ARG, "NULL assembler");
+  if (dvnum && a->initialized)
+    return fail(TG_ERR_STATE, "design-variable numbers after initialize");
   if (t) a->thick_h.assign(t, t + a->nelem);
-  if (dvnum) {
-    if (a->initialized)
-      return fail(TG_ERR_STATE, "design-variable numbers after initialize");
-    a->dvnum_h.assign(dvnum, dvnum + a->nelem);
-  }
+  if (dvnum) a->dvnum_h.assign(dvnum, dvnum + a->nelem);
   if (a->initialized && t) {
     cudaError_t e = cudaMemcpy(a->d_thick, a->thick_h.data(),
                                a->nelem * sizeof(double),
@@ -154,12 +154,12 @@ int tg_assembler_set_pressure(tg_assembler *a, int n, const int *elems,
     return fail(TG_ERR_ARG, "pressure loads are defined for shells");
   if (a->initialized)
     return fail(TG_ERR_STATE, "tg_assembler_set_pressure after initialize");
-  a->pres_h.assign((size_t)4 * a->nelem, 0.0);
-  for (int k = 0; k < n; k++) {
+  for (int k = 0; k < n; k++)  // validate before changing anything
     if (elems[k] < 0 || elems[k] >= a->nelem)
       return fail(TG_ERR_ARG, "pressure element out of range");
+  a->pres_h.assign((size_t)4 * a->nelem, 0.0);
+  for (int k = 0; k < n; k++)
     for (int j = 0; j < 4; j++) a->pres_h[4 * elems[k] + j] += vals[4 * k + j];
-  }
   a->has_pres = n > 0;
   return 0;
 }
@@ -172,6 +172,9 @@ int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems,
     return fail(TG_ERR_ARG, "face tractions are defined for hex elements");
   if (a->initialized)
     return fail(TG_ERR_STATE, "tg_assembler_set_traction after initialize");
+  for (int k = 0; k < n; k++)  // validate before changing anything
+    if (elems[k] < 0 || elems[k] >= a->nelem || faces[k] < 0 || faces[k] > 5)
+      return fail(TG_ERR_ARG, "traction element/face out of range");
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
@@ -179,11 +182,7 @@ int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems,
   a->trac_ptr_h.assign(a->nelem + 1, 0);
   a->trac_face_h.clear();
   a->trac_val_h.clear();
-  for (int k = 0; k < n; k++) {
-    if (elems[k] < 0 || elems[k] >= a->nelem || faces[k] < 0 || faces[k] > 5)
-      return fail(TG_ERR_ARG, "traction element/face out of range");
-    a->trac_ptr_h[elems[k] + 1]++;
-  }
+  for (int k = 0; k < n; k++) a->trac_ptr_h[elems[k] + 1]++;
   for (int e = 0; e < a->nelem; e++) a->trac_ptr_h[e + 1] += a->trac_ptr_h[e];
   for (int k : order) {
     a->trac_face_h.push_back(faces[k]);
@@ -192,64 +191,26 @@ int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems,
   return 0;
 }
 
-// Node-to-node pattern with the diagonal, sorted columns
-// (TACSAssembler::createMat / computeLocalNodeToNodeCSR).
-static void build_pattern(tg_assembler *a) {
-  const int nn = a->nnodes, npe = a->npe;
-  std::vector<std::vector<int>> adj(nn);
-  for (int i = 0; i < nn; i++) adj[i].push_back(i);
-  for (int e = 0; e < a->nelem; e++)
-    for (int i = 0; i < npe; i++)
-      for (int j = 0; j < npe; j++)
-        adj[a->conn_h[npe * e + i]].push_back(a->conn_h[npe * e + j]);
-  a->rowp_h.assign(nn + 1, 0);
-  a->cols_h.clear();
-  a->diag_h.assign(nn, -1);
-  for (int i = 0; i < nn; i++) {
-    auto &r = adj[i];
-    std::sort(r.begin(), r.end());
-    r.erase(std::unique(r.begin(), r.end()), r.end());
-    for (int c : r) {
-      if (c == i) a->diag_h[i] = (int)a->cols_h.size();
-      a->cols_h.push_back(c);
-    }
-    a->rowp_h[i + 1] = (int)a->cols_h.size();
-    std::vector<int>().swap(r);
-  }
-}
-
-// Greedy element colouring: no two elements of one colour share a node.
-static int build_coloring(tg_assembler *a) {
-  const int npe = a->npe;
-  std::vector<uint64_t> used(a->nnodes, 0);
-  std::vector<int> color(a->nelem, 0);
-  int ncol = 0;
-  for (int e = 0; e < a->nelem; e++) {
-    uint64_t m = 0;
-    for (int i = 0; i < npe; i++) m |= used[a->conn_h[npe * e + i]];
-    int c = 0;
-    while (c < 64 && (m >> c) & 1ull) c++;
-    if (c >= 64) return fail(TG_ERR_ARG, "element colouring needs > 64 colours");
-    color[e] = c;
-    ncol = std::max(ncol, c + 1);
-    for (int i = 0; i < npe; i++) used[a->conn_h[npe * e + i]] |= (1ull << c);
-  }
+// Element colouring (mesh_graph.h): no two elements of one colour share a
+// node; the colours' element lists in element order.
+static void build_coloring(tg_assembler *a) {
+  std::vector<int> color;
+  const int ncol = graph::color_elements(a->nnodes, a->npe, a->nelem,
+                                         a->conn_h.data(), color);
   a->color_ptr_h.assign(ncol + 1, 0);
   for (int e = 0; e < a->nelem; e++) a->color_ptr_h[color[e] + 1]++;
   for (int c = 0; c < ncol; c++) a->color_ptr_h[c + 1] += a->color_ptr_h[c];
   a->color_elems_h.assign(a->nelem, 0);
   std::vector<int> fill(a->color_ptr_h.begin(), a->color_ptr_h.end() - 1);
   for (int e = 0; e < a->nelem; e++) a->color_elems_h[fill[color[e]]++] = e;
-  if (ncol == 0) a->color_ptr_h.assign(1, 0);
-  return 0;
 }
-
 int tg_assembler_initialize(tg_assembler *a) {
   if (!a) return fail(TG_ERR_ARG, "NULL assembler");
   if (a->initialized) return fail(TG_ERR_STATE, "already initialised");
-  build_pattern(a);
-  int rc = build_coloring(a);
-  if (rc) return rc;
+  graph::node_pattern(a->nnodes, a->npe, a->nelem, a->conn_h.data(),
+                      a->rowp_h, a->cols_h, a->diag_h);
+  build_coloring(a);
+  int rc = 0;
   // design-variable -> elements map (element order)
   a->ndv = 0;
   for (int d : a->dvnum_h) a->ndv = std::max(a->ndv, d + 1);
@@ -1120,20 +1081,9 @@ static int pc_create(tg_mat *A, int type, int lev_fill, int precision,
     // neighbours, so with the nodes ordered by colour the ILU(0) factor and
     // both triangular solves proceed one colour at a time
     const int nn = a->nnodes;
-    std::vector<int> color(nn, -1);
-    int ncol = 0;
-    for (int i = 0; i < nn; i++) {
-      uint64_t used = 0;
-      for (int j = a->rowp_h[i]; j < a->rowp_h[i + 1]; j++) {
-        int c = color[a->cols_h[j]];
-        if (c >= 0 && c < 64) used |= (1ull << c);
-      }
-      int c = 0;
-      while (c < 64 && ((used >> c) & 1ull)) c++;
-      color[i] = c;
-      ncol = std::max(ncol, c + 1);
-    }
-    pc->ncolors = ncol;
+    std::vector<int> color;
+    pc->ncolors = graph::color_nodes(nn, a->rowp_h.data(), a->cols_h.data(),
+                                     color);
     std::vector<int> perm(nn), iperm(nn);
     std::iota(perm.begin(), perm.end(), 0);
     std::stable_sort(perm.begin(), perm.end(),
