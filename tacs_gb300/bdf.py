@@ -63,14 +63,17 @@ def _cards(lines):
             card = (head.upper().rstrip("*"), parts[1:])
             continue
         head = line[:8].strip()
-        large = head.endswith("*")
-        width = 16 if large else 8
         if head.startswith("+") or head.startswith("*") or head == "":
+            # continuation: 16-character fields after a large-field marker
+            # ("*..."), 8-character ones otherwise; columns 9-72 either way
             if card is not None:
-                body = line[8:8 + (64 if not large else 64)]
+                width = 16 if head.startswith("*") else 8
+                body = line[8:72]
                 card[1].extend(body[k:k + width]
                                for k in range(0, len(body), width))
             continue
+        large = head.endswith("*")
+        width = 16 if large else 8
         if card is not None:
             yield card
         body = line[8:72]

@@ -45,7 +45,26 @@ FORCE,1,6,0,10.,0.,0.,-1.
 """
 
 
-@pytest.mark.parametrize("text", [SMALL, FREE], ids=["small", "free"])
+def _large_grid(gid, cp, x, y, z):
+    """GRID* in large-field format: 16-character fields, the z coordinate
+    on a '*' continuation line."""
+    def f16(v):
+        return f"{v:>16}"
+    return (f"{'GRID*':<8}{f16(gid)}{f16(cp)}{f16(x)}{f16(y)}*G{gid}\n"
+            f"{'*G' + str(gid):<8}{f16(z)}\n")
+
+
+LARGE = "".join(_large_grid(i + 1, "", x, y, "0.25") for i, (x, y) in enumerate(
+    [("0.", "0."), (".5", "0."), ("1.0", "0."), ("0.", "1.0"), (".5", "1."),
+     ("1.0", "1.0")])) + """CQUAD4        11       1       1       2       5       4
+CQUAD4        12       1       2       3       6       5
+SPC1           1     123       1       4
+FORCE          1       6       0    10.0      0.      0.     -1.
+"""
+
+
+@pytest.mark.parametrize("text", [SMALL, FREE, LARGE],
+                         ids=["small", "free", "large"])
 def test_bdf_cards(tmp_path, text):
     f = tmp_path / "m.bdf"
     f.write_text(text)
@@ -54,6 +73,8 @@ def test_bdf_cards(tmp_path, text):
     xyz = p["xpts"].reshape(-1, 3)
     if text is SMALL:  # CORD2R 5: origin (1, 0, 0), basic axes
         xyz = xyz - np.array([1.0, 0.0, 0.0])
+    if text is LARGE:  # the plate at z = 0.25 (z on the continuation)
+        xyz = xyz - np.array([0.0, 0.0, 0.25])
     assert np.allclose(xyz, ref["xpts"].reshape(-1, 3))
     assert np.array_equal(p["conn"], ref["conn"])
     assert list(p["bc_nodes"]) == [0, 3]
