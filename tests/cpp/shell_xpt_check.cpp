@@ -55,3 +55,48 @@ void sx_derivatives(const double *p, const double *X, const double *u,
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// The whole-mesh sum of the element derivatives, as the kernels scatter
+// it: dfdX[3 nnodes] += d/dX (scale psi^T R + coef f) with the element
+// pressures pres[4 nelem] (nullptr: none) and the state / adjoint with 6
+// entries per node (psi nullptr: no adjoint term).  reverse: the reverse
+// sweep, else the dual form per coordinate.
+void sx_mesh(int nelem, const int *conn, const double *xpts,
+             const double *thick, const double *pres, const double *vars,
+             const double *psi, const double *p, int func, const double *ks,
+             const double *s, int reverse, double *dfdX) {
+  tg::ElemParams ep;
+  ep.elem_type = TG_ELEM_MITC4;
+  ep.rho = 2700.0;
+  ep.E = p[0];
+  ep.nu = p[1];
+  ep.ys = p[2];
+  ep.transform = (int)p[3];
+  for (int i = 0; i < 3; i++) ep.ref_axis[i] = p[4 + i];
+  const tg::KsStats kk{ks[0], ks[1], ks[2]};
+  for (int e = 0; e < nelem; e++) {
+    tg::ShellXptData dt;
+    const int *nd = conn + 4 * e;
+    for (int i = 0; i < 12; i++) dt.X[i] = xpts[3 * nd[i / 3] + i % 3];
+    for (int i = 0; i < 24; i++) {
+      dt.u[i] = vars[6 * nd[i / 6] + i % 6];
+      dt.w[i] = psi ? psi[6 * nd[i / 6] + i % 6] : 0.0;
+    }
+    dt.t = thick[e];
+    dt.has_psi = psi != nullptr;
+    dt.has_pres = pres != nullptr;
+    for (int k = 0; k < 4; k++) dt.pres[k] = pres ? pres[4 * e + k] : 0.0;
+    double dX[12] = {0.0};
+    if (reverse) {
+      tg::shell_xpt_reverse(ep, dt, func, kk, s[0], s[1], s[2], dX);
+    } else {
+      for (int kc = 0; kc < 12; kc++)
+        dX[kc] = tg::shell_xpt_forward(ep, dt, kc, func, kk, s[0], s[1], s[2]);
+    }
+    for (int i = 0; i < 12; i++) dfdX[3 * nd[i / 3] + i % 3] += dX[i];
+  }
+}
+
+}  // extern "C"

@@ -60,6 +60,8 @@ def sx(tmp_path_factory):
     P = C.c_void_p
     lib.sx_derivatives.argtypes = [P, P, P, P, C.c_double, P, C.c_int,
                                    C.c_int, P, P, P, P]
+    lib.sx_mesh.argtypes = [C.c_int, P, P, P, P, P, P, P, C.c_int, P, P,
+                            C.c_int, P]
     return lib
 
 
@@ -135,6 +137,8 @@ def hx(tmp_path_factory):
     P = C.c_void_p
     lib.hx_derivatives.argtypes = [P, P, P, P, C.c_double, C.c_int, C.c_int,
                                    P, P, C.c_int, P, P, P, P]
+    lib.hx_mesh.argtypes = [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P,
+                            C.c_int, P]
     return lib
 
 
@@ -169,6 +173,69 @@ def test_hex_reverse_sweep_equals_dual_derivative(hx, has_psi, func):
                           ptr(tv), func, ptr(ks), ptr(s), ptr(f), ptr(r))
         assert np.abs(f).max() > 0
         assert np.abs(f - r).max() < 1e-12 * np.abs(f).max()
+
+
+def _host_mesh_xpt(sx, hx, prob, func, psi, s, reverse):
+    """The element functions of shell_xpt.cuh / hex_xpt.cuh compiled for
+    the host, summed over the mesh as the kernels scatter them (loads
+    staged as tg_assembler_set_pressure / _set_traction stage them)."""
+    import ctypes as C
+    P = C.c_void_p
+
+    def ptr(a):
+        return None if a is None else a.ctypes.data_as(P)
+
+    ne, nn = int(prob["nelem"]), int(prob["nnodes"])
+    conn = np.ascontiguousarray(prob["conn"], np.int32).ravel()
+    xpts = np.ascontiguousarray(prob["xpts"], np.float64).ravel()
+    thick = np.ascontiguousarray(prob["thick"], np.float64)
+    _, E, nu, ys = [float(v) for v in prob["mat"]]
+    u = np.ascontiguousarray(prob["u_test"], np.float64)
+    w = None if psi is None else np.ascontiguousarray(psi, np.float64)
+    ks = np.array([0.0, 1.0, 100.0])
+    s = np.asarray(s, np.float64)
+    out = np.zeros(3 * nn)
+    if int(prob["elem_type"]) == 0:
+        axis = np.asarray(prob.get("ref_axis", [1.0, 0.0, 0.0]), float)
+        axis = axis / np.linalg.norm(axis)
+        p = np.array([E, nu, ys, int(prob.get("transform", 0)), *axis])
+        pres = None
+        if len(prob.get("pres_elems", [])):
+            pres = np.zeros(4 * ne)
+            for k, e in enumerate(np.asarray(prob["pres_elems"])):
+                pres[4 * e:4 * e + 4] += prob["pres_vals"][4 * k:4 * k + 4]
+        sx.sx_mesh(ne, ptr(conn), ptr(xpts), ptr(thick), ptr(pres), ptr(u),
+                   ptr(w), ptr(p), func, ptr(ks), ptr(s), reverse, ptr(out))
+    else:
+        p = np.array([E, nu, ys])
+        tp = tf = tv = None
+        te = np.asarray(prob.get("trac_elems", []), np.int64)
+        if len(te):
+            order = np.argsort(te, kind="stable")
+            tp = np.zeros(ne + 1, np.int32)
+            np.add.at(tp, te + 1, 1)
+            tp = np.cumsum(tp).astype(np.int32)
+            tf = np.asarray(prob["trac_faces"], np.int32)[order].copy()
+            tv = np.asarray(prob["trac_vals"], np.float64).reshape(-1, 3)
+            tv = np.ascontiguousarray(tv[order]).ravel()
+        hx.hx_mesh(ne, ptr(conn), ptr(xpts), ptr(thick), ptr(tp), ptr(tf),
+                   ptr(tv), ptr(u), ptr(w), ptr(p), func, ptr(ks), ptr(s),
+                   reverse, ptr(out))
+    return out
+
+
+@pytest.mark.parametrize("reverse", [0, 1], ids=["dual", "reverse"])
+@pytest.mark.parametrize("name", XPT_CASES)
+def test_host_element_derivatives_against_reference(sx, hx, name, reverse):
+    """The element derivative code the GPU kernels run, compiled for the
+    host: the compliance derivative and psi^T dR/dX summed over the mesh
+    equal the reference's complex-step values (1e-10), in both forms."""
+    prob, ref = load_case(name)
+    dc = _host_mesh_xpt(sx, hx, prob, 0, None, (1.0, 0.0, 0.0), reverse)
+    assert rel(dc, ref["dfdX_test_comp"]) < XPT_TOL
+    xa = _host_mesh_xpt(sx, hx, prob, -1, prob["psi_test"], (0.0, 1.0, 1.0),
+                        reverse)
+    assert rel(xa, ref["adjxpt_test"]) < XPT_TOL
 
 
 # ------------------------------------------------------------------- GPU
