@@ -1,35 +1,14 @@
 // Device helpers of the hex8 kernels (TACSLinearHexaBasis,
-// TACSLinearElasticity3D with the isotropic TACSSolidConstitutive):
-// Gauss points, shape functions, the 3x3 inverse, the isotropic stiffness,
-// face quadrature and the von Mises value.  Included by the hex kernel
-// translation unit inside namespace tg::<anonymous> (and compiled for the
-// host by the CPU check of the node-coordinate derivative).  The helpers
-// that depend on the node coordinates are templates over the scalar type.
+// TACSLinearElasticity3D with the isotropic TACSSolidConstitutive): shape
+// functions, the isotropic stiffness, face quadrature and the von Mises
+// value (the shared dense helpers are in elem_math.cuh).  Included by the
+// hex kernel translation unit inside namespace tg::<anonymous> (and
+// compiled for the host by the CPU check of the node-coordinate
+// derivative).  The helpers that depend on the node coordinates are
+// templates over the scalar type.
 #pragma once
 
-#define TG_GPT 0.577350269189626
-
-__device__ __forceinline__ double gauss2(int i) {
-  return i ? TG_GPT : -TG_GPT;
-}
-
-template <class R>
-__device__ R inv3(const R *A, R *Ai) {
-  R det = (A[8] * (A[0] * A[4] - A[3] * A[1]) -
-           A[7] * (A[0] * A[5] - A[3] * A[2]) +
-           A[6] * (A[1] * A[5] - A[2] * A[4]));
-  R di = 1.0 / det;
-  Ai[0] = (A[4] * A[8] - A[5] * A[7]) * di;
-  Ai[1] = -(A[1] * A[8] - A[2] * A[7]) * di;
-  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * di;
-  Ai[3] = -(A[3] * A[8] - A[5] * A[6]) * di;
-  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * di;
-  Ai[5] = -(A[0] * A[5] - A[2] * A[3]) * di;
-  Ai[6] = (A[3] * A[7] - A[4] * A[6]) * di;
-  Ai[7] = -(A[0] * A[7] - A[1] * A[6]) * di;
-  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * di;
-  return det;
-}
+#include "elem_math.cuh"
 
 // TACSLinearHexaBasis::computeBasis / computeBasisGradient
 // (src/elements/basis/TACSHexaBasis.cpp:137-170), node m = i + 2j + 4k

@@ -39,19 +39,6 @@ __device__ __constant__ unsigned char c_pair[36][2] = {
     {2, 5}, {2, 6}, {2, 7}, {3, 3}, {3, 4}, {3, 5}, {3, 6}, {3, 7}, {4, 4},
     {4, 5}, {4, 6}, {4, 7}, {5, 5}, {5, 6}, {5, 7}, {6, 6}, {6, 7}, {7, 7}};
 
-__device__ __forceinline__ int find_slot(const int *rowp, const int *cols,
-                                         int row, int col) {
-  int lo = rowp[row], hi = rowp[row + 1] - 1;
-  while (lo <= hi) {
-    int mid = (lo + hi) >> 1;
-    int c = cols[mid];
-    if (c == col) return mid;
-    if (c < col) lo = mid + 1;
-    else hi = mid - 1;
-  }
-  return -1;
-}
-
 __device__ void hex_load(HexSmem &S, const MeshView &m, int e,
                          const double *vars, const double *vars2, int lane) {
   if (lane < 8) S.nodes[lane] = m.conn[8 * e + lane];
