@@ -327,6 +327,13 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0,
                       "max_iters_adj": int(r["iters_adj"].max()),
                       "converged_fwd": int(r["flags_fwd"].sum()),
                       "converged_adj": int(r["flags_adj"].sum())}
+        if r.get("direct") is not None:
+            st = r["direct"].stats()
+            out[label]["direct"] = {
+                k: st[k] for k in ("supernodes", "levels", "factor_bytes",
+                                   "flops", "fell_back_to_fp64",
+                                   "last_refinement_steps",
+                                   "last_backward_error")}
     d = g["mixed"] - g["fp64"]
     out["mixed"]["grad_rel_err_vs_fp64"] = float(
         np.abs(d).max() / np.abs(g["fp64"]).max())

@@ -197,6 +197,18 @@ int tg_direct_solve_f32(tg_direct *d, const float *b, float *x,
    relative accuracy, about cond(A) 2^-24). */
 int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
                             int steps, void *stream);
+/* The same refinement with a stopping test (no reference counterpart; the
+   practice of LAPACK's mixed-precision dsgesv): steps until the normwise
+   backward error eta = ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+   is at most tol, at most max_steps.  Returns TG_ERR_NOCONV (x holds the
+   last iterate) when eta stops halving for two steps or max_steps pass,
+   which happens when cond(A) approaches the inverse of FP32's unit
+   roundoff: factor the matrix in FP64 then.  steps and eta (may be NULL)
+   receive the steps taken and the final eta.  Synchronises the stream
+   once per step. */
+int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
+                                int max_steps, double tol, int *steps,
+                                double *eta, void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

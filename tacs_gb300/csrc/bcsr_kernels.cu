@@ -181,13 +181,15 @@ __global__ void reduce_partial_kernel(const double *x, const double *w,
   for (size_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     if (OP == 0) acc += x[i];
     else if (OP == 1) acc = x[i] > acc ? x[i] : acc;
+    else if (OP == 3) acc = fabs(x[i]) > acc ? fabs(x[i]) : acc;
     else acc += w[i] * exp(ksw * (x[i] - mx));
   }
   sh[threadIdx.x] = acc;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
-      if (OP == 1) sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
+      if (OP == 1 || OP == 3)
+        sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
                                          ? sh[threadIdx.x + s]
                                          : sh[threadIdx.x];
       else sh[threadIdx.x] += sh[threadIdx.x + s];
@@ -195,6 +197,20 @@ __global__ void reduce_partial_kernel(const double *x, const double *w,
     __syncthreads();
   }
   if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+// sum over each scalar row of |A| (for the infinity norm of A)
+__global__ void bcsr_row_abs_sum_kernel(int bs, int nrows,
+                                        const int *__restrict__ rowp,
+                                        const double *__restrict__ vals,
+                                        double *__restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nrows * bs) return;
+  const int i = (int)(t / bs), r = (int)(t % bs);
+  const size_t b2 = (size_t)bs * bs;
+  double acc = 0.0;
+  for (int j = rowp[i]; j < rowp[i + 1]; j++)
+    for (int q = 0; q < bs; q++) acc += fabs(vals[b2 * j + r * bs + q]);
+  out[t] = acc;
 }
 template <int OP>
 __global__ void reduce_final_kernel(const double *partials, int npart,
@@ -902,6 +918,19 @@ void launch_reduce_max(const double *x, size_t n, double *partials, int npart,
   reduce_partial_kernel<1><<<npart, 256, 0, s>>>(x, nullptr, n, nullptr, 0.0,
                                                  partials);
   reduce_final_kernel<1><<<1, 256, 0, s>>>(partials, npart, out);
+}
+void launch_reduce_absmax(const double *x, size_t n, double *partials,
+                          int npart, double *out, cudaStream_t s) {
+  reduce_partial_kernel<3><<<npart, 256, 0, s>>>(x, nullptr, n, nullptr, 0.0,
+                                                 partials);
+  reduce_final_kernel<1><<<1, 256, 0, s>>>(partials, npart, out);
+}
+void launch_bcsr_row_abs_sum(int bsize, int nrows, const int *rowp,
+                             const double *vals, double *out, cudaStream_t s) {
+  const long long n = (long long)nrows * bsize;
+  if (n <= 0) return;
+  bcsr_row_abs_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+      bsize, nrows, rowp, vals, out);
 }
 void launch_reduce_sum(const double *x, size_t n, double *partials, int npart,
                        double *out, cudaStream_t s) {

@@ -16,6 +16,8 @@
 
 // fronts of at most this many scalar rows are factored by one CTA each
 static constexpr int kSmallFront = 256;
+// blocks of the max-|x| reductions of the refinement's stopping test
+static constexpr int kRedParts = 256;
 
 static void bcsr_mult_t(const tg_mat *A, const double *a, const double *x,
                         double *y, cudaStream_t s) {
@@ -54,6 +56,10 @@ struct tg_direct {
         *d_kpb32 = nullptr, *d_a32 = nullptr, *d_r32 = nullptr,
         *d_c32 = nullptr;
   double *d_r = nullptr, *d_t = nullptr;  // refinement residual, scratch
+  // refinement stopping test: reduction partials, 3 device scalars, and
+  // ||A||_inf of the values factored last
+  double *d_red = nullptr, *d_scal = nullptr;
+  double anorm = 0.0;
   int64_t contrib_len = 0;
   int *d_fail = nullptr;
   bool factored = false;
@@ -94,7 +100,7 @@ struct tg_direct {
     dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
     dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
-    dfree(d_c32); dfree(d_r); dfree(d_t);
+    dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
   }
 };
 
@@ -207,6 +213,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_c32, N);
     if (!rc) rc = dalloc(&d->d_r, N);
     if (!rc) rc = dalloc(&d->d_t, N);
+    if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
+    if (!rc) rc = dalloc(&d->d_scal, 4);
   }
   if (!rc) rc = dalloc(&d->d_ypos, N);
   if (!rc) rc = dalloc(&d->d_xpos, N);
@@ -313,6 +321,14 @@ int tg_direct_factor(tg_direct *d, void *s) {
     tg::launch_d2f(A->d_vals, d->d_a32,
                    (size_t)A->nnz * A->bsize * A->bsize, S(s));
     factor_levels<float>(d, S(s));
+    // ||A||_inf of these values, for the refinement's backward error
+    const size_t N = (size_t)d->n * d->bs;
+    tg::launch_bcsr_row_abs_sum(A->bsize, A->nrows, A->a->d_rowp, A->d_vals,
+                                d->d_t, S(s));
+    tg::launch_reduce_absmax(d->d_t, N, d->d_red, kRedParts, d->d_scal,
+                             S(s));
+    TG_CUDA(cudaMemcpyAsync(&d->anorm, d->d_scal, sizeof(double),
+                            cudaMemcpyDeviceToHost, S(s)));
   }
   int hfail = 0;
   TG_CUDA(cudaMemcpyAsync(&hfail, d->d_fail, sizeof(int),
@@ -380,6 +396,70 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
     }
   }
   TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
+                                int max_steps, double tol, int *steps,
+                                double *eta_out, void *s) {
+  if (!d || !b || !x || max_steps < 1 || !(tol > 0.0))
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: bad arguments");
+  if (!d->factored)
+    return fail(TG_ERR_STATE, "tg_direct_solve_refined_tol: not factored");
+  if (d->precision != TG_PREC_FP32)
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: needs the FP32 "
+                            "factorisation");
+  tg_mat *A = d->A;
+  const size_t N = (size_t)d->n * d->bs;
+  double h[2] = {0.0, 0.0};
+  // ||b||_inf
+  tg::launch_reduce_absmax(b, N, d->d_red, kRedParts, d->d_scal, S(s));
+  TG_CUDA(cudaMemcpyAsync(h, d->d_scal, sizeof(double),
+                          cudaMemcpyDeviceToHost, S(s)));
+  TG_CUDA(cudaStreamSynchronize(S(s)));
+  const double bnorm = h[0];
+  TG_CUDA(cudaMemsetAsync(x, 0, N * sizeof(double), S(s)));
+  tg::launch_copy(b, d->d_r, N, S(s));
+  double prev = 0.0, eta = 0.0;
+  int taken = 0, slow = 0, rc = TG_ERR_NOCONV;
+  if (bnorm == 0.0) rc = 0;  // x = 0 is exact
+  while (rc != 0 && taken < max_steps) {
+    tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
+    solve_levels<float>(d, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
+                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
+                        S(s));
+    tg::launch_f2d(d->d_c32, d->d_t, N, S(s));
+    tg::launch_axpy(1.0, d->d_t, x, N, S(s));
+    tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                         A->d_vals, x, d->d_t, S(s));
+    tg::launch_copy(b, d->d_r, N, S(s));
+    tg::launch_axpy(-1.0, d->d_t, d->d_r, N, S(s));
+    tg::launch_reduce_absmax(d->d_r, N, d->d_red, kRedParts, d->d_scal,
+                             S(s));
+    tg::launch_reduce_absmax(x, N, d->d_red, kRedParts, d->d_scal + 1, S(s));
+    TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 2 * sizeof(double),
+                            cudaMemcpyDeviceToHost, S(s)));
+    TG_CUDA(cudaStreamSynchronize(S(s)));
+    taken++;
+    // normwise backward error of x
+    const double den = d->anorm * h[1] + bnorm;
+    eta = den > 0.0 ? h[0] / den : 0.0;
+    if (!(eta == eta)) break;  // NaN: the FP32 factor is unusable
+    if (eta <= tol) {
+      rc = 0;
+      break;
+    }
+    // stagnation: two steps in a row that do not halve eta
+    slow = (taken > 1 && eta > 0.5 * prev) ? slow + 1 : 0;
+    if (slow >= 2) break;
+    prev = eta;
+  }
+  if (steps) *steps = taken;
+  if (eta_out) *eta_out = eta;
+  TG_CUDA(cudaGetLastError());
+  if (rc)
+    return fail(TG_ERR_NOCONV, "tg_direct_solve_refined_tol: refinement did "
+                               "not reach the backward-error tolerance");
   return 0;
 }
 

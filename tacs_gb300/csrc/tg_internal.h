@@ -128,6 +128,11 @@ void launch_reduce_max(const double *x, size_t n, double *partials,
                        int npart, double *out, cudaStream_t s);
 void launch_reduce_sum(const double *x, size_t n, double *partials,
                        int npart, double *out, cudaStream_t s);
+// max |x_i|, and the scalar-row sums of |A| of a BCSR matrix
+void launch_reduce_absmax(const double *x, size_t n, double *partials,
+                          int npart, double *out, cudaStream_t s);
+void launch_bcsr_row_abs_sum(int bsize, int nrows, const int *rowp,
+                             const double *vals, double *out, cudaStream_t s);
 void launch_ks_sum(const double *fail, const double *wdet, size_t n,
                    const double *dmax, double ksw, double *partials,
                    int npart, double *out, cudaStream_t s);

@@ -126,7 +126,15 @@ class Direct:
     """tg_direct: complete multifrontal factorisation of an assembled
     matrix (the reference's direct solve), nested dissection by the node
     coordinates; solve(b) returns A^-1 b for the assembled A with its row
-    boundary conditions."""
+    boundary conditions.
+
+    precision PREC_FP32 factors in FP32 and solves FP64 right-hand sides
+    by iterative refinement (FP64 residuals, FP32 corrections) until the
+    normwise backward error is at most eps sqrt(N) (the test of LAPACK's
+    mixed-precision dsgesv).  Where that cannot work -- the FP32 Cholesky
+    meets a non-positive pivot, or refinement stagnates because cond(A) is
+    near the inverse of FP32's unit roundoff -- the matrix is factored in
+    FP64 instead (`fell_back`), from its values at that moment."""
 
     def __init__(self, mat, use_coords=True, precision=_lib.PREC_FP64):
         h = C.c_void_p()
@@ -134,22 +142,48 @@ class Direct:
                                           int(precision), C.byref(h)),
               "tg_direct_create")
         self.handle, self.mat, self.precision = h, mat, precision
+        self.use_coords = use_coords
+        self._fp64 = None
+        self.fell_back = False
+        self.last_steps, self.last_eta = 0, 0.0
+
+    def _factor_fp64(self):
+        self._fp64 = Direct(self.mat, self.use_coords, _lib.PREC_FP64)
+        self._fp64.factor()
+        self.fell_back = True
 
     def factor(self):
-        check(_lib.lib().tg_direct_factor(self.handle, _stream()),
-              "tg_direct_factor")
+        self._fp64 = None
+        self.fell_back = False
+        rc = _lib.lib().tg_direct_factor(self.handle, _stream())
+        if rc == _lib.ERR_PIVOT and self.precision == _lib.PREC_FP32:
+            self._factor_fp64()  # the FP32 Cholesky broke down
+            return
+        check(rc, "tg_direct_factor")
 
-    def solve(self, b, x=None, steps=6):
+    def solve(self, b, x=None, steps=30, tol=None):
         """x = A^-1 b.  FP64 factorisation: FP64 vectors.  FP32
         factorisation: FP32 vectors are solved in FP32, FP64 ones by
-        `steps` steps of iterative refinement (FP64 residuals, FP32
-        corrections)."""
+        refinement (at most `steps` steps, to the backward error `tol`,
+        default eps sqrt(N)), or by the FP64 factorisation after a
+        fallback."""
         x = torch.empty_like(b) if x is None else x
         L = _lib.lib()
+        if self._fp64 is not None and b.dtype == torch.float64:
+            return self._fp64.solve(b, x)
         if self.precision == _lib.PREC_FP32 and b.dtype == torch.float64:
-            check(L.tg_direct_solve_refined(self.handle, _p(b), _p(x),
-                                            int(steps), _stream()),
-                  "tg_direct_solve_refined")
+            if tol is None:
+                tol = 2.0 ** -53 * float(np.sqrt(b.numel()))
+            st, eta = C.c_int(0), C.c_double(0.0)
+            rc = L.tg_direct_solve_refined_tol(self.handle, _p(b), _p(x),
+                                               int(steps), float(tol),
+                                               C.byref(st), C.byref(eta),
+                                               _stream())
+            self.last_steps, self.last_eta = st.value, eta.value
+            if rc == _lib.ERR_NOCONV:
+                self._factor_fp64()
+                return self._fp64.solve(b, x)
+            check(rc, "tg_direct_solve_refined_tol")
             return x
         fn = (L.tg_direct_solve_f32 if self.precision == _lib.PREC_FP32
               else L.tg_direct_solve)
@@ -161,7 +195,10 @@ class Direct:
         check(_lib.lib().tg_direct_get_stats(self.handle, st.ctypes.data))
         return {"supernodes": int(st[0]), "levels": int(st[1]),
                 "factor_bytes": st[2], "pool_bytes": st[3],
-                "flops": st[4], "max_front": int(st[5])}
+                "flops": st[4], "max_front": int(st[5]),
+                "fell_back_to_fp64": self.fell_back,
+                "last_refinement_steps": self.last_steps,
+                "last_backward_error": self.last_eta}
 
     def __del__(self):
         try:
@@ -546,7 +583,7 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
                                             1.0, -1.0)
     return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,
                 iters_adj=it_a, flags_adj=fl_a, psi=Psi, resnorm_fwd=rn_f,
-                resnorm_adj=rn_a)
+                resnorm_adj=rn_a, direct=dsol if direct else None)
 
 
 def batch_loads(model):

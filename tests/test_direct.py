@@ -197,3 +197,43 @@ def test_direct_as_gmres_preconditioner(gpu):
     x32, flag = ksm32.solve(b)
     assert flag == 1
     assert rel(x32.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+
+
+@pytest.mark.parametrize("thin", [False, True], ids=["t10mm", "t2mm"])
+def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
+    """FP32 factorisation + FP64 refinement stops when the normwise
+    backward error reaches eps sqrt(N); where it cannot (the FP32 Cholesky
+    breaks down or refinement stagnates, cond(K) near 2^24) the solve falls
+    back to an FP64 factorisation.  Either way the result is the FP64
+    direct solution (1e-8) with the FP64 backward error (1e-13)."""
+    from tacs_gb300 import _lib, meshes
+    n = 48
+    prob = meshes.plate(n, n, 2.0, 2.0, t=0.002 if thin else 0.01)
+    e = meshes.plate_edges(n, n).astype(np.int32)
+    prob["bc_nodes"], prob["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
+    prob["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    prob["pres_vals"] = np.full(4 * n * n, 1e3)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    b = _rhs(M, prob, mat)
+    d64 = gpu.Direct(mat)
+    d64.factor()
+    x64 = d64.solve(b)
+    d32 = gpu.Direct(mat, precision=_lib.PREC_FP32)
+    d32.factor()
+    x = d32.solve(b)
+    st = d32.stats()
+    tol = 2.0 ** -53 * np.sqrt(M.ndof)
+    assert st["fell_back_to_fp64"] or st["last_backward_error"] <= tol
+    if not thin:
+        assert not st["fell_back_to_fp64"]
+        assert 1 <= st["last_refinement_steps"] <= 10
+    assert rel(x.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+    r = (mat.mult(x) - b).abs().max().item()
+    from scipy import sparse
+    bs = mat.bsize
+    K = sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
+                           mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
+                          shape=(M.ndof, M.ndof)).tocsr()
+    Kinf = abs(K).sum(axis=1).max()
+    assert r < 1e-13 * (Kinf * x.abs().max().item() + b.abs().max().item())
