@@ -15,6 +15,13 @@
 // (tests/cpp/hex_xpt_check.cpp).
 #pragma once
 
+// stage functions of the reverse sweep keep their own register frames
+#ifdef __CUDACC__
+#define TG_HEX_STAGE __device__ __noinline__
+#else
+#define TG_HEX_STAGE inline
+#endif
+
 // The inputs of one element; the face tractions are ntrac (face, value[3])
 // entries.
 struct HexXptData {
@@ -119,108 +126,117 @@ __device__ __forceinline__ void hex_inv3_rev(const double *Ai, double det,
                        bdet * det * Ai[3 * j + i];
 }
 
+// One Gauss point of the reverse sweep: adds d/dX of that point's terms
+// into bX.
+TG_HEX_STAGE void hex_xpt_point_rev(const ElemParams &ep,
+                                    const HexXptData &dt, const HexC &c,
+                                    int q, int func, KsStats kk, double coef,
+                                    double sc, double *bX) {
+  const double *X = dt.X, *u = dt.u, *w = dt.w;
+  const double t = dt.t;
+  const double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1), gauss2(q >> 2)};
+  double Nxi[24];
+  hex_shape(pt, nullptr, Nxi);
+  double Xd[9], J[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double v = 0.0;
+      for (int mm = 0; mm < 8; mm++) v += Nxi[3 * mm + j] * X[3 * mm + i];
+      Xd[3 * i + j] = v;
+    }
+  const double det = inv3(Xd, J);
+  double Uu[9], Uw[9];
+  for (int i = 0; i < 9; i++) Uu[i] = Uw[i] = 0.0;
+  for (int mm = 0; mm < 8; mm++)
+    for (int j = 0; j < 3; j++) {
+      const double g = Nxi[3 * mm] * J[j] + Nxi[3 * mm + 1] * J[3 + j] +
+                       Nxi[3 * mm + 2] * J[6 + j];
+      for (int i = 0; i < 3; i++) {
+        Uu[3 * i + j] += u[3 * mm + i] * g;
+        Uw[3 * i + j] += w[3 * mm + i] * g;
+      }
+    }
+  const double eu[6] = {Uu[0], Uu[4], Uu[8], Uu[5] + Uu[7], Uu[2] + Uu[6],
+                        Uu[1] + Uu[3]};
+  const double ew[6] = {Uw[0], Uw[4], Uw[8], Uw[5] + Uw[7], Uw[2] + Uw[6],
+                        Uw[1] + Uw[3]};
+  double s[6], sw[6];
+  hex_Ce(c, eu, s);
+  hex_Ce(c, ew, sw);
+  // adjoints of det and of the strains (the stiffness is symmetric)
+  double bdet = 0.0, beu[6] = {0, 0, 0, 0, 0, 0}, bew[6] = {0, 0, 0, 0, 0, 0};
+  if (dt.has_psi) {
+    double v = 0.0;
+    for (int k = 0; k < 6; k++) {
+      v += ew[k] * s[k];
+      bew[k] += sc * det * t * s[k];
+      beu[k] += sc * det * t * sw[k];
+    }
+    bdet += sc * t * v;
+  }
+  if (func == TG_FUNC_COMPLIANCE) {
+    double v = 0.0;
+    for (int k = 0; k < 6; k++) {
+      v += eu[k] * (s[k] * t);
+      beu[k] += coef * det * t * 2.0 * s[k];
+    }
+    bdet += coef * v;
+  } else if (func == TG_FUNC_KS_FAILURE) {
+    const double f = hex_vm(ep, s);
+    const double ex = ::exp(kk.weight * (f - kk.max)) / kk.sum;
+    bdet += coef * ex / kk.weight;
+    // d vonMises / d s (vonMisesFailure3DStressSens)
+    const double fy = f * ep.ys;
+    double bs[6] = {0, 0, 0, 0, 0, 0};
+    if (fy != 0.0) {
+      const double fact = coef * det * ex * 0.5 / (ep.ys * fy);
+      bs[0] = fact * (2.0 * s[0] - s[1] - s[2]);
+      bs[1] = fact * (2.0 * s[1] - s[0] - s[2]);
+      bs[2] = fact * (2.0 * s[2] - s[0] - s[1]);
+      bs[3] = 6.0 * fact * s[3];
+      bs[4] = 6.0 * fact * s[4];
+      bs[5] = 6.0 * fact * s[5];
+    }
+    double cbs[6];
+    hex_Ce(c, bs, cbs);
+    for (int k = 0; k < 6; k++) beu[k] += cbs[k];
+  }
+  // strains -> displacement gradients -> shape gradients -> J -> Xd
+  double bUu[9], bUw[9];
+  bUu[0] = beu[0]; bUu[4] = beu[1]; bUu[8] = beu[2];
+  bUu[5] = bUu[7] = beu[3]; bUu[2] = bUu[6] = beu[4];
+  bUu[1] = bUu[3] = beu[5];
+  bUw[0] = bew[0]; bUw[4] = bew[1]; bUw[8] = bew[2];
+  bUw[5] = bUw[7] = bew[3]; bUw[2] = bUw[6] = bew[4];
+  bUw[1] = bUw[3] = bew[5];
+  double bJ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int mm = 0; mm < 8; mm++)
+    for (int j = 0; j < 3; j++) {
+      double bg = 0.0;
+      for (int i = 0; i < 3; i++)
+        bg += bUu[3 * i + j] * u[3 * mm + i] + bUw[3 * i + j] * w[3 * mm + i];
+      for (int r = 0; r < 3; r++) bJ[3 * r + j] += Nxi[3 * mm + r] * bg;
+    }
+  double bXd[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  hex_inv3_rev(J, det, bJ, bdet, bXd);
+  for (int mm = 0; mm < 8; mm++)
+    for (int i = 0; i < 3; i++)
+      bX[3 * mm + i] += Nxi[3 * mm] * bXd[3 * i] +
+                        Nxi[3 * mm + 1] * bXd[3 * i + 1] +
+                        Nxi[3 * mm + 2] * bXd[3 * i + 2];
+}
+
 // All 24 coordinate derivatives of the quantity above, added into dX.
 __device__ void hex_xpt_reverse(const ElemParams &ep, const HexXptData &dt,
                                 int func, KsStats kk, double coef,
                                 double scale, double lambda, double *dX) {
-  const double *X = dt.X, *u = dt.u, *w = dt.w;
-  const double t = dt.t;
+  const double *X = dt.X, *w = dt.w;
   const HexC c = hex_c(ep);
   const double sc = dt.has_psi ? scale : 0.0;
   double bX[24];
   for (int i = 0; i < 24; i++) bX[i] = 0.0;
-  for (int q = 0; q < 8; q++) {
-    const double pt[3] = {gauss2(q & 1), gauss2((q >> 1) & 1), gauss2(q >> 2)};
-    double Nxi[24];
-    hex_shape(pt, nullptr, Nxi);
-    double Xd[9], J[9];
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) {
-        double v = 0.0;
-        for (int mm = 0; mm < 8; mm++) v += Nxi[3 * mm + j] * X[3 * mm + i];
-        Xd[3 * i + j] = v;
-      }
-    const double det = inv3(Xd, J);
-    double Uu[9], Uw[9];
-    for (int i = 0; i < 9; i++) Uu[i] = Uw[i] = 0.0;
-    for (int mm = 0; mm < 8; mm++)
-      for (int j = 0; j < 3; j++) {
-        const double g = Nxi[3 * mm] * J[j] + Nxi[3 * mm + 1] * J[3 + j] +
-                         Nxi[3 * mm + 2] * J[6 + j];
-        for (int i = 0; i < 3; i++) {
-          Uu[3 * i + j] += u[3 * mm + i] * g;
-          Uw[3 * i + j] += w[3 * mm + i] * g;
-        }
-      }
-    const double eu[6] = {Uu[0], Uu[4], Uu[8], Uu[5] + Uu[7], Uu[2] + Uu[6],
-                          Uu[1] + Uu[3]};
-    const double ew[6] = {Uw[0], Uw[4], Uw[8], Uw[5] + Uw[7], Uw[2] + Uw[6],
-                          Uw[1] + Uw[3]};
-    double s[6], sw[6];
-    hex_Ce(c, eu, s);
-    hex_Ce(c, ew, sw);
-    // adjoints of det and of the strains (the stiffness is symmetric)
-    double bdet = 0.0, beu[6] = {0, 0, 0, 0, 0, 0}, bew[6] = {0, 0, 0, 0, 0, 0};
-    if (dt.has_psi) {
-      double v = 0.0;
-      for (int k = 0; k < 6; k++) {
-        v += ew[k] * s[k];
-        bew[k] += sc * det * t * s[k];
-        beu[k] += sc * det * t * sw[k];
-      }
-      bdet += sc * t * v;
-    }
-    if (func == TG_FUNC_COMPLIANCE) {
-      double v = 0.0;
-      for (int k = 0; k < 6; k++) {
-        v += eu[k] * (s[k] * t);
-        beu[k] += coef * det * t * 2.0 * s[k];
-      }
-      bdet += coef * v;
-    } else if (func == TG_FUNC_KS_FAILURE) {
-      const double f = hex_vm(ep, s);
-      const double ex = ::exp(kk.weight * (f - kk.max)) / kk.sum;
-      bdet += coef * ex / kk.weight;
-      // d vonMises / d s (vonMisesFailure3DStressSens)
-      const double fy = f * ep.ys;
-      double bs[6] = {0, 0, 0, 0, 0, 0};
-      if (fy != 0.0) {
-        const double fact = coef * det * ex * 0.5 / (ep.ys * fy);
-        bs[0] = fact * (2.0 * s[0] - s[1] - s[2]);
-        bs[1] = fact * (2.0 * s[1] - s[0] - s[2]);
-        bs[2] = fact * (2.0 * s[2] - s[0] - s[1]);
-        bs[3] = 6.0 * fact * s[3];
-        bs[4] = 6.0 * fact * s[4];
-        bs[5] = 6.0 * fact * s[5];
-      }
-      double cbs[6];
-      hex_Ce(c, bs, cbs);
-      for (int k = 0; k < 6; k++) beu[k] += cbs[k];
-    }
-    // strains -> displacement gradients -> shape gradients -> J -> Xd
-    double bUu[9], bUw[9];
-    bUu[0] = beu[0]; bUu[4] = beu[1]; bUu[8] = beu[2];
-    bUu[5] = bUu[7] = beu[3]; bUu[2] = bUu[6] = beu[4];
-    bUu[1] = bUu[3] = beu[5];
-    bUw[0] = bew[0]; bUw[4] = bew[1]; bUw[8] = bew[2];
-    bUw[5] = bUw[7] = bew[3]; bUw[2] = bUw[6] = bew[4];
-    bUw[1] = bUw[3] = bew[5];
-    double bJ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int mm = 0; mm < 8; mm++)
-      for (int j = 0; j < 3; j++) {
-        double bg = 0.0;
-        for (int i = 0; i < 3; i++)
-          bg += bUu[3 * i + j] * u[3 * mm + i] + bUw[3 * i + j] * w[3 * mm + i];
-        for (int r = 0; r < 3; r++) bJ[3 * r + j] += Nxi[3 * mm + r] * bg;
-      }
-    double bXd[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    hex_inv3_rev(J, det, bJ, bdet, bXd);
-    for (int mm = 0; mm < 8; mm++)
-      for (int i = 0; i < 3; i++)
-        bX[3 * mm + i] += Nxi[3 * mm] * bXd[3 * i] +
-                          Nxi[3 * mm + 1] * bXd[3 * i + 1] +
-                          Nxi[3 * mm + 2] * bXd[3 * i + 2];
-  }
+  for (int q = 0; q < 8; q++)
+    hex_xpt_point_rev(ep, dt, c, q, func, kk, coef, sc, bX);
   if (dt.has_psi && lambda != 0.0) {
     for (int tk = 0; tk < dt.ntrac; tk++) {
       const int face = dt.trac_face[tk];

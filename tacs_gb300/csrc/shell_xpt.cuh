@@ -27,6 +27,13 @@
 // (tests/cpp/shell_xpt_check.cpp).
 #pragma once
 
+// stage functions of the reverse sweep keep their own register frames
+#ifdef __CUDACC__
+#define TG_XPT_STAGE __device__ __noinline__
+#else
+#define TG_XPT_STAGE inline
+#endif
+
 // The inputs of one element: coordinates, state and adjoint, thickness and
 // nodal pressures.
 struct ShellXptData {
@@ -372,7 +379,7 @@ struct ShellXptFwd {
 };
 
 // The node normals, nodal drilling strains and tying strains (values).
-__device__ void shell_xpt_values(const ElemParams &ep, const ShellXptData &dt,
+TG_XPT_STAGE void shell_xpt_values(const ElemParams &ep, const ShellXptData &dt,
                                  ShellXptFwd &fw) {
   const double *X = dt.X, *u = dt.u, *w = dt.w;
   double N[4], Na[4], Nb[4], Xxi[6];
@@ -457,7 +464,7 @@ __device__ void shell_xpt_values(const ElemParams &ep, const ShellXptData &dt,
 // One Gauss point q, recomputed from the shared values and differentiated
 // backwards: accumulates the adjoints of X, the node normals, the drilling
 // and the tying strains.
-__device__ void shell_xpt_point_rev(const ElemParams &ep,
+TG_XPT_STAGE void shell_xpt_point_rev(const ElemParams &ep,
                                     const ShellXptData &dt,
                                     const ShellXptFwd &fw, int q, int func,
                                     KsStats kk, double coef, double scale,
@@ -678,7 +685,7 @@ __device__ void shell_xpt_point_rev(const ElemParams &ep,
 }
 
 // One tying point backwards: adjoints of X and the node normals.
-__device__ void shell_xpt_tying_rev(const ShellXptData &dt,
+TG_XPT_STAGE void shell_xpt_tying_rev(const ShellXptData &dt,
                                     const ShellXptFwd &fw, int ty,
                                     double bsu, double bsw, double *bX,
                                     double *bfn) {
@@ -721,7 +728,7 @@ __device__ void shell_xpt_tying_rev(const ShellXptData &dt,
 
 // One corner's drilling strain backwards: adjoints of X and that node's
 // normal.
-__device__ void shell_xpt_drill_rev(const ElemParams &ep,
+TG_XPT_STAGE void shell_xpt_drill_rev(const ElemParams &ep,
                                     const ShellXptData &dt,
                                     const ShellXptFwd &fw, int k, double bsu,
                                     double bsw, double *bX, double *bfn) {
