@@ -377,3 +377,72 @@ def test_shape_derivative_against_solves(gpu):
         for k in range(2):
             err = abs(fd[k] - grads[k][j]) / np.abs(grads[k]).max()
             assert err < 1e-5, (node, d, k, fd[k], grads[k][j])
+
+
+def test_element_derivatives_in_bounds_under_sanitizers(tmp_path):
+    """The element derivative code the kernels run (both forms, shell and
+    hex) makes no out-of-bounds access and no undefined operation: the
+    host checks above, with the check libraries built with
+    AddressSanitizer and UndefinedBehaviorSanitizer (any finding aborts),
+    run in a child process that preloads the sanitizer runtimes."""
+    import os
+    import shutil
+    import subprocess
+    import sys
+    from conftest import ROOT
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    rt = [subprocess.run([cxx, f"-print-file-name={lib}"], capture_output=True,
+                         text=True).stdout.strip()
+          for lib in ("libasan.so", "libubsan.so")]
+    if not all(os.path.isabs(p) and os.path.exists(p) for p in rt):
+        pytest.skip("sanitizer runtimes not found")
+    libs = {}
+    for name in ("shell_xpt_check", "hex_xpt_check"):
+        out = str(tmp_path / f"lib{name}.so")
+        r = subprocess.run([cxx, "-O1", "-g", "-std=c++17",
+                            "-fsanitize=address,undefined",
+                            "-fno-sanitize-recover=all", "-shared", "-fPIC",
+                            "-I", os.path.join(ROOT, "tacs_gb300", "csrc"),
+                            os.path.join(ROOT, "tests", "cpp", name + ".cpp"),
+                            "-o", out], capture_output=True, text=True)
+        if r.returncode:
+            pytest.skip("sanitizer build failed: " + r.stderr[-200:])
+        libs[name] = out
+    child = f"""
+import ctypes as C, sys
+sys.path[:0] = [{os.path.join(ROOT, "tests")!r}, {ROOT!r}]
+import test_xpt_sens as T
+P = C.c_void_p
+sx = C.CDLL({libs["shell_xpt_check"]!r})
+sx.sx_derivatives.argtypes = [P, P, P, P, C.c_double, P, C.c_int, C.c_int,
+                              P, P, P, P]
+sx.sx_mesh.argtypes = [C.c_int, P, P, P, P, P, P, P, C.c_int, P, P, C.c_int,
+                       P]
+hx = C.CDLL({libs["hex_xpt_check"]!r})
+hx.hx_derivatives.argtypes = [P, P, P, P, C.c_double, C.c_int, C.c_int, P, P,
+                              C.c_int, P, P, P, P]
+hx.hx_mesh.argtypes = [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P,
+                       C.c_int, P]
+n = 0
+for tr in (0, 1):
+    for flags, func in [(1, -1), (3, -1), (0, 0), (0, 1), (3, 0), (1, 1)]:
+        T.test_shell_reverse_sweep_equals_dual_derivative(sx, tr, flags,
+                                                          func)
+        n += 1
+for hp, func in [(1, -1), (0, 0), (0, 1), (1, 0), (1, 1)]:
+    T.test_hex_reverse_sweep_equals_dual_derivative(hx, hp, func)
+    n += 1
+for name in T.XPT_CASES:
+    for rev in (0, 1):
+        T.test_host_element_derivatives_against_reference(sx, hx, name, rev)
+        n += 1
+print("checked", n)
+"""
+    env = dict(os.environ, LD_PRELOAD=":".join(rt),
+               ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([sys.executable, "-c", child], capture_output=True,
+                       text=True, env=env, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "checked 33" in r.stdout
