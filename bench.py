@@ -102,7 +102,8 @@ def adjoint_section(n, torch, colored=False):
                       "converged": [int(f) for f in r["flags"]],
                       "ilu_schedule": r["pc"].schedule()}
         if label == "fp64_ilu0_natural":
-            out["shape_derivative"] = xpt_timing(M, r, torch)
+            out["shape_derivative"] = guarded(
+                lambda: xpt_timing(M, r, torch))
     ref = grads["fp64_ilu0_natural"]
     for label in [r[0] for r in runs[1:]]:
         out[label]["grad_rel_err_vs_fp64_natural"] = [
@@ -463,6 +464,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def guarded(fn):
+    """Run one optional section of the bench line; a failure is recorded
+    as {"error": ...} in that section so the line itself still prints."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        return {"error": f"{type(e).__name__}: {e}"[:500]}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -671,37 +681,43 @@ def main():
         "gpu_launches": M.ncolors * args.steps + 2 * args.steps,
         "clocks": clk,
     }
+    padj = None
     if rank == 0:
-        # node-coordinate total derivatives on the same plate at a seeded
-        # state and adjoint (the kernel's cost does not depend on values)
-        g = torch.Generator(device="cuda").manual_seed(7)
-        us = 1e-4 * torch.randn(M.ndof, dtype=torch.float64, device="cuda",
-                                generator=g)
-        ps = torch.randn(M.ndof, dtype=torch.float64, device="cuda",
-                         generator=g)
-        line["shape_derivative"] = xpt_timing(M, {"u": us, "psis": [ps, ps]},
-                                              torch)
-        line["shape_derivative"]["workload"] = (
-            f"MITC4 plate {args.size}x{args.size}: df/dX - psi^T dR/dX of "
-            "compliance and KS")
+        def shape_derivative():
+            # node-coordinate total derivatives on the same plate at a
+            # seeded state and adjoint (the kernels' cost does not depend
+            # on the values)
+            g = torch.Generator(device="cuda").manual_seed(7)
+            us = 1e-4 * torch.randn(M.ndof, dtype=torch.float64,
+                                    device="cuda", generator=g)
+            ps = torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                             generator=g)
+            out = xpt_timing(M, {"u": us, "psis": [ps, ps]}, torch)
+            out["workload"] = (f"MITC4 plate {args.size}x{args.size}: "
+                               "df/dX - psi^T dR/dX of compliance and KS")
+            return out
+        line["shape_derivative"] = guarded(shape_derivative)
     if rank == 0 and args.adj_size > 0:
-        adj, padj = adjoint_section(args.adj_size, torch)
-        line["adjoint"] = adj
+        res = guarded(lambda: adjoint_section(args.adj_size, torch))
+        if isinstance(res, tuple):
+            line["adjoint"], padj = res
+        else:
+            line["adjoint"] = res
     if rank == 0 and not args.no_hex:
-        line["hex_c3"] = hex_section(torch)
+        line["hex_c3"] = guarded(lambda: hex_section(torch))
     if rank == 0 and args.c2_adjoint:
-        line["c2_adjoint"] = c2_adjoint_section(torch, args.size)
+        line["c2_adjoint"] = guarded(
+            lambda: c2_adjoint_section(torch, args.size))
     if rank == 0 and not args.no_cylinder:
-        line["cylinder_c5"] = cylinder_section(torch)
+        line["cylinder_c5"] = guarded(lambda: cylinder_section(torch))
     if rank == 0 and args.batch > 0:
-        line["batch_c4"] = batch_section(torch, count=args.batch,
-                                         nmax=args.batch_nmax,
-                                         pc_kind=args.batch_pc,
-                                         lev_fill=args.batch_fill,
-                                         direct=args.batch_direct)
+        line["batch_c4"] = guarded(lambda: batch_section(
+            torch, count=args.batch, nmax=args.batch_nmax,
+            pc_kind=args.batch_pc, lev_fill=args.batch_fill,
+            direct=args.batch_direct))
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(p)
-        if args.adj_size > 0:
+        line["cpu_baseline"] = guarded(lambda: cpu_baseline(p))
+        if padj is not None and "error" not in line["cpu_baseline"]:
             import oracle
             o = oracle.Oracle(padj, nthreads=os.cpu_count() or 1)
             t0 = time.perf_counter()
