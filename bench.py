@@ -128,26 +128,30 @@ def xpt_timing(M, r, torch, reps=3):
     u, psis = r["u"], r["psis"]
     out = {}
     res = {}
-    for label, reverse in (("forward_dual", False), ("reverse_sweep", True)):
-        M.set_xpt_mode(reverse)
-        ms, grads = [], []
-        for fn in (0, 1):
-            M.eval_functions(u, [fn])
-            gX = M.node_vec()
-            M.add_total_xpt_derivative(u, fn, psis[fn], gX)  # warm-up
-            grads.append(gX.clone())
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(reps):
-                M.add_total_xpt_derivative(u, fn, psis[fn], gX)
-            e1.record()
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1) / reps)
-        res[label] = grads
-        out[label] = {"ms_per_function": ms,
-                      "elements_per_s": [M.nelem / (t / 1e3) for t in ms]}
-    M.set_xpt_mode(False)
+    try:
+        for label, reverse in (("forward_dual", False),
+                               ("reverse_sweep", True)):
+            M.set_xpt_mode(reverse)
+            ms, grads = [], []
+            for fn in (0, 1):
+                M.eval_functions(u, [fn])
+                gX = M.node_vec()
+                M.add_total_xpt_derivative(u, fn, psis[fn], gX)  # warm-up
+                grads.append(gX.clone())
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    M.add_total_xpt_derivative(u, fn, psis[fn], gX)
+                e1.record()
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1) / reps)
+            res[label] = grads
+            out[label] = {"ms_per_function": ms,
+                          "elements_per_s": [M.nelem / (t / 1e3)
+                                             for t in ms]}
+    finally:
+        M.set_xpt_mode(False)
     out["reverse_vs_forward_max_rel_diff"] = max(
         float((a - b).abs().max() / b.abs().max())
         for a, b in zip(res["reverse_sweep"], res["forward_dual"]))
