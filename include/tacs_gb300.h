@@ -205,7 +205,8 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
    which happens when cond(A) approaches the inverse of FP32's unit
    roundoff: factor the matrix in FP64 then.  steps and eta (may be NULL)
    receive the steps taken and the final eta.  Synchronises the stream
-   once per step. */
+   once per step.  b and x must be different buffers (both refinement
+   calls; tg_direct_solve itself may solve in place). */
 int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 int max_steps, double tol, int *steps,
                                 double *eta, void *stream);

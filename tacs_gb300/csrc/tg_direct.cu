@@ -371,6 +371,8 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
                             int steps, void *s) {
   if (!d || !b || !x || steps < 1)
     return fail(TG_ERR_ARG, "tg_direct_solve_refined: bad arguments");
+  if ((const void *)b == (const void *)x)  // b is re-read after x is zeroed
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined: b and x alias");
   if (!d->factored)
     return fail(TG_ERR_STATE, "tg_direct_solve_refined: not factored");
   if (d->precision != TG_PREC_FP32)
@@ -404,6 +406,8 @@ int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 double *eta_out, void *s) {
   if (!d || !b || !x || max_steps < 1 || !(tol > 0.0))
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: bad arguments");
+  if ((const void *)b == (const void *)x)  // b is re-read after x is zeroed
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: b and x alias");
   if (!d->factored)
     return fail(TG_ERR_STATE, "tg_direct_solve_refined_tol: not factored");
   if (d->precision != TG_PREC_FP32)

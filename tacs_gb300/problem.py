@@ -174,6 +174,8 @@ class Direct:
         if self.precision == _lib.PREC_FP32 and b.dtype == torch.float64:
             if tol is None:
                 tol = 2.0 ** -53 * float(np.sqrt(b.numel()))
+            if x.data_ptr() == b.data_ptr():  # in place: refine from a copy
+                b = b.clone()
             st, eta = C.c_int(0), C.c_double(0.0)
             rc = L.tg_direct_solve_refined_tol(self.handle, _p(b), _p(x),
                                                int(steps), float(tol),
