@@ -391,6 +391,13 @@ class TACSAssembler {
                                       numAdjoints, ps.data(), ds.data(), 0),
           "addAdjointResProducts");
   }
+  // How the coordinate derivatives below are formed (no reference
+  // counterpart): false dual numbers per coordinate, true the reverse sweep
+  // per element; both exact.
+  void setXptReverseMode(bool reverse) {
+    check(tg_set_xpt_mode(a_, reverse ? TG_XPT_REVERSE : TG_XPT_FORWARD),
+          "setXptReverseMode");
+  }
   // TACSAssembler::addXptSens (src/TACSAssembler.cpp:4858): node vectors
   // from createNodeVec, 3 entries per node
   void addXptSens(double coef, int numFuncs, TACSFunction **funcs,
