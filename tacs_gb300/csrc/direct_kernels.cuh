@@ -243,13 +243,27 @@ __global__ void __launch_bounds__(256)
     Aj[r][q] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : 0.0;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < kTile * kTile; t += blockDim.x) {
-    const int r = t / kTile, c = t % kTile;
-    const int i = i0 + r, j = j0 + c;
-    if (i >= f.M || j >= f.M || j > i) continue;
-    T acc = 0;
-    for (int q = 0; q < nb; q++) acc += Ai[r][q] * Aj[c][q];
-    f.at(i, j) -= acc;
+  // a group owns rows (r, r + 16) x columns (c, c + 16) of the tile: one
+  // pass over q loads 4 operands for 4 products (half the shared-memory
+  // loads per FMA of one entry per pass; each entry keeps its own
+  // summation order over q)
+  constexpr int kHalf = kTile / 2;
+  for (int g = threadIdx.x; g < kHalf * kHalf; g += blockDim.x) {
+    const int r = g / kHalf, c = g % kHalf;
+    T a00 = 0, a01 = 0, a10 = 0, a11 = 0;
+    for (int q = 0; q < nb; q++) {
+      const T x0 = Ai[r][q], x1 = Ai[r + kHalf][q];
+      const T y0 = Aj[c][q], y1 = Aj[c + kHalf][q];
+      a00 += x0 * y0;
+      a01 += x0 * y1;
+      a10 += x1 * y0;
+      a11 += x1 * y1;
+    }
+    const int ia = i0 + r, ib = ia + kHalf, ja = j0 + c, jb = ja + kHalf;
+    if (ia < f.M && ja <= ia) f.at(ia, ja) -= a00;
+    if (ia < f.M && jb <= ia) f.at(ia, jb) -= a01;
+    if (ib < f.M && ja <= ib) f.at(ib, ja) -= a10;
+    if (ib < f.M && jb <= ib) f.at(ib, jb) -= a11;
   }
 }
 
