@@ -172,12 +172,15 @@ __global__ void __launch_bounds__(256)
     for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
       f.at(i, k) *= inv;
     __syncthreads();
-    // trailing update of rows and columns > k
+    // trailing update of rows and columns > k, lower triangle only:
+    // t = a (a + 1) / 2 + b with 0 <= b <= a < w
     const int w = f.M - k - 1;
-    const size_t total = (size_t)w * w;
-    for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const int i = k + 1 + (int)(t / w), j = k + 1 + (int)(t % w);
-      if (j > i) continue;
+    const int total = w * (w + 1) / 2;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      int a = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+      while ((a + 1) * (a + 2) / 2 <= t) a++;  // exact integer fix-up
+      while (a * (a + 1) / 2 > t) a--;
+      const int i = k + 1 + a, j = k + 1 + (t - a * (a + 1) / 2);
       f.at(i, j) -= f.at(i, k) * f.at(j, k);
     }
     __syncthreads();
