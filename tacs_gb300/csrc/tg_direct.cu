@@ -14,8 +14,12 @@
 #include "direct_symbolic.h"
 #include "tg_objects.h"
 
-// fronts of at most this many scalar rows are factored by one CTA each
-static constexpr int kSmallFront = 256;
+// fronts of at most this many scalar rows are factored by one CTA each,
+// all fronts of a level in one launch; larger ones by 32-column panels.
+// On a 512 x 512 plate 25 k of the 36 k fronts have at most 256 rows and
+// 9.9 k have 257 - 512 (12 % of the flops): on the panel path those would
+// cost ~14 serialised launches each.
+static constexpr int kSmallFront = 512;
 // blocks of the max-|x| reductions of the refinement's stopping test
 static constexpr int kRedParts = 256;
 

@@ -174,8 +174,8 @@ def _bcmask(prob):
 
 @pytest.mark.parametrize("name,prob", list(_problems()),
                          ids=[p[0] for p in _problems()])
-@pytest.mark.parametrize("small_max,coords", [(256, True), (0, True),
-                                              (1 << 30, False)])
+@pytest.mark.parametrize("small_max,coords", [(256, True), (512, True),
+                                              (0, True), (1 << 30, False)])
 def test_gpu_kernels_on_cpu_solve_assembled_system(de, name, prob, small_max,
                                                    coords):
     """small_max 0 sends every front through the panel + trailing-tile
