@@ -37,18 +37,14 @@ void launch_direct_factor_small(const DirectView &v, const int *sn,
 }
 
 template <class T>
-void launch_direct_factor_large(const DirectView &v, int sn, int M, int C,
-                                int *fail, cudaStream_t s) {
-  for (int k0 = 0; k0 < C; k0 += kPanel) {
-    const int nb = C - k0 < kPanel ? C - k0 : kPanel;
-    direct_panel_kernel<T><<<1, 256, 0, s>>>(v, sn, k0, nb, fail);
-    const int rest = M - (k0 + nb);
-    if (rest > 0) {
-      const int tiles = (rest + kTile - 1) / kTile;
-      direct_trailing_kernel<T><<<dim3(tiles, tiles), 256, 0, s>>>(v, sn, k0,
-                                                                    nb);
-    }
-  }
+void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
+                              const int *tprefix, int tiles, int k0,
+                              int *fail, cudaStream_t s) {
+  if (count <= 0) return;
+  direct_panel_kernel<T><<<count, 256, 0, s>>>(v, sn, count, k0, fail);
+  if (tiles > 0)
+    direct_trailing_kernel<T><<<tiles, 256, 0, s>>>(v, sn, tprefix, count,
+                                                     k0);
 }
 
 template <class T>
@@ -113,8 +109,9 @@ void direct_set_smem(int max_front) {
   template void launch_direct_factor_small<T>(const DirectView &,          \
                                               const int *, int, int *,     \
                                               cudaStream_t);               \
-  template void launch_direct_factor_large<T>(const DirectView &, int, int,  \
-                                              int, int *, cudaStream_t);   \
+  template void launch_direct_panel_step<T>(const DirectView &, const int *, \
+                                            int, const int *, int, int,      \
+                                            int *, cudaStream_t);            \
   template void launch_direct_forward<T>(const DirectView &, const int *,  \
                                          int, int, T *, T *, cudaStream_t); \
   template void launch_direct_backward<T>(const DirectView &, const int *, \

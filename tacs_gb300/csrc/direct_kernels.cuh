@@ -187,13 +187,20 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Large fronts.  Panel step: columns [k0, k0 + nb) of one front, all rows
-// from k0, factored by one CTA with the panel's own columns updated
-// left-looking inside the panel.
+// Large fronts, in panel steps batched over the large fronts of a level
+// (direct::panel_steps).  Panel step: columns [k0, k0 + nb) of front
+// sn[blockIdx.x], all rows from k0, nb = min(kPanel, C - k0) > 0, factored
+// by one CTA with the panel's own columns updated left-looking inside the
+// panel.
+constexpr int kTile = kDirectTile, kPanel = kDirectPanel;
 template <class T>
 __global__ void __launch_bounds__(256)
-    direct_panel_kernel(DirectView v, int s, int k0, int nb, int *fail) {
+    direct_panel_kernel(DirectView v, const int *__restrict__ sn, int count,
+                        int k0, int *fail) {
+  if ((int)blockIdx.x >= count) return;
+  const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
+  const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
   __shared__ T piv;
   for (int k = k0; k < k0 + nb; k++) {
     if (threadIdx.x == 0) {
@@ -226,17 +233,31 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Trailing update after a panel: F(i, j) -= sum_q F(i, q) F(j, q) over the
-// panel's columns q, for k1 <= j <= i < M, in 32 x 32 tiles (blockIdx.x =
-// tile column, blockIdx.y = tile row; tiles above the diagonal exit).
-constexpr int kTile = 32, kPanel = 32;
+// Trailing update after a panel step: F(i, j) -= sum_q F(i, q) F(j, q)
+// over the panel's columns q, for k1 <= j <= i < M, in 32 x 32 tiles.  One
+// CTA per lower-triangular tile of all the step's fronts: CTA b belongs to
+// the last front f with tprefix[f] <= b (fronts without tiles are skipped
+// that way) and is its tile tau = b - tprefix[f] = ti (ti + 1) / 2 + tj.
 template <class T>
 __global__ void __launch_bounds__(256)
-    direct_trailing_kernel(DirectView v, int s, int k0, int nb) {
-  const Front<T> f = front_of<T>(v, s);
+    direct_trailing_kernel(DirectView v, const int *__restrict__ sn,
+                           const int *__restrict__ tprefix, int count,
+                           int k0) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tprefix[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const Front<T> f = front_of<T>(v, sn[lo]);
+  const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
+  const int tau = b - tprefix[lo];
+  int ti = (int)((sqrtf(8.0f * (float)tau + 1.0f) - 1.0f) * 0.5f);
+  while ((ti + 1) * (ti + 2) / 2 <= tau) ti++;  // exact integer fix-up
+  while (ti * (ti + 1) / 2 > tau) ti--;
+  const int tj = tau - ti * (ti + 1) / 2;
   const int k1 = k0 + nb;
-  const int tj = blockIdx.x, ti = blockIdx.y;
-  if (tj > ti) return;
   const int i0 = k1 + ti * kTile, j0 = k1 + tj * kTile;
   if (i0 >= f.M || j0 >= f.M) return;
   __shared__ T Ai[kTile][kPanel + 1], Aj[kTile][kPanel + 1];

@@ -679,5 +679,60 @@ inline void plan_storage(Analysis &a) {
   a.u_peak = pool.peak();
 }
 
+// The factor's launch plan for fronts of more than small_max scalar rows:
+// they are factored level by level in panel steps of `panel` columns,
+// step p of a level taking the p-th panel of every large front of the
+// level that has one, then one grid over the lower-triangular
+// tile x tile blocks of all their trailing matrices.  Step t covers
+// fronts[front_off[t] .. + count[t]) at column k0[t]; tprefix[tile_off[t]
+// .. + count[t] + 1) is the prefix sum of their tile counts (total[t] in
+// all).  Shared by the runtime and the CPU emulation of its launches.
+struct PanelSteps {
+  std::vector<int> level, k0, front_off, count, tile_off, total;
+  std::vector<int> fronts, tprefix;
+};
+
+inline PanelSteps panel_steps(const Analysis &an, int bs, int small_max,
+                              int panel, int tile) {
+  PanelSteps ps;
+  const int nl = (int)an.level_ptr.size() - 1;
+  std::vector<int> large;
+  for (int L = 0; L < nl; L++) {
+    large.clear();
+    int maxc = 0;
+    for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+      const int s = an.level_sn[t];
+      const int M = (an.sn_rowptr[s + 1] - an.sn_rowptr[s]) * bs;
+      const int C = (an.sn_col[s + 1] - an.sn_col[s]) * bs;
+      if (M <= small_max) continue;
+      large.push_back(s);
+      maxc = std::max(maxc, C);
+    }
+    for (int k0 = 0; k0 < maxc; k0 += panel) {
+      ps.level.push_back(L);
+      ps.k0.push_back(k0);
+      ps.front_off.push_back((int)ps.fronts.size());
+      ps.tile_off.push_back((int)ps.tprefix.size());
+      int cnt = 0, tiles = 0;
+      ps.tprefix.push_back(0);
+      for (int s : large) {
+        const int M = (an.sn_rowptr[s + 1] - an.sn_rowptr[s]) * bs;
+        const int C = (an.sn_col[s + 1] - an.sn_col[s]) * bs;
+        if (C <= k0) continue;
+        const int nb = std::min(panel, C - k0);
+        const int rest = M - (k0 + nb);
+        const int nt = rest > 0 ? (rest + tile - 1) / tile : 0;
+        ps.fronts.push_back(s);
+        tiles += nt * (nt + 1) / 2;
+        ps.tprefix.push_back(tiles);
+        cnt++;
+      }
+      ps.count.push_back(cnt);
+      ps.total.push_back(tiles);
+    }
+  }
+  return ps;
+}
+
 }  // namespace direct
 }  // namespace tg

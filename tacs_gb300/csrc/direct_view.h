@@ -7,6 +7,9 @@
 
 namespace tg {
 
+// panel width and trailing tile of the large fronts' factorisation
+constexpr int kDirectPanel = 32, kDirectTile = 32;
+
 struct DirectView {
   int bs;
   const int *perm, *bcmask;  // position -> node; boundary dof mask per node

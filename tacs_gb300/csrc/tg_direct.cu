@@ -41,9 +41,11 @@ struct tg_direct {
   int precision = TG_PREC_FP64;
   tg::direct::Analysis an;
   std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
-  // per level: its small fronts (one launch, d_small) and its large ones
-  std::vector<int> small_ptr_h, large_ptr_h, large_h;
-  int *d_small = nullptr;
+  // per level: its small fronts (one launch, d_small) and the panel steps
+  // of its large ones (steps of level L: step_ptr_h[L] .. [L + 1])
+  std::vector<int> small_ptr_h, step_ptr_h;
+  tg::direct::PanelSteps steps;
+  int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr;
   // device copies of the analysis
   int *d_perm = nullptr, *d_bcmask = nullptr, *d_sn_col = nullptr,
       *d_sn_rowptr = nullptr, *d_sn_rows = nullptr, *d_sn_parent = nullptr,
@@ -102,6 +104,7 @@ struct tg_direct {
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
     dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
+    dfree(d_step_fronts); dfree(d_step_tprefix);
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
     dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
@@ -164,15 +167,20 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   }
   std::vector<int> small_h;
   d->small_ptr_h.assign(1, 0);
-  d->large_ptr_h.assign(1, 0);
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
       const int sn = an.level_sn[t];
-      if (d->front_m_h[sn] > kSmallFront) d->large_h.push_back(sn);
-      else small_h.push_back(sn);
+      if (d->front_m_h[sn] <= kSmallFront) small_h.push_back(sn);
     }
     d->small_ptr_h.push_back((int)small_h.size());
-    d->large_ptr_h.push_back((int)d->large_h.size());
+  }
+  d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
+                                     tg::kDirectTile);
+  {
+    const int nlev = (int)an.level_ptr.size() - 1;
+    d->step_ptr_h.assign(nlev + 1, 0);
+    for (int L : d->steps.level) d->step_ptr_h[L + 1]++;
+    for (int L = 0; L < nlev; L++) d->step_ptr_h[L + 1] += d->step_ptr_h[L];
   }
   std::vector<int> bcmask(d->n, 0);
   for (size_t k = 0; k < a->bc_nodes_h.size(); k++)
@@ -196,6 +204,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_ch_list, ch_list);
   if (!rc) rc = upload(&d->d_level_sn, an.level_sn);
   if (!rc) rc = upload(&d->d_small, small_h);
+  if (!rc) rc = upload(&d->d_step_fronts, d->steps.fronts);
+  if (!rc) rc = upload(&d->d_step_tprefix, d->steps.tprefix);
   if (!rc) rc = upload(&d->d_l_off, an.l_off);
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
@@ -259,10 +269,12 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
     const int sb = d->small_ptr_h[L], se = d->small_ptr_h[L + 1];
     tg::launch_direct_factor_small<T>(v, d->d_small + sb, se - sb, d->d_fail,
                                       s);
-    for (int t = d->large_ptr_h[L]; t < d->large_ptr_h[L + 1]; t++) {
-      const int sn = d->large_h[t];
-      tg::launch_direct_factor_large<T>(v, sn, d->front_m_h[sn],
-                                        d->front_c_h[sn], d->d_fail, s);
+    for (int t = d->step_ptr_h[L]; t < d->step_ptr_h[L + 1]; t++) {
+      const tg::direct::PanelSteps &ps = d->steps;
+      tg::launch_direct_panel_step<T>(
+          v, d->d_step_fronts + ps.front_off[t], ps.count[t],
+          d->d_step_tprefix + ps.tile_off[t], ps.total[t], ps.k0[t],
+          d->d_fail, s);
     }
   }
 }

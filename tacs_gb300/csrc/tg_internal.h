@@ -285,9 +285,13 @@ void launch_direct_level_assemble(const DirectView &v, const int *sn,
 template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s);
+// one panel step of the large fronts of a level (direct::panel_steps):
+// the panels of fronts sn[0 .. count) at column k0, then their trailing
+// tiles (tiles in all, prefix sums tprefix[0 .. count])
 template <class T>
-void launch_direct_factor_large(const DirectView &v, int sn, int M, int C,
-                                int *fail, cudaStream_t s);
+void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
+                              const int *tprefix, int tiles, int k0,
+                              int *fail, cudaStream_t s);
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
                            int max_front, T *y, T *contrib, cudaStream_t s);

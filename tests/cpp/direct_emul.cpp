@@ -133,17 +133,18 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   set_store(v, lstore.data(), pool.data());
 
   // factor: the sequence of tg_direct_factor (small fronts of a level in
-  // one launch, large ones panel by panel)
-  std::vector<int> small_h, small_ptr(1, 0), large_h, large_ptr(1, 0);
+  // one launch, large ones in panel steps batched over the level)
+  std::vector<int> small_h, small_ptr(1, 0);
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
       const int sn = an.level_sn[t];
-      if (fm[sn] > small_max) large_h.push_back(sn);
-      else small_h.push_back(sn);
+      if (fm[sn] <= small_max) small_h.push_back(sn);
     }
     small_ptr.push_back((int)small_h.size());
-    large_ptr.push_back((int)large_h.size());
   }
+  const tg::direct::PanelSteps ps = tg::direct::panel_steps(
+      an, bs, small_max, tg::kDirectPanel, tg::kDirectTile);
+  size_t step = 0;
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
     const int *lv = an.level_sn.data() + lb;
@@ -155,17 +156,14 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     if (se > sb)
       launch(direct_factor_small_kernel<T>, se - sb, 1, 0, v,
              (const int *)small_h.data() + sb, se - sb, &failflag);
-    for (int t = large_ptr[L]; t < large_ptr[L + 1]; t++) {
-      const int sn = large_h[t];
-      for (int k0 = 0; k0 < fc[sn]; k0 += kPanel) {
-        const int nb = std::min(kPanel, fc[sn] - k0);
-        launch(direct_panel_kernel<T>, 1, 1, 0, v, sn, k0, nb, &failflag);
-        const int rest = fm[sn] - (k0 + nb);
-        if (rest > 0) {
-          const unsigned tiles = (rest + kTile - 1) / kTile;
-          launch(direct_trailing_kernel<T>, tiles, tiles, 0, v, sn, k0, nb);
-        }
-      }
+    for (; step < ps.level.size() && ps.level[step] == (int)L; step++) {
+      const int *fr = ps.fronts.data() + ps.front_off[step];
+      const int *tp = ps.tprefix.data() + ps.tile_off[step];
+      launch(direct_panel_kernel<T>, ps.count[step], 1, 0, v, fr,
+             ps.count[step], ps.k0[step], &failflag);
+      if (ps.total[step] > 0)
+        launch(direct_trailing_kernel<T>, ps.total[step], 1, 0, v, fr, tp,
+               ps.count[step], ps.k0[step]);
     }
   }
   if (failflag) return failflag;
