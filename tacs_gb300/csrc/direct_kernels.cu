@@ -38,10 +38,13 @@ void launch_direct_factor_small(const DirectView &v, const int *sn,
 
 template <class T>
 void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
-                              const int *tprefix, int tiles, int k0,
+                              const int *tprefix, int tiles,
+                              const int *rprefix, int rblocks, int k0,
                               int *fail, cudaStream_t s) {
   if (count <= 0) return;
   direct_panel_kernel<T><<<count, 256, 0, s>>>(v, sn, count, k0, fail);
+  if (rblocks > 0)
+    direct_trsm_kernel<T><<<rblocks, 256, 0, s>>>(v, sn, rprefix, count, k0);
   if (tiles > 0)
     direct_trailing_kernel<T><<<tiles, 256, 0, s>>>(v, sn, tprefix, count,
                                                      k0);
@@ -110,8 +113,9 @@ void direct_set_smem(int max_front) {
                                               const int *, int, int *,     \
                                               cudaStream_t);               \
   template void launch_direct_panel_step<T>(const DirectView &, const int *, \
-                                            int, const int *, int, int,      \
-                                            int *, cudaStream_t);            \
+                                            int, const int *, int,           \
+                                            const int *, int, int, int *,    \
+                                            cudaStream_t);                   \
   template void launch_direct_forward<T>(const DirectView &, const int *,  \
                                          int, int, T *, T *, cudaStream_t); \
   template void launch_direct_backward<T>(const DirectView &, const int *, \

@@ -188,10 +188,11 @@ __global__ void __launch_bounds__(256)
 }
 
 // Large fronts, in panel steps batched over the large fronts of a level
-// (direct::panel_steps).  Panel step: columns [k0, k0 + nb) of front
-// sn[blockIdx.x], all rows from k0, nb = min(kPanel, C - k0) > 0, factored
-// by one CTA with the panel's own columns updated left-looking inside the
-// panel.
+// (direct::panel_steps).  A step has three launches: this kernel factors
+// the nb x nb diagonal block of columns [k0, k0 + nb) of front
+// sn[blockIdx.x] (nb = min(kPanel, C - k0) > 0, one CTA, right-looking);
+// direct_trsm_kernel solves the rows below against it; the trailing
+// kernel updates the rest of the front.
 constexpr int kTile = kDirectTile, kPanel = kDirectPanel;
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -215,13 +216,14 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     const T inv = T(1) / piv;
-    for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
+    const int kend = k0 + nb;
+    for (int i = k + 1 + threadIdx.x; i < kend; i += blockDim.x)
       f.at(i, k) *= inv;
     __syncthreads();
-    // update the rest of the panel's columns (k, k0 + nb)
-    const int w = k0 + nb - k - 1;
+    // update the rest of the diagonal block's columns (k, k0 + nb)
+    const int w = kend - k - 1;
     if (w > 0) {
-      const int rows = f.M - k - 1;
+      const int rows = kend - k - 1;
       const size_t total = (size_t)rows * w;
       for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
         const int i = k + 1 + (int)(t / w), j = k + 1 + (int)(t % w);
@@ -230,6 +232,51 @@ __global__ void __launch_bounds__(256)
       }
     }
     __syncthreads();
+  }
+}
+
+// Rows below a panel's diagonal block: L21 = A21 L11^-T, row by row
+// (forward substitution against the diagonal block, held in shared
+// memory), one thread per row, kTrsmRows rows per CTA; CTA b belongs to
+// the last front f with rprefix[f] <= b and takes its row block
+// b - rprefix[f].
+constexpr int kTrsmRows = kDirectTrsmRows;
+template <class T>
+__global__ void __launch_bounds__(256)
+    direct_trsm_kernel(DirectView v, const int *__restrict__ sn,
+                       const int *__restrict__ rprefix, int count, int k0) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (rprefix[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const Front<T> f = front_of<T>(v, sn[lo]);
+  const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
+  const int r0 = k0 + nb + (b - rprefix[lo]) * kTrsmRows;
+  const int r1 = r0 + kTrsmRows < f.M ? r0 + kTrsmRows : f.M;
+  __shared__ T Ld[kPanel][kPanel + 1];
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    Ld[r][c] = c <= r ? f.at(k0 + r, k0 + c) : T(0);
+  }
+  __syncthreads();
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    T x[kPanel];
+#pragma unroll
+    for (int k = 0; k < kPanel; k++) {
+      if (k < nb) {
+        T acc = f.at(i, k0 + k);
+#pragma unroll
+        for (int q = 0; q < kPanel; q++)
+          if (q < k) acc -= x[q] * Ld[k][q];
+        x[k] = acc / Ld[k][k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kPanel; k++)
+      if (k < nb) f.at(i, k0 + k) = x[k];
   }
 }
 

@@ -687,13 +687,16 @@ inline void plan_storage(Analysis &a) {
 // fronts[front_off[t] .. + count[t]) at column k0[t]; tprefix[tile_off[t]
 // .. + count[t] + 1) is the prefix sum of their tile counts (total[t] in
 // all).  Shared by the runtime and the CPU emulation of its launches.
+//   Below each panel's diagonal block, the rows solved against it go in blocks
+// of `rows` rows: rprefix[tile_off[t] .. + count[t] + 1) is the prefix sum
+// of the fronts' row-block counts (rtotal[t] in all).
 struct PanelSteps {
-  std::vector<int> level, k0, front_off, count, tile_off, total;
-  std::vector<int> fronts, tprefix;
+  std::vector<int> level, k0, front_off, count, tile_off, total, rtotal;
+  std::vector<int> fronts, tprefix, rprefix;
 };
 
 inline PanelSteps panel_steps(const Analysis &an, int bs, int small_max,
-                              int panel, int tile) {
+                              int panel, int tile, int rows) {
   PanelSteps ps;
   const int nl = (int)an.level_ptr.size() - 1;
   std::vector<int> large;
@@ -713,8 +716,9 @@ inline PanelSteps panel_steps(const Analysis &an, int bs, int small_max,
       ps.k0.push_back(k0);
       ps.front_off.push_back((int)ps.fronts.size());
       ps.tile_off.push_back((int)ps.tprefix.size());
-      int cnt = 0, tiles = 0;
+      int cnt = 0, tiles = 0, rblocks = 0;
       ps.tprefix.push_back(0);
+      ps.rprefix.push_back(0);
       for (int s : large) {
         const int M = (an.sn_rowptr[s + 1] - an.sn_rowptr[s]) * bs;
         const int C = (an.sn_col[s + 1] - an.sn_col[s]) * bs;
@@ -725,10 +729,13 @@ inline PanelSteps panel_steps(const Analysis &an, int bs, int small_max,
         ps.fronts.push_back(s);
         tiles += nt * (nt + 1) / 2;
         ps.tprefix.push_back(tiles);
+        rblocks += rest > 0 ? (rest + rows - 1) / rows : 0;
+        ps.rprefix.push_back(rblocks);
         cnt++;
       }
       ps.count.push_back(cnt);
       ps.total.push_back(tiles);
+      ps.rtotal.push_back(rblocks);
     }
   }
   return ps;

@@ -9,6 +9,8 @@ namespace tg {
 
 // panel width and trailing tile of the large fronts' factorisation
 constexpr int kDirectPanel = 32, kDirectTile = 32;
+// rows of a panel's off-diagonal part solved by one CTA (one per thread)
+constexpr int kDirectTrsmRows = 256;
 
 struct DirectView {
   int bs;

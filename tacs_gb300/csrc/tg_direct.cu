@@ -45,7 +45,8 @@ struct tg_direct {
   // of its large ones (steps of level L: step_ptr_h[L] .. [L + 1])
   std::vector<int> small_ptr_h, step_ptr_h;
   tg::direct::PanelSteps steps;
-  int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr;
+  int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr,
+      *d_step_rprefix = nullptr;
   // device copies of the analysis
   int *d_perm = nullptr, *d_bcmask = nullptr, *d_sn_col = nullptr,
       *d_sn_rowptr = nullptr, *d_sn_rows = nullptr, *d_sn_parent = nullptr,
@@ -104,7 +105,7 @@ struct tg_direct {
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
     dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
-    dfree(d_step_fronts); dfree(d_step_tprefix);
+    dfree(d_step_fronts); dfree(d_step_tprefix); dfree(d_step_rprefix);
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
     dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
@@ -175,7 +176,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     d->small_ptr_h.push_back((int)small_h.size());
   }
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
-                                     tg::kDirectTile);
+                                     tg::kDirectTile, tg::kDirectTrsmRows);
   {
     const int nlev = (int)an.level_ptr.size() - 1;
     d->step_ptr_h.assign(nlev + 1, 0);
@@ -206,6 +207,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_small, small_h);
   if (!rc) rc = upload(&d->d_step_fronts, d->steps.fronts);
   if (!rc) rc = upload(&d->d_step_tprefix, d->steps.tprefix);
+  if (!rc) rc = upload(&d->d_step_rprefix, d->steps.rprefix);
   if (!rc) rc = upload(&d->d_l_off, an.l_off);
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
@@ -273,7 +275,8 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
       const tg::direct::PanelSteps &ps = d->steps;
       tg::launch_direct_panel_step<T>(
           v, d->d_step_fronts + ps.front_off[t], ps.count[t],
-          d->d_step_tprefix + ps.tile_off[t], ps.total[t], ps.k0[t],
+          d->d_step_tprefix + ps.tile_off[t], ps.total[t],
+          d->d_step_rprefix + ps.tile_off[t], ps.rtotal[t], ps.k0[t],
           d->d_fail, s);
     }
   }

@@ -286,11 +286,13 @@ template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s);
 // one panel step of the large fronts of a level (direct::panel_steps):
-// the panels of fronts sn[0 .. count) at column k0, then their trailing
-// tiles (tiles in all, prefix sums tprefix[0 .. count])
+// the diagonal blocks of fronts sn[0 .. count) at column k0, the rows
+// below them (rblocks row blocks, prefix sums rprefix[0 .. count]), then
+// their trailing tiles (tiles in all, prefix sums tprefix[0 .. count])
 template <class T>
 void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
-                              const int *tprefix, int tiles, int k0,
+                              const int *tprefix, int tiles,
+                              const int *rprefix, int rblocks, int k0,
                               int *fail, cudaStream_t s);
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,

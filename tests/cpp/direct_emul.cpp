@@ -143,7 +143,8 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     small_ptr.push_back((int)small_h.size());
   }
   const tg::direct::PanelSteps ps = tg::direct::panel_steps(
-      an, bs, small_max, tg::kDirectPanel, tg::kDirectTile);
+      an, bs, small_max, tg::kDirectPanel, tg::kDirectTile,
+      tg::kDirectTrsmRows);
   size_t step = 0;
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
@@ -159,8 +160,12 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     for (; step < ps.level.size() && ps.level[step] == (int)L; step++) {
       const int *fr = ps.fronts.data() + ps.front_off[step];
       const int *tp = ps.tprefix.data() + ps.tile_off[step];
+      const int *rp = ps.rprefix.data() + ps.tile_off[step];
       launch(direct_panel_kernel<T>, ps.count[step], 1, 0, v, fr,
              ps.count[step], ps.k0[step], &failflag);
+      if (ps.rtotal[step] > 0)
+        launch(direct_trsm_kernel<T>, ps.rtotal[step], 1, 0, v, fr, rp,
+               ps.count[step], ps.k0[step]);
       if (ps.total[step] > 0)
         launch(direct_trailing_kernel<T>, ps.total[step], 1, 0, v, fr, tp,
                ps.count[step], ps.k0[step]);
