@@ -40,17 +40,7 @@ UNIT = "elements/s"
 
 def c2_problem(n=512, L=2.0, seed=2):
     from tacs_gb300 import meshes
-    rng = np.random.default_rng(seed)
-    p = meshes.plate(n, n, L, L, t=0.01, E=70e9, nu=0.3, rho=2700.0,
-                     ys=2.7e8, thick=rng.uniform(0.005, 0.02, n * n))
-    e = meshes.plate_edges(n, n).astype(np.int32)
-    p["bc_nodes"], p["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
-    xyz = p["xpts"].reshape(-1, 3)
-    pn = 1e3 * (1.0 + 0.5 * np.sin(np.pi * xyz[:, 0]) * np.sin(np.pi * xyz[:, 1]))
-    conn = p["conn"].reshape(-1, 4)
-    p["pres_elems"] = np.arange(n * n, dtype=np.int32)
-    p["pres_vals"] = pn[conn].ravel()
-    return p
+    return meshes.plate_c2(n, L, seed)
 
 
 def clamped_plate(n, seed=5):

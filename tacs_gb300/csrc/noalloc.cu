@@ -56,7 +56,7 @@ __global__ void finalize_funcs_kernel(const double *scalars, double ksw,
                                       double *vals) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     vals[0] = scalars[0];
-    vals[1] = scalars[1] + log(scalars[2] / 1.0) / ksw;
+    vals[1] = scalars[1] + log(scalars[2]) / ksw;
   }
 }
 

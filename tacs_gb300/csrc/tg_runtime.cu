@@ -419,7 +419,7 @@ int tg_eval_functions(tg_assembler *a, const double *vars, int nfuncs,
   for (int i = 0; i < nfuncs; i++) {
     if (funcs[i] == TG_FUNC_COMPLIANCE) vals[i] = h[0];
     else if (funcs[i] == TG_FUNC_KS_FAILURE)
-      vals[i] = h[1] + std::log(h[2] / 1.0) / ks_weight;
+      vals[i] = h[1] + std::log(h[2]) / ks_weight;
     else return fail(TG_ERR_ARG, "tg_eval_functions: unknown function");
   }
   if (!std::isfinite(h[0]) || !std::isfinite(h[1]) || !std::isfinite(h[2]))

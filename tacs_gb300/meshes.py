@@ -230,6 +230,26 @@ def clamped_plate(n, L=1.0, thick=None, pressure=1e3, t=0.01):
     return p
 
 
+def plate_c2(n=512, L=2.0, seed=2):
+    """Simply supported MITC4 plate: n x n elements on an L x L square,
+    per-element thickness ~ U[0.005, 0.02] (numpy default_rng(seed)),
+    E 70e9, nu 0.3, rho 2700, ys 2.7e8; edge nodes hold u, v, w (mask 0x07);
+    nodal pressure p(x, y) = 1e3 (1 + 0.5 sin(pi x) sin(pi y)) with x, y in
+    metres on every element."""
+    rng = np.random.default_rng(seed)
+    p = plate(n, n, L, L, t=0.01, E=70e9, nu=0.3, rho=2700.0, ys=2.7e8,
+              thick=rng.uniform(0.005, 0.02, n * n))
+    e = plate_edges(n, n).astype(np.int32)
+    p["bc_nodes"], p["bc_masks"] = e, np.full(len(e), 0x07, np.int32)
+    xyz = p["xpts"].reshape(-1, 3)
+    pn = 1e3 * (1.0 + 0.5 * np.sin(np.pi * xyz[:, 0])
+                * np.sin(np.pi * xyz[:, 1]))
+    conn = p["conn"].reshape(-1, 4)
+    p["pres_elems"] = np.arange(n * n, dtype=np.int32)
+    p["pres_vals"] = pn[conn].ravel()
+    return p
+
+
 def batch_plates(count=48, seed=4, nmin=16, nmax=256, L=1.0, tmin=0.004,
                  tmax=0.02, pressure=1e3, point_load=1e3):
     """Independent clamped MITC4 plates of seeded uneven sizes in one problem.

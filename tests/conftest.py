@@ -28,13 +28,18 @@ def _late(item):
                 or item.get_closest_marker("late"))
 
 
+def _last(item):
+    return os.path.basename(str(item.fspath)) == "test_zz_no_alloc.py"
+
+
 def pytest_collection_modifyitems(session, config, items):
     """Tests of the direct factorisation and of other newer kernels run
     after the others (stable order otherwise): the established parity tests
     come first, so that under -x a failure in a newer path cannot stop
-    them."""
-    items[:] = ([i for i in items if not _late(i)]
-                + [i for i in items if _late(i)])
+    them.  The allocation-free entry point's tests run last of all."""
+    items[:] = ([i for i in items if not _late(i) and not _last(i)]
+                + [i for i in items if _late(i) and not _last(i)]
+                + [i for i in items if _last(i)])
 
 
 def load_case(name):

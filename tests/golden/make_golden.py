@@ -264,7 +264,7 @@ CASES = {
 
 # Large reference arrays that are not stored for the bigger cases (their
 # content is covered by the smaller ones); scalars and vectors always are.
-DROP_LARGE = {"shell_c1": {"jac_nobc_vals", "jac_vals"}}
+DROP_LARGE = {"shell_c1": {"jac_nobc_vals"}}
 
 
 def main(names=None):
@@ -310,5 +310,8 @@ if __name__ == "__main__":
         add_keys(sys.argv[2:], GEN_CPLX, XPT_KEYS)
     elif sys.argv[1:2] == ["--iluk"]:
         add_keys(sys.argv[2:], GEN, ILUK_KEYS)
+    elif sys.argv[1:2] == ["--keys"]:
+        # --keys k1,k2 case...: add the named reference outputs
+        add_keys(sys.argv[3:], GEN, tuple(sys.argv[2].split(",")))
     else:
         main(sys.argv[1:] or None)

@@ -1,11 +1,13 @@
 """The allocation-free entry point tg_eval_functions_noalloc, called
 through the C ABI, against the allocating path (tg_eval_functions).
 
-This file sorts after the other tests of the iterative path (only the
-direct factorisation's tests follow it) so that a run stopping at its
-first failure has already run those; it must also pass alone in a fresh
-process
-(the first call on the device performs the scratch-address set-up).
+Callers that cannot allocate device memory (a host framework that hands
+out views of its own pre-allocated arena, or a loop that has frozen its
+memory footprint) use this entry point.  The test file sorts after every
+other test (tests/conftest.py orders it last), so that a run stopping at its
+first failure has already run the rest; it must also pass alone in a fresh
+process, where the first call on the device performs the scratch-address
+set-up.
 """
 import ctypes as C
 
@@ -62,7 +64,13 @@ def test_noalloc_matches_allocating_path_twice():
             u = M.vec(scale * rng.standard_normal(M.ndof))
             ref = M.eval_functions(u, (0, 1))
             out = torch.full((2,), np.nan, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             assert _noalloc(L, prob, u, out) == 0, L.tg_last_error()
+            if call == 1:
+                # the first call may load kernel modules; the second one
+                # must leave the device's free memory exactly as it was
+                assert torch.cuda.mem_get_info()[0] == free0
             got = out.cpu().numpy()
             assert rel(got, ref) < TOL, (call, got, ref)
 
