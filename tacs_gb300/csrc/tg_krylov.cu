@@ -351,6 +351,9 @@ int fetch(std::vector<T> &h, const T *d, size_t n, cudaStream_t s) {
 // for some system, the remaining passes run the all-FP64 solve (an FP64
 // factor of the same matrix, made then, and the FP64 mat-vec) to the full
 // tolerance, and a system stops when a pass no longer halves its residual.
+// A system whose FP64 passes stop there with a true residual at or below
+// eps (|A| |x| + |b|), the accuracy FP64 arithmetic can attain, has
+// converged (where rtol |r0| lies below that floor no solver meets it).
 int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
                   int zero_guess, int *iters, int *flags, double *resn,
                   cudaStream_t s) {
@@ -372,6 +375,23 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
   const int mode_in = mode;
   // TG_KSM_TRACE=1 prints each refinement pass's relative true residuals
   const bool trace = std::getenv("TG_KSM_TRACE") != nullptr;
+  // Mixed precision: the accuracy an FP64 iterate can attain is about
+  // eps (|A| |x| + |b|) per system (normwise backward error at the unit
+  // roundoff), with |A| the 2-norm of the row 1-norms (not below the
+  // Frobenius or spectral norm).  A system whose FP64 passes stagnate at or
+  // below it has converged as far as FP64 arithmetic allows, even where
+  // rtol |r0| lies below that floor (thin shells: cond(A) ~ 1e12).
+  std::vector<double> anorm, bnorm, xnorm, floor_(ns, 0.0);
+  if (mode_in == 1) {
+    launch_bcsr_row_abs_sum(A->bsize, A->nrows, A->a->d_rowp, A->d_vals,
+                            k->d_X, s);
+    for (int l = 1; l < k->nrhs; l++)
+      TG_CUDA(cudaMemcpyAsync(k->d_X + (size_t)l * k->n, k->d_X,
+                              k->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                              s));
+    if ((rc = seg_norms(k, k->d_X, anorm, s))) return rc;
+    if ((rc = seg_norms(k, k->d_Bo, bnorm, s))) return rc;
+  }
   for (int outer = 0; outer <= max_outer; outer++) {
     launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
                      A->d_vals, k->d_Xo, k->d_B, s, k->nrhs, k->n);
@@ -406,10 +426,19 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
           }
       }
     }
+    if (mode_in == 1) {
+      if ((rc = seg_norms(k, k->d_Xo, xnorm, s))) return rc;
+      for (int i = 0; i < ns; i++)
+        floor_[i] = 0x1p-53 * (anorm[i] * xnorm[i] + bnorm[i]);
+    }
     for (int i = 0; i < ns; i++) {
       if (!std::isfinite(rn[i]))
         return fail(TG_ERR_NONFINITE, "GMRES: non-finite true residual");
-      if (done[i]) continue;
+      if (done[i]) {
+        // a system stopped (taken back) at the FP64 accuracy floor
+        if (mode_in == 1 && !conv[i] && rn[i] <= floor_[i]) conv[i] = 1;
+        continue;
+      }
       const bool met = rn[i] <= k->rtol * r0[i] || rn[i] < k->atol;
       if (met) {
         done[i] = 1;
@@ -421,7 +450,11 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
         // FP64
         to_fp64 = true;
       } else if (stuck[i] || (outer > 0 && rn[i] > 0.5 * prev[i])) {
-        if (mode_in == 1 && mode == 0 && !fresh[i]) {
+        if (mode_in == 1 && mode == 0 && rn[i] <= floor_[i]) {
+          // the FP64 passes stagnated at the attainable accuracy
+          done[i] = 1;
+          conv[i] = 1;
+        } else if (mode_in == 1 && mode == 0 && !fresh[i]) {
           // the FP64 passes stalled from the mixed-precision iterate (its
           // residual is left in the hardest modes, where restarted GMRES
           // stagnates): solve this system again from zero, all in FP64
@@ -432,6 +465,7 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
         }
       } else if (outer == max_outer) {
         done[i] = 1;
+        if (mode_in == 1 && mode == 0 && rn[i] <= floor_[i]) conv[i] = 1;
       }
     }
     if (to_fp64) {

@@ -1,14 +1,18 @@
 // Static analysis with adjoint gradients through the C++ interface
-// (include/tacs_gb300.hpp), written the way a TACS C++ driver does it
-// (examples/plate/plate.cpp with the solve and adjoint recipe of
-// tests/integration_tests/static_analysis_base_test.py:359-427): the
-// 32 x 32 clamped MITC4 plate under 1e3 Pa, t = 0.01, one thickness design
-// variable per element.  Prints one JSON object: the compliance, the KS
-// failure value and both gradients.  With the argument "direct" both
-// solves use TACSSchurPc (the complete factorisation) instead of GMRES
-// with ILU(0).
+// (include/tacs_gb300.hpp), written with the reference's classes and call
+// pattern (an MPI communicator, per-element TACSIsoShellConstitutive /
+// TACSQuad4Shell objects through setElements(TACSElement **), TACSShellPressure
+// auxiliary elements, createMat / createSchurMat, TACSAdditiveSchwarz or
+// TACSSchurPc inside GMRES, incref / decref; the order of examples/plate/
+// plate.cpp and of the solve and adjoint recipe of tests/integration_tests/
+// static_analysis_base_test.py:359-427): the 32 x 32 clamped MITC4 plate
+// under 1e3 Pa, t = 0.01, one thickness design variable per element.
+// Prints one JSON object: the compliance, the KS failure value and both
+// gradients (thickness and node coordinates).  With the argument "direct"
+// the solves use TACSSchurPc (the complete factorisation) as GMRES's
+// preconditioner instead of ILU(0).
 #include <cstdio>
-#include <string>
+#include <cstring>
 #include <vector>
 
 #include "tacs_gb300.hpp"
@@ -16,9 +20,18 @@
 using namespace tacs_gb300;
 
 int main(int argc, char **argv) {
-  const bool direct = argc > 1 && std::string(argv[1]) == "direct";
-  const int n = 32, nx = n + 1, nnodes = nx * nx, nelems = n * n;
-  std::vector<int> ptr(nelems + 1), conn(4 * nelems);
+  const bool direct = argc > 1 && std::strcmp(argv[1], "direct") == 0;
+  MPI_Comm comm = MPI_COMM_WORLD;
+  const int n = 32, nx = n + 1, numNodes = nx * nx, numElements = n * n;
+  const int varsPerNode = 6;
+
+  TACSAssembler *assembler =
+      new TACSAssembler(comm, varsPerNode, numNodes, numElements);
+  assembler->incref();
+
+  int *ptr = new int[numElements + 1];
+  int *conn = new int[4 * numElements];
+  ptr[0] = 0;
   for (int j = 0; j < n; j++)
     for (int i = 0; i < n; i++) {
       const int e = i + n * j, n0 = i + nx * j;
@@ -26,90 +39,105 @@ int main(int argc, char **argv) {
       conn[4 * e + 1] = n0 + 1;
       conn[4 * e + 2] = n0 + nx;
       conn[4 * e + 3] = n0 + nx + 1;
+      ptr[e + 1] = 4 * (e + 1);
     }
-  for (int e = 0; e <= nelems; e++) ptr[e] = 4 * e;
+  assembler->setElementConnectivity(ptr, conn);
+  delete[] conn;
+  delete[] ptr;
 
-  TACSAssembler assembler(6, nnodes, nelems);
-  assembler.setElementConnectivity(ptr.data(), conn.data());
-  TACSElementSpec spec;
-  spec.elem_type = TG_ELEM_MITC4;
-  spec.rho = 2700.0;
-  spec.E = 70e9;
-  spec.nu = 0.3;
-  spec.ys = 2.7e8;
-  spec.t.assign(nelems, 0.01);
-  for (int e = 0; e < nelems; e++) spec.tNum.push_back(e);
-  assembler.setElements(spec);
+  TacsScalar rho = 2700.0, specific_heat = 0.0, E = 70e9, nu = 0.3;
+  TacsScalar ys = 2.7e8, cte = 0.0, kappa = 0.0;
+  TACSMaterialProperties *props =
+      new TACSMaterialProperties(rho, specific_heat, E, nu, ys, cte, kappa);
+  TACSShellTransform *transform = new TACSShellNaturalTransform();
+  TACSElement **elements = new TACSElement *[numElements];
+  for (int e = 0; e < numElements; e++) {
+    TACSShellConstitutive *con = new TACSIsoShellConstitutive(props, 0.01, e);
+    elements[e] = new TACSQuad4Shell(transform, con);
+  }
+  assembler->setElements(elements);
+  delete[] elements;
+
   std::vector<int> edge;
-  for (int k = 0; k < nnodes; k++) {
+  for (int k = 0; k < numNodes; k++) {
     const int i = k % nx, j = k / nx;
     if (i == 0 || j == 0 || i == n || j == n) edge.push_back(k);
   }
-  assembler.addBCs((int)edge.size(), edge.data());
-  TACSAuxElements aux;
-  const double p[4] = {1e3, 1e3, 1e3, 1e3};
-  for (int e = 0; e < nelems; e++) aux.addPressure(e, p);
-  assembler.setAuxElements(aux);
-  assembler.initialize();
+  assembler->addBCs((int)edge.size(), edge.data());
 
-  TACSBVec *X = assembler.createNodeVec();
-  std::vector<double> xyz(3 * nnodes);
-  for (int k = 0; k < nnodes; k++) {
+  TACSAuxElements *aux = new TACSAuxElements(numElements);
+  TACSElement *pressure = new TACSShellPressure(1e3);
+  for (int e = 0; e < numElements; e++) aux->addElement(e, pressure);
+  assembler->setAuxElements(aux);
+
+  if (assembler->initialize() != 0) {
+    assembler->decref();
+    return 1;
+  }
+
+  TACSBVec *X = assembler->createNodeVec();
+  X->incref();
+  std::vector<TacsScalar> xyz(3 * numNodes);
+  for (int k = 0; k < numNodes; k++) {
     xyz[3 * k] = (k % nx) / (double)n;
     xyz[3 * k + 1] = (k / nx) / (double)n;
     xyz[3 * k + 2] = 0.0;
   }
-  X->setValues(xyz.data());
-  assembler.setNodes(X);
+  X->copyFromHost(xyz.data());
+  assembler->setNodes(X);
 
-  TACSBVec *res = assembler.createVec(), *ans = assembler.createVec();
-  BCSRMat *mat = assembler.createMat();
-  assembler.zeroVariables();
-  assembler.assembleJacobian(1.0, 0.0, 0.0, res, mat);
-  TACSAdditiveSchwarz pc(mat, 0, 10.0);
-  pc.factor();
-  GMRES gmres(mat, &pc, 300, 10, 0);
-  gmres.setTolerances(1e-12, 1e-30);
-  TACSSchurPc *schur = nullptr;
-  if (direct) {
-    schur = new TACSSchurPc(mat);
-    schur->factor();
-  }
-  auto solve = [&](TACSBVec *b, TACSBVec *x) {
-    if (!direct) return gmres.solve(b, x);
-    schur->applyFactor(b, x);
-    return 1;
-  };
-  const int flag = solve(res, ans);
+  TACSBVec *res = assembler->createVec();
+  TACSBVec *ans = assembler->createVec();
+  res->incref();
+  ans->incref();
+
+  TACSParallelMat *mat =
+      direct ? assembler->createSchurMat() : assembler->createMat();
+  mat->incref();
+  TACSPc *pc = nullptr;
+  if (direct)
+    pc = new TACSSchurPc(static_cast<TACSSchurMat *>(mat), 1000, 10.0, 1);
+  else
+    pc = new TACSAdditiveSchwarz(mat, 0, 10.0);
+  pc->incref();
+  GMRES *gmres = new GMRES(mat, pc, 300, 10, 0);
+  gmres->incref();
+  gmres->setTolerances(1e-12, 1e-30);
+
+  assembler->zeroVariables();
+  assembler->assembleJacobian(1.0, 0.0, 0.0, res, mat);
+  pc->factor();
+  const int flag = gmres->solve(res, ans);
   ans->scale(-1.0);
-  assembler.setVariables(ans);
+  assembler->setVariables(ans);
 
-  TACSCompliance comp(&assembler);
-  TACSKSFailure ks(&assembler, 100.0);
-  TACSFunction *funcs[2] = {&comp, &ks};
-  double fvals[2];
-  assembler.evalFunctions(2, funcs, fvals);
+  TACSFunction *funcs[2] = {new TACSCompliance(assembler),
+                            new TACSKSFailure(assembler, 100.0)};
+  for (TACSFunction *f : funcs) f->incref();
+  TacsScalar fvals[2];
+  assembler->evalFunctions(2, funcs, fvals);
 
-  std::vector<double> grads[2], gradX[2];
+  std::vector<TacsScalar> grads[2], gradX[2];
   for (int k = 0; k < 2; k++) {
-    TACSBVec *dfdu = assembler.createVec(), *psi = assembler.createVec();
-    TACSBVec *dfdx = assembler.createDesignVec();
-    TACSBVec *dfdX = assembler.createNodeVec();
-    assembler.addSVSens(1.0, 0.0, 0.0, 1, &funcs[k], &dfdu);
-    assembler.applyBCs(dfdu);
-    solve(dfdu, psi);
-    assembler.addDVSens(1.0, 1, &funcs[k], &dfdx);
-    assembler.addAdjointResProducts(-1.0, 1, &psi, &dfdx);
-    assembler.addXptSens(1.0, 1, &funcs[k], &dfdX);
-    assembler.addAdjointResXptSensProducts(-1.0, 1, &psi, &dfdX);
-    grads[k].resize(dfdx->getSize());
-    dfdx->getValues(grads[k].data());
-    gradX[k].resize(dfdX->getSize());
-    dfdX->getValues(gradX[k].data());
-    delete dfdu;
-    delete psi;
-    delete dfdx;
-    delete dfdX;
+    TACSBVec *dfdu = assembler->createVec(), *psi = assembler->createVec();
+    TACSBVec *dfdx = assembler->createDesignVec();
+    TACSBVec *dfdX = assembler->createNodeVec();
+    for (TACSBVec *v : {dfdu, psi, dfdx, dfdX}) v->incref();
+    assembler->addSVSens(1.0, 0.0, 0.0, 1, &funcs[k], &dfdu);
+    assembler->applyBCs(dfdu);
+    gmres->solve(dfdu, psi);
+    assembler->addDVSens(1.0, 1, &funcs[k], &dfdx);
+    assembler->addAdjointResProducts(-1.0, 1, &psi, &dfdx);
+    assembler->addXptSens(1.0, 1, &funcs[k], &dfdX);
+    assembler->addAdjointResXptSensProducts(-1.0, 1, &psi, &dfdX);
+    int size;
+    dfdx->getSize(&size);
+    grads[k].resize(size);
+    dfdx->copyToHost(grads[k].data());
+    dfdX->getSize(&size);
+    gradX[k].resize(size);
+    dfdX->copyToHost(gradX[k].data());
+    for (TACSBVec *v : {dfdu, psi, dfdx, dfdX}) v->decref();
   }
   std::printf("{\"flag\": %d, \"funcs\": [%.17g, %.17g]", flag, fvals[0],
               fvals[1]);
@@ -124,10 +152,13 @@ int main(int argc, char **argv) {
     std::printf("]");
   }
   std::printf("}\n");
-  delete schur;
-  delete X;
-  delete res;
-  delete ans;
-  delete mat;
+  for (TACSFunction *f : funcs) f->decref();
+  gmres->decref();
+  pc->decref();
+  mat->decref();
+  ans->decref();
+  res->decref();
+  X->decref();
+  assembler->decref();
   return 0;
 }

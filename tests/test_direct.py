@@ -7,7 +7,10 @@ and the kernels are also checked on the CPU in test_direct_symbolic.py).
   times cond(K);
 * a thin simply supported plate, where ILU(0)-GMRES stalls: the true
   residual at rounding level (1e-13 of |K| |u|) and agreement with a sparse
-  LU on the host (1e-6);
+  LU on the host within 10x the rounding spread of that exact solve (the
+  distance between its solutions for two elimination orders; cond(K) is
+  about 1e12 on these plates, so two exact FP64 solvers differ by ~1e-5 in
+  the displacements and ~1e-9 in the compliance);
 * both orders (node coordinates and level structures) and refactoring
   after new matrix values;
 * the reference harness's adjoint gradients with both solves direct.
@@ -27,6 +30,24 @@ def gpu():
         pytest.fail("CUDA device required for -m gpu tests")
     from tacs_gb300 import problem
     return problem
+
+
+def _host_matrix(mat, ndof):
+    from scipy import sparse
+    bs = mat.bsize
+    return sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
+                              mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
+                             shape=(ndof, ndof)).tocsc()
+
+
+def _exact_and_spread(K, b):
+    """Sparse LU solution on the host and its rounding spread: the relative
+    distance between the solutions of two elimination orders, for the
+    displacements (max norm) and for the compliance b^T x."""
+    from scipy.sparse.linalg import splu
+    x1 = splu(K, permc_spec="COLAMD").solve(b)
+    x2 = splu(K, permc_spec="MMD_AT_PLUS_A").solve(b)
+    return x1, rel(x2, x1), abs(b @ x2 - b @ x1) / abs(b @ x1)
 
 
 def _rhs(M, prob, mat):
@@ -54,8 +75,6 @@ def test_direct_static_solve_matches_reference(gpu, name, coords):
 
 
 def test_direct_thin_plate_where_ilu_stalls(gpu):
-    from scipy import sparse
-    from scipy.sparse.linalg import spsolve
     from tacs_gb300 import meshes
     n = 48
     prob = meshes.plate(n, n, 2.0, 2.0, t=0.002)
@@ -69,14 +88,14 @@ def test_direct_thin_plate_where_ilu_stalls(gpu):
     d = gpu.Direct(mat)
     d.factor()
     u = d.solve(b).cpu().numpy()
-    bs = mat.bsize
-    K = sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
-                           mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
-                          shape=(M.ndof, M.ndof)).tocsr()
+    K = _host_matrix(mat, M.ndof)
     bh = b.cpu().numpy()
     Kinf = abs(K).sum(axis=1).max()
     assert np.abs(K @ u - bh).max() < 1e-13 * Kinf * np.abs(u).max()
-    assert rel(u, spsolve(K.tocsc(), bh)) < 1e-6
+    x_ref, spread, spread_c = _exact_and_spread(K, bh)
+    assert rel(u, x_ref) < max(1e-8, 10.0 * spread)
+    assert abs(bh @ u - bh @ x_ref) / abs(bh @ x_ref) < max(1e-12,
+                                                            10.0 * spread_c)
 
 
 def test_direct_refactor_after_new_values(gpu):
@@ -172,8 +191,11 @@ def test_mixed_direct_adjoint_gradients(gpu, name):
 def test_direct_as_gmres_preconditioner(gpu):
     """The complete factorisation as a GMRES preconditioner (TG_PC_DIRECT):
     one or two iterations in FP64; in FP32 inside FP64 flexible GMRES with
-    refinement (GMRES-IR), the FP64 solution on a thin simply supported
-    plate to the true-residual tolerance."""
+    refinement (GMRES-IR) on a thin simply supported plate, where the
+    requested true residual (1e-12 |r0|) lies below what FP64 attains
+    (cond(K) ~ 1e12): converged at the FP64 accuracy floor, the true
+    residual at rounding level, and the FP64 solution within 10x the
+    rounding spread of an exact solve."""
     from tacs_gb300 import _lib, meshes
     n = 32
     prob = meshes.plate(n, n, 2.0, 2.0, t=0.002)
@@ -196,7 +218,15 @@ def test_direct_as_gmres_preconditioner(gpu):
     ksm32.set_tolerances(1e-12)
     x32, flag = ksm32.solve(b)
     assert flag == 1
-    assert rel(x32.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+    K = _host_matrix(mat, M.ndof)
+    bh, xh = b.cpu().numpy(), x32.cpu().numpy()
+    Kinf = abs(K).sum(axis=1).max()
+    assert np.abs(K @ xh - bh).max() < 1e-13 * Kinf * np.abs(xh).max()
+    _, spread, spread_c = _exact_and_spread(K, bh)
+    x64h = x64.cpu().numpy()
+    assert rel(xh, x64h) < max(1e-8, 10.0 * spread)
+    assert abs(bh @ xh - bh @ x64h) / abs(bh @ x64h) < max(1e-12,
+                                                            10.0 * spread_c)
 
 
 @pytest.mark.parametrize("thin", [False, True], ids=["t10mm", "t2mm"])
@@ -204,8 +234,9 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
     """FP32 factorisation + FP64 refinement stops when the normwise
     backward error reaches eps sqrt(N); where it cannot (the FP32 Cholesky
     breaks down or refinement stagnates, cond(K) near 2^24) the solve falls
-    back to an FP64 factorisation.  Either way the result is the FP64
-    direct solution (1e-8) with the FP64 backward error (1e-13)."""
+    back to an FP64 factorisation.  Either way the result has the FP64
+    backward error (1e-13) and is the FP64 direct solution to within 10x
+    the rounding spread of an exact solve (1e-8 where that is smaller)."""
     from tacs_gb300 import _lib, meshes
     n = 48
     prob = meshes.plate(n, n, 2.0, 2.0, t=0.002 if thin else 0.01)
@@ -228,12 +259,12 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
     if not thin:
         assert not st["fell_back_to_fp64"]
         assert 1 <= st["last_refinement_steps"] <= 10
-    assert rel(x.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+    K = _host_matrix(mat, M.ndof)
+    bh, xh, x64h = b.cpu().numpy(), x.cpu().numpy(), x64.cpu().numpy()
+    _, spread, spread_c = _exact_and_spread(K, bh)
+    assert rel(xh, x64h) < max(1e-8, 10.0 * spread)
+    assert abs(bh @ xh - bh @ x64h) / abs(bh @ x64h) < max(1e-12,
+                                                            10.0 * spread_c)
     r = (mat.mult(x) - b).abs().max().item()
-    from scipy import sparse
-    bs = mat.bsize
-    K = sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
-                           mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
-                          shape=(M.ndof, M.ndof)).tocsr()
     Kinf = abs(K).sum(axis=1).max()
     assert r < 1e-13 * (Kinf * x.abs().max().item() + b.abs().max().item())
