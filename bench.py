@@ -244,6 +244,65 @@ def hex_section(torch, steps=5):
     return out
 
 
+def fixed_geometry_section(torch, p, steps=20, label="", bs=6):
+    """Fixed-geometry assembly (tg_assembler_set_fixed_geometry) of the same
+    workload: the residual and Jacobian from per-geometry coefficient
+    matrices, each BCSR block summed from its contributions and written
+    once.  Times the one-off build (classes, coefficient table, loads) and
+    the steady-state assembly (CUDA events, inputs larger than L2), and
+    checks the result against the element kernels on the same state."""
+    from tacs_gb300 import problem
+    M = problem.GpuModel(p)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    u = 1e-4 * torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                           generator=g)
+    mat0, res0 = M.new_mat(), M.vec()
+    M.assemble_jacobian(u, mat0, res0)  # element kernels
+    M.set_fixed_geometry(True)
+    mat, res = M.new_mat(), M.vec()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    M.assemble_jacobian(u, mat, res)  # builds the cache
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    dv = float((mat.vals - mat0.vals).abs().max() / mat0.vals.abs().max())
+    dr = float((res - res0).abs().max() / res0.abs().max())
+    del mat0, res0
+    for _ in range(3):
+        M.assemble_jacobian(u, mat, res)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        M.assemble_jacobian(u, mat, res)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    nn, ne = p["nnodes"], p["nelem"]
+    npe = 4 if bs == 6 else 8
+    algo = (nn * (3 + bs) * 8 + ne * (4 * npe + 8) + nn * bs * 8
+            + mat.nnz * bs * bs * 8)
+    peak, src = measured_peaks()
+    info = M.fixed_geometry_info()
+    ach = algo / (ms / 1e3) / 1e9
+    out = {"workload": label, "elements": int(ne), "bcsr_blocks": int(mat.nnz),
+           "build_s": build_s, "ms_per_step": ms,
+           "elements_per_s": ne / (ms / 1e3), "geometry_classes":
+           info["classes"], "table_bytes": info["table_bytes"],
+           "plan_bytes": info["plan_bytes"],
+           "rel_diff_vs_element_kernels": {"K": dv, "R": dr},
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": peak,
+                        "unit": "GB/s", "frac": ach / peak,
+                        "peak_source": src, "kernel": "geo_assembly_kernel",
+                        "algorithmic_bytes": int(algo)},
+           "gpu_launches_per_step": 1}
+    del M, mat, res, u
+    torch.cuda.empty_cache()
+    return out
+
+
 def cylinder_section(torch, nc=384, nz=256):
     """Cylinder (384 x 256 MITC4, 592k dof): static solve and compliance
     adjoint gradient, all-FP64 against mixed precision (FP32 factor and
@@ -548,6 +607,8 @@ def main():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--adj-size", type=int, default=64)
     ap.add_argument("--no-hex", action="store_true")
+    ap.add_argument("--no-fixed", action="store_true",
+                    help="skip the fixed-geometry assembly section")
     ap.add_argument("--no-cylinder", action="store_true")
     ap.add_argument("--c2-adjoint", action="store_true",
                     help="the 512 x 512 plate's autograd gradient with "
@@ -697,6 +758,17 @@ def main():
             line["adjoint"], padj = res
         else:
             line["adjoint"] = res
+    if rank == 0 and not args.no_fixed:
+        line["fixed_geometry"] = guarded(lambda: fixed_geometry_section(
+            torch, p, args.steps, f"MITC4 plate {args.size}x{args.size}, "
+            "assembleRes+assembleJacobian with the fixed-geometry cache"))
+        if not args.no_hex:
+            from tacs_gb300 import meshes
+            line["fixed_geometry_hex"] = guarded(
+                lambda: fixed_geometry_section(
+                    torch, meshes.hex_c3(), 5, "hex8 SIMP block 128x128x64, "
+                    "assembleRes+assembleJacobian with the fixed-geometry "
+                    "cache", bs=3))
     if rank == 0 and not args.no_hex:
         line["hex_c3"] = guarded(lambda: hex_section(torch))
     if rank == 0 and args.c2_adjoint:

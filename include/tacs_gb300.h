@@ -121,6 +121,24 @@ int tg_assembler_set_pressure(tg_assembler *a, int n, const int *elems_host,
 int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems_host,
                               const int *faces_host, const double *vals_host);
 
+/* No reference counterpart.  Fixed-geometry assembly: with enable != 0,
+   tg_assemble_res and tg_assemble_jacobian produce the same residual and
+   matrix (to rounding) from coefficient matrices formed once per distinct
+   element geometry: the linear MITC4 element over TACSIsoShellConstitutive
+   (tOffset 0) has K = t K1 + t^3 K3, the hex8 element over
+   TACSSolidConstitutive K = t K1, and R = K u + lambda R(u = 0); elements
+   whose node coordinates relative to their first node are bitwise equal
+   share K1 and K3 (one class for a uniform structured mesh).  Each matrix
+   block is then summed from its contributions and written once.  The
+   classes, coefficients and R(u = 0) are built at the first assembly after
+   enabling and after every tg_assembler_set_nodes (synchronous, allocates);
+   t (tg_assembler_set_design_vars) and u may change freely. */
+int tg_assembler_set_fixed_geometry(tg_assembler *a, int enable);
+/* Geometry classes, coefficient-table bytes (0 before the first build)
+   and the bytes of the per-block contribution lists. */
+int tg_assembler_get_fixed_geometry(tg_assembler *a, int *nclasses,
+                                    double *table_bytes, double *plan_bytes);
+
 /* TACSAssembler::assembleRes(res, lambda, applyBCs)
    (src/TACSAssembler.cpp:4133).  vars: state (device). */
 int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,

@@ -44,6 +44,8 @@ SIGNATURES = [
     ("tg_assembler_set_design_vars", _I, [_P, _P, _P]),
     ("tg_assembler_set_pressure", _I, [_P, _I, _P, _P]),
     ("tg_assembler_set_traction", _I, [_P, _I, _P, _P, _P]),
+    ("tg_assembler_set_fixed_geometry", _I, [_P, _I]),
+    ("tg_assembler_get_fixed_geometry", _I, [_P, _IP, _DP, _DP]),
     ("tg_assemble_res", _I, [_P, _P, _D, _I, _P, _P]),
     ("tg_assemble_jacobian", _I, [_P, _D, _D, _D, _P, _P, _P, _I, _D, _I,
                                   _P]),

@@ -17,7 +17,8 @@ LIB = os.path.join(HERE, "libtacs_gb300.so")
 OBJ = os.path.join(HERE, "_build")
 SOURCES = ["tg_runtime.cu", "tg_krylov.cu", "shell_kernels.cu",
            "hex_kernels.cu", "bcsr_kernels.cu", "krylov_kernels.cu",
-           "noalloc.cu", "shell_team.cu", "tg_direct.cu", "direct_kernels.cu"]
+           "noalloc.cu", "shell_team.cu", "tg_direct.cu", "direct_kernels.cu",
+           "geo_cache.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr"]

@@ -1030,19 +1030,23 @@ template <int BS, int NR, typename T>
 static void cluster_launch(const IluPlan &p, const T *F, const T *x, T *y,
                            T *tmp, size_t ld, cudaStream_t s) {
   auto kern = ilu_cluster_kernel<BS, NR, (BS == 6 ? 4 : 8), T>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                         1);
-    attr = true;
-  }
+  // kernel attributes are per device: set on each device, recorded only
+  // when the call succeeded
+  constexpr int kMaxDevices = 64;
+  static bool attr[kMaxDevices] = {};
+  static size_t smem_set[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    dev = 0;
+  if (!attr[dev] &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                           1) == cudaSuccess)
+    attr[dev] = true;
   const size_t smem = sizeof(int) * (size_t)p.cluster.max_lp;
-  static size_t smem_set = 0;
-  if (smem > smem_set && smem > 48 * 1024) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    smem_set = smem;
-  }
+  if (smem > smem_set[dev] && smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) == cudaSuccess)
+    smem_set[dev] = smem;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p.cluster.ngroups * p.cluster.cs);
   cfg.blockDim = dim3(256);

@@ -87,22 +87,28 @@ void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
       n, bs, perm, xpos, x);
 }
 
-void direct_set_smem(int max_front) {
-  // the attribute only grows: every factorisation of the process keeps
-  // its solve workspace
-  static int set = 48 * 1024;
+cudaError_t direct_set_smem(int max_front) {
+  // per device (the attribute belongs to the kernel on each device); the
+  // limit only grows, and is recorded only once every call succeeded
+  constexpr int kMaxDevices = 64;
+  static int set[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   const int bytes = (int)sizeof(double) * max_front;
-  if (bytes > set) {
-    set = bytes;
-    cudaFuncSetAttribute(direct_forward_kernel<double>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(direct_backward_kernel<double>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(direct_forward_kernel<float>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(direct_backward_kernel<float>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (bytes <= 48 * 1024 || bytes <= set[dev]) return cudaSuccess;
+  const void *ks[4] = {(const void *)direct_forward_kernel<double>,
+                       (const void *)direct_backward_kernel<double>,
+                       (const void *)direct_forward_kernel<float>,
+                       (const void *)direct_backward_kernel<float>};
+  for (const void *k : ks) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
+    if (e != cudaSuccess) return e;
   }
+  set[dev] = bytes;
+  return cudaSuccess;
 }
 
 #define TG_DIRECT_INSTANTIATE(T)                                            \

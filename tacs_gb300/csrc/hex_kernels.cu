@@ -532,6 +532,49 @@ __global__ void __launch_bounds__(128)
   for (int i = 0; i < 24; i++) dfdX[3 * nodes[i / 3] + i % 3] += dX[i];
 }
 
+// Fixed-geometry class table (geo_plan.h): TACSSolidConstitutive's stress
+// is t C e, so K(t) = t K1 with K1 = sum_q detXd_q B_q^T C B_q, formed in
+// the closed isotropic form of the team kernel at t = 1.  One warp per
+// representative element writes the 64 node blocks (a, b) of 3 x 3; pairs
+// a <= b are formed and mirrored (K1 exactly symmetric).
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    hex_geo_build_kernel(ElemParams ep, MeshView m,
+                         const int *__restrict__ reps, int nreps,
+                         double *__restrict__ table) {
+  __shared__ HexSmem smem[WARPS];
+  HexSmem &S = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const HexC c = hex_c(ep);
+  for (int cl = gw; cl < nreps; cl += nw) {
+    hex_load(S, m, reps[cl], nullptr, nullptr, lane);
+    hex_geometry(S, lane);
+    double *out = table + (size_t)cl * 576;
+    for (int p = lane; p < 36; p += 32) {
+      const int a = c_pair[p][0], b = c_pair[p][1];
+      double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int q = 0; q < 8; q++) {
+        const double wq = S.det[q];
+        const double ga[3] = {wq * S.Nx[q][3 * a], wq * S.Nx[q][3 * a + 1],
+                              wq * S.Nx[q][3 * a + 2]};
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) M[3 * i + j] += ga[i] * S.Nx[q][3 * b + j];
+      }
+      const double tr = M[0] + M[4] + M[8];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          const double k = c.c1 * M[3 * i + j] + c.G * M[3 * j + i] +
+                           (i == j ? c.G * tr : 0.0);
+          out[(8 * a + b) * 9 + 3 * i + j] = k;
+          out[(8 * b + a) * 9 + 3 * j + i] = k;
+        }
+    }
+    __syncwarp();
+  }
+}
+
 constexpr int kWarps = 8;
 
 int grid_for(int count) {
@@ -567,6 +610,13 @@ void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
   if (grid > sms * 16) grid = sms * 16;
   hex_team_assembly_kernel<<<grid, 64, 0, s>>>(ep, m, cr, vars, lambda, res,
                                                mat);
+}
+void launch_hex_geo_build(const ElemParams &ep, const MeshView &m,
+                          const int *reps, int nreps, double *table,
+                          cudaStream_t s) {
+  if (nreps <= 0) return;
+  hex_geo_build_kernel<kWarps><<<grid_for(nreps), kWarps * 32, 0, s>>>(
+      ep, m, reps, nreps, table);
 }
 void launch_hex_points(const ElemParams &ep, const MeshView &m,
                        const double *vars, double *elem_fail,

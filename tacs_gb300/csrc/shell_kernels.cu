@@ -428,6 +428,67 @@ __global__ void __launch_bounds__(128)
   for (int i = 0; i < 12; i++) dfdX[3 * nodes[i / 3] + i % 3] += dX[i];
 }
 
+// Fixed-geometry class table (geo_plan.h): for the linear MITC4 element
+// with TACSIsoShellConstitutive (tOffset 0) the tangent is
+// C(t) = t C1 + t^3 C3 (A, As and the drilling stiffness grow with t, D with
+// t^3; TACSIsoShellConstitutive.cpp:181-217), so
+//   K(t) = sum_q detXd_q B_q^T C(t) B_q = t K1 + t^3 K3
+// with B_q the strain operator of the residual (shell_build_B).  One warp
+// per representative element writes K1 and K3 as the 16 node blocks
+// (a, b) of 6 x 6; the upper triangle is formed and mirrored, so every
+// element matrix is exactly symmetric like the team kernel's.
+struct ShellGeoSmem {
+  ShellSmem s;
+  double CB[4][9][24];  // detXd_q C(t = 1) B_q
+};
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    shell_geo_build_kernel(ElemParams ep, MeshView m,
+                           const int *__restrict__ reps, int nreps,
+                           double *__restrict__ table) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ShellGeoSmem &G = reinterpret_cast<ShellGeoSmem *>(smem_raw)[threadIdx.x >> 5];
+  ShellSmem &S = G.s;
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int nw = gridDim.x * WARPS;
+  const ShellStiff c1 = shell_stiff(ep, 1.0);
+  for (int c = gw; c < nreps; c += nw) {
+    load_element(S, m, reps[c], nullptr, nullptr, lane);
+    shell_build_B(S, ep, lane);
+    for (int idx = lane; idx < 96; idx += 32) {
+      const int q = idx / 24, j = idx - 24 * q;
+      double ev[9];
+      for (int r = 0; r < 9; r++) ev[r] = S.B[q][r][j];
+      for (int r = 0; r < 9; r++)
+        G.CB[q][r][j] = S.det[q] * shell_stress_row(c1, ev, r);
+    }
+    __syncwarp();
+    double *out = table + (size_t)c * 1152;
+    for (int idx = lane; idx < 300; idx += 32) {
+      int j = 0, base = 0;
+      while (base + j + 1 <= idx) {
+        base += j + 1;
+        j++;
+      }
+      const int i = idx - base;  // i <= j
+      double k1 = 0.0, k3 = 0.0;
+      for (int q = 0; q < 4; q++) {
+        for (int r = 0; r < 3; r++) k1 += S.B[q][r][i] * G.CB[q][r][j];
+        for (int r = 6; r < 9; r++) k1 += S.B[q][r][i] * G.CB[q][r][j];
+        for (int r = 3; r < 6; r++) k3 += S.B[q][r][i] * G.CB[q][r][j];
+      }
+      const int a = i / 6, ri = i - 6 * a, b = j / 6, cj = j - 6 * b;
+      out[(4 * a + b) * 36 + 6 * ri + cj] = k1;
+      out[576 + (4 * a + b) * 36 + 6 * ri + cj] = k3;
+      out[(4 * b + a) * 36 + 6 * cj + ri] = k1;
+      out[576 + (4 * b + a) * 36 + 6 * cj + ri] = k3;
+    }
+    __syncwarp();
+  }
+}
+
 constexpr int kWarps = 4;
 
 int grid_for(int count, int ctas_per_sm) {
@@ -444,14 +505,19 @@ int grid_for(int count, int ctas_per_sm) {
   return need < cap ? need : cap;
 }
 
+// The dynamic shared-memory limit is a per-device attribute of a kernel:
+// set once on each device, kept only once the call succeeded.
+constexpr int kMaxDevices = 64;
 template <typename K>
-void prep(K kernel) {
-  static bool done = false;
-  if (!done) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(ShellSmem) * kWarps));
-    done = true;
-  }
+void prep(K kernel, size_t bytes = sizeof(ShellSmem) * kWarps) {
+  static bool done[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return;
+  if (!done[dev] &&
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)bytes) == cudaSuccess)
+    done[dev] = true;
 }
 
 }  // namespace
@@ -487,6 +553,16 @@ void launch_shell_dv(const ElemParams &ep, const MeshView &m,
   prep(k);
   k<<<grid_for(m.nelem, 2), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
       ep, m, vars, func, ks, coef, psi, scale, out);
+}
+
+void launch_shell_geo_build(const ElemParams &ep, const MeshView &m,
+                            const int *reps, int nreps, double *table,
+                            cudaStream_t s) {
+  if (nreps <= 0) return;
+  auto k = shell_geo_build_kernel<kWarps>;
+  const size_t bytes = sizeof(ShellGeoSmem) * kWarps;
+  prep(k, bytes);
+  k<<<grid_for(nreps, 2), kWarps * 32, bytes, s>>>(ep, m, reps, nreps, table);
 }
 
 void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,

@@ -489,14 +489,18 @@ void launch_shell_team_assembly(const ElemParams &ep, const MeshView &m,
                                 double lambda, double *res, double *mat,
                                 int *err_flag, cudaStream_t s) {
   if (cr.count <= 0) return;
-  static bool init = false;
+  // the shared-memory limit is a per-device kernel attribute: set on each
+  // device once, recorded only when the call succeeded
+  constexpr int kMaxDevices = 64;
+  static bool init[kMaxDevices] = {};
   const size_t smem = sizeof(TeamSmem) * kTeamsPerCta;
-  if (!init) {
-    cudaFuncSetAttribute(shell_team_assembly_kernel,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    init = true;
-  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices &&
+      !init[dev] &&
+      cudaFuncSetAttribute(shell_team_assembly_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) == cudaSuccess)
+    init[dev] = true;
   int need = (cr.count + kTeamsPerCta - 1) / kTeamsPerCta;
   int cap = sm_count() * 3;
   int grid = need < cap ? need : cap;

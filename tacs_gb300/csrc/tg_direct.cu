@@ -244,7 +244,11 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     tg_direct_decref(d);
     return rc;
   }
-  tg::direct_set_smem(d->max_front);
+  const cudaError_t se = tg::direct_set_smem(d->max_front);
+  if (se != cudaSuccess) {
+    tg_direct_decref(d);
+    return cuda_check(se, "tg_direct_create: solve workspace attribute");
+  }
   *out = d;
   return 0;
 }

@@ -54,6 +54,44 @@ void launch_hex_assembly(const ElemParams &ep, const MeshView &m,
                          double *res, double *mat, int transpose,
                          cudaStream_t s);
 
+// Fixed-geometry assembly (geo_cache.cu; the plan in geo_plan.h).  The
+// class table holds, per geometry class, ncoef coefficient matrices
+// (shell: K1 at t = 1 of membrane, shear and drilling, K3 at t = 1 of
+// bending; hex: K1) as npe x npe node blocks of bs x bs, row-major:
+// table[((cls * ncoef + coef) * npe * npe + npe * a + b) * bs * bs + ...].
+struct GeoView {
+  int nrows, nwarps;
+  const int *rowp, *cols;   // BCSR pattern (rows = nodes)
+  const int *cptr;          // nnz + 1: contribution ranges per slot
+  const int *contrib;       // (e << 6) | (npe a + b), element order
+  const int *cls;           // geometry class per element
+  const int *node_bc;       // constraint mask per node
+  const int *warp_kmax;     // longest row of each 32-row group
+  const double *thick;      // element scale t
+  const double *table;      // class table
+  const double *f0;         // R(u = 0, lambda = 1) without constraints
+  // entries (r * bs + c) non-zero in some class: bit set (coefficient 1, 3)
+  unsigned long long mask1, mask3;
+};
+// Builds the class table of the representative elements (one warp each).
+void launch_shell_geo_build(const ElemParams &ep, const MeshView &m,
+                            const int *reps, int nreps, double *table,
+                            cudaStream_t s);
+void launch_hex_geo_build(const ElemParams &ep, const MeshView &m,
+                          const int *reps, int nreps, double *table,
+                          cudaStream_t s);
+// OR of the non-zero entry bits of every table block into masks[ncoef].
+void launch_geo_masks(int bs, int ncoef, int nblocks_per_coef_cls, int ncls,
+                      const double *table, unsigned long long *masks,
+                      cudaStream_t s);
+// K = sum of t K1 (+ t^3 K3) over each block's contributions, row
+// constraints applied when apply_bcs; R = K u + lambda f0 with the
+// constrained entries set to u (or 0 without vars).  vals and res may each
+// be nullptr.
+void launch_geo_assembly(int bs, const GeoView &g, const double *vars,
+                         double lambda, int apply_bcs, double *res,
+                         double *vals, cudaStream_t s);
+
 // Point quantities.  Pass 1 writes per-element, per-point failure values
 // and detXd-weighted strain energies; the KS reduction and the sensitivity
 // passes read them back.
@@ -309,7 +347,7 @@ void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
 template <class T>
 void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
                              T *x, cudaStream_t s);
-void direct_set_smem(int max_front);
+cudaError_t direct_set_smem(int max_front);
 
 // error reporting
 void set_error(const std::string &msg);

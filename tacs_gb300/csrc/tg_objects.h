@@ -86,6 +86,18 @@ struct tg_assembler {
   KsStats *d_seg_ks = nullptr;
   double *d_seg_comp = nullptr;
   bool seg_ks_valid = false;
+  // fixed-geometry assembly (geo_plan.h, geo_cache.cu): the plan depends on
+  // the connectivity and constraints, the class table and f0 on the node
+  // coordinates (set_nodes invalidates them)
+  bool geo_enabled = false;
+  bool geo_plan_ready = false, geo_table_valid = false;
+  int geo_ncls = 0, geo_nwarps = 0;
+  unsigned long long geo_mask[2] = {0, 0};
+  size_t geo_table_doubles = 0, geo_plan_bytes = 0;
+  int *d_geo_cptr = nullptr, *d_geo_contrib = nullptr, *d_geo_cls = nullptr;
+  int *d_geo_node_bc = nullptr, *d_geo_kmax = nullptr, *d_geo_reps = nullptr;
+  double *d_geo_table = nullptr, *d_geo_f0 = nullptr;
+  unsigned long long *d_geo_masks = nullptr;
 
   int nq() const { return ep.elem_type == TG_ELEM_MITC4 ? 4 : 8; }
 
@@ -132,6 +144,9 @@ struct tg_assembler {
     dfree(d_elem_val); dfree(d_partials); dfree(d_scalars);
     dfree(d_elem_seg); dfree(d_seg_elem_ptr); dfree(d_seg_ks);
     dfree(d_seg_comp);
+    dfree(d_geo_cptr); dfree(d_geo_contrib); dfree(d_geo_cls);
+    dfree(d_geo_node_bc); dfree(d_geo_kmax); dfree(d_geo_reps);
+    dfree(d_geo_table); dfree(d_geo_f0); dfree(d_geo_masks);
   }
 };
 

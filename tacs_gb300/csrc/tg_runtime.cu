@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "mesh_graph.h"
+#include "geo_plan.h"
 #include "tg_objects.h"
 
 namespace tg {
@@ -260,6 +261,123 @@ int tg_assembler_set_nodes(tg_assembler *a, const double *xpts, void *s) {
   if (!xpts) return fail(TG_ERR_ARG, "NULL node vector");
   TG_CUDA(cudaMemcpyAsync(a->d_xpts, xpts, sizeof(double) * 3 * a->nnodes,
                           cudaMemcpyDeviceToDevice, S(s)));
+  a->geo_table_valid = false;  // new geometry: classes, table and loads
+  return 0;
+}
+
+// ------------------------------------------------ fixed-geometry assembly
+// The plan (contribution lists, row schedule, node constraint masks) once
+// per assembler; the geometry classes, their coefficient table and the
+// loads f0 = R(u = 0, lambda = 1) once per node set.
+static int geo_prepare(tg_assembler *a, cudaStream_t s) {
+  const bool shell = a->ep.elem_type == TG_ELEM_MITC4;
+  const int bs = a->vpn, npe = a->npe, ncoef = shell ? 2 : 1;
+  int rc = 0;
+  if (!a->geo_plan_ready) {
+    std::vector<int> cptr, contrib, kmax, node_bc;
+    if (geo::contributions(a->nelem, npe, a->conn_h.data(), a->rowp_h,
+                           a->cols_h, cptr, contrib))
+      return fail(TG_ERR_ARG, "fixed geometry: more than 2^25 elements");
+    geo::warp_row_lengths(a->rowp_h, kmax);
+    geo::node_bc_masks(a->nnodes, a->bc_nodes_h, a->bc_masks_h, node_bc);
+    if ((rc = upload(&a->d_geo_cptr, cptr))) return rc;
+    if ((rc = upload(&a->d_geo_contrib, contrib))) return rc;
+    if ((rc = upload(&a->d_geo_kmax, kmax))) return rc;
+    if ((rc = upload(&a->d_geo_node_bc, node_bc))) return rc;
+    if ((rc = dalloc(&a->d_geo_f0, (size_t)bs * a->nnodes))) return rc;
+    if ((rc = dalloc(&a->d_geo_masks, 2))) return rc;
+    a->geo_nwarps = (int)kmax.size();
+    a->geo_plan_bytes = sizeof(int) * (cptr.size() + contrib.size() +
+                                       kmax.size() + node_bc.size());
+    a->geo_plan_ready = true;
+  }
+  if (!a->geo_table_valid) {
+    std::vector<double> x((size_t)3 * a->nnodes);
+    TG_CUDA(cudaMemcpyAsync(x.data(), a->d_xpts, x.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> cls, reps;
+    const int ncls = geo::geometry_classes(a->nelem, npe, a->conn_h.data(),
+                                           x.data(), cls, reps);
+    dfree(a->d_geo_cls);
+    dfree(a->d_geo_reps);
+    if ((rc = upload(&a->d_geo_cls, cls))) return rc;
+    if ((rc = upload(&a->d_geo_reps, reps))) return rc;
+    const size_t per = (size_t)ncoef * npe * npe * bs * bs;
+    if ((size_t)ncls * per > a->geo_table_doubles) {
+      dfree(a->d_geo_table);
+      if ((rc = dalloc(&a->d_geo_table, (size_t)ncls * per))) return rc;
+      a->geo_table_doubles = (size_t)ncls * per;
+    }
+    MeshView m = a->view();
+    if (shell)
+      launch_shell_geo_build(a->ep, m, a->d_geo_reps, ncls, a->d_geo_table, s);
+    else
+      launch_hex_geo_build(a->ep, m, a->d_geo_reps, ncls, a->d_geo_table, s);
+    TG_CUDA(cudaMemsetAsync(a->d_geo_masks, 0, 2 * sizeof(unsigned long long),
+                            s));
+    launch_geo_masks(bs, ncoef, npe * npe, ncls, a->d_geo_table,
+                     a->d_geo_masks, s);
+    TG_CUDA(cudaMemcpyAsync(a->geo_mask, a->d_geo_masks,
+                            2 * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s));
+    // loads: the residual at u = 0 without constraints (t does not enter)
+    const size_t n = (size_t)bs * a->nnodes;
+    TG_CUDA(cudaMemsetAsync(a->d_geo_f0, 0, n * sizeof(double), s));
+    for (int c = 0; c < a->ncolors(); c++) {
+      if (shell)
+        launch_shell_team_assembly(a->ep, m, a->color(c), nullptr, 1.0,
+                                   a->d_geo_f0, nullptr, nullptr, s);
+      else
+        launch_hex_assembly(a->ep, m, a->color(c), nullptr, 1.0, a->d_geo_f0,
+                            nullptr, 0, s);
+    }
+    TG_CUDA(cudaStreamSynchronize(s));
+    TG_CUDA(cudaGetLastError());
+    a->geo_ncls = ncls;
+    a->geo_table_valid = true;
+  }
+  return 0;
+}
+
+static GeoView geo_view(const tg_assembler *a) {
+  GeoView g;
+  g.nrows = a->nnodes;
+  g.nwarps = a->geo_nwarps;
+  g.rowp = a->d_rowp;
+  g.cols = a->d_cols;
+  g.cptr = a->d_geo_cptr;
+  g.contrib = a->d_geo_contrib;
+  g.cls = a->d_geo_cls;
+  g.node_bc = a->d_geo_node_bc;
+  g.warp_kmax = a->d_geo_kmax;
+  g.thick = a->d_thick;
+  g.table = a->d_geo_table;
+  g.f0 = a->d_geo_f0;
+  g.mask1 = a->geo_mask[0];
+  g.mask3 = a->geo_mask[1];
+  return g;
+}
+
+int tg_assembler_set_fixed_geometry(tg_assembler *a, int enable) {
+  if (!a || !a->initialized)
+    return fail(TG_ERR_STATE, "tg_assembler_set_fixed_geometry before "
+                              "initialize");
+  a->geo_enabled = enable != 0;
+  return 0;
+}
+
+int tg_assembler_get_fixed_geometry(tg_assembler *a, int *nclasses,
+                                    double *table_bytes, double *plan_bytes) {
+  if (!a) return fail(TG_ERR_ARG, "NULL assembler");
+  if (nclasses) *nclasses = a->geo_table_valid ? a->geo_ncls : 0;
+  if (table_bytes)
+    *table_bytes = a->geo_table_valid
+                       ? (double)a->geo_ncls * (a->ep.elem_type == TG_ELEM_MITC4
+                                                    ? 2 * 16 * 36
+                                                    : 64 * 9) * 8.0
+                       : 0.0;
+  if (plan_bytes) *plan_bytes = (double)a->geo_plan_bytes;
   return 0;
 }
 
@@ -285,6 +403,13 @@ int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,
   if (rc) return rc;
   if (!res) return fail(TG_ERR_ARG, "tg_assemble_res: NULL residual");
   const size_t n = (size_t)a->vpn * a->nnodes;
+  if (a->geo_enabled) {
+    if ((rc = geo_prepare(a, S(s)))) return rc;
+    launch_geo_assembly(a->vpn, geo_view(a), vars, lambda, apply_bcs, res,
+                        nullptr, S(s));
+    TG_CUDA(cudaGetLastError());
+    return 0;
+  }
   TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
   MeshView m = a->view();
   for (int c = 0; c < a->ncolors(); c++) {
@@ -358,6 +483,14 @@ int tg_assemble_jacobian(tg_assembler *a, double alpha, double beta,
     return fail(TG_ERR_ARG,
                 "tg_assemble_jacobian: static elements need alpha=1, beta=gamma=0");
   const size_t n = (size_t)a->vpn * a->nnodes;
+  if (a->geo_enabled) {
+    // element matrices are symmetric: the transpose assembly is the same
+    if ((rc = geo_prepare(a, S(s)))) return rc;
+    launch_geo_assembly(a->vpn, geo_view(a), vars, lambda, apply_bcs, res,
+                        A->d_vals, S(s));
+    TG_CUDA(cudaGetLastError());
+    return 0;
+  }
   if (res) TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
   TG_CUDA(cudaMemsetAsync(A->d_vals, 0,
                           sizeof(double) * (size_t)A->nnz * A->bsize * A->bsize,

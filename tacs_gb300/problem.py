@@ -338,6 +338,22 @@ class GpuModel:
         check(_lib.lib().tg_assembler_set_nodes(self.handle, _p(xpts),
                                                 _stream()), "set_nodes")
 
+    def set_fixed_geometry(self, enable=True):
+        """Fixed-geometry assembly (tg_assembler_set_fixed_geometry): the
+        residual and Jacobian from per-geometry coefficient matrices, built
+        at the next assembly and after every set_nodes."""
+        check(_lib.lib().tg_assembler_set_fixed_geometry(self.handle,
+                                                         int(enable)),
+              "set_fixed_geometry")
+
+    def fixed_geometry_info(self):
+        n, tb, pb = C.c_int(0), C.c_double(0.0), C.c_double(0.0)
+        check(_lib.lib().tg_assembler_get_fixed_geometry(
+            self.handle, C.byref(n), C.byref(tb), C.byref(pb)),
+            "get_fixed_geometry")
+        return {"classes": n.value, "table_bytes": tb.value,
+                "plan_bytes": pb.value}
+
     def set_design_vars(self, dvs):
         check(_lib.lib().tg_assembler_set_design_vars(self.handle, _p(dvs),
                                                       _stream()), "set_dvs")
