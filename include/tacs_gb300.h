@@ -216,12 +216,16 @@ int tg_direct_solve_f32(tg_direct *d, const float *b, float *x,
 int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
                             int steps, void *stream);
 /* The same refinement with a stopping test (no reference counterpart; the
-   practice of LAPACK's mixed-precision dsgesv): steps until the normwise
-   backward error eta = ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
-   is at most tol, at most max_steps.  Returns TG_ERR_NOCONV (x holds the
-   last iterate) when eta stops halving for two steps or max_steps pass,
-   which happens when cond(A) approaches the inverse of FP32's unit
-   roundoff: factor the matrix in FP64 then.  steps and eta (may be NULL)
+   test of LAPACK's mixed-precision dsgesv, refined further): steps while
+   they halve the normwise backward error
+   eta = ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), at most
+   max_steps; converged when eta reached tol (the steps continue past it
+   until one no longer halves eta, since eta <= tol alone still admits a
+   residual far above an FP64 factorisation's where |A| |x| >> |b|).
+   Returns TG_ERR_NOCONV (x holds the last iterate) when eta stops halving
+   for two steps before reaching tol or max_steps pass, which happens when
+   cond(A) approaches the inverse of FP32's unit roundoff: factor the
+   matrix in FP64 then.  steps and eta (may be NULL)
    receive the steps taken and the final eta.  Synchronises the stream
    once per step.  b and x must be different buffers (both refinement
    calls; tg_direct_solve itself may solve in place). */

@@ -53,7 +53,7 @@ struct __align__(16) TeamSmem {
   double pres[4];
   double sd[9];   // sqrt of the LDL^T pivots of G
   double y[kNchan];
-  double res[24];
+  double prd[4];  // interpolated pressure x -detXd at the 4 points
   double t;
   double Z[kNchan][24];  // rows 0..8 start as Bty; 9..24 hold M/CM first
   TeamGeo g;
@@ -70,6 +70,53 @@ __device__ __forceinline__ void shape_at(int which, double *N, double *Na,
   else
     shape2(gauss2((which - 4) & 1), gauss2((which - 4) >> 1), N, Na, Nb);
 }
+// The same values read from the CTA's table (filled once per CTA: 8
+// evaluation points = 4 nodes + 4 Gauss points, then the 9 tying points),
+// so that no phase spends FP64 issue slots re-evaluating constants.
+struct ShapeTab {
+  double N[17][4], Na[17][4], Nb[17][4];
+};
+__device__ __forceinline__ void shape_tab(const ShapeTab &T, int which,
+                                          double *N, double *Na, double *Nb) {
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    N[k] = T.N[which][k];
+    Na[k] = T.Na[which][k];
+    Nb[k] = T.Nb[which][k];
+  }
+}
+
+// Row of tying strain t for node mm (TACSShellLinearModel::
+// computeTyingStrain, TACSShellElementModel.h:28-140): the displacement
+// part cx X,xi + cy X,eta + cn n0 and the director part
+// g sum_i X,(c)[i] dmap(fn_mm, i, b), in one form for the five tying
+// fields so that lanes with different fields run the same instructions.
+__device__ __forceinline__ void tying_row(int f, int mm, const double *N,
+                                          const double *Na, const double *Nb,
+                                          const double *Xxi, const double *n0,
+                                          const double *fn, double *z) {
+  double cx = 0.0, cy = 0.0, cn = 0.0, g = 0.0;
+  int c = 0;
+  if (f == 0) cx = Na[mm];
+  else if (f == 1) cy = Nb[mm];
+  else if (f == 2) {
+    cx = 0.5 * Nb[mm];
+    cy = 0.5 * Na[mm];
+  } else {
+    cn = f == 3 ? 0.5 * Nb[mm] : 0.5 * Na[mm];
+    g = 0.5 * N[mm];
+    c = f == 3 ? 1 : 0;
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+    z[6 * mm + a] = cx * Xxi[2 * a] + cy * Xxi[2 * a + 1] + cn * n0[a];
+  const double x0 = Xxi[c], x1 = Xxi[2 + c], x2 = Xxi[4 + c];
+  const double *fm = &fn[3 * mm];
+  // rows of dmap: [0, f2, -f1], [-f2, 0, f0], [f1, -f0, 0]
+  z[6 * mm + 3] = g * (x1 * -fm[2] + x2 * fm[1]);
+  z[6 * mm + 4] = g * (x0 * fm[2] + x2 * -fm[0]);
+  z[6 * mm + 5] = g * (x0 * -fm[1] + x1 * fm[0]);
+}
 
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
     shell_team_assembly_kernel(ElemParams ep, MeshView m, ColorRange cr,
@@ -78,6 +125,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
                                double *__restrict__ mat, int *err_flag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned char s_tile[36][2];
+  __shared__ ShapeTab s_shape;
   TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
   const int lane = threadIdx.x & 31;
   const int tl = lane & (kTeam - 1);
@@ -94,6 +142,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
     }
     s_tile[k][0] = (unsigned char)(k - base);
     s_tile[k][1] = (unsigned char)tj;
+  }
+  for (int k = threadIdx.x; k < 17; k += blockDim.x) {
+    if (k < 8)
+      shape_at(k, s_shape.N[k], s_shape.Na[k], s_shape.Nb[k]);
+    else
+      shape2(c_ty_pt[k - 8][0], c_ty_pt[k - 8][1], s_shape.N[k],
+             s_shape.Na[k], s_shape.Nb[k]);
   }
   __syncthreads();
 
@@ -137,7 +192,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
     // --------------------------------------------------- node normals
     double N[4], Na[4], Nb[4], Xxi[6];
     if (tl < 4) {
-      shape_at(tl, N, Na, Nb);
+      shape_tab(s_shape, tl, N, Na, Nb);
       grad3(Na, Nb, S.X, Xxi);
       double a[3] = {Xxi[0], Xxi[2], Xxi[4]}, b[3] = {Xxi[1], Xxi[3], Xxi[5]};
       double f[3];
@@ -153,7 +208,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
 
     // ------------- frames at the 4 nodes (lanes 0-3) and 4 points (4-7)
     {
-      shape_at(tl, N, Na, Nb);
+      shape_tab(s_shape, tl, N, Na, Nb);
       grad3(Na, Nb, S.X, Xxi);
       double nv[3];
       if (tl < 4) {
@@ -206,6 +261,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
         S.det[q] = det;
         S.n0[q][0] = nv[0]; S.n0[q][1] = nv[1]; S.n0[q][2] = nv[2];
         S.sdet[q] = sqrt(fabs(det));
+        // TACSShellPressure::addResidual (TACSShellPressure.h:56-90): the
+        // interpolated pressure times -detXd at this point
+        if (m.pres) {
+          const double pr = N[0] * S.pres[0] + N[1] * S.pres[1] +
+                            N[2] * S.pres[2] + N[3] * S.pres[3];
+          S.prd[q] = pr * -det;
+        }
         if (!(det > 0.0) && active && err_flag) atomicCAS(err_flag, 0, 1);
       }
     }
@@ -213,39 +275,20 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
 
     // ---------------------------------------- tying-strain rows (Bty)
     // (TACSShellLinearModel::computeTyingStrain, TACSShellElementModel.h:28)
-    for (int t = tl; t < 9; t += kTeam) {
+    // tying points 0..7 one per lane; point 8 with one node per lane
+    {
       double n0[3];
-      shape2(c_ty_pt[t][0], c_ty_pt[t][1], N, Na, Nb);
+      shape_tab(s_shape, 8 + tl, N, Na, Nb);
       grad3(Na, Nb, S.X, Xxi);
       interp3(N, S.fn, n0);
-      const int f = c_ty_field[t];
-      // row = al*X,xi + be*X,eta + ga*n0 coefficients per node
-      for (int mm = 0; mm < 4; mm++) {
-        double al, be, ga;
-        if (f == 0) { al = Na[mm]; be = 0.0; ga = 0.0; }
-        else if (f == 1) { al = 0.0; be = Nb[mm]; ga = 0.0; }
-        else if (f == 2) { al = 0.5 * Nb[mm]; be = 0.5 * Na[mm]; ga = 0.0; }
-        else if (f == 3) { al = 0.0; be = 0.0; ga = 0.5 * Nb[mm]; }
-        else { al = 0.0; be = 0.0; ga = 0.5 * Na[mm]; }
-        for (int a = 0; a < 3; a++) {
-          double v;
-          if (f == 0) v = al * Xxi[2 * a];
-          else if (f == 1) v = be * Xxi[2 * a + 1];
-          else if (f == 2) v = 0.5 * (Na[mm] * Xxi[2 * a + 1] + Nb[mm] * Xxi[2 * a]);
-          else v = n0[a] * ga;
-          S.Z[t][6 * mm + a] = v;
-        }
-        for (int b = 0; b < 3; b++) {
-          double v = 0.0;
-          if (f >= 3) {
-            const int c = (f == 3) ? 1 : 0;
-            double acc = 0.0;
-            for (int i = 0; i < 3; i++)
-              acc += Xxi[2 * i + c] * dmap(&S.fn[3 * mm], i, b);
-            v = 0.5 * N[mm] * acc;
-          }
-          S.Z[t][6 * mm + 3 + b] = v;
-        }
+      const int f = c_ty_field[tl];
+      for (int mm = 0; mm < 4; mm++)
+        tying_row(f, mm, N, Na, Nb, Xxi, n0, S.fn, S.Z[tl]);
+      if (tl < 4) {
+        shape_tab(s_shape, 16, N, Na, Nb);
+        grad3(Na, Nb, S.X, Xxi);
+        interp3(N, S.fn, n0);
+        tying_row(c_ty_field[8], tl, N, Na, Nb, Xxi, n0, S.fn, S.Z[8]);
       }
     }
     __syncwarp();
@@ -358,10 +401,15 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
       const double d22 = Del[5] - L20 * L20 - L21 * L21;
       L22 = d22 > 0.0 ? sqrt(d22) : 0.0;
     }
+    // units (q, node, dof): the 48 displacement dofs first, then the 48
+    // rotations, so that every round of the team runs one of the two paths
     for (int k = tl; k < 96; k += kTeam) {
-      const int q = k / 24, c = k % 24;
-      shape_at(4 + q, N, Na, Nb);
-      const int mm = c / 6, a = c - 6 * mm;
+      const bool rot = k >= 48;
+      const int kk = rot ? k - 48 : k;
+      const int q = kk / 12, mm = (kk - 12 * q) / 3;
+      const int a = (rot ? 3 : 0) + (kk - 12 * q - 3 * mm);
+      const int c = 6 * mm + a;
+      shape_tab(s_shape, 4 + q, N, Na, Nb);
       const double *T = S.g.T[q], *P = S.g.P[q], *Qm = S.g.Q[q];
       double bb[3];
       if (a < 3) {
@@ -392,7 +440,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
     const double sdrill = drill > 0.0 ? sqrt(drill) : 0.0;
     for (int k = tl; k < 96; k += kTeam) {
       const int q = k / 24, c = k % 24;
-      shape_at(4 + q, N, Na, Nb);
+      shape_tab(s_shape, 4 + q, N, Na, Nb);
       double v = 0.0;
       for (int kk = 0; kk < 4; kk++) v += N[kk] * S.g.Bd[kk][c];
       S.Z[21 + q][c] = (S.sdet[q] * sdrill) * v;
@@ -414,12 +462,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
         const int mm = i / 6, a = i - 6 * mm;
         if (m.pres && a < 3) {
           double aux = 0.0;
-          for (int q = 0; q < 4; q++) {
-            shape_at(4 + q, N, Na, Nb);
-            const double pr = N[0] * S.pres[0] + N[1] * S.pres[1] +
-                              N[2] * S.pres[2] + N[3] * S.pres[3];
-            aux += N[mm] * (pr * -S.det[q] * S.n0[q][a]);
-          }
+          for (int q = 0; q < 4; q++)
+            aux += s_shape.N[4 + q][mm] * (S.prd[q] * S.n0[q][a]);
           r += lambda * aux;
         }
         if (active) res[6 * S.nodes[mm] + a] += r;

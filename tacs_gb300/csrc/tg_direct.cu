@@ -449,6 +449,7 @@ int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
   tg::launch_copy(b, d->d_r, N, S(s));
   double prev = 0.0, eta = 0.0;
   int taken = 0, slow = 0, rc = TG_ERR_NOCONV;
+  bool met = false;
   if (bnorm == 0.0) rc = 0;  // x = 0 is exact
   while (rc != 0 && taken < max_steps) {
     tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
@@ -471,16 +472,21 @@ int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
     // normwise backward error of x
     const double den = d->anorm * h[1] + bnorm;
     eta = den > 0.0 ? h[0] / den : 0.0;
-    if (!(eta == eta)) break;  // NaN: the FP32 factor is unusable
-    if (eta <= tol) {
-      rc = 0;
+    if (!(eta == eta)) {  // NaN: the FP32 factor is unusable
+      met = false;
       break;
     }
-    // stagnation: two steps in a row that do not halve eta
+    if (eta <= tol) met = true;
+    // The backward-error test alone stops early where |A| |x| >> |b| (thin
+    // shells): there eta reaches eps sqrt(N) with a residual still far
+    // above an FP64 factorisation's.  So the steps go on while they halve
+    // eta, and stop at the first step that does not once the tolerance is
+    // met (two such steps in a row before it: stagnation).
     slow = (taken > 1 && eta > 0.5 * prev) ? slow + 1 : 0;
-    if (slow >= 2) break;
+    if (slow >= (met ? 1 : 2)) break;
     prev = eta;
   }
+  if (met) rc = 0;
   if (steps) *steps = taken;
   if (eta_out) *eta_out = eta;
   TG_CUDA(cudaGetLastError());

@@ -131,7 +131,7 @@ class Direct:
     precision PREC_FP32 factors in FP32 and solves FP64 right-hand sides
     by iterative refinement (FP64 residuals, FP32 corrections) until the
     normwise backward error is at most eps sqrt(N) (the test of LAPACK's
-    mixed-precision dsgesv).  Where that cannot work -- the FP32 Cholesky
+    mixed-precision dsgesv) and a further step no longer halves it.  Where that cannot work -- the FP32 Cholesky
     meets a non-positive pivot, or refinement stagnates because cond(A) is
     near the inverse of FP32's unit roundoff -- the matrix is factored in
     FP64 instead (`fell_back`), from its values at that moment."""

@@ -12,14 +12,14 @@ Tolerances (norm-wise max|a-b| / max|b|): element-level results (residual,
 every Jacobian entry, mat-vec, functions, state and design sensitivities,
 adjoint products) 1e-12, the KS design sensitivity 1e-11 (its exponential
 weights amplify rounding); solution, functions at the solution and the
-adjoint gradients 1e-7 (cond(K) x rounding of two different exact solvers:
-the GPU multifrontal factorisation against scipy's sparse LU of the oracle's
-matrix).
+adjoint gradients 1e-7 (two different exact solvers: the GPU multifrontal
+factorisation against a symmetric sparse factorisation of the oracle's
+matrix on the host).
 """
 import numpy as np
 import pytest
 
-from conftest import rel
+from conftest import exact_solve, rel
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -113,29 +113,28 @@ def test_element_level_parity_on_workload_shape(gpu, name):
 
 def _checker_adjoint(prob):
     """Static solve and adjoint gradients on the CPU: the oracle's matrix,
-    residual, functions and element sensitivities, with scipy's sparse LU as
-    the exact solver, in the order of the reference harness (K and R at
+    residual, functions and element sensitivities, with an exact sparse
+    solve (conftest.exact_solve) as the solver, in the order of the
+    reference harness (K and R at
     u = 0, u = -K^-1 (R - f), psi = K^-1 dfdu with the row-BC matrix,
     grad = dfdx - psi^T dR/dx)."""
     import oracle
     from scipy import sparse
-    from scipy.sparse.linalg import splu
     o = oracle.Oracle(prob)
     n = o.ndof
     r0, A = o.assemble_jac(np.zeros(n))
     rowp, cols, vals = o.bcsr_arrays(A)
     b = o.vpn
     K = sparse.bsr_matrix((vals.reshape(-1, b, b), cols, rowp),
-                          shape=(n, n)).tocsc()
+                          shape=(n, n)).tocsr()
     o.free(A)
-    lu = splu(K)
     f = _bc_zero(prob, prob["force"])
-    u = -lu.solve(r0 - f)
+    u = -exact_solve(K, r0 - f, prob)
     funcs = o.eval_funcs(u)
     grads = []
     for w in (0, 1):
         dfdu = _bc_zero(prob, o.sv_sens(u, w))
-        psi = lu.solve(dfdu)
+        psi = exact_solve(K, dfdu, prob)
         grads.append(o.dv_sens(u, w) + o.adj_res_product(u, psi, -1.0))
     return u, funcs, grads
 

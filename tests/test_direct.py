@@ -6,11 +6,11 @@ and the kernels are also checked on the CPU in test_direct_symbolic.py).
   (golden fixtures): 1e-7, the GMRES tolerance of the reference's solve
   times cond(K);
 * a thin simply supported plate, where ILU(0)-GMRES stalls: the true
-  residual at rounding level (1e-13 of |K| |u|) and agreement with a sparse
-  LU on the host within 10x the rounding spread of that exact solve (the
-  distance between its solutions for two elimination orders; cond(K) is
-  about 1e12 on these plates, so two exact FP64 solvers differ by ~1e-5 in
-  the displacements and ~1e-9 in the compliance);
+  residual at rounding level (1e-13 of |K| |u|) and agreement with an exact
+  sparse solve on the host (conftest.exact_solve: constrained dofs
+  removed, unit-diagonal scaling, symmetric factorisation) within 1e-8 or
+  10x the rounding spread of that solve (its distance between two
+  elimination orders), whichever is larger;
 * both orders (node coordinates and level structures) and refactoring
   after new matrix values;
 * the reference harness's adjoint gradients with both solves direct.
@@ -18,7 +18,7 @@ and the kernels are also checked on the CPU in test_direct_symbolic.py).
 import numpy as np
 import pytest
 
-from conftest import load_case, rel
+from conftest import exact_and_spread, load_case, rel
 
 torch = pytest.importorskip("torch")
 pytestmark = [pytest.mark.gpu, pytest.mark.direct]
@@ -38,16 +38,6 @@ def _host_matrix(mat, ndof):
     return sparse.bsr_matrix((mat.vals.cpu().numpy().reshape(-1, bs, bs),
                               mat.cols.cpu().numpy(), mat.rowp.cpu().numpy()),
                              shape=(ndof, ndof)).tocsc()
-
-
-def _exact_and_spread(K, b):
-    """Sparse LU solution on the host and its rounding spread: the relative
-    distance between the solutions of two elimination orders, for the
-    displacements (max norm) and for the compliance b^T x."""
-    from scipy.sparse.linalg import splu
-    x1 = splu(K, permc_spec="COLAMD").solve(b)
-    x2 = splu(K, permc_spec="MMD_AT_PLUS_A").solve(b)
-    return x1, rel(x2, x1), abs(b @ x2 - b @ x1) / abs(b @ x1)
 
 
 def _rhs(M, prob, mat):
@@ -92,7 +82,7 @@ def test_direct_thin_plate_where_ilu_stalls(gpu):
     bh = b.cpu().numpy()
     Kinf = abs(K).sum(axis=1).max()
     assert np.abs(K @ u - bh).max() < 1e-13 * Kinf * np.abs(u).max()
-    x_ref, spread, spread_c = _exact_and_spread(K, bh)
+    x_ref, spread, spread_c = exact_and_spread(K, bh, prob)
     assert rel(u, x_ref) < max(1e-8, 10.0 * spread)
     assert abs(bh @ u - bh @ x_ref) / abs(bh @ x_ref) < max(1e-12,
                                                             10.0 * spread_c)
@@ -222,7 +212,7 @@ def test_direct_as_gmres_preconditioner(gpu):
     bh, xh = b.cpu().numpy(), x32.cpu().numpy()
     Kinf = abs(K).sum(axis=1).max()
     assert np.abs(K @ xh - bh).max() < 1e-13 * Kinf * np.abs(xh).max()
-    _, spread, spread_c = _exact_and_spread(K, bh)
+    _, spread, spread_c = exact_and_spread(K, bh, prob)
     x64h = x64.cpu().numpy()
     assert rel(xh, x64h) < max(1e-8, 10.0 * spread)
     assert abs(bh @ xh - bh @ x64h) / abs(bh @ x64h) < max(1e-12,
@@ -231,8 +221,9 @@ def test_direct_as_gmres_preconditioner(gpu):
 
 @pytest.mark.parametrize("thin", [False, True], ids=["t10mm", "t2mm"])
 def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
-    """FP32 factorisation + FP64 refinement stops when the normwise
-    backward error reaches eps sqrt(N); where it cannot (the FP32 Cholesky
+    """FP32 factorisation + FP64 refinement converges when the normwise
+    backward error reaches eps sqrt(N) (and refines on while the steps halve
+    it); where it cannot (the FP32 Cholesky
     breaks down or refinement stagnates, cond(K) near 2^24) the solve falls
     back to an FP64 factorisation.  Either way the result has the FP64
     backward error (1e-13) and is the FP64 direct solution to within 10x
@@ -261,7 +252,7 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
         assert 1 <= st["last_refinement_steps"] <= 10
     K = _host_matrix(mat, M.ndof)
     bh, xh, x64h = b.cpu().numpy(), x.cpu().numpy(), x64.cpu().numpy()
-    _, spread, spread_c = _exact_and_spread(K, bh)
+    _, spread, spread_c = exact_and_spread(K, bh, prob)
     assert rel(xh, x64h) < max(1e-8, 10.0 * spread)
     assert abs(bh @ xh - bh @ x64h) / abs(bh @ x64h) < max(1e-12,
                                                             10.0 * spread_c)
