@@ -54,16 +54,18 @@ template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
                            int max_front, T *y, T *contrib, cudaStream_t s) {
   if (count <= 0) return;
-  direct_forward_kernel<T><<<count, 256, sizeof(T) * max_front, s>>>(
-      v, sn, count, y, contrib);
+  direct_forward_kernel<T>
+      <<<count, 256, sizeof(T) * (max_front + kDirectSolveDiag), s>>>(
+          v, sn, count, y, contrib);
 }
 
 template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
                             int max_front, const T *y, T *x, cudaStream_t s) {
   if (count <= 0) return;
-  direct_backward_kernel<T><<<count, 256, sizeof(T) * max_front, s>>>(
-      v, sn, count, y, x);
+  direct_backward_kernel<T>
+      <<<count, 256, sizeof(T) * (max_front + kDirectSolveDiag), s>>>(
+          v, sn, count, y, x);
 }
 
 template <class T>
@@ -96,7 +98,7 @@ cudaError_t direct_set_smem(int max_front) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  const int bytes = (int)sizeof(double) * max_front;
+  const int bytes = (int)sizeof(double) * (max_front + kDirectSolveDiag);
   if (bytes <= 48 * 1024 || bytes <= set[dev]) return cudaSuccess;
   const void *ks[4] = {(const void *)direct_forward_kernel<double>,
                        (const void *)direct_backward_kernel<double>,

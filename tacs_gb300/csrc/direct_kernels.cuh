@@ -339,6 +339,47 @@ __global__ void __launch_bounds__(256)
 }
 
 // ----------------------------------------------------------------- solves
+// Both solves go through the panel in blocks of kDirectSolveBlock columns:
+// the block's diagonal part is staged in shared memory (rows padded to an
+// odd length) and solved by one warp, and the block's off-diagonal part
+// updates the rest of the front in one pass whose threads read contiguous
+// panel rows (forward) or consecutive columns (backward).  Two CTA
+// barriers per block instead of two per column.  Dynamic shared memory:
+// the front's M entries of z, then the diagonal block.
+
+// Triangular solve of the staged diagonal block D (nb x nb, row stride
+// kDirectSolveBlock + 1) on zb[0..nb): lower (L zb = zb) or its transpose.
+// Warp 0 works on it; the others wait at the caller's barrier.
+template <class T, bool kTranspose>
+__device__ __forceinline__ void dk_block_solve(const T *D, int nb, T *zb) {
+  constexpr int P = kDirectSolveBlock + 1;
+  if (threadIdx.x >= 32) return;
+  const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
+  for (int kk = 0; kk < nb; kk++) {
+    const int k = kTranspose ? nb - 1 - kk : kk;
+    if (threadIdx.x == 0) zb[k] /= D[k * P + k];
+    __syncwarp();
+    const T zk = zb[k];
+    if (kTranspose) {
+      for (int j = threadIdx.x; j < k; j += ls) zb[j] -= D[k * P + j] * zk;
+    } else {
+      for (int j = k + 1 + threadIdx.x; j < nb; j += ls)
+        zb[j] -= D[j * P + k] * zk;
+    }
+    __syncwarp();
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void dk_stage_block(const Front<T> &f, int kb,
+                                               int nb, T *D) {
+  constexpr int P = kDirectSolveBlock + 1;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    D[r * P + c] = f.lp[(size_t)(kb + r) * f.C + kb + c];
+  }
+}
+
 // Forward: z = front rows of the supernode (own rows from y, the rows
 // below zero), plus the children's contribution vectors; L11 z1 = z1 and
 // z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
@@ -350,6 +391,7 @@ __global__ void __launch_bounds__(256)
   DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
+  T *D = z + f.M;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   for (int t = threadIdx.x; t < f.M; t += blockDim.x)
@@ -365,12 +407,19 @@ __global__ void __launch_bounds__(256)
       z[rel[t / bs] * bs + t % bs] += w[t];
     __syncthreads();
   }
-  for (int k = 0; k < f.C; k++) {
-    if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
+  for (int kb = 0; kb < f.C; kb += kDirectSolveBlock) {
+    const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
+    dk_stage_block(f, kb, nb, D);
     __syncthreads();
-    const T zk = z[k];
-    for (int i = k + 1 + threadIdx.x; i < f.M; i += blockDim.x)
-      z[i] -= f.lp[(size_t)i * f.C + k] * zk;
+    dk_block_solve<T, false>(D, nb, z + kb);
+    __syncthreads();
+    // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb)
+    for (int i = kb + nb + threadIdx.x; i < f.M; i += blockDim.x) {
+      const T *Li = f.lp + (size_t)i * f.C + kb;
+      T acc = 0;
+      for (int c = 0; c < nb; c++) acc += Li[c] * z[kb + c];
+      z[i] -= acc;
+    }
     __syncthreads();
   }
   for (int t = threadIdx.x; t < f.C; t += blockDim.x)
@@ -382,7 +431,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // Backward: z1 = y1 - L21^T x2 (x2 from the ancestors, already final),
-// then L11^T z1 = z1; own rows to x.
+// then L11^T z1 = z1 from the last block up; own rows to x.
 template <class T>
 __global__ void __launch_bounds__(256)
     direct_backward_kernel(DirectView v, const int *__restrict__ sn,
@@ -391,6 +440,7 @@ __global__ void __launch_bounds__(256)
   DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
+  T *D = z + f.M;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   for (int t = threadIdx.x; t < f.M; t += blockDim.x) {
@@ -404,12 +454,20 @@ __global__ void __launch_bounds__(256)
     z[j] -= acc;
   }
   __syncthreads();
-  for (int k = f.C - 1; k >= 0; k--) {
-    if (threadIdx.x == 0) z[k] /= f.lp[(size_t)k * f.C + k];
+  for (int kb = ((f.C - 1) / kDirectSolveBlock) * kDirectSolveBlock; kb >= 0;
+       kb -= kDirectSolveBlock) {
+    const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
+    dk_stage_block(f, kb, nb, D);
     __syncthreads();
-    const T zk = z[k];
-    for (int j = threadIdx.x; j < k; j += blockDim.x)
-      z[j] -= f.lp[(size_t)k * f.C + j] * zk;
+    dk_block_solve<T, true>(D, nb, z + kb);
+    __syncthreads();
+    // columns before the block: z_j -= sum_k L(kb + k, j) z(kb + k)
+    for (int j = threadIdx.x; j < kb; j += blockDim.x) {
+      T acc = 0;
+      for (int k = 0; k < nb; k++)
+        acc += f.lp[(size_t)(kb + k) * f.C + j] * z[kb + k];
+      z[j] -= acc;
+    }
     __syncthreads();
   }
   for (int t = threadIdx.x; t < f.C; t += blockDim.x)

@@ -11,6 +11,10 @@ namespace tg {
 constexpr int kDirectPanel = 32, kDirectTile = 32;
 // rows of a panel's off-diagonal part solved by one CTA (one per thread)
 constexpr int kDirectTrsmRows = 256;
+// column block of the triangular solves, and the shared memory of its
+// staged diagonal block (rows padded to kDirectSolveBlock + 1 entries)
+constexpr int kDirectSolveBlock = 32;
+constexpr int kDirectSolveDiag = kDirectSolveBlock * (kDirectSolveBlock + 1);
 
 struct DirectView {
   int bs;

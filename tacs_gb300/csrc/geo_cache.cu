@@ -18,8 +18,9 @@
 // rows' k-th blocks together (k = 0 .. longest row - 1), so on structured
 // meshes all lanes of a step have the same number of contributions and the
 // FP64 FMAs carry no idle lanes.  Entries that are zero in every class
-// (the masks) are not summed: a flat plate's membrane-bending coupling
-// blocks are exactly zero.  Each step's 32 blocks are staged in shared
+// are not summed (a compile-time pattern, chosen by the host from the
+// table): a flat plate's membrane-bending coupling entries are exactly
+// zero.  Each step's 32 blocks are staged in shared
 // memory and written back with consecutive lanes on consecutive doubles.
 // The residual sums over k in registers: every output has one fixed
 // summation order (deterministic).
@@ -30,7 +31,21 @@ namespace {
 
 constexpr int kGeoWarps = 4;
 
-template <int BS, int NCOEF, int NPE>
+// Entry patterns (bit r * bs + c) of the coefficient blocks.  A flat
+// shell in a coordinate plane couples (u, v, theta_z) and (w, theta_x,
+// theta_y) only, and its bending part only (theta_x, theta_y): 18 and 4 of
+// the 36 entries.  The kernel is instantiated per pattern so that the
+// skipped entries cost no instruction at all (a run-time mask still issues
+// predicated FMAs); the host picks the pattern that covers the table's
+// non-zero entries.
+constexpr unsigned long long kAll36 = (1ull << 36) - 1, kAll9 = (1ull << 9) - 1;
+constexpr unsigned long long kFlatK1 =
+    (0x23ull << 0) | (0x23ull << 6) | (0x1Cull << 12) | (0x1Cull << 18) |
+    (0x1Cull << 24) | (0x23ull << 30);
+constexpr unsigned long long kFlatK3 = (0x18ull << 18) | (0x18ull << 24);
+
+template <int BS, int NCOEF, int NPE, unsigned long long M1,
+          unsigned long long M3>
 __global__ void __launch_bounds__(kGeoWarps * 32)
     geo_assembly_kernel(GeoView g, const double *__restrict__ vars,
                         double lambda, int apply_bcs,
@@ -49,7 +64,7 @@ __global__ void __launch_bounds__(kGeoWarps * 32)
   const int p0 = rv ? g.rowp[row] : 0, p1 = rv ? g.rowp[row + 1] : 0;
   const int kmax = g.warp_kmax[gw];
   const int bcm = (rv && apply_bcs) ? g.node_bc[row] : 0;
-  const unsigned long long m1 = g.mask1, m3 = g.mask3, mu = m1 | m3;
+  constexpr unsigned long long m1 = M1, m3 = M3, mu = M1 | M3;
   double y[BS];
 #pragma unroll
   for (int r = 0; r < BS; r++) y[r] = 0.0;
@@ -141,12 +156,13 @@ __global__ void geo_mask_kernel(const double *__restrict__ table, int ncoef,
   if (m) atomicOr(&masks[(blk / (B2 == 36 ? 16 : 64)) % ncoef], m);
 }
 
-template <int BS, int NCOEF, int NPE>
+template <int BS, int NCOEF, int NPE, unsigned long long M1,
+          unsigned long long M3>
 void launch_geo(const GeoView &g, const double *vars, double lambda,
                 int apply_bcs, double *res, double *vals, cudaStream_t s) {
   const int grid = (g.nwarps + kGeoWarps - 1) / kGeoWarps;
-  geo_assembly_kernel<BS, NCOEF, NPE><<<grid, kGeoWarps * 32, 0, s>>>(
-      g, vars, lambda, apply_bcs, res, vals);
+  geo_assembly_kernel<BS, NCOEF, NPE, M1, M3>
+      <<<grid, kGeoWarps * 32, 0, s>>>(g, vars, lambda, apply_bcs, res, vals);
 }
 
 }  // namespace
@@ -167,10 +183,16 @@ void launch_geo_assembly(int bs, const GeoView &g, const double *vars,
                          double lambda, int apply_bcs, double *res,
                          double *vals, cudaStream_t s) {
   if (g.nwarps <= 0) return;
-  if (bs == 6)
-    launch_geo<6, 2, 4>(g, vars, lambda, apply_bcs, res, vals, s);
-  else
-    launch_geo<3, 1, 8>(g, vars, lambda, apply_bcs, res, vals, s);
+  if (bs == 6) {
+    if ((g.mask1 & ~kFlatK1) == 0 && (g.mask3 & ~kFlatK3) == 0)
+      launch_geo<6, 2, 4, kFlatK1, kFlatK3>(g, vars, lambda, apply_bcs, res,
+                                            vals, s);
+    else
+      launch_geo<6, 2, 4, kAll36, kAll36>(g, vars, lambda, apply_bcs, res,
+                                          vals, s);
+  } else {
+    launch_geo<3, 1, 8, kAll9, 0>(g, vars, lambda, apply_bcs, res, vals, s);
+  }
 }
 
 }  // namespace tg

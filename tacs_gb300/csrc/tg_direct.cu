@@ -237,7 +237,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = dalloc(&d->d_pb, N);
   if (!rc) rc = dalloc(&d->d_kpb, N);
   if (!rc) rc = dalloc(&d->d_fail, 1);
-  if (!rc && (size_t)d->max_front * sizeof(double) > 227 * 1024)
+  if (!rc && (size_t)(d->max_front + tg::kDirectSolveDiag) * sizeof(double) >
+                 227 * 1024)
     rc = fail(TG_ERR_ARG, "tg_direct_create: front too large for a CTA's "
                           "solve workspace");
   if (rc) {

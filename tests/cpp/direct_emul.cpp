@@ -23,6 +23,7 @@ static EmuDim3 threadIdx{0, 0, 0}, blockIdx{0, 0, 0}, blockDim{1, 1, 1},
 #define __shared__ static
 #define __launch_bounds__(n)
 #define __syncthreads() ((void)0)
+#define __syncwarp() ((void)0)
 static std::vector<double> g_dyn;
 static double *dk_dyn_smem() { return g_dyn.data(); }
 static inline int atomicCAS(int *a, int cmp, int val) {
@@ -189,13 +190,15 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   const int nl = (int)an.level_ptr.size() - 1;
   for (int L = 0; L < nl; L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_forward_kernel<T>, le - lb, 1, max_front, v,
+    launch(direct_forward_kernel<T>, le - lb, 1,
+           max_front + tg::kDirectSolveDiag, v,
            (const int *)an.level_sn.data() + lb, le - lb, ypos.data(),
            contrib.data());
   }
   for (int L = nl - 1; L >= 0; L--) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_backward_kernel<T>, le - lb, 1, max_front, v,
+    launch(direct_backward_kernel<T>, le - lb, 1,
+           max_front + tg::kDirectSolveDiag, v,
            (const int *)an.level_sn.data() + lb, le - lb,
            (const T *)ypos.data(), xpos.data());
   }

@@ -249,7 +249,8 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
     assert st["fell_back_to_fp64"] or st["last_backward_error"] <= tol
     if not thin:
         assert not st["fell_back_to_fp64"]
-        assert 1 <= st["last_refinement_steps"] <= 10
+        # refinement runs on while a step halves the backward error
+        assert 1 <= st["last_refinement_steps"] <= 30
     K = _host_matrix(mat, M.ndof)
     bh, xh, x64h = b.cpu().numpy(), x.cpu().numpy(), x64.cpu().numpy()
     _, spread, spread_c = exact_and_spread(K, bh, prob)
