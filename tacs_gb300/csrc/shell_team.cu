@@ -33,14 +33,13 @@ namespace {
 
 constexpr int kTeam = 8;
 constexpr int kTeamsPerWarp = 32 / kTeam;
-constexpr int kWarpsPerCta = 2;
+constexpr int kWarpsPerCta = 1;
 constexpr int kTeamsPerCta = kTeamsPerWarp * kWarpsPerCta;
 constexpr int kNchan = 25;
 
 struct TeamGeo {
   double Bd[4][24];
   double T[4][9], P[4][9], Q[4][9];
-  double G[9][9];
 };
 
 struct __align__(16) TeamSmem {
@@ -50,13 +49,13 @@ struct __align__(16) TeamSmem {
   double n0[4][3];
   double det[4];
   double sdet[4];
-  double pres[4];
-  double sd[9];   // sqrt of the LDL^T pivots of G
-  double y[kNchan];
   double prd[4];  // interpolated pressure x -detXd at the 4 points
   double t;
-  double Z[kNchan][24];  // rows 0..8 start as Bty; 9..24 hold M/CM first
-  TeamGeo g;
+  // rows 0..8 start as Bty; rows 9..23 hold M_q / C M_q, then rows 9..12
+  // G (its L D L^T in place) and the pivots' square roots, then the
+  // bending and drilling channels
+  double Z[kNchan][24];
+  TeamGeo g;  // T is reused for the residual's channel projections
   int nodes[4];
   int slot[16];
   int pad[2];
@@ -173,7 +172,6 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
     if (active) {
       if (tl < 4) {
         S.nodes[tl] = m.conn[4 * e + tl];
-        S.pres[tl] = m.pres ? m.pres[4 * e + tl] : 0.0;
       }
       if (tl == 0) S.t = m.thick[e];
     }
@@ -264,8 +262,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
         // TACSShellPressure::addResidual (TACSShellPressure.h:56-90): the
         // interpolated pressure times -detXd at this point
         if (m.pres) {
-          const double pr = N[0] * S.pres[0] + N[1] * S.pres[1] +
-                            N[2] * S.pres[2] + N[3] * S.pres[3];
+          const double *pe = m.pres + 4 * (size_t)e;
+          const double pr = N[0] * pe[0] + N[1] * pe[1] + N[2] * pe[2] +
+                            N[3] * pe[3];
           S.prd[q] = pr * -det;
         }
         if (!(det > 0.0) && active && err_flag) atomicCAS(err_flag, 0, 1);
@@ -341,27 +340,51 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
       CMq[k] = v * S.det[q];
     }
     __syncwarp();
-    // G = sum_q detXd_q M_q^T C M_q (lower triangle, 45 entries)
-    for (int k = tl; k < 45; k += kTeam) {
-      int a = 0, base = 0;
-      while (base + a + 1 <= k) {
-        base += a + 1;
-        a++;
+    // G = sum_q detXd_q M_q^T C M_q (lower triangle, 45 entries), formed
+    // in registers and stored over the consumed M_q (Z rows 9..12)
+    double (*G)[9] = reinterpret_cast<double (*)[9]>(&S.Z[9][0]);
+    double *sd = &S.Z[9][0] + 81;  // sqrt of the LDL^T pivots of G
+    {
+      double gv[6];
+#pragma unroll
+      for (int jj = 0; jj < 6; jj++) {
+        const int k = tl + kTeam * jj;
+        gv[jj] = 0.0;
+        if (k < 45) {
+          int a = 0, base = 0;
+          while (base + a + 1 <= k) {
+            base += a + 1;
+            a++;
+          }
+          const int b = k - base;  // b <= a
+          double v = 0.0;
+          for (int q = 0; q < 4; q++)
+            for (int r = 0; r < 5; r++)
+              v += Mq[45 * q + 9 * r + a] * CMq[45 * q + 9 * r + b];
+          gv[jj] = v;
+        }
       }
-      const int b = k - base;  // b <= a
-      double v = 0.0;
-      for (int q = 0; q < 4; q++)
-        for (int r = 0; r < 5; r++)
-          v += Mq[45 * q + 9 * r + a] * CMq[45 * q + 9 * r + b];
-      S.g.G[a][b] = v;
+      __syncwarp();
+#pragma unroll
+      for (int jj = 0; jj < 6; jj++) {
+        const int k = tl + kTeam * jj;
+        if (k < 45) {
+          int a = 0, base = 0;
+          while (base + a + 1 <= k) {
+            base += a + 1;
+            a++;
+          }
+          G[a][k - base] = gv[jj];
+        }
+      }
     }
     __syncwarp();
     // LDL^T of G (right-looking); L stored below the diagonal
     for (int k = 0; k < 9; k++) {
-      const double dk = S.g.G[k][k];
+      const double dk = G[k][k];
       const double inv = dk > 0.0 ? 1.0 / dk : 0.0;
       __syncwarp();
-      for (int i = k + 1 + tl; i < 9; i += kTeam) S.g.G[i][k] *= inv;
+      for (int i = k + 1 + tl; i < 9; i += kTeam) G[i][k] *= inv;
       __syncwarp();
       const int nr = 8 - k;
       for (int p = tl; p < nr * (nr + 1) / 2; p += kTeam) {
@@ -371,9 +394,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
           ii++;
         }
         const int i = k + 1 + ii, j = k + 1 + (p - base);
-        S.g.G[i][j] -= S.g.G[i][k] * S.g.G[j][k] * dk;
+        G[i][j] -= G[i][k] * G[j][k] * dk;
       }
-      if (tl == 0) S.sd[k] = dk > 0.0 ? sqrt(dk) : 0.0;
+      if (tl == 0) sd[k] = dk > 0.0 ? sqrt(dk) : 0.0;
       __syncwarp();
     }
     // membrane/shear channels: z_t = sd_t (L^T Bty)_t, column by column
@@ -382,8 +405,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
       for (int t = 0; t < 9; t++) b[t] = S.Z[t][c];
       for (int t = 0; t < 9; t++) {
         double v = b[t];
-        for (int t2 = t + 1; t2 < 9; t2++) v += S.g.G[t2][t] * b[t2];
-        S.Z[t][c] = S.sd[t] * v;
+        for (int t2 = t + 1; t2 < 9; t2++) v += G[t2][t] * b[t2];
+        S.Z[t][c] = sd[t] * v;
       }
     }
     __syncwarp();
@@ -449,15 +472,16 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
 
     // ------------------------------------------------------- residual
     if (res) {
+      double *ybuf = &S.g.T[0][0];  // T is not read after the bending rows
       for (int c = tl; c < kNchan; c += kTeam) {
         double v = 0.0;
         for (int i = 0; i < 24; i++) v += S.Z[c][i] * S.u[i];
-        S.y[c] = v;
+        ybuf[c] = v;
       }
       __syncwarp();
       for (int i = tl; i < 24; i += kTeam) {
         double r = 0.0;
-        for (int c = 0; c < kNchan; c++) r += S.Z[c][i] * S.y[c];
+        for (int c = 0; c < kNchan; c++) r += S.Z[c][i] * ybuf[c];
         // TACSShellPressure::addResidual (TACSShellPressure.h:56-90)
         const int mm = i / 6, a = i - 6 * mm;
         if (m.pres && a < 3) {
@@ -545,8 +569,20 @@ void launch_shell_team_assembly(const ElemParams &ep, const MeshView &m,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) == cudaSuccess)
     init[dev] = true;
+  // resident CTAs per SM (shared memory bound), once per device
+  static int per_sm[kMaxDevices] = {};
+  if (dev >= 0 && dev < kMaxDevices && !per_sm[dev]) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, shell_team_assembly_kernel, kWarpsPerCta * 32, smem) ==
+            cudaSuccess &&
+        nb > 0)
+      per_sm[dev] = nb;
+  }
+  const int resident = (dev >= 0 && dev < kMaxDevices && per_sm[dev])
+                           ? per_sm[dev] : 1;
   int need = (cr.count + kTeamsPerCta - 1) / kTeamsPerCta;
-  int cap = sm_count() * 3;
+  int cap = sm_count() * resident;
   int grid = need < cap ? need : cap;
   if (grid < 1) grid = 1;
   shell_team_assembly_kernel<<<grid, kWarpsPerCta * 32, smem, s>>>(
