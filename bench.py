@@ -244,6 +244,119 @@ def hex_section(torch, steps=5):
     return out
 
 
+def c3_solve_section(torch, pc_kind=0, nfd=32, h=1e-6):
+    """The 128 x 128 x 64 SIMP block solved and differentiated: FP64 GMRES
+    with ILU(0) (pc_kind: natural or colour-reordered), compliance and its
+    gradient with respect to the 1,048,576 densities through the autograd
+    backward (dC/drho = 3 rho^2 dC/dt), checked three ways:
+      * central differences with h on nfd seeded elements (seed 33): the
+        difference C(rho + h e_k) - C(rho - h e_k) is evaluated as
+        -(t(rho_k + h) - t(rho_k - h)) u+^T K_k u-, with u+ and u- solved
+        for the perturbed densities (exact for the linear problem with a
+        symmetric K and density-independent loads; a plain subtraction of
+        two compliances would lose the 1e-12 relative change to rounding);
+      * a directional central difference along a seeded positive direction
+        (seed 34), two compliances subtracted;
+      * the oracle's addDVSens + addAdjointResProducts at the GPU's state
+        and adjoint against the GPU's (element level)."""
+    import oracle
+    from tacs_gb300 import autograd as ag
+    from tacs_gb300 import meshes, problem
+    p = meshes.hex_c3()
+    M = problem.GpuModel(p)
+    M.set_fixed_geometry(True)
+    solver = ag.StaticSolver(M, np.zeros(M.ndof), m=200, nrestart=40,
+                             rtol=1e-10, pc_kind=pc_kind)
+    rho0 = torch.as_tensor(p["rho"], device="cuda")
+    x = rho0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c = ag.static_functional(x ** 3, solver, 0).sum()
+    c.backward()
+    torch.cuda.synchronize()
+    s_grad = time.perf_counter() - t0
+    g = x.grad.detach()
+    u = solver.u[0].clone()
+    comp = float(c.detach())
+    gmax = float(g.abs().max())
+    out = {"workload": "hex8 SIMP block 128x128x64, compliance gradient wrt "
+                       "densities, GMRES(200) + ILU(0) to 1e-10",
+           "elements": int(p["nelem"]), "dof": int(M.ndof),
+           "preconditioner": "natural ILU(0)" if pc_kind == 0
+           else "colour-reordered ILU(0)",
+           "s_per_gradient": s_grad, "compliance": comp,
+           "iters": [int(np.max(i)) for i in solver.iters]}
+    # central differences on seeded elements
+    t0v = rho0 ** 3
+    zero = M.vec()
+    mat_p = M.new_mat()
+    ksm_p = problem.Ksm(mat_p, solver.pc, 200, 10)
+    rng = np.random.default_rng(33)
+    elems = rng.choice(int(p["nelem"]), nfd, replace=False)
+
+    def perturbed(tv, x0, rtol):
+        M.set_design_vars(tv)
+        r0 = M.vec()
+        M.assemble_jacobian(zero, mat_p, r0)
+        b = -r0
+        ksm_p.set_tolerances(rtol, 1e-30)
+        xs, flag = ksm_p.solve(b, x=x0.clone(), zero_guess=False)
+        return xs, b, flag
+
+    t0 = time.perf_counter()
+    errs, flags = [], []
+    for k in elems:
+        us = []
+        for sgn in (1.0, -1.0):
+            tv = t0v.clone()
+            tv[k] = (rho0[k] + sgn * h) ** 3
+            xs, _, fl = perturbed(tv, u, 1e-8)
+            us.append(xs)
+            flags.append(fl)
+        prod = M.dv_vec()
+        M.add_adjoint_res_products(us[1], [us[0]], [prod])
+        dt = float((rho0[k] + h) ** 3 - (rho0[k] - h) ** 3)
+        fd = -dt * float(prod[k]) / (2.0 * h)
+        errs.append(abs(fd - float(g[k])) / gmax)
+    out["fd_elements"] = {"h": h, "count": nfd, "seed": 33,
+                          "max_err_rel_to_max_grad": max(errs),
+                          "converged": int(sum(flags)),
+                          "s": time.perf_counter() - t0}
+    # directional central difference
+    d = torch.as_tensor(np.random.default_rng(34).random(int(p["nelem"])),
+                        device="cuda")
+    cs = []
+    for sgn in (1.0, -1.0):
+        xs, b, fl = perturbed((rho0 + sgn * h * d) ** 3, u, 1e-10)
+        cs.append(float(M.eval_functions(xs, [0])[0]))
+    fd_dir = (cs[0] - cs[1]) / (2.0 * h)
+    adj_dir = float((g * d).sum())
+    out["fd_direction"] = {"h": h, "seed": 34, "fd": fd_dir, "adjoint": adj_dir,
+                           "rel_err": abs(fd_dir - adj_dir) / abs(adj_dir)}
+    M.set_design_vars(t0v)
+    # oracle: addDVSens + addAdjointResProducts at the GPU state and adjoint
+    dfdu = M.vec()
+    M.eval_functions(u, [0])
+    M.add_sv_sens(u, [0], [dfdu])
+    M.apply_bcs(dfdu)
+    psi, _ = solver.ksm.solve(dfdu)
+    gt = M.dv_vec()
+    M.add_total_derivative(u, 0, psi, gt, 1.0, -1.0)
+    o = oracle.Oracle(p, nthreads=os.cpu_count() or 1)
+    uh, ph = u.cpu().numpy(), psi.cpu().numpy()
+    t0 = time.perf_counter()
+    go = o.dv_sens(uh, 0) + o.adj_res_product(uh, ph, -1.0)
+    gth = gt.cpu().numpy()
+    out["oracle_dv_adjres"] = {
+        "rel_err": float(np.abs(gth - go).max() / np.abs(go).max()),
+        "chain_rule_rel_err": float(
+            (3.0 * rho0 ** 2 * gt - g).abs().max() / g.abs().max()),
+        "oracle_s": time.perf_counter() - t0}
+    del M, solver, mat_p, ksm_p
+    torch.cuda.empty_cache()
+    return out
+
+
 def fixed_geometry_section(torch, p, steps=20, label="", bs=6):
     """Fixed-geometry assembly (tg_assembler_set_fixed_geometry) of the same
     workload: the residual and Jacobian from per-geometry coefficient
@@ -426,13 +539,25 @@ def replica_time(ms, dist=None, device=None):
     return float(t.item())
 
 
+# Figures carried over from the committed ncu capture of one colour launch
+# (16,384 elements) of the 256 x 256 plate
+# (profiles/shell_team_assembly_mitc4_256_full.md); the bench line labels
+# them as such, beside the CUDA-event timings it measures itself.
+SHELL_PROFILE = {
+    "source": "profiles/shell_team_assembly_mitc4_256_full.md (ncu --set "
+              "full, one colour launch, 256x256 plate)",
+    "dram_bytes_per_launch": 100.64e6 + 36.31e6,
+    "elements_per_launch": 16384,
+    "fp64_pipe_active": 0.872,
+}
+
+
 def traffic_per_step(nelem):
-    """DRAM bytes (read + write) of the assembly kernel per step: ncu
-    measured 135.4 MB for one colour launch of 16,384 elements of the
-    256 x 256 plate (dram__bytes_read.sum + dram__bytes_write.sum); the
-    per-element traffic is size independent (colour-by-colour block
-    read-modify-write), so it scales with the elements of a step."""
-    return int(135.4e6 / 16384 * nelem)
+    """DRAM bytes (read + write) of the assembly kernel per step, scaled
+    from the capture by elements (the per-element traffic is size
+    independent: colour-by-colour block read-modify-write)."""
+    return int(SHELL_PROFILE["dram_bytes_per_launch"]
+               / SHELL_PROFILE["elements_per_launch"] * nelem)
 
 
 # FP64 work per element of one residual + Jacobian assembly (flops: add,
@@ -444,7 +569,7 @@ def traffic_per_step(nelem):
 #    DMUL thread instructions over one colour launch of 16,384 elements
 #    (shell: 256 x 256 plate; hex: 64 x 64 x 32 block)
 FP64_FLOPS_PER_ELEMENT = {
-    "shell": {"reference": 153602, "executed": 39574},
+    "shell": {"reference": 153602, "executed": 37745},
     "hex": {"reference": 149808, "executed": 14204},
 }
 # nominal FP64 peak: 152 SMs x 2 FMA lanes per clock x 2 flops x 2.07 GHz
@@ -624,6 +749,10 @@ def main():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--adj-size", type=int, default=64)
     ap.add_argument("--no-hex", action="store_true")
+    ap.add_argument("--c3-solve", action="store_true",
+                    help="solve and differentiate the 128x128x64 hex block")
+    ap.add_argument("--c3-pc", type=int, default=0,
+                    help="its ILU(0): 0 natural order, 2 colour-reordered")
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the fixed-geometry assembly section")
     ap.add_argument("--no-cylinder", action="store_true")
@@ -741,7 +870,11 @@ def main():
                      "traffic_unit": "bytes per step (ncu, scaled)",
                      # the kernel's binding resource: ncu's
                      # sm__pipe_fp64_cycles_active on one colour launch
-                     "fp64_pipe_active": 0.705,
+                     "fp64_pipe_active": SHELL_PROFILE["fp64_pipe_active"],
+                     "carried_from_profile": {
+                         "fields": ["traffic", "fp64_pipe_active",
+                                    "fp64.executed_flops_per_element"],
+                         "source": SHELL_PROFILE["source"]},
                      "peak_source": peak_src,
                      "kernel": "shell_team_assembly_kernel",
                      "kernel_ms": kern_ms, "algorithmic_bytes": algo,
@@ -788,6 +921,9 @@ def main():
                     "cache", bs=3))
     if rank == 0 and not args.no_hex:
         line["hex_c3"] = guarded(lambda: hex_section(torch))
+    if rank == 0 and args.c3_solve:
+        line["c3_solve"] = guarded(lambda: c3_solve_section(
+            torch, pc_kind=args.c3_pc))
     if rank == 0 and args.c2_adjoint:
         line["c2_adjoint"] = guarded(
             lambda: c2_adjoint_section(torch, args.size))
