@@ -542,7 +542,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
 
 def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
                     pc_kind=_lib.PC_ILU0, mixed=False, func=1, lev_fill=0,
-                    direct=False):
+                    direct=False, direct_solver=None, mat=None):
     """Independent meshes (element / node segments set from the problem's
     seg_elem_ptr / seg_node_ptr) under several load cases, solved and
     differentiated together: one batched GMRES for all forward solves, the
@@ -553,19 +553,28 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     (nlc, ndof), per-mesh function values (nlc, nseg), per-element gradients
     (nlc, ndv), per-system iteration counts and convergence flags of both
     solves (index load_case * nseg + mesh).
+
+    direct_solver (with the matrix mat it was made for): a Direct from an
+    earlier call, whose analysis (ordering, supernodes, storage) is reused
+    -- the next design of an optimisation loop refactors it only.
     """
     prob = model.prob
     model.set_segments(prob["seg_elem_ptr"])
     nlc = loads.shape[0]
     u0 = model.vec()
-    mat = model.new_mat()
+    if direct_solver is not None:
+        if mat is None:
+            raise ValueError("direct_solver needs the matrix it was made for")
+    else:
+        mat = model.new_mat()
     model.assemble_jacobian(u0, mat, model.vec())
     if direct:
         # one complete factorisation of the block-diagonal matrix (FP32 with
         # FP64 refinement for direct="mixed"); every load case and mesh is
         # then solved directly (reported as converged in 0 iterations)
-        dsol = Direct(mat, precision=_lib.PREC_FP32 if direct == "mixed"
-                      else _lib.PREC_FP64)
+        dsol = direct_solver if direct_solver is not None else Direct(
+            mat, precision=_lib.PREC_FP32 if direct == "mixed"
+            else _lib.PREC_FP64)
         dsol.factor()
         nsys = nlc * model.nseg
 
@@ -601,7 +610,7 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
                                             1.0, -1.0)
     return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,
                 iters_adj=it_a, flags_adj=fl_a, psi=Psi, resnorm_fwd=rn_f,
-                resnorm_adj=rn_a, direct=dsol if direct else None)
+                resnorm_adj=rn_a, direct=dsol if direct else None, mat=mat)
 
 
 def batch_loads(model):
