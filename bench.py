@@ -90,7 +90,8 @@ def adjoint_section(n, torch, colored=False):
         grads[label] = [g.cpu().numpy() for g in r["grads"]]
         out[label] = {"s_per_gradient": dt, "iters": r["iters"],
                       "converged": [int(f) for f in r["flags"]],
-                      "ilu_schedule": r["pc"].schedule()}
+                      "ilu_schedule": r["pc"].schedule(),
+                      "launch": r["ksm"].graph_info()}
         if label == "fp64_ilu0_natural":
             out["shape_derivative"] = guarded(
                 lambda: xpt_timing(M, r, torch))
@@ -161,6 +162,7 @@ def c2_adjoint_section(torch, n=512):
     from tacs_gb300 import problem
     p = c2_problem(n=n)
     M = problem.GpuModel(p)
+    M.set_fixed_geometry(True)  # thicknesses change, the nodes do not
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     solver = ag.StaticSolver(M, np.zeros(M.ndof), direct=True)
@@ -244,21 +246,18 @@ def hex_section(torch, steps=5):
     return out
 
 
-def c3_solve_section(torch, pc_kind=0, nfd=32, h=1e-6):
+def c3_solve_section(torch, pc_kind=0, h=1e-6):
     """The 128 x 128 x 64 SIMP block solved and differentiated: FP64 GMRES
     with ILU(0) (pc_kind: natural or colour-reordered), compliance and its
     gradient with respect to the 1,048,576 densities through the autograd
-    backward (dC/drho = 3 rho^2 dC/dt), checked three ways:
-      * central differences with h on nfd seeded elements (seed 33): the
-        difference C(rho + h e_k) - C(rho - h e_k) is evaluated as
-        -(t(rho_k + h) - t(rho_k - h)) u+^T K_k u-, with u+ and u- solved
-        for the perturbed densities (exact for the linear problem with a
-        symmetric K and density-independent loads; a plain subtraction of
-        two compliances would lose the 1e-12 relative change to rounding);
-      * a directional central difference along a seeded positive direction
-        (seed 34), two compliances subtracted;
+    backward (dC/drho = 3 rho^2 dC/dt), checked by
+      * a central difference with h along a seeded positive direction
+        (seed 34) over all densities, two compliances subtracted (a single
+        density moves the compliance by ~1e-12 of itself at h = 1e-6, below
+        FP64 resolution; the per-element central differences on 32 seeded
+        elements run on a reduced block in tests/test_autograd.py);
       * the oracle's addDVSens + addAdjointResProducts at the GPU's state
-        and adjoint against the GPU's (element level)."""
+        and adjoint (psi = 2 u for compliance) against the GPU's."""
     import oracle
     from tacs_gb300 import autograd as ag
     from tacs_gb300 import meshes, problem
@@ -277,70 +276,39 @@ def c3_solve_section(torch, pc_kind=0, nfd=32, h=1e-6):
     s_grad = time.perf_counter() - t0
     g = x.grad.detach()
     u = solver.u[0].clone()
-    comp = float(c.detach())
-    gmax = float(g.abs().max())
     out = {"workload": "hex8 SIMP block 128x128x64, compliance gradient wrt "
                        "densities, GMRES(200) + ILU(0) to 1e-10",
            "elements": int(p["nelem"]), "dof": int(M.ndof),
            "preconditioner": "natural ILU(0)" if pc_kind == 0
            else "colour-reordered ILU(0)",
-           "s_per_gradient": s_grad, "compliance": comp,
+           "s_per_gradient": s_grad, "compliance": float(c.detach()),
            "iters": [int(np.max(i)) for i in solver.iters]}
-    # central differences on seeded elements
-    t0v = rho0 ** 3
+    # directional central difference, warm-started solves
     zero = M.vec()
     mat_p = M.new_mat()
-    ksm_p = problem.Ksm(mat_p, solver.pc, 200, 10)
-    rng = np.random.default_rng(33)
-    elems = rng.choice(int(p["nelem"]), nfd, replace=False)
-
-    def perturbed(tv, x0, rtol):
-        M.set_design_vars(tv)
-        r0 = M.vec()
-        M.assemble_jacobian(zero, mat_p, r0)
-        b = -r0
-        ksm_p.set_tolerances(rtol, 1e-30)
-        xs, flag = ksm_p.solve(b, x=x0.clone(), zero_guess=False)
-        return xs, b, flag
-
-    t0 = time.perf_counter()
-    errs, flags = [], []
-    for k in elems:
-        us = []
-        for sgn in (1.0, -1.0):
-            tv = t0v.clone()
-            tv[k] = (rho0[k] + sgn * h) ** 3
-            xs, _, fl = perturbed(tv, u, 1e-8)
-            us.append(xs)
-            flags.append(fl)
-        prod = M.dv_vec()
-        M.add_adjoint_res_products(us[1], [us[0]], [prod])
-        dt = float((rho0[k] + h) ** 3 - (rho0[k] - h) ** 3)
-        fd = -dt * float(prod[k]) / (2.0 * h)
-        errs.append(abs(fd - float(g[k])) / gmax)
-    out["fd_elements"] = {"h": h, "count": nfd, "seed": 33,
-                          "max_err_rel_to_max_grad": max(errs),
-                          "converged": int(sum(flags)),
-                          "s": time.perf_counter() - t0}
-    # directional central difference
+    ksm_p = problem.Ksm(mat_p, solver.pc, 200, 40)
+    ksm_p.set_tolerances(1e-9, 1e-30)
     d = torch.as_tensor(np.random.default_rng(34).random(int(p["nelem"])),
                         device="cuda")
+    t0 = time.perf_counter()
     cs = []
     for sgn in (1.0, -1.0):
-        xs, b, fl = perturbed((rho0 + sgn * h * d) ** 3, u, 1e-10)
+        M.set_design_vars((rho0 + sgn * h * d) ** 3)
+        r0 = M.vec()
+        M.assemble_jacobian(zero, mat_p, r0)
+        xs, fl = ksm_p.solve(-r0, x=u.clone(), zero_guess=False)
         cs.append(float(M.eval_functions(xs, [0])[0]))
+    M.set_design_vars(rho0 ** 3)
     fd_dir = (cs[0] - cs[1]) / (2.0 * h)
     adj_dir = float((g * d).sum())
-    out["fd_direction"] = {"h": h, "seed": 34, "fd": fd_dir, "adjoint": adj_dir,
-                           "rel_err": abs(fd_dir - adj_dir) / abs(adj_dir)}
-    M.set_design_vars(t0v)
-    # oracle: addDVSens + addAdjointResProducts at the GPU state and adjoint
-    dfdu = M.vec()
-    M.eval_functions(u, [0])
-    M.add_sv_sens(u, [0], [dfdu])
-    M.apply_bcs(dfdu)
-    psi, _ = solver.ksm.solve(dfdu)
+    out["fd_direction"] = {"h": h, "seed": 34, "fd": fd_dir,
+                           "adjoint": adj_dir,
+                           "rel_err": abs(fd_dir - adj_dir) / abs(adj_dir),
+                           "s": time.perf_counter() - t0}
+    # oracle: addDVSens + addAdjointResProducts at the GPU state
+    psi = 2.0 * u
     gt = M.dv_vec()
+    M.eval_functions(u, [0])
     M.add_total_derivative(u, 0, psi, gt, 1.0, -1.0)
     o = oracle.Oracle(p, nthreads=os.cpu_count() or 1)
     uh, ph = u.cpu().numpy(), psi.cpu().numpy()
@@ -465,6 +433,9 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0,
     from tacs_gb300 import _lib, meshes, problem
     bp = meshes.batch_plates(count=count, nmax=nmax)
     M = problem.GpuModel(bp)
+    # the meshes do not move: assembly, functions and sensitivities from
+    # the per-geometry tables (one class per plate size here)
+    M.set_fixed_geometry(True)
     F = problem.batch_loads(M)
     out = {"workload": f"{count} clamped MITC4 plates N~logU[16,{nmax}] "
                        "(seed 4), 4 load cases each, KS(100) adjoint "
@@ -503,6 +474,8 @@ def batch_section(torch, count=48, nmax=256, m=100, nrestart=100, pc_kind=0,
                       "max_iters_adj": int(r["iters_adj"].max()),
                       "converged_fwd": int(r["flags_fwd"].sum()),
                       "converged_adj": int(r["flags_adj"].sum())}
+        if r.get("ksm") is not None:
+            out[label]["launch"] = r["ksm"].graph_info()
         if r.get("direct") is not None:
             dsol = r["direct"]
             st = dsol.stats()

@@ -132,7 +132,11 @@ int tg_assembler_set_traction(tg_assembler *a, int n, const int *elems_host,
    block is then summed from its contributions and written once.  The
    classes, coefficients and R(u = 0) are built at the first assembly after
    enabling and after every tg_assembler_set_nodes (synchronous, allocates);
-   t (tg_assembler_set_design_vars) and u may change freely. */
+   t (tg_assembler_set_design_vars) and u may change freely.  For shells
+   the build also keeps each class's strain operators, which the function
+   and sensitivity entry points (tg_eval_functions*, tg_add_sv_sens*,
+   tg_add_dv_sens, tg_add_adjoint_res_products, tg_add_total_derivative*)
+   then read instead of forming them per element. */
 int tg_assembler_set_fixed_geometry(tg_assembler *a, int enable);
 /* Geometry classes, coefficient-table bytes (0 before the first build)
    and the bytes of the per-block contribution lists. */
@@ -387,6 +391,15 @@ int tg_ksm_set_segments(tg_ksm *k, int nseg, const int *row_ptr);
 int tg_ksm_solve_multi(tg_ksm *k, int nrhs, const double *B, double *X,
                        int zero_guess, int *iters, int *flags,
                        double *resnorms, void *stream);
+/* No reference counterpart.  How the solves of the current layout (after a
+   first solve) are launched: cycle_graph 1 when each restart cycle is one
+   graph whose device-side WHILE node repeats the Arnoldi step (one host
+   synchronisation per cycle), 0 when the host launches the step graph and
+   checks every few steps; step_nodes / step_nodes_fp32 the graph nodes
+   (kernel launches and copies) of one Arnoldi step with the FP64 and (mixed
+   precision) FP32 operator.  Any pointer may be NULL. */
+int tg_ksm_get_graph_info(tg_ksm *k, int *cycle_graph, int *step_nodes,
+                          int *step_nodes_fp32);
 
 /* ------------------------------------------------- allocation-free entry */
 /* No counterpart in the reference.  Compliance and KS failure (the values of

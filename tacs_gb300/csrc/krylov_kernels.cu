@@ -356,6 +356,14 @@ __global__ void kr_solve_y(KrylovState st) {
   st.iters[s] += ni;
 }
 
+// Loop control of a restart cycle's WHILE node: continue while a system is
+// active and the cycle has room for another step (kr_arnoldi advances
+// *st.it every step, kr_cycle_init resets it: at most m steps per cycle).
+__global__ void kr_loop_control(KrylovState st, cudaGraphConditionalHandle h,
+                                int m) {
+  cudaGraphSetConditional(h, (*st.nactive > 0 && *st.it < m) ? 1u : 0u);
+}
+
 int grid_chunks(int nchunks) {
   int cap = sm_count() * 8;
   return nchunks < cap ? (nchunks > 0 ? nchunks : 1) : cap;
@@ -428,6 +436,11 @@ void launch_kr_cycle_init(const KrylovState &st, cudaStream_t s) {
 }
 void launch_kr_arnoldi(const KrylovState &st, cudaStream_t s) {
   kr_arnoldi<<<1, ((st.nsys + 31) / 32) * 32, 0, s>>>(st);
+}
+void launch_kr_loop_control(const KrylovState &st,
+                            cudaGraphConditionalHandle h, int m,
+                            cudaStream_t s) {
+  kr_loop_control<<<1, 1, 0, s>>>(st, h, m);
 }
 void launch_kr_solve_y(const KrylovState &st, cudaStream_t s) {
   kr_solve_y<<<(st.nsys + 127) / 128, 128, 0, s>>>(st);

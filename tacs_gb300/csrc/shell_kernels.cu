@@ -209,6 +209,21 @@ __device__ void shell_build_B(ShellSmem &S, const ElemParams &ep, int lane) {
   __syncwarp();
 }
 
+// B_q and detXd_q of element e: from the fixed-geometry class table when
+// the view carries one, else formed from the node coordinates
+__device__ __forceinline__ void shell_B(ShellSmem &S, const ElemParams &ep,
+                                        const MeshView &m, int e, int lane) {
+  if (m.geo_B) {
+    const double *src = m.geo_B + (size_t)m.geo_cls[e] * 868;
+    double *dst = &S.B[0][0][0];
+    for (int i = lane; i < 864; i += 32) dst[i] = src[i];
+    if (lane < 4) S.det[lane] = src[864 + lane];
+    __syncwarp();
+  } else {
+    shell_build_B(S, ep, lane);
+  }
+}
+
 // strains e_q = B_q v for the 4 points (36 outputs), v in shared memory
 __device__ __forceinline__ void shell_strains(ShellSmem &S, const double *v,
                                              double (*e)[9], int lane) {
@@ -249,7 +264,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   const int nw = gridDim.x * WARPS;
   for (int e = gw; e < m.nelem; e += nw) {
     load_element(S, m, e, vars, nullptr, lane);
-    shell_build_B(S, ep, lane);
+    shell_B(S, ep, m, e, lane);
     shell_strains(S, S.u, S.e, lane);
     if (lane < 4) {
       const int q = lane;
@@ -285,7 +300,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int e = cr.elem_list[idx];
     const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
     load_element(S, m, e, vars, nullptr, lane);
-    shell_build_B(S, ep, lane);
+    shell_B(S, ep, m, e, lane);
     shell_strains(S, S.u, S.e, lane);
     if (lane < 4) {
       const int q = lane;
@@ -333,7 +348,7 @@ __global__ void __launch_bounds__(WARPS * 32)
   for (int e = gw; e < m.nelem; e += nw) {
     const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
     load_element(S, m, e, vars, psi, lane);
-    shell_build_B(S, ep, lane);
+    shell_B(S, ep, m, e, lane);
     shell_strains(S, S.u, S.e, lane);
     if (psi) shell_strains(S, S.w, S.g, lane);
     if (lane < 4) {
@@ -446,7 +461,8 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
     shell_geo_build_kernel(ElemParams ep, MeshView m,
                            const int *__restrict__ reps, int nreps,
-                           double *__restrict__ table) {
+                           double *__restrict__ table,
+                           double *__restrict__ btab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ShellGeoSmem &G = reinterpret_cast<ShellGeoSmem *>(smem_raw)[threadIdx.x >> 5];
   ShellSmem &S = G.s;
@@ -457,6 +473,12 @@ __global__ void __launch_bounds__(WARPS * 32)
   for (int c = gw; c < nreps; c += nw) {
     load_element(S, m, reps[c], nullptr, nullptr, lane);
     shell_build_B(S, ep, lane);
+    if (btab) {  // the strain operators and detXd for the function kernels
+      double *bo = btab + (size_t)c * 868;
+      const double *bs = &S.B[0][0][0];
+      for (int i = lane; i < 864; i += 32) bo[i] = bs[i];
+      if (lane < 4) bo[864 + lane] = S.det[lane];
+    }
     for (int idx = lane; idx < 96; idx += 32) {
       const int q = idx / 24, j = idx - 24 * q;
       double ev[9];
@@ -557,12 +579,13 @@ void launch_shell_dv(const ElemParams &ep, const MeshView &m,
 
 void launch_shell_geo_build(const ElemParams &ep, const MeshView &m,
                             const int *reps, int nreps, double *table,
-                            cudaStream_t s) {
+                            double *btab, cudaStream_t s) {
   if (nreps <= 0) return;
   auto k = shell_geo_build_kernel<kWarps>;
   const size_t bytes = sizeof(ShellGeoSmem) * kWarps;
   prep(k, bytes);
-  k<<<grid_for(nreps, 2), kWarps * 32, bytes, s>>>(ep, m, reps, nreps, table);
+  k<<<grid_for(nreps, 2), kWarps * 32, bytes, s>>>(ep, m, reps, nreps, table,
+                                                    btab);
 }
 
 void launch_shell_xpt(const ElemParams &ep, const MeshView &m, ColorRange cr,

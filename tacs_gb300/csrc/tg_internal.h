@@ -29,6 +29,11 @@ struct MeshView {
   // is set, the KS sensitivities of element e use seg_ks[elem_seg[e]]
   const int *elem_seg;
   const struct KsStats *seg_ks;
+  // fixed-geometry mode (shells): per geometry class the strain operators
+  // B_q (4 x 9 x 24) and detXd_q (4), 868 doubles, and the class of each
+  // element; nullptr: the kernels form B from the node coordinates
+  const double *geo_B;
+  const int *geo_cls;
 };
 
 // One launch of an element kernel covers the elements of one colour:
@@ -74,9 +79,11 @@ struct GeoView {
   unsigned long long mask1, mask3;
 };
 // Builds the class table of the representative elements (one warp each).
+// (shells: also the classes' strain operators and detXd into btab, 868
+// doubles per class, when btab is not nullptr)
 void launch_shell_geo_build(const ElemParams &ep, const MeshView &m,
                             const int *reps, int nreps, double *table,
-                            cudaStream_t s);
+                            double *btab, cudaStream_t s);
 void launch_hex_geo_build(const ElemParams &ep, const MeshView &m,
                           const int *reps, int nreps, double *table,
                           cudaStream_t s);
@@ -314,6 +321,11 @@ void launch_kr_mask(double *x, const KrylovChunks &ch, const double *scale,
 void launch_kr_cycle_init(const KrylovState &st, cudaStream_t s);
 void launch_kr_arnoldi(const KrylovState &st, cudaStream_t s);
 void launch_kr_solve_y(const KrylovState &st, cudaStream_t s);
+// Sets the conditional handle of a graph's WHILE node to 1 while systems
+// are still iterating and fewer than m Arnoldi steps ran this cycle.
+void launch_kr_loop_control(const KrylovState &st,
+                            cudaGraphConditionalHandle h, int m,
+                            cudaStream_t s);
 
 // ------------------------------------------------ direct factorisation
 // multifrontal factorisation (direct_kernels.cu), T = double or float

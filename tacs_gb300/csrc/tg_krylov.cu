@@ -5,8 +5,12 @@
 // layout: the cycle start (true residual, per-system norms, first basis
 // vector), one Arnoldi step (operator, two classical Gram-Schmidt passes,
 // norm, Givens update on the device) replayed up to m times, and the cycle
-// end (back-substitution and x += M^{-1} V y).  The host reads one integer
-// (systems still iterating) every few steps to stop a cycle early.
+// end (back-substitution and x += M^{-1} V y).  They are also composed into
+// one graph per cycle whose WHILE node repeats the Arnoldi step on the
+// device until every system converged or m steps ran; the host then reads
+// one integer (systems still iterating) per cycle.  Without conditional
+// nodes the host launches the step graph and reads that integer every few
+// steps.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -115,7 +119,7 @@ void enqueue_end(tg_ksm *k, cudaStream_t s) {
 }
 
 template <typename F>
-int capture(cudaGraphExec_t *out, F &&body) {
+int capture(cudaGraphExec_t *out, F &&body, int *nodes = nullptr) {
   cudaStream_t cs;
   TG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
@@ -124,10 +128,81 @@ int capture(cudaGraphExec_t *out, F &&body) {
     body(cs);
     e = cudaStreamEndCapture(cs, &g);
   }
+  if (e == cudaSuccess && nodes) {
+    size_t n = 0;
+    e = cudaGraphGetNodes(g, nullptr, &n);
+    *nodes = (int)n;
+  }
   if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
   if (g) cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
   if (e != cudaSuccess) return cuda_check(e, "GMRES graph capture");
+  return 0;
+}
+
+// One restart cycle as one graph: start, loop control, a WHILE node whose
+// body is the Arnoldi step of the given operator mode followed by the loop
+// control, then the end of the cycle.  The steps run back to back on the
+// device with no host round trip; the loop runs at most m times.  Returns
+// 0 with *out null (not an error) where the driver or runtime does not
+// build conditional nodes.
+int capture_cycle(tg_ksm *k, int mode, cudaGraphExec_t *out) {
+  *out = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaStream_t cs = nullptr, cb = nullptr;
+  cudaGraphConditionalHandle h{};
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess)
+    e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cb, cudaStreamNonBlocking);
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    enqueue_start(k, cs);
+    launch_kr_loop_control(k->st, h, k->m, cs);
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    cudaGraphNode_t wn = nullptr;
+    cudaGraphNodeParams np = {};
+    e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+    if (e == cudaSuccess) {
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      e = cudaGraphAddNode(&wn, cg, deps, nullptr, nd, &np);
+    }
+    if (e == cudaSuccess)
+      e = cudaStreamUpdateCaptureDependencies(cs, &wn, nullptr, 1,
+                                              cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) {
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      e = cudaStreamBeginCaptureToGraph(cb, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        enqueue_iter(k, mode, cb);
+        launch_kr_loop_control(k->st, h, k->m, cb);
+        cudaGraph_t bo = nullptr;
+        e = cudaStreamEndCapture(cb, &bo);
+      }
+    }
+    if (e == cudaSuccess) enqueue_end(k, cs);
+    cudaGraph_t go = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &go);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (cb) cudaStreamDestroy(cb);
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    cudaGetLastError();  // the per-step graphs remain in use
+  }
   return 0;
 }
 
@@ -260,7 +335,10 @@ int ensure_layout(tg_ksm *k, int nrhs) {
     rc = capture(&k->g_end, [&](cudaStream_t cs) { enqueue_end(k, cs); });
   for (int mode = 0; mode < (k->mixed ? 2 : 1) && !rc; mode++)
     rc = capture(&k->g_iter[mode],
-                 [&](cudaStream_t cs) { enqueue_iter(k, mode, cs); });
+                 [&](cudaStream_t cs) { enqueue_iter(k, mode, cs); },
+                 &k->step_nodes[mode]);
+  for (int mode = 0; mode < (k->mixed ? 2 : 1) && !rc; mode++)
+    rc = capture_cycle(k, mode, &k->g_cycle[mode]);
   if (rc) k->free_layout();
   return rc;
 }
@@ -289,6 +367,15 @@ int run_cycles(tg_ksm *k, int mode, int stall, cudaStream_t s,
   const int ncyc = max_cycles > 0 ? std::min(max_cycles, k->nrestart + 1)
                                   : k->nrestart + 1;
   for (int cycle = 0; cycle < ncyc; cycle++) {
+    if (k->g_cycle[mode]) {
+      // the whole cycle on the device; one read of the active count
+      TG_CUDA(cudaGraphLaunch(k->g_cycle[mode], s));
+      TG_CUDA(cudaMemcpyAsync(k->h_pinned, st.nactive, sizeof(int),
+                              cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaStreamSynchronize(s));
+      if (hp[0] == 0) break;
+      continue;
+    }
     TG_CUDA(cudaGraphLaunch(k->g_start, s));
     TG_CUDA(cudaMemcpyAsync(k->h_pinned, st.nactive, sizeof(int),
                             cudaMemcpyDeviceToHost, s));
@@ -569,6 +656,15 @@ int solve_refined(tg_ksm *k, int mode, const double *B, double *X,
 }  // namespace
 
 extern "C" {
+
+int tg_ksm_get_graph_info(tg_ksm *k, int *cycle_graph, int *step_nodes,
+                          int *step_nodes_fp32) {
+  if (!k) return fail(TG_ERR_ARG, "tg_ksm_get_graph_info: NULL");
+  if (cycle_graph) *cycle_graph = k->g_cycle[0] ? 1 : 0;
+  if (step_nodes) *step_nodes = k->step_nodes[0];
+  if (step_nodes_fp32) *step_nodes_fp32 = k->step_nodes[1];
+  return 0;
+}
 
 int tg_ksm_create(tg_mat *A, tg_pc *pc, int m, int nrestart, int mixed,
                   tg_ksm **out) {

@@ -97,6 +97,7 @@ struct tg_assembler {
   int *d_geo_cptr = nullptr, *d_geo_contrib = nullptr, *d_geo_cls = nullptr;
   int *d_geo_node_bc = nullptr, *d_geo_kmax = nullptr, *d_geo_reps = nullptr;
   double *d_geo_table = nullptr, *d_geo_f0 = nullptr;
+  double *d_geo_B = nullptr;  // shells: B_q and detXd_q per class
   unsigned long long *d_geo_masks = nullptr;
 
   int nq() const { return ep.elem_type == TG_ELEM_MITC4 ? 4 : 8; }
@@ -118,6 +119,9 @@ struct tg_assembler {
     m.cols = d_cols;
     m.elem_seg = nullptr;
     m.seg_ks = nullptr;
+    const bool geo = geo_enabled && geo_table_valid && d_geo_B;
+    m.geo_B = geo ? d_geo_B : nullptr;
+    m.geo_cls = geo ? d_geo_cls : nullptr;
     return m;
   }
   // view whose KS sensitivities use the per-segment statistics
@@ -146,7 +150,7 @@ struct tg_assembler {
     dfree(d_seg_comp);
     dfree(d_geo_cptr); dfree(d_geo_contrib); dfree(d_geo_cls);
     dfree(d_geo_node_bc); dfree(d_geo_kmax); dfree(d_geo_reps);
-    dfree(d_geo_table); dfree(d_geo_f0); dfree(d_geo_masks);
+    dfree(d_geo_table); dfree(d_geo_f0); dfree(d_geo_masks); dfree(d_geo_B);
   }
 };
 
@@ -254,12 +258,19 @@ struct tg_ksm {
   // operator for mixed precision) and cycle end
   cudaGraphExec_t g_start = nullptr, g_iter[2] = {nullptr, nullptr},
                   g_end = nullptr;
+  // a whole restart cycle per operator mode: start, a device-side WHILE
+  // node over the Arnoldi step, end (null where conditional graph nodes are
+  // not available: the three graphs above are launched from the host then)
+  cudaGraphExec_t g_cycle[2] = {nullptr, nullptr};
+  int step_nodes[2] = {0, 0};  // graph nodes (launches) of one Arnoldi step
   void free_layout() {
     if (g_start) cudaGraphExecDestroy(g_start);
     if (g_end) cudaGraphExecDestroy(g_end);
     for (int i = 0; i < 2; i++) {
       if (g_iter[i]) cudaGraphExecDestroy(g_iter[i]);
+      if (g_cycle[i]) cudaGraphExecDestroy(g_cycle[i]);
       g_iter[i] = nullptr;
+      g_cycle[i] = nullptr;
     }
     g_start = g_end = nullptr;
     dfree(d_W); dfree(d_v); dfree(d_w); dfree(d_z); dfree(d_z2); dfree(d_B);

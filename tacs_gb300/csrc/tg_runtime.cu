@@ -310,9 +310,14 @@ static int geo_prepare(tg_assembler *a, cudaStream_t s) {
       a->geo_table_doubles = (size_t)ncls * per;
     }
     MeshView m = a->view();
-    if (shell)
-      launch_shell_geo_build(a->ep, m, a->d_geo_reps, ncls, a->d_geo_table, s);
-    else
+    m.geo_B = nullptr;  // the build forms B itself
+    if (shell) {
+      dfree(a->d_geo_B);
+      if ((rc = dalloc(&a->d_geo_B, (size_t)ncls * 868))) return rc;
+      launch_shell_geo_build(a->ep, m, a->d_geo_reps, ncls, a->d_geo_table,
+                             a->d_geo_B, s);
+    }
+    if (!shell)
       launch_hex_geo_build(a->ep, m, a->d_geo_reps, ncls, a->d_geo_table, s);
     TG_CUDA(cudaMemsetAsync(a->d_geo_masks, 0, 2 * sizeof(unsigned long long),
                             s));
@@ -532,6 +537,9 @@ int tg_eval_functions(tg_assembler *a, const double *vars, int nfuncs,
   if (rc) return rc;
   if (nfuncs < 0 || (nfuncs > 0 && (!funcs || !vals)) || !vars)
     return fail(TG_ERR_ARG, "tg_eval_functions: bad arguments");
+  // fixed-geometry mode: the class table (and the shells' strain operators)
+  // serve the function and sensitivity kernels too
+  if (a->geo_enabled && (rc = geo_prepare(a, S(s)))) return rc;
   launch_points(a, vars, S(s));
   const size_t nq = (size_t)a->nq() * a->nelem;
   // d_scalars: [0] compliance, [1] KS max, [2] KS sum
@@ -758,6 +766,7 @@ int tg_eval_functions_segments(tg_assembler *a, const double *vars, int func,
     return fail(TG_ERR_ARG, "tg_eval_functions_segments: bad arguments");
   if (func != TG_FUNC_COMPLIANCE && func != TG_FUNC_KS_FAILURE)
     return fail(TG_ERR_ARG, "tg_eval_functions_segments: unknown function");
+  if (a->geo_enabled && (rc = geo_prepare(a, S(s)))) return rc;
   launch_points(a, vars, S(s));
   launch_segment_functions(a->d_elem_fail, a->d_elem_wdet, a->d_elem_sed,
                            a->nq(), a->d_seg_elem_ptr, a->nseg, ks_weight,

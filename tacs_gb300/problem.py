@@ -233,6 +233,16 @@ class Ksm:
         self.iters, self.resnorm = it.value, rn.value
         return x, flag
 
+    def graph_info(self):
+        """tg_ksm_get_graph_info: whether a restart cycle runs as one graph
+        (device-side loop over the Arnoldi step) and the launches of one
+        step."""
+        cyc, n64, n32 = C.c_int(0), C.c_int(0), C.c_int(0)
+        check(_lib.lib().tg_ksm_get_graph_info(self.handle, C.byref(cyc),
+                                                C.byref(n64), C.byref(n32)))
+        return {"cycle_graph": bool(cyc.value), "step_launches": n64.value,
+                "step_launches_fp32": n32.value}
+
     def set_segments(self, row_ptr):
         """Independent row ranges (block-diagonal matrix): one system each."""
         rp = np.ascontiguousarray(row_ptr, np.int32)
@@ -585,6 +595,7 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
             z = np.zeros(nsys, np.int32)
             return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1
     else:
+        dsol = None
         prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64
         pc = Pc(mat, pc_kind, prec, lev_fill=lev_fill)
         pc.factor()
@@ -610,7 +621,8 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
                                             1.0, -1.0)
     return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,
                 iters_adj=it_a, flags_adj=fl_a, psi=Psi, resnorm_fwd=rn_f,
-                resnorm_adj=rn_a, direct=dsol if direct else None, mat=mat)
+                resnorm_adj=rn_a, direct=dsol if direct else None, mat=mat,
+                ksm=None if direct else ksm)
 
 
 def batch_loads(model):

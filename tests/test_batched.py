@@ -125,3 +125,33 @@ def test_batched_meshes_match_independent_solves(gpu, pc_kind, mixed, tmin,
             Mg.add_total_derivative(u, _lib.FUNC_KS_FAILURE, psi, gr, 1.0,
                                     -1.0)
             assert rel(_h(r["grads"][lc, eptr[g]:eptr[g + 1]]), _h(gr)) < TOL
+
+
+@pytest.mark.gpu
+def test_restart_cycle_runs_as_one_graph():
+    """Each GMRES restart cycle is one graph whose WHILE node repeats the
+    Arnoldi step on the device (tg_ksm_get_graph_info), in FP64 and mixed
+    precision, and the solves it runs meet their tolerance."""
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from tacs_gb300 import _lib, meshes, problem
+    prob = meshes.clamped_plate(16)
+    M = problem.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    b = -r0
+    for mixed in (False, True):
+        pc = problem.Pc(mat, _lib.PC_ILU0,
+                        _lib.PREC_FP32 if mixed else _lib.PREC_FP64)
+        pc.factor()
+        ksm = problem.Ksm(mat, pc, 30, 20, mixed)
+        ksm.set_tolerances(1e-10)
+        x, flag = ksm.solve(b)
+        info = ksm.graph_info()
+        assert flag == 1
+        assert info["cycle_graph"] and info["step_launches"] > 0
+        assert (info["step_launches_fp32"] > 0) == mixed
+        r = mat.mult(x) - b
+        assert float(r.norm() / b.norm()) < 1e-9
+

@@ -11,7 +11,11 @@ element-level tolerance 1e-12 (norm-wise, every Jacobian entry):
 * the cache follows the design: new thicknesses after the build;
 * set_nodes invalidates the cache: after moving nodes the results are
   those of the new geometry (oracle), not the old;
-* a uniform structured plate has one geometry class.
+* a uniform structured plate has one geometry class;
+* the function and sensitivity kernels (compliance, KS, addSVSens,
+  addDVSens, addAdjointResProducts) with the cached strain operators
+  against the reference's outputs, and a batched adjoint of several meshes
+  against the same computation without the cache.
 """
 import numpy as np
 import pytest
@@ -136,3 +140,43 @@ def test_fixed_geometry_follows_design_and_nodes(gpu):
     assert rel(_h(res), r_ref3) < ELEM_TOL
     assert rel(vals3, vals) > 1e-6  # the geometry did change
     assert M.fixed_geometry_info()["classes"] > 1
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fixed_geometry_functions_and_sensitivities(gpu, name):
+    prob, ref = load_case(name)
+    if "u_test" not in prob:
+        pytest.skip("no unit state in this case")
+    M = gpu.GpuModel(prob)
+    M.set_fixed_geometry(True)
+    u = M.vec(prob["u_test"])
+    assert rel(M.eval_functions(u), ref["funcs_test"]) < ELEM_TOL
+    dc, dk = M.vec(), M.vec()
+    M.add_sv_sens(u, [0, 1], [dc, dk])
+    assert rel(_h(dc), ref["dfdu_test_comp"]) < ELEM_TOL
+    assert rel(_h(dk), ref["dfdu_test_ks"]) < ELEM_TOL
+    xc, xk = M.dv_vec(), M.dv_vec()
+    M.add_dv_sens(u, [0, 1], [xc, xk])
+    assert rel(_h(xc), ref["dfdx_test_comp"]) < ELEM_TOL
+    assert rel(_h(xk), ref["dfdx_test_ks"]) < 1e-11
+    xa = M.dv_vec()
+    M.add_adjoint_res_products(u, [M.vec(prob["psi_test"])], [xa])
+    assert rel(_h(xa), ref["adjres_test"]) < ELEM_TOL
+
+
+def test_fixed_geometry_batched_adjoint(gpu):
+    from tacs_gb300 import _lib, meshes
+    bp = meshes.batch_plates(count=4, nmax=24, seed=8)
+    out = []
+    for fixed in (False, True):
+        M = gpu.GpuModel(bp)
+        if fixed:
+            M.set_fixed_geometry(True)
+        F = gpu.batch_loads(M)
+        r = gpu.batched_adjoint(M, F, m=60, nrestart=40, rtol=1e-12,
+                                func=_lib.FUNC_KS_FAILURE)
+        assert r["flags_fwd"].all() and r["flags_adj"].all()
+        out.append((r["funcs"], _h(r["grads"])))
+    assert rel(out[1][0], out[0][0]) < 1e-9
+    assert rel(out[1][1], out[0][1]) < 1e-7
+
