@@ -21,12 +21,15 @@ int grid_1d(size_t n) {
 
 template <class T>
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
-                                  int count, const double *A,
-                                  cudaStream_t s) {
+                                  int count, const double *A, int nchild,
+                                  int ychunks, cudaStream_t s) {
   if (count <= 0) return;
   direct_zero_kernel<T><<<count, 256, 0, s>>>(v, sn, count);
   direct_assemble_kernel<T><<<count, 256, 0, s>>>(v, sn, count, A);
-  direct_extend_add_kernel<T><<<count, 256, 0, s>>>(v, sn, count);
+  if (ychunks > 0)
+    for (int k = 0; k < nchild; k++)
+      direct_extend_add_kernel<T>
+          <<<dim3(count, ychunks), 256, 0, s>>>(v, sn, count, k);
 }
 
 template <class T>
@@ -116,7 +119,8 @@ cudaError_t direct_set_smem(int max_front) {
 #define TG_DIRECT_INSTANTIATE(T)                                            \
   template void launch_direct_level_assemble<T>(const DirectView &,        \
                                                 const int *, int,          \
-                                                const double *, cudaStream_t); \
+                                                const double *, int, int,  \
+                                                cudaStream_t);             \
   template void launch_direct_factor_small<T>(const DirectView &,          \
                                               const int *, int, int *,     \
                                               cudaStream_t);               \

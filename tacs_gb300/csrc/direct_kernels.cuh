@@ -119,30 +119,39 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// the children's update matrices into each parent front (one CTA per
-// parent, children one after another)
+// The children's update matrices into their parent fronts.  One launch
+// per child position kchild (the kchild-th child of every parent of the
+// level, children in increasing order across launches, so every parent
+// entry receives its children's terms in one fixed order); within a launch
+// a parent's child is split over CTAs by kExtendRows rows of its update
+// matrix (blockIdx.y), one warp per row and the lanes along it.  A child
+// maps its entries one-to-one into its parent, so no two threads of a
+// launch write one entry.
+constexpr int kExtendRows = kDirectExtendRows;
 template <class T>
 __global__ void __launch_bounds__(256)
     direct_extend_add_kernel(DirectView v, const int *__restrict__ sn,
-                             int count) {
+                             int count, int kchild) {
   if ((int)blockIdx.x >= count) return;
   const int s = sn[blockIdx.x];
+  if (kchild >= v.ch_ptr[s + 1] - v.ch_ptr[s]) return;
+  const int c = v.ch_list[v.ch_ptr[s] + kchild];
   const Front<T> f = front_of<T>(v, s);
+  const Front<T> fc = front_of<T>(v, c);
+  const int um = fc.M - fc.C;
+  const int r0 = (int)blockIdx.y * kExtendRows;
+  if (r0 >= um) return;
+  const int r1 = r0 + kExtendRows < um ? r0 + kExtendRows : um;
   const int bs = v.bs;
-  for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
-    const int c = v.ch_list[k];
-    const Front<T> fc = front_of<T>(v, c);
-    const int um = fc.M - fc.C;
-    const int *rel = v.ea_rel + v.ea_ptr[c];
-    const size_t total = (size_t)um * um;
-    for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const int ur = (int)(t / um), uc = (int)(t % um);
-      if (uc > ur) continue;
-      const int i = rel[ur / bs] * bs + ur % bs;
-      const int j = rel[uc / bs] * bs + uc % bs;
-      f.at(i, j) += fc.up[t];
-    }
-    __syncthreads();
+  const int *rel = v.ea_rel + v.ea_ptr[c];
+  const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
+  const int nw = blockDim.x < 32 ? 1 : (int)blockDim.x / 32;
+  const int w = (int)threadIdx.x / 32, lane = (int)threadIdx.x % 32;
+  for (int ur = r0 + w; ur < r1; ur += nw) {
+    const int i = rel[ur / bs] * bs + ur % bs;
+    const T *src = fc.up + (size_t)ur * um;
+    for (int uc = lane; uc <= ur; uc += ls)
+      f.at(i, rel[uc / bs] * bs + uc % bs) += src[uc];
   }
 }
 

@@ -14,6 +14,8 @@ constexpr int kDirectTrsmRows = 256;
 // column block of the triangular solves, and the shared memory of its
 // staged diagonal block (rows padded to kDirectSolveBlock + 1 entries)
 constexpr int kDirectSolveBlock = 32;
+// rows of a child's update matrix added into its parent by one CTA
+constexpr int kDirectExtendRows = 32;
 constexpr int kDirectSolveDiag = kDirectSolveBlock * (kDirectSolveBlock + 1);
 
 struct DirectView {

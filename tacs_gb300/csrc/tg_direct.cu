@@ -15,11 +15,12 @@
 #include "tg_objects.h"
 
 // fronts of at most this many scalar rows are factored by one CTA each,
-// all fronts of a level in one launch; larger ones by 32-column panels.
-// On a 512 x 512 plate 25 k of the 36 k fronts have at most 256 rows and
-// 9.9 k have 257 - 512 (12 % of the flops): on the panel path those would
-// cost ~14 serialised launches each.
-static constexpr int kSmallFront = 512;
+// all fronts of a level in one launch; larger ones by 32-column panels,
+// batched over the level's large fronts.
+#ifndef TG_DIRECT_SMALL_FRONT
+#define TG_DIRECT_SMALL_FRONT 512
+#endif
+static constexpr int kSmallFront = TG_DIRECT_SMALL_FRONT;
 // blocks of the max-|x| reductions of the refinement's stopping test
 static constexpr int kRedParts = 256;
 
@@ -44,6 +45,9 @@ struct tg_direct {
   // per level: its small fronts (one launch, d_small) and the panel steps
   // of its large ones (steps of level L: step_ptr_h[L] .. [L + 1])
   std::vector<int> small_ptr_h, step_ptr_h;
+  // per level: the most children of one of its supernodes and the row
+  // blocks of its largest child update matrix (the extend-add launches)
+  std::vector<int> ext_nch_h, ext_y_h;
   tg::direct::PanelSteps steps;
   int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr,
       *d_step_rprefix = nullptr;
@@ -177,6 +181,18 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   }
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
                                      tg::kDirectTile, tg::kDirectTrsmRows);
+  for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+    int nch = 0, um = 0;
+    for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+      const int sn = an.level_sn[t];
+      nch = std::max(nch, ch_ptr[sn + 1] - ch_ptr[sn]);
+      for (int k = ch_ptr[sn]; k < ch_ptr[sn + 1]; k++)
+        um = std::max(um, d->front_m_h[ch_list[k]] - d->front_c_h[ch_list[k]]);
+    }
+    d->ext_nch_h.push_back(nch);
+    d->ext_y_h.push_back((um + tg::kDirectExtendRows - 1) /
+                         tg::kDirectExtendRows);
+  }
   {
     const int nlev = (int)an.level_ptr.size() - 1;
     d->step_ptr_h.assign(nlev + 1, 0);
@@ -271,7 +287,8 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
   for (size_t L = 0; L + 1 < d->level_ptr_h.size(); L++) {
     const int b = d->level_ptr_h[L], e = d->level_ptr_h[L + 1];
     tg::launch_direct_level_assemble<T>(v, d->d_level_sn + b, e - b,
-                                        d->A->d_vals, s);
+                                        d->A->d_vals, d->ext_nch_h[L],
+                                        d->ext_y_h[L], s);
     // the level's small fronts in one launch, its large ones by panels
     const int sb = d->small_ptr_h[L], se = d->small_ptr_h[L + 1];
     tg::launch_direct_factor_small<T>(v, d->d_small + sb, se - sb, d->d_fail,

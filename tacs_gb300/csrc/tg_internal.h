@@ -330,8 +330,11 @@ void launch_kr_loop_control(const KrylovState &st,
 // ------------------------------------------------ direct factorisation
 // multifrontal factorisation (direct_kernels.cu), T = double or float
 template <class T>
+// (zero, matrix scatter, then nchild extend-add launches of ychunks row
+// blocks: the largest child count and child update size of the level)
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
-                                  int count, const double *A, cudaStream_t s);
+                                  int count, const double *A, int nchild,
+                                  int ychunks, cudaStream_t s);
 template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s);

@@ -153,7 +153,17 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     const int cnt = le - lb;
     launch(direct_zero_kernel<T>, cnt, 1, 0, v, lv, cnt);
     launch(direct_assemble_kernel<T>, cnt, 1, 0, v, lv, cnt, vals);
-    launch(direct_extend_add_kernel<T>, cnt, 1, 0, v, lv, cnt);
+    int nch = 0, um = 0;  // the extend-add launches of tg_direct.cu
+    for (int t = 0; t < cnt; t++) {
+      const int sn = lv[t];
+      nch = std::max(nch, ch_ptr[sn + 1] - ch_ptr[sn]);
+      for (int k = ch_ptr[sn]; k < ch_ptr[sn + 1]; k++)
+        um = std::max(um, fm[ch_list[k]] - fc[ch_list[k]]);
+    }
+    const int ych = (um + tg::kDirectExtendRows - 1) / tg::kDirectExtendRows;
+    if (ych > 0)
+      for (int k = 0; k < nch; k++)
+        launch(direct_extend_add_kernel<T>, cnt, ych, 0, v, lv, cnt, k);
     const int sb = small_ptr[L], se = small_ptr[L + 1];
     if (se > sb)
       launch(direct_factor_small_kernel<T>, se - sb, 1, 0, v,
