@@ -71,6 +71,74 @@ void launch_direct_backward(const DirectView &v, const int *sn, int count,
           v, sn, count, y, x);
 }
 
+// Large fronts: kDirectSolveCluster CTAs per front in one thread-block
+// cluster; shared memory for the rank owning the most rows.
+static size_t cluster_smem(int max_front, size_t elem) {
+  const int nbk = (max_front + 31) / 32;
+  const int mine = (nbk + kDirectSolveCluster - 1) / kDirectSolveCluster;
+  return elem * ((size_t)mine * 32 + kDirectSolveDiag);
+}
+
+template <class K, class... Args>
+static cudaError_t cluster_launch_dk(K kernel, int count, size_t smem,
+                                     cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(count * kDirectSolveCluster));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kDirectSolveCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+template <class T>
+void launch_direct_forward_cluster(const DirectView &v, const int *sn,
+                                   int count, int max_front, T *y, T *contrib,
+                                   cudaStream_t s) {
+  if (count <= 0) return;
+  cluster_launch_dk(direct_forward_cluster_kernel<T>, count,
+                    cluster_smem(max_front, sizeof(T)), s, v, sn, count, y,
+                    contrib);
+}
+
+template <class T>
+void launch_direct_backward_cluster(const DirectView &v, const int *sn,
+                                    int count, int max_front, const T *y,
+                                    T *x, cudaStream_t s) {
+  if (count <= 0) return;
+  cluster_launch_dk(direct_backward_cluster_kernel<T>, count,
+                    cluster_smem(max_front, sizeof(T)), s, v, sn, count, y, x);
+}
+
+// whether the device schedules the solve clusters (at least one active)
+bool direct_cluster_solve_ok() {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kDirectSolveCluster);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = cluster_smem(1 << 15, sizeof(double));
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kDirectSolveCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(
+      &n, (void *)direct_forward_cluster_kernel<double>, &cfg);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
 template <class T>
 void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
                            T *out, cudaStream_t s) {
@@ -133,6 +201,11 @@ cudaError_t direct_set_smem(int max_front) {
   template void launch_direct_backward<T>(const DirectView &, const int *, \
                                           int, int, const T *, T *,        \
                                           cudaStream_t);                   \
+  template void launch_direct_forward_cluster<T>(                          \
+      const DirectView &, const int *, int, int, T *, T *, cudaStream_t);  \
+  template void launch_direct_backward_cluster<T>(                         \
+      const DirectView &, const int *, int, int, const T *, T *,           \
+      cudaStream_t);                                                        \
   template void launch_direct_bc_mask<T>(int, int, const int *, const T *, \
                                          T *, cudaStream_t);               \
   template void launch_direct_rhs<T>(int, int, const int *, const T *,     \

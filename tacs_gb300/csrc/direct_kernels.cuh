@@ -22,6 +22,10 @@
 // CTAs write one entry.
 #pragma once
 
+#ifndef DK_EMULATE
+#include <cooperative_groups.h>
+#endif
+
 #include "direct_view.h"
 
 #ifdef DK_EMULATE
@@ -482,6 +486,171 @@ __global__ void __launch_bounds__(256)
   for (int t = threadIdx.x; t < f.C; t += blockDim.x)
     x[(size_t)rows[t / bs] * bs + t % bs] = z[t];
 }
+
+#ifndef DK_EMULATE
+// Large fronts: one thread-block cluster of kDirectSolveCluster CTAs per
+// front, so that the front's triangular solves use that many SMs' FP64
+// pipes (one CTA per front leaves the top of the tree, a handful of fronts
+// with thousands of rows, on one SM each).  The front's rows are dealt out
+// in 32-row blocks: block b belongs to rank b % nr and sits in that CTA's
+// shared memory at slot (b / nr) * 32.  For column block kb its owner
+// solves the staged diagonal block and publishes the 32 values; after one
+// hardware cluster barrier every rank reads them through distributed
+// shared memory and updates its own rows (forward: rows below; backward:
+// columns before).  The control flow is the same in every CTA of a
+// cluster (each cluster exits together, and every barrier is reached by
+// all of its CTAs); a final barrier keeps each CTA's shared memory alive
+// until the others are done reading it.  Dynamic shared memory: the owned
+// rows (rounded up to whole blocks), then the diagonal block.
+template <class T>
+struct ClusterRows {
+  int nr, rank;
+  __device__ __forceinline__ bool owns(int r) const {
+    return ((r >> 5) % nr) == rank;
+  }
+  __device__ __forceinline__ int slot(int r) const {
+    return ((r >> 5) / nr) * 32 + (r & 31);
+  }
+  // the i-th row owned by this rank, i < count(M)
+  __device__ __forceinline__ int row(int i) const {
+    return ((i >> 5) * nr + rank) * 32 + (i & 31);
+  }
+  __device__ __forceinline__ int count(int M) const {
+    const int nbk = (M + 31) >> 5;
+    const int mine = nbk > rank ? (nbk - rank + nr - 1) / nr : 0;
+    return mine * 32;
+  }
+};
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
+                                  int count, T *y, T *contrib) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const ClusterRows<T> cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  const int fi = (int)blockIdx.x / cr.nr;  // the same in the whole cluster
+  if (fi >= count) return;
+  DK_DYN_SMEM(T, z);
+  __shared__ T zb[32], zk[32];
+  const int s = sn[fi];
+  const Front<T> f = front_of<T>(v, s);
+  const int bs = v.bs;
+  const int *rows = v.sn_rows + v.sn_rowptr[s];
+  const int nown = cr.count(f.M);
+  T *D = z + nown;
+  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+    const int r = cr.row(t);
+    z[t] = (r < f.C) ? y[(size_t)rows[r / bs] * bs + r % bs] : T(0);
+  }
+  __syncthreads();
+  for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
+    const int c = v.ch_list[k];
+    const Front<T> fc = front_of<T>(v, c);
+    const int um = fc.M - fc.C;
+    const int *rel = v.ea_rel + v.ea_ptr[c];
+    const T *w = contrib + v.v_off[c];
+    for (int t = threadIdx.x; t < um; t += blockDim.x) {
+      const int r = rel[t / bs] * bs + t % bs;
+      if (cr.owns(r)) z[cr.slot(r)] += w[t];
+    }
+    __syncthreads();
+  }
+  for (int kb = 0; kb < f.C; kb += 32) {
+    const int nb = f.C - kb < 32 ? f.C - kb : 32;
+    const int owner = (kb >> 5) % cr.nr;
+    if (owner == cr.rank) {
+      dk_stage_block(f, kb, nb, D);
+      __syncthreads();
+      dk_block_solve<T, false>(D, nb, z + cr.slot(kb));
+      __syncthreads();
+      for (int t = threadIdx.x; t < nb; t += blockDim.x)
+        zb[t] = z[cr.slot(kb) + t];
+    }
+    cl.sync();
+    const T *src = cl.map_shared_rank(zb, owner);
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) zk[t] = src[t];
+    __syncthreads();
+    // own rows below the block: z_r -= L(r, kb .. kb+nb) zk
+    for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+      const int r = cr.row(t);
+      if (r < kb + nb || r >= f.M) continue;
+      const T *Lr = f.lp + (size_t)r * f.C + kb;
+      T acc = 0;
+      for (int c = 0; c < nb; c++) acc += Lr[c] * zk[c];
+      z[t] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+    const int r = cr.row(t);
+    if (r < f.C) y[(size_t)rows[r / bs] * bs + r % bs] = z[t];
+    else if (r < f.M && v.sn_parent[s] >= 0)
+      contrib[v.v_off[s] + (r - f.C)] = z[t];
+  }
+  cl.sync();  // the other ranks may still read zb
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    direct_backward_cluster_kernel(DirectView v, const int *__restrict__ sn,
+                                   int count, const T *y, T *x) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const ClusterRows<T> cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  const int fi = (int)blockIdx.x / cr.nr;
+  if (fi >= count) return;
+  DK_DYN_SMEM(T, z);
+  __shared__ T zb[32], zk[32];
+  const int s = sn[fi];
+  const Front<T> f = front_of<T>(v, s);
+  const int bs = v.bs;
+  const int *rows = v.sn_rows + v.sn_rowptr[s];
+  const int nown = cr.count(f.M);
+  T *D = z + nown;
+  // own rows of the triangle: y1 - L21^T x2 (x2 final, from the ancestors)
+  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+    const int j = cr.row(t);
+    if (j >= f.C) continue;
+    T acc = 0;
+    for (int i = f.C; i < f.M; i++)
+      acc += f.lp[(size_t)i * f.C + j] * x[(size_t)rows[i / bs] * bs + i % bs];
+    z[t] = y[(size_t)rows[j / bs] * bs + j % bs] - acc;
+  }
+  __syncthreads();
+  for (int kb = ((f.C - 1) >> 5) << 5; kb >= 0; kb -= 32) {
+    const int nb = f.C - kb < 32 ? f.C - kb : 32;
+    const int owner = (kb >> 5) % cr.nr;
+    if (owner == cr.rank) {
+      dk_stage_block(f, kb, nb, D);
+      __syncthreads();
+      dk_block_solve<T, true>(D, nb, z + cr.slot(kb));
+      __syncthreads();
+      for (int t = threadIdx.x; t < nb; t += blockDim.x)
+        zb[t] = z[cr.slot(kb) + t];
+    }
+    cl.sync();
+    const T *src = cl.map_shared_rank(zb, owner);
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) zk[t] = src[t];
+    __syncthreads();
+    // own columns before the block: z_j -= sum_k L(kb + k, j) zk_k
+    for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+      const int j = cr.row(t);
+      if (j >= kb) continue;
+      T acc = 0;
+      for (int k = 0; k < nb; k++)
+        acc += f.lp[(size_t)(kb + k) * f.C + j] * zk[k];
+      z[t] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+    const int r = cr.row(t);
+    if (r < f.C) x[(size_t)rows[r / bs] * bs + r % bs] = z[t];
+  }
+  cl.sync();
+}
+#endif  // DK_EMULATE
 
 // b' = b - K P b + P b (P keeps the boundary dofs) is formed as
 // tmp = P b, then K tmp by the mat-vec, then this kernel; and the

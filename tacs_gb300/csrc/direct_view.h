@@ -16,6 +16,10 @@ constexpr int kDirectTrsmRows = 256;
 constexpr int kDirectSolveBlock = 32;
 // rows of a child's update matrix added into its parent by one CTA
 constexpr int kDirectExtendRows = 32;
+// CTAs of the thread-block cluster that solves one large front, and the
+// front rows above which a front is solved that way
+constexpr int kDirectSolveCluster = 8;
+constexpr int kDirectClusterFront = 768;
 constexpr int kDirectSolveDiag = kDirectSolveBlock * (kDirectSolveBlock + 1);
 
 struct DirectView {

@@ -18,7 +18,7 @@
 // all fronts of a level in one launch; larger ones by 32-column panels,
 // batched over the level's large fronts.
 #ifndef TG_DIRECT_SMALL_FRONT
-#define TG_DIRECT_SMALL_FRONT 512
+#define TG_DIRECT_SMALL_FRONT 64
 #endif
 static constexpr int kSmallFront = TG_DIRECT_SMALL_FRONT;
 // blocks of the max-|x| reductions of the refinement's stopping test
@@ -48,6 +48,12 @@ struct tg_direct {
   // per level: the most children of one of its supernodes and the row
   // blocks of its largest child update matrix (the extend-add launches)
   std::vector<int> ext_nch_h, ext_y_h;
+  // the solves' fronts per level: one CTA each (d_solve_sn, solve_ptr_h)
+  // and, above kDirectClusterFront rows, one thread-block cluster each
+  // (d_csolve_sn, csolve_ptr_h)
+  std::vector<int> solve_ptr_h, csolve_ptr_h;
+  int *d_solve_sn = nullptr, *d_csolve_sn = nullptr;
+  std::vector<int> solve_sn_h, csolve_sn_h;
   tg::direct::PanelSteps steps;
   int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr,
       *d_step_rprefix = nullptr;
@@ -106,6 +112,7 @@ struct tg_direct {
     dfree(d_sn_rows); dfree(d_sn_parent); dfree(d_ea_ptr); dfree(d_ea_rel);
     dfree(d_asm_ptr); dfree(d_asm_blk); dfree(d_asm_row); dfree(d_asm_col);
     dfree(d_ch_ptr); dfree(d_ch_list); dfree(d_level_sn); dfree(d_l_off);
+    dfree(d_solve_sn); dfree(d_csolve_sn);
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
     dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
@@ -181,6 +188,25 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   }
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
                                      tg::kDirectTile, tg::kDirectTrsmRows);
+  {
+    const bool clusters = tg::direct_cluster_solve_ok();
+    std::vector<int> a, b;
+    d->solve_ptr_h.assign(1, 0);
+    d->csolve_ptr_h.assign(1, 0);
+    for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+      for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+        const int sn = an.level_sn[t];
+        if (clusters && d->front_m_h[sn] > tg::kDirectClusterFront)
+          b.push_back(sn);
+        else
+          a.push_back(sn);
+      }
+      d->solve_ptr_h.push_back((int)a.size());
+      d->csolve_ptr_h.push_back((int)b.size());
+    }
+    d->solve_sn_h = a;
+    d->csolve_sn_h = b;
+  }
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     int nch = 0, um = 0;
     for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
@@ -220,6 +246,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_ch_ptr, ch_ptr);
   if (!rc) rc = upload(&d->d_ch_list, ch_list);
   if (!rc) rc = upload(&d->d_level_sn, an.level_sn);
+  if (!rc) rc = upload(&d->d_solve_sn, d->solve_sn_h);
+  if (!rc) rc = upload(&d->d_csolve_sn, d->csolve_sn_h);
   if (!rc) rc = upload(&d->d_small, small_h);
   if (!rc) rc = upload(&d->d_step_fronts, d->steps.fronts);
   if (!rc) rc = upload(&d->d_step_tprefix, d->steps.tprefix);
@@ -317,14 +345,20 @@ static void solve_levels(tg_direct *d, const T *b, T *x, const T *a, T *pb,
   tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, b, kpb, pb, ypos, s);
   const int nl = (int)d->level_ptr_h.size() - 1;
   for (int L = 0; L < nl; L++) {
-    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
-    tg::launch_direct_forward<T>(v, d->d_level_sn + lb, le - lb,
+    const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
+    tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
                                  d->max_front, ypos, contrib, s);
+    const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+    tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
+                                         d->max_front, ypos, contrib, s);
   }
   for (int L = nl - 1; L >= 0; L--) {
-    const int lb = d->level_ptr_h[L], le = d->level_ptr_h[L + 1];
-    tg::launch_direct_backward<T>(v, d->d_level_sn + lb, le - lb,
+    const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
+    tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
                                   d->max_front, ypos, xpos, s);
+    const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+    tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
+                                          d->max_front, ypos, xpos, s);
   }
   tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, x, s);
 }

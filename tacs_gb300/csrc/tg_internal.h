@@ -353,6 +353,17 @@ void launch_direct_forward(const DirectView &v, const int *sn, int count,
 template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
                             int max_front, const T *y, T *x, cudaStream_t s);
+// the same solves for large fronts, one thread-block cluster of
+// kDirectSolveCluster CTAs per front
+template <class T>
+void launch_direct_forward_cluster(const DirectView &v, const int *sn,
+                                   int count, int max_front, T *y, T *contrib,
+                                   cudaStream_t s);
+template <class T>
+void launch_direct_backward_cluster(const DirectView &v, const int *sn,
+                                    int count, int max_front, const T *y,
+                                    T *x, cudaStream_t s);
+bool direct_cluster_solve_ok();
 template <class T>
 void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
                            T *out, cudaStream_t s);

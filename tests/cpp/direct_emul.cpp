@@ -184,7 +184,10 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   }
   if (failflag) return failflag;
 
-  // solve: the sequence of tg_direct_solve
+  // solve: the sequence of tg_direct_solve (on the GPU fronts of more than
+  // kDirectClusterFront rows take the cluster kernels, one thread-block
+  // cluster per front, checked by the GPU tests; here every front takes the
+  // one-CTA kernels, which form each row's sums in the same order)
   launch(direct_bc_mask_kernel<T>, 1, 1, 0, n, bs,
          (const int *)bcmask.data(), b, pb.data());
   for (int i = 0; i < n; i++)  // the BCSR mat-vec, in T
