@@ -211,6 +211,12 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
                      tg_direct **out);
 int tg_direct_factor(tg_direct *d, void *stream);
 int tg_direct_solve(tg_direct *d, const double *b, double *x, void *stream);
+/* nrhs right-hand sides of n x bs entries back to back (no reference
+   counterpart: the batched load cases of one matrix); the solve passes over
+   the factor once for up to four of them.  Each right-hand side's result
+   is bitwise the one tg_direct_solve gives it. */
+int tg_direct_solve_multi(tg_direct *d, int nrhs, const double *b, double *x,
+                          void *stream);
 int tg_direct_solve_f32(tg_direct *d, const float *b, float *x,
                         void *stream);
 /* Mixed precision: x = A^-1 b in FP64 from an FP32 factorisation by
@@ -236,6 +242,14 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
 int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 int max_steps, double tol, int *steps,
                                 double *eta, void *stream);
+/* The same for nrhs right-hand sides back to back, refined together (up to
+   four per pass over the factor) with the stopping test applied to each:
+   one that has stopped keeps its iterate while the others go on.  steps
+   and eta (may be NULL) are arrays of nrhs entries; TG_ERR_NOCONV when any
+   right-hand side did not reach tol.  b and x must not overlap. */
+int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
+                                  double *x, int max_steps, double tol,
+                                  int *steps, double *eta, void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

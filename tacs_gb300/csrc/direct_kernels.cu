@@ -1,4 +1,5 @@
 // Launches of the multifrontal block Cholesky kernels (direct_kernels.cuh).
+#include <algorithm>
 #include <cmath>
 
 #include "direct_kernels.cuh"
@@ -53,30 +54,59 @@ void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                                                      k0);
 }
 
+// the solves' kernels for NR = 1, 2 or 4 right-hand sides at once
+template <class T>
+static void forward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
+                          const DirectView &v, const int *sn, int count,
+                          T *y, T *contrib) {
+  if (nr == 4)
+    direct_forward_kernel<T, 4><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+  else if (nr == 2)
+    direct_forward_kernel<T, 2><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+  else
+    direct_forward_kernel<T, 1><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+}
+template <class T>
+static void backward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
+                           const DirectView &v, const int *sn, int count,
+                           const T *y, T *x) {
+  if (nr == 4)
+    direct_backward_kernel<T, 4><<<g, 256, smem, s>>>(v, sn, count, y, x);
+  else if (nr == 2)
+    direct_backward_kernel<T, 2><<<g, 256, smem, s>>>(v, sn, count, y, x);
+  else
+    direct_backward_kernel<T, 1><<<g, 256, smem, s>>>(v, sn, count, y, x);
+}
+
+size_t direct_solve_smem(int front, int nr, size_t elem) {
+  return elem * ((size_t)front * nr + kDirectSolveDiag);
+}
+
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
-                           int max_front, T *y, T *contrib, cudaStream_t s) {
+                           int max_front, int nr, T *y, T *contrib,
+                           cudaStream_t s) {
   if (count <= 0) return;
-  direct_forward_kernel<T>
-      <<<count, 256, sizeof(T) * (max_front + kDirectSolveDiag), s>>>(
-          v, sn, count, y, contrib);
+  forward_plain<T>(nr, dim3(count), direct_solve_smem(max_front, nr, sizeof(T)),
+                   s, v, sn, count, y, contrib);
 }
 
 template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
-                            int max_front, const T *y, T *x, cudaStream_t s) {
+                            int max_front, int nr, const T *y, T *x,
+                            cudaStream_t s) {
   if (count <= 0) return;
-  direct_backward_kernel<T>
-      <<<count, 256, sizeof(T) * (max_front + kDirectSolveDiag), s>>>(
-          v, sn, count, y, x);
+  backward_plain<T>(nr, dim3(count),
+                    direct_solve_smem(max_front, nr, sizeof(T)), s, v, sn,
+                    count, y, x);
 }
 
 // Large fronts: kDirectSolveCluster CTAs per front in one thread-block
 // cluster; shared memory for the rank owning the most rows.
-static size_t cluster_smem(int max_front, size_t elem) {
+size_t direct_cluster_smem(int max_front, int nr, size_t elem) {
   const int nbk = (max_front + 31) / 32;
   const int mine = (nbk + kDirectSolveCluster - 1) / kDirectSolveCluster;
-  return elem * ((size_t)mine * 32 + kDirectSolveDiag);
+  return elem * ((size_t)mine * 32 * nr + kDirectSolveDiag);
 }
 
 template <class K, class... Args>
@@ -99,21 +129,36 @@ static cudaError_t cluster_launch_dk(K kernel, int count, size_t smem,
 
 template <class T>
 void launch_direct_forward_cluster(const DirectView &v, const int *sn,
-                                   int count, int max_front, T *y, T *contrib,
-                                   cudaStream_t s) {
+                                   int count, int max_front, int nr, T *y,
+                                   T *contrib, cudaStream_t s) {
   if (count <= 0) return;
-  cluster_launch_dk(direct_forward_cluster_kernel<T>, count,
-                    cluster_smem(max_front, sizeof(T)), s, v, sn, count, y,
-                    contrib);
+  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T));
+  if (nr == 4)
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 4>, count, smem, s, v,
+                      sn, count, y, contrib);
+  else if (nr == 2)
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 2>, count, smem, s, v,
+                      sn, count, y, contrib);
+  else
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 1>, count, smem, s, v,
+                      sn, count, y, contrib);
 }
 
 template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
-                                    int count, int max_front, const T *y,
-                                    T *x, cudaStream_t s) {
+                                    int count, int max_front, int nr,
+                                    const T *y, T *x, cudaStream_t s) {
   if (count <= 0) return;
-  cluster_launch_dk(direct_backward_cluster_kernel<T>, count,
-                    cluster_smem(max_front, sizeof(T)), s, v, sn, count, y, x);
+  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T));
+  if (nr == 4)
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 4>, count, smem, s,
+                      v, sn, count, y, x);
+  else if (nr == 2)
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 2>, count, smem, s,
+                      v, sn, count, y, x);
+  else
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 1>, count, smem, s,
+                      v, sn, count, y, x);
 }
 
 // whether the device schedules the solve clusters (at least one active)
@@ -121,7 +166,7 @@ bool direct_cluster_solve_ok() {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kDirectSolveCluster);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = cluster_smem(1 << 15, sizeof(double));
+  cfg.dynamicSmemBytes = direct_cluster_smem(1 << 15, 1, sizeof(double));
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = kDirectSolveCluster;
@@ -131,7 +176,7 @@ bool direct_cluster_solve_ok() {
   cfg.numAttrs = 1;
   int n = 0;
   const cudaError_t e = cudaOccupancyMaxActiveClusters(
-      &n, (void *)direct_forward_cluster_kernel<double>, &cfg);
+      &n, (void *)direct_forward_cluster_kernel<double, 1>, &cfg);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -141,46 +186,82 @@ bool direct_cluster_solve_ok() {
 
 template <class T>
 void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
-                           T *out, cudaStream_t s) {
-  direct_bc_mask_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
-      n, bs, bcmask, b, out);
+                           T *out, int nrhs, size_t ld, cudaStream_t s) {
+  direct_bc_mask_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
+      n, bs, bcmask, b, out, nrhs, ld);
 }
 
 template <class T>
 void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
-                       const T *Kpb, const T *pb, T *ypos, cudaStream_t s) {
-  direct_rhs_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
-      n, bs, perm, b, Kpb, pb, ypos);
+                       const T *Kpb, const T *pb, T *ypos, int nrhs,
+                       size_t ld, cudaStream_t s) {
+  direct_rhs_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
+      n, bs, perm, b, Kpb, pb, ypos, nrhs, ld);
 }
 
 template <class T>
 void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
-                             T *x, cudaStream_t s) {
-  direct_unpermute_kernel<T><<<grid_1d((size_t)n * bs), 256, 0, s>>>(
-      n, bs, perm, xpos, x);
+                             T *x, int nrhs, size_t ld, cudaStream_t s) {
+  direct_unpermute_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
+      n, bs, perm, xpos, x, nrhs, ld);
 }
 
-cudaError_t direct_set_smem(int max_front) {
-  // per device (the attribute belongs to the kernel on each device); the
-  // limit only grows, and is recorded only once every call succeeded
+// Dynamic shared memory of the solve kernels above the default 48 KB, for
+// fronts of up to plain_front rows on one CTA and cluster_front rows on a
+// cluster, nr right-hand sides at most.  Per device (the attribute belongs
+// to the kernel on each device); the limits only grow, and are recorded
+// only once every call succeeded.
+template <class T, int NR>
+static cudaError_t set_solve_smem(int plain_front, int cluster_front) {
+  const size_t pb = direct_solve_smem(plain_front, NR, sizeof(T));
+  const size_t cb = direct_cluster_smem(cluster_front, NR, sizeof(T));
+  const void *plain[2] = {(const void *)direct_forward_kernel<T, NR>,
+                          (const void *)direct_backward_kernel<T, NR>};
+  const void *clus[2] = {(const void *)direct_forward_cluster_kernel<T, NR>,
+                         (const void *)direct_backward_cluster_kernel<T, NR>};
+  cudaError_t e = cudaSuccess;
+  if (pb > 48 * 1024)
+    for (const void *k : plain)
+      if ((e = cudaFuncSetAttribute(k,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pb)) != cudaSuccess)
+        return e;
+  if (cluster_front > 0 && cb > 48 * 1024)
+    for (const void *k : clus)
+      if ((e = cudaFuncSetAttribute(k,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cb)) != cudaSuccess)
+        return e;
+  return e;
+}
+
+cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
   constexpr int kMaxDevices = 64;
-  static int set[kMaxDevices] = {};
+  static int set_plain[kMaxDevices] = {}, set_cluster[kMaxDevices] = {},
+             set_nr[kMaxDevices] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  const int bytes = (int)sizeof(double) * (max_front + kDirectSolveDiag);
-  if (bytes <= 48 * 1024 || bytes <= set[dev]) return cudaSuccess;
-  const void *ks[4] = {(const void *)direct_forward_kernel<double>,
-                       (const void *)direct_backward_kernel<double>,
-                       (const void *)direct_forward_kernel<float>,
-                       (const void *)direct_backward_kernel<float>};
-  for (const void *k : ks) {
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes);
-    if (e != cudaSuccess) return e;
+  if (plain_front <= set_plain[dev] && cluster_front <= set_cluster[dev] &&
+      max_nr <= set_nr[dev])
+    return cudaSuccess;
+  const int pf = std::max(plain_front, set_plain[dev]);
+  const int cf = std::max(cluster_front, set_cluster[dev]);
+  const int mn = std::max(max_nr, set_nr[dev]);
+  if ((e = set_solve_smem<double, 1>(pf, cf)) != cudaSuccess) return e;
+  if ((e = set_solve_smem<float, 1>(pf, cf)) != cudaSuccess) return e;
+  if (mn >= 2) {
+    if ((e = set_solve_smem<double, 2>(pf, cf)) != cudaSuccess) return e;
+    if ((e = set_solve_smem<float, 2>(pf, cf)) != cudaSuccess) return e;
   }
-  set[dev] = bytes;
+  if (mn >= 4) {
+    if ((e = set_solve_smem<double, 4>(pf, cf)) != cudaSuccess) return e;
+    if ((e = set_solve_smem<float, 4>(pf, cf)) != cudaSuccess) return e;
+  }
+  set_plain[dev] = pf;
+  set_cluster[dev] = cf;
+  set_nr[dev] = mn;
   return cudaSuccess;
 }
 
@@ -197,22 +278,25 @@ cudaError_t direct_set_smem(int max_front) {
                                             const int *, int, int, int *,    \
                                             cudaStream_t);                   \
   template void launch_direct_forward<T>(const DirectView &, const int *,  \
-                                         int, int, T *, T *, cudaStream_t); \
+                                         int, int, int, T *, T *,          \
+                                         cudaStream_t);                    \
   template void launch_direct_backward<T>(const DirectView &, const int *, \
-                                          int, int, const T *, T *,        \
+                                          int, int, int, const T *, T *,   \
                                           cudaStream_t);                   \
   template void launch_direct_forward_cluster<T>(                          \
-      const DirectView &, const int *, int, int, T *, T *, cudaStream_t);  \
+      const DirectView &, const int *, int, int, int, T *, T *,            \
+      cudaStream_t);                                                        \
   template void launch_direct_backward_cluster<T>(                         \
-      const DirectView &, const int *, int, int, const T *, T *,           \
+      const DirectView &, const int *, int, int, int, const T *, T *,      \
       cudaStream_t);                                                        \
   template void launch_direct_bc_mask<T>(int, int, const int *, const T *, \
-                                         T *, cudaStream_t);               \
+                                         T *, int, size_t, cudaStream_t);  \
   template void launch_direct_rhs<T>(int, int, const int *, const T *,     \
-                                     const T *, const T *, T *,            \
-                                     cudaStream_t);                        \
+                                     const T *, const T *, T *, int,       \
+                                     size_t, cudaStream_t);                \
   template void launch_direct_unpermute<T>(int, int, const int *,          \
-                                           const T *, T *, cudaStream_t);
+                                           const T *, T *, int, size_t,    \
+                                           cudaStream_t);
 TG_DIRECT_INSTANTIATE(double)
 TG_DIRECT_INSTANTIATE(float)
 

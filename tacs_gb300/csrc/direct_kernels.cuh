@@ -352,32 +352,47 @@ __global__ void __launch_bounds__(256)
 }
 
 // ----------------------------------------------------------------- solves
+// NR right-hand sides at once: every vector of the solve (the factor-order
+// vectors y and x, the contribution vectors and the front workspace z)
+// holds entry t of right-hand side r at t * NR + r, so that each factor
+// entry loaded serves NR products; each right-hand side's sums are formed
+// in the same order whatever NR is.
 // Both solves go through the panel in blocks of kDirectSolveBlock columns:
 // the block's diagonal part is staged in shared memory (rows padded to an
 // odd length) and solved by one warp, and the block's off-diagonal part
 // updates the rest of the front in one pass whose threads read contiguous
 // panel rows (forward) or consecutive columns (backward).  Two CTA
 // barriers per block instead of two per column.  Dynamic shared memory:
-// the front's M entries of z, then the diagonal block.
+// the front's M x NR entries of z, then the diagonal block.
 
 // Triangular solve of the staged diagonal block D (nb x nb, row stride
-// kDirectSolveBlock + 1) on zb[0..nb): lower (L zb = zb) or its transpose.
-// Warp 0 works on it; the others wait at the caller's barrier.
-template <class T, bool kTranspose>
+// kDirectSolveBlock + 1) on zb[0..nb) (NR interleaved right-hand sides):
+// lower (L zb = zb) or its transpose.  Warp 0 works on it; the others
+// wait at the caller's barrier.
+template <class T, bool kTranspose, int NR>
 __device__ __forceinline__ void dk_block_solve(const T *D, int nb, T *zb) {
   constexpr int P = kDirectSolveBlock + 1;
   if (threadIdx.x >= 32) return;
   const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
   for (int kk = 0; kk < nb; kk++) {
     const int k = kTranspose ? nb - 1 - kk : kk;
-    if (threadIdx.x == 0) zb[k] /= D[k * P + k];
+    for (int r = threadIdx.x; r < NR; r += ls) zb[k * NR + r] /= D[k * P + k];
     __syncwarp();
-    const T zk = zb[k];
+    T zk[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) zk[r] = zb[k * NR + r];
     if (kTranspose) {
-      for (int j = threadIdx.x; j < k; j += ls) zb[j] -= D[k * P + j] * zk;
+      for (int j = threadIdx.x; j < k; j += ls) {
+        const T d = D[k * P + j];
+#pragma unroll
+        for (int r = 0; r < NR; r++) zb[j * NR + r] -= d * zk[r];
+      }
     } else {
-      for (int j = k + 1 + threadIdx.x; j < nb; j += ls)
-        zb[j] -= D[j * P + k] * zk;
+      for (int j = k + 1 + threadIdx.x; j < nb; j += ls) {
+        const T d = D[j * P + k];
+#pragma unroll
+        for (int r = 0; r < NR; r++) zb[j * NR + r] -= d * zk[r];
+      }
     }
     __syncwarp();
   }
@@ -393,10 +408,15 @@ __device__ __forceinline__ void dk_stage_block(const Front<T> &f, int kb,
   }
 }
 
+// position of front row i of supernode s in a factor-order vector
+__device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
+  return (size_t)rows[i / bs] * bs + i % bs;
+}
+
 // Forward: z = front rows of the supernode (own rows from y, the rows
 // below zero), plus the children's contribution vectors; L11 z1 = z1 and
 // z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
-template <class T>
+template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
                           T *y, T *contrib) {
@@ -404,48 +424,62 @@ __global__ void __launch_bounds__(256)
   DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
-  T *D = z + f.M;
+  T *D = z + (size_t)f.M * NR;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
-  for (int t = threadIdx.x; t < f.M; t += blockDim.x)
-    z[t] = t < f.C ? y[(size_t)rows[t / bs] * bs + t % bs] : 0.0;
+  for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
+    const int i = t / NR, r = t - NR * (t / NR);
+    z[t] = i < f.C ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
+  }
   __syncthreads();
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
     const int c = v.ch_list[k];
     const Front<T> fc = front_of<T>(v, c);
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
-    const T *w = contrib + v.v_off[c];
-    for (int t = threadIdx.x; t < um; t += blockDim.x)
-      z[rel[t / bs] * bs + t % bs] += w[t];
+    const T *w = contrib + v.v_off[c] * NR;
+    for (int t = threadIdx.x; t < um * NR; t += blockDim.x) {
+      const int i = t / NR, r = t - NR * (t / NR);
+      z[(rel[i / bs] * bs + i % bs) * NR + r] += w[t];
+    }
     __syncthreads();
   }
   for (int kb = 0; kb < f.C; kb += kDirectSolveBlock) {
     const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
     dk_stage_block(f, kb, nb, D);
     __syncthreads();
-    dk_block_solve<T, false>(D, nb, z + kb);
+    dk_block_solve<T, false, NR>(D, nb, z + kb * NR);
     __syncthreads();
     // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb)
     for (int i = kb + nb + threadIdx.x; i < f.M; i += blockDim.x) {
       const T *Li = f.lp + (size_t)i * f.C + kb;
-      T acc = 0;
-      for (int c = 0; c < nb; c++) acc += Li[c] * z[kb + c];
-      z[i] -= acc;
+      T acc[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[r] = 0;
+      for (int c = 0; c < nb; c++) {
+        const T l = Li[c];
+#pragma unroll
+        for (int r = 0; r < NR; r++) acc[r] += l * z[(kb + c) * NR + r];
+      }
+#pragma unroll
+      for (int r = 0; r < NR; r++) z[i * NR + r] -= acc[r];
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < f.C; t += blockDim.x)
-    y[(size_t)rows[t / bs] * bs + t % bs] = z[t];
+  for (int t = threadIdx.x; t < f.C * NR; t += blockDim.x) {
+    const int i = t / NR, r = t - NR * (t / NR);
+    y[dk_pos(rows, bs, i) * NR + r] = z[t];
+  }
   if (v.sn_parent[s] >= 0) {
-    T *w = contrib + v.v_off[s];
-    for (int t = f.C + threadIdx.x; t < f.M; t += blockDim.x) w[t - f.C] = z[t];
+    T *w = contrib + v.v_off[s] * NR;
+    for (int t = f.C * NR + threadIdx.x; t < f.M * NR; t += blockDim.x)
+      w[t - f.C * NR] = z[t];
   }
 }
 
 // Backward: z1 = y1 - L21^T x2 (x2 from the ancestors, already final),
 // then L11^T z1 = z1 from the last block up; own rows to x.
-template <class T>
+template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_backward_kernel(DirectView v, const int *__restrict__ sn,
                            int count, const T *y, T *x) {
@@ -453,18 +487,26 @@ __global__ void __launch_bounds__(256)
   DK_DYN_SMEM(T, z);
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
-  T *D = z + f.M;
+  T *D = z + (size_t)f.M * NR;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
-  for (int t = threadIdx.x; t < f.M; t += blockDim.x) {
-    const size_t g = (size_t)rows[t / bs] * bs + t % bs;
-    z[t] = t < f.C ? y[g] : x[g];
+  for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
+    const int i = t / NR, r = t - NR * (t / NR);
+    const size_t g = dk_pos(rows, bs, i) * NR + r;
+    z[t] = i < f.C ? y[g] : x[g];
   }
   __syncthreads();
   for (int j = threadIdx.x; j < f.C; j += blockDim.x) {
-    T acc = 0;
-    for (int i = f.C; i < f.M; i++) acc += f.lp[(size_t)i * f.C + j] * z[i];
-    z[j] -= acc;
+    T acc[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) acc[r] = 0;
+    for (int i = f.C; i < f.M; i++) {
+      const T l = f.lp[(size_t)i * f.C + j];
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[r] += l * z[i * NR + r];
+    }
+#pragma unroll
+    for (int r = 0; r < NR; r++) z[j * NR + r] -= acc[r];
   }
   __syncthreads();
   for (int kb = ((f.C - 1) / kDirectSolveBlock) * kDirectSolveBlock; kb >= 0;
@@ -472,19 +514,27 @@ __global__ void __launch_bounds__(256)
     const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
     dk_stage_block(f, kb, nb, D);
     __syncthreads();
-    dk_block_solve<T, true>(D, nb, z + kb);
+    dk_block_solve<T, true, NR>(D, nb, z + kb * NR);
     __syncthreads();
     // columns before the block: z_j -= sum_k L(kb + k, j) z(kb + k)
     for (int j = threadIdx.x; j < kb; j += blockDim.x) {
-      T acc = 0;
-      for (int k = 0; k < nb; k++)
-        acc += f.lp[(size_t)(kb + k) * f.C + j] * z[kb + k];
-      z[j] -= acc;
+      T acc[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[r] = 0;
+      for (int k = 0; k < nb; k++) {
+        const T l = f.lp[(size_t)(kb + k) * f.C + j];
+#pragma unroll
+        for (int r = 0; r < NR; r++) acc[r] += l * z[(kb + k) * NR + r];
+      }
+#pragma unroll
+      for (int r = 0; r < NR; r++) z[j * NR + r] -= acc[r];
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < f.C; t += blockDim.x)
-    x[(size_t)rows[t / bs] * bs + t % bs] = z[t];
+  for (int t = threadIdx.x; t < f.C * NR; t += blockDim.x) {
+    const int i = t / NR, r = t - NR * (t / NR);
+    x[dk_pos(rows, bs, i) * NR + r] = z[t];
+  }
 }
 
 #ifndef DK_EMULATE
@@ -494,15 +544,14 @@ __global__ void __launch_bounds__(256)
 // with thousands of rows, on one SM each).  The front's rows are dealt out
 // in 32-row blocks: block b belongs to rank b % nr and sits in that CTA's
 // shared memory at slot (b / nr) * 32.  For column block kb its owner
-// solves the staged diagonal block and publishes the 32 values; after one
-// hardware cluster barrier every rank reads them through distributed
+// solves the staged diagonal block and publishes the 32 x NR values; after
+// one hardware cluster barrier every rank reads them through distributed
 // shared memory and updates its own rows (forward: rows below; backward:
 // columns before).  The control flow is the same in every CTA of a
 // cluster (each cluster exits together, and every barrier is reached by
 // all of its CTAs); a final barrier keeps each CTA's shared memory alive
 // until the others are done reading it.  Dynamic shared memory: the owned
-// rows (rounded up to whole blocks), then the diagonal block.
-template <class T>
+// rows (rounded up to whole blocks) x NR, then the diagonal block.
 struct ClusterRows {
   int nr, rank;
   __device__ __forceinline__ bool owns(int r) const {
@@ -522,26 +571,26 @@ struct ClusterRows {
   }
 };
 
-template <class T>
+template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
                                   int count, T *y, T *contrib) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
-  const ClusterRows<T> cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
   const int fi = (int)blockIdx.x / cr.nr;  // the same in the whole cluster
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
-  __shared__ T zb[32], zk[32];
+  __shared__ T zb[32 * NR], zk[32 * NR];
   const int s = sn[fi];
   const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const int nown = cr.count(f.M);
-  T *D = z + nown;
-  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
-    const int r = cr.row(t);
-    z[t] = (r < f.C) ? y[(size_t)rows[r / bs] * bs + r % bs] : T(0);
+  T *D = z + (size_t)nown * NR;
+  for (int t = threadIdx.x; t < nown * NR; t += blockDim.x) {
+    const int i = cr.row(t / NR), r = t - NR * (t / NR);
+    z[t] = (i < f.C) ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
   }
   __syncthreads();
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
@@ -549,10 +598,11 @@ __global__ void __launch_bounds__(256)
     const Front<T> fc = front_of<T>(v, c);
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
-    const T *w = contrib + v.v_off[c];
-    for (int t = threadIdx.x; t < um; t += blockDim.x) {
-      const int r = rel[t / bs] * bs + t % bs;
-      if (cr.owns(r)) z[cr.slot(r)] += w[t];
+    const T *w = contrib + v.v_off[c] * NR;
+    for (int t = threadIdx.x; t < um * NR; t += blockDim.x) {
+      const int i = t / NR, q = t - NR * (t / NR);
+      const int r = rel[i / bs] * bs + i % bs;
+      if (cr.owns(r)) z[cr.slot(r) * NR + q] += w[t];
     }
     __syncthreads();
   }
@@ -562,60 +612,75 @@ __global__ void __launch_bounds__(256)
     if (owner == cr.rank) {
       dk_stage_block(f, kb, nb, D);
       __syncthreads();
-      dk_block_solve<T, false>(D, nb, z + cr.slot(kb));
+      dk_block_solve<T, false, NR>(D, nb, z + cr.slot(kb) * NR);
       __syncthreads();
-      for (int t = threadIdx.x; t < nb; t += blockDim.x)
-        zb[t] = z[cr.slot(kb) + t];
+      for (int t = threadIdx.x; t < nb * NR; t += blockDim.x)
+        zb[t] = z[cr.slot(kb) * NR + t];
     }
     cl.sync();
     const T *src = cl.map_shared_rank(zb, owner);
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) zk[t] = src[t];
+    for (int t = threadIdx.x; t < nb * NR; t += blockDim.x) zk[t] = src[t];
     __syncthreads();
     // own rows below the block: z_r -= L(r, kb .. kb+nb) zk
     for (int t = threadIdx.x; t < nown; t += blockDim.x) {
       const int r = cr.row(t);
       if (r < kb + nb || r >= f.M) continue;
       const T *Lr = f.lp + (size_t)r * f.C + kb;
-      T acc = 0;
-      for (int c = 0; c < nb; c++) acc += Lr[c] * zk[c];
-      z[t] -= acc;
+      T acc[NR];
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[q] = 0;
+      for (int c = 0; c < nb; c++) {
+        const T l = Lr[c];
+#pragma unroll
+        for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
+      }
+#pragma unroll
+      for (int q = 0; q < NR; q++) z[t * NR + q] -= acc[q];
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
-    const int r = cr.row(t);
-    if (r < f.C) y[(size_t)rows[r / bs] * bs + r % bs] = z[t];
+  for (int t = threadIdx.x; t < nown * NR; t += blockDim.x) {
+    const int r = cr.row(t / NR), q = t - NR * (t / NR);
+    if (r < f.C) y[dk_pos(rows, bs, r) * NR + q] = z[t];
     else if (r < f.M && v.sn_parent[s] >= 0)
-      contrib[v.v_off[s] + (r - f.C)] = z[t];
+      contrib[(v.v_off[s] + (r - f.C)) * NR + q] = z[t];
   }
   cl.sync();  // the other ranks may still read zb
 }
 
-template <class T>
+template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_backward_cluster_kernel(DirectView v, const int *__restrict__ sn,
                                    int count, const T *y, T *x) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
-  const ClusterRows<T> cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
   const int fi = (int)blockIdx.x / cr.nr;
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
-  __shared__ T zb[32], zk[32];
+  __shared__ T zb[32 * NR], zk[32 * NR];
   const int s = sn[fi];
   const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const int nown = cr.count(f.M);
-  T *D = z + nown;
+  T *D = z + (size_t)nown * NR;
   // own rows of the triangle: y1 - L21^T x2 (x2 final, from the ancestors)
   for (int t = threadIdx.x; t < nown; t += blockDim.x) {
     const int j = cr.row(t);
     if (j >= f.C) continue;
-    T acc = 0;
-    for (int i = f.C; i < f.M; i++)
-      acc += f.lp[(size_t)i * f.C + j] * x[(size_t)rows[i / bs] * bs + i % bs];
-    z[t] = y[(size_t)rows[j / bs] * bs + j % bs] - acc;
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; q++) acc[q] = 0;
+    for (int i = f.C; i < f.M; i++) {
+      const T l = f.lp[(size_t)i * f.C + j];
+      const size_t g = dk_pos(rows, bs, i) * NR;
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[q] += l * x[g + q];
+    }
+    const size_t gj = dk_pos(rows, bs, j) * NR;
+#pragma unroll
+    for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - acc[q];
   }
   __syncthreads();
   for (int kb = ((f.C - 1) >> 5) << 5; kb >= 0; kb -= 32) {
@@ -624,67 +689,79 @@ __global__ void __launch_bounds__(256)
     if (owner == cr.rank) {
       dk_stage_block(f, kb, nb, D);
       __syncthreads();
-      dk_block_solve<T, true>(D, nb, z + cr.slot(kb));
+      dk_block_solve<T, true, NR>(D, nb, z + cr.slot(kb) * NR);
       __syncthreads();
-      for (int t = threadIdx.x; t < nb; t += blockDim.x)
-        zb[t] = z[cr.slot(kb) + t];
+      for (int t = threadIdx.x; t < nb * NR; t += blockDim.x)
+        zb[t] = z[cr.slot(kb) * NR + t];
     }
     cl.sync();
     const T *src = cl.map_shared_rank(zb, owner);
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) zk[t] = src[t];
+    for (int t = threadIdx.x; t < nb * NR; t += blockDim.x) zk[t] = src[t];
     __syncthreads();
     // own columns before the block: z_j -= sum_k L(kb + k, j) zk_k
     for (int t = threadIdx.x; t < nown; t += blockDim.x) {
       const int j = cr.row(t);
       if (j >= kb) continue;
-      T acc = 0;
-      for (int k = 0; k < nb; k++)
-        acc += f.lp[(size_t)(kb + k) * f.C + j] * zk[k];
-      z[t] -= acc;
+      T acc[NR];
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[q] = 0;
+      for (int k = 0; k < nb; k++) {
+        const T l = f.lp[(size_t)(kb + k) * f.C + j];
+#pragma unroll
+        for (int q = 0; q < NR; q++) acc[q] += l * zk[k * NR + q];
+      }
+#pragma unroll
+      for (int q = 0; q < NR; q++) z[t * NR + q] -= acc[q];
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
-    const int r = cr.row(t);
-    if (r < f.C) x[(size_t)rows[r / bs] * bs + r % bs] = z[t];
+  for (int t = threadIdx.x; t < nown * NR; t += blockDim.x) {
+    const int r = cr.row(t / NR), q = t - NR * (t / NR);
+    if (r < f.C) x[dk_pos(rows, bs, r) * NR + q] = z[t];
   }
   cl.sync();
 }
 #endif  // DK_EMULATE
 
-// b' = b - K P b + P b (P keeps the boundary dofs) is formed as
-// tmp = P b, then K tmp by the mat-vec, then this kernel; and the
-// permutations into and out of the factor's order
+// b' = b - K P b + P b (P keeps the boundary dofs) for nrhs right-hand
+// sides ld apart (node order): tmp = P b, K tmp by the mat-vec, then the
+// right-hand-side kernel, which also permutes into the factor's order and
+// interleaves (ypos[t * nrhs + r]); the unpermute kernel undoes both.
 template <class T>
 __global__ void direct_bc_mask_kernel(int n, int bs, const int *bcmask,
-                                      const T *b, T *out) {
-  const size_t N = (size_t)n * bs;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+                                      const T *b, T *out, int nrhs,
+                                      size_t ld) {
+  const size_t N = (size_t)n * bs, tot = N * nrhs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
        t += (size_t)gridDim.x * blockDim.x) {
-    const int node = (int)(t / bs), r = (int)(t % bs);
-    out[t] = ((bcmask[node] >> r) & 1) ? b[t] : T(0);
+    const size_t r = t / N, e = t - N * r;
+    const int node = (int)(e / bs), q = (int)(e % bs);
+    out[t] = ((bcmask[node] >> q) & 1) ? b[r * ld + e] : T(0);
   }
 }
 template <class T>
 __global__ void direct_rhs_kernel(int n, int bs, const int *perm,
                                   const T *b, const T *Kpb, const T *pb,
-                                  T *ypos) {
-  const size_t N = (size_t)n * bs;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+                                  T *ypos, int nrhs, size_t ld) {
+  const size_t N = (size_t)n * bs, tot = N * nrhs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
        t += (size_t)gridDim.x * blockDim.x) {
-    const int pos = (int)(t / bs), r = (int)(t % bs);
-    const size_t g = (size_t)perm[pos] * bs + r;
-    ypos[t] = b[g] - Kpb[g] + pb[g];
+    const size_t e = t / nrhs, r = t - nrhs * e;
+    const int pos = (int)(e / bs), q = (int)(e % bs);
+    const size_t g = (size_t)perm[pos] * bs + q;
+    ypos[t] = b[r * ld + g] - Kpb[r * N + g] + pb[r * N + g];
   }
 }
 template <class T>
 __global__ void direct_unpermute_kernel(int n, int bs, const int *perm,
-                                        const T *xpos, T *x) {
-  const size_t N = (size_t)n * bs;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N;
+                                        const T *xpos, T *x, int nrhs,
+                                        size_t ld) {
+  const size_t N = (size_t)n * bs, tot = N * nrhs;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
        t += (size_t)gridDim.x * blockDim.x) {
-    const int pos = (int)(t / bs), r = (int)(t % bs);
-    x[(size_t)perm[pos] * bs + r] = xpos[t];
+    const size_t e = t / nrhs, r = t - nrhs * e;
+    const int pos = (int)(e / bs), q = (int)(e % bs);
+    x[r * ld + (size_t)perm[pos] * bs + q] = xpos[t];
   }
 }
 

@@ -39,6 +39,10 @@ struct tg_direct {
   int refcount = 1;
   tg_mat *A = nullptr;
   int n = 0, bs = 0, ns = 0, max_front = 0;
+  // the largest front solved by one CTA and by one cluster, and the most
+  // right-hand sides one solve pass takes (1, 2 or 4; the solve vectors
+  // and refinement scratch hold that many)
+  int plain_front = 0, cluster_front = 0, max_nr = 1;
   int precision = TG_PREC_FP64;
   tg::direct::Analysis an;
   std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
@@ -196,10 +200,13 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
       for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
         const int sn = an.level_sn[t];
-        if (clusters && d->front_m_h[sn] > tg::kDirectClusterFront)
+        if (clusters && d->front_m_h[sn] > tg::kDirectClusterFront) {
           b.push_back(sn);
-        else
+          d->cluster_front = std::max(d->cluster_front, d->front_m_h[sn]);
+        } else {
           a.push_back(sn);
+          d->plain_front = std::max(d->plain_front, d->front_m_h[sn]);
+        }
       }
       d->solve_ptr_h.push_back((int)a.size());
       d->csolve_ptr_h.push_back((int)b.size());
@@ -256,40 +263,53 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
   d->contrib_len = vacc;
+  // right-hand sides per solve pass: 4, unless the workspace of the largest
+  // front would not fit a CTA's shared memory
+  constexpr size_t kSmemMax = 227 * 1024;
+  for (int nr : {4, 2, 1}) {
+    d->max_nr = nr;
+    if (tg::direct_solve_smem(d->plain_front, nr, sizeof(double)) <=
+            kSmemMax &&
+        tg::direct_cluster_smem(d->cluster_front, nr, sizeof(double)) <=
+            kSmemMax)
+      break;
+  }
+  const size_t R = (size_t)d->max_nr;
   if (precision == TG_PREC_FP64) {
     if (!rc) rc = dalloc(&d->d_lstore, (size_t)an.l_total * b2);
     if (!rc) rc = dalloc(&d->d_pool, (size_t)an.u_peak * b2);
-    if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc);
+    if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc * R);
+    if (!rc) rc = dalloc(&d->d_ypos, N * R);
+    if (!rc) rc = dalloc(&d->d_xpos, N * R);
+    if (!rc) rc = dalloc(&d->d_pb, N * R);
+    if (!rc) rc = dalloc(&d->d_kpb, N * R);
   } else {
     if (!rc) rc = dalloc(&d->d_lstore32, (size_t)an.l_total * b2);
     if (!rc) rc = dalloc(&d->d_pool32, (size_t)an.u_peak * b2);
-    if (!rc) rc = dalloc(&d->d_contrib32, (size_t)vacc);
-    if (!rc) rc = dalloc(&d->d_ypos32, N);
-    if (!rc) rc = dalloc(&d->d_xpos32, N);
-    if (!rc) rc = dalloc(&d->d_pb32, N);
-    if (!rc) rc = dalloc(&d->d_kpb32, N);
+    if (!rc) rc = dalloc(&d->d_contrib32, (size_t)vacc * R);
+    if (!rc) rc = dalloc(&d->d_ypos32, N * R);
+    if (!rc) rc = dalloc(&d->d_xpos32, N * R);
+    if (!rc) rc = dalloc(&d->d_pb32, N * R);
+    if (!rc) rc = dalloc(&d->d_kpb32, N * R);
     if (!rc) rc = dalloc(&d->d_a32, (size_t)A->nnz * b2);
-    if (!rc) rc = dalloc(&d->d_r32, N);
-    if (!rc) rc = dalloc(&d->d_c32, N);
-    if (!rc) rc = dalloc(&d->d_r, N);
-    if (!rc) rc = dalloc(&d->d_t, N);
+    if (!rc) rc = dalloc(&d->d_r32, N * R);
+    if (!rc) rc = dalloc(&d->d_c32, N * R);
+    if (!rc) rc = dalloc(&d->d_r, N * R);
+    if (!rc) rc = dalloc(&d->d_t, N * R);
     if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
-    if (!rc) rc = dalloc(&d->d_scal, 4);
+    if (!rc) rc = dalloc(&d->d_scal, 2 * R + 2);
   }
-  if (!rc) rc = dalloc(&d->d_ypos, N);
-  if (!rc) rc = dalloc(&d->d_xpos, N);
-  if (!rc) rc = dalloc(&d->d_pb, N);
-  if (!rc) rc = dalloc(&d->d_kpb, N);
   if (!rc) rc = dalloc(&d->d_fail, 1);
-  if (!rc && (size_t)(d->max_front + tg::kDirectSolveDiag) * sizeof(double) >
-                 227 * 1024)
+  if (!rc && tg::direct_solve_smem(d->plain_front, 1, sizeof(double)) >
+                 kSmemMax)
     rc = fail(TG_ERR_ARG, "tg_direct_create: front too large for a CTA's "
                           "solve workspace");
   if (rc) {
     tg_direct_decref(d);
     return rc;
   }
-  const cudaError_t se = tg::direct_set_smem(d->max_front);
+  const cudaError_t se =
+      tg::direct_set_smem(d->plain_front, d->cluster_front, d->max_nr);
   if (se != cudaSuccess) {
     tg_direct_decref(d);
     return cuda_check(se, "tg_direct_create: solve workspace attribute");
@@ -332,57 +352,159 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
   }
 }
 
-// x = A^-1 b in T: b' = b - K P b + P b, into the factor's order, the
-// level sweeps, back to the node order (K a: the matrix values in T)
+// X = A^-1 B in T for nrhs right-hand sides N = n bs apart: per pass of
+// at most max_nr of them, b' = b - K P b + P b, into the factor's order
+// (interleaved), the level sweeps, back to the node order (K a: the
+// matrix values in T)
 template <class T>
-static void solve_levels(tg_direct *d, const T *b, T *x, const T *a, T *pb,
-                         T *kpb, T *ypos, T *xpos, T *contrib,
-                         cudaStream_t s) {
+static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
+                         const T *a, T *pb, T *kpb, T *ypos, T *xpos,
+                         T *contrib, cudaStream_t s) {
   const tg::DirectView v = d->view();
   tg_mat *A = d->A;
-  tg::launch_direct_bc_mask<T>(d->n, d->bs, d->d_bcmask, b, pb, s);
-  bcsr_mult_t(A, a, pb, kpb, s);
-  tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, b, kpb, pb, ypos, s);
+  const size_t N = (size_t)d->n * d->bs;
   const int nl = (int)d->level_ptr_h.size() - 1;
-  for (int L = 0; L < nl; L++) {
-    const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
-    tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
-                                 d->max_front, ypos, contrib, s);
-    const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
-    tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
-                                         d->max_front, ypos, contrib, s);
+  for (int r0 = 0; r0 < nrhs;) {
+    const int left = nrhs - r0;
+    const int nr = left >= 4 && d->max_nr >= 4 ? 4
+                   : left >= 2 && d->max_nr >= 2 ? 2 : 1;
+    const T *bb = b + (size_t)r0 * N;
+    T *xx = x + (size_t)r0 * N;
+    tg::launch_direct_bc_mask<T>(d->n, d->bs, d->d_bcmask, bb, pb, nr, N, s);
+    for (int r = 0; r < nr; r++)
+      bcsr_mult_t(A, a, pb + r * N, kpb + r * N, s);
+    tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, bb, kpb, pb, ypos, nr, N,
+                             s);
+    for (int L = 0; L < nl; L++) {
+      const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
+      tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
+                                   d->plain_front, nr, ypos, contrib, s);
+      const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+      tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
+                                           d->cluster_front, nr, ypos,
+                                           contrib, s);
+    }
+    for (int L = nl - 1; L >= 0; L--) {
+      const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
+      tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
+                                    d->plain_front, nr, ypos, xpos, s);
+      const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+      tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
+                                            d->cluster_front, nr, ypos, xpos,
+                                            s);
+    }
+    tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, xx, nr, N,
+                                   s);
+    r0 += nr;
   }
-  for (int L = nl - 1; L >= 0; L--) {
-    const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
-    tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
-                                  d->max_front, ypos, xpos, s);
-    const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
-    tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
-                                          d->max_front, ypos, xpos, s);
-  }
-  tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, x, s);
 }
 
 namespace tg {
 
-int direct_enqueue_solve(tg_direct *d, const void *b, void *x, bool f32,
-                         cudaStream_t s) {
-  if (!d || !b || !x)
-    return fail(TG_ERR_ARG, "direct solve: NULL argument");
+int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
+                         bool f32, cudaStream_t s) {
+  if (!d || !b || !x || nrhs < 1)
+    return fail(TG_ERR_ARG, "direct solve: bad arguments");
   if (f32 != (d->precision == TG_PREC_FP32))
     return fail(TG_ERR_ARG, "direct solve: precision of the factorisation");
   if (f32)
-    solve_levels<float>(d, (const float *)b, (float *)x, d->d_a32, d->d_pb32,
-                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
-                        s);
+    solve_levels<float>(d, nrhs, (const float *)b, (float *)x, d->d_a32,
+                        d->d_pb32, d->d_kpb32, d->d_ypos32, d->d_xpos32,
+                        d->d_contrib32, s);
   else
-    solve_levels<double>(d, (const double *)b, (double *)x, d->A->d_vals,
-                         d->d_pb, d->d_kpb, d->d_ypos, d->d_xpos,
-                         d->d_contrib, s);
+    solve_levels<double>(d, nrhs, (const double *)b, (double *)x,
+                         d->A->d_vals, d->d_pb, d->d_kpb, d->d_ypos,
+                         d->d_xpos, d->d_contrib, s);
   return 0;
 }
 
 }  // namespace tg
+
+// Iterative refinement of nr <= max_nr right-hand sides (N apart) with the
+// FP32 factorisation and the stopping test of tg_direct_solve_refined_tol,
+// per right-hand side; one that has stopped keeps its x (its residual is
+// zeroed before the FP32 solve, whose correction is then exactly zero).
+static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
+                       int max_steps, double tol, int *steps, double *eta_out,
+                       cudaStream_t s) {
+  tg_mat *A = d->A;
+  const size_t N = (size_t)d->n * d->bs;
+  double h[2 * 4 + 2];
+  double bnorm[4], prev[4], eta[4];
+  int slow[4], taken[4];
+  bool met[4], done[4];
+  for (int r = 0; r < nr; r++)
+    tg::launch_reduce_absmax(b + r * N, N, d->d_red, kRedParts, d->d_scal + r,
+                             s);
+  TG_CUDA(cudaMemcpyAsync(h, d->d_scal, nr * sizeof(double),
+                          cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  bool all_done = true;
+  for (int r = 0; r < nr; r++) {
+    bnorm[r] = h[r];
+    prev[r] = eta[r] = 0.0;
+    slow[r] = taken[r] = 0;
+    met[r] = done[r] = bnorm[r] == 0.0;  // x = 0 is exact
+    all_done = all_done && done[r];
+  }
+  TG_CUDA(cudaMemsetAsync(x, 0, N * nr * sizeof(double), s));
+  tg::launch_copy(b, d->d_r, N * nr, s);
+  for (int step = 0; step < max_steps && !all_done; step++) {
+    tg::launch_d2f(d->d_r, d->d_r32, N * nr, s);
+    for (int r = 0; r < nr; r++)
+      if (done[r])
+        TG_CUDA(cudaMemsetAsync(d->d_r32 + r * N, 0, N * sizeof(float), s));
+    solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
+                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
+                        s);
+    tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
+    tg::launch_axpy(1.0, d->d_t, x, N * nr, s);
+    tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
+                         A->d_vals, x, d->d_t, s, nr, N);
+    tg::launch_copy(b, d->d_r, N * nr, s);
+    tg::launch_axpy(-1.0, d->d_t, d->d_r, N * nr, s);
+    for (int r = 0; r < nr; r++) {
+      tg::launch_reduce_absmax(d->d_r + r * N, N, d->d_red, kRedParts,
+                               d->d_scal + 2 * r, s);
+      tg::launch_reduce_absmax(x + r * N, N, d->d_red, kRedParts,
+                               d->d_scal + 2 * r + 1, s);
+    }
+    TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 2 * nr * sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    all_done = true;
+    for (int r = 0; r < nr; r++) {
+      if (done[r]) continue;
+      taken[r]++;
+      // normwise backward error of x
+      const double den = d->anorm * h[2 * r + 1] + bnorm[r];
+      eta[r] = den > 0.0 ? h[2 * r] / den : 0.0;
+      if (!(eta[r] == eta[r])) {  // NaN: the FP32 factor is unusable
+        met[r] = false;
+        done[r] = true;
+        continue;
+      }
+      if (eta[r] <= tol) met[r] = true;
+      // The backward-error test alone stops early where |A| |x| >> |b|
+      // (thin shells): there eta reaches eps sqrt(N) with a residual still
+      // far above an FP64 factorisation's.  So the steps go on while they
+      // halve eta, and stop at the first step that does not once the
+      // tolerance is met (two such steps in a row before it: stagnation).
+      slow[r] = (taken[r] > 1 && eta[r] > 0.5 * prev[r]) ? slow[r] + 1 : 0;
+      if (slow[r] >= (met[r] ? 1 : 2)) done[r] = true;
+      prev[r] = eta[r];
+      all_done = all_done && done[r];
+    }
+  }
+  int rc = 0;
+  for (int r = 0; r < nr; r++) {
+    if (steps) steps[r] = taken[r];
+    if (eta_out) eta_out[r] = eta[r];
+    if (!met[r]) rc = TG_ERR_NOCONV;
+  }
+  TG_CUDA(cudaGetLastError());
+  return rc;
+}
 
 extern "C" {
 
@@ -421,12 +543,18 @@ int tg_direct_factor(tg_direct *d, void *s) {
 }
 
 int tg_direct_solve(tg_direct *d, const double *b, double *x, void *s) {
-  if (!d || !b || !x) return fail(TG_ERR_ARG, "tg_direct_solve: NULL");
+  return tg_direct_solve_multi(d, 1, b, x, s);
+}
+
+int tg_direct_solve_multi(tg_direct *d, int nrhs, const double *b, double *x,
+                          void *s) {
+  if (!d || !b || !x || nrhs < 1)
+    return fail(TG_ERR_ARG, "tg_direct_solve: bad arguments");
   if (!d->factored) return fail(TG_ERR_STATE, "tg_direct_solve: not factored");
   if (d->precision != TG_PREC_FP64)
     return fail(TG_ERR_ARG, "tg_direct_solve: FP32 factorisation "
                             "(use tg_direct_solve_f32)");
-  tg::direct_enqueue_solve(d, b, x, false, S(s));
+  tg::direct_enqueue_solve(d, nrhs, b, x, false, S(s));
   TG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -437,7 +565,7 @@ int tg_direct_solve_f32(tg_direct *d, const float *b, float *x, void *s) {
     return fail(TG_ERR_STATE, "tg_direct_solve_f32: not factored");
   if (d->precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_direct_solve_f32: FP64 factorisation");
-  tg::direct_enqueue_solve(d, b, x, true, S(s));
+  tg::direct_enqueue_solve(d, 1, b, x, true, S(s));
   TG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -460,7 +588,7 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
   tg::launch_copy(b, d->d_r, N, S(s));
   for (int k = 0; k < steps; k++) {
     tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
-    solve_levels<float>(d, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
+    solve_levels<float>(d, 1, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
                         d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
                         S(s));
     tg::launch_f2d(d->d_c32, d->d_t, N, S(s));
@@ -479,69 +607,34 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
 int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 int max_steps, double tol, int *steps,
                                 double *eta_out, void *s) {
-  if (!d || !b || !x || max_steps < 1 || !(tol > 0.0))
+  return tg_direct_solve_refined_multi(d, 1, b, x, max_steps, tol, steps,
+                                       eta_out, s);
+}
+
+int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
+                                  double *x, int max_steps, double tol,
+                                  int *steps, double *eta_out, void *s) {
+  if (!d || !b || !x || nrhs < 1 || max_steps < 1 || !(tol > 0.0))
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: bad arguments");
-  if ((const void *)b == (const void *)x)  // b is re-read after x is zeroed
+  const size_t N = (size_t)d->n * d->bs;
+  // b is re-read after x is zeroed
+  const char *bb = (const char *)b, *xb = (const char *)x;
+  if (bb < xb + N * nrhs * sizeof(double) && xb < bb + N * nrhs * sizeof(double))
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: b and x alias");
   if (!d->factored)
     return fail(TG_ERR_STATE, "tg_direct_solve_refined_tol: not factored");
   if (d->precision != TG_PREC_FP32)
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: needs the FP32 "
                             "factorisation");
-  tg_mat *A = d->A;
-  const size_t N = (size_t)d->n * d->bs;
-  double h[2] = {0.0, 0.0};
-  // ||b||_inf
-  tg::launch_reduce_absmax(b, N, d->d_red, kRedParts, d->d_scal, S(s));
-  TG_CUDA(cudaMemcpyAsync(h, d->d_scal, sizeof(double),
-                          cudaMemcpyDeviceToHost, S(s)));
-  TG_CUDA(cudaStreamSynchronize(S(s)));
-  const double bnorm = h[0];
-  TG_CUDA(cudaMemsetAsync(x, 0, N * sizeof(double), S(s)));
-  tg::launch_copy(b, d->d_r, N, S(s));
-  double prev = 0.0, eta = 0.0;
-  int taken = 0, slow = 0, rc = TG_ERR_NOCONV;
-  bool met = false;
-  if (bnorm == 0.0) rc = 0;  // x = 0 is exact
-  while (rc != 0 && taken < max_steps) {
-    tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
-    solve_levels<float>(d, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
-                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
-                        S(s));
-    tg::launch_f2d(d->d_c32, d->d_t, N, S(s));
-    tg::launch_axpy(1.0, d->d_t, x, N, S(s));
-    tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
-                         A->d_vals, x, d->d_t, S(s));
-    tg::launch_copy(b, d->d_r, N, S(s));
-    tg::launch_axpy(-1.0, d->d_t, d->d_r, N, S(s));
-    tg::launch_reduce_absmax(d->d_r, N, d->d_red, kRedParts, d->d_scal,
-                             S(s));
-    tg::launch_reduce_absmax(x, N, d->d_red, kRedParts, d->d_scal + 1, S(s));
-    TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 2 * sizeof(double),
-                            cudaMemcpyDeviceToHost, S(s)));
-    TG_CUDA(cudaStreamSynchronize(S(s)));
-    taken++;
-    // normwise backward error of x
-    const double den = d->anorm * h[1] + bnorm;
-    eta = den > 0.0 ? h[0] / den : 0.0;
-    if (!(eta == eta)) {  // NaN: the FP32 factor is unusable
-      met = false;
-      break;
-    }
-    if (eta <= tol) met = true;
-    // The backward-error test alone stops early where |A| |x| >> |b| (thin
-    // shells): there eta reaches eps sqrt(N) with a residual still far
-    // above an FP64 factorisation's.  So the steps go on while they halve
-    // eta, and stop at the first step that does not once the tolerance is
-    // met (two such steps in a row before it: stagnation).
-    slow = (taken > 1 && eta > 0.5 * prev) ? slow + 1 : 0;
-    if (slow >= (met ? 1 : 2)) break;
-    prev = eta;
+  int rc = 0;
+  for (int r0 = 0; r0 < nrhs; r0 += d->max_nr) {
+    const int nr = nrhs - r0 < d->max_nr ? nrhs - r0 : d->max_nr;
+    const int e = refine_pass(d, nr, b + r0 * N, x + r0 * N, max_steps, tol,
+                              steps ? steps + r0 : nullptr,
+                              eta_out ? eta_out + r0 : nullptr, S(s));
+    if (e && e != TG_ERR_NOCONV) return e;
+    if (e) rc = e;
   }
-  if (met) rc = 0;
-  if (steps) *steps = taken;
-  if (eta_out) *eta_out = eta;
-  TG_CUDA(cudaGetLastError());
   if (rc)
     return fail(TG_ERR_NOCONV, "tg_direct_solve_refined_tol: refinement did "
                                "not reach the backward-error tolerance");

@@ -349,31 +349,39 @@ void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                               int *fail, cudaStream_t s);
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
-                           int max_front, T *y, T *contrib, cudaStream_t s);
+                           int max_front, int nr, T *y, T *contrib,
+                           cudaStream_t s);
 template <class T>
 void launch_direct_backward(const DirectView &v, const int *sn, int count,
-                            int max_front, const T *y, T *x, cudaStream_t s);
+                            int max_front, int nr, const T *y, T *x,
+                            cudaStream_t s);
 // the same solves for large fronts, one thread-block cluster of
 // kDirectSolveCluster CTAs per front
 template <class T>
 void launch_direct_forward_cluster(const DirectView &v, const int *sn,
-                                   int count, int max_front, T *y, T *contrib,
-                                   cudaStream_t s);
+                                   int count, int max_front, int nr, T *y,
+                                   T *contrib, cudaStream_t s);
 template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
-                                    int count, int max_front, const T *y,
-                                    T *x, cudaStream_t s);
+                                    int count, int max_front, int nr,
+                                    const T *y, T *x, cudaStream_t s);
 bool direct_cluster_solve_ok();
+// dynamic shared memory of a solve over fronts of `front` rows with nr
+// right-hand sides (one CTA per front, or one cluster per front)
+size_t direct_solve_smem(int front, int nr, size_t elem);
+size_t direct_cluster_smem(int front, int nr, size_t elem);
+// nrhs right-hand sides ld apart (node order); ypos / xpos interleaved
 template <class T>
 void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
-                           T *out, cudaStream_t s);
+                           T *out, int nrhs, size_t ld, cudaStream_t s);
 template <class T>
 void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
-                       const T *Kpb, const T *pb, T *ypos, cudaStream_t s);
+                       const T *Kpb, const T *pb, T *ypos, int nrhs,
+                       size_t ld, cudaStream_t s);
 template <class T>
 void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
-                             T *x, cudaStream_t s);
-cudaError_t direct_set_smem(int max_front);
+                             T *x, int nrhs, size_t ld, cudaStream_t s);
+cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr);
 
 // error reporting
 void set_error(const std::string &msg);

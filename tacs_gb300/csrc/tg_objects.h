@@ -301,9 +301,10 @@ int pc_factor_fp64(tg_pc *pc, cudaStream_t s);
 // Allocate (not factor) whatever pc_factor_fp64 will fill, so that graphs
 // captured before the fallback see its buffers
 int pc_prepare_fp64(tg_pc *pc);
-// Enqueue x = A^-1 b with a direct factorisation whether or not it is
-// factored yet (graph capture; tg_direct.cu): FP64 b, x for an FP64
-// factorisation, FP32 for an FP32 one
-int direct_enqueue_solve(tg_direct *d, const void *b, void *x, bool f32,
-                         cudaStream_t s);
+// Enqueue X = A^-1 B (nrhs vectors of n x bs entries back to back) with a
+// direct factorisation whether or not it is factored yet (graph capture;
+// tg_direct.cu): FP64 vectors for an FP64 factorisation, FP32 for an FP32
+// one
+int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
+                         bool f32, cudaStream_t s);
 }  // namespace tg

@@ -1521,18 +1521,21 @@ int pc_launch(tg_pc *pc, int nrhs, size_t ld, const void *in, void *out,
   const int bs = pc->A->bsize, nr = pc->A->nrows;
   const bool f64 = use_f64 < 0 ? pc->precision == TG_PREC_FP64 : use_f64 != 0;
   if (pc->type == TG_PC_DIRECT) {
-    // one direct solve per right-hand side (FP64 solves of an FP32 pc use
-    // its FP64 factorisation).  Enqueued without the factored check: a
+    // the direct solves of all right-hand sides (FP64 solves of an FP32 pc
+    // use its FP64 factorisation), several per pass over the factor when
+    // they lie back to back.  Enqueued without the factored check: a
     // Krylov graph is captured before the FP64 fallback factors direct64.
-    tg_direct *d = pc->precision == TG_PREC_FP64 ? pc->direct : pc->direct64;
+    tg_direct *d = f64 ? (pc->precision == TG_PREC_FP64 ? pc->direct
+                                                        : pc->direct64)
+                       : pc->direct;
+    const size_t N = (size_t)nr * bs;
+    if (ld == N || nrhs == 1)
+      return direct_enqueue_solve(d, nrhs, in, out, !f64, s);
+    const size_t esz = f64 ? sizeof(double) : sizeof(float);
     for (int r = 0; r < nrhs; r++) {
-      int rc;
-      if (f64)
-        rc = direct_enqueue_solve(d, (const double *)in + r * ld,
-                                  (double *)out + r * ld, false, s);
-      else
-        rc = direct_enqueue_solve(pc->direct, (const float *)in + r * ld,
-                                  (float *)out + r * ld, true, s);
+      const int rc = direct_enqueue_solve(
+          d, 1, (const char *)in + r * ld * esz, (char *)out + r * ld * esz,
+          !f64, s);
       if (rc) return rc;
     }
     return 0;

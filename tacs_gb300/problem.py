@@ -162,34 +162,44 @@ class Direct:
         check(rc, "tg_direct_factor")
 
     def solve(self, b, x=None, steps=30, tol=None):
-        """x = A^-1 b.  FP64 factorisation: FP64 vectors.  FP32
-        factorisation: FP32 vectors are solved in FP32, FP64 ones by
-        refinement (at most `steps` steps, to the backward error `tol`,
-        default eps sqrt(N)), or by the FP64 factorisation after a
-        fallback."""
+        """x = A^-1 b; b a vector or an (nrhs, n) tensor of right-hand sides
+        (solved together, up to four per pass over the factor).  FP64
+        factorisation: FP64 vectors.  FP32 factorisation: FP32 vectors are
+        solved in FP32, FP64 ones by refinement (at most `steps` steps, to
+        the backward error `tol`, default eps sqrt(n), per right-hand
+        side), or by the FP64 factorisation after a fallback."""
         x = torch.empty_like(b) if x is None else x
         L = _lib.lib()
+        nrhs = b.shape[0] if b.dim() == 2 else 1
         if self._fp64 is not None and b.dtype == torch.float64:
             return self._fp64.solve(b, x)
         if self.precision == _lib.PREC_FP32 and b.dtype == torch.float64:
+            n = b.shape[-1]
             if tol is None:
-                tol = 2.0 ** -53 * float(np.sqrt(b.numel()))
+                tol = 2.0 ** -53 * float(np.sqrt(n))
             if x.data_ptr() == b.data_ptr():  # in place: refine from a copy
                 b = b.clone()
-            st, eta = C.c_int(0), C.c_double(0.0)
-            rc = L.tg_direct_solve_refined_tol(self.handle, _p(b), _p(x),
-                                               int(steps), float(tol),
-                                               C.byref(st), C.byref(eta),
-                                               _stream())
-            self.last_steps, self.last_eta = st.value, eta.value
+            st = np.zeros(nrhs, np.int32)
+            eta = np.zeros(nrhs)
+            rc = L.tg_direct_solve_refined_multi(
+                self.handle, nrhs, _p(b), _p(x), int(steps), float(tol),
+                st.ctypes.data, eta.ctypes.data, _stream())
+            self.last_steps, self.last_eta = int(st.max()), float(eta.max())
             if rc == _lib.ERR_NOCONV:
                 self._factor_fp64()
                 return self._fp64.solve(b, x)
-            check(rc, "tg_direct_solve_refined_tol")
+            check(rc, "tg_direct_solve_refined_multi")
             return x
-        fn = (L.tg_direct_solve_f32 if self.precision == _lib.PREC_FP32
-              else L.tg_direct_solve)
-        check(fn(self.handle, _p(b), _p(x), _stream()), "tg_direct_solve")
+        if self.precision == _lib.PREC_FP32:
+            if nrhs > 1:
+                for r in range(nrhs):
+                    self.solve(b[r], x[r])
+                return x
+            check(L.tg_direct_solve_f32(self.handle, _p(b), _p(x), _stream()),
+                  "tg_direct_solve_f32")
+            return x
+        check(L.tg_direct_solve_multi(self.handle, nrhs, _p(b), _p(x),
+                                      _stream()), "tg_direct_solve_multi")
         return x
 
     def stats(self):
@@ -589,9 +599,7 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
         nsys = nlc * model.nseg
 
         def solve_multi(B):
-            X = torch.empty_like(B)
-            for lc in range(B.shape[0]):
-                dsol.solve(B[lc], X[lc])
+            X = dsol.solve(B.contiguous())
             z = np.zeros(nsys, np.int32)
             return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1
     else:

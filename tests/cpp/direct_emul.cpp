@@ -68,16 +68,38 @@ static void set_store(tg::DirectView &v, float *l, float *p) {
   v.pool32 = p;
 }
 
-// x = A^-1 b for the assembled BCSR matrix A with row boundary conditions
-// (bcmask per node), by the GPU kernels run on the CPU in T (double: the
-// FP64 factorisation; float: the FP32 one, b and x converted).  small_max:
-// fronts of at most this many scalar rows take the one-CTA kernel, larger
-// ones the panel path.  Returns 0, or the failing supernode + 1.
+// the solve passes of tg_direct.cu's solve_levels for NR right-hand sides
+template <class T, int NR>
+static void de_solve_pass(const tg::DirectView &v,
+                          const tg::direct::Analysis &an, int max_front,
+                          T *ypos, T *xpos, T *contrib) {
+  const int nl = (int)an.level_ptr.size() - 1;
+  const size_t smem = (size_t)max_front * NR + tg::kDirectSolveDiag;
+  for (int L = 0; L < nl; L++) {
+    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
+    launch(direct_forward_kernel<T, NR>, le - lb, 1, smem, v,
+           (const int *)an.level_sn.data() + lb, le - lb, ypos, contrib);
+  }
+  for (int L = nl - 1; L >= 0; L--) {
+    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
+    launch(direct_backward_kernel<T, NR>, le - lb, 1, smem, v,
+           (const int *)an.level_sn.data() + lb, le - lb, (const T *)ypos,
+           xpos);
+  }
+}
+
+// X = A^-1 B for the assembled BCSR matrix A with row boundary conditions
+// (bcmask per node) and nrhs right-hand sides back to back, by the GPU
+// kernels run on the CPU in T (double: the FP64 factorisation; float: the
+// FP32 one, b and x converted), in passes of 4, 2 and 1 right-hand sides
+// as on the GPU.  small_max: fronts of at most this many scalar rows take
+// the one-CTA kernel, larger ones the panel path.  Returns 0, or the
+// failing supernode + 1.
 template <class T>
 static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
                       const double *vals, const int *bcmask_in,
-                      const double *xyz, int small_max, const double *b_in,
-                      double *x_out) {
+                      const double *xyz, int small_max, int nrhs,
+                      const double *b_in, double *x_out) {
   std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
   std::vector<int> perm = tg::direct::nested_dissection(rp, cs, 64, xyz);
   tg::direct::Analysis an = tg::direct::analyse(rp, cs, perm);
@@ -104,9 +126,11 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   std::vector<int> bcmask(bcmask_in, bcmask_in + n);
   // sized exactly as tg_direct.cu allocates them, so that a sanitizer
   // build sees any access the GPU would make out of bounds
+  const int max_nr = nrhs >= 4 ? 4 : nrhs >= 2 ? 2 : 1;
   std::vector<T> lstore((size_t)an.l_total * b2),
-      pool((size_t)an.u_peak * b2), contrib(vacc), ypos(N), xpos(N),
-      pb(N), kpb(N), bt(b_in, b_in + N), xt(N), vt(vals, vals + rowp[n] * b2);
+      pool((size_t)an.u_peak * b2), contrib(vacc * max_nr),
+      ypos(N * max_nr), xpos(N * max_nr), pb(N * max_nr), kpb(N * max_nr),
+      bt(b_in, b_in + N * nrhs), xt(N * nrhs), vt(vals, vals + rowp[n] * b2);
   const T *b = bt.data();
   T *x = xt.data();
   int failflag = 0;
@@ -188,36 +212,40 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   // kDirectClusterFront rows take the cluster kernels, one thread-block
   // cluster per front, checked by the GPU tests; here every front takes the
   // one-CTA kernels, which form each row's sums in the same order)
-  launch(direct_bc_mask_kernel<T>, 1, 1, 0, n, bs,
-         (const int *)bcmask.data(), b, pb.data());
-  for (int i = 0; i < n; i++)  // the BCSR mat-vec, in T
-    for (int r = 0; r < bs; r++) {
-      T acc = 0;
-      for (int j = rowp[i]; j < rowp[i + 1]; j++)
-        for (int q = 0; q < bs; q++)
-          acc += vt[b2 * j + r * bs + q] * pb[(size_t)cols[j] * bs + q];
-      kpb[(size_t)i * bs + r] = acc;
-    }
-  launch(direct_rhs_kernel<T>, 1, 1, 0, n, bs, (const int *)an.perm.data(), b,
-         (const T *)kpb.data(), (const T *)pb.data(), ypos.data());
-  const int nl = (int)an.level_ptr.size() - 1;
-  for (int L = 0; L < nl; L++) {
-    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_forward_kernel<T>, le - lb, 1,
-           max_front + tg::kDirectSolveDiag, v,
-           (const int *)an.level_sn.data() + lb, le - lb, ypos.data(),
-           contrib.data());
+  for (int r0 = 0; r0 < nrhs;) {
+    const int left = nrhs - r0;
+    const int nr = left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    const T *bb = b + (size_t)r0 * N;
+    launch(direct_bc_mask_kernel<T>, 1, 1, 0, n, bs,
+           (const int *)bcmask.data(), bb, pb.data(), nr, N);
+    for (int q = 0; q < nr; q++)  // the BCSR mat-vec, in T
+      for (int i = 0; i < n; i++)
+        for (int r = 0; r < bs; r++) {
+          T acc = 0;
+          for (int j = rowp[i]; j < rowp[i + 1]; j++)
+            for (int c = 0; c < bs; c++)
+              acc += vt[b2 * j + r * bs + c] *
+                     pb[q * N + (size_t)cols[j] * bs + c];
+          kpb[q * N + (size_t)i * bs + r] = acc;
+        }
+    launch(direct_rhs_kernel<T>, 1, 1, 0, n, bs, (const int *)an.perm.data(),
+           bb, (const T *)kpb.data(), (const T *)pb.data(), ypos.data(), nr,
+           N);
+    if (nr == 4)
+      de_solve_pass<T, 4>(v, an, max_front, ypos.data(), xpos.data(),
+                          contrib.data());
+    else if (nr == 2)
+      de_solve_pass<T, 2>(v, an, max_front, ypos.data(), xpos.data(),
+                          contrib.data());
+    else
+      de_solve_pass<T, 1>(v, an, max_front, ypos.data(), xpos.data(),
+                          contrib.data());
+    launch(direct_unpermute_kernel<T>, 1, 1, 0, n, bs,
+           (const int *)an.perm.data(), (const T *)xpos.data(),
+           x + (size_t)r0 * N, nr, N);
+    r0 += nr;
   }
-  for (int L = nl - 1; L >= 0; L--) {
-    const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
-    launch(direct_backward_kernel<T>, le - lb, 1,
-           max_front + tg::kDirectSolveDiag, v,
-           (const int *)an.level_sn.data() + lb, le - lb,
-           (const T *)ypos.data(), xpos.data());
-  }
-  launch(direct_unpermute_kernel<T>, 1, 1, 0, n, bs,
-         (const int *)an.perm.data(), (const T *)xpos.data(), x);
-  for (size_t k = 0; k < N; k++) x_out[k] = (double)x[k];
+  for (size_t k = 0; k < N * nrhs; k++) x_out[k] = (double)x[k];
   return 0;
 }
 
@@ -229,9 +257,21 @@ int de_solve(int n, int bs, const int *rowp, const int *cols,
              int small_max, int precision, const double *b, double *x) {
   if (precision == 1)
     return de_solve_t<float>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
-                             b, x);
+                             1, b, x);
   return de_solve_t<double>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
-                            b, x);
+                            1, b, x);
+}
+
+// nrhs right-hand sides back to back
+int de_solve_multi(int n, int bs, const int *rowp, const int *cols,
+                   const double *vals, const int *bcmask, const double *xyz,
+                   int small_max, int precision, int nrhs, const double *b,
+                   double *x) {
+  if (precision == 1)
+    return de_solve_t<float>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
+                             nrhs, b, x);
+  return de_solve_t<double>(n, bs, rowp, cols, vals, bcmask, xyz, small_max,
+                            nrhs, b, x);
 }
 
 }  // extern "C"

@@ -162,6 +162,8 @@ def de(tmp_path_factory):
     P = C.c_void_p
     lib.de_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int,
                              C.c_int, P, P]
+    lib.de_solve_multi.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int,
+                                   C.c_int, C.c_int, P, P]
     return lib
 
 
@@ -349,3 +351,29 @@ def test_gpu_kernels_in_bounds_under_sanitizers(tmp_path):
                                text=True, timeout=300)
             assert r.returncode == 0, r.stdout + r.stderr[-3000:]
             assert len(r.stdout.split()) == 4
+
+
+@pytest.mark.parametrize("name,prob", list(_problems())[:3],
+                         ids=[p[0] for p in _problems()][:3])
+@pytest.mark.parametrize("nrhs", [2, 3, 4, 7])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_kernels_on_cpu_multi_rhs(de, name, prob, nrhs, prec):
+    """Several right-hand sides per pass over the factor (passes of 4, 2
+    and 1, interleaved vectors): each right-hand side's solution is bitwise
+    the one a single solve gives it, in FP64 and FP32."""
+    n, bs, rowp, cols, vals = _matrix(prob)
+    N = n * bs
+    B = np.random.default_rng(nrhs).standard_normal((nrhs, N))
+    xyz = np.ascontiguousarray(prob["xpts"], np.float64)
+    mask = _bcmask(prob)
+    X = np.zeros_like(B)
+    assert de.de_solve_multi(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
+                             _ptr(mask), _ptr(xyz), 64, prec, nrhs, _ptr(B),
+                             _ptr(X)) == 0
+    for r in range(nrhs):
+        b = np.ascontiguousarray(B[r])
+        x = np.zeros(N)
+        assert de.de_solve(n, bs, _ptr(rowp), _ptr(cols), _ptr(vals),
+                           _ptr(mask), _ptr(xyz), 64, prec, _ptr(b),
+                           _ptr(x)) == 0
+        assert np.array_equal(X[r], x)
