@@ -244,12 +244,18 @@ int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 double *eta, void *stream);
 /* The same for nrhs right-hand sides back to back, refined together (up to
    four per pass over the factor) with the stopping test applied to each:
-   one that has stopped keeps its iterate while the others go on.  steps
-   and eta (may be NULL) are arrays of nrhs entries; TG_ERR_NOCONV when any
-   right-hand side did not reach tol.  b and x must not overlap. */
+   one that has stopped keeps its iterate while the others go on.  ftol > 0
+   adds a forward test: a right-hand side has converged once a step's
+   correction is at most ftol ||x||_inf (its error is then about ftol times
+   the contraction of one step, below ftol), for callers that need the
+   solution to a stated accuracy rather than to FP64 rounding; ftol = 0
+   keeps the backward-error test alone.  steps and eta (may be NULL) are
+   arrays of nrhs entries; TG_ERR_NOCONV when any right-hand side did not
+   converge.  b and x must not overlap. */
 int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
                                   double *x, int max_steps, double tol,
-                                  int *steps, double *eta, void *stream);
+                                  double ftol, int *steps, double *eta,
+                                  void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

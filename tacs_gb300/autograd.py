@@ -101,9 +101,7 @@ class StaticSolver:
         factorisation one load case at a time (exact, 0 iterations)."""
         if self.direct is None:
             return self.ksm.solve_multi(B)
-        X = torch.empty_like(B)
-        for lc in range(B.shape[0]):
-            self.direct.solve(B[lc], X[lc])
+        X = self.direct.solve(B.contiguous())
         nsys = B.shape[0] * (self.model.nseg if self.segments else 1)
         return (X, np.zeros(nsys, np.int32), np.ones(nsys, np.int32),
                 np.zeros(nsys), 1)

@@ -22,10 +22,10 @@ int grid_1d(size_t n) {
 
 template <class T>
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
-                                  int count, const double *A, int nchild,
-                                  int ychunks, cudaStream_t s) {
+                                  int count, const double *A, int zchunks,
+                                  int nchild, int ychunks, cudaStream_t s) {
   if (count <= 0) return;
-  direct_zero_kernel<T><<<count, 256, 0, s>>>(v, sn, count);
+  direct_zero_kernel<T><<<dim3(count, zchunks), 256, 0, s>>>(v, sn, count);
   direct_assemble_kernel<T><<<count, 256, 0, s>>>(v, sn, count, A);
   if (ychunks > 0)
     for (int k = 0; k < nchild; k++)
@@ -40,18 +40,27 @@ void launch_direct_factor_small(const DirectView &v, const int *sn,
   direct_factor_small_kernel<T><<<count, 256, 0, s>>>(v, sn, count, fail);
 }
 
+size_t direct_panel_smem(size_t elem) {
+  return elem * kDirectTrsmRows * (kDirectPanel + 1);
+}
+
 template <class T>
 void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                               const int *tprefix, int tiles,
                               const int *rprefix, int rblocks, int k0,
-                              int *fail, cudaStream_t s) {
+                              int tile, int *fail, cudaStream_t s) {
   if (count <= 0) return;
   direct_panel_kernel<T><<<count, 256, 0, s>>>(v, sn, count, k0, fail);
   if (rblocks > 0)
-    direct_trsm_kernel<T><<<rblocks, 256, 0, s>>>(v, sn, rprefix, count, k0);
-  if (tiles > 0)
-    direct_trailing_kernel<T><<<tiles, 256, 0, s>>>(v, sn, tprefix, count,
-                                                     k0);
+    direct_trsm_kernel<T><<<rblocks, 256, direct_panel_smem(sizeof(T)), s>>>(
+        v, sn, rprefix, count, k0);
+  if (tiles <= 0) return;
+  if (tile == 64)
+    direct_trailing_kernel<T, 64><<<tiles, 256, 0, s>>>(v, sn, tprefix,
+                                                         count, k0);
+  else
+    direct_trailing_kernel<T, 32><<<tiles, 256, 0, s>>>(v, sn, tprefix,
+                                                         count, k0);
 }
 
 // the solves' kernels for NR = 1, 2 or 4 right-hand sides at once
@@ -106,7 +115,7 @@ void launch_direct_backward(const DirectView &v, const int *sn, int count,
 size_t direct_cluster_smem(int max_front, int nr, size_t elem) {
   const int nbk = (max_front + 31) / 32;
   const int mine = (nbk + kDirectSolveCluster - 1) / kDirectSolveCluster;
-  return elem * ((size_t)mine * 32 * nr + kDirectSolveDiag);
+  return elem * ((size_t)mine * 32 * nr);
 }
 
 template <class K, class... Args>
@@ -246,6 +255,19 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
   if (plain_front <= set_plain[dev] && cluster_front <= set_cluster[dev] &&
       max_nr <= set_nr[dev])
     return cudaSuccess;
+  if (set_nr[dev] == 0) {  // first call on this device: the row solves
+    const size_t pb = direct_panel_smem(sizeof(double));
+    if ((e = cudaFuncSetAttribute(
+             (const void *)direct_trsm_kernel<double>,
+             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pb)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaFuncSetAttribute(
+             (const void *)direct_trsm_kernel<float>,
+             cudaFuncAttributeMaxDynamicSharedMemorySize,
+             (int)direct_panel_smem(sizeof(float)))) != cudaSuccess)
+      return e;
+  }
   const int pf = std::max(plain_front, set_plain[dev]);
   const int cf = std::max(cluster_front, set_cluster[dev]);
   const int mn = std::max(max_nr, set_nr[dev]);
@@ -269,14 +291,14 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
   template void launch_direct_level_assemble<T>(const DirectView &,        \
                                                 const int *, int,          \
                                                 const double *, int, int,  \
-                                                cudaStream_t);             \
+                                                int, cudaStream_t);        \
   template void launch_direct_factor_small<T>(const DirectView &,          \
                                               const int *, int, int *,     \
                                               cudaStream_t);               \
   template void launch_direct_panel_step<T>(const DirectView &, const int *, \
                                             int, const int *, int,           \
-                                            const int *, int, int, int *,    \
-                                            cudaStream_t);                   \
+                                            const int *, int, int, int,      \
+                                            int *, cudaStream_t);            \
   template void launch_direct_forward<T>(const DirectView &, const int *,  \
                                          int, int, int, T *, T *,          \
                                          cudaStream_t);                    \

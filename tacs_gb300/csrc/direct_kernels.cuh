@@ -70,6 +70,13 @@ __device__ __forceinline__ float *dk_store(const DirectView &v, bool pool,
   return pool ? v.pool32 : v.lstore32;
 }
 
+__device__ __forceinline__ double *dk_dinv(const DirectView &v, double *) {
+  return v.dinv;
+}
+__device__ __forceinline__ float *dk_dinv(const DirectView &v, float *) {
+  return v.dinv32;
+}
+
 template <class T>
 __device__ __forceinline__ Front<T> front_of(const DirectView &v, int s) {
   Front<T> f;
@@ -83,17 +90,23 @@ __device__ __forceinline__ Front<T> front_of(const DirectView &v, int s) {
   return f;
 }
 
-// zero the fronts of the level's supernodes (one CTA each)
+// zero the fronts of the level's supernodes: front blockIdx.x, entries
+// [blockIdx.y kZeroChunk, (blockIdx.y + 1) kZeroChunk) of its panel and
+// update matrix taken as one range (the grid's y extent covers the
+// level's largest front)
+constexpr int kZeroChunk = kDirectZeroChunk;
 template <class T>
 __global__ void __launch_bounds__(256)
     direct_zero_kernel(DirectView v, const int *__restrict__ sn, int count) {
   if ((int)blockIdx.x >= count) return;
   const Front<T> f = front_of<T>(v, sn[blockIdx.x]);
   const size_t npan = (size_t)f.M * f.C;
-  for (size_t k = threadIdx.x; k < npan; k += blockDim.x) f.lp[k] = 0.0;
-  if (f.up) {
-    const size_t nu = (size_t)(f.M - f.C) * (f.M - f.C);
-    for (size_t k = threadIdx.x; k < nu; k += blockDim.x) f.up[k] = 0.0;
+  const size_t nu = f.up ? (size_t)(f.M - f.C) * (f.M - f.C) : 0;
+  const size_t lo = (size_t)blockIdx.y * kZeroChunk;
+  const size_t hi = lo + kZeroChunk < npan + nu ? lo + kZeroChunk : npan + nu;
+  for (size_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+    if (k < npan) f.lp[k] = T(0);
+    else f.up[k - npan] = T(0);
   }
 }
 
@@ -203,9 +216,10 @@ __global__ void __launch_bounds__(256)
 // Large fronts, in panel steps batched over the large fronts of a level
 // (direct::panel_steps).  A step has three launches: this kernel factors
 // the nb x nb diagonal block of columns [k0, k0 + nb) of front
-// sn[blockIdx.x] (nb = min(kPanel, C - k0) > 0, one CTA, right-looking);
-// direct_trsm_kernel solves the rows below against it; the trailing
-// kernel updates the rest of the front.
+// sn[blockIdx.x] (nb = min(kPanel, C - k0) > 0), staged in shared memory
+// and factored by one warp (right-looking, the operations of the one-CTA
+// kernel in its order); direct_trsm_kernel solves the rows below against
+// it; the trailing kernel updates the rest of the front.
 constexpr int kTile = kDirectTile, kPanel = kDirectPanel;
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -215,44 +229,75 @@ __global__ void __launch_bounds__(256)
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
   const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
-  __shared__ T piv;
-  for (int k = k0; k < k0 + nb; k++) {
-    if (threadIdx.x == 0) {
-      const T d = f.at(k, k);
-      if (!(d > 0.0) || !dk_isfinite(d)) {
-        atomicCAS(fail, 0, s + 1);
-        piv = 1.0;
-      } else {
-        piv = dk_sqrt(d);
+  __shared__ T Ld[kPanel][kPanel + 1];
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    Ld[r][c] = c <= r ? f.at(k0 + r, k0 + c) : T(0);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
+    for (int k = 0; k < nb; k++) {
+      if (threadIdx.x == 0) {
+        const T d = Ld[k][k];
+        if (!(d > 0.0) || !dk_isfinite(d)) {
+          atomicCAS(fail, 0, s + 1);
+          Ld[k][k] = T(1);
+        } else {
+          Ld[k][k] = dk_sqrt(d);
+        }
       }
-      f.at(k, k) = piv;
+      __syncwarp();
+      const T inv = T(1) / Ld[k][k];
+      for (int i = k + 1 + threadIdx.x; i < nb; i += ls) Ld[i][k] *= inv;
+      __syncwarp();
+      for (int i = k + 1 + threadIdx.x; i < nb; i += ls)
+        for (int j = k + 1; j <= i; j++) Ld[i][j] -= Ld[i][k] * Ld[j][k];
+      __syncwarp();
     }
-    __syncthreads();
-    const T inv = T(1) / piv;
-    const int kend = k0 + nb;
-    for (int i = k + 1 + threadIdx.x; i < kend; i += blockDim.x)
-      f.at(i, k) *= inv;
-    __syncthreads();
-    // update the rest of the diagonal block's columns (k, k0 + nb)
-    const int w = kend - k - 1;
-    if (w > 0) {
-      const int rows = kend - k - 1;
-      const size_t total = (size_t)rows * w;
-      for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
-        const int i = k + 1 + (int)(t / w), j = k + 1 + (int)(t % w);
-        if (j > i) continue;
-        f.at(i, j) -= f.at(i, k) * f.at(j, k);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    if (c <= r) f.at(k0 + r, k0 + c) = Ld[r][c];
+  }
+  if (v.dinv_off[s] < 0) return;
+  // X = L^-1 of the factored block, row by row: X(i, :) = (e_i -
+  // sum_{q < i} L(i, q) X(q, :)) / L(i, i) (warp 0, lane j on column j);
+  // stored row-major in a 32 x 32 slot, zero elsewhere
+  __shared__ T X[kPanel][kPanel + 1];
+  if (threadIdx.x < 32) {
+    const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
+    for (int i = 0; i < nb; i++) {
+      for (int j = threadIdx.x; j < kPanel; j += ls) {
+        T acc = i == j ? T(1) : T(0);
+        if (j <= i) {
+          for (int q = j; q < i; q++) acc -= Ld[i][q] * X[q][j];
+          acc = acc / Ld[i][i];
+        } else {
+          acc = T(0);
+        }
+        X[i][j] = acc;
       }
+      __syncwarp();
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  T *out = dk_dinv(v, (T *)nullptr) + v.dinv_off[s] + (size_t)(k0 / kPanel) *
+                                                         kPanel * kPanel;
+  for (int t = threadIdx.x; t < kPanel * kPanel; t += blockDim.x) {
+    const int r = t / kPanel, c = t - kPanel * (t / kPanel);
+    out[t] = r < nb ? X[r][c] : T(0);
   }
 }
 
 // Rows below a panel's diagonal block: L21 = A21 L11^-T, row by row
-// (forward substitution against the diagonal block, held in shared
-// memory), one thread per row, kTrsmRows rows per CTA; CTA b belongs to
-// the last front f with rprefix[f] <= b and takes its row block
-// b - rprefix[f].
+// (forward substitution against the factored diagonal block, held in
+// shared memory), one thread per row, kTrsmRows rows per CTA; CTA b
+// belongs to the last front f with rprefix[f] <= b and takes its row block
+// b - rprefix[f].  The rows are staged through shared memory, so that
+// global loads and stores run along contiguous panel rows.  Dynamic shared
+// memory: kTrsmRows x (kPanel + 1) entries.
 constexpr int kTrsmRows = kDirectTrsmRows;
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -269,40 +314,51 @@ __global__ void __launch_bounds__(256)
   const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
   const int r0 = k0 + nb + (b - rprefix[lo]) * kTrsmRows;
   const int r1 = r0 + kTrsmRows < f.M ? r0 + kTrsmRows : f.M;
+  const int nr = r1 > r0 ? r1 - r0 : 0;
   __shared__ T Ld[kPanel][kPanel + 1];
+  DK_DYN_SMEM(T, X);  // kTrsmRows x (kPanel + 1)
+  constexpr int P = kPanel + 1;
   for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-    const int r = t / nb, c = t % nb;
+    const int r = t / nb, c = t - nb * (t / nb);
     Ld[r][c] = c <= r ? f.at(k0 + r, k0 + c) : T(0);
   }
+  for (int t = threadIdx.x; t < nr * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    X[r * P + c] = f.lp[(size_t)(r0 + r) * f.C + k0 + c];
+  }
   __syncthreads();
-  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-    T x[kPanel];
-#pragma unroll
-    for (int k = 0; k < kPanel; k++) {
-      if (k < nb) {
-        T acc = f.at(i, k0 + k);
-#pragma unroll
-        for (int q = 0; q < kPanel; q++)
-          if (q < k) acc -= x[q] * Ld[k][q];
-        x[k] = acc / Ld[k][k];
-      }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    T *xi = X + i * P;
+    for (int k = 0; k < nb; k++) {
+      T acc = xi[k];
+      for (int q = 0; q < k; q++) acc -= xi[q] * Ld[k][q];
+      xi[k] = acc / Ld[k][k];
     }
-#pragma unroll
-    for (int k = 0; k < kPanel; k++)
-      if (k < nb) f.at(i, k0 + k) = x[k];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nr * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    f.lp[(size_t)(r0 + r) * f.C + k0 + c] = X[r * P + c];
   }
 }
 
 // Trailing update after a panel step: F(i, j) -= sum_q F(i, q) F(j, q)
-// over the panel's columns q, for k1 <= j <= i < M, in 32 x 32 tiles.  One
-// CTA per lower-triangular tile of all the step's fronts: CTA b belongs to
-// the last front f with tprefix[f] <= b (fronts without tiles are skipped
-// that way) and is its tile tau = b - tprefix[f] = ti (ti + 1) / 2 + tj.
-template <class T>
+// over the panel's columns q, for k1 <= j <= i < M, in TILE x TILE tiles
+// (32 for the FP64 factorisation, bound by the FP64 pipe; 64 for the FP32
+// one, where shared-memory loads per FMA set the pace).  One CTA per
+// lower-triangular tile of all the step's fronts: CTA b belongs to the
+// last front f with tprefix[f] <= b (fronts without tiles are skipped that
+// way) and is its tile tau = b - tprefix[f] = ti (ti + 1) / 2 + tj.  Thread
+// (ty, tx) = (t / 16, t % 16) owns the R x R entries (ty + 16 a, tx + 16 b)
+// of the tile (R = TILE / 16): one pass over q loads 2 R operands for R^2
+// products, and each entry keeps its own summation order over q (the
+// result does not depend on TILE).
+template <class T, int TILE>
 __global__ void __launch_bounds__(256)
     direct_trailing_kernel(DirectView v, const int *__restrict__ sn,
                            const int *__restrict__ tprefix, int count,
                            int k0) {
+  constexpr int R = TILE / 16;
   const int b = blockIdx.x;
   int lo = 0, hi = count - 1;
   while (lo < hi) {
@@ -318,36 +374,43 @@ __global__ void __launch_bounds__(256)
   while (ti * (ti + 1) / 2 > tau) ti--;
   const int tj = tau - ti * (ti + 1) / 2;
   const int k1 = k0 + nb;
-  const int i0 = k1 + ti * kTile, j0 = k1 + tj * kTile;
+  const int i0 = k1 + ti * TILE, j0 = k1 + tj * TILE;
   if (i0 >= f.M || j0 >= f.M) return;
-  __shared__ T Ai[kTile][kPanel + 1], Aj[kTile][kPanel + 1];
-  for (int t = threadIdx.x; t < kTile * nb; t += blockDim.x) {
+  __shared__ T Ai[TILE][kPanel + 1], Aj[TILE][kPanel + 1];
+  for (int t = threadIdx.x; t < TILE * nb; t += blockDim.x) {
     const int r = t / nb, q = t % nb;
-    Ai[r][q] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : 0.0;
-    Aj[r][q] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : 0.0;
+    Ai[r][q] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : T(0);
+    Aj[r][q] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : T(0);
   }
   __syncthreads();
-  // a group owns rows (r, r + 16) x columns (c, c + 16) of the tile: one
-  // pass over q loads 4 operands for 4 products (half the shared-memory
-  // loads per FMA of one entry per pass; each entry keeps its own
-  // summation order over q)
-  constexpr int kHalf = kTile / 2;
-  for (int g = threadIdx.x; g < kHalf * kHalf; g += blockDim.x) {
-    const int r = g / kHalf, c = g % kHalf;
-    T a00 = 0, a01 = 0, a10 = 0, a11 = 0;
+  for (int g = threadIdx.x; g < 256; g += blockDim.x) {
+    const int ty = g / 16, tx = g % 16;
+    T acc[R][R];
+#pragma unroll
+    for (int a = 0; a < R; a++)
+#pragma unroll
+      for (int c = 0; c < R; c++) acc[a][c] = 0;
     for (int q = 0; q < nb; q++) {
-      const T x0 = Ai[r][q], x1 = Ai[r + kHalf][q];
-      const T y0 = Aj[c][q], y1 = Aj[c + kHalf][q];
-      a00 += x0 * y0;
-      a01 += x0 * y1;
-      a10 += x1 * y0;
-      a11 += x1 * y1;
+      T x[R], y[R];
+#pragma unroll
+      for (int a = 0; a < R; a++) x[a] = Ai[ty + 16 * a][q];
+#pragma unroll
+      for (int c = 0; c < R; c++) y[c] = Aj[tx + 16 * c][q];
+#pragma unroll
+      for (int a = 0; a < R; a++)
+#pragma unroll
+        for (int c = 0; c < R; c++) acc[a][c] += x[a] * y[c];
     }
-    const int ia = i0 + r, ib = ia + kHalf, ja = j0 + c, jb = ja + kHalf;
-    if (ia < f.M && ja <= ia) f.at(ia, ja) -= a00;
-    if (ia < f.M && jb <= ia) f.at(ia, jb) -= a01;
-    if (ib < f.M && ja <= ib) f.at(ib, ja) -= a10;
-    if (ib < f.M && jb <= ib) f.at(ib, jb) -= a11;
+#pragma unroll
+    for (int a = 0; a < R; a++) {
+      const int i = i0 + ty + 16 * a;
+      if (i >= f.M) continue;
+#pragma unroll
+      for (int c = 0; c < R; c++) {
+        const int j = j0 + tx + 16 * c;
+        if (j <= i) f.at(i, j) -= acc[a][c];
+      }
+    }
   }
 }
 
@@ -538,20 +601,27 @@ __global__ void __launch_bounds__(256)
 }
 
 #ifndef DK_EMULATE
-// Large fronts: one thread-block cluster of kDirectSolveCluster CTAs per
-// front, so that the front's triangular solves use that many SMs' FP64
-// pipes (one CTA per front leaves the top of the tree, a handful of fronts
-// with thousands of rows, on one SM each).  The front's rows are dealt out
-// in 32-row blocks: block b belongs to rank b % nr and sits in that CTA's
-// shared memory at slot (b / nr) * 32.  For column block kb its owner
-// solves the staged diagonal block and publishes the 32 x NR values; after
-// one hardware cluster barrier every rank reads them through distributed
-// shared memory and updates its own rows (forward: rows below; backward:
-// columns before).  The control flow is the same in every CTA of a
-// cluster (each cluster exits together, and every barrier is reached by
-// all of its CTAs); a final barrier keeps each CTA's shared memory alive
-// until the others are done reading it.  Dynamic shared memory: the owned
-// rows (rounded up to whole blocks) x NR, then the diagonal block.
+// Large fronts: one thread-block cluster of kDirectSolveCluster CTAs (256
+// threads each) per front, so that the front's triangular solves use that
+// many SMs (one CTA per front leaves the top of the tree, a handful of
+// fronts with thousands of rows, on one SM each).  The front's rows are
+// dealt out in 32-row blocks: block b belongs to rank b % nr and sits in
+// that CTA's shared memory at slot (b / nr) * 32.  Column block k is
+// solved by its owner with the inverse of its diagonal block (kept by the
+// factorisation, dinv: a 32 x 32 product instead of 32 dependent steps)
+// and published in shared memory; the others read it through distributed
+// shared memory after the cluster barrier.  The solve is pipelined one
+// block ahead: once block k is known, the owner of block k + 1 first
+// applies it to its 32 rows (forward) or columns (backward) of block k + 1,
+// solves and publishes that block and arrives at the barrier, and only
+// then applies block k to the rest of its rows; the others arrive as soon
+// as they have read block k.  So the chain of dependent blocks costs one
+// barrier, one 32-row update and one 32 x 32 product per block, and the
+// bulk of the work runs beside it.  Every CTA of a cluster executes the
+// same sequence of barrier arrivals and waits (block counts depend on the
+// front only); a final barrier keeps each CTA's shared memory alive until
+// the others are done reading it.  Dynamic shared memory: the owned rows
+// (rounded up to whole blocks) x NR.
 struct ClusterRows {
   int nr, rank;
   __device__ __forceinline__ bool owns(int r) const {
@@ -571,6 +641,88 @@ struct ClusterRows {
   }
 };
 
+// a 32 x 32 inverse block through registers into shared memory (256
+// threads, 4 entries each, coalesced): load early, store when needed
+template <class T>
+__device__ __forceinline__ void dk_inv_load(T (&pre)[4], const T *src) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) pre[q] = src[threadIdx.x + 256 * q];
+}
+template <class T>
+__device__ __forceinline__ void dk_inv_store(const T (&pre)[4],
+                                             T (*Ls)[33]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int t = threadIdx.x + 256 * q;
+    Ls[t >> 5][t & 31] = pre[q];
+  }
+}
+
+// z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < 32 of a 32-row
+// group with bit i of `valid` set, by one warp: lane c multiplies column c
+// of every row (each row a coalesced load), then a butterfly of shuffles
+// sums the 32 rows' products so that lane i holds row i's sum (31 shuffles
+// for 32 rows).  L0: row r0's column kb; ldl: the panel's row stride;
+// zrow(i): row i's NR entries of z.
+template <class T, int NR, class ZRow>
+__device__ __forceinline__ void dk_warp_rows32(const T *L0, size_t ldl,
+                                               int nb, const T *zk,
+                                               unsigned valid, ZRow zrow) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (int q = 0; q < NR; q++) {
+    const T zc = lane < nb ? zk[lane * NR + q] : T(0);
+    T v[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+      v[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane] * zc
+                                              : T(0);
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+      const bool up = (lane & h) != 0;
+#pragma unroll
+      for (int i = 0; i < h; i++) {
+        const T send = up ? v[i] : v[i + h];
+        const T keep = up ? v[i + h] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+      }
+    }
+    if ((valid >> lane) & 1u) zrow(lane)[q] -= v[0];
+  }
+}
+
+// Block solve with the staged inverse X (warp 0): forward z = X z, or
+// backward z = X^T z, on the block's nb entries; the result also goes to
+// the published buffer zbuf
+template <class T, int NR, bool kTranspose>
+__device__ __forceinline__ void dk_inv_solve(const T (*X)[33], int nb, T *z,
+                                             T *zbuf) {
+  if (threadIdx.x >= 32) return;
+  const int i = threadIdx.x;
+  T out[NR];
+#pragma unroll
+  for (int q = 0; q < NR; q++) out[q] = 0;
+  if (i < nb) {
+    if (kTranspose) {
+      for (int j = i; j < nb; j++) {
+        const T a = X[j][i];
+#pragma unroll
+        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
+      }
+    } else {
+      for (int j = 0; j <= i; j++) {
+        const T a = X[i][j];
+#pragma unroll
+        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
+      }
+    }
+  }
+  __syncwarp();
+  if (i < nb)
+#pragma unroll
+    for (int q = 0; q < NR; q++) z[i * NR + q] = zbuf[i * NR + q] = out[q];
+}
+
 template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
@@ -581,13 +733,16 @@ __global__ void __launch_bounds__(256)
   const int fi = (int)blockIdx.x / cr.nr;  // the same in the whole cluster
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
-  __shared__ T zb[32 * NR], zk[32 * NR];
+  __shared__ T zb[2][32 * NR], zk[32 * NR];
+  __shared__ T Ls[32][33];
   const int s = sn[fi];
   const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const int nown = cr.count(f.M);
-  T *D = z + (size_t)nown * NR;
+  const T *inv = dk_dinv(v, (T *)nullptr) + v.dinv_off[s];
+  const int nblk = (f.C + 31) >> 5;
+  const int warp = (int)threadIdx.x >> 5, nwarp = (int)blockDim.x >> 5;
   for (int t = threadIdx.x; t < nown * NR; t += blockDim.x) {
     const int i = cr.row(t / NR), r = t - NR * (t / NR);
     z[t] = (i < f.C) ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
@@ -606,36 +761,54 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
   }
-  for (int kb = 0; kb < f.C; kb += 32) {
-    const int nb = f.C - kb < 32 ? f.C - kb : 32;
-    const int owner = (kb >> 5) % cr.nr;
-    if (owner == cr.rank) {
-      dk_stage_block(f, kb, nb, D);
-      __syncthreads();
-      dk_block_solve<T, false, NR>(D, nb, z + cr.slot(kb) * NR);
-      __syncthreads();
-      for (int t = threadIdx.x; t < nb * NR; t += blockDim.x)
-        zb[t] = z[cr.slot(kb) * NR + t];
-    }
-    cl.sync();
-    const T *src = cl.map_shared_rank(zb, owner);
+  T pre[4];
+  if (cr.rank == 0) {  // block 0: its rows are complete
+    dk_inv_load(pre, inv);
+    dk_inv_store(pre, Ls);
+    __syncthreads();
+    dk_inv_solve<T, NR, false>(Ls, f.C < 32 ? f.C : 32, z, zb[0]);
+    __syncthreads();
+  }
+  cl.barrier_arrive();
+  for (int k = 0; k < nblk; k++) {
+    const int kb = k << 5, nb = f.C - kb < 32 ? f.C - kb : 32;
+    const int k1 = k + 1, r1 = k1 << 5;
+    const bool next_mine = k1 < nblk && k1 % cr.nr == cr.rank;
+    const int nb1 = next_mine ? (f.C - r1 < 32 ? f.C - r1 : 32) : 0;
+    if (next_mine) dk_inv_load(pre, inv + (size_t)k1 * 1024);
+    cl.barrier_wait();
+    const T *src = cl.map_shared_rank(&zb[k & 1][0], k % cr.nr);
     for (int t = threadIdx.x; t < nb * NR; t += blockDim.x) zk[t] = src[t];
     __syncthreads();
-    // own rows below the block: z_r -= L(r, kb .. kb+nb) zk
-    for (int t = threadIdx.x; t < nown; t += blockDim.x) {
-      const int r = cr.row(t);
-      if (r < kb + nb || r >= f.M) continue;
-      const T *Lr = f.lp + (size_t)r * f.C + kb;
-      T acc[NR];
-#pragma unroll
-      for (int q = 0; q < NR; q++) acc[q] = 0;
-      for (int c = 0; c < nb; c++) {
-        const T l = Lr[c];
-#pragma unroll
-        for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
+    if (next_mine) {
+      dk_inv_store(pre, Ls);
+      if (warp == 0) {
+        T *zr1 = z + (size_t)cr.slot(r1) * NR;
+        dk_warp_rows32<T, NR>(
+            f.lp + (size_t)r1 * f.C + kb, f.C, nb, zk,
+            nb1 == 32 ? 0xffffffffu : (1u << nb1) - 1u,
+            [&](int i) { return zr1 + i * NR; });
       }
-#pragma unroll
-      for (int q = 0; q < NR; q++) z[t * NR + q] -= acc[q];
+      __syncthreads();
+      dk_inv_solve<T, NR, false>(Ls, nb1, z + (size_t)cr.slot(r1) * NR,
+                                 zb[k1 & 1]);
+      __syncthreads();
+    }
+    if (k1 < nblk) cl.barrier_arrive();
+    // the rest of this rank's rows below block k, a 32-row block per warp
+    for (int g = warp; g < (nown >> 5); g += nwarp) {
+      const int r0 = cr.row(g << 5);
+      if (r0 + 32 <= kb + nb || r0 >= f.M) continue;
+      unsigned valid = 0;
+      for (int i = 0; i < 32; i++) {
+        const int r = r0 + i;
+        const bool ahead = r >= r1 && r < r1 + nb1;  // done ahead
+        if (r >= kb + nb && r < f.M && !ahead) valid |= 1u << i;
+      }
+      if (!valid) continue;
+      T *zg = z + (size_t)(g << 5) * NR;
+      dk_warp_rows32<T, NR>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk, valid,
+                            [&](int i) { return zg + i * NR; });
     }
     __syncthreads();
   }
@@ -658,13 +831,15 @@ __global__ void __launch_bounds__(256)
   const int fi = (int)blockIdx.x / cr.nr;
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
-  __shared__ T zb[32 * NR], zk[32 * NR];
+  __shared__ T zb[2][32 * NR], zk[32 * NR];
+  __shared__ T Ls[32][33];
   const int s = sn[fi];
   const Front<T> f = front_of<T>(v, s);
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const int nown = cr.count(f.M);
-  T *D = z + (size_t)nown * NR;
+  const T *inv = dk_dinv(v, (T *)nullptr) + v.dinv_off[s];
+  const int nblk = (f.C + 31) >> 5;
   // own rows of the triangle: y1 - L21^T x2 (x2 final, from the ancestors)
   for (int t = threadIdx.x; t < nown; t += blockDim.x) {
     const int j = cr.row(t);
@@ -683,32 +858,61 @@ __global__ void __launch_bounds__(256)
     for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - acc[q];
   }
   __syncthreads();
-  for (int kb = ((f.C - 1) >> 5) << 5; kb >= 0; kb -= 32) {
-    const int nb = f.C - kb < 32 ? f.C - kb : 32;
-    const int owner = (kb >> 5) % cr.nr;
-    if (owner == cr.rank) {
-      dk_stage_block(f, kb, nb, D);
-      __syncthreads();
-      dk_block_solve<T, true, NR>(D, nb, z + cr.slot(kb) * NR);
-      __syncthreads();
-      for (int t = threadIdx.x; t < nb * NR; t += blockDim.x)
-        zb[t] = z[cr.slot(kb) * NR + t];
-    }
-    cl.sync();
-    const T *src = cl.map_shared_rank(zb, owner);
+  T pre[4];
+  const int kt = nblk - 1;
+  if (kt % cr.nr == cr.rank) {  // the last block: its rows are complete
+    dk_inv_load(pre, inv + (size_t)kt * 1024);
+    dk_inv_store(pre, Ls);
+    __syncthreads();
+    dk_inv_solve<T, NR, true>(Ls, f.C - (kt << 5),
+                              z + (size_t)cr.slot(kt << 5) * NR, zb[kt & 1]);
+    __syncthreads();
+  }
+  cl.barrier_arrive();
+  for (int k = kt; k >= 0; k--) {
+    const int kb = k << 5, nb = f.C - kb < 32 ? f.C - kb : 32;
+    const int k1 = k - 1, r1 = k1 << 5;
+    const bool next_mine = k1 >= 0 && k1 % cr.nr == cr.rank;
+    if (next_mine) dk_inv_load(pre, inv + (size_t)k1 * 1024);
+    cl.barrier_wait();
+    const T *src = cl.map_shared_rank(&zb[k & 1][0], k % cr.nr);
     for (int t = threadIdx.x; t < nb * NR; t += blockDim.x) zk[t] = src[t];
     __syncthreads();
-    // own columns before the block: z_j -= sum_k L(kb + k, j) zk_k
+    if (next_mine) {
+      dk_inv_store(pre, Ls);
+      // this rank's columns of block k - 1 (a whole block: 32)
+      if (threadIdx.x < 32) {
+        const int j = r1 + (int)threadIdx.x;
+        T acc[NR];
+#pragma unroll
+        for (int q = 0; q < NR; q++) acc[q] = 0;
+        for (int c = 0; c < nb; c++) {
+          const T l = f.lp[(size_t)(kb + c) * f.C + j];
+#pragma unroll
+          for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
+        }
+        T *zj = z + (size_t)cr.slot(j) * NR;
+#pragma unroll
+        for (int q = 0; q < NR; q++) zj[q] -= acc[q];
+      }
+      __syncthreads();
+      dk_inv_solve<T, NR, true>(Ls, 32, z + (size_t)cr.slot(r1) * NR,
+                                zb[k1 & 1]);
+      __syncthreads();
+    }
+    if (k1 >= 0) cl.barrier_arrive();
+    // the rest of this rank's columns before block k
     for (int t = threadIdx.x; t < nown; t += blockDim.x) {
       const int j = cr.row(t);
       if (j >= kb) continue;
+      if (next_mine && j >= r1) continue;  // done ahead
       T acc[NR];
 #pragma unroll
       for (int q = 0; q < NR; q++) acc[q] = 0;
-      for (int k = 0; k < nb; k++) {
-        const T l = f.lp[(size_t)(kb + k) * f.C + j];
+      for (int c = 0; c < nb; c++) {
+        const T l = f.lp[(size_t)(kb + c) * f.C + j];
 #pragma unroll
-        for (int q = 0; q < NR; q++) acc[q] += l * zk[k * NR + q];
+        for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
       }
 #pragma unroll
       for (int q = 0; q < NR; q++) z[t * NR + q] -= acc[q];

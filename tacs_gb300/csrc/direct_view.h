@@ -7,10 +7,13 @@
 
 namespace tg {
 
-// panel width and trailing tile of the large fronts' factorisation
-constexpr int kDirectPanel = 32, kDirectTile = 32;
+// panel width and trailing tile of the large fronts' factorisation (the
+// FP32 factorisation uses kDirectTile32)
+constexpr int kDirectPanel = 32, kDirectTile = 32, kDirectTile32 = 64;
 // rows of a panel's off-diagonal part solved by one CTA (one per thread)
 constexpr int kDirectTrsmRows = 256;
+// entries of a front zeroed by one CTA
+constexpr int kDirectZeroChunk = 16384;
 // column block of the triangular solves, and the shared memory of its
 // staged diagonal block (rows padded to kDirectSolveBlock + 1 entries)
 constexpr int kDirectSolveBlock = 32;
@@ -31,6 +34,13 @@ struct DirectView {
   const int64_t *l_off, *u_off, *v_off;
   double *lstore, *pool;     // FP64 factor panels and update pool
   float *lstore32, *pool32;  // the same storage for an FP32 factorisation
+  // inverses of the 32 x 32 diagonal blocks of the fronts solved by
+  // thread-block clusters (row-major, zero above the diagonal and beyond
+  // the block): panel p of supernode s at dinv_off[s] + p * 1024, or
+  // dinv_off[s] = -1 (none kept)
+  const int64_t *dinv_off;
+  double *dinv;
+  float *dinv32;
 };
 
 }  // namespace tg

@@ -16,6 +16,7 @@
 // so do the node-coordinate sensitivities (shell_xpt_kernel), which run the
 // same kinematics in dual arithmetic.
 #include <cmath>
+#include <mutex>
 
 #include "dual.cuh"
 #include "tg_internal.h"
@@ -380,6 +381,176 @@ __global__ void __launch_bounds__(WARPS * 32)
 }
 
 // ---------------------------------------------------------------------------
+// Fixed-geometry forms of the three kernels above.  With the strain
+// operators B_q and detXd_q in the class table (m.geo_B: 4 x 9 x 24 then
+// 4 dets per geometry class) an element needs no kinematics, so it is
+// owned by 4 lanes -- lane 4 j + q on Gauss point q of the warp's j-th
+// element, 8 elements per warp -- and every lane does its point's FP64
+// work (the warp-per-element forms leave 28 of 32 lanes idle there).  Each
+// quantity is formed with the operations of the forms above, in their
+// order (the sums over the 4 points included).
+constexpr int kGeoWarps = 4;
+
+__device__ __forceinline__ void geo_load_u(const MeshView &m, int e,
+                                           const double *vars, double *u) {
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int n = m.conn[4 * e + a];
+#pragma unroll
+    for (int i = 0; i < 6; i++) u[6 * a + i] = vars ? vars[6 * n + i] : 0.0;
+  }
+}
+
+// e = B_q v (9 strains; B_q row-major 9 x 24)
+__device__ __forceinline__ void geo_strains(const double *Bq,
+                                            const double *v, double *e) {
+#pragma unroll 1
+  for (int r = 0; r < 9; r++) {
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 24; k++) acc += Bq[r * 24 + k] * v[k];
+    e[r] = acc;
+  }
+}
+
+// ((c0 + c1) + c2) + c3 over the element's 4 lanes, on lane q = 0
+__device__ __forceinline__ double geo_point_sum(double c) {
+  const double c1 = __shfl_down_sync(0xffffffffu, c, 1);
+  const double c2 = __shfl_down_sync(0xffffffffu, c, 2);
+  const double c3 = __shfl_down_sync(0xffffffffu, c, 3);
+  return ((c + c1) + c2) + c3;
+}
+
+__global__ void __launch_bounds__(kGeoWarps * 32)
+    shell_points_geo_kernel(ElemParams ep, MeshView m,
+                            const double *__restrict__ vars,
+                            double *__restrict__ elem_fail,
+                            double *__restrict__ elem_wdet,
+                            double *__restrict__ elem_sed) {
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const int gw = blockIdx.x * kGeoWarps + (threadIdx.x >> 5);
+  const int nw = gridDim.x * kGeoWarps;
+  for (int e0 = 8 * gw; e0 < m.nelem; e0 += 8 * nw) {
+    const int e = e0 + (lane >> 2);
+    const bool on = e < m.nelem;
+    double c = 0.0;
+    if (on) {
+      const double *tab = m.geo_B + (size_t)m.geo_cls[e] * 868;
+      double u[24], ev[9];
+      geo_load_u(m, e, vars, u);
+      geo_strains(tab + 216 * q, u, ev);
+      ev[8] = 0.0;
+      const double t = m.thick[e];
+      const ShellStiff cs = shell_stiff(ep, t);
+      double sed = 0.0;
+      for (int r = 0; r < 9; r++) sed += ev[r] * shell_stress_row(cs, ev, r);
+      const FailOut fo = shell_failure(ep, t, ev);
+      const double det = tab[864 + q];
+      elem_fail[4 * (size_t)e + q] = fo.f;
+      elem_wdet[4 * (size_t)e + q] = det;
+      c = det * sed;
+    }
+    const double sum = geo_point_sum(c);
+    if (on && q == 0) elem_sed[e] = sum;
+  }
+}
+
+__global__ void __launch_bounds__(kGeoWarps * 32)
+    shell_sv_geo_kernel(ElemParams ep, MeshView m, ColorRange cr,
+                        const double *__restrict__ vars, int func, KsStats ks,
+                        double alpha, double *__restrict__ dfdu) {
+  // each point's 24 weighted B_q^T g_q terms, summed per dof by its lane
+  __shared__ double vbuf[kGeoWarps][8][4][24];
+  const int lane = threadIdx.x & 31, q = lane & 3, j = lane >> 2;
+  const int w = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kGeoWarps + w;
+  const int nw = gridDim.x * kGeoWarps;
+  for (int i0 = 8 * gw; i0 < cr.count; i0 += 8 * nw) {
+    const bool on = i0 + j < cr.count;
+    const int e = on ? cr.elem_list[i0 + j] : 0;
+    if (on) {
+      const double *tab = m.geo_B + (size_t)m.geo_cls[e] * 868;
+      const double *Bq = tab + 216 * q;
+      const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
+      double u[24], ev[9], g[9], coef;
+      geo_load_u(m, e, vars, u);
+      geo_strains(Bq, u, ev);
+      ev[8] = 0.0;
+      const double t = m.thick[e], det = tab[864 + q];
+      if (func == TG_FUNC_COMPLIANCE) {
+        const ShellStiff cs = shell_stiff(ep, t);
+        for (int r = 0; r < 9; r++) g[r] = 2.0 * shell_stress_row(cs, ev, r);
+        coef = det;
+      } else {
+        const FailOut fo = shell_failure(ep, t, ev);
+        for (int r = 0; r < 6; r++) g[r] = fo.dfde[r];
+        g[6] = g[7] = g[8] = 0.0;
+        coef = exp(kk.weight * (fo.f - kk.max)) / kk.sum * det;
+      }
+      for (int k = 0; k < 24; k++) {
+        double v = 0.0;
+        for (int r = 0; r < 8; r++) v += Bq[r * 24 + k] * g[r];
+        vbuf[w][j][q][k] = coef * v;
+      }
+    }
+    __syncwarp();
+    if (on) {
+      const int node = m.conn[4 * e + q];
+      for (int i = 0; i < 6; i++) {
+        double acc = 0.0;
+        for (int p = 0; p < 4; p++) acc += vbuf[w][j][p][6 * q + i];
+        dfdu[6 * node + i] += alpha * acc;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(kGeoWarps * 32)
+    shell_dv_geo_kernel(ElemParams ep, MeshView m,
+                        const double *__restrict__ vars, int func, KsStats ks,
+                        double coef, const double *__restrict__ psi,
+                        double scale, double *__restrict__ out) {
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const int gw = blockIdx.x * kGeoWarps + (threadIdx.x >> 5);
+  const int nw = gridDim.x * kGeoWarps;
+  for (int e0 = 8 * gw; e0 < m.nelem; e0 += 8 * nw) {
+    const int e = e0 + (lane >> 2);
+    const bool on = e < m.nelem;
+    double acc = 0.0;
+    if (on) {
+      const double *tab = m.geo_B + (size_t)m.geo_cls[e] * 868;
+      const double *Bq = tab + 216 * q;
+      const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
+      const double t = m.thick[e], det = tab[864 + q];
+      double u[24], e9[9];
+      geo_load_u(m, e, vars, u);
+      geo_strains(Bq, u, e9);
+      if (func >= 0) {
+        double ev[9];
+        for (int r = 0; r < 9; r++) ev[r] = e9[r];
+        ev[8] = 0.0;
+        if (func == TG_FUNC_COMPLIANCE) {
+          acc += coef * det * shell_stress_dv(ep, t, ev, ev);
+        } else {
+          const FailOut fo = shell_failure(ep, t, ev);
+          const double dfdq = det * exp(kk.weight * (fo.f - kk.max)) / kk.sum;
+          acc += coef * dfdq * fo.dfdt;
+        }
+      }
+      if (psi) {
+        double w[24], g9[9];
+        geo_load_u(m, e, psi, w);
+        geo_strains(Bq, w, g9);
+        acc += scale * det * shell_stress_dv(ep, t, e9, g9);
+      }
+    }
+    const double sum = geo_point_sum(acc);
+    if (on && q == 0) out[e] = sum;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Node-coordinate sensitivities (TACSAssembler::addXptSens and
 // addAdjointResXptSensProducts, src/TACSAssembler.cpp:4858-4920,5136-5205):
 // per element, d/dX of scale psi^T R_e + coef f_e (shell residual and
@@ -527,19 +698,57 @@ int grid_for(int count, int ctas_per_sm) {
   return need < cap ? need : cap;
 }
 
-// The dynamic shared-memory limit is a per-device attribute of a kernel:
-// set once on each device, kept only once the call succeeded.
+// Per kernel and device: the dynamic shared-memory limit (a per-device
+// attribute of a kernel, set once and kept only once the call succeeded)
+// and the CTAs one SM holds at that footprint, which caps the grid (the
+// element loops are grid-strided, so a resident grid hides the latency of
+// the warp-per-element work best).  Returns the CTAs per SM.
 constexpr int kMaxDevices = 64;
+struct KernelSlot {
+  const void *kernel;
+  int dev;
+  bool attr;
+  int resident;
+};
 template <typename K>
-void prep(K kernel, size_t bytes = sizeof(ShellSmem) * kWarps) {
-  static bool done[kMaxDevices] = {};
+int prep(K kernel, size_t bytes = sizeof(ShellSmem) * kWarps) {
+  static std::mutex mu;
+  static KernelSlot slots[64];
+  static int nslots = 0;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-    return;
-  if (!done[dev] &&
+    return 2;
+  std::lock_guard<std::mutex> lock(mu);
+  KernelSlot *sl = nullptr;
+  for (int i = 0; i < nslots; i++)
+    if (slots[i].kernel == (const void *)kernel && slots[i].dev == dev)
+      sl = &slots[i];
+  if (!sl) {
+    if (nslots == 64) return 2;
+    sl = &slots[nslots++];
+    *sl = KernelSlot{(const void *)kernel, dev, false, 0};
+  }
+  if (!sl->attr &&
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)bytes) == cudaSuccess)
-    done[dev] = true;
+    sl->attr = true;
+  if (sl->attr && !sl->resident) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kWarps * 32,
+                                                      bytes) == cudaSuccess &&
+        nb > 0)
+      sl->resident = nb;
+  }
+  return sl->resident ? sl->resident : 2;
+}
+
+// grid of the fixed-geometry forms: 8 elements per warp, at most the CTAs
+// the SMs hold
+int geo_grid(int count, int ctas_per_sm) {
+  const int per_cta = 8 * kWarps;
+  const int need = (count + per_cta - 1) / per_cta;
+  const int cap = grid_for(1 << 30, ctas_per_sm);
+  return need < 1 ? 1 : (need < cap ? need : cap);
 }
 
 }  // namespace
@@ -549,9 +758,16 @@ void launch_shell_points(const ElemParams &ep, const MeshView &m,
                          double *elem_wdet, double *elem_sed,
                          cudaStream_t s) {
   if (m.nelem <= 0) return;
+  if (m.geo_B) {
+    const int occ = prep(shell_points_geo_kernel, 0);
+    shell_points_geo_kernel<<<geo_grid(m.nelem, occ), kGeoWarps * 32, 0,
+                              s>>>(ep, m, vars, elem_fail, elem_wdet,
+                                   elem_sed);
+    return;
+  }
   auto k = shell_points_kernel<kWarps>;
-  prep(k);
-  k<<<grid_for(m.nelem, 2), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
+  const int occ = prep(k);
+  k<<<grid_for(m.nelem, occ), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
       ep, m, vars, elem_fail, elem_wdet, elem_sed);
 }
 
@@ -560,9 +776,15 @@ void launch_shell_sv_sens(const ElemParams &ep, const MeshView &m,
                           KsStats ks, double alpha, double *dfdu,
                           cudaStream_t s) {
   if (cr.count <= 0) return;
+  if (m.geo_B) {
+    const int occ = prep(shell_sv_geo_kernel, 0);
+    shell_sv_geo_kernel<<<geo_grid(cr.count, occ), kGeoWarps * 32, 0, s>>>(
+        ep, m, cr, vars, func, ks, alpha, dfdu);
+    return;
+  }
   auto k = shell_sv_kernel<kWarps>;
-  prep(k);
-  k<<<grid_for(cr.count, 2), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
+  const int occ = prep(k);
+  k<<<grid_for(cr.count, occ), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
       ep, m, cr, vars, func, ks, alpha, dfdu);
 }
 
@@ -571,9 +793,15 @@ void launch_shell_dv(const ElemParams &ep, const MeshView &m,
                      const double *psi, double scale, double *out,
                      cudaStream_t s) {
   if (m.nelem <= 0) return;
+  if (m.geo_B) {
+    const int occ = prep(shell_dv_geo_kernel, 0);
+    shell_dv_geo_kernel<<<geo_grid(m.nelem, occ), kGeoWarps * 32, 0, s>>>(
+        ep, m, vars, func, ks, coef, psi, scale, out);
+    return;
+  }
   auto k = shell_dv_kernel<kWarps>;
-  prep(k);
-  k<<<grid_for(m.nelem, 2), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
+  const int occ = prep(k);
+  k<<<grid_for(m.nelem, occ), kWarps * 32, sizeof(ShellSmem) * kWarps, s>>>(
       ep, m, vars, func, ks, coef, psi, scale, out);
 }
 
@@ -583,8 +811,8 @@ void launch_shell_geo_build(const ElemParams &ep, const MeshView &m,
   if (nreps <= 0) return;
   auto k = shell_geo_build_kernel<kWarps>;
   const size_t bytes = sizeof(ShellGeoSmem) * kWarps;
-  prep(k, bytes);
-  k<<<grid_for(nreps, 2), kWarps * 32, bytes, s>>>(ep, m, reps, nreps, table,
+  const int occ = prep(k, bytes);
+  k<<<grid_for(nreps, occ), kWarps * 32, bytes, s>>>(ep, m, reps, nreps, table,
                                                     btab);
 }
 

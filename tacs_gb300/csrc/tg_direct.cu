@@ -50,8 +50,10 @@ struct tg_direct {
   // of its large ones (steps of level L: step_ptr_h[L] .. [L + 1])
   std::vector<int> small_ptr_h, step_ptr_h;
   // per level: the most children of one of its supernodes and the row
-  // blocks of its largest child update matrix (the extend-add launches)
-  std::vector<int> ext_nch_h, ext_y_h;
+  // blocks of its largest child update matrix (the extend-add launches),
+  // and the zeroing chunks of its largest front
+  std::vector<int> ext_nch_h, ext_y_h, zero_y_h;
+  int tile = tg::kDirectTile;  // trailing tile of the panel steps
   // the solves' fronts per level: one CTA each (d_solve_sn, solve_ptr_h)
   // and, above kDirectClusterFront rows, one thread-block cluster each
   // (d_csolve_sn, csolve_ptr_h)
@@ -67,7 +69,11 @@ struct tg_direct {
       *d_ea_ptr = nullptr, *d_ea_rel = nullptr, *d_asm_ptr = nullptr,
       *d_asm_blk = nullptr, *d_asm_row = nullptr, *d_asm_col = nullptr,
       *d_ch_ptr = nullptr, *d_ch_list = nullptr, *d_level_sn = nullptr;
-  int64_t *d_l_off = nullptr, *d_u_off = nullptr, *d_v_off = nullptr;
+  int64_t *d_l_off = nullptr, *d_u_off = nullptr, *d_v_off = nullptr,
+          *d_dinv_off = nullptr;
+  // inverses of the diagonal blocks of the cluster-solved fronts
+  double *d_dinv = nullptr;
+  float *d_dinv32 = nullptr;
   double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
   double *d_ypos = nullptr, *d_xpos = nullptr, *d_pb = nullptr,
          *d_kpb = nullptr;
@@ -108,6 +114,9 @@ struct tg_direct {
     v.pool = d_pool;
     v.lstore32 = d_lstore32;
     v.pool32 = d_pool32;
+    v.dinv_off = d_dinv_off;
+    v.dinv = d_dinv;
+    v.dinv32 = d_dinv32;
     return v;
   }
   ~tg_direct() {
@@ -124,6 +133,7 @@ struct tg_direct {
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
     dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
+    dfree(d_dinv_off); dfree(d_dinv); dfree(d_dinv32);
   }
 };
 
@@ -190,8 +200,9 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     }
     d->small_ptr_h.push_back((int)small_h.size());
   }
+  d->tile = precision == TG_PREC_FP32 ? tg::kDirectTile32 : tg::kDirectTile;
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
-                                     tg::kDirectTile, tg::kDirectTrsmRows);
+                                     d->tile, tg::kDirectTrsmRows);
   {
     const bool clusters = tg::direct_cluster_solve_ok();
     std::vector<int> a, b;
@@ -214,14 +225,28 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     d->solve_sn_h = a;
     d->csolve_sn_h = b;
   }
+  // the cluster-solved fronts keep the inverses of their diagonal blocks
+  std::vector<int64_t> dinv_off(d->ns, -1);
+  int64_t dinv_len = 0;
+  for (int sn : d->csolve_sn_h) {
+    dinv_off[sn] = dinv_len;
+    dinv_len += (int64_t)((d->front_c_h[sn] + tg::kDirectPanel - 1) /
+                          tg::kDirectPanel) *
+                tg::kDirectPanel * tg::kDirectPanel;
+  }
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     int nch = 0, um = 0;
+    int64_t zmax = 0;
     for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
       const int sn = an.level_sn[t];
+      const int64_t M = d->front_m_h[sn], C = d->front_c_h[sn];
+      zmax = std::max(zmax, M * C + (M - C) * (M - C));
       nch = std::max(nch, ch_ptr[sn + 1] - ch_ptr[sn]);
       for (int k = ch_ptr[sn]; k < ch_ptr[sn + 1]; k++)
         um = std::max(um, d->front_m_h[ch_list[k]] - d->front_c_h[ch_list[k]]);
     }
+    d->zero_y_h.push_back(
+        (int)((zmax + tg::kDirectZeroChunk - 1) / tg::kDirectZeroChunk));
     d->ext_nch_h.push_back(nch);
     d->ext_y_h.push_back((um + tg::kDirectExtendRows - 1) /
                          tg::kDirectExtendRows);
@@ -262,6 +287,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_l_off, an.l_off);
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
+  if (!rc) rc = upload(&d->d_dinv_off, dinv_off);
   d->contrib_len = vacc;
   // right-hand sides per solve pass: 4, unless the workspace of the largest
   // front would not fit a CTA's shared memory
@@ -278,6 +304,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (precision == TG_PREC_FP64) {
     if (!rc) rc = dalloc(&d->d_lstore, (size_t)an.l_total * b2);
     if (!rc) rc = dalloc(&d->d_pool, (size_t)an.u_peak * b2);
+    if (!rc && dinv_len) rc = dalloc(&d->d_dinv, (size_t)dinv_len);
     if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc * R);
     if (!rc) rc = dalloc(&d->d_ypos, N * R);
     if (!rc) rc = dalloc(&d->d_xpos, N * R);
@@ -286,6 +313,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   } else {
     if (!rc) rc = dalloc(&d->d_lstore32, (size_t)an.l_total * b2);
     if (!rc) rc = dalloc(&d->d_pool32, (size_t)an.u_peak * b2);
+    if (!rc && dinv_len) rc = dalloc(&d->d_dinv32, (size_t)dinv_len);
     if (!rc) rc = dalloc(&d->d_contrib32, (size_t)vacc * R);
     if (!rc) rc = dalloc(&d->d_ypos32, N * R);
     if (!rc) rc = dalloc(&d->d_xpos32, N * R);
@@ -297,7 +325,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_r, N * R);
     if (!rc) rc = dalloc(&d->d_t, N * R);
     if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
-    if (!rc) rc = dalloc(&d->d_scal, 2 * R + 2);
+    if (!rc) rc = dalloc(&d->d_scal, 3 * R + 2);  // refine_pass: 3 per rhs
   }
   if (!rc) rc = dalloc(&d->d_fail, 1);
   if (!rc && tg::direct_solve_smem(d->plain_front, 1, sizeof(double)) >
@@ -335,8 +363,8 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
   for (size_t L = 0; L + 1 < d->level_ptr_h.size(); L++) {
     const int b = d->level_ptr_h[L], e = d->level_ptr_h[L + 1];
     tg::launch_direct_level_assemble<T>(v, d->d_level_sn + b, e - b,
-                                        d->A->d_vals, d->ext_nch_h[L],
-                                        d->ext_y_h[L], s);
+                                        d->A->d_vals, d->zero_y_h[L],
+                                        d->ext_nch_h[L], d->ext_y_h[L], s);
     // the level's small fronts in one launch, its large ones by panels
     const int sb = d->small_ptr_h[L], se = d->small_ptr_h[L + 1];
     tg::launch_direct_factor_small<T>(v, d->d_small + sb, se - sb, d->d_fail,
@@ -347,7 +375,7 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
           v, d->d_step_fronts + ps.front_off[t], ps.count[t],
           d->d_step_tprefix + ps.tile_off[t], ps.total[t],
           d->d_step_rprefix + ps.tile_off[t], ps.rtotal[t], ps.k0[t],
-          d->d_fail, s);
+          d->tile, d->d_fail, s);
     }
   }
 }
@@ -421,15 +449,15 @@ int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
 }  // namespace tg
 
 // Iterative refinement of nr <= max_nr right-hand sides (N apart) with the
-// FP32 factorisation and the stopping test of tg_direct_solve_refined_tol,
+// FP32 factorisation and the stopping tests of tg_direct_solve_refined_multi,
 // per right-hand side; one that has stopped keeps its x (its residual is
 // zeroed before the FP32 solve, whose correction is then exactly zero).
 static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
-                       int max_steps, double tol, int *steps, double *eta_out,
-                       cudaStream_t s) {
+                       int max_steps, double tol, double ftol, int *steps,
+                       double *eta_out, cudaStream_t s) {
   tg_mat *A = d->A;
   const size_t N = (size_t)d->n * d->bs;
-  double h[2 * 4 + 2];
+  double h[3 * 4];
   double bnorm[4], prev[4], eta[4];
   int slow[4], taken[4];
   bool met[4], done[4];
@@ -458,6 +486,10 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
                         d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
                         s);
     tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
+    if (ftol > 0.0)  // the step's correction, max |dx|
+      for (int r = 0; r < nr; r++)
+        tg::launch_reduce_absmax(d->d_t + r * N, N, d->d_red, kRedParts,
+                                 d->d_scal + 3 * r + 2, s);
     tg::launch_axpy(1.0, d->d_t, x, N * nr, s);
     tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
                          A->d_vals, x, d->d_t, s, nr, N);
@@ -465,11 +497,11 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
     tg::launch_axpy(-1.0, d->d_t, d->d_r, N * nr, s);
     for (int r = 0; r < nr; r++) {
       tg::launch_reduce_absmax(d->d_r + r * N, N, d->d_red, kRedParts,
-                               d->d_scal + 2 * r, s);
+                               d->d_scal + 3 * r, s);
       tg::launch_reduce_absmax(x + r * N, N, d->d_red, kRedParts,
-                               d->d_scal + 2 * r + 1, s);
+                               d->d_scal + 3 * r + 1, s);
     }
-    TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 2 * nr * sizeof(double),
+    TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 3 * nr * sizeof(double),
                             cudaMemcpyDeviceToHost, s));
     TG_CUDA(cudaStreamSynchronize(s));
     all_done = true;
@@ -477,14 +509,20 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
       if (done[r]) continue;
       taken[r]++;
       // normwise backward error of x
-      const double den = d->anorm * h[2 * r + 1] + bnorm[r];
-      eta[r] = den > 0.0 ? h[2 * r] / den : 0.0;
+      const double den = d->anorm * h[3 * r + 1] + bnorm[r];
+      eta[r] = den > 0.0 ? h[3 * r] / den : 0.0;
       if (!(eta[r] == eta[r])) {  // NaN: the FP32 factor is unusable
         met[r] = false;
         done[r] = true;
         continue;
       }
       if (eta[r] <= tol) met[r] = true;
+      // forward test: a correction of at most ftol |x| leaves x within
+      // about ftol times the step's contraction of the solution
+      if (ftol > 0.0 && h[3 * r + 2] <= ftol * h[3 * r + 1]) {
+        met[r] = done[r] = true;
+        continue;
+      }
       // The backward-error test alone stops early where |A| |x| >> |b|
       // (thin shells): there eta reaches eps sqrt(N) with a residual still
       // far above an FP64 factorisation's.  So the steps go on while they
@@ -607,14 +645,16 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
 int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 int max_steps, double tol, int *steps,
                                 double *eta_out, void *s) {
-  return tg_direct_solve_refined_multi(d, 1, b, x, max_steps, tol, steps,
-                                       eta_out, s);
+  return tg_direct_solve_refined_multi(d, 1, b, x, max_steps, tol, 0.0,
+                                       steps, eta_out, s);
 }
 
 int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
                                   double *x, int max_steps, double tol,
-                                  int *steps, double *eta_out, void *s) {
-  if (!d || !b || !x || nrhs < 1 || max_steps < 1 || !(tol > 0.0))
+                                  double ftol, int *steps, double *eta_out,
+                                  void *s) {
+  if (!d || !b || !x || nrhs < 1 || max_steps < 1 || !(tol > 0.0) ||
+      !(ftol >= 0.0))
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: bad arguments");
   const size_t N = (size_t)d->n * d->bs;
   // b is re-read after x is zeroed
@@ -630,7 +670,7 @@ int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
   for (int r0 = 0; r0 < nrhs; r0 += d->max_nr) {
     const int nr = nrhs - r0 < d->max_nr ? nrhs - r0 : d->max_nr;
     const int e = refine_pass(d, nr, b + r0 * N, x + r0 * N, max_steps, tol,
-                              steps ? steps + r0 : nullptr,
+                              ftol, steps ? steps + r0 : nullptr,
                               eta_out ? eta_out + r0 : nullptr, S(s));
     if (e && e != TG_ERR_NOCONV) return e;
     if (e) rc = e;

@@ -333,20 +333,23 @@ template <class T>
 // (zero, matrix scatter, then nchild extend-add launches of ychunks row
 // blocks: the largest child count and child update size of the level)
 void launch_direct_level_assemble(const DirectView &v, const int *sn,
-                                  int count, const double *A, int nchild,
-                                  int ychunks, cudaStream_t s);
+                                  int count, const double *A, int zchunks,
+                                  int nchild, int ychunks, cudaStream_t s);
 template <class T>
 void launch_direct_factor_small(const DirectView &v, const int *sn,
                                 int count, int *fail, cudaStream_t s);
 // one panel step of the large fronts of a level (direct::panel_steps):
-// the diagonal blocks of fronts sn[0 .. count) at column k0, the rows
+// the diagonal blocks of fronts sn[0 .. count) at column k0 and the rows
 // below them (rblocks row blocks, prefix sums rprefix[0 .. count]), then
-// their trailing tiles (tiles in all, prefix sums tprefix[0 .. count])
+// their trailing tiles (tile x tile, 32 or 64; tiles in all, prefix sums
+// tprefix[0 .. count])
 template <class T>
 void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                               const int *tprefix, int tiles,
                               const int *rprefix, int rblocks, int k0,
-                              int *fail, cudaStream_t s);
+                              int tile, int *fail, cudaStream_t s);
+// dynamic shared memory of the panel kernel (staged rows)
+size_t direct_panel_smem(size_t elem);
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
                            int max_front, int nr, T *y, T *contrib,

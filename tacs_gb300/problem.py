@@ -161,13 +161,14 @@ class Direct:
             return
         check(rc, "tg_direct_factor")
 
-    def solve(self, b, x=None, steps=30, tol=None):
+    def solve(self, b, x=None, steps=30, tol=None, ftol=0.0):
         """x = A^-1 b; b a vector or an (nrhs, n) tensor of right-hand sides
         (solved together, up to four per pass over the factor).  FP64
         factorisation: FP64 vectors.  FP32 factorisation: FP32 vectors are
         solved in FP32, FP64 ones by refinement (at most `steps` steps, to
-        the backward error `tol`, default eps sqrt(n), per right-hand
-        side), or by the FP64 factorisation after a fallback."""
+        the backward error `tol`, default eps sqrt(n), per right-hand side;
+        ftol > 0: or until a step's correction is at most ftol |x|), or by
+        the FP64 factorisation after a fallback."""
         x = torch.empty_like(b) if x is None else x
         L = _lib.lib()
         nrhs = b.shape[0] if b.dim() == 2 else 1
@@ -183,7 +184,7 @@ class Direct:
             eta = np.zeros(nrhs)
             rc = L.tg_direct_solve_refined_multi(
                 self.handle, nrhs, _p(b), _p(x), int(steps), float(tol),
-                st.ctypes.data, eta.ctypes.data, _stream())
+                float(ftol), st.ctypes.data, eta.ctypes.data, _stream())
             self.last_steps, self.last_eta = int(st.max()), float(eta.max())
             if rc == _lib.ERR_NOCONV:
                 self._factor_fp64()
@@ -576,7 +577,9 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
 
     direct_solver (with the matrix mat it was made for): a Direct from an
     earlier call, whose analysis (ordering, supernodes, storage) is reused
-    -- the next design of an optimisation loop refactors it only.
+    -- the next design of an optimisation loop refactors it only.  With
+    direct="mixed" each solve's refinement stops once a step's correction
+    is at most rtol |x| (Direct.solve's ftol), not at FP64 rounding.
     """
     prob = model.prob
     model.set_segments(prob["seg_elem_ptr"])
@@ -599,7 +602,10 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
         nsys = nlc * model.nseg
 
         def solve_multi(B):
-            X = dsol.solve(B.contiguous())
+            # mixed: the refinement stops once a step's correction is at
+            # most rtol |x| (the accuracy the iterative path asks for)
+            X = dsol.solve(B.contiguous(),
+                           ftol=rtol if direct == "mixed" else 0.0)
             z = np.zeros(nsys, np.int32)
             return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1
     else:

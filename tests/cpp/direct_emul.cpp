@@ -155,6 +155,11 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   v.v_off = v_off.data();
   v.lstore = v.pool = nullptr;
   v.lstore32 = v.pool32 = nullptr;
+  // no cluster-solved fronts here: no diagonal-block inverses kept
+  std::vector<int64_t> dinv_off(ns, -1);
+  v.dinv_off = dinv_off.data();
+  v.dinv = nullptr;
+  v.dinv32 = nullptr;
   set_store(v, lstore.data(), pool.data());
 
   // factor: the sequence of tg_direct_factor (small fronts of a level in
@@ -167,15 +172,24 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     }
     small_ptr.push_back((int)small_h.size());
   }
+  // the trailing tile of tg_direct.cu: 64 for the FP32 factorisation
+  const int tile = sizeof(T) == sizeof(float) ? tg::kDirectTile32
+                                              : tg::kDirectTile;
   const tg::direct::PanelSteps ps = tg::direct::panel_steps(
-      an, bs, small_max, tg::kDirectPanel, tg::kDirectTile,
-      tg::kDirectTrsmRows);
+      an, bs, small_max, tg::kDirectPanel, tile, tg::kDirectTrsmRows);
   size_t step = 0;
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
     const int *lv = an.level_sn.data() + lb;
     const int cnt = le - lb;
-    launch(direct_zero_kernel<T>, cnt, 1, 0, v, lv, cnt);
+    int64_t zmax = 0;  // the zeroing chunks of tg_direct.cu
+    for (int t = 0; t < cnt; t++) {
+      const int64_t M = fm[lv[t]], Cc = fc[lv[t]];
+      zmax = std::max(zmax, M * Cc + (M - Cc) * (M - Cc));
+    }
+    launch(direct_zero_kernel<T>, cnt,
+           (unsigned)((zmax + tg::kDirectZeroChunk - 1) / tg::kDirectZeroChunk),
+           0, v, lv, cnt);
     launch(direct_assemble_kernel<T>, cnt, 1, 0, v, lv, cnt, vals);
     int nch = 0, um = 0;  // the extend-add launches of tg_direct.cu
     for (int t = 0; t < cnt; t++) {
@@ -199,11 +213,17 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
       launch(direct_panel_kernel<T>, ps.count[step], 1, 0, v, fr,
              ps.count[step], ps.k0[step], &failflag);
       if (ps.rtotal[step] > 0)
-        launch(direct_trsm_kernel<T>, ps.rtotal[step], 1, 0, v, fr, rp,
-               ps.count[step], ps.k0[step]);
-      if (ps.total[step] > 0)
-        launch(direct_trailing_kernel<T>, ps.total[step], 1, 0, v, fr, tp,
-               ps.count[step], ps.k0[step]);
+        launch(direct_trsm_kernel<T>, ps.rtotal[step], 1,
+               (size_t)tg::kDirectTrsmRows * (tg::kDirectPanel + 1), v, fr,
+               rp, ps.count[step], ps.k0[step]);
+      if (ps.total[step] > 0) {
+        if (tile == 64)
+          launch(direct_trailing_kernel<T, 64>, ps.total[step], 1, 0, v, fr,
+                 tp, ps.count[step], ps.k0[step]);
+        else
+          launch(direct_trailing_kernel<T, 32>, ps.total[step], 1, 0, v, fr,
+                 tp, ps.count[step], ps.k0[step]);
+      }
     }
   }
   if (failflag) return failflag;

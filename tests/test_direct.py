@@ -294,3 +294,34 @@ def test_direct_multi_rhs(gpu, nrhs):
         assert rel(X32[r].cpu().numpy(), X[r].cpu().numpy()) < 1e-10
         x1 = d32.solve(B[r].clone())
         assert rel(x1.cpu().numpy(), X32[r].cpu().numpy()) < 1e-13
+
+
+def test_mixed_direct_forward_tolerance(gpu):
+    """Refinement with the forward test (ftol): every right-hand side stops
+    once a correction is at most ftol |x|, in no more steps than refinement
+    to FP64 rounding, and lies within 10 ftol of the FP64 solution."""
+    from tacs_gb300 import _lib, meshes
+    prob = meshes.clamped_plate(24, t=0.01)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    B = torch.randn(4, M.ndof, dtype=torch.float64, device="cuda",
+                    generator=g)
+    B[0] = -r0
+    for r in range(4):
+        M.apply_bcs(B[r])
+    d = gpu.Direct(mat)
+    d.factor()
+    X = d.solve(B)
+    d32 = gpu.Direct(mat, precision=_lib.PREC_FP32)
+    d32.factor()
+    d32.solve(B)
+    full = d32.stats()["last_refinement_steps"]
+    for ftol in (1e-8, 1e-10):
+        Xf = d32.solve(B, ftol=ftol)
+        assert not d32.stats()["fell_back_to_fp64"]
+        assert d32.stats()["last_refinement_steps"] <= full
+        for r in range(4):
+            assert rel(Xf[r].cpu().numpy(), X[r].cpu().numpy()) < 10 * ftol
