@@ -114,7 +114,7 @@ def xpt_timing(M, r, torch, reps=3):
     and KS from a solved state and its adjoints (the fused addXptSens +
     addAdjointResXptSensProducts pass), CUDA-event time per function, for
     both exact forms of the shell derivative: dual numbers per coordinate
-    (the default) and the reverse sweep per element; their largest
+    and the reverse sweep per element (the default); their largest
     relative difference is reported beside the times."""
     u, psis = r["u"], r["psis"]
     out = {}
@@ -142,7 +142,7 @@ def xpt_timing(M, r, torch, reps=3):
                           "elements_per_s": [M.nelem / (t / 1e3)
                                              for t in ms]}
     finally:
-        M.set_xpt_mode(False)
+        M.set_xpt_mode(True)
     out["reverse_vs_forward_max_rel_diff"] = max(
         float((a - b).abs().max() / b.abs().max())
         for a, b in zip(res["reverse_sweep"], res["forward_dual"]))

@@ -63,8 +63,8 @@ SIGNATURES = [
     ("tg_direct_solve_refined", _I, [_P, _P, _P, _I, _P]),
     ("tg_direct_solve_refined_tol", _I, [_P, _P, _P, _I, _D, _IP,
                                          C.POINTER(C.c_double), _P]),
-    ("tg_direct_solve_refined_multi", _I, [_P, _I, _P, _P, _I, _D, _D, _P,
-                                           _P, _P]),
+    ("tg_direct_solve_refined_multi", _I, [_P, _I, _P, _P, _I, _D, _D, _D,
+                                           _P, _P, _P]),
     ("tg_direct_get_stats", _I, [_P, _P]),
     ("tg_direct_decref", _I, [_P]),
     ("tg_add_xpt_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),

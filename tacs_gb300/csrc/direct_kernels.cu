@@ -69,22 +69,22 @@ static void forward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
                           const DirectView &v, const int *sn, int count,
                           T *y, T *contrib) {
   if (nr == 4)
-    direct_forward_kernel<T, 4><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 4><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
   else if (nr == 2)
-    direct_forward_kernel<T, 2><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 2><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
   else
-    direct_forward_kernel<T, 1><<<g, 256, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 1><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
 }
 template <class T>
 static void backward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
                            const DirectView &v, const int *sn, int count,
                            const T *y, T *x) {
   if (nr == 4)
-    direct_backward_kernel<T, 4><<<g, 256, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 4><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
   else if (nr == 2)
-    direct_backward_kernel<T, 2><<<g, 256, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 2><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
   else
-    direct_backward_kernel<T, 1><<<g, 256, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 1><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
 }
 
 size_t direct_solve_smem(int front, int nr, size_t elem) {

@@ -471,6 +471,131 @@ __device__ __forceinline__ void dk_stage_block(const Front<T> &f, int kb,
   }
 }
 
+// A 32 x 32 inverse of a diagonal block (dinv, row-major) into shared
+// memory with padded rows: directly, or through registers (256 threads, 4
+// entries each, coalesced) loaded before they are needed.
+template <class T>
+__device__ __forceinline__ void dk_inv_stage(T (*Ls)[33], const T *src) {
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) Ls[t >> 5][t & 31] = src[t];
+}
+#ifndef DK_EMULATE
+template <class T>
+__device__ __forceinline__ void dk_inv_load(T (&pre)[4], const T *src) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) pre[q] = src[threadIdx.x + 256 * q];
+}
+template <class T>
+__device__ __forceinline__ void dk_inv_store(const T (&pre)[4],
+                                             T (*Ls)[33]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int t = threadIdx.x + 256 * q;
+    Ls[t >> 5][t & 31] = pre[q];
+  }
+}
+#endif
+
+// Block solve with a staged inverse X: forward z = X z, or backward
+// z = X^T z, on the block's nb entries (NR interleaved right-hand sides);
+// the result also goes to zbuf when given.  Warp 0, lane i on entry i (the
+// others return).
+template <class T, int NR, bool kTranspose>
+__device__ __forceinline__ void dk_inv_solve(const T (*X)[33], int nb, T *z,
+                                             T *zbuf) {
+#ifdef DK_EMULATE
+  T out[32 * NR];
+  for (int i = 0; i < nb; i++)
+    for (int q = 0; q < NR; q++) {
+      T acc = 0;
+      if (kTranspose)
+        for (int j = i; j < nb; j++) acc += X[j][i] * z[j * NR + q];
+      else
+        for (int j = 0; j <= i; j++) acc += X[i][j] * z[j * NR + q];
+      out[i * NR + q] = acc;
+    }
+  for (int t = 0; t < nb * NR; t++) {
+    z[t] = out[t];
+    if (zbuf) zbuf[t] = out[t];
+  }
+#else
+  if (threadIdx.x >= 32) return;
+  const int i = threadIdx.x;
+  T out[NR];
+#pragma unroll
+  for (int q = 0; q < NR; q++) out[q] = 0;
+  if (i < nb) {
+    if (kTranspose) {
+      for (int j = i; j < nb; j++) {
+        const T a = X[j][i];
+#pragma unroll
+        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
+      }
+    } else {
+      for (int j = 0; j <= i; j++) {
+        const T a = X[i][j];
+#pragma unroll
+        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
+      }
+    }
+  }
+  __syncwarp();
+  if (i < nb)
+#pragma unroll
+    for (int q = 0; q < NR; q++) {
+      z[i * NR + q] = out[q];
+      if (zbuf) zbuf[i * NR + q] = out[q];
+    }
+#endif
+}
+
+// z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < G (G = 32 or
+// 16) of a row group with bit i of `valid` set, by one warp: lane c
+// multiplies column c of every row (each row a coalesced load), then a
+// butterfly of shuffles sums the rows' products so that lane i holds row
+// i's sum (G - 1 shuffles for G rows, one more for G = 16, whose two
+// half-warps sum 16 columns each).  L0: row r0's column kb; ldl: the
+// panel's row stride; zrow(i): row i's NR entries of z.  (The CPU
+// emulation forms each row's sum in column order.)
+template <class T, int NR, int G, class ZRow>
+__device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
+                                             const T *zk, unsigned valid,
+                                             ZRow zrow) {
+  static_assert(G == 32 || G == 16, "row group of 16 or 32");
+#ifdef DK_EMULATE
+  for (int i = 0; i < G; i++) {
+    if (!((valid >> i) & 1u)) continue;
+    for (int q = 0; q < NR; q++) {
+      T acc = 0;
+      for (int c = 0; c < nb; c++) acc += L0[(size_t)i * ldl + c] * zk[c * NR + q];
+      zrow(i)[q] -= acc;
+    }
+  }
+#else
+  const int lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (int q = 0; q < NR; q++) {
+    const T zc = lane < nb ? zk[lane * NR + q] : T(0);
+    T v[G];
+#pragma unroll
+    for (int i = 0; i < G; i++)
+      v[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane] * zc
+                                              : T(0);
+#pragma unroll
+    for (int h = G / 2; h >= 1; h >>= 1) {
+      const bool up = (lane & h) != 0;
+#pragma unroll
+      for (int i = 0; i < h; i++) {
+        const T send = up ? v[i] : v[i + h];
+        const T keep = up ? v[i + h] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+      }
+    }
+    if (G == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 16);
+    if (lane < G && ((valid >> lane) & 1u)) zrow(lane)[q] -= v[0];
+  }
+#endif
+}
+
 // position of front row i of supernode s in a factor-order vector
 __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
   return (size_t)rows[i / bs] * bs + i % bs;
@@ -479,17 +604,25 @@ __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
 // Forward: z = front rows of the supernode (own rows from y, the rows
 // below zero), plus the children's contribution vectors; L11 z1 = z1 and
 // z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
+// Per column block: the block solve (with the kept inverse when the
+// front was factored by panels, else by substitution), then the rows below
+// it in 16-row groups, one per warp.  kDirectPlainThreads threads.
 template <class T, int NR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kDirectPlainThreads)
     direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
                           T *y, T *contrib) {
   if ((int)blockIdx.x >= count) return;
   DK_DYN_SMEM(T, z);
+  __shared__ T Ls[32][33];
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
   T *D = z + (size_t)f.M * NR;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
+  const bool inv = v.dinv_off[s] >= 0;
+  const T *Xg = inv ? dk_dinv(v, (T *)nullptr) + v.dinv_off[s] : nullptr;
+  const int warp = (int)threadIdx.x >> 5;
+  const int nwarp = blockDim.x >= 32 ? (int)blockDim.x >> 5 : 1;
   for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
     const int i = t / NR, r = t - NR * (t / NR);
     z[t] = i < f.C ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
@@ -509,23 +642,26 @@ __global__ void __launch_bounds__(256)
   }
   for (int kb = 0; kb < f.C; kb += kDirectSolveBlock) {
     const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
-    dk_stage_block(f, kb, nb, D);
+    if (inv) {
+      dk_inv_stage(Ls, Xg + (size_t)(kb >> 5) * 1024);
+      __syncthreads();
+      dk_inv_solve<T, NR, false>(Ls, nb, z + kb * NR, (T *)nullptr);
+    } else {
+      dk_stage_block(f, kb, nb, D);
+      __syncthreads();
+      dk_block_solve<T, false, NR>(D, nb, z + kb * NR);
+    }
     __syncthreads();
-    dk_block_solve<T, false, NR>(D, nb, z + kb * NR);
-    __syncthreads();
-    // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb)
-    for (int i = kb + nb + threadIdx.x; i < f.M; i += blockDim.x) {
-      const T *Li = f.lp + (size_t)i * f.C + kb;
-      T acc[NR];
-#pragma unroll
-      for (int r = 0; r < NR; r++) acc[r] = 0;
-      for (int c = 0; c < nb; c++) {
-        const T l = Li[c];
-#pragma unroll
-        for (int r = 0; r < NR; r++) acc[r] += l * z[(kb + c) * NR + r];
-      }
-#pragma unroll
-      for (int r = 0; r < NR; r++) z[i * NR + r] -= acc[r];
+    // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb), in
+    // 16-row groups, one per warp
+    const int r0 = kb + nb, ngrp = (f.M - r0 + 15) >> 4;
+    for (int g = warp; g < ngrp; g += nwarp) {
+      const int rg = r0 + (g << 4);
+      const int cnt = f.M - rg < 16 ? f.M - rg : 16;
+      T *zg = z + (size_t)rg * NR;
+      dk_warp_rows<T, NR, 16>(f.lp + (size_t)rg * f.C + kb, f.C, nb,
+                              z + kb * NR, (1u << cnt) - 1u,
+                              [&](int i) { return zg + i * NR; });
     }
     __syncthreads();
   }
@@ -541,18 +677,23 @@ __global__ void __launch_bounds__(256)
 }
 
 // Backward: z1 = y1 - L21^T x2 (x2 from the ancestors, already final),
-// then L11^T z1 = z1 from the last block up; own rows to x.
+// then L11^T z1 = z1 from the last block up (with the kept inverse when
+// the front was factored by panels); own rows to x.  kDirectPlainThreads
+// threads.
 template <class T, int NR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kDirectPlainThreads)
     direct_backward_kernel(DirectView v, const int *__restrict__ sn,
                            int count, const T *y, T *x) {
   if ((int)blockIdx.x >= count) return;
   DK_DYN_SMEM(T, z);
+  __shared__ T Ls[32][33];
   const int s = sn[blockIdx.x];
   const Front<T> f = front_of<T>(v, s);
   T *D = z + (size_t)f.M * NR;
   const int bs = v.bs;
   const int *rows = v.sn_rows + v.sn_rowptr[s];
+  const bool inv = v.dinv_off[s] >= 0;
+  const T *Xg = inv ? dk_dinv(v, (T *)nullptr) + v.dinv_off[s] : nullptr;
   for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
     const int i = t / NR, r = t - NR * (t / NR);
     const size_t g = dk_pos(rows, bs, i) * NR + r;
@@ -575,9 +716,15 @@ __global__ void __launch_bounds__(256)
   for (int kb = ((f.C - 1) / kDirectSolveBlock) * kDirectSolveBlock; kb >= 0;
        kb -= kDirectSolveBlock) {
     const int nb = f.C - kb < kDirectSolveBlock ? f.C - kb : kDirectSolveBlock;
-    dk_stage_block(f, kb, nb, D);
-    __syncthreads();
-    dk_block_solve<T, true, NR>(D, nb, z + kb * NR);
+    if (inv) {
+      dk_inv_stage(Ls, Xg + (size_t)(kb >> 5) * 1024);
+      __syncthreads();
+      dk_inv_solve<T, NR, true>(Ls, nb, z + kb * NR, (T *)nullptr);
+    } else {
+      dk_stage_block(f, kb, nb, D);
+      __syncthreads();
+      dk_block_solve<T, true, NR>(D, nb, z + kb * NR);
+    }
     __syncthreads();
     // columns before the block: z_j -= sum_k L(kb + k, j) z(kb + k)
     for (int j = threadIdx.x; j < kb; j += blockDim.x) {
@@ -641,88 +788,6 @@ struct ClusterRows {
   }
 };
 
-// a 32 x 32 inverse block through registers into shared memory (256
-// threads, 4 entries each, coalesced): load early, store when needed
-template <class T>
-__device__ __forceinline__ void dk_inv_load(T (&pre)[4], const T *src) {
-#pragma unroll
-  for (int q = 0; q < 4; q++) pre[q] = src[threadIdx.x + 256 * q];
-}
-template <class T>
-__device__ __forceinline__ void dk_inv_store(const T (&pre)[4],
-                                             T (*Ls)[33]) {
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    const int t = threadIdx.x + 256 * q;
-    Ls[t >> 5][t & 31] = pre[q];
-  }
-}
-
-// z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < 32 of a 32-row
-// group with bit i of `valid` set, by one warp: lane c multiplies column c
-// of every row (each row a coalesced load), then a butterfly of shuffles
-// sums the 32 rows' products so that lane i holds row i's sum (31 shuffles
-// for 32 rows).  L0: row r0's column kb; ldl: the panel's row stride;
-// zrow(i): row i's NR entries of z.
-template <class T, int NR, class ZRow>
-__device__ __forceinline__ void dk_warp_rows32(const T *L0, size_t ldl,
-                                               int nb, const T *zk,
-                                               unsigned valid, ZRow zrow) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll 1
-  for (int q = 0; q < NR; q++) {
-    const T zc = lane < nb ? zk[lane * NR + q] : T(0);
-    T v[32];
-#pragma unroll
-    for (int i = 0; i < 32; i++)
-      v[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane] * zc
-                                              : T(0);
-#pragma unroll
-    for (int h = 16; h >= 1; h >>= 1) {
-      const bool up = (lane & h) != 0;
-#pragma unroll
-      for (int i = 0; i < h; i++) {
-        const T send = up ? v[i] : v[i + h];
-        const T keep = up ? v[i + h] : v[i];
-        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
-      }
-    }
-    if ((valid >> lane) & 1u) zrow(lane)[q] -= v[0];
-  }
-}
-
-// Block solve with the staged inverse X (warp 0): forward z = X z, or
-// backward z = X^T z, on the block's nb entries; the result also goes to
-// the published buffer zbuf
-template <class T, int NR, bool kTranspose>
-__device__ __forceinline__ void dk_inv_solve(const T (*X)[33], int nb, T *z,
-                                             T *zbuf) {
-  if (threadIdx.x >= 32) return;
-  const int i = threadIdx.x;
-  T out[NR];
-#pragma unroll
-  for (int q = 0; q < NR; q++) out[q] = 0;
-  if (i < nb) {
-    if (kTranspose) {
-      for (int j = i; j < nb; j++) {
-        const T a = X[j][i];
-#pragma unroll
-        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
-      }
-    } else {
-      for (int j = 0; j <= i; j++) {
-        const T a = X[i][j];
-#pragma unroll
-        for (int q = 0; q < NR; q++) out[q] += a * z[j * NR + q];
-      }
-    }
-  }
-  __syncwarp();
-  if (i < nb)
-#pragma unroll
-    for (int q = 0; q < NR; q++) z[i * NR + q] = zbuf[i * NR + q] = out[q];
-}
-
 template <class T, int NR>
 __global__ void __launch_bounds__(256)
     direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
@@ -784,7 +849,7 @@ __global__ void __launch_bounds__(256)
       dk_inv_store(pre, Ls);
       if (warp == 0) {
         T *zr1 = z + (size_t)cr.slot(r1) * NR;
-        dk_warp_rows32<T, NR>(
+        dk_warp_rows<T, NR, 32>(
             f.lp + (size_t)r1 * f.C + kb, f.C, nb, zk,
             nb1 == 32 ? 0xffffffffu : (1u << nb1) - 1u,
             [&](int i) { return zr1 + i * NR; });
@@ -807,7 +872,7 @@ __global__ void __launch_bounds__(256)
       }
       if (!valid) continue;
       T *zg = z + (size_t)(g << 5) * NR;
-      dk_warp_rows32<T, NR>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk, valid,
+      dk_warp_rows<T, NR, 32>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk, valid,
                             [&](int i) { return zg + i * NR; });
     }
     __syncthreads();

@@ -17,6 +17,8 @@ constexpr int kDirectZeroChunk = 16384;
 // column block of the triangular solves, and the shared memory of its
 // staged diagonal block (rows padded to kDirectSolveBlock + 1 entries)
 constexpr int kDirectSolveBlock = 32;
+// threads of the one-CTA-per-front solve kernels
+constexpr int kDirectPlainThreads = 128;
 // rows of a child's update matrix added into its parent by one CTA
 constexpr int kDirectExtendRows = 32;
 // CTAs of the thread-block cluster that solves one large front, and the
@@ -34,10 +36,10 @@ struct DirectView {
   const int64_t *l_off, *u_off, *v_off;
   double *lstore, *pool;     // FP64 factor panels and update pool
   float *lstore32, *pool32;  // the same storage for an FP32 factorisation
-  // inverses of the 32 x 32 diagonal blocks of the fronts solved by
-  // thread-block clusters (row-major, zero above the diagonal and beyond
-  // the block): panel p of supernode s at dinv_off[s] + p * 1024, or
-  // dinv_off[s] = -1 (none kept)
+  // inverses of the 32 x 32 diagonal blocks of the fronts factored by
+  // panels (row-major, zero above the diagonal and beyond the block):
+  // panel p of supernode s at dinv_off[s] + p * 1024, or dinv_off[s] = -1
+  // (none kept: a front factored whole by one CTA)
   const int64_t *dinv_off;
   double *dinv;
   float *dinv32;

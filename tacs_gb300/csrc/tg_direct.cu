@@ -71,7 +71,7 @@ struct tg_direct {
       *d_ch_ptr = nullptr, *d_ch_list = nullptr, *d_level_sn = nullptr;
   int64_t *d_l_off = nullptr, *d_u_off = nullptr, *d_v_off = nullptr,
           *d_dinv_off = nullptr;
-  // inverses of the diagonal blocks of the cluster-solved fronts
+  // inverses of the diagonal blocks of the fronts factored by panels
   double *d_dinv = nullptr;
   float *d_dinv32 = nullptr;
   double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
@@ -225,10 +225,12 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     d->solve_sn_h = a;
     d->csolve_sn_h = b;
   }
-  // the cluster-solved fronts keep the inverses of their diagonal blocks
+  // the fronts factored by panels keep the inverses of their diagonal
+  // blocks (the solves' block steps become 32 x 32 products)
   std::vector<int64_t> dinv_off(d->ns, -1);
   int64_t dinv_len = 0;
-  for (int sn : d->csolve_sn_h) {
+  for (int sn = 0; sn < d->ns; sn++) {
+    if (d->front_m_h[sn] <= kSmallFront) continue;
     dinv_off[sn] = dinv_len;
     dinv_len += (int64_t)((d->front_c_h[sn] + tg::kDirectPanel - 1) /
                           tg::kDirectPanel) *
@@ -322,11 +324,13 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_a32, (size_t)A->nnz * b2);
     if (!rc) rc = dalloc(&d->d_r32, N * R);
     if (!rc) rc = dalloc(&d->d_c32, N * R);
-    if (!rc) rc = dalloc(&d->d_r, N * R);
-    if (!rc) rc = dalloc(&d->d_t, N * R);
-    if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
-    if (!rc) rc = dalloc(&d->d_scal, 3 * R + 2);  // refine_pass: 3 per rhs
   }
+  // refinement (both precisions): residuals, corrections, the max-|x|
+  // reductions and their scalars (3 per right-hand side)
+  if (!rc) rc = dalloc(&d->d_r, N * R);
+  if (!rc) rc = dalloc(&d->d_t, N * R);
+  if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
+  if (!rc) rc = dalloc(&d->d_scal, 3 * R + 2);
   if (!rc) rc = dalloc(&d->d_fail, 1);
   if (!rc && tg::direct_solve_smem(d->plain_front, 1, sizeof(double)) >
                  kSmemMax)
@@ -448,15 +452,19 @@ int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
 
 }  // namespace tg
 
-// Iterative refinement of nr <= max_nr right-hand sides (N apart) with the
-// FP32 factorisation and the stopping tests of tg_direct_solve_refined_multi,
-// per right-hand side; one that has stopped keeps its x (its residual is
-// zeroed before the FP32 solve, whose correction is then exactly zero).
+// Iterative refinement of nr <= max_nr right-hand sides (N apart): x = 0,
+// then per step x += (the factorisation's solve of r = b - A x), r in FP64
+// (an FP32 factorisation solves FP32 copies of r), with the stopping tests
+// of tg_direct_solve_refined_multi per right-hand side; one that has
+// stopped keeps its x (its residual is zeroed before the solve, whose
+// correction is then exactly zero).
 static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
-                       int max_steps, double tol, double ftol, int *steps,
-                       double *eta_out, cudaStream_t s) {
+                       int max_steps, double tol, double ftol, double rtol,
+                       int *steps, double *eta_out, cudaStream_t s) {
   tg_mat *A = d->A;
   const size_t N = (size_t)d->n * d->bs;
+  const bool f32 = d->precision == TG_PREC_FP32;
+  const bool stated = ftol > 0.0 || rtol > 0.0;
   double h[3 * 4];
   double bnorm[4], prev[4], eta[4];
   int slow[4], taken[4];
@@ -478,14 +486,22 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
   TG_CUDA(cudaMemsetAsync(x, 0, N * nr * sizeof(double), s));
   tg::launch_copy(b, d->d_r, N * nr, s);
   for (int step = 0; step < max_steps && !all_done; step++) {
-    tg::launch_d2f(d->d_r, d->d_r32, N * nr, s);
-    for (int r = 0; r < nr; r++)
-      if (done[r])
-        TG_CUDA(cudaMemsetAsync(d->d_r32 + r * N, 0, N * sizeof(float), s));
-    solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
-                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
-                        s);
-    tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
+    if (f32) {
+      tg::launch_d2f(d->d_r, d->d_r32, N * nr, s);
+      for (int r = 0; r < nr; r++)
+        if (done[r])
+          TG_CUDA(cudaMemsetAsync(d->d_r32 + r * N, 0, N * sizeof(float), s));
+      solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
+                          d->d_kpb32, d->d_ypos32, d->d_xpos32,
+                          d->d_contrib32, s);
+      tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
+    } else {
+      for (int r = 0; r < nr; r++)
+        if (done[r])
+          TG_CUDA(cudaMemsetAsync(d->d_r + r * N, 0, N * sizeof(double), s));
+      solve_levels<double>(d, nr, d->d_r, d->d_t, d->A->d_vals, d->d_pb,
+                           d->d_kpb, d->d_ypos, d->d_xpos, d->d_contrib, s);
+    }
     if (ftol > 0.0)  // the step's correction, max |dx|
       for (int r = 0; r < nr; r++)
         tg::launch_reduce_absmax(d->d_t + r * N, N, d->d_red, kRedParts,
@@ -511,23 +527,28 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
       // normwise backward error of x
       const double den = d->anorm * h[3 * r + 1] + bnorm[r];
       eta[r] = den > 0.0 ? h[3 * r] / den : 0.0;
-      if (!(eta[r] == eta[r])) {  // NaN: the FP32 factor is unusable
+      if (!(eta[r] == eta[r])) {  // NaN: the factorisation is unusable
         met[r] = false;
         done[r] = true;
         continue;
       }
-      if (eta[r] <= tol) met[r] = true;
-      // forward test: a correction of at most ftol |x| leaves x within
-      // about ftol times the step's contraction of the solution
-      if (ftol > 0.0 && h[3 * r + 2] <= ftol * h[3 * r + 1]) {
+      // stated accuracy: stop as soon as every given test holds
+      if (stated && eta[r] <= tol &&
+          (ftol <= 0.0 || h[3 * r + 2] <= ftol * h[3 * r + 1]) &&
+          (rtol <= 0.0 || h[3 * r] <= rtol * bnorm[r])) {
         met[r] = done[r] = true;
         continue;
       }
+      if (eta[r] <= tol) met[r] = true;
       // The backward-error test alone stops early where |A| |x| >> |b|
       // (thin shells): there eta reaches eps sqrt(N) with a residual still
       // far above an FP64 factorisation's.  So the steps go on while they
       // halve eta, and stop at the first step that does not once the
       // tolerance is met (two such steps in a row before it: stagnation).
+      // This also ends a stated test that FP64 cannot reach: a residual
+      // below the rounding of A x itself (about eps |A| |x|, which on thin
+      // shells is far above rtol |b|) is accepted at that floor, as the
+      // Krylov solves accept it.
       slow[r] = (taken[r] > 1 && eta[r] > 0.5 * prev[r]) ? slow[r] + 1 : 0;
       if (slow[r] >= (met[r] ? 1 : 2)) done[r] = true;
       prev[r] = eta[r];
@@ -556,7 +577,9 @@ int tg_direct_factor(tg_direct *d, void *s) {
     tg::launch_d2f(A->d_vals, d->d_a32,
                    (size_t)A->nnz * A->bsize * A->bsize, S(s));
     factor_levels<float>(d, S(s));
-    // ||A||_inf of these values, for the refinement's backward error
+  }
+  {  // ||A||_inf of these values, for the refinement's backward error
+    const tg_mat *A = d->A;
     const size_t N = (size_t)d->n * d->bs;
     tg::launch_bcsr_row_abs_sum(A->bsize, A->nrows, A->a->d_rowp, A->d_vals,
                                 d->d_t, S(s));
@@ -645,16 +668,19 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
 int tg_direct_solve_refined_tol(tg_direct *d, const double *b, double *x,
                                 int max_steps, double tol, int *steps,
                                 double *eta_out, void *s) {
-  return tg_direct_solve_refined_multi(d, 1, b, x, max_steps, tol, 0.0,
+  if (d && d->precision != TG_PREC_FP32)
+    return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: needs the FP32 "
+                            "factorisation");
+  return tg_direct_solve_refined_multi(d, 1, b, x, max_steps, tol, 0.0, 0.0,
                                        steps, eta_out, s);
 }
 
 int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
                                   double *x, int max_steps, double tol,
-                                  double ftol, int *steps, double *eta_out,
-                                  void *s) {
+                                  double ftol, double rtol, int *steps,
+                                  double *eta_out, void *s) {
   if (!d || !b || !x || nrhs < 1 || max_steps < 1 || !(tol > 0.0) ||
-      !(ftol >= 0.0))
+      !(ftol >= 0.0) || !(rtol >= 0.0))
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: bad arguments");
   const size_t N = (size_t)d->n * d->bs;
   // b is re-read after x is zeroed
@@ -663,14 +689,11 @@ int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
     return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: b and x alias");
   if (!d->factored)
     return fail(TG_ERR_STATE, "tg_direct_solve_refined_tol: not factored");
-  if (d->precision != TG_PREC_FP32)
-    return fail(TG_ERR_ARG, "tg_direct_solve_refined_tol: needs the FP32 "
-                            "factorisation");
   int rc = 0;
   for (int r0 = 0; r0 < nrhs; r0 += d->max_nr) {
     const int nr = nrhs - r0 < d->max_nr ? nrhs - r0 : d->max_nr;
     const int e = refine_pass(d, nr, b + r0 * N, x + r0 * N, max_steps, tol,
-                              ftol, steps ? steps + r0 : nullptr,
+                              ftol, rtol, steps ? steps + r0 : nullptr,
                               eta_out ? eta_out + r0 : nullptr, S(s));
     if (e && e != TG_ERR_NOCONV) return e;
     if (e) rc = e;

@@ -78,7 +78,7 @@ struct tg_assembler {
   KsStats ks{0.0, 1.0, 100.0};
   bool ks_valid = false;
   // node-coordinate derivatives: 0 forward (dual), 1 reverse sweep
-  int xpt_mode = 0;
+  int xpt_mode = TG_XPT_REVERSE;  // the faster of the two exact forms
   // element segments (independent meshes): contiguous element ranges
   int nseg = 0;
   std::vector<int> seg_elem_ptr_h;

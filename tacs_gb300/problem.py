@@ -161,20 +161,25 @@ class Direct:
             return
         check(rc, "tg_direct_factor")
 
-    def solve(self, b, x=None, steps=30, tol=None, ftol=0.0):
+    def solve(self, b, x=None, steps=30, tol=None, ftol=0.0, rtol=0.0):
         """x = A^-1 b; b a vector or an (nrhs, n) tensor of right-hand sides
         (solved together, up to four per pass over the factor).  FP64
-        factorisation: FP64 vectors.  FP32 factorisation: FP32 vectors are
-        solved in FP32, FP64 ones by refinement (at most `steps` steps, to
-        the backward error `tol`, default eps sqrt(n), per right-hand side;
-        ftol > 0: or until a step's correction is at most ftol |x|), or by
-        the FP64 factorisation after a fallback."""
+        factorisation: FP64 vectors, one solve, or with rtol > 0 refined
+        in FP64 until the residual is at most rtol |b| (max norms).  FP32
+        factorisation: FP32 vectors are solved in FP32, FP64 ones by
+        refinement (at most `steps` steps, to the backward error `tol`,
+        default eps sqrt(n), per right-hand side; with ftol > 0 or
+        rtol > 0 until every given test holds: a step's correction at most
+        ftol |x|, the residual at most rtol |b|), or by the FP64
+        factorisation after a fallback."""
         x = torch.empty_like(b) if x is None else x
         L = _lib.lib()
         nrhs = b.shape[0] if b.dim() == 2 else 1
         if self._fp64 is not None and b.dtype == torch.float64:
-            return self._fp64.solve(b, x)
-        if self.precision == _lib.PREC_FP32 and b.dtype == torch.float64:
+            return self._fp64.solve(b, x, steps=steps, rtol=rtol)
+        refine = b.dtype == torch.float64 and (
+            self.precision == _lib.PREC_FP32 or rtol > 0.0)
+        if refine:
             n = b.shape[-1]
             if tol is None:
                 tol = 2.0 ** -53 * float(np.sqrt(n))
@@ -184,11 +189,12 @@ class Direct:
             eta = np.zeros(nrhs)
             rc = L.tg_direct_solve_refined_multi(
                 self.handle, nrhs, _p(b), _p(x), int(steps), float(tol),
-                float(ftol), st.ctypes.data, eta.ctypes.data, _stream())
+                float(ftol), float(rtol), st.ctypes.data, eta.ctypes.data,
+                _stream())
             self.last_steps, self.last_eta = int(st.max()), float(eta.max())
-            if rc == _lib.ERR_NOCONV:
+            if rc == _lib.ERR_NOCONV and self.precision == _lib.PREC_FP32:
                 self._factor_fp64()
-                return self._fp64.solve(b, x)
+                return self._fp64.solve(b, x, steps=steps, rtol=rtol)
             check(rc, "tg_direct_solve_refined_multi")
             return x
         if self.precision == _lib.PREC_FP32:
@@ -577,9 +583,11 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
 
     direct_solver (with the matrix mat it was made for): a Direct from an
     earlier call, whose analysis (ordering, supernodes, storage) is reused
-    -- the next design of an optimisation loop refactors it only.  With
-    direct="mixed" each solve's refinement stops once a step's correction
-    is at most rtol |x| (Direct.solve's ftol), not at FP64 rounding.
+    -- the next design of an optimisation loop refactors it only.  The
+    direct solves are refined to the relative residual rtol (max norms)
+    like the iterative ones; with direct="mixed" also until a step's
+    correction is at most rtol |x| (Direct.solve's rtol, ftol), not to
+    FP64 rounding.
     """
     prob = model.prob
     model.set_segments(prob["seg_elem_ptr"])
@@ -602,9 +610,10 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
         nsys = nlc * model.nseg
 
         def solve_multi(B):
-            # mixed: the refinement stops once a step's correction is at
-            # most rtol |x| (the accuracy the iterative path asks for)
-            X = dsol.solve(B.contiguous(),
+            # both precisions to the relative residual rtol of the
+            # iterative path; mixed refinement also until a step's
+            # correction is at most rtol |x|
+            X = dsol.solve(B.contiguous(), rtol=rtol,
                            ftol=rtol if direct == "mixed" else 0.0)
             z = np.zeros(nsys, np.int32)
             return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1

@@ -63,6 +63,14 @@ static void set_store(tg::DirectView &v, double *l, double *p) {
   v.lstore = l;
   v.pool = p;
 }
+static void set_dinv(tg::DirectView &v, double *p) {
+  v.dinv = p;
+  v.dinv32 = nullptr;
+}
+static void set_dinv(tg::DirectView &v, float *p) {
+  v.dinv = nullptr;
+  v.dinv32 = p;
+}
 static void set_store(tg::DirectView &v, float *l, float *p) {
   v.lstore32 = l;
   v.pool32 = p;
@@ -155,11 +163,19 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   v.v_off = v_off.data();
   v.lstore = v.pool = nullptr;
   v.lstore32 = v.pool32 = nullptr;
-  // no cluster-solved fronts here: no diagonal-block inverses kept
+  // the fronts factored by panels keep the inverses of their diagonal
+  // blocks, as in tg_direct.cu
   std::vector<int64_t> dinv_off(ns, -1);
+  int64_t dinv_len = 0;
+  for (int sn = 0; sn < ns; sn++) {
+    if (fm[sn] <= small_max) continue;
+    dinv_off[sn] = dinv_len;
+    dinv_len += (int64_t)((fc[sn] + tg::kDirectPanel - 1) / tg::kDirectPanel) *
+                tg::kDirectPanel * tg::kDirectPanel;
+  }
+  std::vector<T> dinv(dinv_len > 0 ? (size_t)dinv_len : 1);
   v.dinv_off = dinv_off.data();
-  v.dinv = nullptr;
-  v.dinv32 = nullptr;
+  set_dinv(v, dinv.data());
   set_store(v, lstore.data(), pool.data());
 
   // factor: the sequence of tg_direct_factor (small fronts of a level in

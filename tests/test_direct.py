@@ -325,3 +325,39 @@ def test_mixed_direct_forward_tolerance(gpu):
         assert d32.stats()["last_refinement_steps"] <= full
         for r in range(4):
             assert rel(Xf[r].cpu().numpy(), X[r].cpu().numpy()) < 10 * ftol
+
+
+def test_fp64_direct_refined_to_relative_residual(gpu):
+    """An FP64 factorisation refined in FP64 (rtol) on a thin simply
+    supported plate: every right-hand side ends with a residual at most
+    rtol |b|, or at the FP64 floor eps sqrt(n) (|K| |u| + |b|) where rtol
+    |b| lies below the rounding of K u itself (max norms; |K| |u| >> |b|
+    here, as the Krylov solves' floor acceptance), and the refined
+    solution stays within 1e-8 of the single solve."""
+    from tacs_gb300 import meshes
+    prob = meshes.plate_c2(64, 2.0 * 64 / 512, seed=2)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    B = torch.randn(3, M.ndof, dtype=torch.float64, device="cuda",
+                    generator=g)
+    B[0] = -r0
+    for r in range(3):
+        M.apply_bcs(B[r])
+    d = gpu.Direct(mat)
+    d.factor()
+    X1 = d.solve(B)
+    K = _host_matrix(mat, M.ndof)
+    knorm = float(abs(K).sum(axis=1).max())
+    floor_tol = 2.0 ** -53 * np.sqrt(M.ndof)
+    for rtol in (1e-10, 1e-12):
+        X = d.solve(B, rtol=rtol)
+        assert d.stats()["last_refinement_steps"] >= 1
+        for r in range(3):
+            res = float((mat.mult(X[r]) - B[r]).abs().max())
+            bn = float(B[r].abs().max())
+            floor = floor_tol * (knorm * float(X[r].abs().max()) + bn)
+            assert res <= max(rtol * bn, floor)
+            assert rel(X[r].cpu().numpy(), X1[r].cpu().numpy()) < 1e-8

@@ -294,7 +294,7 @@ def test_reverse_kernel_matches_reference(gpu, name):
         M.add_xpt_sens(u, [0, 1], [dc, dk])
         M.add_adjoint_res_xpt_products(u, [psi], [xa])
         out[reverse] = [_h(dc), _h(dk), _h(xa)]
-    M.set_xpt_mode(False)
+    M.set_xpt_mode(True)
     for got, key in zip(out[True], ("dfdX_test_comp", "dfdX_test_ks",
                                     "adjxpt_test")):
         assert rel(got, ref[key]) < XPT_TOL
