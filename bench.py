@@ -156,8 +156,9 @@ def c2_adjoint_section(torch, n=512):
     pressure field): compliance and its gradient with respect to the
     262,144 thicknesses through torch.autograd, both solves by the complete
     multifrontal factorisation (GMRES(80) + ILU(0) does not converge on
-    this plate).  Times the analysis, the factorisation, one solve and the
-    whole gradient."""
+    this plate), refined to the 1e-10 relative residual of the stated
+    GMRES tolerance (or the FP64 floor).  Times the analysis, the
+    factorisation, one solve and the whole gradient."""
     from tacs_gb300 import autograd as ag
     from tacs_gb300 import problem
     p = c2_problem(n=n)
@@ -165,7 +166,7 @@ def c2_adjoint_section(torch, n=512):
     M.set_fixed_geometry(True)  # thicknesses change, the nodes do not
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    solver = ag.StaticSolver(M, np.zeros(M.ndof), direct=True)
+    solver = ag.StaticSolver(M, np.zeros(M.ndof), rtol=1e-10, direct=True)
     torch.cuda.synchronize()
     t_analysis = time.perf_counter() - t0
     x = torch.as_tensor(np.asarray(p["thick"]), device="cuda")
@@ -389,7 +390,9 @@ def cylinder_section(torch, nc=384, nz=256):
     adjoint gradient, all-FP64 against mixed precision (FP32 factor and
     mat-vec inside FP64 GMRES with true-residual refinement), both with the
     colour-reordered ILU(0) (the natural order of a closed cylinder is one
-    sequential chain of 98,688 rows)."""
+    sequential chain of 98,688 rows); beside them the complete
+    factorisation in FP64 and in FP32 with FP64 refinement.  Each
+    gradient's error is against the FP64 ILU(0) arm."""
     from tacs_gb300 import _lib, meshes, problem
     c = meshes.cylinder_c5(nc, nz)
     M = problem.GpuModel(c)
@@ -398,26 +401,41 @@ def cylinder_section(torch, nc=384, nz=256):
                        "compliance adjoint gradient",
            "elements": int(c["nelem"]), "dof": int(M.ndof)}
     g = {}
-    for label, mixed in (("fp64_ilu0_colored", False),
-                         ("mixed_ilu0_colored", True)):
+    # the configured solver (FP32 / FP64 ILU(0) inside FP64 GMRES), then the
+    # complete factorisation in FP64 and in FP32 with FP64 refinement, all
+    # to the same 1e-10 relative residual
+    arms = (("fp64_ilu0_colored", dict(pc_kind=_lib.PC_ILU0_COLORED)),
+            ("mixed_ilu0_colored", dict(pc_kind=_lib.PC_ILU0_COLORED,
+                                        mixed=True)),
+            ("fp64_direct", dict(direct="fp64")),
+            ("mixed_direct", dict(direct="mixed")))
+    for label, kw in arms:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r = problem.static_adjoint(M, c["force"], 200, 30, 1e-10,
-                                   pc_kind=_lib.PC_ILU0_COLORED, mixed=mixed,
-                                   funcs=(0,))
+                                   funcs=(0,), **kw)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         g[label] = (r["grads"][0].cpu().numpy(), r["funcs"][0])
         out[label] = {"s_per_gradient": dt, "iters": r["iters"],
                       "converged": [int(f) for f in r["flags"]],
                       "compliance": float(r["funcs"][0])}
-    a, b = g["mixed_ilu0_colored"], g["fp64_ilu0_colored"]
-    out["mixed_ilu0_colored"]["grad_rel_err_vs_fp64"] = float(
-        np.abs(a[0] - b[0]).max() / np.abs(b[0]).max())
-    out["mixed_ilu0_colored"]["compliance_rel_err_vs_fp64"] = float(
-        abs(a[1] - b[1]) / abs(b[1]))
+        if r.get("direct") is not None:
+            out[label]["direct"] = {
+                k: r["direct"].stats()[k]
+                for k in ("flops", "factor_bytes", "fell_back_to_fp64")}
+    b = g["fp64_ilu0_colored"]
+    for label in ("mixed_ilu0_colored", "fp64_direct", "mixed_direct"):
+        a = g[label]
+        out[label]["grad_rel_err_vs_fp64"] = float(
+            np.abs(a[0] - b[0]).max() / np.abs(b[0]).max())
+        out[label]["compliance_rel_err_vs_fp64"] = float(
+            abs(a[1] - b[1]) / abs(b[1]))
     out["mixed_speedup_vs_fp64"] = (out["fp64_ilu0_colored"]["s_per_gradient"]
                                     / out["mixed_ilu0_colored"]["s_per_gradient"])
+    out["mixed_direct_speedup_vs_fp64_direct"] = (
+        out["fp64_direct"]["s_per_gradient"]
+        / out["mixed_direct"]["s_per_gradient"])
     del M
     torch.cuda.empty_cache()
     return out
@@ -738,16 +756,17 @@ def main():
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the fixed-geometry assembly section")
     ap.add_argument("--no-cylinder", action="store_true")
-    ap.add_argument("--c2-adjoint", action="store_true",
-                    help="the 512 x 512 plate's autograd gradient with "
-                         "direct solves")
-    ap.add_argument("--batch", type=int, default=12)
-    ap.add_argument("--batch-nmax", type=int, default=96)
+    ap.add_argument("--no-c2-adjoint", action="store_true",
+                    help="skip the 512 x 512 plate's autograd gradient "
+                         "(direct solves)")
+    ap.add_argument("--batch", type=int, default=48)
+    ap.add_argument("--batch-nmax", type=int, default=256)
     ap.add_argument("--batch-pc", type=int, default=0)
     ap.add_argument("--batch-fill", type=int, default=0,
                     help="ILU fill level of the batched solves")
-    ap.add_argument("--batch-direct", action="store_true",
-                    help="batched solves by the complete factorisation")
+    ap.add_argument("--batch-ilu", action="store_true",
+                    help="batched solves by GMRES + ILU instead of the "
+                         "complete factorisation")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -906,7 +925,7 @@ def main():
     if rank == 0 and args.c3_solve:
         line["c3_solve"] = guarded(lambda: c3_solve_section(
             torch, pc_kind=args.c3_pc))
-    if rank == 0 and args.c2_adjoint:
+    if rank == 0 and not args.no_c2_adjoint:
         line["c2_adjoint"] = guarded(
             lambda: c2_adjoint_section(torch, args.size))
     if rank == 0 and not args.no_cylinder:
@@ -915,7 +934,7 @@ def main():
         line["batch_c4"] = guarded(lambda: batch_section(
             torch, count=args.batch, nmax=args.batch_nmax,
             pc_kind=args.batch_pc, lev_fill=args.batch_fill,
-            direct=args.batch_direct))
+            direct=not args.batch_ilu))
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = guarded(lambda: cpu_baseline(p))
         if padj is not None and "error" not in line["cpu_baseline"]:

@@ -205,8 +205,9 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
    tg_direct_solve_f32, e.g. as the preconditioner of an FP64 iteration.
    tg_direct_factor synchronises and returns TG_ERR_PIVOT on a
    non-positive pivot.
-   stats: supernodes, tree levels, factor bytes (FP64 storage), update-pool
-   bytes (FP64), dense flops, largest front (scalar rows), precision. */
+   stats (8 doubles): supernodes, tree levels, factor bytes (FP64
+   storage), update-pool bytes (FP64), dense flops, largest front (scalar
+   rows), precision, fronts solved by thread-block clusters. */
 int tg_direct_create(tg_mat *A, int use_coords, int precision,
                      tg_direct **out);
 int tg_direct_factor(tg_direct *d, void *stream);

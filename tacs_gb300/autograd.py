@@ -54,10 +54,13 @@ class StaticSolver:
             model.set_segments(model.prob["seg_elem_ptr"])
         self.mat = model.new_mat()
         # direct: True / "fp64" complete factorisation, "mixed" in FP32
-        # with FP64 refinement of every solve
+        # with FP64 refinement of every solve; either refined to the
+        # relative residual rtol (or the FP64 floor) like the Krylov solves
         self.direct = Direct(self.mat, precision=_lib.PREC_FP32
                              if direct == "mixed" else _lib.PREC_FP64) \
             if direct else None
+        self.rtol = rtol
+        self.mixed_direct = direct == "mixed"
         if direct:
             self.pc = self.ksm = None
         else:
@@ -101,7 +104,8 @@ class StaticSolver:
         factorisation one load case at a time (exact, 0 iterations)."""
         if self.direct is None:
             return self.ksm.solve_multi(B)
-        X = self.direct.solve(B.contiguous())
+        X = self.direct.solve(B.contiguous(), rtol=self.rtol,
+                              ftol=self.rtol if self.mixed_direct else 0.0)
         nsys = B.shape[0] * (self.model.nseg if self.segments else 1)
         return (X, np.zeros(nsys, np.int32), np.ones(nsys, np.int32),
                 np.zeros(nsys), 1)

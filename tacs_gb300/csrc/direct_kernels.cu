@@ -170,12 +170,22 @@ void launch_direct_backward_cluster(const DirectView &v, const int *sn,
                       v, sn, count, y, x);
 }
 
-// whether the device schedules the solve clusters (at least one active)
+// whether the device schedules the solve clusters (at least one active),
+// asked with the dynamic shared memory of a 32 k-row front (the attribute
+// set first: with the kernel's static shared memory it passes 48 KB)
 bool direct_cluster_solve_ok() {
+  const size_t bytes = direct_cluster_smem(1 << 15, 1, sizeof(double));
+  if (cudaFuncSetAttribute(
+          (const void *)direct_forward_cluster_kernel<double, 1>,
+          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kDirectSolveCluster);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = direct_cluster_smem(1 << 15, 1, sizeof(double));
+  cfg.dynamicSmemBytes = bytes;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = kDirectSolveCluster;
@@ -215,9 +225,9 @@ void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
       n, bs, perm, xpos, x, nrhs, ld);
 }
 
-// Dynamic shared memory of the solve kernels above the default 48 KB, for
-// fronts of up to plain_front rows on one CTA and cluster_front rows on a
-// cluster, nr right-hand sides at most.  Per device (the attribute belongs
+// Dynamic shared memory of the solve kernels for fronts of up to
+// plain_front rows on one CTA and cluster_front rows on a cluster, nr
+// right-hand sides at most.  Per device (the attribute belongs
 // to the kernel on each device); the limits only grow, and are recorded
 // only once every call succeeded.
 template <class T, int NR>
@@ -228,14 +238,15 @@ static cudaError_t set_solve_smem(int plain_front, int cluster_front) {
                           (const void *)direct_backward_kernel<T, NR>};
   const void *clus[2] = {(const void *)direct_forward_cluster_kernel<T, NR>,
                          (const void *)direct_backward_cluster_kernel<T, NR>};
+  // set whatever the size: the kernels' static shared memory (staged
+  // rows, inverse blocks) counts against the same 48 KB default
   cudaError_t e = cudaSuccess;
-  if (pb > 48 * 1024)
-    for (const void *k : plain)
-      if ((e = cudaFuncSetAttribute(k,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)pb)) != cudaSuccess)
-        return e;
-  if (cluster_front > 0 && cb > 48 * 1024)
+  for (const void *k : plain)
+    if ((e = cudaFuncSetAttribute(k,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pb)) != cudaSuccess)
+      return e;
+  if (cluster_front > 0)
     for (const void *k : clus)
       if ((e = cudaFuncSetAttribute(k,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -606,7 +606,7 @@ __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
 // z2 -= L21 z1; own rows back to y, z2 to the supernode's contribution.
 // Per column block: the block solve (with the kept inverse when the
 // front was factored by panels, else by substitution), then the rows below
-// it in 16-row groups, one per warp.  kDirectPlainThreads threads.
+// it.  kDirectPlainThreads threads.
 template <class T, int NR>
 __global__ void __launch_bounds__(kDirectPlainThreads)
     direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
@@ -621,11 +621,16 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const bool inv = v.dinv_off[s] >= 0;
   const T *Xg = inv ? dk_dinv(v, (T *)nullptr) + v.dinv_off[s] : nullptr;
-  const int warp = (int)threadIdx.x >> 5;
-  const int nwarp = blockDim.x >= 32 ? (int)blockDim.x >> 5 : 1;
-  for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
-    const int i = t / NR, r = t - NR * (t / NR);
-    z[t] = i < f.C ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
+  for (int i = threadIdx.x; i < f.M; i += blockDim.x) {
+    T *zi = z + (size_t)i * NR;
+    if (i < f.C) {
+      const T *yi = y + dk_pos(rows, bs, i) * NR;
+#pragma unroll
+      for (int q = 0; q < NR; q++) zi[q] = yi[q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < NR; q++) zi[q] = T(0);
+    }
   }
   __syncthreads();
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
@@ -634,9 +639,11 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
     const T *w = contrib + v.v_off[c] * NR;
-    for (int t = threadIdx.x; t < um * NR; t += blockDim.x) {
-      const int i = t / NR, r = t - NR * (t / NR);
-      z[(rel[i / bs] * bs + i % bs) * NR + r] += w[t];
+    for (int i = threadIdx.x; i < um; i += blockDim.x) {
+      T *zi = z + (size_t)(rel[i / bs] * bs + i % bs) * NR;
+      const T *wi = w + (size_t)i * NR;
+#pragma unroll
+      for (int q = 0; q < NR; q++) zi[q] += wi[q];
     }
     __syncthreads();
   }
@@ -652,22 +659,30 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
       dk_block_solve<T, false, NR>(D, nb, z + kb * NR);
     }
     __syncthreads();
-    // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb), in
-    // 16-row groups, one per warp
-    const int r0 = kb + nb, ngrp = (f.M - r0 + 15) >> 4;
-    for (int g = warp; g < ngrp; g += nwarp) {
-      const int rg = r0 + (g << 4);
-      const int cnt = f.M - rg < 16 ? f.M - rg : 16;
-      T *zg = z + (size_t)rg * NR;
-      dk_warp_rows<T, NR, 16>(f.lp + (size_t)rg * f.C + kb, f.C, nb,
-                              z + kb * NR, (1u << cnt) - 1u,
-                              [&](int i) { return zg + i * NR; });
+    // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb), one
+    // thread per row (its 32 loads independent, every one serving the NR
+    // right-hand sides; measured faster here than warp-per-row-group
+    // reductions or rows staged through shared memory)
+    for (int i = kb + nb + threadIdx.x; i < f.M; i += blockDim.x) {
+      const T *Li = f.lp + (size_t)i * f.C + kb;
+      T acc[NR];
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[q] = 0;
+      for (int c = 0; c < nb; c++) {
+        const T l = Li[c];
+#pragma unroll
+        for (int q = 0; q < NR; q++) acc[q] += l * z[(kb + c) * NR + q];
+      }
+#pragma unroll
+      for (int q = 0; q < NR; q++) z[(size_t)i * NR + q] -= acc[q];
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < f.C * NR; t += blockDim.x) {
-    const int i = t / NR, r = t - NR * (t / NR);
-    y[dk_pos(rows, bs, i) * NR + r] = z[t];
+  for (int i = threadIdx.x; i < f.C; i += blockDim.x) {
+    const T *zi = z + (size_t)i * NR;
+    T *yi = y + dk_pos(rows, bs, i) * NR;
+#pragma unroll
+    for (int q = 0; q < NR; q++) yi[q] = zi[q];
   }
   if (v.sn_parent[s] >= 0) {
     T *w = contrib + v.v_off[s] * NR;
@@ -694,10 +709,12 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const bool inv = v.dinv_off[s] >= 0;
   const T *Xg = inv ? dk_dinv(v, (T *)nullptr) + v.dinv_off[s] : nullptr;
-  for (int t = threadIdx.x; t < f.M * NR; t += blockDim.x) {
-    const int i = t / NR, r = t - NR * (t / NR);
-    const size_t g = dk_pos(rows, bs, i) * NR + r;
-    z[t] = i < f.C ? y[g] : x[g];
+  for (int i = threadIdx.x; i < f.M; i += blockDim.x) {
+    const size_t g = dk_pos(rows, bs, i) * NR;
+    const T *src = i < f.C ? y + g : x + g;
+    T *zi = z + (size_t)i * NR;
+#pragma unroll
+    for (int q = 0; q < NR; q++) zi[q] = src[q];
   }
   __syncthreads();
   for (int j = threadIdx.x; j < f.C; j += blockDim.x) {
@@ -741,9 +758,11 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < f.C * NR; t += blockDim.x) {
-    const int i = t / NR, r = t - NR * (t / NR);
-    x[dk_pos(rows, bs, i) * NR + r] = z[t];
+  for (int i = threadIdx.x; i < f.C; i += blockDim.x) {
+    const T *zi = z + (size_t)i * NR;
+    T *xi = x + dk_pos(rows, bs, i) * NR;
+#pragma unroll
+    for (int q = 0; q < NR; q++) xi[q] = zi[q];
   }
 }
 
@@ -808,9 +827,17 @@ __global__ void __launch_bounds__(256)
   const T *inv = dk_dinv(v, (T *)nullptr) + v.dinv_off[s];
   const int nblk = (f.C + 31) >> 5;
   const int warp = (int)threadIdx.x >> 5, nwarp = (int)blockDim.x >> 5;
-  for (int t = threadIdx.x; t < nown * NR; t += blockDim.x) {
-    const int i = cr.row(t / NR), r = t - NR * (t / NR);
-    z[t] = (i < f.C) ? y[dk_pos(rows, bs, i) * NR + r] : T(0);
+  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
+    const int i = cr.row(t);
+    T *zt = z + (size_t)t * NR;
+    if (i < f.C) {
+      const T *yi = y + dk_pos(rows, bs, i) * NR;
+#pragma unroll
+      for (int q = 0; q < NR; q++) zt[q] = yi[q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < NR; q++) zt[q] = T(0);
+    }
   }
   __syncthreads();
   for (int k = v.ch_ptr[s]; k < v.ch_ptr[s + 1]; k++) {
@@ -819,10 +846,13 @@ __global__ void __launch_bounds__(256)
     const int um = fc.M - fc.C;
     const int *rel = v.ea_rel + v.ea_ptr[c];
     const T *w = contrib + v.v_off[c] * NR;
-    for (int t = threadIdx.x; t < um * NR; t += blockDim.x) {
-      const int i = t / NR, q = t - NR * (t / NR);
+    for (int i = threadIdx.x; i < um; i += blockDim.x) {
       const int r = rel[i / bs] * bs + i % bs;
-      if (cr.owns(r)) z[cr.slot(r) * NR + q] += w[t];
+      if (!cr.owns(r)) continue;
+      T *zr = z + (size_t)cr.slot(r) * NR;
+      const T *wi = w + (size_t)i * NR;
+#pragma unroll
+      for (int q = 0; q < NR; q++) zr[q] += wi[q];
     }
     __syncthreads();
   }
@@ -872,8 +902,8 @@ __global__ void __launch_bounds__(256)
       }
       if (!valid) continue;
       T *zg = z + (size_t)(g << 5) * NR;
-      dk_warp_rows<T, NR, 32>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk, valid,
-                            [&](int i) { return zg + i * NR; });
+      dk_warp_rows<T, NR, 32>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk,
+                              valid, [&](int i) { return zg + i * NR; });
     }
     __syncthreads();
   }

@@ -292,8 +292,9 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_dinv_off, dinv_off);
   d->contrib_len = vacc;
   // right-hand sides per solve pass: 4, unless the workspace of the largest
-  // front would not fit a CTA's shared memory
-  constexpr size_t kSmemMax = 227 * 1024;
+  // front would not fit a CTA's shared memory beside the solve kernels'
+  // static shared memory (at most 32 KB: staged rows, inverse blocks)
+  constexpr size_t kSmemMax = (227 - 32) * 1024;
   for (int nr : {4, 2, 1}) {
     d->max_nr = nr;
     if (tg::direct_solve_smem(d->plain_front, nr, sizeof(double)) <=
@@ -714,6 +715,7 @@ int tg_direct_get_stats(tg_direct *d, double *stats) {
   stats[4] = (double)d->an.flops_scalar(d->bs);
   stats[5] = d->max_front;
   stats[6] = d->precision;
+  stats[7] = (double)d->csolve_sn_h.size();
   return 0;
 }
 

@@ -215,6 +215,7 @@ class Direct:
         return {"supernodes": int(st[0]), "levels": int(st[1]),
                 "factor_bytes": st[2], "pool_bytes": st[3],
                 "flops": st[4], "max_front": int(st[5]),
+                "cluster_fronts": int(st[7]),
                 "fell_back_to_fp64": self.fell_back,
                 "last_refinement_steps": self.last_steps,
                 "last_backward_error": self.last_eta}
@@ -518,8 +519,11 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     reference harness (tests/integration_tests/static_analysis_base_test.py:
     359-427): K(u=0) and R(0), ILU(0), GMRES for R - f, functions, dfdu,
     adjoint solve with the same row-BC matrix, dfdx - psi^T dR/dx.  With
-    direct, both solves use the complete factorisation (Direct) instead;
-    direct="mixed" factors in FP32 and refines every solve in FP64."""
+    direct, both solves use the complete factorisation (Direct) instead,
+    refined to the relative residual rtol (or the FP64 floor) like the
+    Krylov solves; direct="mixed" factors in FP32 and refines every solve in
+    FP64, also until a step's correction is at most rtol |x|.  `iters`
+    then counts refinement steps."""
     dev = torch.device("cuda")
     u0 = model.vec()
     res = model.vec()
@@ -535,7 +539,10 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
             iters = 0
 
             def solve(self, b):
-                return dsol.solve(b), 1
+                x = dsol.solve(b, rtol=rtol,
+                               ftol=rtol if direct == "mixed" else 0.0)
+                self.iters = dsol.last_steps
+                return x, 1
         ksm = _Exact()
     else:
         prec = _lib.PREC_FP32 if mixed else _lib.PREC_FP64

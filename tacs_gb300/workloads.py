@@ -4,12 +4,19 @@
     python -m tacs_gb300.workloads hex [--n 64]
     python -m tacs_gb300.workloads spmv [--n 512]
     python -m tacs_gb300.workloads assemble [--n 256]
+    python -m tacs_gb300.workloads direct [--n 512]
+    python -m tacs_gb300.workloads batch [--count 48] [--nmax 256]
 
 gmres: one restart cycle of GMRES(m) + natural-order ILU(0) on an n x n
 clamped MITC4 plate (random right-hand side); hex: three residual +
 Jacobian assemblies of an n x n x n/2 hex8 SIMP block; spmv: five BCSR
 mat-vecs on an n x n clamped plate; assemble: three MITC4 assemblies of an
-n x n plate.  Each prints one line and exits 0 on success.
+n x n plate; direct: the complete factorisation of the simply supported
+n x n plate (2 m at 512 x 512) in FP64 and in FP32, one factorisation and
+one solve each; batch: the factorisation of the batch of clamped plates
+(N log-uniform in [16, nmax]) in FP32 and in FP64, then one 4-load-case
+solve of each (the FP32 one as one refinement step).  Each prints one line
+and exits 0 on success.
 """
 from __future__ import annotations
 
@@ -66,9 +73,52 @@ def assemble(n=256):
     return f"assemble elements={n * n} colours={M.ncolors}"
 
 
+def direct(n=512):
+    from . import _lib
+    p = meshes.plate_c2(n, 2.0 * n / 512)
+    M = problem.GpuModel(p)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    out = []
+    for prec in (_lib.PREC_FP64, _lib.PREC_FP32):
+        d = problem.Direct(mat, precision=prec)
+        d.factor()
+        b = -r0 if prec == _lib.PREC_FP64 else (-r0).float()
+        d.solve(b)
+        torch.cuda.synchronize()
+        out.append(f"prec={prec} supernodes={d.stats()['supernodes']}")
+        del d
+    return "direct " + " ".join(out)
+
+
+def batch(count=48, nmax=256):
+    from . import _lib
+    bp = meshes.batch_plates(count=count, nmax=nmax)
+    M = problem.GpuModel(bp)
+    M.set_fixed_geometry(True)
+    F = problem.batch_loads(M)
+    mat = M.new_mat()
+    M.assemble_jacobian(M.vec(), mat, M.vec())
+    for prec in (_lib.PREC_FP32, _lib.PREC_FP64):
+        d = problem.Direct(mat, precision=prec)
+        d.factor()
+        # FP32: one refinement step = one 4-right-hand-side FP32 solve
+        if prec == _lib.PREC_FP32:
+            d.solve(F, steps=1, tol=1.0)
+        else:
+            d.solve(F)
+        del d
+    torch.cuda.synchronize()
+    return f"batch plates={count} elements={bp['nelem']}"
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["gmres", "hex", "spmv", "assemble"])
+    ap.add_argument("case", choices=["gmres", "hex", "spmv", "assemble",
+                                     "direct", "batch"])
+    ap.add_argument("--count", type=int, default=48)
+    ap.add_argument("--nmax", type=int, default=256)
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--m", type=int, default=30)
     ap.add_argument("--mixed", action="store_true")
@@ -79,6 +129,10 @@ def main(argv=None):
         print(hex_block(a.n or 64))
     elif a.case == "spmv":
         print(spmv(a.n or 512))
+    elif a.case == "direct":
+        print(direct(a.n or 512))
+    elif a.case == "batch":
+        print(batch(a.count, a.nmax))
     else:
         print(assemble(a.n or 256))
 

@@ -19,6 +19,7 @@ static EmuDim3 threadIdx{0, 0, 0}, blockIdx{0, 0, 0}, blockDim{1, 1, 1},
     gridDim{1, 1, 1};
 #define __global__
 #define __device__
+#define __host__
 #define __forceinline__ inline
 #define __shared__ static
 #define __launch_bounds__(n)

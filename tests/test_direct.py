@@ -263,18 +263,29 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
 
 
 @pytest.mark.parametrize("nrhs", [3, 4, 6])
-def test_direct_multi_rhs(gpu, nrhs):
+@pytest.mark.parametrize("case", ["shell_c1", "plate_c2_128"])
+def test_direct_multi_rhs(gpu, nrhs, case):
     """Several right-hand sides per pass over the factor
     (tg_direct_solve_multi, tg_direct_solve_refined_multi): FP64 solutions
     are bitwise those of single solves; the FP32 factorisation refines all
     of them together with a stopping test per right-hand side, and each
     ends within 1e-10 of the FP64 solution, as a single refined solve
-    does."""
-    from tacs_gb300 import _lib
-    prob, _ = load_case("shell_c1")
-    M = gpu.GpuModel(prob)
-    mat = M.new_mat()
-    b0 = _rhs(M, prob, mat)
+    does.  On the C1 fixture and on a 128 x 128 plate (fronts solved by
+    one CTA up to 768 rows and by thread-block clusters above)."""
+    from tacs_gb300 import _lib, meshes
+    if case == "plate_c2_128":  # fronts of up to ~1,500 rows: the one-CTA
+        # solves' largest workspace and the cluster solves
+        prob = meshes.plate_c2(128, 0.5, seed=2)
+        M = gpu.GpuModel(prob)
+        mat = M.new_mat()
+        b0 = M.vec()
+        M.assemble_jacobian(M.vec(), mat, b0)
+        b0 = -b0
+    else:
+        prob, _ = load_case(case)
+        M = gpu.GpuModel(prob)
+        mat = M.new_mat()
+        b0 = _rhs(M, prob, mat)
     g = torch.Generator(device="cuda").manual_seed(nrhs)
     B = torch.randn(nrhs, M.ndof, dtype=torch.float64, device="cuda",
                     generator=g)
@@ -283,6 +294,8 @@ def test_direct_multi_rhs(gpu, nrhs):
         M.apply_bcs(B[r])
     d = gpu.Direct(mat)
     d.factor()
+    if case == "plate_c2_128":
+        assert d.stats()["cluster_fronts"] > 0
     X = d.solve(B)
     for r in range(nrhs):
         assert torch.equal(X[r], d.solve(B[r].clone()))
