@@ -40,6 +40,13 @@ void launch_direct_factor_small(const DirectView &v, const int *sn,
   direct_factor_small_kernel<T><<<count, 256, 0, s>>>(v, sn, count, fail);
 }
 
+template <class T>
+void launch_direct_inverses(const DirectView &v, const int *inv_sn,
+                            const int *inv_k0, int count, cudaStream_t s) {
+  if (count <= 0) return;
+  direct_inverse_kernel<T><<<count, 32, 0, s>>>(v, inv_sn, inv_k0, count);
+}
+
 size_t direct_panel_smem(size_t elem) {
   return elem * kDirectTrsmRows * (kDirectPanel + 1);
 }
@@ -63,28 +70,33 @@ void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                                                          count, k0);
 }
 
-// the solves' kernels for NR = 1, 2 or 4 right-hand sides at once
+// the solves' kernels for NR = 1, 2 or 4 right-hand sides at once; a
+// level whose fronts have at most 128 rows takes CTAs of 64 threads (more
+// of them resident per SM, beside the smaller shared memory)
+static int plain_threads(int max_front) {
+  return max_front <= 128 ? 64 : kDirectPlainThreads;
+}
 template <class T>
-static void forward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
+static void forward_plain(int nr, dim3 g, int nt, size_t smem, cudaStream_t s,
                           const DirectView &v, const int *sn, int count,
                           T *y, T *contrib) {
   if (nr == 4)
-    direct_forward_kernel<T, 4><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 4><<<g, nt, smem, s>>>(v, sn, count, y, contrib);
   else if (nr == 2)
-    direct_forward_kernel<T, 2><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 2><<<g, nt, smem, s>>>(v, sn, count, y, contrib);
   else
-    direct_forward_kernel<T, 1><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, contrib);
+    direct_forward_kernel<T, 1><<<g, nt, smem, s>>>(v, sn, count, y, contrib);
 }
 template <class T>
-static void backward_plain(int nr, dim3 g, size_t smem, cudaStream_t s,
-                           const DirectView &v, const int *sn, int count,
-                           const T *y, T *x) {
+static void backward_plain(int nr, dim3 g, int nt, size_t smem,
+                           cudaStream_t s, const DirectView &v, const int *sn,
+                           int count, const T *y, T *x) {
   if (nr == 4)
-    direct_backward_kernel<T, 4><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 4><<<g, nt, smem, s>>>(v, sn, count, y, x);
   else if (nr == 2)
-    direct_backward_kernel<T, 2><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 2><<<g, nt, smem, s>>>(v, sn, count, y, x);
   else
-    direct_backward_kernel<T, 1><<<g, kDirectPlainThreads, smem, s>>>(v, sn, count, y, x);
+    direct_backward_kernel<T, 1><<<g, nt, smem, s>>>(v, sn, count, y, x);
 }
 
 size_t direct_solve_smem(int front, int nr, size_t elem) {
@@ -96,8 +108,9 @@ void launch_direct_forward(const DirectView &v, const int *sn, int count,
                            int max_front, int nr, T *y, T *contrib,
                            cudaStream_t s) {
   if (count <= 0) return;
-  forward_plain<T>(nr, dim3(count), direct_solve_smem(max_front, nr, sizeof(T)),
-                   s, v, sn, count, y, contrib);
+  forward_plain<T>(nr, dim3(count), plain_threads(max_front),
+                   direct_solve_smem(max_front, nr, sizeof(T)), s, v, sn,
+                   count, y, contrib);
 }
 
 template <class T>
@@ -105,7 +118,7 @@ void launch_direct_backward(const DirectView &v, const int *sn, int count,
                             int max_front, int nr, const T *y, T *x,
                             cudaStream_t s) {
   if (count <= 0) return;
-  backward_plain<T>(nr, dim3(count),
+  backward_plain<T>(nr, dim3(count), plain_threads(max_front),
                     direct_solve_smem(max_front, nr, sizeof(T)), s, v, sn,
                     count, y, x);
 }
@@ -303,6 +316,8 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
                                                 const int *, int,          \
                                                 const double *, int, int,  \
                                                 int, cudaStream_t);        \
+  template void launch_direct_inverses<T>(const DirectView &, const int *, \
+                                         const int *, int, cudaStream_t);  \
   template void launch_direct_factor_small<T>(const DirectView &,          \
                                               const int *, int, int *,     \
                                               cudaStream_t);               \

@@ -261,30 +261,49 @@ __global__ void __launch_bounds__(256)
     const int r = t / nb, c = t - nb * (t / nb);
     if (c <= r) f.at(k0 + r, k0 + c) = Ld[r][c];
   }
-  if (v.dinv_off[s] < 0) return;
-  // X = L^-1 of the factored block, row by row: X(i, :) = (e_i -
-  // sum_{q < i} L(i, q) X(q, :)) / L(i, i) (warp 0, lane j on column j);
-  // stored row-major in a 32 x 32 slot, zero elsewhere
-  __shared__ T X[kPanel][kPanel + 1];
-  if (threadIdx.x < 32) {
-    const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
-    for (int i = 0; i < nb; i++) {
-      for (int j = threadIdx.x; j < kPanel; j += ls) {
-        T acc = i == j ? T(1) : T(0);
-        if (j <= i) {
-          for (int q = j; q < i; q++) acc -= Ld[i][q] * X[q][j];
-          acc = acc / Ld[i][i];
-        } else {
-          acc = T(0);
-        }
-        X[i][j] = acc;
-      }
-      __syncwarp();
-    }
+}
+
+// Inverses of the factored 32 x 32 diagonal blocks, for the solves (one
+// launch after the factorisation, off its critical path): block b is
+// panel inv_k0[b] of supernode inv_sn[b]; one warp each.  X = L^-1 row by
+// row, X(i, :) = (e_i - sum_{q < i} L(i, q) X(q, :)) / L(i, i) with the
+// reciprocal pivots formed once (lane j on column j), stored row-major in
+// the block's 32 x 32 slot of dinv, zero elsewhere.
+template <class T>
+__global__ void __launch_bounds__(32)
+    direct_inverse_kernel(DirectView v, const int *__restrict__ inv_sn,
+                          const int *__restrict__ inv_k0, int count) {
+  const int b = blockIdx.x;
+  if (b >= count) return;
+  const int s = inv_sn[b], k0 = inv_k0[b];
+  const Front<T> f = front_of<T>(v, s);
+  const int nb = f.C - k0 < kPanel ? f.C - k0 : kPanel;
+  __shared__ T Ld[kPanel][kPanel + 1], X[kPanel][kPanel + 1];
+  __shared__ T rd[kPanel];
+  const int ls = blockDim.x < 32 ? (int)blockDim.x : 32;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t - nb * (t / nb);
+    Ld[r][c] = c <= r ? f.at(k0 + r, k0 + c) : T(0);
   }
-  __syncthreads();
-  T *out = dk_dinv(v, (T *)nullptr) + v.dinv_off[s] + (size_t)(k0 / kPanel) *
-                                                         kPanel * kPanel;
+  __syncwarp();
+  for (int i = threadIdx.x; i < nb; i += ls) rd[i] = T(1) / Ld[i][i];
+  __syncwarp();
+  for (int i = 0; i < nb; i++) {
+    for (int j = threadIdx.x; j < kPanel; j += ls) {
+      T x = T(0);
+      if (j == i) {
+        x = rd[i];
+      } else if (j < i) {
+        T acc = T(0);
+        for (int q = j; q < i; q++) acc += Ld[i][q] * X[q][j];
+        x = -acc * rd[i];
+      }
+      X[i][j] = x;
+    }
+    __syncwarp();
+  }
+  T *out = dk_dinv(v, (T *)nullptr) + v.dinv_off[s] +
+           (size_t)(k0 / kPanel) * kPanel * kPanel;
   for (int t = threadIdx.x; t < kPanel * kPanel; t += blockDim.x) {
     const int r = t / kPanel, c = t - kPanel * (t / kPanel);
     out[t] = r < nb ? X[r][c] : T(0);

@@ -58,6 +58,9 @@ struct tg_direct {
   // and, above kDirectClusterFront rows, one thread-block cluster each
   // (d_csolve_sn, csolve_ptr_h)
   std::vector<int> solve_ptr_h, csolve_ptr_h;
+  // per level: the largest front solved by one CTA (the launch's shared
+  // memory and CTA size)
+  std::vector<int> solve_front_h;
   int *d_solve_sn = nullptr, *d_csolve_sn = nullptr;
   std::vector<int> solve_sn_h, csolve_sn_h;
   tg::direct::PanelSteps steps;
@@ -71,7 +74,10 @@ struct tg_direct {
       *d_ch_ptr = nullptr, *d_ch_list = nullptr, *d_level_sn = nullptr;
   int64_t *d_l_off = nullptr, *d_u_off = nullptr, *d_v_off = nullptr,
           *d_dinv_off = nullptr;
-  // inverses of the diagonal blocks of the fronts factored by panels
+  // inverses of the diagonal blocks of the fronts factored by panels, and
+  // the (supernode, first column) list of those blocks
+  int *d_inv_sn = nullptr, *d_inv_k0 = nullptr;
+  int inv_count = 0;
   double *d_dinv = nullptr;
   float *d_dinv32 = nullptr;
   double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
@@ -134,6 +140,7 @@ struct tg_direct {
     dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
     dfree(d_dinv_off); dfree(d_dinv); dfree(d_dinv32);
+    dfree(d_inv_sn); dfree(d_inv_k0);
   }
 };
 
@@ -221,6 +228,10 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
       }
       d->solve_ptr_h.push_back((int)a.size());
       d->csolve_ptr_h.push_back((int)b.size());
+      int pf = 0;
+      for (int t = d->solve_ptr_h[L]; t < d->solve_ptr_h[L + 1]; t++)
+        pf = std::max(pf, d->front_m_h[a[t]]);
+      d->solve_front_h.push_back(pf);
     }
     d->solve_sn_h = a;
     d->csolve_sn_h = b;
@@ -228,14 +239,18 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   // the fronts factored by panels keep the inverses of their diagonal
   // blocks (the solves' block steps become 32 x 32 products)
   std::vector<int64_t> dinv_off(d->ns, -1);
+  std::vector<int> inv_sn, inv_k0;
   int64_t dinv_len = 0;
   for (int sn = 0; sn < d->ns; sn++) {
     if (d->front_m_h[sn] <= kSmallFront) continue;
     dinv_off[sn] = dinv_len;
-    dinv_len += (int64_t)((d->front_c_h[sn] + tg::kDirectPanel - 1) /
-                          tg::kDirectPanel) *
-                tg::kDirectPanel * tg::kDirectPanel;
+    for (int k0 = 0; k0 < d->front_c_h[sn]; k0 += tg::kDirectPanel) {
+      inv_sn.push_back(sn);
+      inv_k0.push_back(k0);
+      dinv_len += (int64_t)tg::kDirectPanel * tg::kDirectPanel;
+    }
   }
+  d->inv_count = (int)inv_sn.size();
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
     int nch = 0, um = 0;
     int64_t zmax = 0;
@@ -290,6 +305,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_u_off, an.u_off);
   if (!rc) rc = upload(&d->d_v_off, v_off);
   if (!rc) rc = upload(&d->d_dinv_off, dinv_off);
+  if (!rc && d->inv_count) rc = upload(&d->d_inv_sn, inv_sn);
+  if (!rc && d->inv_count) rc = upload(&d->d_inv_k0, inv_k0);
   d->contrib_len = vacc;
   // right-hand sides per solve pass: 4, unless the workspace of the largest
   // front would not fit a CTA's shared memory beside the solve kernels'
@@ -383,6 +400,8 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
           d->tile, d->d_fail, s);
     }
   }
+  tg::launch_direct_inverses<T>(v, d->d_inv_sn, d->d_inv_k0, d->inv_count,
+                                s);
 }
 
 // X = A^-1 B in T for nrhs right-hand sides N = n bs apart: per pass of
@@ -411,7 +430,7 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
     for (int L = 0; L < nl; L++) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
       tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
-                                   d->plain_front, nr, ypos, contrib, s);
+                                   d->solve_front_h[L], nr, ypos, contrib, s);
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
       tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
                                            d->cluster_front, nr, ypos,
@@ -420,7 +439,7 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
     for (int L = nl - 1; L >= 0; L--) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
       tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
-                                    d->plain_front, nr, ypos, xpos, s);
+                                    d->solve_front_h[L], nr, ypos, xpos, s);
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
       tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
                                             d->cluster_front, nr, ypos, xpos,

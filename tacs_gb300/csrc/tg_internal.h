@@ -350,6 +350,11 @@ void launch_direct_panel_step(const DirectView &v, const int *sn, int count,
                               int tile, int *fail, cudaStream_t s);
 // dynamic shared memory of the panel kernel (staged rows)
 size_t direct_panel_smem(size_t elem);
+// the inverses of the factored diagonal blocks (count blocks: panel
+// inv_k0[b] of supernode inv_sn[b]), after the factorisation
+template <class T>
+void launch_direct_inverses(const DirectView &v, const int *inv_sn,
+                            const int *inv_k0, int count, cudaStream_t s);
 template <class T>
 void launch_direct_forward(const DirectView &v, const int *sn, int count,
                            int max_front, int nr, T *y, T *contrib,

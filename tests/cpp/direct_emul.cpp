@@ -167,12 +167,16 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
   // the fronts factored by panels keep the inverses of their diagonal
   // blocks, as in tg_direct.cu
   std::vector<int64_t> dinv_off(ns, -1);
+  std::vector<int> inv_sn, inv_k0;
   int64_t dinv_len = 0;
   for (int sn = 0; sn < ns; sn++) {
     if (fm[sn] <= small_max) continue;
     dinv_off[sn] = dinv_len;
-    dinv_len += (int64_t)((fc[sn] + tg::kDirectPanel - 1) / tg::kDirectPanel) *
-                tg::kDirectPanel * tg::kDirectPanel;
+    for (int k0 = 0; k0 < fc[sn]; k0 += tg::kDirectPanel) {
+      inv_sn.push_back(sn);
+      inv_k0.push_back(k0);
+      dinv_len += (int64_t)tg::kDirectPanel * tg::kDirectPanel;
+    }
   }
   std::vector<T> dinv(dinv_len > 0 ? (size_t)dinv_len : 1);
   v.dinv_off = dinv_off.data();
@@ -244,6 +248,11 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     }
   }
   if (failflag) return failflag;
+  // the inverses of the diagonal blocks, after the factorisation
+  if (!inv_sn.empty())
+    launch(direct_inverse_kernel<T>, (unsigned)inv_sn.size(), 1, 0, v,
+           (const int *)inv_sn.data(), (const int *)inv_k0.data(),
+           (int)inv_sn.size());
 
   // solve: the sequence of tg_direct_solve (on the GPU fronts of more than
   // kDirectClusterFront rows take the cluster kernels, one thread-block
