@@ -77,6 +77,54 @@ inline int color_elements(int nn, int npe, int nelem, const int *conn,
   return ncol;
 }
 
+// First writers of a 4-node element assembly launched colour by colour
+// (colour_ptr / colour_elems, in launch order): bit 4 a + b of first[e]
+// is set when element e is the first to write block (node a, node b) of
+// the pattern (rowp, cols), bit 16 + a when it is the first to write
+// node a's residual rows.  Elements of one colour share no node, so each
+// block and node has exactly one first writer, which can store instead of
+// add (no zero fill).  Returns false -- and no masks -- when a node is in
+// no element (its rows would never be written).
+inline bool first_writers(int nn, int nelem, const int *conn,
+                          const std::vector<int> &rowp,
+                          const std::vector<int> &cols,
+                          const std::vector<int> &color_ptr,
+                          const std::vector<int> &color_elems,
+                          std::vector<uint32_t> &first) {
+  std::vector<char> node_seen(nn, 0), blk_seen(cols.size(), 0);
+  first.assign(nelem, 0u);
+  for (size_t c = 0; c + 1 < color_ptr.size(); c++)
+    for (int k = color_ptr[c]; k < color_ptr[c + 1]; k++) {
+      const int e = color_elems[k];
+      const int *nd = conn + 4 * (size_t)e;
+      uint32_t m = 0;
+      for (int a = 0; a < 4; a++) {
+        if (!node_seen[nd[a]]) {
+          node_seen[nd[a]] = 1;
+          m |= 1u << (16 + a);
+        }
+        for (int b = 0; b < 4; b++) {
+          const int *lo = cols.data() + rowp[nd[a]];
+          const int *hi = cols.data() + rowp[nd[a] + 1];
+          const int *it = std::lower_bound(lo, hi, nd[b]);
+          if (it == hi || *it != nd[b]) return false;
+          const size_t slot = (size_t)(it - cols.data());
+          if (!blk_seen[slot]) {
+            blk_seen[slot] = 1;
+            m |= 1u << (4 * a + b);
+          }
+        }
+      }
+      first[e] = m;
+    }
+  for (int i = 0; i < nn; i++)
+    if (!node_seen[i]) {
+      first.clear();
+      return false;
+    }
+  return true;
+}
+
 // Greedy colouring of the node graph (rowp, cols) in node order: each node
 // takes the smallest colour none of its already coloured neighbours has.
 // Returns the number of colours.

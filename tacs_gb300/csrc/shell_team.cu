@@ -21,7 +21,9 @@
 // rows) are those of TACSShellElement::addJacobian
 // (src/elements/shell/TACSShellElement.h:436-641) as in shell_kernels.cu.
 // Elements of one launch share no node (colouring): the BCSR
-// read-modify-write and the residual scatter need no atomics.
+// read-modify-write and the residual scatter need no atomics, and the
+// first writer of each block and residual row (MeshView::first) stores
+// instead of adding, so neither needs a zero fill.
 #include <cmath>
 
 #include "tg_internal.h"
@@ -58,7 +60,8 @@ struct __align__(16) TeamSmem {
   TeamGeo g;  // T is reused for the residual's channel projections
   int nodes[4];
   int slot[16];
-  int pad[2];
+  unsigned first;  // MeshView::first of the element (0: add everything)
+  int pad;
 };
 
 // Shape functions of node k or Gauss point q (index < 4: node, else point)
@@ -173,7 +176,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
       if (tl < 4) {
         S.nodes[tl] = m.conn[4 * e + tl];
       }
-      if (tl == 0) S.t = m.thick[e];
+      if (tl == 0) {
+        S.t = m.thick[e];
+        S.first = m.first ? m.first[e] : 0u;
+      }
     }
     __syncwarp();
     if (active) {
@@ -490,7 +496,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
             aux += s_shape.N[4 + q][mm] * (S.prd[q] * S.n0[q][a]);
           r += lambda * aux;
         }
-        if (active) res[6 * S.nodes[mm] + a] += r;
+        if (active) {
+          double &dst = res[6 * S.nodes[mm] + a];
+          dst = ((S.first >> (16 + mm)) & 1u) ? r : dst + r;
+        }
       }
     }
 
@@ -514,23 +523,40 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
         const int a = ti >> 1, b = tj >> 1;
         const int ii0 = 3 * (ti & 1), jj0 = 3 * (tj & 1);
         const int s_ab = S.slot[4 * a + b];
+        // the element's first write of a block stores (no zero fill)
         if (s_ab >= 0) {
           double *blk = mat + 36 * (size_t)s_ab;
+          if ((S.first >> (4 * a + b)) & 1u) {
 #pragma unroll
-          for (int r = 0; r < 3; r++)
+            for (int r = 0; r < 3; r++)
 #pragma unroll
-            for (int q = 0; q < 3; q++)
-              blk[6 * (ii0 + r) + jj0 + q] += v[3 * r + q];
+              for (int q = 0; q < 3; q++)
+                blk[6 * (ii0 + r) + jj0 + q] = v[3 * r + q];
+          } else {
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+              for (int q = 0; q < 3; q++)
+                blk[6 * (ii0 + r) + jj0 + q] += v[3 * r + q];
+          }
         }
         if (ti != tj) {
           const int s_ba = S.slot[4 * b + a];
           if (s_ba >= 0) {
             double *blk = mat + 36 * (size_t)s_ba;
+            if ((S.first >> (4 * b + a)) & 1u) {
 #pragma unroll
-            for (int r = 0; r < 3; r++)
+              for (int r = 0; r < 3; r++)
 #pragma unroll
-              for (int q = 0; q < 3; q++)
-                blk[6 * (jj0 + q) + ii0 + r] += v[3 * r + q];
+                for (int q = 0; q < 3; q++)
+                  blk[6 * (jj0 + q) + ii0 + r] = v[3 * r + q];
+            } else {
+#pragma unroll
+              for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+                  blk[6 * (jj0 + q) + ii0 + r] += v[3 * r + q];
+            }
           }
         }
       }

@@ -21,6 +21,10 @@
 #define TG_DIRECT_SMALL_FRONT 64
 #endif
 static constexpr int kSmallFront = TG_DIRECT_SMALL_FRONT;
+// trailing tile of the FP64 factorisation (32 or 64; the FP32 one uses 64)
+#ifndef TG_DIRECT_TILE_F64
+#define TG_DIRECT_TILE_F64 32
+#endif
 // blocks of the max-|x| reductions of the refinement's stopping test
 static constexpr int kRedParts = 256;
 
@@ -207,7 +211,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     }
     d->small_ptr_h.push_back((int)small_h.size());
   }
-  d->tile = precision == TG_PREC_FP32 ? tg::kDirectTile32 : tg::kDirectTile;
+  d->tile = precision == TG_PREC_FP32 ? tg::kDirectTile32 : TG_DIRECT_TILE_F64;
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
                                      d->tile, tg::kDirectTrsmRows);
   {

@@ -34,6 +34,10 @@ struct MeshView {
   // element; nullptr: the kernels form B from the node coordinates
   const double *geo_B;
   const int *geo_cls;
+  // shell assembly: the blocks and residual rows element e writes first
+  // in the colour order (mesh_graph.h first_writers): stored, not added,
+  // so the matrix and residual need no zero fill; nullptr: add everything
+  const unsigned *first;
 };
 
 // One launch of an element kernel covers the elements of one colour:

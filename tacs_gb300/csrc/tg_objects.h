@@ -70,6 +70,8 @@ struct tg_assembler {
   int *d_bc_nodes = nullptr, *d_bc_masks = nullptr;
   int *d_rowp = nullptr, *d_cols = nullptr, *d_diag = nullptr;
   int *d_color_elems = nullptr;
+  // first-writer masks of the shell assembly (empty: zero fill and add)
+  unsigned *d_first = nullptr;
   int *d_dv_ptr = nullptr, *d_dv_elems = nullptr;
   double *d_elem_fail = nullptr, *d_elem_wdet = nullptr;
   double *d_elem_sed = nullptr, *d_elem_val = nullptr;
@@ -122,6 +124,7 @@ struct tg_assembler {
     const bool geo = geo_enabled && geo_table_valid && d_geo_B;
     m.geo_B = geo ? d_geo_B : nullptr;
     m.geo_cls = geo ? d_geo_cls : nullptr;
+    m.first = d_first;
     return m;
   }
   // view whose KS sensitivities use the per-segment statistics
@@ -144,6 +147,7 @@ struct tg_assembler {
     dfree(d_dvnum); dfree(d_trac_ptr); dfree(d_trac_face); dfree(d_trac_val);
     dfree(d_bc_nodes); dfree(d_bc_masks); dfree(d_rowp); dfree(d_cols);
     dfree(d_diag); dfree(d_color_elems); dfree(d_dv_ptr); dfree(d_dv_elems);
+    dfree(d_first);
     dfree(d_elem_fail); dfree(d_elem_wdet); dfree(d_elem_sed);
     dfree(d_elem_val); dfree(d_partials); dfree(d_scalars);
     dfree(d_elem_seg); dfree(d_seg_elem_ptr); dfree(d_seg_ks);

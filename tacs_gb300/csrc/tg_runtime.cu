@@ -242,6 +242,15 @@ int tg_assembler_initialize(tg_assembler *a) {
   if ((rc = upload(&a->d_cols, a->cols_h))) return rc;
   if ((rc = upload(&a->d_diag, a->diag_h))) return rc;
   if ((rc = upload(&a->d_color_elems, a->color_elems_h))) return rc;
+  if (a->ep.elem_type == TG_ELEM_MITC4) {
+    std::vector<uint32_t> first;
+    if (graph::first_writers(a->nnodes, a->nelem, a->conn_h.data(),
+                             a->rowp_h, a->cols_h, a->color_ptr_h,
+                             a->color_elems_h, first)) {
+      std::vector<unsigned> fu(first.begin(), first.end());
+      if ((rc = upload(&a->d_first, fu))) return rc;
+    }
+  }
   if ((rc = upload(&a->d_dv_ptr, dv_ptr))) return rc;
   if ((rc = upload(&a->d_dv_elems, dv_elems))) return rc;
   const size_t nq = (size_t)a->nq() * a->nelem;
@@ -415,8 +424,10 @@ int tg_assemble_res(tg_assembler *a, const double *vars, double lambda,
     TG_CUDA(cudaGetLastError());
     return 0;
   }
-  TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
   MeshView m = a->view();
+  // the shell kernels store what they write first (no zero fill)
+  const bool first = m.first && a->ep.elem_type == TG_ELEM_MITC4;
+  if (!first) TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
   for (int c = 0; c < a->ncolors(); c++) {
     if (a->ep.elem_type == TG_ELEM_MITC4)
       launch_shell_team_assembly(a->ep, m, a->color(c), vars, lambda, res,
@@ -496,11 +507,15 @@ int tg_assemble_jacobian(tg_assembler *a, double alpha, double beta,
     TG_CUDA(cudaGetLastError());
     return 0;
   }
-  if (res) TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
-  TG_CUDA(cudaMemsetAsync(A->d_vals, 0,
-                          sizeof(double) * (size_t)A->nnz * A->bsize * A->bsize,
-                          S(s)));
   MeshView m = a->view();
+  // the shell kernels store what they write first (no zero fill)
+  const bool first = m.first && a->ep.elem_type == TG_ELEM_MITC4;
+  if (!first) {
+    if (res) TG_CUDA(cudaMemsetAsync(res, 0, n * sizeof(double), S(s)));
+    TG_CUDA(cudaMemsetAsync(
+        A->d_vals, 0, sizeof(double) * (size_t)A->nnz * A->bsize * A->bsize,
+        S(s)));
+  }
   for (int c = 0; c < a->ncolors(); c++) {
     if (a->ep.elem_type == TG_ELEM_MITC4)
       launch_shell_team_assembly(a->ep, m, a->color(c), vars, lambda, res,

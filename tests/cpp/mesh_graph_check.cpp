@@ -30,4 +30,22 @@ int mg_pattern_and_node_colors(int nn, int npe, int nelem, const int *conn,
   return (int)cs.size();
 }
 
+// first-writer masks of a 4-node mesh assembled colour by colour (the
+// colouring of color_elements); returns 1 with first[nelem] filled, or 0
+int mg_first_writers(int nn, int nelem, const int *conn, unsigned *first) {
+  std::vector<int> rp, cs, dg, c;
+  tg::graph::node_pattern(nn, 4, nelem, conn, rp, cs, dg);
+  const int ncol = tg::graph::color_elements(nn, 4, nelem, conn, c);
+  std::vector<int> cptr(ncol + 1, 0), celems(nelem);
+  for (int e = 0; e < nelem; e++) cptr[c[e] + 1]++;
+  for (int k = 0; k < ncol; k++) cptr[k + 1] += cptr[k];
+  std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+  for (int e = 0; e < nelem; e++) celems[fill[c[e]]++] = e;
+  std::vector<uint32_t> f;
+  if (!tg::graph::first_writers(nn, nelem, conn, rp, cs, cptr, celems, f))
+    return 0;
+  for (int e = 0; e < nelem; e++) first[e] = f[e];
+  return 1;
+}
+
 }  // extern "C"

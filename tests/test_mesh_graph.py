@@ -37,6 +37,7 @@ def mg(tmp_path_factory):
     lib.mg_color_elements.argtypes = [C.c_int, C.c_int, C.c_int, P, P]
     lib.mg_pattern_and_node_colors.argtypes = [C.c_int, C.c_int, C.c_int, P,
                                                C.c_int, P, P, P, P]
+    lib.mg_first_writers.argtypes = [C.c_int, C.c_int, P, P]
     return lib
 
 
@@ -238,3 +239,44 @@ def test_setters_validate_before_changing_state(L):
         assert [s.value for s in sizes[:3]] == [6, nn, 4]
     finally:
         L.tg_assembler_decref(h)
+
+
+@pytest.mark.parametrize("mesh", ["plate", "fan", "random"])
+def test_first_writers(mg, mesh):
+    """The shell assembly's first-writer masks (mesh_graph.h first_writers):
+    every pattern block (node pair of an element) and every node has
+    exactly one first writer, and it is the element of the lowest colour
+    among those that touch it (colours are launched in order, and elements
+    of one colour share no node).  A node in no element yields no masks."""
+    nn, npe, conn = {"plate": lambda: _quad_plate(9, 7),
+                     "fan": lambda: _fan(96),
+                     "random": lambda: _random_mesh(3)}[mesh]()
+    if npe != 4:
+        pytest.skip("4-node meshes only")
+    ne = len(conn) // 4
+    col = np.zeros(ne, np.int32)
+    mg.mg_color_elements(nn, 4, ne, _p(conn), _p(col))
+    first = np.zeros(ne, np.uint32)
+    assert mg.mg_first_writers(nn, ne, _p(conn), _p(first)) == 1
+    c4 = conn.reshape(-1, 4)
+    blk, nod = {}, {}
+    for e in range(ne):
+        for a in range(4):
+            nod.setdefault(int(c4[e, a]), []).append(e)
+            for b in range(4):
+                blk.setdefault((int(c4[e, a]), int(c4[e, b])), []).append(
+                    (e, a, b))
+    for key, users in blk.items():
+        owners = [(e, a, b) for e, a, b in users
+                  if (int(first[e]) >> (4 * a + b)) & 1]
+        assert len(owners) == 1
+        assert col[owners[0][0]] == min(col[e] for e, _, _ in users)
+    for node, users in nod.items():
+        owners = [e for e in users
+                  if any((int(first[e]) >> (16 + a)) & 1
+                         for a in range(4) if c4[e, a] == node)]
+        assert len(owners) == 1
+        assert col[owners[0]] == min(col[e] for e in users)
+    # a node in no element: no masks (the assembly falls back to zero fill)
+    conn2 = np.concatenate([conn, np.zeros(0, np.int32)])
+    assert mg.mg_first_writers(nn + 1, ne, _p(conn2), _p(first)) == 0
