@@ -205,9 +205,10 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
    tg_direct_solve_f32, e.g. as the preconditioner of an FP64 iteration.
    tg_direct_factor synchronises and returns TG_ERR_PIVOT on a
    non-positive pivot.
-   stats (8 doubles): supernodes, tree levels, factor bytes (FP64
+   stats (9 doubles): supernodes, tree levels, factor bytes (FP64
    storage), update-pool bytes (FP64), dense flops, largest front (scalar
-   rows), precision, fronts solved by thread-block clusters. */
+   rows), precision, fronts solved by thread-block clusters, the front
+   rows above which they are. */
 int tg_direct_create(tg_mat *A, int use_coords, int precision,
                      tg_direct **out);
 int tg_direct_factor(tg_direct *d, void *stream);
@@ -266,6 +267,16 @@ int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
                                   double *x, int max_steps, double tol,
                                   double ftol, double rtol, int *steps,
                                   double *eta, void *stream);
+/* Launch-shape autotuner of the solves (no reference counterpart): times a
+   solve of the factored matrix for each threshold above which fronts are
+   solved by thread-block clusters (384, 768, 1536 rows; one CTA each
+   below) and keeps the fastest.  The choice is cached per (rows, blocks,
+   block size, precision, device), so another factorisation of the same
+   shape reuses it without timing.  threshold and ms (3 doubles, may be
+   NULL) receive the choice and the per-solve times (0 when cached).
+   Synchronises the stream. */
+int tg_direct_autotune(tg_direct *d, int *threshold, double *ms,
+                       void *stream);
 int tg_direct_get_stats(tg_direct *d, double *stats);
 int tg_direct_decref(tg_direct *d);
 

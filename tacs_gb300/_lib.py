@@ -65,6 +65,7 @@ SIGNATURES = [
                                          C.POINTER(C.c_double), _P]),
     ("tg_direct_solve_refined_multi", _I, [_P, _I, _P, _P, _I, _D, _D, _D,
                                            _P, _P, _P]),
+    ("tg_direct_autotune", _I, [_P, _IP, _P, _P]),
     ("tg_direct_get_stats", _I, [_P, _P]),
     ("tg_direct_decref", _I, [_P]),
     ("tg_add_xpt_sens", _I, [_P, _P, _I, _P, _D, _P, _P]),

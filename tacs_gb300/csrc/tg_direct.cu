@@ -9,6 +9,9 @@
 // too (symmetric positive definite) and P keeping the boundary dofs.
 #include <algorithm>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "direct_symbolic.h"
@@ -47,6 +50,10 @@ struct tg_direct {
   // right-hand sides one solve pass takes (1, 2 or 4; the solve vectors
   // and refinement scratch hold that many)
   int plain_front = 0, cluster_front = 0, max_nr = 1;
+  // fronts above cluster_threshold rows are solved by clusters (when the
+  // device schedules them); tg_direct_autotune picks it
+  bool clusters_ok = false;
+  int cluster_threshold = tg::kDirectClusterFront;
   int precision = TG_PREC_FP64;
   tg::direct::Analysis an;
   std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
@@ -148,6 +155,53 @@ struct tg_direct {
   }
 };
 
+// the largest front the autotuner may leave to the one-CTA solves
+static constexpr int kTuneMaxFront = 1536;
+
+// The solves' per-level front lists for a cluster threshold: fronts of more
+// than `threshold` rows take the cluster kernels (when the device schedules
+// them), the others one CTA each; uploads the lists and sets the kernels'
+// shared-memory attributes.
+static int build_solve_lists(tg_direct *d, int threshold) {
+  const tg::direct::Analysis &an = d->an;
+  std::vector<int> a, b;
+  d->solve_ptr_h.assign(1, 0);
+  d->csolve_ptr_h.assign(1, 0);
+  d->solve_front_h.clear();
+  d->plain_front = d->cluster_front = 0;
+  for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
+    int pf = 0;
+    for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
+      const int sn = an.level_sn[t];
+      if (d->clusters_ok && d->front_m_h[sn] > threshold) {
+        b.push_back(sn);
+        d->cluster_front = std::max(d->cluster_front, d->front_m_h[sn]);
+      } else {
+        a.push_back(sn);
+        pf = std::max(pf, d->front_m_h[sn]);
+      }
+    }
+    d->plain_front = std::max(d->plain_front, pf);
+    d->solve_ptr_h.push_back((int)a.size());
+    d->csolve_ptr_h.push_back((int)b.size());
+    d->solve_front_h.push_back(pf);
+  }
+  d->solve_sn_h = a;
+  d->csolve_sn_h = b;
+  d->cluster_threshold = threshold;
+  tg::dfree(d->d_solve_sn);
+  tg::dfree(d->d_csolve_sn);
+  d->d_solve_sn = d->d_csolve_sn = nullptr;
+  int rc = upload(&d->d_solve_sn, d->solve_sn_h);
+  if (!rc) rc = upload(&d->d_csolve_sn, d->csolve_sn_h);
+  if (rc) return rc;
+  const cudaError_t se =
+      tg::direct_set_smem(d->plain_front, d->cluster_front, d->max_nr);
+  return se == cudaSuccess
+             ? 0
+             : cuda_check(se, "tg_direct: solve workspace attribute");
+}
+
 extern "C" {
 
 int tg_direct_create(tg_mat *A, int use_coords, int precision,
@@ -214,32 +268,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   d->tile = precision == TG_PREC_FP32 ? tg::kDirectTile32 : TG_DIRECT_TILE_F64;
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
                                      d->tile, tg::kDirectTrsmRows);
-  {
-    const bool clusters = tg::direct_cluster_solve_ok();
-    std::vector<int> a, b;
-    d->solve_ptr_h.assign(1, 0);
-    d->csolve_ptr_h.assign(1, 0);
-    for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
-      for (int t = an.level_ptr[L]; t < an.level_ptr[L + 1]; t++) {
-        const int sn = an.level_sn[t];
-        if (clusters && d->front_m_h[sn] > tg::kDirectClusterFront) {
-          b.push_back(sn);
-          d->cluster_front = std::max(d->cluster_front, d->front_m_h[sn]);
-        } else {
-          a.push_back(sn);
-          d->plain_front = std::max(d->plain_front, d->front_m_h[sn]);
-        }
-      }
-      d->solve_ptr_h.push_back((int)a.size());
-      d->csolve_ptr_h.push_back((int)b.size());
-      int pf = 0;
-      for (int t = d->solve_ptr_h[L]; t < d->solve_ptr_h[L + 1]; t++)
-        pf = std::max(pf, d->front_m_h[a[t]]);
-      d->solve_front_h.push_back(pf);
-    }
-    d->solve_sn_h = a;
-    d->csolve_sn_h = b;
-  }
+  d->clusters_ok = tg::direct_cluster_solve_ok();
+  if (!d->clusters_ok) d->cluster_threshold = 1 << 30;
   // the fronts factored by panels keep the inverses of their diagonal
   // blocks (the solves' block steps become 32 x 32 products)
   std::vector<int64_t> dinv_off(d->ns, -1);
@@ -299,8 +329,6 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = upload(&d->d_ch_ptr, ch_ptr);
   if (!rc) rc = upload(&d->d_ch_list, ch_list);
   if (!rc) rc = upload(&d->d_level_sn, an.level_sn);
-  if (!rc) rc = upload(&d->d_solve_sn, d->solve_sn_h);
-  if (!rc) rc = upload(&d->d_csolve_sn, d->csolve_sn_h);
   if (!rc) rc = upload(&d->d_small, small_h);
   if (!rc) rc = upload(&d->d_step_fronts, d->steps.fronts);
   if (!rc) rc = upload(&d->d_step_tprefix, d->steps.tprefix);
@@ -316,11 +344,13 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   // front would not fit a CTA's shared memory beside the solve kernels'
   // static shared memory (at most 32 KB: staged rows, inverse blocks)
   constexpr size_t kSmemMax = (227 - 32) * 1024;
+  // (for every cluster threshold the autotuner may pick)
+  const int pf_max = d->clusters_ok ? std::min(d->max_front, kTuneMaxFront)
+                                    : d->max_front;
   for (int nr : {4, 2, 1}) {
     d->max_nr = nr;
-    if (tg::direct_solve_smem(d->plain_front, nr, sizeof(double)) <=
-            kSmemMax &&
-        tg::direct_cluster_smem(d->cluster_front, nr, sizeof(double)) <=
+    if (tg::direct_solve_smem(pf_max, nr, sizeof(double)) <= kSmemMax &&
+        tg::direct_cluster_smem(d->max_front, nr, sizeof(double)) <=
             kSmemMax)
       break;
   }
@@ -354,19 +384,13 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
   if (!rc) rc = dalloc(&d->d_scal, 3 * R + 2);
   if (!rc) rc = dalloc(&d->d_fail, 1);
-  if (!rc && tg::direct_solve_smem(d->plain_front, 1, sizeof(double)) >
-                 kSmemMax)
+  if (!rc && tg::direct_solve_smem(pf_max, 1, sizeof(double)) > kSmemMax)
     rc = fail(TG_ERR_ARG, "tg_direct_create: front too large for a CTA's "
                           "solve workspace");
+  if (!rc) rc = build_solve_lists(d, d->cluster_threshold);
   if (rc) {
     tg_direct_decref(d);
     return rc;
-  }
-  const cudaError_t se =
-      tg::direct_set_smem(d->plain_front, d->cluster_front, d->max_nr);
-  if (se != cudaSuccess) {
-    tg_direct_decref(d);
-    return cuda_check(se, "tg_direct_create: solve workspace attribute");
   }
   *out = d;
   return 0;
@@ -728,6 +752,77 @@ int tg_direct_solve_refined_multi(tg_direct *d, int nrhs, const double *b,
   return 0;
 }
 
+int tg_direct_autotune(tg_direct *d, int *threshold, double *ms,
+                       void *s) {
+  if (!d) return fail(TG_ERR_ARG, "tg_direct_autotune: NULL");
+  if (!d->factored)
+    return fail(TG_ERR_STATE, "tg_direct_autotune: not factored");
+  static const int cand[3] = {384, tg::kDirectClusterFront, kTuneMaxFront};
+  if (ms)
+    for (int k = 0; k < 3; k++) ms[k] = 0.0;
+  int best = d->cluster_threshold;
+  if (d->clusters_ok) {
+    // the choice per matrix shape, precision and device
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int, int>, int> cache;
+    int dev = 0;
+    TG_CUDA(cudaGetDevice(&dev));
+    const auto key = std::make_tuple(d->n, d->A->nnz, d->bs, d->precision, dev);
+    bool cached = false;
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      auto it = cache.find(key);
+      if (it != cache.end()) {
+        best = it->second;
+        cached = true;
+      }
+    }
+    if (!cached) {
+      const size_t N = (size_t)d->n * d->bs;
+      const bool f32 = d->precision == TG_PREC_FP32;
+      tg::launch_fill(d->d_r, 1.0, N, S(s));
+      if (f32) tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
+      const void *b = f32 ? (const void *)d->d_r32 : (const void *)d->d_r;
+      void *x = f32 ? (void *)d->d_c32 : (void *)d->d_t;
+      cudaEvent_t e0, e1;
+      TG_CUDA(cudaEventCreate(&e0));
+      TG_CUDA(cudaEventCreate(&e1));
+      float bestms = 0.0f;
+      for (int k = 0; k < 3; k++) {
+        int rc = build_solve_lists(d, cand[k]);
+        if (!rc) rc = tg::direct_enqueue_solve(d, 1, b, x, f32, S(s));  // warm
+        if (rc) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return rc;
+        }
+        TG_CUDA(cudaEventRecord(e0, S(s)));
+        for (int r = 0; r < 3; r++)
+          tg::direct_enqueue_solve(d, 1, b, x, f32, S(s));
+        TG_CUDA(cudaEventRecord(e1, S(s)));
+        TG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.0f;
+        TG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        t /= 3.0f;
+        if (ms) ms[k] = t;
+        if (k == 0 || t < bestms) {
+          bestms = t;
+          best = cand[k];
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      std::lock_guard<std::mutex> lock(mu);
+      cache[key] = best;
+    }
+    const int rc = build_solve_lists(d, best);
+    if (rc) return rc;
+  }
+  if (threshold) *threshold = best;
+  TG_CUDA(cudaGetLastError());
+  return 0;
+}
+
 int tg_direct_get_stats(tg_direct *d, double *stats) {
   if (!d || !stats) return fail(TG_ERR_ARG, "tg_direct_get_stats: NULL");
   const size_t b2 = (size_t)d->bs * d->bs;
@@ -739,6 +834,7 @@ int tg_direct_get_stats(tg_direct *d, double *stats) {
   stats[5] = d->max_front;
   stats[6] = d->precision;
   stats[7] = (double)d->csolve_sn_h.size();
+  stats[8] = d->cluster_threshold;
   return 0;
 }
 

@@ -136,7 +136,8 @@ class Direct:
     near the inverse of FP32's unit roundoff -- the matrix is factored in
     FP64 instead (`fell_back`), from its values at that moment."""
 
-    def __init__(self, mat, use_coords=True, precision=_lib.PREC_FP64):
+    def __init__(self, mat, use_coords=True, precision=_lib.PREC_FP64,
+                 autotune=True):
         h = C.c_void_p()
         check(_lib.lib().tg_direct_create(mat.handle, int(use_coords),
                                           int(precision), C.byref(h)),
@@ -146,6 +147,10 @@ class Direct:
         self._fp64 = None
         self.fell_back = False
         self.last_steps, self.last_eta = 0, 0.0
+        # after the first factorisation: the solves' launch shapes
+        # (tg_direct_autotune), then cached per matrix shape
+        self.autotune = autotune
+        self.tuned = None
 
     def _factor_fp64(self):
         self._fp64 = Direct(self.mat, self.use_coords, _lib.PREC_FP64)
@@ -160,6 +165,15 @@ class Direct:
             self._factor_fp64()  # the FP32 Cholesky broke down
             return
         check(rc, "tg_direct_factor")
+        if self.autotune and self.tuned is None:
+            thr = C.c_int(0)
+            ms = np.zeros(3)
+            check(_lib.lib().tg_direct_autotune(self.handle, C.byref(thr),
+                                                 ms.ctypes.data, _stream()),
+                  "tg_direct_autotune")
+            self.tuned = {"cluster_threshold": thr.value,
+                          "candidates": [384, 768, 1536],
+                          "solve_ms": ms.tolist()}
 
     def solve(self, b, x=None, steps=30, tol=None, ftol=0.0, rtol=0.0):
         """x = A^-1 b; b a vector or an (nrhs, n) tensor of right-hand sides
@@ -210,12 +224,14 @@ class Direct:
         return x
 
     def stats(self):
-        st = np.zeros(8)
+        st = np.zeros(9)
         check(_lib.lib().tg_direct_get_stats(self.handle, st.ctypes.data))
         return {"supernodes": int(st[0]), "levels": int(st[1]),
                 "factor_bytes": st[2], "pool_bytes": st[3],
                 "flops": st[4], "max_front": int(st[5]),
                 "cluster_fronts": int(st[7]),
+                "cluster_threshold": int(st[8]),
+                "tuned": self.tuned,
                 "fell_back_to_fp64": self.fell_back,
                 "last_refinement_steps": self.last_steps,
                 "last_backward_error": self.last_eta}

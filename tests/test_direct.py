@@ -374,3 +374,35 @@ def test_fp64_direct_refined_to_relative_residual(gpu):
             floor = floor_tol * (knorm * float(X[r].abs().max()) + bn)
             assert res <= max(rtol * bn, floor)
             assert rel(X[r].cpu().numpy(), X1[r].cpu().numpy()) < 1e-8
+
+
+def test_direct_autotune(gpu):
+    """The solves' launch-shape autotuner (tg_direct_autotune, run after
+    the first factorisation): it times a solve per cluster threshold and
+    keeps one of the candidates; a second factorisation of the same matrix
+    shape takes the cached choice without timing; the solution is the
+    same to rounding whatever the threshold."""
+    from tacs_gb300 import meshes
+    # a shape no other test factors (the choice is cached per shape)
+    prob = meshes.plate_c2(120, 0.5, seed=2)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    b = -r0
+    d = gpu.Direct(mat)
+    d.factor()
+    t = d.stats()["tuned"]
+    assert t["cluster_threshold"] in t["candidates"]
+    assert all(ms > 0 for ms in t["solve_ms"])
+    assert d.stats()["cluster_threshold"] == t["cluster_threshold"]
+    x = d.solve(b)
+    d2 = gpu.Direct(mat)
+    d2.factor()
+    t2 = d2.stats()["tuned"]
+    assert t2["cluster_threshold"] == t["cluster_threshold"]
+    assert all(ms == 0 for ms in t2["solve_ms"])  # cached
+    d3 = gpu.Direct(mat, autotune=False)
+    d3.factor()
+    assert d3.stats()["cluster_threshold"] == 768
+    assert rel(x.cpu().numpy(), d3.solve(b).cpu().numpy()) < 1e-10
