@@ -158,7 +158,9 @@ def c2_adjoint_section(torch, n=512):
     multifrontal factorisation (GMRES(80) + ILU(0) does not converge on
     this plate), refined to the 1e-10 relative residual of the stated
     GMRES tolerance (or the FP64 floor).  Times the analysis, the
-    factorisation, one solve and the whole gradient."""
+    factorisation, one solve and the whole gradient, and the whole gradient
+    with the FP32 factorisation and FP64 refinement (`mixed`, with its
+    error against the FP64 gradient)."""
     from tacs_gb300 import autograd as ag
     from tacs_gb300 import problem
     p = c2_problem(n=n)
@@ -184,6 +186,27 @@ def c2_adjoint_section(torch, n=512):
         dt = time.perf_counter() - t0
     out["s_per_gradient"] = dt
     out["compliance"] = float(f.item())
+    g64 = xr.grad.clone()
+    # the same gradient with the FP32 factorisation and FP64 refinement
+    solver32 = ag.StaticSolver(M, np.zeros(M.ndof), rtol=1e-10,
+                               direct="mixed")
+    for rep in range(2):
+        xr = x.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f32 = ag.static_functional(xr, solver32, 0)
+        f32.sum().backward()
+        torch.cuda.synchronize()
+        dt32 = time.perf_counter() - t0
+    st32 = solver32.direct.stats()
+    out["mixed"] = {
+        "s_per_gradient": dt32,
+        "speedup_vs_fp64": dt / dt32,
+        "grad_rel_err_vs_fp64": float((xr.grad - g64).abs().max()
+                                      / g64.abs().max()),
+        "refinement_steps": st32["last_refinement_steps"],
+        "fell_back_to_fp64": st32["fell_back_to_fp64"]}
+    del solver32
     b = M.vec()
     M.assemble_res(M.vec(), res=b)
     e0 = torch.cuda.Event(enable_timing=True)

@@ -833,6 +833,9 @@ __global__ void __launch_bounds__(256)
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  // the shared memory is sized for kDirectSolveCluster ranks: any other
+  // cluster shape leaves (the whole cluster sees the same size)
+  if (cr.nr != kDirectSolveCluster) return;
   const int fi = (int)blockIdx.x / cr.nr;  // the same in the whole cluster
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
@@ -942,6 +945,7 @@ __global__ void __launch_bounds__(256)
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
+  if (cr.nr != kDirectSolveCluster) return;  // as in the forward kernel
   const int fi = (int)blockIdx.x / cr.nr;
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
