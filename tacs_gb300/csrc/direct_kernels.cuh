@@ -567,40 +567,28 @@ __device__ __forceinline__ void dk_inv_solve(const T (*X)[33], int nb, T *z,
 #endif
 }
 
-// z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < G (G = 32 or
-// 16) of a row group with bit i of `valid` set, by one warp: lane c
-// multiplies column c of every row (each row a coalesced load), then a
-// butterfly of shuffles sums the rows' products so that lane i holds row
-// i's sum (G - 1 shuffles for G rows, one more for G = 16, whose two
-// half-warps sum 16 columns each).  L0: row r0's column kb; ldl: the
-// panel's row stride; zrow(i): row i's NR entries of z.  (The CPU
-// emulation forms each row's sum in column order.)
-template <class T, int NR, int G, class ZRow>
+#ifndef DK_EMULATE
+// z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < 32 of a row
+// group with bit i of `valid` set, by one warp: lane c multiplies column c
+// of every row (each row a coalesced load), then a butterfly of shuffles
+// sums the rows' products so that lane i holds row i's sum (31 shuffles for
+// 32 rows).  L0: row r0's column kb; ldl: the panel's row stride; zrow(i):
+// row i's NR entries of z.
+template <class T, int NR, class ZRow>
 __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
                                              const T *zk, unsigned valid,
                                              ZRow zrow) {
-  static_assert(G == 32 || G == 16, "row group of 16 or 32");
-#ifdef DK_EMULATE
-  for (int i = 0; i < G; i++) {
-    if (!((valid >> i) & 1u)) continue;
-    for (int q = 0; q < NR; q++) {
-      T acc = 0;
-      for (int c = 0; c < nb; c++) acc += L0[(size_t)i * ldl + c] * zk[c * NR + q];
-      zrow(i)[q] -= acc;
-    }
-  }
-#else
   const int lane = threadIdx.x & 31;
 #pragma unroll 1
   for (int q = 0; q < NR; q++) {
     const T zc = lane < nb ? zk[lane * NR + q] : T(0);
-    T v[G];
+    T v[32];
 #pragma unroll
-    for (int i = 0; i < G; i++)
+    for (int i = 0; i < 32; i++)
       v[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane] * zc
                                               : T(0);
 #pragma unroll
-    for (int h = G / 2; h >= 1; h >>= 1) {
+    for (int h = 16; h >= 1; h >>= 1) {
       const bool up = (lane & h) != 0;
 #pragma unroll
       for (int i = 0; i < h; i++) {
@@ -609,11 +597,10 @@ __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
       }
     }
-    if (G == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 16);
-    if (lane < G && ((valid >> lane) & 1u)) zrow(lane)[q] -= v[0];
+    if ((valid >> lane) & 1u) zrow(lane)[q] -= v[0];
   }
-#endif
 }
+#endif  // DK_EMULATE
 
 // position of front row i of supernode s in a factor-order vector
 __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
@@ -901,7 +888,7 @@ __global__ void __launch_bounds__(256)
       dk_inv_store(pre, Ls);
       if (warp == 0) {
         T *zr1 = z + (size_t)cr.slot(r1) * NR;
-        dk_warp_rows<T, NR, 32>(
+        dk_warp_rows<T, NR>(
             f.lp + (size_t)r1 * f.C + kb, f.C, nb, zk,
             nb1 == 32 ? 0xffffffffu : (1u << nb1) - 1u,
             [&](int i) { return zr1 + i * NR; });
@@ -924,7 +911,7 @@ __global__ void __launch_bounds__(256)
       }
       if (!valid) continue;
       T *zg = z + (size_t)(g << 5) * NR;
-      dk_warp_rows<T, NR, 32>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk,
+      dk_warp_rows<T, NR>(f.lp + (size_t)r0 * f.C + kb, f.C, nb, zk,
                               valid, [&](int i) { return zg + i * NR; });
     }
     __syncthreads();
