@@ -100,7 +100,7 @@ static void backward_plain(int nr, dim3 g, int nt, size_t smem,
 }
 
 size_t direct_solve_smem(int front, int nr, size_t elem) {
-  return elem * ((size_t)front * nr + kDirectSolveDiag);
+  return elem * ((size_t)front * nr + direct_plain_extra(nr, (int)elem));
 }
 
 template <class T>
@@ -136,7 +136,7 @@ static cudaError_t cluster_launch_dk(K kernel, int count, size_t smem,
                                      cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(count * kDirectSolveCluster));
-  cfg.blockDim = dim3(256);
+  cfg.blockDim = dim3(kDirectClusterThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
@@ -217,18 +217,21 @@ bool direct_cluster_solve_ok() {
 }
 
 template <class T>
-void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
-                           T *out, int nrhs, size_t ld, cudaStream_t s) {
-  direct_bc_mask_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
-      n, bs, bcmask, b, out, nrhs, ld);
+void launch_direct_rhs(int n, int bs, const int *perm, const T *b, T *ypos,
+                       int nrhs, size_t ld, cudaStream_t s) {
+  direct_rhs_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
+      n, bs, perm, b, ypos, nrhs, ld);
 }
 
 template <class T>
-void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
-                       const T *Kpb, const T *pb, T *ypos, int nrhs,
-                       size_t ld, cudaStream_t s) {
-  direct_rhs_kernel<T><<<grid_1d((size_t)n * bs * nrhs), 256, 0, s>>>(
-      n, bs, perm, b, Kpb, pb, ypos, nrhs, ld);
+void launch_direct_bc_couple(const DirectBc &c, int bs, const T *a,
+                             const T *b, T *ypos, int nrhs, size_t ld,
+                             cudaStream_t s) {
+  if (c.nrow == 0) return;
+  direct_bc_couple_kernel<T>
+      <<<grid_1d((size_t)c.nrow * bs * nrhs), 256, 0, s>>>(
+          c.nrow, bs, c.row, c.pos, c.ptr, c.blk, c.cols, c.bcmask, a, b,
+          ypos, nrhs, ld);
 }
 
 template <class T>
@@ -337,11 +340,11 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
   template void launch_direct_backward_cluster<T>(                         \
       const DirectView &, const int *, int, int, int, const T *, T *,      \
       cudaStream_t);                                                        \
-  template void launch_direct_bc_mask<T>(int, int, const int *, const T *, \
-                                         T *, int, size_t, cudaStream_t);  \
   template void launch_direct_rhs<T>(int, int, const int *, const T *,     \
-                                     const T *, const T *, T *, int,       \
-                                     size_t, cudaStream_t);                \
+                                     T *, int, size_t, cudaStream_t);      \
+  template void launch_direct_bc_couple<T>(const DirectBc &, int,          \
+                                           const T *, const T *, T *, int, \
+                                           size_t, cudaStream_t);          \
   template void launch_direct_unpermute<T>(int, int, const int *,          \
                                            const T *, T *, int, size_t,    \
                                            cudaStream_t);

@@ -602,6 +602,86 @@ __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
 }
 #endif  // DK_EMULATE
 
+// Row i's entries kb .. kb + nb of a panel times the block's solved
+// entries zk (NR interleaved right-hand sides), added to acc in column
+// order, with loads W entries wide (DkVec): a panel row of C entries starts
+// on a W-entry boundary when the panel does and C is a multiple of W (kb
+// is a multiple of 32), which dk_vec_width checks per front.
+template <class T, int W>
+struct alignas(sizeof(T) * W) DkVec {
+  T v[W];
+};
+template <class T>
+__device__ __forceinline__ int dk_vec_width(const T *lp, int C) {
+  const unsigned long long a = (unsigned long long)lp;
+  if (sizeof(T) == 4 && C % 4 == 0 && a % 16 == 0) return 4;
+  if (C % 2 == 0 && a % (2 * sizeof(T)) == 0 && 2 * sizeof(T) <= 16)
+    return 2;
+  return 1;
+}
+template <class T, int NR, int W>
+__device__ __forceinline__ void dk_row_dot_w(const T *Li, int nb,
+                                             const T *zk, T (&acc)[NR]) {
+  int c = 0;
+  for (; c + W <= nb; c += W) {
+    const DkVec<T, W> l = *reinterpret_cast<const DkVec<T, W> *>(Li + c);
+#pragma unroll
+    for (int w = 0; w < W; w++)
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[q] += l.v[w] * zk[(c + w) * NR + q];
+  }
+  for (; c < nb; c++)
+#pragma unroll
+    for (int q = 0; q < NR; q++) acc[q] += Li[c] * zk[c * NR + q];
+}
+template <class T, int NR>
+__device__ __forceinline__ void dk_row_dot(int W, const T *Li, int nb,
+                                           const T *zk, T (&acc)[NR]) {
+  if constexpr (sizeof(T) == 4) {
+    if (W == 4) {
+      dk_row_dot_w<T, NR, 4>(Li, nb, zk, acc);
+      return;
+    }
+  }
+  if (W == 2)
+    dk_row_dot_w<T, NR, 2>(Li, nb, zk, acc);
+  else
+    dk_row_dot_w<T, NR, 1>(Li, nb, zk, acc);
+}
+
+// Columns j0 .. j0 + W of a panel (Lc = its entry in row 0, ldl = C)
+// against z over the rows i0, i0 + step, .. < i1: acc[w] += L(i, j0 + w)
+// z_i (NR interleaved right-hand sides), one W-wide load per row.
+template <class T, int NR, int W>
+__device__ __forceinline__ void dk_col_dot_w(const T *Lc, int ldl, int i0,
+                                             int i1, int step, const T *z,
+                                             T (&acc)[4][NR]) {
+#pragma unroll 4
+  for (int i = i0; i < i1; i += step) {
+    const DkVec<T, W> l =
+        *reinterpret_cast<const DkVec<T, W> *>(Lc + (size_t)i * ldl);
+#pragma unroll
+    for (int w = 0; w < W; w++)
+#pragma unroll
+      for (int q = 0; q < NR; q++) acc[w][q] += l.v[w] * z[i * NR + q];
+  }
+}
+template <class T, int NR>
+__device__ __forceinline__ void dk_col_dot(int W, const T *Lc, int ldl,
+                                           int i0, int i1, int step,
+                                           const T *z, T (&acc)[4][NR]) {
+  if constexpr (sizeof(T) == 4) {
+    if (W == 4) {
+      dk_col_dot_w<T, NR, 4>(Lc, ldl, i0, i1, step, z, acc);
+      return;
+    }
+  }
+  if (W == 2)
+    dk_col_dot_w<T, NR, 2>(Lc, ldl, i0, i1, step, z, acc);
+  else
+    dk_col_dot_w<T, NR, 1>(Lc, ldl, i0, i1, step, z, acc);
+}
+
 // position of front row i of supernode s in a factor-order vector
 __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
   return (size_t)rows[i / bs] * bs + i % bs;
@@ -627,6 +707,7 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
   const int *rows = v.sn_rows + v.sn_rowptr[s];
   const bool inv = v.dinv_off[s] >= 0;
   const T *Xg = inv ? dk_dinv(v, (T *)nullptr) + v.dinv_off[s] : nullptr;
+  const int W = dk_vec_width(f.lp, f.C);
   for (int i = threadIdx.x; i < f.M; i += blockDim.x) {
     T *zi = z + (size_t)i * NR;
     if (i < f.C) {
@@ -666,19 +747,15 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
     }
     __syncthreads();
     // rows below the block: z_i -= L(i, kb .. kb+nb) z(kb .. kb+nb), one
-    // thread per row (its 32 loads independent, every one serving the NR
-    // right-hand sides; measured faster here than warp-per-row-group
-    // reductions or rows staged through shared memory)
+    // thread per row (its loads independent and W entries wide, every one
+    // serving the NR right-hand sides; measured faster here than
+    // warp-per-row-group reductions or rows staged through shared memory)
     for (int i = kb + nb + threadIdx.x; i < f.M; i += blockDim.x) {
-      const T *Li = f.lp + (size_t)i * f.C + kb;
       T acc[NR];
 #pragma unroll
       for (int q = 0; q < NR; q++) acc[q] = 0;
-      for (int c = 0; c < nb; c++) {
-        const T l = Li[c];
-#pragma unroll
-        for (int q = 0; q < NR; q++) acc[q] += l * z[(kb + c) * NR + q];
-      }
+      dk_row_dot<T, NR>(W, f.lp + (size_t)i * f.C + kb, nb, z + kb * NR,
+                        acc);
 #pragma unroll
       for (int q = 0; q < NR; q++) z[(size_t)i * NR + q] -= acc[q];
     }
@@ -723,17 +800,43 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
     for (int q = 0; q < NR; q++) zi[q] = src[q];
   }
   __syncthreads();
-  for (int j = threadIdx.x; j < f.C; j += blockDim.x) {
-    T acc[NR];
+  // own rows: z_j -= sum_{i >= C} L(i, j) z_i.  Tasks form a grid of
+  // column groups (W adjacent columns, one W-wide load per row) by P
+  // interleaved parts of the rows, at most kDirectPlainThreads tasks; the
+  // parts' sums meet in shared memory after z (the staging area of the
+  // block solves, free until they start) in a fixed order.
+  {
+    const int W = dk_vec_width(f.lp, f.C);
+    const int ncg = f.C / W;  // W divides C
+    int P = kDirectPlainThreads / (ncg > 0 ? ncg : 1);
+    P = P < 1 ? 1 : P;
+    for (int t = threadIdx.x; t < ncg * P; t += blockDim.x) {
+      const int cg = t % ncg, pp = t / ncg, j0 = cg * W;
+      T acc[4][NR];
 #pragma unroll
-    for (int r = 0; r < NR; r++) acc[r] = 0;
-    for (int i = f.C; i < f.M; i++) {
-      const T l = f.lp[(size_t)i * f.C + j];
+      for (int w = 0; w < 4; w++)
 #pragma unroll
-      for (int r = 0; r < NR; r++) acc[r] += l * z[i * NR + r];
+        for (int q = 0; q < NR; q++) acc[w][q] = 0;
+      dk_col_dot<T, NR>(W, f.lp + j0, f.C, f.C + pp, f.M, P, z, acc);
+#pragma unroll
+      for (int w = 0; w < 4; w++)
+#pragma unroll
+        for (int q = 0; q < NR; q++) {
+          if (w >= W) continue;
+          if (P == 1)
+            z[(j0 + w) * NR + q] -= acc[w][q];
+          else
+            D[((size_t)pp * f.C + j0 + w) * NR + q] = acc[w][q];
+        }
     }
-#pragma unroll
-    for (int r = 0; r < NR; r++) z[j * NR + r] -= acc[r];
+    if (P > 1) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < f.C * NR; t += blockDim.x) {
+        T sum = 0;
+        for (int pp = 0; pp < P; pp++) sum += D[(size_t)pp * f.C * NR + t];
+        z[t] -= sum;
+      }
+    }
   }
   __syncthreads();
   for (int kb = ((f.C - 1) / kDirectSolveBlock) * kDirectSolveBlock; kb >= 0;
@@ -794,6 +897,11 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
 // front only); a final barrier keeps each CTA's shared memory alive until
 // the others are done reading it.  Dynamic shared memory: the owned rows
 // (rounded up to whole blocks) x NR.
+constexpr int kClusterWarps = kDirectClusterThreads / 32;
+// the first phase of the backward solve keeps one 32 x NR partial sum per
+// warp in the 32 x 33 staging area of the inverses
+static_assert(kClusterWarps * 32 * 4 <= 32 * 33, "cluster partial sums");
+
 struct ClusterRows {
   int nr, rank;
   __device__ __forceinline__ bool owns(int r) const {
@@ -814,7 +922,7 @@ struct ClusterRows {
 };
 
 template <class T, int NR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kDirectClusterThreads)
     direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
                                   int count, T *y, T *contrib) {
   namespace cg = cooperative_groups;
@@ -926,7 +1034,7 @@ __global__ void __launch_bounds__(256)
 }
 
 template <class T, int NR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kDirectClusterThreads)
     direct_backward_cluster_kernel(DirectView v, const int *__restrict__ sn,
                                    int count, const T *y, T *x) {
   namespace cg = cooperative_groups;
@@ -945,24 +1053,63 @@ __global__ void __launch_bounds__(256)
   const int nown = cr.count(f.M);
   const T *inv = dk_dinv(v, (T *)nullptr) + v.dinv_off[s];
   const int nblk = (f.C + 31) >> 5;
-  // own rows of the triangle: y1 - L21^T x2 (x2 final, from the ancestors)
-  for (int t = threadIdx.x; t < nown; t += blockDim.x) {
-    const int j = cr.row(t);
-    if (j >= f.C) continue;
-    T acc[NR];
+  const int warp = (int)threadIdx.x >> 5;
+  // own rows of the triangle: y1 - L21^T x2 (x2 final, from the
+  // ancestors).  A warp takes one of this rank's 32-column blocks (lane =
+  // column, each row's load coalesced, x2 a broadcast) and, when the rank
+  // has fewer blocks than warps, one of P interleaved parts of the update
+  // rows, so that every warp streams rows; the parts' sums meet in shared
+  // memory (the inverse's staging area, free until the chain starts) in a
+  // fixed order.
+  {
+    const int lane = (int)threadIdx.x & 31;
+    const int nob = cr.count(f.C) >> 5;
+    const int P = nob >= kClusterWarps ? 1 : kClusterWarps / (nob > 0 ? nob : 1);
+    T(*part)[32 * NR] = reinterpret_cast<T(*)[32 * NR]>(&Ls[0][0]);
+    for (int task = warp; task < nob * P; task += kClusterWarps) {
+      const int ob = task % nob, pp = task / nob;
+      const int t = (ob << 5) + lane;
+      const int j = cr.row(t);
+      T acc[NR];
 #pragma unroll
-    for (int q = 0; q < NR; q++) acc[q] = 0;
-    for (int i = f.C; i < f.M; i++) {
-      const T l = f.lp[(size_t)i * f.C + j];
-      const size_t g = dk_pos(rows, bs, i) * NR;
+      for (int q = 0; q < NR; q++) acc[q] = 0;
+      if (j < f.C) {
+        const T *Lj = f.lp + j;
+#pragma unroll 8
+        for (int i = f.C + pp; i < f.M; i += P) {
+          const T l = Lj[(size_t)i * f.C];
+          const size_t g = dk_pos(rows, bs, i) * NR;
 #pragma unroll
-      for (int q = 0; q < NR; q++) acc[q] += l * x[g + q];
+          for (int q = 0; q < NR; q++) acc[q] += l * x[g + q];
+        }
+      }
+      if (P == 1) {
+        if (j < f.C) {
+          const size_t gj = dk_pos(rows, bs, j) * NR;
+#pragma unroll
+          for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - acc[q];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < NR; q++) part[task][lane * NR + q] = acc[q];
+      }
     }
-    const size_t gj = dk_pos(rows, bs, j) * NR;
+    __syncthreads();
+    if (P > 1)
+      for (int t = threadIdx.x; t < nob * 32; t += blockDim.x) {
+        const int j = cr.row(t);
+        if (j >= f.C) continue;
+        const size_t gj = dk_pos(rows, bs, j) * NR;
 #pragma unroll
-    for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - acc[q];
+        for (int q = 0; q < NR; q++) {
+          T sum = 0;
+          for (int pp = 0; pp < P; pp++)
+            sum += part[pp * nob + (t >> 5)][(t & 31) * NR + q];
+          z[t * NR + q] = y[gj + q] - sum;
+        }
+      }
+    __syncthreads();
   }
-  __syncthreads();
   T pre[4];
   const int kt = nblk - 1;
   if (kt % cr.nr == cr.rank) {  // the last block: its rows are complete
@@ -1032,33 +1179,51 @@ __global__ void __launch_bounds__(256)
 }
 #endif  // DK_EMULATE
 
-// b' = b - K P b + P b (P keeps the boundary dofs) for nrhs right-hand
-// sides ld apart (node order): tmp = P b, K tmp by the mat-vec, then the
-// right-hand-side kernel, which also permutes into the factor's order and
-// interleaves (ypos[t * nrhs + r]); the unpermute kernel undoes both.
-template <class T>
-__global__ void direct_bc_mask_kernel(int n, int bs, const int *bcmask,
-                                      const T *b, T *out, int nrhs,
-                                      size_t ld) {
-  const size_t N = (size_t)n * bs, tot = N * nrhs;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
-       t += (size_t)gridDim.x * blockDim.x) {
-    const size_t r = t / N, e = t - N * r;
-    const int node = (int)(e / bs), q = (int)(e % bs);
-    out[t] = ((bcmask[node] >> q) & 1) ? b[r * ld + e] : T(0);
-  }
-}
+// b' = b - A_{:,c} b_c on the free dofs, b' = b on the constrained ones
+// (c: the constrained dofs, whose rows of A are the identity), for nrhs
+// right-hand sides ld apart (node order).  The right-hand-side kernel
+// permutes b into the factor's order and interleaves it (ypos[t * nrhs +
+// r]); the coupling kernel then subtracts A_{i,c} b_c on the block rows
+// that have a block in a constrained column (bc_row[k] at factor position
+// bc_pos[k], its blocks bc_blk[bc_ptr[k] .. bc_ptr[k + 1]), BCSR value
+// indices), one thread per (row, dof, right-hand side); the unpermute
+// kernel undoes the permutation.
 template <class T>
 __global__ void direct_rhs_kernel(int n, int bs, const int *perm,
-                                  const T *b, const T *Kpb, const T *pb,
-                                  T *ypos, int nrhs, size_t ld) {
+                                  const T *b, T *ypos, int nrhs, size_t ld) {
   const size_t N = (size_t)n * bs, tot = N * nrhs;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
        t += (size_t)gridDim.x * blockDim.x) {
     const size_t e = t / nrhs, r = t - nrhs * e;
     const int pos = (int)(e / bs), q = (int)(e % bs);
-    const size_t g = (size_t)perm[pos] * bs + q;
-    ypos[t] = b[r * ld + g] - Kpb[r * N + g] + pb[r * N + g];
+    ypos[t] = b[r * ld + (size_t)perm[pos] * bs + q];
+  }
+}
+template <class T>
+__global__ void direct_bc_couple_kernel(int nrow, int bs,
+                                        const int *__restrict__ bc_row,
+                                        const int *__restrict__ bc_pos,
+                                        const int *__restrict__ bc_ptr,
+                                        const int *__restrict__ bc_blk,
+                                        const int *__restrict__ cols,
+                                        const int *__restrict__ bcmask,
+                                        const T *__restrict__ a, const T *b,
+                                        T *ypos, int nrhs, size_t ld) {
+  const size_t per = (size_t)bs * nrhs, tot = (size_t)nrow * per;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = t / per, e = t - per * k;
+    const int q = (int)(e / nrhs), r = (int)(e - (size_t)nrhs * q);
+    if ((bcmask[bc_row[k]] >> q) & 1) continue;  // a constrained row
+    T acc = 0;
+    for (int m = bc_ptr[k]; m < bc_ptr[k + 1]; m++) {
+      const int blk = bc_blk[m], j = cols[blk], mask = bcmask[j];
+      const T *Aq = a + ((size_t)blk * bs + q) * bs;
+      const T *bj = b + r * ld + (size_t)j * bs;
+      for (int p = 0; p < bs; p++)
+        if ((mask >> p) & 1) acc += Aq[p] * bj[p];
+    }
+    ypos[((size_t)bc_pos[k] * bs + q) * nrhs + r] -= acc;
   }
 }
 template <class T>

@@ -741,5 +741,34 @@ inline PanelSteps panel_steps(const Analysis &an, int bs, int small_max,
   return ps;
 }
 
+// The coupling of the right-hand side to the constrained dofs: the
+// assembled matrix keeps the columns of the constrained dofs (only their
+// rows are the identity), while the factorisation holds the matrix with
+// those rows and columns removed, so a solve takes b' = b - A_{:,c} b_c on
+// the free dofs.  Listed here: the block rows i with a block in a column
+// whose node has a constrained dof (row[k] = i, pos[k] = i's position in
+// the factor order, its blocks blk[ptr[k] .. ptr[k + 1]) as indices into
+// the BCSR value array), so that the correction touches those blocks only.
+struct BcCoupling {
+  std::vector<int> row, pos, ptr{0}, blk;
+};
+inline BcCoupling bc_coupling(const std::vector<int> &rowp,
+                              const std::vector<int> &cols,
+                              const std::vector<int> &bcmask,
+                              const std::vector<int> &iperm) {
+  BcCoupling c;
+  const int n = (int)rowp.size() - 1;
+  for (int i = 0; i < n; i++) {
+    const size_t before = c.blk.size();
+    for (int k = rowp[i]; k < rowp[i + 1]; k++)
+      if (bcmask[cols[k]]) c.blk.push_back(k);
+    if (c.blk.size() == before) continue;
+    c.row.push_back(i);
+    c.pos.push_back(iperm[i]);
+    c.ptr.push_back((int)c.blk.size());
+  }
+  return c;
+}
+
 }  // namespace direct
 }  // namespace tg

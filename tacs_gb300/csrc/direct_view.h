@@ -19,13 +19,35 @@ constexpr int kDirectZeroChunk = 16384;
 constexpr int kDirectSolveBlock = 32;
 // threads of the one-CTA-per-front solve kernels
 constexpr int kDirectPlainThreads = 128;
+// Shared memory of the one-CTA solves beyond the front's rows, in entries
+// of elem bytes for nr right-hand sides: the staged diagonal block, which
+// the backward solve's partial column sums (at most kDirectPlainThreads
+// column groups of 16 bytes of entries, nr each) reuse.
+constexpr int direct_plain_extra(int nr, int elem) {
+  return kDirectPlainThreads * (16 / elem) * nr >
+                 kDirectSolveBlock * (kDirectSolveBlock + 1)
+             ? kDirectPlainThreads * (16 / elem) * nr
+             : kDirectSolveBlock * (kDirectSolveBlock + 1);
+}
 // rows of a child's update matrix added into its parent by one CTA
 constexpr int kDirectExtendRows = 32;
 // CTAs of the thread-block cluster that solves one large front, and the
 // front rows above which a front is solved that way
 constexpr int kDirectSolveCluster = 8;
+// threads of a CTA of the cluster solves
+constexpr int kDirectClusterThreads = 256;
 constexpr int kDirectClusterFront = 768;
 constexpr int kDirectSolveDiag = kDirectSolveBlock * (kDirectSolveBlock + 1);
+
+// The right-hand side's coupling to the constrained dofs
+// (direct::bc_coupling, on the device): nrow block rows with their factor
+// positions and blocks, the matrix's column indices and the per-node masks
+// of constrained dofs.
+struct DirectBc {
+  int nrow = 0;
+  const int *row = nullptr, *pos = nullptr, *ptr = nullptr, *blk = nullptr,
+            *cols = nullptr, *bcmask = nullptr;
+};
 
 struct DirectView {
   int bs;

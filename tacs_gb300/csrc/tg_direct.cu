@@ -31,17 +31,6 @@ static constexpr int kSmallFront = TG_DIRECT_SMALL_FRONT;
 // blocks of the max-|x| reductions of the refinement's stopping test
 static constexpr int kRedParts = 256;
 
-static void bcsr_mult_t(const tg_mat *A, const double *a, const double *x,
-                        double *y, cudaStream_t s) {
-  tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols, a, x,
-                       y, s);
-}
-static void bcsr_mult_t(const tg_mat *A, const float *a, const float *x,
-                        float *y, cudaStream_t s) {
-  tg::launch_bcsr_mult_f32(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols, a,
-                           x, y, s);
-}
-
 struct tg_direct {
   int refcount = 1;
   tg_mat *A = nullptr;
@@ -92,13 +81,15 @@ struct tg_direct {
   double *d_dinv = nullptr;
   float *d_dinv32 = nullptr;
   double *d_lstore = nullptr, *d_pool = nullptr, *d_contrib = nullptr;
-  double *d_ypos = nullptr, *d_xpos = nullptr, *d_pb = nullptr,
-         *d_kpb = nullptr;
+  double *d_ypos = nullptr, *d_xpos = nullptr;
+  // the right-hand side's coupling to the constrained dofs
+  int *d_bc_row = nullptr, *d_bc_pos = nullptr, *d_bc_ptr = nullptr,
+      *d_bc_blk = nullptr;
+  int bc_nrow = 0;
   // FP32 factorisation: its storage, solve vectors and the matrix in FP32
   float *d_lstore32 = nullptr, *d_pool32 = nullptr, *d_contrib32 = nullptr;
-  float *d_ypos32 = nullptr, *d_xpos32 = nullptr, *d_pb32 = nullptr,
-        *d_kpb32 = nullptr, *d_a32 = nullptr, *d_r32 = nullptr,
-        *d_c32 = nullptr;
+  float *d_ypos32 = nullptr, *d_xpos32 = nullptr, *d_a32 = nullptr,
+        *d_r32 = nullptr, *d_c32 = nullptr;
   double *d_r = nullptr, *d_t = nullptr;  // refinement residual, scratch
   // refinement stopping test: reduction partials, 3 device scalars, and
   // ||A||_inf of the values factored last
@@ -107,6 +98,23 @@ struct tg_direct {
   int64_t contrib_len = 0;
   int *d_fail = nullptr;
   bool factored = false;
+  // a level's one-CTA and cluster solves touch different fronts: the
+  // one-CTA launch runs on side_stream beside the cluster launch (forked
+  // and joined through the two events), so a level costs the longer of
+  // the two rather than their sum
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  tg::DirectBc bc() const {
+    tg::DirectBc c;
+    c.nrow = bc_nrow;
+    c.row = d_bc_row;
+    c.pos = d_bc_pos;
+    c.ptr = d_bc_ptr;
+    c.blk = d_bc_blk;
+    c.cols = A->a->d_cols;
+    c.bcmask = d_bcmask;
+    return c;
+  }
   tg::DirectView view() const {
     tg::DirectView v;
     v.bs = bs;
@@ -144,14 +152,18 @@ struct tg_direct {
     dfree(d_ch_ptr); dfree(d_ch_list); dfree(d_level_sn); dfree(d_l_off);
     dfree(d_solve_sn); dfree(d_csolve_sn);
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
-    dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_pb);
-    dfree(d_kpb); dfree(d_fail); dfree(d_small); dfree(d_lstore32);
+    dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_bc_row);
+    dfree(d_bc_pos); dfree(d_bc_ptr); dfree(d_bc_blk);
+    dfree(d_fail); dfree(d_small); dfree(d_lstore32);
     dfree(d_step_fronts); dfree(d_step_tprefix); dfree(d_step_rprefix);
     dfree(d_pool32); dfree(d_contrib32); dfree(d_ypos32); dfree(d_xpos32);
-    dfree(d_pb32); dfree(d_kpb32); dfree(d_a32); dfree(d_r32);
+    dfree(d_a32); dfree(d_r32);
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
     dfree(d_dinv_off); dfree(d_dinv); dfree(d_dinv32);
     dfree(d_inv_sn); dfree(d_inv_k0);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side_stream) cudaStreamDestroy(side_stream);
   }
 };
 
@@ -216,6 +228,18 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   tg_direct *d = new tg_direct();
   d->A = A;
   A->refcount++;
+  {
+    cudaError_t e =
+        cudaStreamCreateWithFlags(&d->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+      e = cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+      e = cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      tg_direct_decref(d);
+      return cuda_check(e, "tg_direct_create: solve streams");
+    }
+  }
   d->n = A->nrows;
   d->bs = A->bsize;
   d->precision = precision;
@@ -316,6 +340,15 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   int rc = 0;
   if (!rc) rc = upload(&d->d_perm, an.perm);
   if (!rc) rc = upload(&d->d_bcmask, bcmask);
+  {
+    const tg::direct::BcCoupling c =
+        tg::direct::bc_coupling(a->rowp_h, a->cols_h, bcmask, an.iperm);
+    d->bc_nrow = (int)c.row.size();
+    if (!rc && d->bc_nrow) rc = upload(&d->d_bc_row, c.row);
+    if (!rc && d->bc_nrow) rc = upload(&d->d_bc_pos, c.pos);
+    if (!rc && d->bc_nrow) rc = upload(&d->d_bc_ptr, c.ptr);
+    if (!rc && d->bc_nrow) rc = upload(&d->d_bc_blk, c.blk);
+  }
   if (!rc) rc = upload(&d->d_sn_col, an.sn_col);
   if (!rc) rc = upload(&d->d_sn_rowptr, an.sn_rowptr);
   if (!rc) rc = upload(&d->d_sn_rows, an.sn_rows);
@@ -362,8 +395,6 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_contrib, (size_t)vacc * R);
     if (!rc) rc = dalloc(&d->d_ypos, N * R);
     if (!rc) rc = dalloc(&d->d_xpos, N * R);
-    if (!rc) rc = dalloc(&d->d_pb, N * R);
-    if (!rc) rc = dalloc(&d->d_kpb, N * R);
   } else {
     if (!rc) rc = dalloc(&d->d_lstore32, (size_t)an.l_total * b2);
     if (!rc) rc = dalloc(&d->d_pool32, (size_t)an.u_peak * b2);
@@ -371,8 +402,6 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
     if (!rc) rc = dalloc(&d->d_contrib32, (size_t)vacc * R);
     if (!rc) rc = dalloc(&d->d_ypos32, N * R);
     if (!rc) rc = dalloc(&d->d_xpos32, N * R);
-    if (!rc) rc = dalloc(&d->d_pb32, N * R);
-    if (!rc) rc = dalloc(&d->d_kpb32, N * R);
     if (!rc) rc = dalloc(&d->d_a32, (size_t)A->nnz * b2);
     if (!rc) rc = dalloc(&d->d_r32, N * R);
     if (!rc) rc = dalloc(&d->d_c32, N * R);
@@ -436,12 +465,28 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
 // at most max_nr of them, b' = b - K P b + P b, into the factor's order
 // (interleaved), the level sweeps, back to the node order (K a: the
 // matrix values in T)
+// The stream of a level's one-CTA solves: the side stream, forked from s
+// after the levels before, when the level also has cluster solves (which
+// stay on s); else s itself.  level_join puts s behind the side stream's
+// launches.  Inside a stream capture the fork and join become graph edges.
+static cudaStream_t level_fork(tg_direct *d, bool both, cudaStream_t s) {
+  if (!both) return s;
+  cudaEventRecord(d->ev_fork, s);
+  cudaStreamWaitEvent(d->side_stream, d->ev_fork, 0);
+  return d->side_stream;
+}
+static void level_join(tg_direct *d, cudaStream_t sp, cudaStream_t s) {
+  if (sp == s) return;
+  cudaEventRecord(d->ev_join, sp);
+  cudaStreamWaitEvent(s, d->ev_join, 0);
+}
+
 template <class T>
 static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
-                         const T *a, T *pb, T *kpb, T *ypos, T *xpos,
-                         T *contrib, cudaStream_t s) {
+                         const T *a, T *ypos, T *xpos, T *contrib,
+                         cudaStream_t s) {
   const tg::DirectView v = d->view();
-  tg_mat *A = d->A;
+  const tg::DirectBc bc = d->bc();
   const size_t N = (size_t)d->n * d->bs;
   const int nl = (int)d->level_ptr_h.size() - 1;
   for (int r0 = 0; r0 < nrhs;) {
@@ -450,28 +495,30 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
                    : left >= 2 && d->max_nr >= 2 ? 2 : 1;
     const T *bb = b + (size_t)r0 * N;
     T *xx = x + (size_t)r0 * N;
-    tg::launch_direct_bc_mask<T>(d->n, d->bs, d->d_bcmask, bb, pb, nr, N, s);
-    for (int r = 0; r < nr; r++)
-      bcsr_mult_t(A, a, pb + r * N, kpb + r * N, s);
-    tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, bb, kpb, pb, ypos, nr, N,
-                             s);
+    tg::launch_direct_rhs<T>(d->n, d->bs, d->d_perm, bb, ypos, nr, N, s);
+    tg::launch_direct_bc_couple<T>(bc, d->bs, a, bb, ypos, nr, N, s);
     for (int L = 0; L < nl; L++) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
-      tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
-                                   d->solve_front_h[L], nr, ypos, contrib, s);
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+      const cudaStream_t sp = level_fork(d, le > lb && ce > cb, s);
+      tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
+                                   d->solve_front_h[L], nr, ypos, contrib,
+                                   sp);
       tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
                                            d->cluster_front, nr, ypos,
                                            contrib, s);
+      level_join(d, sp, s);
     }
     for (int L = nl - 1; L >= 0; L--) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
-      tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
-                                    d->solve_front_h[L], nr, ypos, xpos, s);
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
+      const cudaStream_t sp = level_fork(d, le > lb && ce > cb, s);
+      tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
+                                    d->solve_front_h[L], nr, ypos, xpos, sp);
       tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
                                             d->cluster_front, nr, ypos, xpos,
                                             s);
+      level_join(d, sp, s);
     }
     tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, xx, nr, N,
                                    s);
@@ -489,12 +536,11 @@ int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
     return fail(TG_ERR_ARG, "direct solve: precision of the factorisation");
   if (f32)
     solve_levels<float>(d, nrhs, (const float *)b, (float *)x, d->d_a32,
-                        d->d_pb32, d->d_kpb32, d->d_ypos32, d->d_xpos32,
-                        d->d_contrib32, s);
+                        d->d_ypos32, d->d_xpos32, d->d_contrib32, s);
   else
     solve_levels<double>(d, nrhs, (const double *)b, (double *)x,
-                         d->A->d_vals, d->d_pb, d->d_kpb, d->d_ypos,
-                         d->d_xpos, d->d_contrib, s);
+                         d->A->d_vals, d->d_ypos, d->d_xpos, d->d_contrib,
+                         s);
   return 0;
 }
 
@@ -539,16 +585,15 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
       for (int r = 0; r < nr; r++)
         if (done[r])
           TG_CUDA(cudaMemsetAsync(d->d_r32 + r * N, 0, N * sizeof(float), s));
-      solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
-                          d->d_kpb32, d->d_ypos32, d->d_xpos32,
-                          d->d_contrib32, s);
+      solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_ypos32,
+                          d->d_xpos32, d->d_contrib32, s);
       tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
     } else {
       for (int r = 0; r < nr; r++)
         if (done[r])
           TG_CUDA(cudaMemsetAsync(d->d_r + r * N, 0, N * sizeof(double), s));
-      solve_levels<double>(d, nr, d->d_r, d->d_t, d->A->d_vals, d->d_pb,
-                           d->d_kpb, d->d_ypos, d->d_xpos, d->d_contrib, s);
+      solve_levels<double>(d, nr, d->d_r, d->d_t, d->A->d_vals, d->d_ypos,
+                           d->d_xpos, d->d_contrib, s);
     }
     if (ftol > 0.0)  // the step's correction, max |dx|
       for (int r = 0; r < nr; r++)
@@ -697,9 +742,8 @@ int tg_direct_solve_refined(tg_direct *d, const double *b, double *x,
   tg::launch_copy(b, d->d_r, N, S(s));
   for (int k = 0; k < steps; k++) {
     tg::launch_d2f(d->d_r, d->d_r32, N, S(s));
-    solve_levels<float>(d, 1, d->d_r32, d->d_c32, d->d_a32, d->d_pb32,
-                        d->d_kpb32, d->d_ypos32, d->d_xpos32, d->d_contrib32,
-                        S(s));
+    solve_levels<float>(d, 1, d->d_r32, d->d_c32, d->d_a32, d->d_ypos32,
+                        d->d_xpos32, d->d_contrib32, S(s));
     tg::launch_f2d(d->d_c32, d->d_t, N, S(s));
     tg::launch_axpy(1.0, d->d_t, x, N, S(s));
     if (k + 1 < steps) {

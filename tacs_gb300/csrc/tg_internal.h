@@ -384,12 +384,12 @@ size_t direct_solve_smem(int front, int nr, size_t elem);
 size_t direct_cluster_smem(int front, int nr, size_t elem);
 // nrhs right-hand sides ld apart (node order); ypos / xpos interleaved
 template <class T>
-void launch_direct_bc_mask(int n, int bs, const int *bcmask, const T *b,
-                           T *out, int nrhs, size_t ld, cudaStream_t s);
+void launch_direct_rhs(int n, int bs, const int *perm, const T *b, T *ypos,
+                       int nrhs, size_t ld, cudaStream_t s);
 template <class T>
-void launch_direct_rhs(int n, int bs, const int *perm, const T *b,
-                       const T *Kpb, const T *pb, T *ypos, int nrhs,
-                       size_t ld, cudaStream_t s);
+void launch_direct_bc_couple(const DirectBc &c, int bs, const T *a,
+                             const T *b, T *ypos, int nrhs, size_t ld,
+                             cudaStream_t s);
 template <class T>
 void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
                              T *x, int nrhs, size_t ld, cudaStream_t s);

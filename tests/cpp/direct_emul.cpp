@@ -83,7 +83,10 @@ static void de_solve_pass(const tg::DirectView &v,
                           const tg::direct::Analysis &an, int max_front,
                           T *ypos, T *xpos, T *contrib) {
   const int nl = (int)an.level_ptr.size() - 1;
-  const size_t smem = (size_t)max_front * NR + tg::kDirectSolveDiag;
+  // in doubles: the GPU's entries of T rounded up
+  const size_t smem =
+      ((size_t)max_front * NR + tg::direct_plain_extra(NR, (int)sizeof(T))) *
+          sizeof(T) / sizeof(double) + 1;
   for (int L = 0; L < nl; L++) {
     const int lb = an.level_ptr[L], le = an.level_ptr[L + 1];
     launch(direct_forward_kernel<T, NR>, le - lb, 1, smem, v,
@@ -133,13 +136,14 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
       if (an.sn_parent[s] >= 0) ch_list[fill[an.sn_parent[s]]++] = s;
   }
   std::vector<int> bcmask(bcmask_in, bcmask_in + n);
+  const tg::direct::BcCoupling bcc =
+      tg::direct::bc_coupling(rp, cs, bcmask, an.iperm);
   // sized exactly as tg_direct.cu allocates them, so that a sanitizer
   // build sees any access the GPU would make out of bounds
   const int max_nr = nrhs >= 4 ? 4 : nrhs >= 2 ? 2 : 1;
   std::vector<T> lstore((size_t)an.l_total * b2),
       pool((size_t)an.u_peak * b2), contrib(vacc * max_nr),
-      ypos(N * max_nr), xpos(N * max_nr), pb(N * max_nr), kpb(N * max_nr),
-      bt(b_in, b_in + N * nrhs), xt(N * nrhs), vt(vals, vals + rowp[n] * b2);
+      ypos(N * max_nr), xpos(N * max_nr), bt(b_in, b_in + N * nrhs), xt(N * nrhs), vt(vals, vals + rowp[n] * b2);
   const T *b = bt.data();
   T *x = xt.data();
   int failflag = 0;
@@ -262,21 +266,14 @@ static int de_solve_t(int n, int bs, const int *rowp, const int *cols,
     const int left = nrhs - r0;
     const int nr = left >= 4 ? 4 : left >= 2 ? 2 : 1;
     const T *bb = b + (size_t)r0 * N;
-    launch(direct_bc_mask_kernel<T>, 1, 1, 0, n, bs,
-           (const int *)bcmask.data(), bb, pb.data(), nr, N);
-    for (int q = 0; q < nr; q++)  // the BCSR mat-vec, in T
-      for (int i = 0; i < n; i++)
-        for (int r = 0; r < bs; r++) {
-          T acc = 0;
-          for (int j = rowp[i]; j < rowp[i + 1]; j++)
-            for (int c = 0; c < bs; c++)
-              acc += vt[b2 * j + r * bs + c] *
-                     pb[q * N + (size_t)cols[j] * bs + c];
-          kpb[q * N + (size_t)i * bs + r] = acc;
-        }
     launch(direct_rhs_kernel<T>, 1, 1, 0, n, bs, (const int *)an.perm.data(),
-           bb, (const T *)kpb.data(), (const T *)pb.data(), ypos.data(), nr,
-           N);
+           bb, ypos.data(), nr, N);
+    if (!bcc.row.empty())
+      launch(direct_bc_couple_kernel<T>, 1, 1, 0, (int)bcc.row.size(), bs,
+             (const int *)bcc.row.data(), (const int *)bcc.pos.data(),
+             (const int *)bcc.ptr.data(), (const int *)bcc.blk.data(),
+             (const int *)cols, (const int *)bcmask.data(),
+             (const T *)vt.data(), bb, ypos.data(), nr, N);
     if (nr == 4)
       de_solve_pass<T, 4>(v, an, max_front, ypos.data(), xpos.data(),
                           contrib.data());
