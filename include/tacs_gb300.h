@@ -375,6 +375,18 @@ int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out);
    (src/bpmat/BCSRMat.cpp:625); levFill = 0 is tg_pc_create(TG_PC_ILU0).
    The pattern is built here on the host, once. */
 int tg_pc_create_iluk(tg_mat *A, int lev_fill, int precision, tg_pc **out);
+/* TACSSerialPivotPc over an existing factorisation
+   (src/bpmat/TACSSerialPivotMat.h:66): a TG_PC_DIRECT preconditioner that
+   shares d (its precision, its factor, a reference to it) instead of
+   factoring the matrix again, so that GMRES can take an FP32
+   factorisation that plain iterative refinement does not converge with
+   (GMRES-IR).  tg_direct_factor(d) refactors; tg_pc_factor on this pc only
+   refreshes the FP32 copy of the matrix values that mixed GMRES uses. */
+int tg_pc_create_direct(tg_direct *d, tg_pc **out);
+/* No reference counterpart.  *used = 1 when an FP32 pc's FP64 factor of
+   the same matrix has been made since its last tg_pc_factor (the mixed
+   GMRES passes switched to it), else 0. */
+int tg_pc_get_fp64_used(tg_pc *pc, int *used);
 /* Level of fill and the factor's block count (nnz(ILU)). */
 int tg_pc_get_fill(tg_pc *pc, int *lev_fill, int *nnz_factor);
 int tg_pc_decref(tg_pc *pc);

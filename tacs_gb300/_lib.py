@@ -80,6 +80,8 @@ SIGNATURES = [
     ("tg_mat_mult_f32", _I, [_P, _P, _P, _P]),
     ("tg_pc_create", _I, [_P, _I, _I, C.POINTER(_P)]),
     ("tg_pc_create_iluk", _I, [_P, _I, _I, _P]),
+    ("tg_pc_create_direct", _I, [_P, C.POINTER(_P)]),
+    ("tg_pc_get_fp64_used", _I, [_P, _IP]),
     ("tg_pc_get_fill", _I, [_P, _P, _P]),
     ("tg_pc_decref", _I, [_P]),
     ("tg_pc_factor", _I, [_P, _P]),

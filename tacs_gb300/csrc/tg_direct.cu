@@ -528,6 +528,11 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
 
 namespace tg {
 
+tg_mat *direct_matrix(const tg_direct *d) { return d->A; }
+int direct_precision(const tg_direct *d) { return d->precision; }
+bool direct_is_factored(const tg_direct *d) { return d->factored; }
+void direct_incref(tg_direct *d) { d->refcount++; }
+
 int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
                          bool f32, cudaStream_t s) {
   if (!d || !b || !x || nrhs < 1)

@@ -210,6 +210,9 @@ struct tg_pc {
   // TG_PC_DIRECT: the factorisation in the pc's precision, and for an FP32
   // pc the FP64 one its FP64 fallback passes use
   tg_direct *direct = nullptr, *direct64 = nullptr;
+  // direct is the caller's factorisation (tg_pc_create_direct): the pc
+  // never factors it
+  bool shared_direct = false;
   ~tg_pc() {
     if (direct) tg_direct_decref(direct);
     if (direct64) tg_direct_decref(direct64);
@@ -311,4 +314,10 @@ int pc_prepare_fp64(tg_pc *pc);
 // one
 int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
                          bool f32, cudaStream_t s);
+// a factorisation's matrix, precision and factored state, and one more
+// reference to it (tg_pc_create_direct; tg_direct.cu)
+tg_mat *direct_matrix(const tg_direct *d);
+int direct_precision(const tg_direct *d);
+bool direct_is_factored(const tg_direct *d);
+void direct_incref(tg_direct *d);
 }  // namespace tg

@@ -1314,6 +1314,40 @@ static int pc_create(tg_mat *A, int type, int lev_fill, int precision,
 int tg_pc_create(tg_mat *A, int type, int precision, tg_pc **out) {
   return pc_create(A, type, 0, precision, out);
 }
+int tg_pc_create_direct(tg_direct *d, tg_pc **out) {
+  if (!d || !out) return fail(TG_ERR_ARG, "tg_pc_create_direct: NULL argument");
+  *out = nullptr;
+  tg_pc *pc = new tg_pc();
+  pc->A = tg::direct_matrix(d);
+  pc->A->refcount++;
+  pc->type = TG_PC_DIRECT;
+  pc->precision = tg::direct_precision(d);
+  pc->fnnz = pc->A->nnz;
+  pc->direct = d;
+  pc->shared_direct = true;
+  tg::direct_incref(d);
+  const size_t n = (size_t)pc->A->nrows * pc->A->bsize;
+  int rc = dalloc(&pc->d_fail, 1);
+  if (!rc) rc = dalloc(&pc->d_gx, n);
+  if (!rc) rc = dalloc(&pc->d_gy, n);
+  if (!rc && pc->precision == TG_PREC_FP32) rc = dalloc(&pc->d_x32, n);
+  if (!rc && pc->precision == TG_PREC_FP32) rc = dalloc(&pc->d_y32, n);
+  if (rc) {
+    tg_pc_decref(pc);
+    return rc;
+  }
+  pc->plan.bsize = pc->A->bsize;
+  pc->plan.nrows = pc->A->nrows;
+  *out = pc;
+  return 0;
+}
+
+int tg_pc_get_fp64_used(tg_pc *pc, int *used) {
+  if (!pc || !used) return fail(TG_ERR_ARG, "tg_pc_get_fp64_used: NULL");
+  *used = pc->precision == TG_PREC_FP32 && pc->fp64_ready ? 1 : 0;
+  return 0;
+}
+
 int tg_pc_create_iluk(tg_mat *A, int lev_fill, int precision, tg_pc **out) {
   return pc_create(A, TG_PC_ILU0, lev_fill, precision, out);
 }
@@ -1446,6 +1480,16 @@ extern "C" {
 int tg_pc_factor(tg_pc *pc, void *s) {
   if (!pc) return fail(TG_ERR_ARG, "tg_pc_factor: NULL pc");
   tg_mat *A = pc->A;
+  if (pc->type == TG_PC_DIRECT && pc->shared_direct) {
+    if (!tg::direct_is_factored(pc->direct))
+      return fail(TG_ERR_STATE, "tg_pc_factor: the shared factorisation is "
+                                "not factored");
+    int rc = pc->precision == TG_PREC_FP32 ? ensure_f32(A, S(s)) : 0;
+    if (rc) return rc;
+    pc->factored = true;
+    pc->fp64_ready = false;
+    return 0;
+  }
   if (pc->type == TG_PC_DIRECT) {
     int rc = tg_direct_factor(pc->direct, s);
     if (!rc && pc->precision == TG_PREC_FP32) rc = ensure_f32(A, S(s));

@@ -73,6 +73,23 @@ class Mat:
 class Pc:
     """tg_pc: ILU(k) / block-Jacobi preconditioner, FP64 or FP32."""
 
+    @classmethod
+    def from_direct(cls, direct):
+        """tg_pc_create_direct: a preconditioner sharing the factorisation
+        of a Direct (factor() then only refreshes the FP32 matrix copy)."""
+        h = C.c_void_p()
+        check(_lib.lib().tg_pc_create_direct(direct.handle, C.byref(h)),
+              "tg_pc_create_direct")
+        pc = cls.__new__(cls)
+        pc.handle, pc.mat, pc.direct = h, direct.mat, direct
+        return pc
+
+    def fp64_used(self):
+        """True when mixed GMRES switched to an FP64 factor of the matrix."""
+        u = C.c_int(0)
+        check(_lib.lib().tg_pc_get_fp64_used(self.handle, C.byref(u)))
+        return bool(u.value)
+
     def __init__(self, mat, kind=_lib.PC_ILU0, precision=_lib.PREC_FP64,
                  lev_fill=0):
         h = C.c_void_p()
@@ -131,10 +148,22 @@ class Direct:
     precision PREC_FP32 factors in FP32 and solves FP64 right-hand sides
     by iterative refinement (FP64 residuals, FP32 corrections) until the
     normwise backward error is at most eps sqrt(N) (the test of LAPACK's
-    mixed-precision dsgesv) and a further step no longer halves it.  Where that cannot work -- the FP32 Cholesky
-    meets a non-positive pivot, or refinement stagnates because cond(A) is
-    near the inverse of FP32's unit roundoff -- the matrix is factored in
-    FP64 instead (`fell_back`), from its values at that moment."""
+    mixed-precision dsgesv) and a further step no longer halves it.  Where
+    refinement stagnates (cond(A) near the inverse of FP32's unit
+    roundoff, so that one FP32 solve contracts the error too little), the
+    solve is done again by FP64 GMRES preconditioned by the same FP32
+    factorisation (GMRES-IR, `mode` "gmres_ir", which later solves then
+    take directly); where that fails too, or the FP32 Cholesky meets a
+    non-positive pivot, the matrix is factored in FP64 instead
+    (`fell_back`), from its values at that moment.
+
+    autotune: tg_direct_autotune picks the solves' launch shapes once per
+    matrix shape.  It costs about a dozen solves, so it runs at the second
+    factor() of this object (a factorisation reused for a design loop), or
+    at the first when this process has tuned the shape before (then it
+    only applies the cached choice)."""
+
+    _tuned_shapes = set()
 
     def __init__(self, mat, use_coords=True, precision=_lib.PREC_FP64,
                  autotune=True):
@@ -151,21 +180,35 @@ class Direct:
         # (tg_direct_autotune), then cached per matrix shape
         self.autotune = autotune
         self.tuned = None
+        self.nfactor = 0
+        # FP32: how FP64 right-hand sides are solved ("refine", or
+        # "gmres_ir" after refinement stagnated on this matrix)
+        self.mode = "refine"
+        self._ir = None
+        self.last_gmres_iters = 0
 
     def _factor_fp64(self):
         self._fp64 = Direct(self.mat, self.use_coords, _lib.PREC_FP64)
         self._fp64.factor()
         self.fell_back = True
 
+    def _shape(self):
+        m = self.mat
+        return (m.nrows, m.nnz, m.bsize, self.precision,
+                torch.cuda.current_device())
+
     def factor(self):
         self._fp64 = None
         self.fell_back = False
+        self.nfactor += 1
         rc = _lib.lib().tg_direct_factor(self.handle, _stream())
         if rc == _lib.ERR_PIVOT and self.precision == _lib.PREC_FP32:
             self._factor_fp64()  # the FP32 Cholesky broke down
             return
         check(rc, "tg_direct_factor")
-        if self.autotune and self.tuned is None:
+        if self.autotune and self.tuned is None and (
+                self.nfactor >= 2 or self._shape() in Direct._tuned_shapes):
+            Direct._tuned_shapes.add(self._shape())
             thr = C.c_int(0)
             ms = np.zeros(3)
             check(_lib.lib().tg_direct_autotune(self.handle, C.byref(thr),
@@ -199,6 +242,9 @@ class Direct:
                 tol = 2.0 ** -53 * float(np.sqrt(n))
             if x.data_ptr() == b.data_ptr():  # in place: refine from a copy
                 b = b.clone()
+            f32 = self.precision == _lib.PREC_FP32
+            if f32 and self.mode == "gmres_ir":
+                return self._gmres_ir_or_fp64(b, x, steps, rtol)
             st = np.zeros(nrhs, np.int32)
             eta = np.zeros(nrhs)
             rc = L.tg_direct_solve_refined_multi(
@@ -206,9 +252,10 @@ class Direct:
                 float(ftol), float(rtol), st.ctypes.data, eta.ctypes.data,
                 _stream())
             self.last_steps, self.last_eta = int(st.max()), float(eta.max())
-            if rc == _lib.ERR_NOCONV and self.precision == _lib.PREC_FP32:
-                self._factor_fp64()
-                return self._fp64.solve(b, x, steps=steps, rtol=rtol)
+            if rc == _lib.ERR_NOCONV and f32:
+                # refinement stagnated: this matrix needs GMRES-IR
+                self.mode = "gmres_ir"
+                return self._gmres_ir_or_fp64(b, x, steps, rtol)
             check(rc, "tg_direct_solve_refined_multi")
             return x
         if self.precision == _lib.PREC_FP32:
@@ -223,6 +270,30 @@ class Direct:
                                       _stream()), "tg_direct_solve_multi")
         return x
 
+    def _gmres_ir_or_fp64(self, b, x, steps, rtol):
+        """FP64 flexible GMRES(30) preconditioned by this FP32
+        factorisation (GMRES-IR) to the relative residual rtol (1e-12 when
+        none is given), restarted up to max(steps, 10) times; the FP64
+        factorisation when it does not converge."""
+        n = b.shape[-1]
+        if self._ir is None:
+            pc = Pc.from_direct(self)
+            # FP64 Arnoldi and mat-vec, the FP32 factorisation applied to
+            # FP32 copies of the Krylov vectors (flexible GMRES)
+            self._ir = (pc, Ksm(self.mat, pc, m=30, nrestart=max(steps, 10),
+                                mixed=False))
+        pc, ksm = self._ir
+        pc.factor()  # the FP32 copy of the current matrix values
+        ksm.set_tolerances(rtol if rtol > 0.0 else 1e-12)
+        X, it, fl, rn, rc = ksm.solve_multi(b.reshape(-1, n),
+                                            x.reshape(-1, n))
+        self.last_gmres_iters = int(it.max())
+        self.last_steps = 0
+        if rc == 1:
+            return x
+        self._factor_fp64()
+        return self._fp64.solve(b, x, steps=steps, rtol=rtol)
+
     def stats(self):
         st = np.zeros(9)
         check(_lib.lib().tg_direct_get_stats(self.handle, st.ctypes.data))
@@ -233,6 +304,11 @@ class Direct:
                 "cluster_threshold": int(st[8]),
                 "tuned": self.tuned,
                 "fell_back_to_fp64": self.fell_back,
+                "fp32_mode": self.mode if self.precision ==
+                _lib.PREC_FP32 else None,
+                "last_gmres_iters": self.last_gmres_iters,
+                "gmres_ir_fp64_factor": bool(self._ir is not None
+                                             and self._ir[0].fp64_used()),
                 "last_refinement_steps": self.last_steps,
                 "last_backward_error": self.last_eta}
 

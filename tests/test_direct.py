@@ -223,11 +223,12 @@ def test_direct_as_gmres_preconditioner(gpu):
 def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
     """FP32 factorisation + FP64 refinement converges when the normwise
     backward error reaches eps sqrt(N) (and refines on while the steps halve
-    it); where it cannot (the FP32 Cholesky
-    breaks down or refinement stagnates, cond(K) near 2^24) the solve falls
-    back to an FP64 factorisation.  Either way the result has the FP64
-    backward error (1e-13) and is the FP64 direct solution to within 10x
-    the rounding spread of an exact solve (1e-8 where that is smaller)."""
+    it); where it cannot (refinement stagnates, cond(K) near 2^24) the
+    solve is done by GMRES preconditioned by the FP32 factorisation
+    (GMRES-IR), and where the FP32 Cholesky breaks down by an FP64
+    factorisation.  Every way the result has the FP64 backward error
+    (1e-13) and is the FP64 direct solution to within 10x the rounding
+    spread of an exact solve (1e-8 where that is smaller)."""
     from tacs_gb300 import _lib, meshes
     n = 48
     prob = meshes.plate(n, n, 2.0, 2.0, t=0.002 if thin else 0.01)
@@ -246,9 +247,10 @@ def test_mixed_direct_stops_on_backward_error_or_falls_back(gpu, thin):
     x = d32.solve(b)
     st = d32.stats()
     tol = 2.0 ** -53 * np.sqrt(M.ndof)
-    assert st["fell_back_to_fp64"] or st["last_backward_error"] <= tol
+    assert (st["fell_back_to_fp64"] or st["fp32_mode"] == "gmres_ir"
+            or st["last_backward_error"] <= tol)
     if not thin:
-        assert not st["fell_back_to_fp64"]
+        assert not st["fell_back_to_fp64"] and st["fp32_mode"] == "refine"
         # refinement runs on while a step halves the backward error
         assert 1 <= st["last_refinement_steps"] <= 30
     K = _host_matrix(mat, M.ndof)
@@ -377,11 +379,11 @@ def test_fp64_direct_refined_to_relative_residual(gpu):
 
 
 def test_direct_autotune(gpu):
-    """The solves' launch-shape autotuner (tg_direct_autotune, run after
-    the first factorisation): it times a solve per cluster threshold and
-    keeps one of the candidates; a second factorisation of the same matrix
-    shape takes the cached choice without timing; the solution is the
-    same to rounding whatever the threshold."""
+    """The solves' launch-shape autotuner (tg_direct_autotune, run at the
+    second factorisation of a Direct): it times a solve per cluster
+    threshold and keeps one of the candidates; another Direct of the same
+    matrix shape takes the cached choice at its first factorisation without
+    timing; the solution is the same to rounding whatever the threshold."""
     from tacs_gb300 import meshes
     # a shape no other test factors (the choice is cached per shape)
     prob = meshes.plate_c2(120, 0.5, seed=2)
@@ -391,6 +393,11 @@ def test_direct_autotune(gpu):
     M.assemble_jacobian(M.vec(), mat, r0)
     b = -r0
     d = gpu.Direct(mat)
+    d.factor()
+    # a first factorisation solves with the default shapes; the second
+    # (the factorisation reused) tunes them
+    assert d.stats()["tuned"] is None
+    assert d.stats()["cluster_threshold"] == 768
     d.factor()
     t = d.stats()["tuned"]
     assert t["cluster_threshold"] in t["candidates"]
@@ -406,3 +413,49 @@ def test_direct_autotune(gpu):
     d3.factor()
     assert d3.stats()["cluster_threshold"] == 768
     assert rel(x.cpu().numpy(), d3.solve(b).cpu().numpy()) < 1e-10
+
+
+def test_mixed_direct_gmres_ir(gpu):
+    """Where refinement with the FP32 factorisation does not reach the
+    tolerance (here forced: one step allowed), the FP32 Direct solves by
+    GMRES preconditioned by its own factorisation (tg_pc_create_direct,
+    GMRES-IR) instead of factoring in FP64, and later solves go there
+    directly; the solutions match the FP64 factorisation's to the GMRES
+    tolerance, for one and for several right-hand sides."""
+    from tacs_gb300 import _lib, meshes
+    prob = meshes.plate_c2(64, 2.0 * 64 / 512, seed=2)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    b = -r0
+    d64 = gpu.Direct(mat)
+    d64.factor()
+    x64 = d64.solve(b)
+    d32 = gpu.Direct(mat, precision=_lib.PREC_FP32)
+    d32.factor()
+    x = d32.solve(b, steps=1, rtol=1e-12)
+    st = d32.stats()
+    assert st["fp32_mode"] == "gmres_ir"
+    assert not st["fell_back_to_fp64"] and not st["gmres_ir_fp64_factor"]
+    assert st["last_gmres_iters"] >= 1
+    assert rel(x.cpu().numpy(), x64.cpu().numpy()) < 1e-8
+    g = torch.Generator(device="cuda").manual_seed(5)
+    B = torch.randn(3, M.ndof, dtype=torch.float64, device="cuda",
+                    generator=g)
+    for r in range(3):
+        M.apply_bcs(B[r])
+    X = d32.solve(B, rtol=1e-12)  # straight to GMRES-IR: no refinement
+    assert d32.stats()["last_refinement_steps"] == 0
+    X64 = d64.solve(B)
+    for r in range(3):
+        assert rel(X[r].cpu().numpy(), X64[r].cpu().numpy()) < 1e-8
+    # a new factorisation of changed values keeps the mode and refreshes
+    # the preconditioner's FP32 copy of the matrix
+    t2 = torch.as_tensor(1.3 * np.asarray(prob["thick"]), device="cuda")
+    M.set_design_vars(t2)
+    M.assemble_jacobian(M.vec(), mat, r0)
+    d32.factor()
+    d64.factor()
+    x2 = d32.solve(b, rtol=1e-12)
+    assert rel(x2.cpu().numpy(), d64.solve(b).cpu().numpy()) < 1e-8
