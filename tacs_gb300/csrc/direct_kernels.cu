@@ -167,20 +167,39 @@ void launch_direct_forward_cluster(const DirectView &v, const int *sn,
 }
 
 template <class T>
+void launch_direct_bwd_gemv(const DirectView &v, const int *sn,
+                            const int *tprefix, const int64_t *poff,
+                            int count, int total, int nr, const T *x,
+                            T *part, cudaStream_t s) {
+  if (count <= 0 || total <= 0) return;
+  const unsigned g = (unsigned)((total + 7) / 8);
+  if (nr == 4)
+    direct_bwd_gemv_kernel<T, 4><<<g, 256, 0, s>>>(v, sn, tprefix, poff,
+                                                   count, total, x, part);
+  else if (nr == 2)
+    direct_bwd_gemv_kernel<T, 2><<<g, 256, 0, s>>>(v, sn, tprefix, poff,
+                                                   count, total, x, part);
+  else
+    direct_bwd_gemv_kernel<T, 1><<<g, 256, 0, s>>>(v, sn, tprefix, poff,
+                                                   count, total, x, part);
+}
+
+template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
-                                    int count, int max_front, int nr,
-                                    const T *y, T *x, cudaStream_t s) {
+                                    const int64_t *poff, int count,
+                                    int max_front, int nr, const T *y, T *x,
+                                    const T *part, cudaStream_t s) {
   if (count <= 0) return;
   const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T));
   if (nr == 4)
     cluster_launch_dk(direct_backward_cluster_kernel<T, 4>, count, smem, s,
-                      v, sn, count, y, x);
+                      v, sn, poff, count, y, x, part);
   else if (nr == 2)
     cluster_launch_dk(direct_backward_cluster_kernel<T, 2>, count, smem, s,
-                      v, sn, count, y, x);
+                      v, sn, poff, count, y, x, part);
   else
     cluster_launch_dk(direct_backward_cluster_kernel<T, 1>, count, smem, s,
-                      v, sn, count, y, x);
+                      v, sn, poff, count, y, x, part);
 }
 
 // whether the device schedules the solve clusters (at least one active),
@@ -337,9 +356,12 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
   template void launch_direct_forward_cluster<T>(                          \
       const DirectView &, const int *, int, int, int, T *, T *,            \
       cudaStream_t);                                                        \
+  template void launch_direct_bwd_gemv<T>(                                 \
+      const DirectView &, const int *, const int *, const int64_t *, int,  \
+      int, int, const T *, T *, cudaStream_t);                              \
   template void launch_direct_backward_cluster<T>(                         \
-      const DirectView &, const int *, int, int, int, const T *, T *,      \
-      cudaStream_t);                                                        \
+      const DirectView &, const int *, const int64_t *, int, int, int,     \
+      const T *, T *, const T *, cudaStream_t);                             \
   template void launch_direct_rhs<T>(int, int, const int *, const T *,     \
                                      T *, int, size_t, cudaStream_t);      \
   template void launch_direct_bc_couple<T>(const DirectBc &, int,          \

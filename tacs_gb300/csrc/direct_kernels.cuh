@@ -569,24 +569,34 @@ __device__ __forceinline__ void dk_inv_solve(const T (*X)[33], int nb, T *z,
 
 #ifndef DK_EMULATE
 // z(r0 + i) -= L(r0 + i, kb .. kb + nb) zk for the rows i < 32 of a row
-// group with bit i of `valid` set, by one warp: lane c multiplies column c
-// of every row (each row a coalesced load), then a butterfly of shuffles
-// sums the rows' products so that lane i holds row i's sum (31 shuffles for
-// 32 rows).  L0: row r0's column kb; ldl: the panel's row stride; zrow(i):
+// group with bit i of `valid` set, by one warp: lane c loads column c of
+// every row (each row a coalesced load, all 32 issued together), then per
+// butterfly the products of 32 / NR rows with the NR right-hand sides
+// (entry i NR + q: row i, right-hand side q) are summed across the lanes
+// by shuffles so that lane j holds entry j's sum (31 shuffles per 32
+// sums).  L0: row r0's column kb; ldl: the panel's row stride; zrow(i):
 // row i's NR entries of z.
 template <class T, int NR, class ZRow>
 __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
                                              const T *zk, unsigned valid,
                                              ZRow zrow) {
+  constexpr int RB = 32 / NR;  // rows per butterfly
   const int lane = threadIdx.x & 31;
-#pragma unroll 1
-  for (int q = 0; q < NR; q++) {
-    const T zc = lane < nb ? zk[lane * NR + q] : T(0);
+  T zc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; q++) zc[q] = lane < nb ? zk[lane * NR + q] : T(0);
+  T l[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    l[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane]
+                                            : T(0);
+#pragma unroll
+  for (int g = 0; g < NR; g++) {
     T v[32];
 #pragma unroll
-    for (int i = 0; i < 32; i++)
-      v[i] = ((valid >> i) & 1u) && lane < nb ? L0[(size_t)i * ldl + lane] * zc
-                                              : T(0);
+    for (int i = 0; i < RB; i++)
+#pragma unroll
+      for (int q = 0; q < NR; q++) v[i * NR + q] = l[g * RB + i] * zc[q];
 #pragma unroll
     for (int h = 16; h >= 1; h >>= 1) {
       const bool up = (lane & h) != 0;
@@ -597,7 +607,8 @@ __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
       }
     }
-    if ((valid >> lane) & 1u) zrow(lane)[q] -= v[0];
+    const int r = g * RB + lane / NR;
+    if ((valid >> r) & 1u) zrow(r)[lane % NR] -= v[0];
   }
 }
 #endif  // DK_EMULATE
@@ -779,7 +790,7 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
 // the front was factored by panels); own rows to x.  kDirectPlainThreads
 // threads.
 template <class T, int NR>
-__global__ void __launch_bounds__(kDirectPlainThreads)
+__global__ void __launch_bounds__(kDirectPlainThreads, 6)
     direct_backward_kernel(DirectView v, const int *__restrict__ sn,
                            int count, const T *y, T *x) {
   if ((int)blockIdx.x >= count) return;
@@ -876,6 +887,75 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
 }
 
 #ifndef DK_EMULATE
+// The backward solve's products L21^T x2 of the fronts solved by clusters
+// (the part of their work that does not wait for the chain of diagonal
+// blocks), over the whole GPU.  Tile = (front k of the level's list,
+// 32-column block, chunk of kDirectGemvRows update rows), one warp each:
+// lane = column (each row's load coalesced); the chunk's entries of x2
+// are gathered once, lane i holding those of the rows i mod 32, and
+// broadcast by shuffles.  part[(poff[k] + chunk C + j) NR + q] = the
+// chunk's sum for column j (one writer per entry; the cluster kernel adds
+// the chunks in order).  tprefix[k]: the tiles of fronts 0 .. k.
+template <class T, int NR>
+__global__ void __launch_bounds__(256)
+    direct_bwd_gemv_kernel(DirectView v, const int *__restrict__ sn,
+                           const int *__restrict__ tprefix,
+                           const int64_t *__restrict__ poff, int count,
+                           int total, const T *__restrict__ x,
+                           T *__restrict__ part) {
+  constexpr int U = kDirectGemvRows / 32;
+  const int tile = (int)blockIdx.x * 8 + ((int)threadIdx.x >> 5);
+  if (tile >= total) return;
+  const int lane = (int)threadIdx.x & 31;
+  int lo = 0, hi = count - 1;  // the first front whose prefix passes tile
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (tprefix[mid] > tile) hi = mid;
+    else lo = mid + 1;
+  }
+  const int k = lo;
+  const int lt = tile - (k > 0 ? tprefix[k - 1] : 0);
+  const int s = sn[k];
+  const Front<T> f = front_of<T>(v, s);
+  const int ncb = (f.C + 31) >> 5;
+  const int cb = lt % ncb, rc = lt / ncb;
+  const int i0 = f.C + rc * kDirectGemvRows;
+  const int nrow = f.M - i0 < kDirectGemvRows ? f.M - i0 : kDirectGemvRows;
+  const int *rows = v.sn_rows + v.sn_rowptr[s];
+  T xr[U][NR];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int r = lane + 32 * u;
+    const size_t g = r < nrow ? dk_pos(rows, v.bs, i0 + r) * NR : 0;
+#pragma unroll
+    for (int q = 0; q < NR; q++) xr[u][q] = r < nrow ? x[g + q] : T(0);
+  }
+  const int j = cb * 32 + lane;
+  const T *Lj = f.lp + (size_t)i0 * f.C + (j < f.C ? j : 0);
+  T acc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; q++) acc[q] = 0;
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+#pragma unroll 16
+    for (int w = 0; w < 32; w++) {
+      const int r = 32 * u + w;
+      if (r < nrow) {  // the same for the whole warp
+        const T l = Lj[(size_t)r * f.C];
+#pragma unroll
+        for (int q = 0; q < NR; q++)
+          acc[q] += l * __shfl_sync(0xffffffffu, xr[u][q], w);
+      }
+    }
+  }
+  if (j < f.C)
+#pragma unroll
+    for (int q = 0; q < NR; q++)
+      part[(poff[k] + (int64_t)rc * f.C + j) * NR + q] = acc[q];
+}
+#endif  // DK_EMULATE
+
+#ifndef DK_EMULATE
 // Large fronts: one thread-block cluster of kDirectSolveCluster CTAs (256
 // threads each) per front, so that the front's triangular solves use that
 // many SMs (one CTA per front leaves the top of the tree, a handful of
@@ -897,11 +977,6 @@ __global__ void __launch_bounds__(kDirectPlainThreads)
 // front only); a final barrier keeps each CTA's shared memory alive until
 // the others are done reading it.  Dynamic shared memory: the owned rows
 // (rounded up to whole blocks) x NR.
-constexpr int kClusterWarps = kDirectClusterThreads / 32;
-// the first phase of the backward solve keeps one 32 x NR partial sum per
-// warp in the 32 x 33 staging area of the inverses
-static_assert(kClusterWarps * 32 * 4 <= 32 * 33, "cluster partial sums");
-
 struct ClusterRows {
   int nr, rank;
   __device__ __forceinline__ bool owns(int r) const {
@@ -1034,9 +1109,11 @@ __global__ void __launch_bounds__(kDirectClusterThreads)
 }
 
 template <class T, int NR>
-__global__ void __launch_bounds__(kDirectClusterThreads)
+__global__ void __launch_bounds__(kDirectClusterThreads, 4)
     direct_backward_cluster_kernel(DirectView v, const int *__restrict__ sn,
-                                   int count, const T *y, T *x) {
+                                   const int64_t *__restrict__ poff,
+                                   int count, const T *y, T *x,
+                                   const T *part) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
@@ -1053,61 +1130,27 @@ __global__ void __launch_bounds__(kDirectClusterThreads)
   const int nown = cr.count(f.M);
   const T *inv = dk_dinv(v, (T *)nullptr) + v.dinv_off[s];
   const int nblk = (f.C + 31) >> 5;
-  const int warp = (int)threadIdx.x >> 5;
   // own rows of the triangle: y1 - L21^T x2 (x2 final, from the
-  // ancestors).  A warp takes one of this rank's 32-column blocks (lane =
-  // column, each row's load coalesced, x2 a broadcast) and, when the rank
-  // has fewer blocks than warps, one of P interleaved parts of the update
-  // rows, so that every warp streams rows; the parts' sums meet in shared
-  // memory (the inverse's staging area, free until the chain starts) in a
-  // fixed order.
+  // ancestors), the products summed over the update-row chunks of
+  // direct_bwd_gemv_kernel in order
   {
-    const int lane = (int)threadIdx.x & 31;
-    const int nob = cr.count(f.C) >> 5;
-    const int P = nob >= kClusterWarps ? 1 : kClusterWarps / (nob > 0 ? nob : 1);
-    T(*part)[32 * NR] = reinterpret_cast<T(*)[32 * NR]>(&Ls[0][0]);
-    for (int task = warp; task < nob * P; task += kClusterWarps) {
-      const int ob = task % nob, pp = task / nob;
-      const int t = (ob << 5) + lane;
+    const int nrc = (f.M - f.C + kDirectGemvRows - 1) / kDirectGemvRows;
+    const T *pf = part + poff[fi] * NR;
+    for (int t = threadIdx.x; t < nown; t += blockDim.x) {
       const int j = cr.row(t);
-      T acc[NR];
+      if (j >= f.C) continue;
+      const size_t gj = dk_pos(rows, bs, j) * NR;
+      T sum[NR];
 #pragma unroll
-      for (int q = 0; q < NR; q++) acc[q] = 0;
-      if (j < f.C) {
-        const T *Lj = f.lp + j;
-#pragma unroll 8
-        for (int i = f.C + pp; i < f.M; i += P) {
-          const T l = Lj[(size_t)i * f.C];
-          const size_t g = dk_pos(rows, bs, i) * NR;
+      for (int q = 0; q < NR; q++) sum[q] = 0;
+#pragma unroll 4
+      for (int rc = 0; rc < nrc; rc++)
 #pragma unroll
-          for (int q = 0; q < NR; q++) acc[q] += l * x[g + q];
-        }
-      }
-      if (P == 1) {
-        if (j < f.C) {
-          const size_t gj = dk_pos(rows, bs, j) * NR;
+        for (int q = 0; q < NR; q++)
+          sum[q] += pf[((size_t)rc * f.C + j) * NR + q];
 #pragma unroll
-          for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - acc[q];
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < NR; q++) part[task][lane * NR + q] = acc[q];
-      }
+      for (int q = 0; q < NR; q++) z[t * NR + q] = y[gj + q] - sum[q];
     }
-    __syncthreads();
-    if (P > 1)
-      for (int t = threadIdx.x; t < nob * 32; t += blockDim.x) {
-        const int j = cr.row(t);
-        if (j >= f.C) continue;
-        const size_t gj = dk_pos(rows, bs, j) * NR;
-#pragma unroll
-        for (int q = 0; q < NR; q++) {
-          T sum = 0;
-          for (int pp = 0; pp < P; pp++)
-            sum += part[pp * nob + (t >> 5)][(t & 31) * NR + q];
-          z[t * NR + q] = y[gj + q] - sum;
-        }
-      }
     __syncthreads();
   }
   T pre[4];

@@ -36,6 +36,9 @@ constexpr int kDirectExtendRows = 32;
 constexpr int kDirectSolveCluster = 8;
 // threads of a CTA of the cluster solves
 constexpr int kDirectClusterThreads = 256;
+// update rows of one tile of the backward solve's L21^T x2 products for
+// the fronts solved by clusters (direct_bwd_gemv_kernel)
+constexpr int kDirectGemvRows = 128;
 constexpr int kDirectClusterFront = 768;
 constexpr int kDirectSolveDiag = kDirectSolveBlock * (kDirectSolveBlock + 1);
 

@@ -43,6 +43,7 @@ struct tg_direct {
   // device schedules them); tg_direct_autotune picks it
   bool clusters_ok = false;
   int cluster_threshold = tg::kDirectClusterFront;
+  long long layout_version = 0;  // build_solve_lists calls
   int precision = TG_PREC_FP64;
   tg::direct::Analysis an;
   std::vector<int> level_ptr_h, level_sn_h, front_m_h, front_c_h;
@@ -63,6 +64,15 @@ struct tg_direct {
   std::vector<int> solve_front_h;
   int *d_solve_sn = nullptr, *d_csolve_sn = nullptr;
   std::vector<int> solve_sn_h, csolve_sn_h;
+  // the backward solve's L21^T x2 tiles of the cluster fronts: per front
+  // of csolve_sn_h the cumulative tiles and the offset of its chunk sums
+  // within its level, per level the tiles; the chunk sums' buffer (entries
+  // of the factor's precision, for max_nr right-hand sides)
+  int *d_gemv_tp = nullptr;
+  int64_t *d_gemv_poff = nullptr;
+  std::vector<int> gemv_total_h;
+  void *d_part = nullptr;
+  size_t part_entries = 0;
   tg::direct::PanelSteps steps;
   int *d_small = nullptr, *d_step_fronts = nullptr, *d_step_tprefix = nullptr,
       *d_step_rprefix = nullptr;
@@ -150,7 +160,9 @@ struct tg_direct {
     dfree(d_sn_rows); dfree(d_sn_parent); dfree(d_ea_ptr); dfree(d_ea_rel);
     dfree(d_asm_ptr); dfree(d_asm_blk); dfree(d_asm_row); dfree(d_asm_col);
     dfree(d_ch_ptr); dfree(d_ch_list); dfree(d_level_sn); dfree(d_l_off);
-    dfree(d_solve_sn); dfree(d_csolve_sn);
+    dfree(d_solve_sn); dfree(d_csolve_sn); dfree(d_gemv_tp);
+    dfree(d_gemv_poff);
+    if (d_part) cudaFree(d_part);
     dfree(d_u_off); dfree(d_v_off); dfree(d_lstore); dfree(d_pool);
     dfree(d_contrib); dfree(d_ypos); dfree(d_xpos); dfree(d_bc_row);
     dfree(d_bc_pos); dfree(d_bc_ptr); dfree(d_bc_blk);
@@ -201,11 +213,50 @@ static int build_solve_lists(tg_direct *d, int threshold) {
   d->solve_sn_h = a;
   d->csolve_sn_h = b;
   d->cluster_threshold = threshold;
+  d->layout_version++;
+  // the backward solve's L21^T x2 tiles of the cluster fronts, per level
+  std::vector<int> tp(b.size());
+  std::vector<int64_t> poff(b.size());
+  d->gemv_total_h.assign(d->csolve_ptr_h.size() - 1, 0);
+  size_t part = 0;
+  for (size_t L = 0; L + 1 < d->csolve_ptr_h.size(); L++) {
+    int tiles = 0;
+    int64_t off = 0;
+    for (int k = d->csolve_ptr_h[L]; k < d->csolve_ptr_h[L + 1]; k++) {
+      const int sn = b[k];
+      const int M = d->front_m_h[sn], C = d->front_c_h[sn];
+      const int nrc = (M - C + tg::kDirectGemvRows - 1) / tg::kDirectGemvRows;
+      tiles += ((C + 31) / 32) * nrc;
+      tp[k] = tiles;
+      poff[k] = off;
+      off += (int64_t)nrc * C;
+    }
+    d->gemv_total_h[L] = tiles;
+    part = std::max(part, (size_t)off);
+  }
   tg::dfree(d->d_solve_sn);
   tg::dfree(d->d_csolve_sn);
+  tg::dfree(d->d_gemv_tp);
+  tg::dfree(d->d_gemv_poff);
   d->d_solve_sn = d->d_csolve_sn = nullptr;
+  d->d_gemv_tp = nullptr;
+  d->d_gemv_poff = nullptr;
   int rc = upload(&d->d_solve_sn, d->solve_sn_h);
   if (!rc) rc = upload(&d->d_csolve_sn, d->csolve_sn_h);
+  if (!rc) rc = upload(&d->d_gemv_tp, tp);
+  if (!rc) rc = upload(&d->d_gemv_poff, poff);
+  if (!rc && part > d->part_entries) {
+    if (d->d_part) cudaFree(d->d_part);
+    d->d_part = nullptr;
+    d->part_entries = 0;
+    const size_t elem =
+        d->precision == TG_PREC_FP32 ? sizeof(float) : sizeof(double);
+    const cudaError_t e =
+        cudaMalloc(&d->d_part, part * (size_t)d->max_nr * elem);
+    if (e != cudaSuccess)
+      return cuda_check(e, "tg_direct: backward solve chunk sums");
+    d->part_entries = part;
+  }
   if (rc) return rc;
   const cudaError_t se =
       tg::direct_set_smem(d->plain_front, d->cluster_front, d->max_nr);
@@ -515,9 +566,13 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
       const cudaStream_t sp = level_fork(d, le > lb && ce > cb, s);
       tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
                                     d->solve_front_h[L], nr, ypos, xpos, sp);
-      tg::launch_direct_backward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
-                                            d->cluster_front, nr, ypos, xpos,
-                                            s);
+      tg::launch_direct_bwd_gemv<T>(v, d->d_csolve_sn + cb, d->d_gemv_tp + cb,
+                                    d->d_gemv_poff + cb, ce - cb,
+                                    d->gemv_total_h[L], nr, xpos,
+                                    (T *)d->d_part, s);
+      tg::launch_direct_backward_cluster<T>(
+          v, d->d_csolve_sn + cb, d->d_gemv_poff + cb, ce - cb,
+          d->cluster_front, nr, ypos, xpos, (const T *)d->d_part, s);
       level_join(d, sp, s);
     }
     tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, xx, nr, N,
@@ -528,6 +583,9 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
 
 namespace tg {
 
+long long direct_layout_version(const tg_direct *d) {
+  return d ? d->layout_version : 0;
+}
 tg_mat *direct_matrix(const tg_direct *d) { return d->A; }
 int direct_precision(const tg_direct *d) { return d->precision; }
 bool direct_is_factored(const tg_direct *d) { return d->factored; }

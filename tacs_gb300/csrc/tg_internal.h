@@ -373,10 +373,21 @@ template <class T>
 void launch_direct_forward_cluster(const DirectView &v, const int *sn,
                                    int count, int max_front, int nr, T *y,
                                    T *contrib, cudaStream_t s);
+// The fronts solved by clusters at one level of the backward solve: first
+// their L21^T x2 products in tiles over the whole GPU (total tiles,
+// tprefix / poff per front: cumulative tiles and the offset of its chunk
+// sums in part, in entries per right-hand side), then the clusters, which
+// add the chunk sums in order
+template <class T>
+void launch_direct_bwd_gemv(const DirectView &v, const int *sn,
+                            const int *tprefix, const int64_t *poff,
+                            int count, int total, int nr, const T *x,
+                            T *part, cudaStream_t s);
 template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
-                                    int count, int max_front, int nr,
-                                    const T *y, T *x, cudaStream_t s);
+                                    const int64_t *poff, int count,
+                                    int max_front, int nr, const T *y, T *x,
+                                    const T *part, cudaStream_t s);
 bool direct_cluster_solve_ok();
 // dynamic shared memory of a solve over fronts of `front` rows with nr
 // right-hand sides (one CTA per front, or one cluster per front)

@@ -209,8 +209,10 @@ int capture_cycle(tg_ksm *k, int mode, cudaGraphExec_t *out) {
 // Allocate buffers, the chunk list and the state for nrhs vectors, and
 // capture the cycle graphs.
 int ensure_layout(tg_ksm *k, int nrhs) {
-  if (k->nrhs == nrhs) return 0;
+  const long long pv = pc_layout_version(k->pc);
+  if (k->nrhs == nrhs && k->pc_version == pv) return 0;
   k->free_layout();
+  k->pc_version = pv;
   const int nseg = (int)k->seg_rows.size() - 1;
   const int nsys = nseg * nrhs;
   if (nsys > kMaxSystems)

@@ -240,6 +240,9 @@ struct tg_ksm {
   size_t n = 0;                 // rows x block size of A
   std::vector<int> seg_rows;    // nseg + 1 block-row offsets of the systems
   int nrhs = 0;                 // current multivector width (0: not laid out)
+  // the preconditioner's launch layout the graphs were captured with
+  // (pc_layout_version); a change makes the next solve capture again
+  long long pc_version = 0;
   size_t N = 0;                 // nrhs * n
   int nsys = 0;
   // multivector buffers
@@ -314,6 +317,11 @@ int pc_prepare_fp64(tg_pc *pc);
 // one
 int direct_enqueue_solve(tg_direct *d, int nrhs, const void *b, void *x,
                          bool f32, cudaStream_t s);
+// A count that changes whenever the solves of a factorisation are laid out
+// again (the autotuner's new launch lists), and of a pc's factorisations:
+// graphs captured over older lists must be captured again
+long long direct_layout_version(const tg_direct *d);
+long long pc_layout_version(const tg_pc *pc);
 // a factorisation's matrix, precision and factored state, and one more
 // reference to it (tg_pc_create_direct; tg_direct.cu)
 tg_mat *direct_matrix(const tg_direct *d);

@@ -1379,6 +1379,14 @@ int pc_prepare_fp64(tg_pc *pc) {
   return tg_direct_create(pc->A, 1, TG_PREC_FP64, &pc->direct64);
 }
 
+long long pc_layout_version(const tg_pc *pc) {
+  if (!pc || pc->type != TG_PC_DIRECT) return 0;
+  // the two factorisations' counts, combined so that either one changing
+  // changes the sum's pair
+  return direct_layout_version(pc->direct) * 1000003LL +
+         direct_layout_version(pc->direct64);
+}
+
 int pc_factor_fp64(tg_pc *pc, cudaStream_t s) {
   if (pc->precision == TG_PREC_FP64 || pc->fp64_ready) return 0;
   if (pc->type == TG_PC_DIRECT) {

@@ -22,7 +22,7 @@ static EmuDim3 threadIdx{0, 0, 0}, blockIdx{0, 0, 0}, blockDim{1, 1, 1},
 #define __host__
 #define __forceinline__ inline
 #define __shared__ static
-#define __launch_bounds__(n)
+#define __launch_bounds__(...)
 #define __syncthreads() ((void)0)
 #define __syncwarp() ((void)0)
 static std::vector<double> g_dyn;
