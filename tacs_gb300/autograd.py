@@ -104,8 +104,7 @@ class StaticSolver:
         factorisation one load case at a time (exact, 0 iterations)."""
         if self.direct is None:
             return self.ksm.solve_multi(B)
-        X = self.direct.solve(B.contiguous(), rtol=self.rtol,
-                              ftol=self.rtol if self.mixed_direct else 0.0)
+        X = self.direct.solve(B.contiguous(), rtol=self.rtol)
         nsys = B.shape[0] * (self.model.nseg if self.segments else 1)
         return (X, np.zeros(nsys, np.int32), np.ones(nsys, np.int32),
                 np.zeros(nsys), 1)

@@ -48,6 +48,13 @@ __device__ __forceinline__ T dk_sqrt(T x) { return sqrt(x); }
 #endif
 
 
+// W consecutive entries of T loaded or stored as one vector access (the
+// address must be W entries aligned)
+template <class T, int W>
+struct alignas(sizeof(T) * W) DkVec {
+  T v[W];
+};
+
 // T = double for the FP64 factorisation, float for the FP32 one (whose
 // storage is lstore32 / pool32)
 template <class T>
@@ -367,10 +374,12 @@ __global__ void __launch_bounds__(256)
 // one, where shared-memory loads per FMA set the pace).  One CTA per
 // lower-triangular tile of all the step's fronts: CTA b belongs to the
 // last front f with tprefix[f] <= b (fronts without tiles are skipped that
-// way) and is its tile tau = b - tprefix[f] = ti (ti + 1) / 2 + tj.  Thread
-// (ty, tx) = (t / 16, t % 16) owns the R x R entries (ty + 16 a, tx + 16 b)
-// of the tile (R = TILE / 16): one pass over q loads 2 R operands for R^2
-// products, and each entry keeps its own summation order over q (the
+// way) and is its tile tau = b - tprefix[f] = ti (ti + 1) / 2 + tj.  The
+// two operand tiles are staged transposed (Ai[q][r] = F(i0 + r, k0 + q)),
+// so that thread (ty, tx) = (t / 16, t % 16), owning the R x R entries
+// (ty R + a, tx R + c) of the tile (R = TILE / 16), reads its R row
+// operands and R column operands of one q as two R-wide vectors: 2 loads
+// for R^2 products.  Each entry keeps its own summation order over q (the
 // result does not depend on TILE).
 template <class T, int TILE>
 __global__ void __launch_bounds__(256)
@@ -378,6 +387,7 @@ __global__ void __launch_bounds__(256)
                            const int *__restrict__ tprefix, int count,
                            int k0) {
   constexpr int R = TILE / 16;
+  constexpr int LD = TILE + 16 / (int)sizeof(T);  // 16-byte rows, padded
   const int b = blockIdx.x;
   int lo = 0, hi = count - 1;
   while (lo < hi) {
@@ -395,11 +405,12 @@ __global__ void __launch_bounds__(256)
   const int k1 = k0 + nb;
   const int i0 = k1 + ti * TILE, j0 = k1 + tj * TILE;
   if (i0 >= f.M || j0 >= f.M) return;
-  __shared__ T Ai[TILE][kPanel + 1], Aj[TILE][kPanel + 1];
+  alignas(16) __shared__ T Ai[kPanel][LD];
+  alignas(16) __shared__ T Aj[kPanel][LD];
   for (int t = threadIdx.x; t < TILE * nb; t += blockDim.x) {
     const int r = t / nb, q = t % nb;
-    Ai[r][q] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : T(0);
-    Aj[r][q] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : T(0);
+    Ai[q][r] = i0 + r < f.M ? f.at(i0 + r, k0 + q) : T(0);
+    Aj[q][r] = j0 + r < f.M ? f.at(j0 + r, k0 + q) : T(0);
   }
   __syncthreads();
   for (int g = threadIdx.x; g < 256; g += blockDim.x) {
@@ -410,11 +421,27 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int c = 0; c < R; c++) acc[a][c] = 0;
     for (int q = 0; q < nb; q++) {
+#ifdef DK_EMULATE
+      T x[R], y[R];
+      for (int a = 0; a < R; a++) x[a] = Ai[q][ty * R + a];
+      for (int c = 0; c < R; c++) y[c] = Aj[q][tx * R + c];
+#else
+      // 16-byte vectors (R entries, or R / VW vectors of VW)
+      constexpr int VW = R * sizeof(T) <= 16 ? R : 16 / (int)sizeof(T);
       T x[R], y[R];
 #pragma unroll
-      for (int a = 0; a < R; a++) x[a] = Ai[ty + 16 * a][q];
+      for (int h = 0; h < R; h += VW) {
+        const DkVec<T, VW> xv =
+            *reinterpret_cast<const DkVec<T, VW> *>(&Ai[q][ty * R + h]);
+        const DkVec<T, VW> yv =
+            *reinterpret_cast<const DkVec<T, VW> *>(&Aj[q][tx * R + h]);
 #pragma unroll
-      for (int c = 0; c < R; c++) y[c] = Aj[tx + 16 * c][q];
+        for (int w = 0; w < VW; w++) {
+          x[h + w] = xv.v[w];
+          y[h + w] = yv.v[w];
+        }
+      }
+#endif
 #pragma unroll
       for (int a = 0; a < R; a++)
 #pragma unroll
@@ -422,11 +449,11 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int a = 0; a < R; a++) {
-      const int i = i0 + ty + 16 * a;
+      const int i = i0 + ty * R + a;
       if (i >= f.M) continue;
 #pragma unroll
       for (int c = 0; c < R; c++) {
-        const int j = j0 + tx + 16 * c;
+        const int j = j0 + tx * R + c;
         if (j <= i) f.at(i, j) -= acc[a][c];
       }
     }
@@ -618,10 +645,6 @@ __device__ __forceinline__ void dk_warp_rows(const T *L0, size_t ldl, int nb,
 // order, with loads W entries wide (DkVec): a panel row of C entries starts
 // on a W-entry boundary when the panel does and C is a multiple of W (kb
 // is a multiple of 32), which dk_vec_width checks per front.
-template <class T, int W>
-struct alignas(sizeof(T) * W) DkVec {
-  T v[W];
-};
 template <class T>
 __device__ __forceinline__ int dk_vec_width(const T *lp, int C) {
   const unsigned long long a = (unsigned long long)lp;

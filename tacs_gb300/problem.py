@@ -614,7 +614,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
     direct, both solves use the complete factorisation (Direct) instead,
     refined to the relative residual rtol (or the FP64 floor) like the
     Krylov solves; direct="mixed" factors in FP32 and refines every solve in
-    FP64, also until a step's correction is at most rtol |x|.  `iters`
+    FP64 to the same relative residual.  `iters`
     then counts refinement steps."""
     dev = torch.device("cuda")
     u0 = model.vec()
@@ -631,8 +631,7 @@ def static_adjoint(model, force, m=100, nrestart=2, rtol=1e-12, atol=1e-30,
             iters = 0
 
             def solve(self, b):
-                x = dsol.solve(b, rtol=rtol,
-                               ftol=rtol if direct == "mixed" else 0.0)
+                x = dsol.solve(b, rtol=rtol)
                 self.iters = dsol.last_steps
                 return x, 1
         ksm = _Exact()
@@ -710,10 +709,8 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
 
         def solve_multi(B):
             # both precisions to the relative residual rtol of the
-            # iterative path; mixed refinement also until a step's
-            # correction is at most rtol |x|
-            X = dsol.solve(B.contiguous(), rtol=rtol,
-                           ftol=rtol if direct == "mixed" else 0.0)
+            # iterative path (the FP32 factorisation by FP64 refinement)
+            X = dsol.solve(B.contiguous(), rtol=rtol)
             z = np.zeros(nsys, np.int32)
             return X, z, np.ones(nsys, np.int32), np.zeros(nsys), 1
     else:
