@@ -465,6 +465,9 @@ def cylinder_section(torch, nc=384, nz=256):
     out["mixed_direct_speedup_vs_fp64_direct"] = (
         out["fp64_direct"]["s_per_gradient"]
         / out["mixed_direct"]["s_per_gradient"])
+    a, b = g["mixed_direct"], g["fp64_direct"]
+    out["mixed_direct"]["grad_rel_err_vs_fp64_direct"] = float(
+        np.abs(a[0] - b[0]).max() / np.abs(b[0]).max())
     del M
     torch.cuda.empty_cache()
     return out

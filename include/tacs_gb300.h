@@ -337,6 +337,15 @@ int tg_add_sv_sens_segments(tg_assembler *a, const double *vars, int func,
 int tg_add_total_derivative_segments(tg_assembler *a, const double *vars,
                                      int func, double coef, const double *psi,
                                      double scale, double *dfdx, void *stream);
+/* No reference counterpart.  The per-range KS statistics that the last
+   tg_eval_functions_segments kept (3 doubles per range: the maximum, the
+   sum of exp(weight (f - max)) and the weight), copied to / from the
+   device buffer ks (3 nseg doubles), so that the sensitivities of several
+   state vectors can be formed after all of them were evaluated: save
+   after each evaluation, restore before that state's sensitivity calls.
+   Asynchronous on the stream. */
+int tg_segment_ks_save(tg_assembler *a, double *ks, void *stream);
+int tg_segment_ks_restore(tg_assembler *a, const double *ks, void *stream);
 
 /* --------------------------------------------------------------- vectors */
 /* TACSBVec::axpy / scale / dot (src/bpmat/TACSBVec.cpp:215-408) on device

@@ -100,6 +100,8 @@ SIGNATURES = [
     ("tg_add_sv_sens_segments", _I, [_P, _P, _I, _D, _P, _P]),
     ("tg_add_total_derivative_segments", _I, [_P, _P, _I, _D, _P, _D, _P,
                                               _P]),
+    ("tg_segment_ks_save", _I, [_P, _P, _P]),
+    ("tg_segment_ks_restore", _I, [_P, _P, _P]),
     ("tg_ksm_solve_multi", _I, [_P, _I, _P, _P, _I, _P, _P, _P, _P]),
     ("tg_ksm_get_graph_info", _I, [_P, _IP, _IP, _IP]),
     ("tg_eval_functions_noalloc", _I, [_I, _I, _P, _P, _P, _D, _D, _D, _I,

@@ -806,6 +806,30 @@ int tg_eval_functions_segments(tg_assembler *a, const double *vars, int func,
   return 0;
 }
 
+int tg_segment_ks_save(tg_assembler *a, double *ks, void *s) {
+  int rc = check_ready(a, "tg_segment_ks_save");
+  if (rc) return rc;
+  if (!ks || a->nseg <= 0)
+    return fail(TG_ERR_ARG, "tg_segment_ks_save: bad arguments");
+  if (!a->seg_ks_valid)
+    return fail(TG_ERR_STATE, "evaluate the segment KS functions first");
+  static_assert(sizeof(KsStats) == 3 * sizeof(double), "KsStats layout");
+  TG_CUDA(cudaMemcpyAsync(ks, a->d_seg_ks, a->nseg * sizeof(KsStats),
+                          cudaMemcpyDeviceToDevice, S(s)));
+  return 0;
+}
+
+int tg_segment_ks_restore(tg_assembler *a, const double *ks, void *s) {
+  int rc = check_ready(a, "tg_segment_ks_restore");
+  if (rc) return rc;
+  if (!ks || a->nseg <= 0)
+    return fail(TG_ERR_ARG, "tg_segment_ks_restore: bad arguments");
+  TG_CUDA(cudaMemcpyAsync(a->d_seg_ks, ks, a->nseg * sizeof(KsStats),
+                          cudaMemcpyDeviceToDevice, S(s)));
+  a->seg_ks_valid = true;
+  return 0;
+}
+
 int tg_add_sv_sens_segments(tg_assembler *a, const double *vars, int func,
                             double alpha, double *dfdu, void *s) {
   int rc = check_ready(a, "tg_add_sv_sens_segments");

@@ -597,6 +597,22 @@ class GpuModel:
             self.handle, _p(u), int(func), alpha, _p(dfdu), _stream()),
             "tg_add_sv_sens_segments")
 
+    def segment_ks_save(self, ks=None):
+        """The per-range KS statistics of the last
+        eval_functions_segments (3 per range), into a device tensor."""
+        ks = torch.empty(3 * self.nseg, dtype=torch.float64,
+                         device="cuda") if ks is None else ks
+        check(_lib.lib().tg_segment_ks_save(self.handle, _p(ks), _stream()),
+              "tg_segment_ks_save")
+        return ks
+
+    def segment_ks_restore(self, ks):
+        """Make saved per-range KS statistics current again, for the
+        sensitivities of the state they were evaluated at."""
+        check(_lib.lib().tg_segment_ks_restore(self.handle, _p(ks),
+                                               _stream()),
+              "tg_segment_ks_restore")
+
     def add_total_derivative_segments(self, u, func, psi, dfdx, coef=1.0,
                                       scale=-1.0):
         check(_lib.lib().tg_add_total_derivative_segments(
@@ -728,14 +744,18 @@ def batched_adjoint(model, loads, m=100, nrestart=50, rtol=1e-10, atol=1e-30,
     U, it_f, fl_f, rn_f, _ = solve_multi(F)
     fvals = np.zeros((nlc, model.nseg))
     dfdu = torch.zeros_like(U)
+    # each load case's KS statistics, kept for its total derivative after
+    # the adjoint solve (instead of evaluating the functions again)
+    ks = torch.empty(nlc, 3 * model.nseg, dtype=torch.float64, device="cuda")
     for lc in range(nlc):
         fvals[lc] = model.eval_functions_segments(U[lc], func)
+        model.segment_ks_save(ks[lc])
         model.add_sv_sens_segments(U[lc], func, dfdu[lc])
         model.apply_bcs(dfdu[lc])
     Psi, it_a, fl_a, rn_a, _ = solve_multi(dfdu)
     grads = torch.zeros(nlc, model.ndv, dtype=torch.float64, device="cuda")
     for lc in range(nlc):
-        model.eval_functions_segments(U[lc], func)
+        model.segment_ks_restore(ks[lc])
         model.add_total_derivative_segments(U[lc], func, Psi[lc], grads[lc],
                                             1.0, -1.0)
     return dict(u=U, funcs=fvals, grads=grads, iters_fwd=it_f, flags_fwd=fl_f,

@@ -158,3 +158,33 @@ def test_restart_cycle_runs_as_one_graph():
         r = mat.mult(x) - b
         assert float(r.norm() / b.norm()) < 1e-9
 
+
+
+def test_segment_ks_save_restore(gpu):
+    """The per-range KS statistics saved after one state's evaluation and
+    restored after another's give that state's total derivative bitwise
+    (tg_segment_ks_save / tg_segment_ks_restore); restoring without a
+    saved buffer of the right kind is refused before any evaluation."""
+    from tacs_gb300 import _lib, meshes
+    bp = meshes.batch_plates(count=3, seed=4, nmin=8, nmax=12)
+    M = gpu.GpuModel(bp)
+    M.set_segments(bp["seg_elem_ptr"])
+    g = torch.Generator(device="cuda").manual_seed(11)
+    U = 1e-4 * torch.randn(2, M.ndof, dtype=torch.float64, device="cuda",
+                           generator=g)
+    psi = torch.randn(M.ndof, dtype=torch.float64, device="cuda",
+                      generator=g)
+    f = _lib.FUNC_KS_FAILURE
+    M.eval_functions_segments(U[0], f)
+    ks0 = M.segment_ks_save()
+    ref = M.dv_vec()
+    M.add_total_derivative_segments(U[0], f, psi, ref, 1.0, -1.0)
+    M.eval_functions_segments(U[1], f)  # another state's statistics
+    M.segment_ks_restore(ks0)
+    got = M.dv_vec()
+    M.add_total_derivative_segments(U[0], f, psi, got, 1.0, -1.0)
+    assert torch.equal(got, ref)
+    M2 = gpu.GpuModel(bp)
+    M2.set_segments(bp["seg_elem_ptr"])
+    with pytest.raises(_lib.TacsGpuError):
+        M2.segment_ks_save()
