@@ -109,9 +109,11 @@ struct tg_direct {
   int *d_fail = nullptr;
   bool factored = false;
   // a level's one-CTA and cluster solves touch different fronts: the
-  // one-CTA launch runs on side_stream beside the cluster launch (forked
+  // cluster launch runs on side_stream beside the one-CTA launch (forked
   // and joined through the two events), so a level costs the longer of
-  // the two rather than their sum
+  // the two rather than their sum.  The side stream has the device's
+  // highest priority, so that a cluster's CTAs, which must find room on
+  // one GPC together, are placed before the one-CTA fronts take the SMs.
   cudaStream_t side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   tg::DirectBc bc() const {
@@ -280,8 +282,11 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   d->A = A;
   A->refcount++;
   {
-    cudaError_t e =
-        cudaStreamCreateWithFlags(&d->side_stream, cudaStreamNonBlocking);
+    int lo_prio = 0, hi_prio = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (e == cudaSuccess)
+      e = cudaStreamCreateWithPriority(&d->side_stream, cudaStreamNonBlocking,
+                                       hi_prio);
     if (e == cudaSuccess)
       e = cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess)
@@ -516,8 +521,8 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
 // at most max_nr of them, b' = b - K P b + P b, into the factor's order
 // (interleaved), the level sweeps, back to the node order (K a: the
 // matrix values in T)
-// The stream of a level's one-CTA solves: the side stream, forked from s
-// after the levels before, when the level also has cluster solves (which
+// The stream of a level's cluster solves: the side stream, forked from s
+// after the levels before, when the level also has one-CTA solves (which
 // stay on s); else s itself.  level_join puts s behind the side stream's
 // launches.  Inside a stream capture the fork and join become graph edges.
 static cudaStream_t level_fork(tg_direct *d, bool both, cudaStream_t s) {
@@ -551,29 +556,28 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
     for (int L = 0; L < nl; L++) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
-      const cudaStream_t sp = level_fork(d, le > lb && ce > cb, s);
-      tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
-                                   d->solve_front_h[L], nr, ypos, contrib,
-                                   sp);
+      const cudaStream_t sc = level_fork(d, le > lb && ce > cb, s);
       tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
                                            d->cluster_front, nr, ypos,
-                                           contrib, s);
-      level_join(d, sp, s);
+                                           contrib, sc);
+      tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
+                                   d->solve_front_h[L], nr, ypos, contrib, s);
+      level_join(d, sc, s);
     }
     for (int L = nl - 1; L >= 0; L--) {
       const int lb = d->solve_ptr_h[L], le = d->solve_ptr_h[L + 1];
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
-      const cudaStream_t sp = level_fork(d, le > lb && ce > cb, s);
-      tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
-                                    d->solve_front_h[L], nr, ypos, xpos, sp);
+      const cudaStream_t sc = level_fork(d, le > lb && ce > cb, s);
       tg::launch_direct_bwd_gemv<T>(v, d->d_csolve_sn + cb, d->d_gemv_tp + cb,
                                     d->d_gemv_poff + cb, ce - cb,
                                     d->gemv_total_h[L], nr, xpos,
-                                    (T *)d->d_part, s);
+                                    (T *)d->d_part, sc);
       tg::launch_direct_backward_cluster<T>(
           v, d->d_csolve_sn + cb, d->d_gemv_poff + cb, ce - cb,
-          d->cluster_front, nr, ypos, xpos, (const T *)d->d_part, s);
-      level_join(d, sp, s);
+          d->cluster_front, nr, ypos, xpos, (const T *)d->d_part, sc);
+      tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
+                                    d->solve_front_h[L], nr, ypos, xpos, s);
+      level_join(d, sc, s);
     }
     tg::launch_direct_unpermute<T>(d->n, d->bs, d->d_perm, xpos, xx, nr, N,
                                    s);
