@@ -656,6 +656,21 @@ __device__ __forceinline__ int dk_vec_width(const T *lp, int C) {
 template <class T, int NR, int W>
 __device__ __forceinline__ void dk_row_dot_w(const T *Li, int nb,
                                              const T *zk, T (&acc)[NR]) {
+  if (nb == 32) {  // a whole block: every load issued before the products
+    constexpr int NV = 32 / W;
+    DkVec<T, W> l[NV];
+#pragma unroll
+    for (int u = 0; u < NV; u++)
+      l[u] = *reinterpret_cast<const DkVec<T, W> *>(Li + u * W);
+#pragma unroll
+    for (int u = 0; u < NV; u++)
+#pragma unroll
+      for (int w = 0; w < W; w++)
+#pragma unroll
+        for (int q = 0; q < NR; q++)
+          acc[q] += l[u].v[w] * zk[(u * W + w) * NR + q];
+    return;
+  }
   int c = 0;
   for (; c + W <= nb; c += W) {
     const DkVec<T, W> l = *reinterpret_cast<const DkVec<T, W> *>(Li + c);
@@ -727,8 +742,19 @@ __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
 // Per column block: the block solve (with the kept inverse when the
 // front was factored by panels, else by substitution), then the rows below
 // it.  kDirectPlainThreads threads.
+// CTAs per SM the one-CTA forward solve is compiled for (the register
+// budget of its row loads in flight against the fronts resident per SM),
+// per scalar type and right-hand-side count, as measured on the 48-plate
+// batch: FP32 8 (one right-hand side) or 6, FP64 4 (one) or 8
 template <class T, int NR>
-__global__ void __launch_bounds__(kDirectPlainThreads)
+struct DkForwardBlocks {
+  static constexpr int value =
+      sizeof(T) == 4 ? (NR == 1 ? 8 : 6) : (NR == 1 ? 4 : 8);
+};
+
+template <class T, int NR>
+__global__ void __launch_bounds__(kDirectPlainThreads,
+                                  DkForwardBlocks<T, NR>::value)
     direct_forward_kernel(DirectView v, const int *__restrict__ sn, int count,
                           T *y, T *contrib) {
   if ((int)blockIdx.x >= count) return;
@@ -887,14 +913,30 @@ __global__ void __launch_bounds__(kDirectPlainThreads, 6)
     }
     __syncthreads();
     // columns before the block: z_j -= sum_k L(kb + k, j) z(kb + k)
+    // (a whole block's 32 loads issued 16 at a time, before their products)
     for (int j = threadIdx.x; j < kb; j += blockDim.x) {
       T acc[NR];
 #pragma unroll
       for (int r = 0; r < NR; r++) acc[r] = 0;
-      for (int k = 0; k < nb; k++) {
-        const T l = f.lp[(size_t)(kb + k) * f.C + j];
+      if (nb == 32) {
 #pragma unroll
-        for (int r = 0; r < NR; r++) acc[r] += l * z[(kb + k) * NR + r];
+        for (int h = 0; h < 32; h += 16) {
+          T l[16];
+#pragma unroll
+          for (int k = 0; k < 16; k++)
+            l[k] = f.lp[(size_t)(kb + h + k) * f.C + j];
+#pragma unroll
+          for (int k = 0; k < 16; k++)
+#pragma unroll
+            for (int r = 0; r < NR; r++)
+              acc[r] += l[k] * z[(kb + h + k) * NR + r];
+        }
+      } else {
+        for (int k = 0; k < nb; k++) {
+          const T l = f.lp[(size_t)(kb + k) * f.C + j];
+#pragma unroll
+          for (int r = 0; r < NR; r++) acc[r] += l * z[(kb + k) * NR + r];
+        }
       }
 #pragma unroll
       for (int r = 0; r < NR; r++) z[j * NR + r] -= acc[r];
