@@ -198,6 +198,60 @@ __global__ void reduce_partial_kernel(const double *x, const double *w,
   }
   if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
 }
+// max |x| of k vectors n apart (blockIdx.y = vector), in the fixed
+// partition of reduce_partial_kernel; the final pass writes vector v's
+// maximum to out[v * stride]
+__global__ void absmax_multi_partial_kernel(const double *x, size_t n,
+                                            double *partials) {
+  __shared__ double sh[256];
+  const double *xv = x + (size_t)blockIdx.y * n;
+  size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  size_t b = chunk * blockIdx.x, e = b + chunk < n ? b + chunk : n;
+  double acc = 0.0;
+  for (size_t i = b + threadIdx.x; i < e; i += blockDim.x)
+    acc = fabs(xv[i]) > acc ? fabs(xv[i]) : acc;
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
+                            ? sh[threadIdx.x + s]
+                            : sh[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+__global__ void absmax_multi_final_kernel(const double *partials, int npart,
+                                          double *out, int stride) {
+  __shared__ double sh[256];
+  const double *p = partials + (size_t)blockIdx.x * npart;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < npart; i += blockDim.x)
+    acc = p[i] > acc ? p[i] : acc;
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      sh[threadIdx.x] = sh[threadIdx.x + s] > sh[threadIdx.x]
+                            ? sh[threadIdx.x + s]
+                            : sh[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[(size_t)blockIdx.x * stride] = sh[0];
+}
+// r = b - t
+__global__ void residual_kernel(const double *b, const double *t, double *r,
+                                size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - t[i];
+}
+// x += c (c in FP32)
+__global__ void f2d_add_kernel(const float *c, double *x, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    x[i] += (double)c[i];
+}
 // sum over each scalar row of |A| (for the infinity norm of A)
 __global__ void bcsr_row_abs_sum_kernel(int bs, int nrows,
                                         const int *__restrict__ rowp,
@@ -924,6 +978,22 @@ void launch_reduce_absmax(const double *x, size_t n, double *partials,
   reduce_partial_kernel<3><<<npart, 256, 0, s>>>(x, nullptr, n, nullptr, 0.0,
                                                  partials);
   reduce_final_kernel<1><<<1, 256, 0, s>>>(partials, npart, out);
+}
+void launch_reduce_absmax_multi(const double *x, int k, size_t n,
+                                double *partials, int npart, double *out,
+                                int stride, cudaStream_t s) {
+  if (k <= 0) return;
+  absmax_multi_partial_kernel<<<dim3(npart, k), 256, 0, s>>>(x, n, partials);
+  absmax_multi_final_kernel<<<k, 256, 0, s>>>(partials, npart, out, stride);
+}
+void launch_residual(const double *b, const double *t, double *r, size_t n,
+                     cudaStream_t s) {
+  if (!n) return;
+  residual_kernel<<<blocks_for(n, 256), 256, 0, s>>>(b, t, r, n);
+}
+void launch_f2d_add(const float *c, double *x, size_t n, cudaStream_t s) {
+  if (!n) return;
+  f2d_add_kernel<<<blocks_for(n, 256), 256, 0, s>>>(c, x, n);
 }
 void launch_bcsr_row_abs_sum(int bsize, int nrows, const int *rowp,
                              const double *vals, double *out, cudaStream_t s) {

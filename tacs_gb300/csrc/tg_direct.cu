@@ -116,6 +116,10 @@ struct tg_direct {
   // one GPC together, are placed before the one-CTA fronts take the SMs.
   cudaStream_t side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the factorisation's launch sequence (every level's assembly, panel
+  // steps and the inverses; fixed by the analysis) as one CUDA graph,
+  // captured at the first factorisation and replayed after
+  cudaGraphExec_t factor_exec = nullptr;
   tg::DirectBc bc() const {
     tg::DirectBc c;
     c.nrow = bc_nrow;
@@ -175,6 +179,7 @@ struct tg_direct {
     dfree(d_c32); dfree(d_r); dfree(d_t); dfree(d_red); dfree(d_scal);
     dfree(d_dinv_off); dfree(d_dinv); dfree(d_dinv32);
     dfree(d_inv_sn); dfree(d_inv_k0);
+    if (factor_exec) cudaGraphExecDestroy(factor_exec);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (side_stream) cudaStreamDestroy(side_stream);
@@ -466,7 +471,7 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   // reductions and their scalars (3 per right-hand side)
   if (!rc) rc = dalloc(&d->d_r, N * R);
   if (!rc) rc = dalloc(&d->d_t, N * R);
-  if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts);
+  if (!rc) rc = dalloc(&d->d_red, (size_t)kRedParts * R);
   if (!rc) rc = dalloc(&d->d_scal, 3 * R + 2);
   if (!rc) rc = dalloc(&d->d_fail, 1);
   if (!rc && tg::direct_solve_smem(pf_max, 1, sizeof(double)) > kSmemMax)
@@ -517,10 +522,6 @@ static void factor_levels(tg_direct *d, cudaStream_t s) {
                                 s);
 }
 
-// X = A^-1 B in T for nrhs right-hand sides N = n bs apart: per pass of
-// at most max_nr of them, b' = b - K P b + P b, into the factor's order
-// (interleaved), the level sweeps, back to the node order (K a: the
-// matrix values in T)
 // The stream of a level's cluster solves: the side stream, forked from s
 // after the levels before, when the level also has one-CTA solves (which
 // stay on s); else s itself.  level_join puts s behind the side stream's
@@ -537,6 +538,10 @@ static void level_join(tg_direct *d, cudaStream_t sp, cudaStream_t s) {
   cudaStreamWaitEvent(s, d->ev_join, 0);
 }
 
+// X = A^-1 B in T for nrhs right-hand sides N = n bs apart: per pass of
+// at most max_nr of them, b into the factor's order (interleaved) less
+// its coupling to the constrained dofs (a: the matrix values in T), the
+// level sweeps, back to the node order
 template <class T>
 static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
                          const T *a, T *ypos, T *xpos, T *contrib,
@@ -630,9 +635,8 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
   double bnorm[4], prev[4], eta[4];
   int slow[4], taken[4];
   bool met[4], done[4];
-  for (int r = 0; r < nr; r++)
-    tg::launch_reduce_absmax(b + r * N, N, d->d_red, kRedParts, d->d_scal + r,
-                             s);
+  tg::launch_reduce_absmax_multi(b, nr, N, d->d_red, kRedParts, d->d_scal, 1,
+                                 s);
   TG_CUDA(cudaMemcpyAsync(h, d->d_scal, nr * sizeof(double),
                           cudaMemcpyDeviceToHost, s));
   TG_CUDA(cudaStreamSynchronize(s));
@@ -654,7 +658,8 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
           TG_CUDA(cudaMemsetAsync(d->d_r32 + r * N, 0, N * sizeof(float), s));
       solve_levels<float>(d, nr, d->d_r32, d->d_c32, d->d_a32, d->d_ypos32,
                           d->d_xpos32, d->d_contrib32, s);
-      tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
+      if (ftol > 0.0)  // the correction itself is tested below
+        tg::launch_f2d(d->d_c32, d->d_t, N * nr, s);
     } else {
       for (int r = 0; r < nr; r++)
         if (done[r])
@@ -663,20 +668,20 @@ static int refine_pass(tg_direct *d, int nr, const double *b, double *x,
                            d->d_xpos, d->d_contrib, s);
     }
     if (ftol > 0.0)  // the step's correction, max |dx|
-      for (int r = 0; r < nr; r++)
-        tg::launch_reduce_absmax(d->d_t + r * N, N, d->d_red, kRedParts,
-                                 d->d_scal + 3 * r + 2, s);
-    tg::launch_axpy(1.0, d->d_t, x, N * nr, s);
+      tg::launch_reduce_absmax_multi(d->d_t, nr, N, d->d_red, kRedParts,
+                                     d->d_scal + 2, 3, s);
+    if (f32 && ftol <= 0.0)
+      tg::launch_f2d_add(d->d_c32, x, N * nr, s);
+    else
+      tg::launch_axpy(1.0, d->d_t, x, N * nr, s);
+    // r = b - A x, then max |r| and max |x| per right-hand side
     tg::launch_bcsr_mult(A->bsize, A->nrows, A->a->d_rowp, A->a->d_cols,
                          A->d_vals, x, d->d_t, s, nr, N);
-    tg::launch_copy(b, d->d_r, N * nr, s);
-    tg::launch_axpy(-1.0, d->d_t, d->d_r, N * nr, s);
-    for (int r = 0; r < nr; r++) {
-      tg::launch_reduce_absmax(d->d_r + r * N, N, d->d_red, kRedParts,
-                               d->d_scal + 3 * r, s);
-      tg::launch_reduce_absmax(x + r * N, N, d->d_red, kRedParts,
-                               d->d_scal + 3 * r + 1, s);
-    }
+    tg::launch_residual(b, d->d_t, d->d_r, N * nr, s);
+    tg::launch_reduce_absmax_multi(d->d_r, nr, N, d->d_red, kRedParts,
+                                   d->d_scal, 3, s);
+    tg::launch_reduce_absmax_multi(x, nr, N, d->d_red, kRedParts,
+                                   d->d_scal + 1, 3, s);
     TG_CUDA(cudaMemcpyAsync(h, d->d_scal, 3 * nr * sizeof(double),
                             cudaMemcpyDeviceToHost, s));
     TG_CUDA(cudaStreamSynchronize(s));
@@ -730,14 +735,31 @@ extern "C" {
 int tg_direct_factor(tg_direct *d, void *s) {
   if (!d) return fail(TG_ERR_ARG, "tg_direct_factor: NULL");
   TG_CUDA(cudaMemsetAsync(d->d_fail, 0, sizeof(int), S(s)));
-  if (d->precision == TG_PREC_FP64) {
-    factor_levels<double>(d, S(s));
-  } else {
-    const tg_mat *A = d->A;
-    tg::launch_d2f(A->d_vals, d->d_a32,
-                   (size_t)A->nnz * A->bsize * A->bsize, S(s));
-    factor_levels<float>(d, S(s));
+  if (!d->factor_exec) {
+    // captured on the side stream (the caller's may be the legacy default
+    // stream, which cannot be captured), launched on the caller's
+    cudaStream_t cs = d->side_stream;
+    TG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (d->precision == TG_PREC_FP64) {
+      factor_levels<double>(d, cs);
+    } else {
+      const tg_mat *A = d->A;
+      tg::launch_d2f(A->d_vals, d->d_a32,
+                     (size_t)A->nnz * A->bsize * A->bsize, cs);
+      factor_levels<float>(d, cs);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cs, &g);
+    cudaError_t ie = ce;
+    if (ce == cudaSuccess)
+      ie = cudaGraphInstantiate(&d->factor_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      d->factor_exec = nullptr;
+      return cuda_check(ie, "tg_direct_factor: factorisation graph");
+    }
   }
+  TG_CUDA(cudaGraphLaunch(d->factor_exec, S(s)));
   {  // ||A||_inf of these values, for the refinement's backward error
     const tg_mat *A = d->A;
     const size_t N = (size_t)d->n * d->bs;

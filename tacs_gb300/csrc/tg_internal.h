@@ -178,6 +178,14 @@ void launch_reduce_max(const double *x, size_t n, double *partials,
 void launch_reduce_sum(const double *x, size_t n, double *partials,
                        int npart, double *out, cudaStream_t s);
 // max |x_i|, and the scalar-row sums of |A| of a BCSR matrix
+// max |x| of k vectors n apart into out[v * stride] (partials: npart k)
+void launch_reduce_absmax_multi(const double *x, int k, size_t n,
+                                double *partials, int npart, double *out,
+                                int stride, cudaStream_t s);
+// r = b - t; x += c (c in FP32)
+void launch_residual(const double *b, const double *t, double *r, size_t n,
+                     cudaStream_t s);
+void launch_f2d_add(const float *c, double *x, size_t n, cudaStream_t s);
 void launch_reduce_absmax(const double *x, size_t n, double *partials,
                           int npart, double *out, cudaStream_t s);
 void launch_bcsr_row_abs_sum(int bsize, int nrows, const int *rowp,
