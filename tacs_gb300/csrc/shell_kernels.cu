@@ -401,11 +401,12 @@ __device__ __forceinline__ void geo_load_u(const MeshView &m, int e,
   }
 }
 
-// e = B_q v (9 strains; B_q row-major 9 x 24)
+// e = B_q v (the first R of the 9 strains; B_q row-major 9 x 24)
+template <int R = 9>
 __device__ __forceinline__ void geo_strains(const double *Bq,
                                             const double *v, double *e) {
 #pragma unroll 1
-  for (int r = 0; r < 9; r++) {
+  for (int r = 0; r < R; r++) {
     double acc = 0.0;
 #pragma unroll
     for (int k = 0; k < 24; k++) acc += Bq[r * 24 + k] * v[k];
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(kGeoWarps * 32)
       const double *tab = m.geo_B + (size_t)m.geo_cls[e] * 868;
       double u[24], ev[9];
       geo_load_u(m, e, vars, u);
-      geo_strains(tab + 216 * q, u, ev);
+      geo_strains<8>(tab + 216 * q, u, ev);  // the 9th is not used here
       ev[8] = 0.0;
       const double t = m.thick[e];
       const ShellStiff cs = shell_stiff(ep, t);
@@ -474,7 +475,7 @@ __global__ void __launch_bounds__(kGeoWarps * 32)
       const KsStats kk = m.elem_seg ? m.seg_ks[m.elem_seg[e]] : ks;
       double u[24], ev[9], g[9], coef;
       geo_load_u(m, e, vars, u);
-      geo_strains(Bq, u, ev);
+      geo_strains<8>(Bq, u, ev);  // the 9th is not used here
       ev[8] = 0.0;
       const double t = m.thick[e], det = tab[864 + q];
       if (func == TG_FUNC_COMPLIANCE) {
