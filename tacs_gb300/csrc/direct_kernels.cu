@@ -123,25 +123,26 @@ void launch_direct_backward(const DirectView &v, const int *sn, int count,
                     count, y, x);
 }
 
-// Large fronts: kDirectSolveCluster CTAs per front in one thread-block
-// cluster; shared memory for the rank owning the most rows.
-size_t direct_cluster_smem(int max_front, int nr, size_t elem) {
+// Large fronts: ncl CTAs per front in one thread-block cluster; shared
+// memory for the rank owning the most rows.
+size_t direct_cluster_smem(int max_front, int nr, size_t elem, int ncl) {
   const int nbk = (max_front + 31) / 32;
-  const int mine = (nbk + kDirectSolveCluster - 1) / kDirectSolveCluster;
+  const int mine = (nbk + ncl - 1) / ncl;
   return elem * ((size_t)mine * 32 * nr);
 }
 
 template <class K, class... Args>
-static cudaError_t cluster_launch_dk(K kernel, int count, size_t smem,
-                                     cudaStream_t s, Args... args) {
+static cudaError_t cluster_launch_dk(K kernel, int count, int ncl,
+                                     size_t smem, cudaStream_t s,
+                                     Args... args) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(count * kDirectSolveCluster));
+  cfg.gridDim = dim3((unsigned)(count * ncl));
   cfg.blockDim = dim3(kDirectClusterThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kDirectSolveCluster;
+  at[0].val.clusterDim.x = ncl;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
@@ -151,19 +152,19 @@ static cudaError_t cluster_launch_dk(K kernel, int count, size_t smem,
 
 template <class T>
 void launch_direct_forward_cluster(const DirectView &v, const int *sn,
-                                   int count, int max_front, int nr, T *y,
-                                   T *contrib, cudaStream_t s) {
+                                   int count, int max_front, int nr, int ncl,
+                                   T *y, T *contrib, cudaStream_t s) {
   if (count <= 0) return;
-  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T));
+  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T), ncl);
   if (nr == 4)
-    cluster_launch_dk(direct_forward_cluster_kernel<T, 4>, count, smem, s, v,
-                      sn, count, y, contrib);
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 4>, count, ncl, smem,
+                      s, v, sn, count, ncl, y, contrib);
   else if (nr == 2)
-    cluster_launch_dk(direct_forward_cluster_kernel<T, 2>, count, smem, s, v,
-                      sn, count, y, contrib);
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 2>, count, ncl, smem,
+                      s, v, sn, count, ncl, y, contrib);
   else
-    cluster_launch_dk(direct_forward_cluster_kernel<T, 1>, count, smem, s, v,
-                      sn, count, y, contrib);
+    cluster_launch_dk(direct_forward_cluster_kernel<T, 1>, count, ncl, smem,
+                      s, v, sn, count, ncl, y, contrib);
 }
 
 template <class T>
@@ -187,26 +188,36 @@ void launch_direct_bwd_gemv(const DirectView &v, const int *sn,
 template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
                                     const int64_t *poff, int count,
-                                    int max_front, int nr, const T *y, T *x,
-                                    const T *part, cudaStream_t s) {
+                                    int max_front, int nr, int ncl,
+                                    const T *y, T *x, const T *part,
+                                    cudaStream_t s) {
   if (count <= 0) return;
-  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T));
+  const size_t smem = direct_cluster_smem(max_front, nr, sizeof(T), ncl);
   if (nr == 4)
-    cluster_launch_dk(direct_backward_cluster_kernel<T, 4>, count, smem, s,
-                      v, sn, poff, count, y, x, part);
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 4>, count, ncl, smem,
+                      s, v, sn, poff, count, ncl, y, x, part);
   else if (nr == 2)
-    cluster_launch_dk(direct_backward_cluster_kernel<T, 2>, count, smem, s,
-                      v, sn, poff, count, y, x, part);
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 2>, count, ncl, smem,
+                      s, v, sn, poff, count, ncl, y, x, part);
   else
-    cluster_launch_dk(direct_backward_cluster_kernel<T, 1>, count, smem, s,
-                      v, sn, poff, count, y, x, part);
+    cluster_launch_dk(direct_backward_cluster_kernel<T, 1>, count, ncl, smem,
+                      s, v, sn, poff, count, ncl, y, x, part);
 }
 
-// whether the device schedules the solve clusters (at least one active),
-// asked with the dynamic shared memory of a 32 k-row front (the attribute
-// set first: with the kernel's static shared memory it passes 48 KB)
-bool direct_cluster_solve_ok() {
-  const size_t bytes = direct_cluster_smem(1 << 15, 1, sizeof(double));
+// whether the device schedules the solve clusters of ncl CTAs (at least
+// one active), asked with the dynamic shared memory of a 32 k-row front
+// (the attribute set first: with the kernel's static shared memory it
+// passes 48 KB; clusters above 8 CTAs also need the non-portable size
+// allowed, which set_solve_smem sets on every cluster kernel)
+bool direct_cluster_solve_ok(int ncl) {
+  const size_t bytes = direct_cluster_smem(1 << 15, 1, sizeof(double), ncl);
+  if (ncl > 8 &&
+      cudaFuncSetAttribute(
+          (const void *)direct_forward_cluster_kernel<double, 1>,
+          cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   if (cudaFuncSetAttribute(
           (const void *)direct_forward_cluster_kernel<double, 1>,
           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
@@ -215,12 +226,12 @@ bool direct_cluster_solve_ok() {
     return false;
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kDirectSolveCluster);
-  cfg.blockDim = dim3(256);
+  cfg.gridDim = dim3(ncl);
+  cfg.blockDim = dim3(kDirectClusterThreads);
   cfg.dynamicSmemBytes = bytes;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kDirectSolveCluster;
+  at[0].val.clusterDim.x = ncl;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
@@ -268,7 +279,8 @@ void launch_direct_unpermute(int n, int bs, const int *perm, const T *xpos,
 template <class T, int NR>
 static cudaError_t set_solve_smem(int plain_front, int cluster_front) {
   const size_t pb = direct_solve_smem(plain_front, NR, sizeof(T));
-  const size_t cb = direct_cluster_smem(cluster_front, NR, sizeof(T));
+  const size_t cb =
+      direct_cluster_smem(cluster_front, NR, sizeof(T), kDirectSolveCluster);
   const void *plain[2] = {(const void *)direct_forward_kernel<T, NR>,
                           (const void *)direct_backward_kernel<T, NR>};
   const void *clus[2] = {(const void *)direct_forward_cluster_kernel<T, NR>,
@@ -282,11 +294,18 @@ static cudaError_t set_solve_smem(int plain_front, int cluster_front) {
                                   (int)pb)) != cudaSuccess)
       return e;
   if (cluster_front > 0)
-    for (const void *k : clus)
+    for (const void *k : clus) {
       if ((e = cudaFuncSetAttribute(k,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)cb)) != cudaSuccess)
         return e;
+      // wide clusters, where the device schedules them (a failure here
+      // only leaves the levels on 8-CTA clusters)
+      if (cudaFuncSetAttribute(k,
+                               cudaFuncAttributeNonPortableClusterSizeAllowed,
+                               1) != cudaSuccess)
+        cudaGetLastError();
+    }
   return e;
 }
 
@@ -354,13 +373,13 @@ cudaError_t direct_set_smem(int plain_front, int cluster_front, int max_nr) {
                                           int, int, int, const T *, T *,   \
                                           cudaStream_t);                   \
   template void launch_direct_forward_cluster<T>(                          \
-      const DirectView &, const int *, int, int, int, T *, T *,            \
+      const DirectView &, const int *, int, int, int, int, T *, T *,       \
       cudaStream_t);                                                        \
   template void launch_direct_bwd_gemv<T>(                                 \
       const DirectView &, const int *, const int *, const int64_t *, int,  \
       int, int, const T *, T *, cudaStream_t);                              \
   template void launch_direct_backward_cluster<T>(                         \
-      const DirectView &, const int *, const int64_t *, int, int, int,     \
+      const DirectView &, const int *, const int64_t *, int, int, int, int,\
       const T *, T *, const T *, cudaStream_t);                             \
   template void launch_direct_rhs<T>(int, int, const int *, const T *,     \
                                      T *, int, size_t, cudaStream_t);      \

@@ -1021,9 +1021,9 @@ __global__ void __launch_bounds__(256)
 #endif  // DK_EMULATE
 
 #ifndef DK_EMULATE
-// Large fronts: one thread-block cluster of kDirectSolveCluster CTAs (256
-// threads each) per front, so that the front's triangular solves use that
-// many SMs (one CTA per front leaves the top of the tree, a handful of
+// Large fronts: one thread-block cluster of ncl CTAs (kDirectSolveCluster,
+// or kDirectSolveClusterWide at the top levels; 256 threads each) per
+// front, so that the front's triangular solves use that many SMs (one CTA per front leaves the top of the tree, a handful of
 // fronts with thousands of rows, on one SM each).  The front's rows are
 // dealt out in 32-row blocks: block b belongs to rank b % nr and sits in
 // that CTA's shared memory at slot (b / nr) * 32.  Column block k is
@@ -1064,13 +1064,13 @@ struct ClusterRows {
 template <class T, int NR>
 __global__ void __launch_bounds__(kDirectClusterThreads)
     direct_forward_cluster_kernel(DirectView v, const int *__restrict__ sn,
-                                  int count, T *y, T *contrib) {
+                                  int count, int ncl, T *y, T *contrib) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
-  // the shared memory is sized for kDirectSolveCluster ranks: any other
-  // cluster shape leaves (the whole cluster sees the same size)
-  if (cr.nr != kDirectSolveCluster) return;
+  // the shared memory is sized for ncl ranks: any other cluster shape
+  // leaves (the whole cluster sees the same size)
+  if (cr.nr != ncl) return;
   const int fi = (int)blockIdx.x / cr.nr;  // the same in the whole cluster
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);
@@ -1177,12 +1177,12 @@ template <class T, int NR>
 __global__ void __launch_bounds__(kDirectClusterThreads, 4)
     direct_backward_cluster_kernel(DirectView v, const int *__restrict__ sn,
                                    const int64_t *__restrict__ poff,
-                                   int count, const T *y, T *x,
+                                   int count, int ncl, const T *y, T *x,
                                    const T *part) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const ClusterRows cr{(int)cl.num_blocks(), (int)cl.block_rank()};
-  if (cr.nr != kDirectSolveCluster) return;  // as in the forward kernel
+  if (cr.nr != ncl) return;  // as in the forward kernel
   const int fi = (int)blockIdx.x / cr.nr;
   if (fi >= count) return;
   DK_DYN_SMEM(T, z);

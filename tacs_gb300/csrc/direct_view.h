@@ -34,6 +34,12 @@ constexpr int kDirectExtendRows = 32;
 // CTAs of the thread-block cluster that solves one large front, and the
 // front rows above which a front is solved that way
 constexpr int kDirectSolveCluster = 8;
+// the cluster size (non-portable, where the device schedules it) of the
+// levels with at most kDirectWideFronts fronts solved by clusters: twice
+// the SMs per front where the chain of blocks, not the level's width,
+// sets the time
+constexpr int kDirectSolveClusterWide = 16;
+constexpr int kDirectWideFronts = 8;
 // threads of a CTA of the cluster solves
 constexpr int kDirectClusterThreads = 256;
 // update rows of one tile of the backward solve's L21^T x2 products for

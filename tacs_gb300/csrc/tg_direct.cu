@@ -42,6 +42,10 @@ struct tg_direct {
   // fronts above cluster_threshold rows are solved by clusters (when the
   // device schedules them); tg_direct_autotune picks it
   bool clusters_ok = false;
+  // the device also schedules kDirectSolveClusterWide-CTA clusters; per
+  // level the cluster size of its cluster launches
+  bool wide_ok = false;
+  std::vector<int> csolve_ncl_h;
   int cluster_threshold = tg::kDirectClusterFront;
   long long layout_version = 0;  // build_solve_lists calls
   int precision = TG_PREC_FP64;
@@ -198,6 +202,7 @@ static int build_solve_lists(tg_direct *d, int threshold) {
   std::vector<int> a, b;
   d->solve_ptr_h.assign(1, 0);
   d->csolve_ptr_h.assign(1, 0);
+  d->csolve_ncl_h.clear();
   d->solve_front_h.clear();
   d->plain_front = d->cluster_front = 0;
   for (size_t L = 0; L + 1 < an.level_ptr.size(); L++) {
@@ -215,6 +220,10 @@ static int build_solve_lists(tg_direct *d, int threshold) {
     d->plain_front = std::max(d->plain_front, pf);
     d->solve_ptr_h.push_back((int)a.size());
     d->csolve_ptr_h.push_back((int)b.size());
+    const int ncf = d->csolve_ptr_h.back() - d->csolve_ptr_h[L];
+    d->csolve_ncl_h.push_back(d->wide_ok && ncf <= tg::kDirectWideFronts
+                                  ? tg::kDirectSolveClusterWide
+                                  : tg::kDirectSolveCluster);
     d->solve_front_h.push_back(pf);
   }
   d->solve_sn_h = a;
@@ -353,7 +362,9 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   d->tile = precision == TG_PREC_FP32 ? tg::kDirectTile32 : TG_DIRECT_TILE_F64;
   d->steps = tg::direct::panel_steps(an, d->bs, kSmallFront, tg::kDirectPanel,
                                      d->tile, tg::kDirectTrsmRows);
-  d->clusters_ok = tg::direct_cluster_solve_ok();
+  d->clusters_ok = tg::direct_cluster_solve_ok(tg::kDirectSolveCluster);
+  d->wide_ok = d->clusters_ok &&
+               tg::direct_cluster_solve_ok(tg::kDirectSolveClusterWide);
   if (!d->clusters_ok) d->cluster_threshold = 1 << 30;
   // the fronts factored by panels keep the inverses of their diagonal
   // blocks (the solves' block steps become 32 x 32 products)
@@ -444,7 +455,8 @@ int tg_direct_create(tg_mat *A, int use_coords, int precision,
   for (int nr : {4, 2, 1}) {
     d->max_nr = nr;
     if (tg::direct_solve_smem(pf_max, nr, sizeof(double)) <= kSmemMax &&
-        tg::direct_cluster_smem(d->max_front, nr, sizeof(double)) <=
+        tg::direct_cluster_smem(d->max_front, nr, sizeof(double),
+                                tg::kDirectSolveCluster) <=
             kSmemMax)
       break;
   }
@@ -563,8 +575,9 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
       const int cb = d->csolve_ptr_h[L], ce = d->csolve_ptr_h[L + 1];
       const cudaStream_t sc = level_fork(d, le > lb && ce > cb, s);
       tg::launch_direct_forward_cluster<T>(v, d->d_csolve_sn + cb, ce - cb,
-                                           d->cluster_front, nr, ypos,
-                                           contrib, sc);
+                                           d->cluster_front, nr,
+                                           d->csolve_ncl_h[L], ypos, contrib,
+                                           sc);
       tg::launch_direct_forward<T>(v, d->d_solve_sn + lb, le - lb,
                                    d->solve_front_h[L], nr, ypos, contrib, s);
       level_join(d, sc, s);
@@ -579,7 +592,8 @@ static void solve_levels(tg_direct *d, int nrhs, const T *b, T *x,
                                     (T *)d->d_part, sc);
       tg::launch_direct_backward_cluster<T>(
           v, d->d_csolve_sn + cb, d->d_gemv_poff + cb, ce - cb,
-          d->cluster_front, nr, ypos, xpos, (const T *)d->d_part, sc);
+          d->cluster_front, nr, d->csolve_ncl_h[L], ypos, xpos,
+          (const T *)d->d_part, sc);
       tg::launch_direct_backward<T>(v, d->d_solve_sn + lb, le - lb,
                                     d->solve_front_h[L], nr, ypos, xpos, s);
       level_join(d, sc, s);

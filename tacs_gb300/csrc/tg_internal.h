@@ -379,8 +379,8 @@ void launch_direct_backward(const DirectView &v, const int *sn, int count,
 // kDirectSolveCluster CTAs per front
 template <class T>
 void launch_direct_forward_cluster(const DirectView &v, const int *sn,
-                                   int count, int max_front, int nr, T *y,
-                                   T *contrib, cudaStream_t s);
+                                   int count, int max_front, int nr, int ncl,
+                                   T *y, T *contrib, cudaStream_t s);
 // The fronts solved by clusters at one level of the backward solve: first
 // their L21^T x2 products in tiles over the whole GPU (total tiles,
 // tprefix / poff per front: cumulative tiles and the offset of its chunk
@@ -394,13 +394,15 @@ void launch_direct_bwd_gemv(const DirectView &v, const int *sn,
 template <class T>
 void launch_direct_backward_cluster(const DirectView &v, const int *sn,
                                     const int64_t *poff, int count,
-                                    int max_front, int nr, const T *y, T *x,
-                                    const T *part, cudaStream_t s);
-bool direct_cluster_solve_ok();
+                                    int max_front, int nr, int ncl,
+                                    const T *y, T *x, const T *part,
+                                    cudaStream_t s);
+// whether clusters of ncl CTAs are scheduled on this device
+bool direct_cluster_solve_ok(int ncl);
 // dynamic shared memory of a solve over fronts of `front` rows with nr
 // right-hand sides (one CTA per front, or one cluster per front)
 size_t direct_solve_smem(int front, int nr, size_t elem);
-size_t direct_cluster_smem(int front, int nr, size_t elem);
+size_t direct_cluster_smem(int front, int nr, size_t elem, int ncl);
 // nrhs right-hand sides ld apart (node order); ypos / xpos interleaved
 template <class T>
 void launch_direct_rhs(int n, int bs, const int *perm, const T *b, T *ypos,
