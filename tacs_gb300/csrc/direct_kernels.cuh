@@ -731,6 +731,34 @@ __device__ __forceinline__ void dk_col_dot(int W, const T *Lc, int ldl,
     dk_col_dot_w<T, NR, 1>(Lc, ldl, i0, i1, step, z, acc);
 }
 
+// acc = sum over c < nb of L(kb + c, j) zk(c) (NR interleaved right-hand
+// sides; Lc = the entry (kb, j), ldl = the row stride), in c order; a
+// whole block's loads are issued 8 at a time before their products.
+template <class T, int NR>
+__device__ __forceinline__ void dk_col_block(const T *Lc, size_t ldl, int nb,
+                                             const T *zk, T (&acc)[NR]) {
+#pragma unroll
+  for (int q = 0; q < NR; q++) acc[q] = 0;
+  if (nb == 32) {
+#pragma unroll 1
+    for (int h = 0; h < 32; h += 8) {
+      T l[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) l[c] = Lc[(size_t)(h + c) * ldl];
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int q = 0; q < NR; q++) acc[q] += l[c] * zk[(h + c) * NR + q];
+    }
+    return;
+  }
+  for (int c = 0; c < nb; c++) {
+    const T l = Lc[(size_t)c * ldl];
+#pragma unroll
+    for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
+  }
+}
+
 // position of front row i of supernode s in a factor-order vector
 __device__ __forceinline__ size_t dk_pos(const int *rows, int bs, int i) {
   return (size_t)rows[i / bs] * bs + i % bs;
@@ -1244,13 +1272,7 @@ __global__ void __launch_bounds__(kDirectClusterThreads, 4)
       if (threadIdx.x < 32) {
         const int j = r1 + (int)threadIdx.x;
         T acc[NR];
-#pragma unroll
-        for (int q = 0; q < NR; q++) acc[q] = 0;
-        for (int c = 0; c < nb; c++) {
-          const T l = f.lp[(size_t)(kb + c) * f.C + j];
-#pragma unroll
-          for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
-        }
+        dk_col_block<T, NR>(f.lp + (size_t)kb * f.C + j, f.C, nb, zk, acc);
         T *zj = z + (size_t)cr.slot(j) * NR;
 #pragma unroll
         for (int q = 0; q < NR; q++) zj[q] -= acc[q];
@@ -1267,13 +1289,7 @@ __global__ void __launch_bounds__(kDirectClusterThreads, 4)
       if (j >= kb) continue;
       if (next_mine && j >= r1) continue;  // done ahead
       T acc[NR];
-#pragma unroll
-      for (int q = 0; q < NR; q++) acc[q] = 0;
-      for (int c = 0; c < nb; c++) {
-        const T l = f.lp[(size_t)(kb + c) * f.C + j];
-#pragma unroll
-        for (int q = 0; q < NR; q++) acc[q] += l * zk[c * NR + q];
-      }
+      dk_col_block<T, NR>(f.lp + (size_t)kb * f.C + j, f.C, nb, zk, acc);
 #pragma unroll
       for (int q = 0; q < NR; q++) z[t * NR + q] -= acc[q];
     }
