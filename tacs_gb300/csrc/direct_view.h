@@ -39,7 +39,7 @@ constexpr int kDirectSolveCluster = 8;
 // the SMs per front where the chain of blocks, not the level's width,
 // sets the time
 constexpr int kDirectSolveClusterWide = 16;
-constexpr int kDirectWideFronts = 8;
+constexpr int kDirectWideFronts = 19;
 // threads of a CTA of the cluster solves
 constexpr int kDirectClusterThreads = 256;
 // update rows of one tile of the backward solve's L21^T x2 products for
