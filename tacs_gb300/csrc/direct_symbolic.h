@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <iterator>
 #include <map>
+#include <set>
 #include <vector>
 
 namespace tg {
@@ -371,10 +372,8 @@ inline Analysis analyse(const std::vector<int> &rowp,
     }
   }
 
-  // column structures of L below the diagonal: the upper neighbours of
-  // column j in A, merged with the structures of j's children minus j
-  // (children come before parents, so one pass in increasing order)
-  std::vector<int> uptr(n + 1, 0), uadj;  // upper neighbours (> r)
+  // the upper neighbours of each position in A (rows > r), sorted
+  std::vector<int> uptr(n + 1, 0), uadj;
   {
     std::vector<int> cnt(n, 0);
     for (int r = 0; r < n; r++)
@@ -386,33 +385,78 @@ inline Analysis analyse(const std::vector<int> &rowp,
       for (int k = lptr[r]; k < lptr[r + 1]; k++)
         uadj[fill[ladj[k]]++] = r;
   }
-  std::vector<int> first_child(n, -1), next_sib(n, -1);
-  for (int j = n - 1; j >= 0; j--) {
-    const int p = a.parent[j];
-    if (p >= 0) {
-      next_sib[j] = first_child[p];
-      first_child[p] = j;
-    }
-  }
-  std::vector<std::vector<int>> colstruct(n);
+  // column counts of L (Gilbert, Ng and Peyton's row-subtree method):
+  // row i of L has its nonzeros on the subtree of the elimination tree
+  // spanned by the columns j < i with A(i, j) != 0; visiting the columns in
+  // postorder, j is a leaf of row i's subtree when its first descendant
+  // comes after the previous leaf's, each leaf adds one to its column and
+  // one less is counted at the least common ancestor of consecutive leaves
+  // (found by path compression); the counts are then these differences
+  // summed over each subtree.  So the supernodes follow without forming
+  // every column's structure.
   std::vector<int> count(n, 0), nchild(n, 0);
-  std::vector<int> mark(n, -1);
-  for (int j = 0; j < n; j++) {
-    std::vector<int> &s = colstruct[j];
-    for (int k = uptr[j]; k < uptr[j + 1]; k++) {
-      s.push_back(uadj[k]);
-      mark[uadj[k]] = j;
+  {
+    std::vector<int> head(n, -1), next(n, -1);
+    for (int j = n - 1; j >= 0; j--) {
+      const int p = a.parent[j];
+      if (p >= 0) {
+        next[j] = head[p];
+        head[p] = j;
+        nchild[p]++;
+      }
     }
-    for (int c = first_child[j]; c >= 0; c = next_sib[c]) {
-      nchild[j]++;
-      for (int i : colstruct[c])
-        if (i != j && mark[i] != j) {
-          mark[i] = j;
-          s.push_back(i);
+    std::vector<int> post, stack;
+    post.reserve(n);
+    for (int r = 0; r < n; r++) {
+      if (a.parent[r] != -1) continue;
+      stack.push_back(r);
+      while (!stack.empty()) {
+        const int j = stack.back();
+        const int c = head[j];
+        if (c == -1) {
+          stack.pop_back();
+          post.push_back(j);
+        } else {
+          head[j] = next[c];
+          stack.push_back(c);
         }
+      }
     }
-    std::sort(s.begin(), s.end());
-    count[j] = (int)s.size();
+    std::vector<int> firstd(n, -1), delta(n, 0), maxfirst(n, -1),
+        prevleaf(n, -1), anc(n);
+    for (int k = 0; k < n; k++) {
+      int j = post[k];
+      delta[j] = firstd[j] == -1 ? 1 : 0;  // a leaf of the tree
+      for (; j != -1 && firstd[j] == -1; j = a.parent[j]) firstd[j] = k;
+    }
+    for (int i = 0; i < n; i++) anc[i] = i;
+    for (int k = 0; k < n; k++) {
+      const int j = post[k];
+      if (a.parent[j] != -1) delta[a.parent[j]]--;
+      for (int q = uptr[j]; q < uptr[j + 1]; q++) {
+        const int i = uadj[q];  // A(i, j) != 0, i > j
+        if (firstd[j] <= maxfirst[i]) continue;  // j not a leaf of row i
+        maxfirst[i] = firstd[j];
+        const int jprev = prevleaf[i];
+        prevleaf[i] = j;
+        delta[j]++;
+        if (jprev == -1) continue;  // row i's first leaf
+        int r = jprev;  // the least common ancestor of jprev and j
+        while (r != anc[r]) r = anc[r];
+        for (int t = jprev; t != r;) {
+          const int up = anc[t];
+          anc[t] = r;
+          t = up;
+        }
+        delta[r]--;
+      }
+      if (a.parent[j] != -1) anc[j] = a.parent[j];
+    }
+    for (int k = 0; k < n; k++) {
+      const int j = post[k];
+      if (a.parent[j] != -1) delta[a.parent[j]] += delta[j];
+    }
+    for (int j = 0; j < n; j++) count[j] = delta[j] - 1;  // below the diagonal
   }
 
   // fundamental supernodes: j + 1 joins j's supernode when it is j's
@@ -431,19 +475,46 @@ inline Analysis analyse(const std::vector<int> &rowp,
   std::vector<int> sn_of(n);
   for (int s = 0; s < ns; s++)
     for (int j = first[s]; j < last[s]; j++) sn_of[j] = s;
-  // fronts: own positions, then the structure of the first column below
-  // the last column
+  // fronts: own positions, then the rows below them -- the upper
+  // neighbours of the supernode's columns and its child supernodes' rows
+  // below their own columns (children come before parents), sorted
   std::vector<std::vector<int>> rows(ns);
-  std::vector<int> spar(ns, -1);
+  std::vector<int> spar(ns, -1), shead(ns, -1), snext(ns, -1);
   for (int s = 0; s < ns; s++) {
-    for (int j = first[s]; j < last[s]; j++) rows[s].push_back(j);
-    for (int i : colstruct[first[s]])
-      if (i >= last[s]) rows[s].push_back(i);
     const int p = a.parent[last[s] - 1];
     spar[s] = p < 0 ? -1 : sn_of[p];
   }
-  colstruct.clear();
-  colstruct.shrink_to_fit();
+  for (int s = ns - 1; s >= 0; s--)
+    if (spar[s] >= 0) {
+      snext[s] = shead[spar[s]];
+      shead[spar[s]] = s;
+    }
+  {
+    std::vector<int> mark(n, -1);
+    for (int s = 0; s < ns; s++) {
+      std::vector<int> &r = rows[s];
+      for (int j = first[s]; j < last[s]; j++) {
+        r.push_back(j);
+        mark[j] = s;
+      }
+      const size_t own = r.size();
+      for (int j = first[s]; j < last[s]; j++)
+        for (int q = uptr[j]; q < uptr[j + 1]; q++)
+          if (mark[uadj[q]] != s) {
+            mark[uadj[q]] = s;
+            r.push_back(uadj[q]);
+          }
+      for (int c = shead[s]; c >= 0; c = snext[c]) {
+        const std::vector<int> &rc = rows[c];
+        for (size_t t = (size_t)(last[c] - first[c]); t < rc.size(); t++)
+          if (mark[rc[t]] != s) {
+            mark[rc[t]] = s;
+            r.push_back(rc[t]);
+          }
+      }
+      std::sort(r.begin() + own, r.end());
+    }
+  }
 
   // relaxed amalgamation: a child whose columns end where its parent's
   // begin is merged into the parent when the explicit zeros this adds to
@@ -590,48 +661,80 @@ inline Analysis analyse(const std::vector<int> &rowp,
   return a;
 }
 
-// First-fit allocator over [0, top) with coalescing free intervals.
+// First-fit allocation in a pool of one address range: an allocation
+// takes the free block of lowest offset that is large enough (or the top
+// of the range), a release merges with free neighbours.  Free blocks are
+// indexed by offset (for merging) and by size class (floor log2 of the
+// size: every block of a higher class fits, so the first fit is the
+// lowest offset among the higher classes' first blocks and the fitting
+// blocks of the request's own class), which keeps each allocation near
+// logarithmic where a scan of all free blocks was linear.
 class PoolPlan {
  public:
   int64_t alloc(int64_t size) {
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second >= size) {
-        const int64_t off = it->first, rest = it->second - size;
-        free_.erase(it);
-        if (rest > 0) free_[off + size] = rest;
-        return off;
+    const int c = cls(size);
+    int64_t best = -1;
+    for (int64_t off : by_cls_[c])
+      if (free_[off] >= size) {
+        best = off;
+        break;
       }
+    for (int k = c + 1; k < kClasses; k++)
+      if (!by_cls_[k].empty() && (best < 0 || *by_cls_[k].begin() < best))
+        best = *by_cls_[k].begin();
+    if (best < 0) {
+      const int64_t off = top_;
+      top_ += size;
+      peak_ = std::max(peak_, top_);
+      return off;
     }
-    const int64_t off = top_;
-    top_ += size;
-    peak_ = std::max(peak_, top_);
-    return off;
+    const int64_t rest = free_[best] - size;
+    erase(best);
+    if (rest > 0) insert(best + size, rest);
+    return best;
   }
   void release(int64_t off, int64_t size) {
     if (size <= 0) return;
-    auto it = free_.emplace(off, size).first;
-    auto nx = std::next(it);
-    if (nx != free_.end() && off + it->second == nx->first) {
-      it->second += nx->second;
-      free_.erase(nx);
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + size == nx->first) {
+      size += nx->second;
+      erase(nx->first);
     }
-    if (it != free_.begin()) {
-      auto pv = std::prev(it);
-      if (pv->first + pv->second == it->first) {
-        pv->second += it->second;
-        free_.erase(it);
-        it = pv;
+    auto pv = free_.lower_bound(off);
+    if (pv != free_.begin()) {
+      --pv;
+      if (pv->first + pv->second == off) {
+        off = pv->first;
+        size += pv->second;
+        erase(off);
       }
     }
-    if (it->first + it->second == top_) {
-      top_ = it->first;
-      free_.erase(it);
+    if (off + size == top_) {
+      top_ = off;
+      return;
     }
+    insert(off, size);
   }
   int64_t peak() const { return peak_; }
 
  private:
+  static constexpr int kClasses = 64;
+  static int cls(int64_t size) {
+    int c = 0;
+    while (c + 1 < kClasses && (size >> (c + 1)) > 0) c++;
+    return c;
+  }
+  void insert(int64_t off, int64_t size) {
+    free_[off] = size;
+    by_cls_[cls(size)].insert(off);
+  }
+  void erase(int64_t off) {
+    auto it = free_.find(off);
+    by_cls_[cls(it->second)].erase(off);
+    free_.erase(it);
+  }
   std::map<int64_t, int64_t> free_;
+  std::set<int64_t> by_cls_[kClasses];
   int64_t top_ = 0, peak_ = 0;
 };
 
