@@ -733,20 +733,22 @@ __device__ __forceinline__ void dk_col_dot(int W, const T *Lc, int ldl,
 
 // acc = sum over c < nb of L(kb + c, j) zk(c) (NR interleaved right-hand
 // sides; Lc = the entry (kb, j), ldl = the row stride), in c order; a
-// whole block's loads are issued 8 at a time before their products.
+// whole block's loads are issued 16 (one right-hand side) or 8 at a time
+// before their products.
 template <class T, int NR>
 __device__ __forceinline__ void dk_col_block(const T *Lc, size_t ldl, int nb,
                                              const T *zk, T (&acc)[NR]) {
 #pragma unroll
   for (int q = 0; q < NR; q++) acc[q] = 0;
   if (nb == 32) {
+    constexpr int H = NR == 1 ? 16 : 8;  // within the 64-register budget
 #pragma unroll 1
-    for (int h = 0; h < 32; h += 8) {
-      T l[8];
+    for (int h = 0; h < 32; h += H) {
+      T l[H];
 #pragma unroll
-      for (int c = 0; c < 8; c++) l[c] = Lc[(size_t)(h + c) * ldl];
+      for (int c = 0; c < H; c++) l[c] = Lc[(size_t)(h + c) * ldl];
 #pragma unroll
-      for (int c = 0; c < 8; c++)
+      for (int c = 0; c < H; c++)
 #pragma unroll
         for (int q = 0; q < NR; q++) acc[q] += l[c] * zk[(h + c) * NR + q];
     }
