@@ -6,7 +6,9 @@
 // large levFill, src/bpmat/TACSSchurMat.cpp:1510-1600) with the same
 // solution; the matrix's row boundary conditions are handled as
 // x = Kt^-1 (b - K P b + P b), Kt being K with the boundary columns zeroed
-// too (symmetric positive definite) and P keeping the boundary dofs.
+// too (symmetric positive definite) and P keeping the boundary dofs; the
+// correction K P b is formed on the block rows that have a block in a
+// constrained column only (direct::bc_coupling).
 #include <algorithm>
 #include <cstdio>
 #include <map>
