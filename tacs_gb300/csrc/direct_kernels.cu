@@ -25,7 +25,9 @@ void launch_direct_level_assemble(const DirectView &v, const int *sn,
                                   int count, const double *A, int zchunks,
                                   int nchild, int ychunks, cudaStream_t s) {
   if (count <= 0) return;
-  direct_zero_kernel<T><<<dim3(count, zchunks), 256, 0, s>>>(v, sn, count);
+  direct_zero_kernel<T>
+      <<<dim3(count, zchunks < 65535 ? zchunks : 65535), 256, 0, s>>>(
+          v, sn, count);
   direct_assemble_kernel<T><<<count, 256, 0, s>>>(v, sn, count, A);
   if (ychunks > 0)
     for (int k = 0; k < nchild; k++)

@@ -109,11 +109,17 @@ __global__ void __launch_bounds__(256)
   const Front<T> f = front_of<T>(v, sn[blockIdx.x]);
   const size_t npan = (size_t)f.M * f.C;
   const size_t nu = f.up ? (size_t)(f.M - f.C) * (f.M - f.C) : 0;
-  const size_t lo = (size_t)blockIdx.y * kZeroChunk;
-  const size_t hi = lo + kZeroChunk < npan + nu ? lo + kZeroChunk : npan + nu;
-  for (size_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-    if (k < npan) f.lp[k] = T(0);
-    else f.up[k - npan] = T(0);
+  // chunks of kZeroChunk entries, gridDim.y of them at a time (the grid's
+  // y extent is at most 65,535; a front of more than ~32 k rows has more
+  // chunks than that)
+  for (size_t lo = (size_t)blockIdx.y * kZeroChunk; lo < npan + nu;
+       lo += (size_t)gridDim.y * kZeroChunk) {
+    const size_t hi =
+        lo + kZeroChunk < npan + nu ? lo + kZeroChunk : npan + nu;
+    for (size_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+      if (k < npan) f.lp[k] = T(0);
+      else f.up[k - npan] = T(0);
+    }
   }
 }
 
