@@ -275,9 +275,11 @@ def hex_section(torch, steps=5):
     return out
 
 
-def c3_solve_section(torch, pc_kind=0, h=1e-6):
+def c3_solve_section(torch, pc_kind=0, h=1e-6, direct=None):
     """The 128 x 128 x 64 SIMP block solved and differentiated: FP64 GMRES
-    with ILU(0) (pc_kind: natural or colour-reordered), compliance and its
+    with ILU(0) (pc_kind: natural or colour-reordered), or with
+    direct="mixed" the complete factorisation in FP32 with FP64 refinement
+    (GMRES-IR where refinement stagnates), compliance and its
     gradient with respect to the 1,048,576 densities through the autograd
     backward (dC/drho = 3 rho^2 dC/dt), checked by
       * a central difference with h along a seeded positive direction
@@ -293,8 +295,12 @@ def c3_solve_section(torch, pc_kind=0, h=1e-6):
     p = meshes.hex_c3()
     M = problem.GpuModel(p)
     M.set_fixed_geometry(True)
+    t0 = time.perf_counter()
     solver = ag.StaticSolver(M, np.zeros(M.ndof), m=200, nrestart=40,
-                             rtol=1e-10, pc_kind=pc_kind)
+                             rtol=1e-10, pc_kind=pc_kind,
+                             direct=direct or False)
+    torch.cuda.synchronize()
+    s_setup = time.perf_counter() - t0  # the direct analysis, once
     rho0 = torch.as_tensor(p["rho"], device="cuda")
     x = rho0.clone().requires_grad_(True)
     torch.cuda.synchronize()
@@ -306,16 +312,33 @@ def c3_solve_section(torch, pc_kind=0, h=1e-6):
     g = x.grad.detach()
     u = solver.u[0].clone()
     out = {"workload": "hex8 SIMP block 128x128x64, compliance gradient wrt "
-                       "densities, GMRES(200) + ILU(0) to 1e-10",
+                       "densities, " + ("complete factorisation in FP32, "
+                                        "FP64 refinement / GMRES-IR"
+                                        if direct else "GMRES(200) + ILU(0)")
+                       + " to 1e-10",
            "elements": int(p["nelem"]), "dof": int(M.ndof),
-           "preconditioner": "natural ILU(0)" if pc_kind == 0
-           else "colour-reordered ILU(0)",
+           "preconditioner": ("complete factorisation (FP32)" if direct
+                              else "natural ILU(0)" if pc_kind == 0
+                              else "colour-reordered ILU(0)"),
            "s_per_gradient": s_grad, "compliance": float(c.detach()),
            "iters": [int(np.max(i)) for i in solver.iters]}
-    # directional central difference, warm-started solves
+    if direct:
+        st = solver.direct.stats()
+        out["direct"] = {"analysis_s": s_setup, **{
+            k: st[k] for k in ("supernodes", "levels", "factor_bytes",
+                               "pool_bytes", "flops", "max_front",
+                               "fp32_mode", "last_gmres_iters",
+                               "fell_back_to_fp64")}}
+    # directional central difference, warm-started solves (with the
+    # factorisation: GMRES preconditioned by the unperturbed FP32 factor)
     zero = M.vec()
     mat_p = M.new_mat()
-    ksm_p = problem.Ksm(mat_p, solver.pc, 200, 40)
+    if direct:
+        pc_p = problem.Pc.from_direct(solver.direct)
+        pc_p.factor()
+        ksm_p = problem.Ksm(mat_p, pc_p, 30, 20)
+    else:
+        ksm_p = problem.Ksm(mat_p, solver.pc, 200, 40)
     ksm_p.set_tolerances(1e-9, 1e-30)
     d = torch.as_tensor(np.random.default_rng(34).random(int(p["nelem"])),
                         device="cuda")
@@ -789,6 +812,9 @@ def main():
                     help="solve and differentiate the 128x128x64 hex block")
     ap.add_argument("--c3-pc", type=int, default=0,
                     help="its ILU(0): 0 natural order, 2 colour-reordered")
+    ap.add_argument("--c3-direct", action="store_true",
+                    help="solve it by the FP32 complete factorisation with "
+                         "FP64 refinement instead of GMRES + ILU(0)")
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the fixed-geometry assembly section")
     ap.add_argument("--no-cylinder", action="store_true")
@@ -953,7 +979,8 @@ def main():
         line["hex_c3"] = guarded(lambda: hex_section(torch))
     if rank == 0 and args.c3_solve:
         line["c3_solve"] = guarded(lambda: c3_solve_section(
-            torch, pc_kind=args.c3_pc))
+            torch, pc_kind=args.c3_pc,
+            direct="mixed" if args.c3_direct else None))
     if rank == 0 and not args.no_c2_adjoint:
         line["c2_adjoint"] = guarded(
             lambda: c2_adjoint_section(torch, args.size))
