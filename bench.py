@@ -812,9 +812,9 @@ def main():
                     help="solve and differentiate the 128x128x64 hex block")
     ap.add_argument("--c3-pc", type=int, default=0,
                     help="its ILU(0): 0 natural order, 2 colour-reordered")
-    ap.add_argument("--c3-direct", action="store_true",
-                    help="solve it by the FP32 complete factorisation with "
-                         "FP64 refinement instead of GMRES + ILU(0)")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="skip the hex block's gradient by the FP32 complete "
+                         "factorisation (c3_direct, ~40 s)")
     ap.add_argument("--no-fixed", action="store_true",
                     help="skip the fixed-geometry assembly section")
     ap.add_argument("--no-cylinder", action="store_true")
@@ -979,8 +979,10 @@ def main():
         line["hex_c3"] = guarded(lambda: hex_section(torch))
     if rank == 0 and args.c3_solve:
         line["c3_solve"] = guarded(lambda: c3_solve_section(
-            torch, pc_kind=args.c3_pc,
-            direct="mixed" if args.c3_direct else None))
+            torch, pc_kind=args.c3_pc))
+    if rank == 0 and not args.no_c3:
+        line["c3_direct"] = guarded(lambda: c3_solve_section(
+            torch, direct="mixed"))
     if rank == 0 and not args.no_c2_adjoint:
         line["c2_adjoint"] = guarded(
             lambda: c2_adjoint_section(torch, args.size))
