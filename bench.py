@@ -329,6 +329,17 @@ def c3_solve_section(torch, pc_kind=0, h=1e-6, direct=None):
                                "pool_bytes", "flops", "max_front",
                                "fp32_mode", "last_gmres_iters",
                                "fell_back_to_fp64")}}
+        # the FP32 factorisation alone, once more (no launch-shape tuning)
+        solver.direct.autotune = False
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        solver.direct.factor()
+        e1.record()
+        torch.cuda.synchronize()
+        fms = e0.elapsed_time(e1)
+        out["direct"]["factor_ms"] = fms
+        out["direct"]["factor_tflops"] = st["flops"] / (fms * 1e-3) / 1e12
     # directional central difference, warm-started solves (with the
     # factorisation: GMRES preconditioned by the unperturbed FP32 factor)
     zero = M.vec()
