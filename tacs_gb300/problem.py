@@ -81,7 +81,10 @@ class Pc:
         check(_lib.lib().tg_pc_create_direct(direct.handle, C.byref(h)),
               "tg_pc_create_direct")
         pc = cls.__new__(cls)
-        pc.handle, pc.mat, pc.direct = h, direct.mat, direct
+        # the C object holds its own reference to the factorisation: no
+        # Python reference back to the Direct (which keeps this pc), so
+        # dropping the Direct frees its device memory at once
+        pc.handle, pc.mat = h, direct.mat
         return pc
 
     def fp64_used(self):
