@@ -22,11 +22,12 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <iterator>
 #include <map>
-#include <set>
+#include <thread>
 #include <vector>
 
 namespace tg {
@@ -50,32 +51,44 @@ class NestedDissection {
   // bisection), the separator being the smaller of the two sides' rows of
   // vertices that touch the other side -- straight cuts on meshes, where
   // level sets from a corner are bent
+  // threads: at most this many threads (0: the host's hardware threads);
+  // the order does not depend on it
   NestedDissection(const std::vector<int> &rowp, const std::vector<int> &cols,
-                   int leaf, const double *xyz = nullptr)
-      : rowp_(rowp), cols_(cols), leaf_(leaf < 1 ? 1 : leaf), xyz_(xyz) {}
+                   int leaf, const double *xyz = nullptr, int threads = 0)
+      : rowp_(rowp), cols_(cols), leaf_(leaf < 1 ? 1 : leaf), xyz_(xyz),
+        threads_(threads) {}
 
   std::vector<int> order() {
     const int n = (int)rowp_.size() - 1;
     part_.assign(n, 0);
     dist_.assign(n, -1);
-    out_.clear();
-    out_.reserve(n);
+    std::vector<int> out;
+    out.reserve(n);
     std::vector<int> all(n);
     for (int i = 0; i < n; i++) all[i] = i;
     next_id_ = 1;
-    split(all, 0);
-    return out_;
+    // the two sides of a cut share no edge and so no vertex that either
+    // side's recursion writes: the top levels run them on two threads
+    // (each side's order is then appended in the same sequence)
+    const unsigned hw = threads_ > 0 ? (unsigned)threads_
+                                     : std::thread::hardware_concurrency();
+    par_depth_ = 0;
+    while (par_depth_ < 4 && (2u << par_depth_) <= hw) par_depth_++;
+    split(all, 0, out, 0);
+    return out;
   }
 
  private:
   const std::vector<int> &rowp_, &cols_;
   int leaf_;
   const double *xyz_;
-  int next_id_ = 1;
+  int threads_;
+  std::atomic<int> next_id_{1};
+  int par_depth_ = 0;
+  static constexpr size_t kParMin = 4096;  // smallest part split on threads
   std::vector<int> part_;  // subgraph id of each unordered vertex, -1 once
                            // ordered or held for a separator
   std::vector<int> dist_;
-  std::vector<int> out_;
 
   // breadth-first search inside subgraph `id` from src: visit order in
   // `vis`, distances in dist_ (reset by the caller through `vis`)
@@ -123,22 +136,23 @@ class NestedDissection {
     return src;
   }
 
-  void emit_rcm(const std::vector<int> &vis) {
+  void emit_rcm(const std::vector<int> &vis, std::vector<int> &out) {
     for (size_t k = vis.size(); k-- > 0;) {
-      out_.push_back(vis[k]);
+      out.push_back(vis[k]);
       part_[vis[k]] = -1;
     }
   }
 
   // order the vertices `verts` (all with part_ == id), one connected part
   // after the other
-  void split(const std::vector<int> &verts, int id) {
+  void split(const std::vector<int> &verts, int id, std::vector<int> &out,
+             int depth) {
     if (verts.empty()) return;
     std::vector<int> vis;
     bfs(id, verts[0], vis);
     clear_dist(vis);
     if (vis.size() == verts.size()) {
-      split_connected(verts, id);
+      split_connected(verts, id, out, depth);
       return;
     }
     std::vector<std::pair<std::vector<int>, int>> parts;
@@ -150,11 +164,58 @@ class NestedDissection {
       for (int w : vis) part_[w] = cid;
       parts.push_back({vis, cid});
     }
-    for (auto &pc : parts) split_connected(pc.first, pc.second);
+    if (depth < par_depth_ && parts.size() > 1 &&
+        verts.size() >= 2 * kParMin) {
+      // the parts share no edge: ordered by a few threads, each taking the
+      // next part, then appended in sequence
+      std::vector<std::vector<int>> outs(parts.size());
+      std::atomic<size_t> next{0};
+      auto work = [&] {
+        for (size_t i; (i = next++) < parts.size();)
+          split_connected(parts[i].first, parts[i].second, outs[i],
+                          par_depth_);
+      };
+      std::vector<std::thread> pool;
+      const size_t nt = std::min(parts.size(), (size_t)1 << par_depth_);
+      for (size_t t = 1; t < nt; t++) {
+        try {
+          pool.emplace_back(work);
+        } catch (...) {  // fewer threads
+          break;
+        }
+      }
+      work();
+      for (auto &t : pool) t.join();
+      for (auto &o : outs) out.insert(out.end(), o.begin(), o.end());
+      return;
+    }
+    for (auto &pc : parts) split_connected(pc.first, pc.second, out, depth);
+  }
+
+  // order the two sides of a cut, a's then b's (no edge joins them)
+  void split_two(const std::vector<int> &a, int ida, const std::vector<int> &b,
+                 int idb, std::vector<int> &out, int depth) {
+    if (depth < par_depth_ && a.size() >= kParMin && b.size() >= kParMin) {
+      std::vector<int> oa, ob;
+      std::thread t;
+      try {
+        t = std::thread([&] { split(a, ida, oa, depth + 1); });
+      } catch (...) {  // no thread: in sequence
+        split(a, ida, oa, depth + 1);
+      }
+      split(b, idb, ob, depth + 1);
+      if (t.joinable()) t.join();
+      out.insert(out.end(), oa.begin(), oa.end());
+      out.insert(out.end(), ob.begin(), ob.end());
+      return;
+    }
+    split(a, ida, out, depth + 1);
+    split(b, idb, out, depth + 1);
   }
 
   // coordinate bisection of a connected part; false when it cannot cut
-  bool split_coords(const std::vector<int> &verts, int id) {
+  bool split_coords(const std::vector<int> &verts, int id,
+                    std::vector<int> &out, int depth) {
     double lo[3], hi[3];
     for (int d = 0; d < 3; d++) lo[d] = hi[d] = xyz_[3 * (size_t)verts[0] + d];
     for (int v : verts)
@@ -202,20 +263,22 @@ class NestedDissection {
       if (part_[v] == ida) a2.push_back(v);
     for (int v : b)
       if (part_[v] == idb) b2.push_back(v);
-    split(a2, ida);
-    split(b2, idb);
-    for (int v : sep) out_.push_back(v);
+    split_two(a2, ida, b2, idb, out, depth);
+    for (int v : sep) out.push_back(v);
     return true;
   }
 
-  void split_connected(const std::vector<int> &verts, int id) {
-    if (xyz_ && (int)verts.size() > leaf_ && split_coords(verts, id)) return;
+  void split_connected(const std::vector<int> &verts, int id,
+                       std::vector<int> &out, int depth) {
+    if (xyz_ && (int)verts.size() > leaf_ &&
+        split_coords(verts, id, out, depth))
+      return;
     std::vector<int> vis;
     peripheral(id, verts[0], vis);
     const int nlev = dist_[vis.back()] + 1;
     if ((int)verts.size() <= leaf_ || nlev < 3) {
       clear_dist(vis);
-      emit_rcm(vis);
+      emit_rcm(vis, out);
       return;
     }
     // separator level: the smallest level set among those where the
@@ -252,17 +315,17 @@ class NestedDissection {
       }
     }
     clear_dist(vis);
-    split(a, ida);
-    split(b, idb);
-    for (int v : sp) out_.push_back(v);
+    split_two(a, ida, b, idb, out, depth);
+    for (int v : sp) out.push_back(v);
   }
 };
 
 inline std::vector<int> nested_dissection(const std::vector<int> &rowp,
                                           const std::vector<int> &cols,
                                           int leaf = 64,
-                                          const double *xyz = nullptr) {
-  NestedDissection nd(rowp, cols, leaf, xyz);
+                                          const double *xyz = nullptr,
+                                          int threads = 0) {
+  NestedDissection nd(rowp, cols, leaf, xyz, threads);
   return nd.order();
 }
 
@@ -475,45 +538,17 @@ inline Analysis analyse(const std::vector<int> &rowp,
   std::vector<int> sn_of(n);
   for (int s = 0; s < ns; s++)
     for (int j = first[s]; j < last[s]; j++) sn_of[j] = s;
-  // fronts: own positions, then the rows below them -- the upper
-  // neighbours of the supernode's columns and its child supernodes' rows
-  // below their own columns (children come before parents), sorted
-  std::vector<std::vector<int>> rows(ns);
-  std::vector<int> spar(ns, -1), shead(ns, -1), snext(ns, -1);
+  // front rows of a supernode: its own positions, then the rows below them
+  // (the structure of L below its last column, count[last - 1] rows), so
+  // the amalgamation below decides on front sizes alone and the rows are
+  // formed only for the supernodes that survive it
+  std::vector<int64_t> msize(ns);
+  for (int s = 0; s < ns; s++)
+    msize[s] = (last[s] - first[s]) + (int64_t)count[last[s] - 1];
+  std::vector<int> spar(ns, -1);
   for (int s = 0; s < ns; s++) {
     const int p = a.parent[last[s] - 1];
     spar[s] = p < 0 ? -1 : sn_of[p];
-  }
-  for (int s = ns - 1; s >= 0; s--)
-    if (spar[s] >= 0) {
-      snext[s] = shead[spar[s]];
-      shead[spar[s]] = s;
-    }
-  {
-    std::vector<int> mark(n, -1);
-    for (int s = 0; s < ns; s++) {
-      std::vector<int> &r = rows[s];
-      for (int j = first[s]; j < last[s]; j++) {
-        r.push_back(j);
-        mark[j] = s;
-      }
-      const size_t own = r.size();
-      for (int j = first[s]; j < last[s]; j++)
-        for (int q = uptr[j]; q < uptr[j + 1]; q++)
-          if (mark[uadj[q]] != s) {
-            mark[uadj[q]] = s;
-            r.push_back(uadj[q]);
-          }
-      for (int c = shead[s]; c >= 0; c = snext[c]) {
-        const std::vector<int> &rc = rows[c];
-        for (size_t t = (size_t)(last[c] - first[c]); t < rc.size(); t++)
-          if (mark[rc[t]] != s) {
-            mark[rc[t]] = s;
-            r.push_back(rc[t]);
-          }
-      }
-      std::sort(r.begin() + own, r.end());
-    }
   }
 
   // relaxed amalgamation: a child whose columns end where its parent's
@@ -542,8 +577,7 @@ inline Analysis analyse(const std::vector<int> &rowp,
         const int c = sn_of[first[p] - 1];
         if (!alive[c] || spar[c] < 0 || find(spar[c]) != p) break;
         const int64_t nc = last[c] - first[c], np = last[p] - first[p];
-        const int64_t mc = (int64_t)rows[c].size(),
-                      mp = (int64_t)rows[p].size();
+        const int64_t mc = msize[c], mp = msize[p];
         const int64_t add = nc * (mp - (mc - nc));
         const int64_t z = zeros[c] + zeros[p] + add;
         const int64_t tot = entries(nc + np, nc + mp);
@@ -552,13 +586,7 @@ inline Analysis analyse(const std::vector<int> &rowp,
                                                                : 0.05;
         if (w > opt.max_columns || (double)z > frac * (double)tot) break;
         // merge c into p
-        std::vector<int> merged;
-        merged.reserve(nc + mp);
-        for (int j = first[c]; j < last[c]; j++) merged.push_back(j);
-        merged.insert(merged.end(), rows[p].begin(), rows[p].end());
-        rows[p].swap(merged);
-        rows[c].clear();
-        rows[c].shrink_to_fit();
+        msize[p] = nc + mp;
         for (int j = first[c]; j < last[c]; j++) sn_of[j] = p;
         first[p] = first[c];
         zeros[p] = z;
@@ -575,21 +603,61 @@ inline Analysis analyse(const std::vector<int> &rowp,
   a.sn_col.assign(nsurv + 1, 0);
   a.sn_rowptr.assign(nsurv + 1, 0);
   a.sn_parent.assign(nsurv, -1);
-  a.sn_rows.clear();
   for (int s = 0; s < ns; s++) {
     if (!alive[s]) continue;
     const int t = newid[s];
     a.sn_col[t] = first[s];
-    a.sn_rows.insert(a.sn_rows.end(), rows[s].begin(), rows[s].end());
-    a.sn_rowptr[t + 1] = (int)a.sn_rows.size();
     a.sn_parent[t] = spar[s] < 0 ? -1 : newid[find(spar[s])];
-    const int64_t m = (int64_t)rows[s].size(), c = last[s] - first[s];
+    a.sn_rowptr[t + 1] = a.sn_rowptr[t] + (int)msize[s];
+    const int64_t m = msize[s], c = last[s] - first[s];
     a.front_blocks += m * m;
     a.factor_blocks += c * (c + 1) / 2 + (m - c) * c;
     a.zero_blocks += zeros[s];
   }
   if (nsurv > 0) a.sn_col[nsurv] = n;
   ns = nsurv;
+  // the rows of each surviving supernode (children before parents): its
+  // own positions, the upper neighbours of its columns and its children's
+  // rows below their own columns, sorted -- the union of its columns'
+  // structures in L
+  a.sn_rows.assign(a.sn_rowptr[ns], 0);
+  {
+    std::vector<int> shead(ns, -1), snext(ns, -1), mark(n, -1);
+    for (int s = ns - 1; s >= 0; s--) {
+      const int p = a.sn_parent[s];
+      if (p >= 0) {
+        snext[s] = shead[p];
+        shead[p] = s;
+      }
+    }
+    for (int s = 0; s < ns; s++) {
+      int *r = &a.sn_rows[a.sn_rowptr[s]];
+      const int m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+      int len = 0;
+      for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++) {
+        r[len++] = j;
+        mark[j] = s;
+      }
+      const int own = len;
+      for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++)
+        for (int q = uptr[j]; q < uptr[j + 1]; q++)
+          if (mark[uadj[q]] != s && len < m) {
+            mark[uadj[q]] = s;
+            r[len++] = uadj[q];
+          }
+      for (int c = shead[s]; c >= 0; c = snext[c]) {
+        const int cown = a.sn_col[c + 1] - a.sn_col[c];
+        for (int t = a.sn_rowptr[c] + cown; t < a.sn_rowptr[c + 1]; t++) {
+          const int i = a.sn_rows[t];
+          if (mark[i] != s && len < m) {
+            mark[i] = s;
+            r[len++] = i;
+          }
+        }
+      }
+      std::sort(r + own, r + len);
+    }
+  }
 
   // levels: leaves 0, a parent one above its highest child
   std::vector<int> lev(ns, 0);
@@ -630,28 +698,38 @@ inline Analysis analyse(const std::vector<int> &rowp,
 
   // the matrix's lower blocks (position i >= j) in the front of j's
   // supernode: block row = index of i in the front rows, block column =
-  // j - first column
+  // j - first column.  Block (i, j) of the permuted matrix is stored in
+  // row perm[i] of A at column perm[j]: the mirror of A's block at (row
+  // perm[j], column perm[i]), found through the transpose map (with sorted
+  // columns, the t-th visit of column c in a pass over rows in increasing
+  // order is the t-th entry of row c); the front row of i through a
+  // scatter of the supernode's rows
+  std::vector<int> mirror(cols.size());
+  {
+    std::vector<int> cur(rowp.begin(), rowp.end() - 1);
+    for (int o = 0; o < n; o++)
+      for (int k = rowp[o]; k < rowp[o + 1]; k++) mirror[k] = cur[cols[k]]++;
+  }
+  std::vector<int> where(n, -1);
   a.asm_ptr.assign(ns + 1, 0);
+  const size_t nlow = (cols.size() + (size_t)n) / 2;  // i >= j blocks
   a.asm_blk.clear();
   a.asm_row.clear();
   a.asm_col.clear();
+  a.asm_blk.reserve(nlow);
+  a.asm_row.reserve(nlow);
+  a.asm_col.reserve(nlow);
   for (int s = 0; s < ns; s++) {
-    const int *rows = &a.sn_rows[a.sn_rowptr[s]];
-    const int m = a.sn_rowptr[s + 1] - a.sn_rowptr[s];
+    for (int t = a.sn_rowptr[s]; t < a.sn_rowptr[s + 1]; t++)
+      where[a.sn_rows[t]] = t - a.sn_rowptr[s];
     for (int j = a.sn_col[s]; j < a.sn_col[s + 1]; j++) {
       const int oj = perm[j];
-      // column j of the permuted matrix = row oj of A (symmetric pattern);
-      // the block stored at (row perm[i], col oj) is A_(i, j)
+      // column j of the permuted matrix = row oj of A (symmetric pattern)
       for (int k = rowp[oj]; k < rowp[oj + 1]; k++) {
         const int i = a.iperm[cols[k]];
         if (i < j) continue;
-        const int pos = (int)(std::lower_bound(rows, rows + m, i) - rows);
-        // block (i, j) of A lives in row perm[i]: find column oj there
-        const int oi = cols[k];
-        const int *rb = &cols[rowp[oi]], *re = &cols[rowp[oi + 1]];
-        const int blk = rowp[oi] + (int)(std::lower_bound(rb, re, oj) - rb);
-        a.asm_blk.push_back(blk);
-        a.asm_row.push_back(pos);
+        a.asm_blk.push_back(mirror[k]);
+        a.asm_row.push_back(where[i]);
         a.asm_col.push_back(j - a.sn_col[s]);
       }
     }
@@ -674,14 +752,15 @@ class PoolPlan {
   int64_t alloc(int64_t size) {
     const int c = cls(size);
     int64_t best = -1;
-    for (int64_t off : by_cls_[c])
-      if (free_[off] >= size) {
-        best = off;
+    for (const auto &blk : by_cls_[c])
+      if (blk.second >= size) {
+        best = blk.first;
         break;
       }
     for (int k = c + 1; k < kClasses; k++)
-      if (!by_cls_[k].empty() && (best < 0 || *by_cls_[k].begin() < best))
-        best = *by_cls_[k].begin();
+      if (!by_cls_[k].empty() &&
+          (best < 0 || by_cls_[k].begin()->first < best))
+        best = by_cls_[k].begin()->first;
     if (best < 0) {
       const int64_t off = top_;
       top_ += size;
@@ -726,7 +805,7 @@ class PoolPlan {
   }
   void insert(int64_t off, int64_t size) {
     free_[off] = size;
-    by_cls_[cls(size)].insert(off);
+    by_cls_[cls(size)].emplace(off, size);
   }
   void erase(int64_t off) {
     auto it = free_.find(off);
@@ -734,7 +813,7 @@ class PoolPlan {
     free_.erase(it);
   }
   std::map<int64_t, int64_t> free_;
-  std::set<int64_t> by_cls_[kClasses];
+  std::map<int64_t, int64_t> by_cls_[kClasses];  // offset -> size
   int64_t top_ = 0, peak_ = 0;
 };
 

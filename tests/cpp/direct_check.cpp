@@ -65,6 +65,18 @@ int dc_analyse(int n, const int *rowp, const int *cols, const int *perm,
   return 0;
 }
 
+// Nested-dissection order with at most `threads` threads (0: the host's):
+// perm (n entries) is the new -> old order.
+int dc_nd(int n, const int *rowp, const int *cols, int leaf,
+          const double *xyz, int threads, int *perm) {
+  std::vector<int> rp(rowp, rowp + n + 1), cs(cols, cols + rowp[n]);
+  std::vector<int> p =
+      tg::direct::nested_dissection(rp, cs, leaf, xyz, threads);
+  if ((int)p.size() != n) return -1;
+  std::copy(p.begin(), p.end(), perm);
+  return 0;
+}
+
 // Storage plan check: out = {factor panel blocks, update pool peak blocks,
 // sum of live update blocks at the busiest level, overlapping live pairs}.
 int dc_plan(int n, const int *rowp, const int *cols, int leaf,

@@ -12,6 +12,7 @@ import ctypes as C
 import os
 import shutil
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -28,13 +29,14 @@ def dc(tmp_path_factory):
     if not cxx:
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("dc") / "libdc.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", INC,
-                    SRC, "-o", out], check=True)
+    subprocess.run([cxx, "-O2", "-std=c++17", "-pthread", "-shared", "-fPIC",
+                    "-I", INC, SRC, "-o", out], check=True)
     lib = C.CDLL(out)
     P = C.c_void_p
     lib.dc_analyse.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, P, P]
     lib.dc_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int, P]
     lib.dc_plan.argtypes = [C.c_int, P, P, C.c_int, P, P]
+    lib.dc_nd.argtypes = [C.c_int, P, P, C.c_int, P, C.c_int, P]
     return lib
 
 
@@ -111,6 +113,99 @@ def test_multifrontal_solve_is_exact(dc, name, prob, leaf, coords):
     assert rel(x, spsolve(K.tocsc(), b)) < 1e-5
 
 
+def _pattern(prob):
+    """Block pattern (every node coupled with the nodes of its elements)
+    and node coordinates of a mesh, without assembling it."""
+    from scipy import sparse
+    conn = np.asarray(prob["conn"]).reshape(prob["nelem"], -1)
+    n, k = prob["nnodes"], conn.shape[1]
+    A = sparse.csr_matrix((np.ones(conn.size * k),
+                           (np.repeat(conn, k, axis=1).ravel(),
+                            np.tile(conn, (1, k)).ravel())), shape=(n, n))
+    A.sum_duplicates()
+    A.sort_indices()
+    return (n, A.indptr.astype(np.int32), A.indices.astype(np.int32),
+            np.ascontiguousarray(prob["xpts"], np.float64))
+
+
+def _nd_cases():
+    from tacs_gb300 import meshes
+    yield "plate 200", meshes.plate_c2(200)
+    yield "cylinder 192x96", meshes.cylinder_c5(192, 96)
+    yield "hex 32x32x16", meshes.hex_c3(32, 32, 16)
+    yield "8 plates", meshes.batch_plates(count=8, nmin=60, nmax=90)
+
+
+@pytest.mark.parametrize("name,prob", list(_nd_cases()),
+                         ids=[p[0] for p in _nd_cases()])
+def test_nested_dissection_order_independent_of_threads(dc, name, prob):
+    """The two sides of each cut at the top of the recursion are ordered on
+    two threads; the order is the sequential one for every thread count,
+    by coordinates and by level structures."""
+    n, rowp, cols, xyz = _pattern(prob)
+    for coords in (xyz, None):
+        ref = np.zeros(n, np.int32)
+        assert dc.dc_nd(n, _ptr(rowp), _ptr(cols), 64, _ptr(coords), 1,
+                        _ptr(ref)) == 0
+        assert np.array_equal(np.sort(ref), np.arange(n))
+        for threads in (2, 3, 8, 16):
+            p = np.zeros(n, np.int32)
+            assert dc.dc_nd(n, _ptr(rowp), _ptr(cols), 64, _ptr(coords),
+                            threads, _ptr(p)) == 0
+            assert np.array_equal(p, ref), (threads, coords is None)
+
+
+def test_nested_dissection_threads_race_free(tmp_path):
+    """ThreadSanitizer finds no data race in the threaded nested dissection
+    (16 threads, by coordinates and by level structures; one plate, and
+    separate plates ordered on threads side by side)."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no g++")
+    tsan = subprocess.run([cxx, "-print-file-name=libtsan.so"],
+                          capture_output=True, text=True).stdout.strip()
+    if not os.path.isabs(tsan):
+        pytest.skip("ThreadSanitizer runtime unavailable")
+    lib = str(tmp_path / "libdc_tsan.so")
+    r = subprocess.run([cxx, "-O1", "-g", "-std=c++17", "-pthread",
+                        "-fsanitize=thread", "-shared", "-fPIC", "-I", INC,
+                        SRC, "-o", lib], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("ThreadSanitizer build failed: " + r.stderr[-200:])
+    from tacs_gb300 import meshes
+    files = []
+    for k, prob in enumerate((meshes.plate_c2(160),
+                              meshes.batch_plates(count=6, nmin=40,
+                                                  nmax=60))):
+        n, rowp, cols, xyz = _pattern(prob)
+        files.append(str(tmp_path / f"pat{k}.npz"))
+        np.savez(files[-1], rowp=rowp, cols=cols, xyz=xyz)
+    code = f"""
+import ctypes as C, numpy as np
+lib = C.CDLL({lib!r})
+P = C.c_void_p
+lib.dc_nd.argtypes = [C.c_int, P, P, C.c_int, P, C.c_int, P]
+for f in {files!r}:
+    d = np.load(f)
+    rowp, cols, xyz = d["rowp"], d["cols"], d["xyz"]
+    n = len(rowp) - 1
+    for coords in (xyz, None):
+        p = np.zeros(n, np.int32)
+        cp = coords.ctypes.data_as(P) if coords is not None else None
+        assert lib.dc_nd(n, rowp.ctypes.data_as(P), cols.ctypes.data_as(P),
+                         64, cp, 16, p.ctypes.data_as(P)) == 0
+        assert np.array_equal(np.sort(p), np.arange(n))
+print("ok")
+"""
+    env = dict(os.environ, LD_PRELOAD=tsan,
+               TSAN_OPTIONS="halt_on_error=1 exitcode=66 "
+                            "report_signal_unsafe=0")
+    r = subprocess.run([sys.executable, "-c", code], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert "ThreadSanitizer" not in r.stderr, r.stderr[-3000:]
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
+
+
 def test_nested_dissection_fills_less(dc):
     from tacs_gb300 import meshes
     n, bs, rowp, cols, vals = _matrix(meshes.clamped_plate(96))
@@ -156,8 +251,8 @@ def de(tmp_path_factory):
     if not cxx:
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("de") / "libde.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", INC,
-                    EMUL, "-o", out], check=True)
+    subprocess.run([cxx, "-O2", "-std=c++17", "-pthread", "-shared", "-fPIC",
+                    "-I", INC, EMUL, "-o", out], check=True)
     lib = C.CDLL(out)
     P = C.c_void_p
     lib.de_solve.argtypes = [C.c_int, C.c_int, P, P, P, P, P, C.c_int,
@@ -329,7 +424,8 @@ def test_gpu_kernels_in_bounds_under_sanitizers(tmp_path):
     exe = str(tmp_path / "de_san")
     r = subprocess.run([cxx, "-O1", "-g", "-std=c++17",
                         "-fsanitize=address,undefined",
-                        "-fno-sanitize-recover=all", "-DDE_MAIN", "-I", INC,
+                        "-fno-sanitize-recover=all", "-pthread", "-DDE_MAIN",
+                        "-I", INC,
                         EMUL, "-o", exe], capture_output=True, text=True)
     if r.returncode != 0:
         pytest.skip("sanitizer runtime unavailable: " + r.stderr[-200:])
