@@ -124,8 +124,12 @@ struct tg_direct {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // the factorisation's launch sequence (every level's assembly, panel
   // steps and the inverses; fixed by the analysis) as one CUDA graph,
-  // captured at the first factorisation and replayed after
+  // captured at the second factorisation and replayed after (the first
+  // launches the kernels directly: a one-off factorisation gains nothing
+  // from a graph, whose capture and instantiation come before its first
+  // kernel runs)
   cudaGraphExec_t factor_exec = nullptr;
+  int factor_calls = 0;
   tg::DirectBc bc() const {
     tg::DirectBc c;
     c.nrow = bc_nrow;
@@ -751,7 +755,17 @@ extern "C" {
 int tg_direct_factor(tg_direct *d, void *s) {
   if (!d) return fail(TG_ERR_ARG, "tg_direct_factor: NULL");
   TG_CUDA(cudaMemsetAsync(d->d_fail, 0, sizeof(int), S(s)));
-  if (!d->factor_exec) {
+  if (d->factor_calls++ == 0) {
+    if (d->precision == TG_PREC_FP64) {
+      factor_levels<double>(d, S(s));
+    } else {
+      const tg_mat *A = d->A;
+      tg::launch_d2f(A->d_vals, d->d_a32,
+                     (size_t)A->nnz * A->bsize * A->bsize, S(s));
+      factor_levels<float>(d, S(s));
+    }
+    TG_CUDA(cudaGetLastError());
+  } else if (!d->factor_exec) {
     // captured on the side stream (the caller's may be the legacy default
     // stream, which cannot be captured), launched on the caller's
     cudaStream_t cs = d->side_stream;
@@ -775,7 +789,7 @@ int tg_direct_factor(tg_direct *d, void *s) {
       return cuda_check(ie, "tg_direct_factor: factorisation graph");
     }
   }
-  TG_CUDA(cudaGraphLaunch(d->factor_exec, S(s)));
+  if (d->factor_exec) TG_CUDA(cudaGraphLaunch(d->factor_exec, S(s)));
   {  // ||A||_inf of these values, for the refinement's backward error
     const tg_mat *A = d->A;
     const size_t N = (size_t)d->n * d->bs;

@@ -378,6 +378,32 @@ def test_fp64_direct_refined_to_relative_residual(gpu):
             assert rel(X[r].cpu().numpy(), X1[r].cpu().numpy()) < 1e-8
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_direct_first_factor_launches_later_ones_replay_graph(gpu, prec):
+    """The first factorisation of a Direct launches its kernels directly;
+    the second captures them as one CUDA graph and the later ones replay
+    it.  All three give the same factor: the same solution to rounding, on
+    a plate whose large fronts take panel steps."""
+    from tacs_gb300 import meshes
+    prob = meshes.plate_c2(128)
+    M = gpu.GpuModel(prob)
+    mat = M.new_mat()
+    r0 = M.vec()
+    M.assemble_jacobian(M.vec(), mat, r0)
+    b = -r0
+    d = gpu.Direct(mat, precision=(_lib.PREC_FP64 if prec == "fp64"
+                                   else _lib.PREC_FP32), autotune=False)
+    assert d.stats()["max_front"] > 768  # scalar rows: panel steps run
+    xs = []
+    for _ in range(3):
+        d.factor()
+        xs.append(d.solve(b).cpu().numpy())
+    r = mat.mult(torch.as_tensor(xs[0], device="cuda")) - b
+    assert (r.abs().max() / b.abs().max()).item() < 1e-9
+    assert rel(xs[1], xs[0]) < 1e-12
+    assert rel(xs[2], xs[0]) < 1e-12
+
+
 def test_direct_autotune(gpu):
     """The solves' launch-shape autotuner (tg_direct_autotune, run at the
     second factorisation of a Direct): it times a solve per cluster
