@@ -384,7 +384,7 @@ def test_direct_first_factor_launches_later_ones_replay_graph(gpu, prec):
     the second captures them as one CUDA graph and the later ones replay
     it.  All three give the same factor: the same solution to rounding, on
     a plate whose large fronts take panel steps."""
-    from tacs_gb300 import meshes
+    from tacs_gb300 import _lib, meshes
     prob = meshes.plate_c2(128)
     M = gpu.GpuModel(prob)
     mat = M.new_mat()
@@ -398,10 +398,15 @@ def test_direct_first_factor_launches_later_ones_replay_graph(gpu, prec):
     for _ in range(3):
         d.factor()
         xs.append(d.solve(b).cpu().numpy())
-    r = mat.mult(torch.as_tensor(xs[0], device="cuda")) - b
-    assert (r.abs().max() / b.abs().max()).item() < 1e-9
     assert rel(xs[1], xs[0]) < 1e-12
     assert rel(xs[2], xs[0]) < 1e-12
+    # normwise backward error at rounding level (a thin plate: |A| |x| is
+    # far above |b|, so the residual relative to |b| is not)
+    A = _host_matrix(mat, M.ndof)
+    bh = b.cpu().numpy()
+    eta = np.abs(A @ xs[0] - bh).max() / (
+        abs(A).sum(axis=1).max() * np.abs(xs[0]).max() + np.abs(bh).max())
+    assert eta < 1e-13, eta
 
 
 def test_direct_autotune(gpu):
