@@ -204,7 +204,9 @@ int tg_add_total_derivative(tg_assembler *a, const double *vars, int func,
    factorisation in FP32 (from the FP64 matrix) applied by
    tg_direct_solve_f32, e.g. as the preconditioner of an FP64 iteration.
    tg_direct_factor synchronises and returns TG_ERR_PIVOT on a
-   non-positive pivot.
+   non-positive pivot.  Its first call on a tg_direct launches the
+   factorisation's kernels on the stream; the second captures them as one
+   CUDA graph, which that call and every later one launch.
    stats (9 doubles): supernodes, tree levels, factor bytes (FP64
    storage), update-pool bytes (FP64), dense flops, largest front (scalar
    rows), precision, fronts solved by thread-block clusters, the front
