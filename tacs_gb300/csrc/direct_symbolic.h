@@ -69,7 +69,8 @@ class NestedDissection {
     next_id_ = 1;
     // the two sides of a cut share no edge and so no vertex that either
     // side's recursion writes: the top levels run them on two threads
-    // (each side's order is then appended in the same sequence)
+    // (each side's order is then appended in the same sequence), at most
+    // 2^par_depth_ <= hw threads at a time
     const unsigned hw = threads_ > 0 ? (unsigned)threads_
                                      : std::thread::hardware_concurrency();
     par_depth_ = 0;
@@ -166,8 +167,9 @@ class NestedDissection {
     }
     if (depth < par_depth_ && parts.size() > 1 &&
         verts.size() >= 2 * kParMin) {
-      // the parts share no edge: ordered by a few threads, each taking the
-      // next part, then appended in sequence
+      // the parts share no edge: ordered by this branch's share of the
+      // threads (2^(par_depth_ - depth)), each taking the next part, then
+      // appended in sequence
       std::vector<std::vector<int>> outs(parts.size());
       std::atomic<size_t> next{0};
       auto work = [&] {
@@ -176,7 +178,8 @@ class NestedDissection {
                           par_depth_);
       };
       std::vector<std::thread> pool;
-      const size_t nt = std::min(parts.size(), (size_t)1 << par_depth_);
+      const size_t nt =
+          std::min(parts.size(), (size_t)1 << (par_depth_ - depth));
       for (size_t t = 1; t < nt; t++) {
         try {
           pool.emplace_back(work);
