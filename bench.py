@@ -502,6 +502,50 @@ def cylinder_section(torch, nc=384, nz=256):
     a, b = g["mixed_direct"], g["fp64_direct"]
     out["mixed_direct"]["grad_rel_err_vs_fp64_direct"] = float(
         np.abs(a[0] - b[0]).max() / np.abs(b[0]).max())
+    # where a one-off direct arm's time goes (outside the timed arms): the
+    # steps of problem.static_adjoint one by one, each behind a
+    # synchronisation
+    for label, prec in (("fp64_direct", _lib.PREC_FP64),
+                        ("mixed_direct", _lib.PREC_FP32)):
+        bd = {}
+        t = [time.perf_counter()]
+
+        def lap(name):
+            torch.cuda.synchronize()
+            t.append(time.perf_counter())
+            bd[name] = bd.get(name, 0.0) + t[-1] - t[-2]
+
+        torch.cuda.synchronize()
+        t[0] = time.perf_counter()
+        mat = M.new_mat()
+        res = M.vec()
+        M.assemble_jacobian(M.vec(), mat, res)
+        lap("assemble")
+        d = problem.Direct(mat, precision=prec)
+        lap("create")
+        d.factor()
+        lap("factor")
+        f = torch.as_tensor(np.asarray(c["force"], np.float64),
+                            device="cuda").clone()
+        M.apply_bcs(f)
+        res -= f
+        lap("load")
+        u = -d.solve(res, rtol=1e-10)
+        lap("solve")
+        M.eval_functions(u, (0,))
+        dfdu = M.vec()
+        M.add_sv_sens(u, [0], [dfdu])
+        M.apply_bcs(dfdu)
+        lap("functions_and_dfdu")
+        psi = d.solve(dfdu, rtol=1e-10)
+        lap("solve")
+        gr = M.dv_vec()
+        M.add_total_derivative(u, 0, psi, gr, 1.0, -1.0)
+        lap("total_derivative")
+        bd["solve_steps"] = d.last_steps
+        bd["sum"] = t[-1] - t[0]
+        out[label]["breakdown_s"] = bd
+        del d, mat, res, f, u, dfdu, psi, gr
     del M
     torch.cuda.empty_cache()
     return out
