@@ -22,6 +22,8 @@ from __future__ import annotations
 
 import argparse
 
+import numpy as np
+
 import torch
 
 from . import meshes, problem
@@ -113,10 +115,45 @@ def batch(count=48, nmax=256):
     return f"batch plates={count} elements={bp['nelem']}"
 
 
+def functions(nc=384, nz=256, reps=5):
+    """The compliance value, its df/du and its total derivative with
+    respect to the thicknesses (adjoint = df/du) on the 384 x 256 MITC4
+    cylinder at a seeded state, `reps` times; prints the time per
+    repetition of each call (host clock, each behind a synchronisation)."""
+    import time
+    c = meshes.cylinder_c5(nc, nz)
+    M = problem.GpuModel(c)
+    rng = np.random.default_rng(5)
+    u = M.vec(1e-4 * rng.standard_normal(M.ndof))
+    M.apply_bcs(u)
+    ms = {"eval_functions": 0.0, "add_sv_sens": 0.0,
+          "add_total_derivative": 0.0}
+
+    def lap(name, t0):
+        torch.cuda.synchronize()
+        ms[name] += (time.perf_counter() - t0) * 1e3 / reps
+
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        M.eval_functions(u, (0,))
+        lap("eval_functions", t0)
+        t0 = time.perf_counter()
+        dfdu = M.vec()
+        M.add_sv_sens(u, [0], [dfdu])
+        lap("add_sv_sens", t0)
+        t0 = time.perf_counter()
+        g = M.dv_vec()
+        M.add_total_derivative(u, 0, dfdu, g, 1.0, -1.0)
+        lap("add_total_derivative", t0)
+    return (f"functions elements={c['nelem']} ms per call: " +
+            " ".join(f"{k}={v:.2f}" for k, v in ms.items()))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["gmres", "hex", "spmv", "assemble",
-                                     "direct", "batch"])
+                                     "direct", "batch", "functions"])
     ap.add_argument("--count", type=int, default=48)
     ap.add_argument("--nmax", type=int, default=256)
     ap.add_argument("--n", type=int, default=None)
@@ -133,6 +170,8 @@ def main(argv=None):
         print(direct(a.n or 512))
     elif a.case == "batch":
         print(batch(a.count, a.nmax))
+    elif a.case == "functions":
+        print(functions())
     else:
         print(assemble(a.n or 256))
 
